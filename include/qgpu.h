@@ -1,0 +1,270 @@
+/*
+ * qgpu.h -- C-ABI of the GB300 engine for the hot path of Q's qdyn.
+ *
+ * The reference (qusers/qsource, Q 5.06) is Fortran 90.  Its hot path lives in
+ * src/md.f90 as zero-argument module subroutines that read and write module
+ * globals.  This header replaces those call points with plain C entry points:
+ * every array is a plain pointer plus a size, no torch or CUDA types appear,
+ * and every call returns an int status (0 = ok, see QGPU_E_*).  The text of the
+ * last error is returned by qgpu_last_error().
+ *
+ * Conventions
+ *   - Atom, group, Q-atom and type indices are 0-based (the Fortran host
+ *     subtracts 1 once when it fills the descriptor).
+ *   - Coordinates, velocities and forces are interleaved xyz FP64 arrays of
+ *     length 3*natom, the layout of md.f90's x(:), v(:), d(:) (src/md.f90:309-313).
+ *   - Charges are already multiplied by sqrt(coulomb_constant), as prep_sim does
+ *     (src/md.f90:16805-16811), so q_i*q_j/r is in kcal/mol.
+ *   - dt and tau_T are in Q's internal time unit (0.020462 * fs,
+ *     src/md.f90:4623,4637).
+ *
+ * A handle holds a batch of ntraj independent trajectories (lambda windows or
+ * replicas).  ntraj == 1 is the drop-in mode that sits behind one qdyn
+ * process; ntraj > 1 is the batched mode that runs many windows in one
+ * launch sequence.
+ */
+#ifndef QGPU_H
+#define QGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QGPU_MAX_STATES 10   /* max_states, src/qatom.f90:37 */
+
+/* status codes */
+#define QGPU_OK               0
+#define QGPU_E_INVALID        1   /* bad descriptor / argument */
+#define QGPU_E_CUDA           2   /* CUDA runtime error */
+#define QGPU_E_LIST_OVERFLOW  3   /* a neighbour list ran out of capacity */
+#define QGPU_E_SHAKE          4   /* SHAKE did not converge in SHAKE_MAX_ITER */
+#define QGPU_E_NAN            5   /* non-finite temperature (md.f90:6654-6656) */
+#define QGPU_E_UNSUPPORTED    6   /* input uses a feature this engine does not run */
+#define QGPU_E_FIXED_RANGE    7   /* a fixed-point accumulator left its range */
+
+/* ------------------------------------------------------------------------ */
+/* System descriptor: the qdyn module state after topology/prep_coord/get_fep/ */
+/* prep_sim/init_shake/make_nbqqlist/shrink_topology (src/qdyn.f90:110-124).  */
+/* ------------------------------------------------------------------------ */
+typedef struct qgpu_system_desc {
+    /* sizes */
+    int32_t natom;          /* nat_pro                                         */
+    int32_t nat_solute;     /* solute atoms come first, waters after           */
+    int32_t solv_atom;      /* atoms per solvent molecule; must be 3           */
+    int32_t nwat;           /* (natom - nat_solute) / solv_atom               */
+    int32_t natyps;         /* atom types                                      */
+    int32_t ncgp;           /* charge groups (solute groups first)             */
+    int32_t ncgp_solute;
+    int32_t nqat;           /* Q atoms                                         */
+    int32_t nstates;        /* FEP/EVB states (<= QGPU_MAX_STATES)             */
+
+    /* coordinates */
+    const double *x;        /* 3*natom starting coordinates                    */
+    const double *v;        /* 3*natom starting velocities (may be NULL)       */
+    const double *xtop;     /* 3*natom topology coordinates (restraint origin) */
+
+    /* per atom */
+    const double  *crg;     /* natom, scaled charges                           */
+    const int32_t *iac;     /* natom, atom type                                */
+    const uint8_t *excl;    /* natom, atom outside the sphere (excluded)       */
+    const uint8_t *shell;   /* natom, atom in the restrained shell             */
+    const int32_t *iqatom;  /* natom, Q-atom index or -1                       */
+
+    /* atom-type library (iaclib) and LJ code matrix (ljcod) */
+    const double *mass;     /* natyps                                          */
+    const double *avdw;     /* natyps*3, [type*3 + (ljcode-1)]                 */
+    const double *bvdw;     /* natyps*3                                        */
+    const int8_t *ljcod;    /* natyps*natyps, values 1 or 2                    */
+    double el14_scale;
+    int32_t ivdw_rule;      /* must be 1 (geometric)                           */
+    int32_t ff_type;        /* 1 GROMOS, 2 AMBER, 3 CHARMM (improper form)     */
+
+    /* SPC-type solvent tables (prep_sim, src/md.f90:16702-16717) */
+    double chg_solv[3];     /* scaled charges of the 3 solvent atoms           */
+    double aLJ_solv[6];     /* [atom*2 + (ljcode-1)]                           */
+    double bLJ_solv[6];
+
+    /* charge groups */
+    const int32_t *cgp_first;   /* ncgp, index into cgpatom                    */
+    const int32_t *cgp_last;    /* ncgp, inclusive                             */
+    const int32_t *cgp_switch;  /* ncgp, switch atom                           */
+    const int32_t *cgpatom;     /* natom                                       */
+
+    /* solute neighbour exclusions and 1-4 pairs (listex/listexlong and
+       list14/list14long merged), each pair stored once with i < j */
+    int32_t nexcl;  const int32_t *excl_pairs;   /* 2*nexcl */
+    int32_t n14;    const int32_t *pairs14;      /* 2*n14   */
+
+    /* Q atoms (src/qatom.f90, get_fep src/md.f90:2884-3074) */
+    const int32_t *iqseq;       /* nqat, atom of each Q atom                   */
+    const double  *qcrg;        /* nqat*nstates [iq*nstates+s], scaled         */
+    int32_t qvdw_flag;          /* Q atoms have their own LJ types per state   */
+    const int32_t *qiac;        /* nqat*nstates, Q-type per state              */
+    int32_t nqlib;              /* Q atom types                                */
+    const double  *qavdw;       /* nqlib*3                                     */
+    const double  *qbvdw;       /* nqlib*3                                     */
+    const double  *sc_lookup;   /* nqat*(natyps+nqat)*nstates, softcore shifts  */
+                                /* [(iq*(natyps+nqat) + col)*nstates + s]      */
+    double lambda[QGPU_MAX_STATES];
+
+    /* Q-atom / solute list inputs that make_qconn derives at start-up       */
+    const uint8_t *qp_skip;     /* natom: any(qconn(:,i,:) <= 3)  (md.f90:10288) */
+    int32_t nqp14;  const int32_t *qp14_pairs; /* 2*n: (iq, atom) with qconn(1,atom,iq)==4 */
+
+    /* nbqqlist (src/md.f90:9691-9804), per state, concatenated               */
+    int32_t nbqq_count[QGPU_MAX_STATES];
+    const int32_t *nbqq_iq;     /* sum(nbqq_count) entries                     */
+    const int32_t *nbqq_j;      /* atom                                        */
+    const int32_t *nbqq_jq;     /* Q atom of j or -1                           */
+    const int8_t  *nbqq_ljcod;
+    const double  *nbqq_elscale;
+
+    /* Q bonded terms (per-state codes, 0 = absent in that state) */
+    int32_t nqbond;  const int32_t *qbnd;      /* nqbond*(2+nstates): i, j, cod[s] (1-based codes) */
+    int32_t nqbcod;  const double  *qbondlib;  /* nqbcod*4: Dmz, amz, r0, fk                      */
+    int32_t nqangle; const int32_t *qang;      /* nqangle*(3+nstates)                              */
+    int32_t nqacod;  const double  *qanglib;   /* nqacod*4: fk, ang0 (rad), ureyfk, ureyr0         */
+    int32_t nqtor;   const int32_t *qtor;      /* nqtor*(4+nstates)                                */
+    int32_t nqtcod;  const double  *qtorlib;   /* nqtcod*3: fk, rmult, deltor (rad)                */
+    int32_t nqimp;   const int32_t *qimp;      /* nqimp*(4+nstates)                                */
+    int32_t nqicod;  const double  *qimplib;   /* nqicod*2: fk, imp0 (rad)                         */
+
+    /* classical bonded terms after shrink_topology (codes 1-based) */
+    int32_t nbonds, nbonds_solute;  const int32_t *bnd;   /* nbonds*3: i, j, cod   */
+    int32_t nbndcod;  const double *bondlib;               /* nbndcod*2: fk, b0     */
+    int32_t nangles, nangles_solute; const int32_t *ang;   /* nangles*4             */
+    int32_t nangcod;  const double *anglib;                /* nangcod*4: fk, ang0 (rad), ureyfk, ureyr0 */
+    int32_t ntors, ntors_solute;    const int32_t *tor;    /* ntors*5               */
+    int32_t ntorcod;  const float  *torlib;                /* ntorcod*4: fk, rmult, deltor (rad), 1/paths (single, as topo.f90) */
+    int32_t nimps, nimps_solute;    const int32_t *imp;    /* nimps*5               */
+    int32_t nimpcod;  const float  *implib;                /* nimpcod*2: fk, imp0 (rad) */
+
+    /* SHAKE (init_shake, src/md.f90:4242-4426), molecules in CSR form */
+    int32_t shake_molecules;
+    const int32_t *shake_first; /* shake_molecules+1                           */
+    const int32_t *shake_i;     /* constraint atoms                            */
+    const int32_t *shake_j;
+    const double  *shake_dist2; /* squared target distance                     */
+
+    /* off-diagonal EVB couplings: Hij = A*exp(-mu*r_kl) (src/md.f90:15444) */
+    int32_t noffd;
+    const int32_t *offd_ij;     /* noffd*2 states                              */
+    const int32_t *offd_kl;     /* noffd*2 Q atoms                             */
+    const double  *offd_Amu;    /* noffd*2: A, mu                              */
+
+    /* simulation sphere (topology + [sphere]/[solvent] sections) */
+    double xpcent[3];           /* solute centre                               */
+    double xwcent[3];           /* solvent centre                              */
+    double rexcl_o;             /* exclusion radius                            */
+    double rwat;                /* water sphere radius                         */
+    double fk_wsphere, Dwmz, awmz;   /* radial solvent restraint               */
+    double fk_pshell, fk_fix;   /* shell / excluded atom restraints            */
+    int32_t wpol_restr;         /* water polarisation restraint requested       */
+
+    /* cut-offs ([cut-offs]) */
+    double Rcpp, Rcww, Rcpw, Rcq, RcLRF;
+    int32_t use_LRF;
+
+    /* MD parameters ([MD]) */
+    double dt;                  /* internal units                              */
+    double Temp0, tau_T;        /* tau_T in internal units                     */
+    int32_t separate_scaling;
+    int32_t NBcycle;
+    int32_t Ndegf, Ndegfree, Ndegf_solvent, Ndegfree_solvent;
+    int32_t Ndegf_solute, Ndegfree_solute, detail_temps;
+} qgpu_system_desc;
+
+/* Energies, the ENERGIES record of src/nrgy.f90:48-54 (sphere subset). */
+typedef struct qgpu_energies {
+    double potential, kinetic, lrf;
+    double p_bond, p_angle, p_torsion, p_improper;
+    double w_bond, w_angle, w_torsion, w_improper;
+    double q_bond, q_angle, q_torsion, q_improper;
+    double pp_el, pp_vdw, pw_el, pw_vdw, ww_el, ww_vdw, qx_el, qx_vdw;
+    double rst_total, rst_fix, rst_shell, rst_protein, rst_solvent_radial, rst_water_pol;
+} qgpu_energies;
+
+/* Per-state Q energies, the Q_ENERGIES record of src/nrgy.f90:56-63 with
+   one group-contribution array (arrays = 1). */
+typedef struct qgpu_qenergy {
+    double lambda;
+    double q_bond, q_angle, q_torsion, q_improper;
+    double qq_el, qq_vdw, qp_el, qp_vdw, qw_el, qw_vdw, qx_el, qx_vdw;
+    double restraint, total;
+} qgpu_qenergy;
+
+/* Which terms qgpu_forces evaluates.  The drop-in split keeps restraints and
+   classical bonded terms on the host (pot_energy, src/md.f90:16100-16150);
+   the persistent run mode needs all of them on the device. */
+#define QGPU_TERMS_NONBOND   0x1   /* pot_energy_nonbonds: pp pw qp ww qw + LRF */
+#define QGPU_TERMS_QQ        0x2   /* nonbond_qq                                 */
+#define QGPU_TERMS_QBONDED   0x4   /* qbond/qangle/qtorsion/qimproper            */
+#define QGPU_TERMS_BONDED    0x8   /* pot_energy_bonds                           */
+#define QGPU_TERMS_RESTRAINT 0x10  /* fix_shell + restrain_solvent               */
+#define QGPU_TERMS_ALL       0x1f
+
+typedef struct qgpu_handle qgpu_handle;
+
+/* Energy sink for qgpu_run_block: called on the host after the block with
+   one row per (trajectory, recorded step). */
+typedef void (*qgpu_ene_sink)(void *user, int32_t traj, int32_t step,
+                              const qgpu_qenergy *eq, int32_t nstates,
+                              const qgpu_energies *e);
+
+/* ---- lifetime ----------------------------------------------------------- */
+/* Copies the descriptors to the device.  Replaces the data set-up that the
+   qdyn master performs before md_run (src/qdyn.f90:110-137).  descs[t]
+   describes trajectory t; the host keeps ownership of its arrays. */
+int qgpu_create(const qgpu_system_desc *descs, int32_t ntraj, qgpu_handle **out);
+int qgpu_destroy(qgpu_handle *h);
+int qgpu_last_error(char *buf, int32_t len);
+int qgpu_ntraj(const qgpu_handle *h);
+
+/* ---- state transfer ----------------------------------------------------- */
+int qgpu_set_coords(qgpu_handle *h, int32_t traj, const double *x, const double *v);
+int qgpu_get_coords(qgpu_handle *h, int32_t traj, double *x, double *v);
+
+/* ---- drop-in call points ------------------------------------------------ */
+/* make_pair_lists (src/md.f90:5985-6071): group centres, pp/pw/ww lists with
+   LRF multipoles for pairs beyond the cut-offs, and (first call only, as the
+   reference with Rcq > rexcl_o) the qp and qw lists.  All trajectories. */
+int qgpu_build_lists(qgpu_handle *h);
+
+/* pot_energy (src/md.f90:16015-16221) restricted to `terms`: forces d (3N,
+   may be NULL), energies E and per-state EQ[nstates] (may be NULL) of
+   trajectory traj.  Evaluates every trajectory; copies back one. */
+int qgpu_forces(qgpu_handle *h, int32_t traj, int32_t terms,
+                double *d, qgpu_energies *E, qgpu_qenergy *EQ);
+
+/* shake (src/md.f90:17581-17679) on trajectory traj: xx = coordinates before
+   the update, x = after; x is corrected in place.  niter = average
+   iterations per molecule, as the reference returns. */
+int qgpu_shake(qgpu_handle *h, int32_t traj, const double *xx, double *x, int32_t *niter);
+
+/* ---- persistent mode ---------------------------------------------------- */
+/* Runs nsteps MD steps of every trajectory on the device (Berendsen leap-frog,
+   SHAKE, lists every NBcycle), each NBcycle-step block replayed from a CUDA
+   graph.  Energies of every `ene_every`-th step are collected on the device
+   and handed to `sink` after the block (sink may be NULL). */
+int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every,
+             qgpu_ene_sink sink, void *user);
+
+/* ---- inspection (tests and tools) --------------------------------------- */
+/* Near charge-group pairs of the last list build, one row per unordered pair
+   (g1 < g2), with g1,g2 0-based group indices.  Returns the count in *npairs;
+   rows are written only if cap >= count. */
+int qgpu_get_group_pairs(qgpu_handle *h, int32_t traj, int32_t *pairs, int64_t cap, int64_t *npairs);
+/* LRF records of the last list build: ncgp rows of 3 centre + 1 + 3 + 9 + 27
+   doubles (cgp_cent, phi0, phi1, phi2, phi3), the LRF_TYPE of md.f90:444-450. */
+int qgpu_get_lrf(qgpu_handle *h, int32_t traj, double *lrf43);
+/* Last temperature record: Temp, Tfree, Tscale_solute, Tscale_solvent. */
+int qgpu_get_temperature(qgpu_handle *h, int32_t traj, double *out4);
+/* Kernel launches issued by the library since creation. */
+int64_t qgpu_kernel_launches(const qgpu_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QGPU_H */

@@ -1,0 +1,146 @@
+"""ctypes wrapper of the FP64 C oracle (oracle/qoracle.c) -- test infrastructure.
+
+Builds liboracle on first use (make in this directory).  The engine never
+imports this module; tests, smoke() and bench.py's CPU baseline do.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from qsource_gb300.abi import Energies, QEnergy, SystemDesc
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(_HERE, "_build", "libqoracle.so")
+_lib = None
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        src = os.path.join(_HERE, "qoracle.c")
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+            build()
+        L = C.CDLL(LIB)
+        vp = C.c_void_p
+        L.oracle_create.restype = vp
+        L.oracle_create.argtypes = [C.POINTER(SystemDesc)]
+        L.oracle_destroy.argtypes = [vp]
+        L.oracle_set_coords.argtypes = [vp, vp, vp]
+        L.oracle_get_coords.argtypes = [vp, vp, vp]
+        L.oracle_make_pair_lists.argtypes = [vp]
+        L.oracle_get_list.restype = C.c_int64
+        L.oracle_get_list.argtypes = [vp, C.c_int, vp, C.c_int64]
+        L.oracle_get_lrf.argtypes = [vp, vp]
+        L.oracle_pot_energy.argtypes = [vp, C.c_int, vp, C.POINTER(Energies), C.POINTER(QEnergy)]
+        L.oracle_shake_arrays.restype = C.c_int
+        L.oracle_shake_arrays.argtypes = [vp, vp, vp]
+        L.oracle_maxwell.argtypes = [vp, C.c_double, C.c_int32]
+        L.oracle_initial_shaking.restype = C.c_int
+        L.oracle_initial_shaking.argtypes = [vp]
+        L.oracle_stop_cm_translation.argtypes = [vp]
+        L.oracle_temperature.argtypes = [vp, vp]
+        L.oracle_offdiag.argtypes = [vp, vp, vp]
+        L.oracle_md_run.restype = C.c_int
+        L.oracle_md_run.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(Energies), C.POINTER(QEnergy), vp]
+        L.oracle_get_energies.argtypes = [vp, C.POINTER(Energies), C.POINTER(QEnergy)]
+        L.oracle_sizeof_desc.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+LIST_NAMES = {"pp": 0, "pw": 1, "ww": 2, "qp": 3, "qw": 4}
+
+
+class Oracle:
+    """One trajectory of the FP64 reference restatement."""
+
+    def __init__(self, system):
+        self.system = system
+        self._desc = system.desc()
+        self.L = lib()
+        self.h = self.L.oracle_create(C.byref(self._desc))
+        self.S = system.nstates
+        self.N = system.natom
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.L.oracle_destroy(self.h)
+        except Exception:
+            pass
+
+    def set_coords(self, x=None, v=None):
+        self.L.oracle_set_coords(self.h, _p(None if x is None else np.ascontiguousarray(x, np.float64)),
+                                 _p(None if v is None else np.ascontiguousarray(v, np.float64)))
+
+    def coords(self):
+        x = np.zeros(3 * self.N); v = np.zeros(3 * self.N)
+        self.L.oracle_get_coords(self.h, _p(x), _p(v))
+        return x, v
+
+    def make_pair_lists(self):
+        self.L.oracle_make_pair_lists(self.h)
+
+    def get_list(self, name: str) -> np.ndarray:
+        w = LIST_NAMES[name]
+        n = self.L.oracle_get_list(self.h, w, None, 0)
+        out = np.zeros((max(n, 1), 3), dtype=np.int32)
+        self.L.oracle_get_list(self.h, w, _p(out), n)
+        return out[:n]
+
+    def get_lrf(self) -> np.ndarray:
+        out = np.zeros((len(self.system.cgp_first), 43))
+        self.L.oracle_get_lrf(self.h, _p(out))
+        return out
+
+    def pot_energy(self, terms: int = 0x1F):
+        d = np.zeros(3 * self.N)
+        E = Energies()
+        EQ = (QEnergy * max(self.S, 1))()
+        self.L.oracle_pot_energy(self.h, terms, _p(d), C.byref(E), EQ)
+        return d, E.as_dict(), [EQ[s].as_dict() for s in range(self.S)]
+
+    def shake(self, xx, x) -> int:
+        return self.L.oracle_shake_arrays(self.h, _p(xx), _p(x))
+
+    def maxwell(self, T: float, seed: int):
+        self.L.oracle_maxwell(self.h, T, seed)
+
+    def initial_shaking(self) -> int:
+        return self.L.oracle_initial_shaking(self.h)
+
+    def stop_cm_translation(self):
+        self.L.oracle_stop_cm_translation(self.h)
+
+    def temperature(self):
+        out = np.zeros(4)
+        self.L.oracle_temperature(self.h, _p(out))
+        return out
+
+    def offdiag(self):
+        n = len(self.system.offd)
+        H = np.zeros(max(n, 1)); r = np.zeros(max(n, 1))
+        self.L.oracle_offdiag(self.h, _p(H), _p(r))
+        return H[:n], r[:n]
+
+    def md_run(self, nsteps: int, terms: int = 0x1F):
+        E = (Energies * nsteps)()
+        EQ = (QEnergy * (nsteps * max(self.S, 1)))()
+        T = np.zeros(nsteps)
+        rc = self.L.oracle_md_run(self.h, nsteps, terms, E, EQ, _p(T))
+        rows = [E[k].as_dict() for k in range(nsteps)]
+        qrows = [[EQ[k * self.S + s].as_dict() for s in range(self.S)] for k in range(nsteps)]
+        return rc, rows, qrows, T

@@ -1,0 +1,1148 @@
+/*
+ * qoracle.c -- FP64 CPU restatement of the qdyn hot path (TEST INFRASTRUCTURE).
+ *
+ * This file is the parity oracle for the GB300 engine.  It is not part of the
+ * product: only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg load it, and only to check or time against it.
+ *
+ * It restates, in their serial (#else) branch semantics, the routines of the
+ * reference qusers/qsource (Q 5.06) listed below.  Every list is built in the
+ * reference's loop order (including the count-once parity rule), so list sets
+ * can be compared exactly.  Compiled with -ffp-contract=off so that the FP64
+ * cut-off tests round like a plain multiply/add sequence.
+ *
+ * Parity pin: tests/test_oracle_golden.py checks this file against the
+ * reference's own step-0 golden energies (tests/basic_tests/SPH_*_benchmark.en
+ * row 1, tests/test2/eval_test.sh:67, tests/test3/eval_test.sh:67).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include "qgpu.h"
+
+#define BOLTZ 0.001986          /* src/md.f90:54 */
+#define SHAKE_TOL 0.0001        /* src/md.f90:460 */
+#define SHAKE_MAX_ITER 1000     /* src/md.f90:461 */
+#define QREAL_EPS 1.0e-14       /* src/sizes.f90:48 (double build) */
+#define NLRF 43                 /* cent[3] phi0 phi1[3] phi2[9] phi3[27] */
+
+typedef struct { int32_t i, j; int8_t lj, qlj; } nbrec;
+
+typedef struct { nbrec *a; int64_t n, cap; } nblist;
+
+typedef struct oracle {
+    qgpu_system_desc d;
+    int N, S;
+    double *x, *v, *xx, *f, *winv;
+    int32_t *iwhich;            /* atom -> charge group */
+    double *lrf;                /* ncgp * NLRF */
+    nblist pp, pw, ww, qp, qw;
+    int qp_done, qw_done;
+    /* exclusion / 1-4 lookup: per solute atom sorted partner lists (j > i) */
+    int32_t *ex_first, *ex_j, *p14_first, *p14_j;
+    qgpu_energies E;
+    qgpu_qenergy EQ[QGPU_MAX_STATES];
+    double Hij[QGPU_MAX_STATES][QGPU_MAX_STATES];
+    double EMorseD[256];
+    /* temperature state */
+    double Temp, Tfree, Tfree_solute, Tfree_solvent, Tscale_solute, Tscale_solvent;
+    int32_t irand, rand_new;
+    int status;
+} oracle;
+
+/* ------------------------------------------------------------------ utils */
+static void *xmalloc(size_t n) { void *p = calloc(1, n ? n : 1); return p; }
+static void *dupbuf(const void *src, size_t n) {
+    void *p = xmalloc(n);
+    if (src && n) memcpy(p, src, n);
+    return p;
+}
+static void nb_push(nblist *l, int32_t i, int32_t j, int lj, int qlj) {
+    if (l->n == l->cap) {
+        l->cap = l->cap ? 2 * l->cap : 1024;
+        l->a = (nbrec *)realloc(l->a, (size_t)l->cap * sizeof(nbrec));
+    }
+    l->a[l->n].i = i; l->a[l->n].j = j; l->a[l->n].lj = (int8_t)lj; l->a[l->n].qlj = (int8_t)qlj;
+    l->n++;
+}
+static inline int ljcod(const oracle *o, int ti, int tj) { return o->d.ljcod[ti * o->d.natyps + tj]; }
+static inline double avdw(const oracle *o, int t, int c) { return o->d.avdw[t * 3 + c - 1]; }
+static inline double bvdw(const oracle *o, int t, int c) { return o->d.bvdw[t * 3 + c - 1]; }
+static inline int is_q(const oracle *o, int i) { return o->d.iqatom[i] >= 0; }
+static inline double qcrg(const oracle *o, int iq, int s) { return o->d.qcrg[iq * o->S + s]; }
+
+static int pair_in(const int32_t *first, const int32_t *js, int i, int j) {
+    for (int k = first[i]; k < first[i + 1]; ++k) if (js[k] == j) return 1;
+    return 0;
+}
+/* listex / listexlong lookup of src/md.f90:8116-8130 (pair stored once, i<j) */
+static int excluded(const oracle *o, int i, int j) {
+    if (i > j) { int t = i; i = j; j = t; }
+    return pair_in(o->ex_first, o->ex_j, i, j);
+}
+/* list14 / list14long lookup of src/md.f90:8144-8166 */
+static int is14(const oracle *o, int i, int j) {
+    if (i > j) { int t = i; i = j; j = t; }
+    return pair_in(o->p14_first, o->p14_j, i, j);
+}
+static void build_pair_csr(int n, int np, const int32_t *pairs, int32_t **first, int32_t **js) {
+    int32_t *f = (int32_t *)xmalloc((size_t)(n + 1) * sizeof(int32_t));
+    int32_t *j = (int32_t *)xmalloc((size_t)(np ? np : 1) * sizeof(int32_t));
+    for (int k = 0; k < np; ++k) {
+        int a = pairs[2 * k], b = pairs[2 * k + 1];
+        int lo = a < b ? a : b;
+        f[lo + 1]++;
+    }
+    for (int i = 0; i < n; ++i) f[i + 1] += f[i];
+    int32_t *fill = (int32_t *)xmalloc((size_t)(n + 1) * sizeof(int32_t));
+    memcpy(fill, f, (size_t)(n + 1) * sizeof(int32_t));
+    for (int k = 0; k < np; ++k) {
+        int a = pairs[2 * k], b = pairs[2 * k + 1];
+        int lo = a < b ? a : b, hi = a < b ? b : a;
+        j[fill[lo]++] = hi;
+    }
+    free(fill);
+    *first = f; *js = j;
+}
+
+/* ---------------------------------------------------------------- create */
+void *oracle_create(const qgpu_system_desc *in) {
+    oracle *o = (oracle *)xmalloc(sizeof(oracle));
+    o->d = *in;
+    int N = in->natom;
+    o->N = N; o->S = in->nstates;
+    o->x = (double *)dupbuf(in->x, 3 * (size_t)N * sizeof(double));
+    o->v = (double *)dupbuf(in->v, 3 * (size_t)N * sizeof(double));
+    o->xx = (double *)xmalloc(3 * (size_t)N * sizeof(double));
+    o->f = (double *)xmalloc(3 * (size_t)N * sizeof(double));
+    o->winv = (double *)xmalloc((size_t)N * sizeof(double));
+    /* winv = 1/mass (prep_sim, src/md.f90:16745) */
+    for (int i = 0; i < N; ++i) o->winv[i] = 1.0 / in->mass[in->iac[i]];
+    o->iwhich = (int32_t *)xmalloc((size_t)N * sizeof(int32_t));
+    for (int g = 0; g < in->ncgp; ++g)
+        for (int k = in->cgp_first[g]; k <= in->cgp_last[g]; ++k) o->iwhich[in->cgpatom[k]] = g;
+    o->lrf = (double *)xmalloc((size_t)in->ncgp * NLRF * sizeof(double));
+    build_pair_csr(N, in->nexcl, in->excl_pairs, &o->ex_first, &o->ex_j);
+    build_pair_csr(N, in->n14, in->pairs14, &o->p14_first, &o->p14_j);
+    for (int s = 0; s < o->S; ++s) o->EQ[s].lambda = in->lambda[s];
+    o->Tscale_solute = o->Tscale_solvent = 1.0;
+    return o;
+}
+
+void oracle_destroy(void *h) {
+    oracle *o = (oracle *)h;
+    if (!o) return;
+    free(o->x); free(o->v); free(o->xx); free(o->f); free(o->winv); free(o->iwhich); free(o->lrf);
+    free(o->pp.a); free(o->pw.a); free(o->ww.a); free(o->qp.a); free(o->qw.a);
+    free(o->ex_first); free(o->ex_j); free(o->p14_first); free(o->p14_j);
+    free(o);
+}
+
+void oracle_set_coords(void *h, const double *x, const double *v) {
+    oracle *o = (oracle *)h;
+    if (x) memcpy(o->x, x, 3 * (size_t)o->N * sizeof(double));
+    if (v) memcpy(o->v, v, 3 * (size_t)o->N * sizeof(double));
+}
+void oracle_get_coords(void *h, double *x, double *v) {
+    oracle *o = (oracle *)h;
+    if (x) memcpy(x, o->x, 3 * (size_t)o->N * sizeof(double));
+    if (v) memcpy(v, o->v, 3 * (size_t)o->N * sizeof(double));
+}
+
+/* ------------------------------------------------------------------ LRF */
+/* cgp_centers, src/md.f90:2253-2288 */
+static void cgp_centers(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    for (int g = 0; g < d->ncgp; ++g) {
+        double *r = o->lrf + (size_t)g * NLRF;
+        memset(r, 0, NLRF * sizeof(double));
+        for (int k = d->cgp_first[g]; k <= d->cgp_last[g]; ++k) {
+            int a = d->cgpatom[k];
+            r[0] += o->x[3 * a]; r[1] += o->x[3 * a + 1]; r[2] += o->x[3 * a + 2];
+        }
+        double n = (double)(d->cgp_last[g] - d->cgp_first[g] + 1);
+        r[0] /= n; r[1] /= n; r[2] /= n;
+    }
+}
+
+/* lrf_update(group1, group2), src/md.f90:5896-5981 (sphere: no shift).
+   Multipoles of the non-Q atoms of group1 expanded about the centre of group2.
+   phi2(a,b) and phi3(a,b,c) are stored row-major, index (a*3+b) and (a*9+b*3+c). */
+static void lrf_update(oracle *o, int g1, int g2) {
+    const qgpu_system_desc *d = &o->d;
+    double *r = o->lrf + (size_t)g2 * NLRF;
+    double *phi1 = r + 4, *phi2 = r + 7, *phi3 = r + 16;
+    for (int k = d->cgp_first[g1]; k <= d->cgp_last[g1]; ++k) {
+        int i = d->cgpatom[k];
+        if (is_q(o, i)) continue;
+        double dr[3] = { o->x[3 * i] - r[0], o->x[3 * i + 1] - r[1], o->x[3 * i + 2] - r[2] };
+        double r2 = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+        double f0 = d->crg[i] / (r2 * sqrt(r2));
+        double f1 = 3.0 * f0 / r2;
+        double f2 = -f1 / r2;
+        r[3] += f0 * r2;
+        for (int a = 0; a < 3; ++a) phi1[a] -= f0 * dr[a];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+                phi2[a * 3 + b] += f1 * dr[a] * dr[b] - (a == b ? f0 : 0.0);
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+                for (int c = 0; c < 3; ++c) {
+                    double t = (a == b ? dr[c] : 0.0) + (a == c ? dr[b] : 0.0) + (b == c ? dr[a] : 0.0);
+                    phi3[a * 9 + b * 3 + c] += f2 * (5.0 * dr[a] * dr[b] * dr[c] - r2 * t);
+                }
+    }
+}
+
+/* lrf_taylor, src/md.f90:5824-5891 */
+static void lrf_taylor(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    for (int i = 0; i < o->N; ++i) {
+        if (d->excl[i] || is_q(o, i)) continue;
+        const double *r = o->lrf + (size_t)o->iwhich[i] * NLRF;
+        const double *phi1 = r + 4, *phi2 = r + 7, *phi3 = r + 16;
+        double dr[3] = { r[0] - o->x[3 * i], r[1] - o->x[3 * i + 1], r[2] - o->x[3 * i + 2] };
+        double V = r[3] + phi1[0] * dr[0] + phi1[1] * dr[1] + phi1[2] * dr[2];
+        for (int a = 0; a < 3; ++a)
+            V += 0.5 * (phi2[a * 3] * dr[0] + phi2[a * 3 + 1] * dr[1] + phi2[a * 3 + 2] * dr[2]) * dr[a];
+        o->E.lrf += 0.5 * d->crg[i] * V;
+        for (int a = 0; a < 3; ++a) {
+            double df = phi1[a] + phi2[a * 3] * dr[0] + phi2[a * 3 + 1] * dr[1] + phi2[a * 3 + 2] * dr[2];
+            for (int b = 0; b < 3; ++b) {
+                const double *p = phi3 + a * 9 + b * 3;
+                df += 0.5 * (p[0] * dr[0] + p[1] * dr[1] + p[2] * dr[2]) * dr[b];
+            }
+            o->f[3 * i + a] -= d->crg[i] * df;
+        }
+    }
+}
+
+/* --------------------------------------------------------------- lists */
+static inline double dist2(const double *x, int i, int j) {
+    double a = x[3 * i] - x[3 * j], b = x[3 * i + 1] - x[3 * j + 1], c = x[3 * i + 2] - x[3 * j + 2];
+    return a * a + b * b + c * c;
+}
+/* count-once parity rule, src/md.f90:8075-8077 (1-based ig+jg has the same
+   parity as the 0-based sum) */
+static inline int parity_skip(int ig, int jg) {
+    return (ig > jg && ((ig + jg) & 1) == 0) || (ig < jg && ((ig + jg) & 1) == 1);
+}
+static int all_zero(const oracle *o, int i, int j) {
+    int ti = o->d.iac[i], tj = o->d.iac[j];
+    int c = ljcod(o, ti, tj);
+    return (o->d.crg[i] * o->d.crg[j] == 0.0) &&
+           (avdw(o, ti, c) * avdw(o, tj, c) == 0.0) &&
+           (bvdw(o, ti, c) * bvdw(o, tj, c) == 0.0);
+}
+
+/* nbpplist_lrf, src/md.f90:7998-8188 */
+static void nbpplist_lrf(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    double rc2 = d->Rcpp * d->Rcpp, rl2 = d->RcLRF * d->RcLRF;
+    o->pp.n = 0;
+    for (int ig = 0; ig < d->ncgp_solute; ++ig) {
+        int is = d->cgp_switch[ig];
+        if (d->excl[is]) continue;
+        for (int jg = 0; jg < d->ncgp_solute; ++jg) {
+            if (parity_skip(ig, jg)) continue;
+            int js = d->cgp_switch[jg];
+            if (d->excl[js]) continue;
+            double r2 = dist2(o->x, is, js);
+            if (r2 <= rc2) {
+                for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig]; ++ka) {
+                    int i = d->cgpatom[ka];
+                    if (is_q(o, i)) continue;
+                    for (int kb = d->cgp_first[jg]; kb <= d->cgp_last[jg]; ++kb) {
+                        int j = d->cgpatom[kb];
+                        if (ig == jg && i >= j) continue;
+                        if (is_q(o, j)) continue;
+                        if (all_zero(o, i, j)) continue;
+                        if (excluded(o, i, j)) continue;
+                        int lj = ljcod(o, d->iac[i], d->iac[j]);
+                        if (is14(o, i, j)) lj = 3;
+                        nb_push(&o->pp, i, j, lj, lj);
+                    }
+                }
+            } else if (d->use_LRF && r2 <= rl2) {
+                lrf_update(o, ig, jg);
+                lrf_update(o, jg, ig);
+            }
+        }
+    }
+}
+
+/* nbpwlist_lrf, src/md.f90:9300-9429 */
+static void nbpwlist_lrf(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    double rc2 = d->Rcpw * d->Rcpw, rl2 = d->RcLRF * d->RcLRF;
+    o->pw.n = 0;
+    for (int ig = 0; ig < d->ncgp_solute; ++ig) {
+        int is = d->cgp_switch[ig];
+        if (d->excl[is]) continue;
+        for (int jw = 0; jw < d->nwat; ++jw) {
+            int ja = d->nat_solute + 3 * jw;
+            int jg = o->iwhich[ja];
+            if (d->excl[ja]) continue;
+            double r2 = dist2(o->x, is, ja);
+            if (r2 <= rc2) {
+                for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig]; ++ka) {
+                    int i = d->cgpatom[ka];
+                    if (is_q(o, i)) continue;
+                    for (int s = 0; s < 3; ++s) {
+                        int j = ja + s;
+                        if (all_zero(o, i, j)) continue;
+                        nb_push(&o->pw, i, j, ljcod(o, d->iac[i], d->iac[j]), 0);
+                    }
+                }
+            } else if (d->use_LRF && r2 <= rl2) {
+                lrf_update(o, ig, jg);
+                lrf_update(o, jg, ig);
+            }
+        }
+    }
+}
+
+/* nbqplist, src/md.f90:10215-10322 (built once when Rcq > rexcl_o) */
+static void nbqplist(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    if (o->qp_done && d->Rcq > d->rexcl_o) return;
+    o->qp.n = 0;
+    double rc2 = d->Rcq * d->Rcq;
+    if (d->nqat == 0) return;
+    for (int ig = 0; ig < d->ncgp_solute; ++ig) {
+        int ia = d->cgp_switch[ig];
+        if (d->excl[ia]) continue;
+        double a = o->x[3 * ia] - d->xpcent[0], b = o->x[3 * ia + 1] - d->xpcent[1], c = o->x[3 * ia + 2] - d->xpcent[2];
+        if (a * a + b * b + c * c > rc2) continue;
+        for (int k = d->cgp_first[ig]; k <= d->cgp_last[ig]; ++k) {
+            int i = d->cgpatom[k];
+            if (d->qp_skip[i]) continue;
+            for (int iq = 0; iq < d->nqat; ++iq) {
+                int lj = ljcod(o, d->iac[i], d->iac[d->iqseq[iq]]);
+                for (int p = 0; p < d->nqp14; ++p)
+                    if (d->qp14_pairs[2 * p] == iq && d->qp14_pairs[2 * p + 1] == i) lj = 3;
+                int qlj = lj == 2 ? 1 : lj;
+                nb_push(&o->qp, iq, i, lj, qlj);
+            }
+        }
+    }
+    o->qp_done = 1;
+}
+
+/* nbwwlist_lrf, src/md.f90:10897-11021 */
+static void nbwwlist_lrf(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    double rc2 = d->Rcww * d->Rcww, rl2 = d->RcLRF * d->RcLRF;
+    o->ww.n = 0;
+    int ns = d->nat_solute;
+    for (int iw = 0; iw < d->nwat; ++iw) {
+        int is = ns + 3 * iw;
+        if (d->excl[is]) continue;
+        int ig = o->iwhich[is];
+        for (int jw = 0; jw < d->nwat; ++jw) {
+            int ja = ns + 3 * jw;
+            if (d->excl[ja]) continue;
+            int jg = o->iwhich[ja];
+            if (parity_skip(iw, jw) || iw == jw) continue;
+            double r2 = dist2(o->x, is, ja);
+            if (r2 <= rc2) {
+                for (int la = 0; la < 3; ++la)
+                    for (int ka = 0; ka < 3; ++ka)
+                        nb_push(&o->ww, is + la, ja + ka, ljcod(o, d->iac[ns + la], d->iac[ns + ka]), 0);
+            } else if (d->use_LRF && r2 <= rl2) {
+                lrf_update(o, ig, jg);
+                lrf_update(o, jg, ig);
+            }
+        }
+    }
+}
+
+/* nbqwlist, src/md.f90:10464-10549 (built once when Rcq > rexcl_o) */
+static void nbqwlist(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    if (o->qw_done && d->Rcq > d->rexcl_o) return;
+    o->qw.n = 0;
+    if (d->nqat == 0) return;
+    double rc2 = d->Rcq * d->Rcq;
+    int ns = d->nat_solute;
+    for (int w = 0; w < d->nwat; ++w) {
+        int ia = ns + 3 * w;
+        if (d->excl[ia]) continue;
+        double a = o->x[3 * ia] - d->xpcent[0], b = o->x[3 * ia + 1] - d->xpcent[1], c = o->x[3 * ia + 2] - d->xpcent[2];
+        if (a * a + b * b + c * c <= rc2)
+            for (int iq = 0; iq < d->nqat; ++iq)
+                for (int s = 0; s < 3; ++s)
+                    nb_push(&o->qw, iq, ia + s, ljcod(o, d->iac[ns + s], d->iac[d->iqseq[iq]]), 0);
+    }
+    o->qw_done = 1;
+}
+
+/* make_pair_lists, sphere + LRF + switch atoms branch, src/md.f90:6043-6058 */
+void oracle_make_pair_lists(void *h) {
+    oracle *o = (oracle *)h;
+    if (o->d.use_LRF) cgp_centers(o);
+    nbpplist_lrf(o);
+    nbpwlist_lrf(o);
+    nbqplist(o);
+    nbwwlist_lrf(o);
+    nbqwlist(o);
+}
+
+/* list export: which 0 pp, 1 pw, 2 ww, 3 qp, 4 qw; rows (i, j, LJcod) */
+int64_t oracle_get_list(void *h, int which, int32_t *out, int64_t cap) {
+    oracle *o = (oracle *)h;
+    nblist *l = which == 0 ? &o->pp : which == 1 ? &o->pw : which == 2 ? &o->ww : which == 3 ? &o->qp : &o->qw;
+    if (out && cap >= l->n)
+        for (int64_t k = 0; k < l->n; ++k) {
+            out[3 * k] = l->a[k].i; out[3 * k + 1] = l->a[k].j; out[3 * k + 2] = l->a[k].lj;
+        }
+    return l->n;
+}
+void oracle_get_lrf(void *h, double *out) {
+    oracle *o = (oracle *)h;
+    memcpy(out, o->lrf, (size_t)o->d.ncgp * NLRF * sizeof(double));
+}
+
+/* ---------------------------------------------------------- nonbonds */
+#define DX(i, j) double dx1 = o->x[3 * (j)] - o->x[3 * (i)], dx2 = o->x[3 * (j) + 1] - o->x[3 * (i) + 1], \
+                        dx3 = o->x[3 * (j) + 2] - o->x[3 * (i) + 2]
+#define ADD_F(i, j, dv) do { double *F = o->f; \
+    F[3*(i)] -= (dv)*dx1; F[3*(i)+1] -= (dv)*dx2; F[3*(i)+2] -= (dv)*dx3; \
+    F[3*(j)] += (dv)*dx1; F[3*(j)+1] += (dv)*dx2; F[3*(j)+2] += (dv)*dx3; } while (0)
+
+/* nonbond_pp, src/md.f90:13069-13155 */
+static void nonbond_pp(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    for (int64_t k = 0; k < o->pp.n; ++k) {
+        int i = o->pp.a[k].i, j = o->pp.a[k].j, c = o->pp.a[k].lj;
+        DX(i, j);
+        double r2 = 1.0 / (dx1 * dx1 + dx2 * dx2 + dx3 * dx3), r = sqrt(r2), r6 = r2 * r2 * r2;
+        double Vel = d->crg[i] * d->crg[j] * r;
+        if (c == 3) Vel *= d->el14_scale;
+        double Va = r6 * r6 * avdw(o, d->iac[i], c) * avdw(o, d->iac[j], c);
+        double Vb = r6 * bvdw(o, d->iac[i], c) * bvdw(o, d->iac[j], c);
+        double dv = r2 * (-Vel - 12.0 * Va + 6.0 * Vb);
+        ADD_F(i, j, dv);
+        o->E.pp_el += Vel; o->E.pp_vdw += Va - Vb;
+    }
+}
+
+/* nonbond_pw, src/md.f90:13282-13365 */
+static void nonbond_pw(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    for (int64_t k = 0; k < o->pw.n; ++k) {
+        int i = o->pw.a[k].i, j = o->pw.a[k].j, c = o->pw.a[k].lj;
+        double aLJ = avdw(o, d->iac[i], c) * avdw(o, d->iac[j], c);
+        double bLJ = bvdw(o, d->iac[i], c) * bvdw(o, d->iac[j], c);
+        DX(i, j);
+        double r2 = 1.0 / (dx1 * dx1 + dx2 * dx2 + dx3 * dx3), r = sqrt(r2), r6 = r2 * r2 * r2;
+        double Vel = d->crg[i] * d->crg[j] * r, Va = aLJ * r6 * r6, Vb = bLJ * r6;
+        double dv = r2 * (-Vel - 12.0 * Va + 6.0 * Vb);
+        ADD_F(i, j, dv);
+        o->E.pw_el += Vel; o->E.pw_vdw += Va - Vb;
+    }
+}
+
+/* nonbond_qp (src/md.f90:13788-13921) and nonbond_qp_qvdw (14097-14230) */
+static void nonbond_qp(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    int nt = d->natyps + d->nqat;
+    for (int64_t k = 0; k < o->qp.n; ++k) {
+        int iq = o->qp.a[k].i, i = d->iqseq[iq], j = o->qp.a[k].j, c = o->qp.a[k].lj, qc = o->qp.a[k].qlj;
+        int tj = d->iac[j];
+        DX(i, j);
+        double r2 = dx1 * dx1 + dx2 * dx2 + dx3 * dx3;
+        if (!d->qvdw_flag) {
+            r2 = 1.0 / r2;
+            double r6 = r2 * r2 * r2, r = sqrt(r2);
+            for (int s = 0; s < o->S; ++s) {
+                int ti = d->iac[i];
+                double aLJ = avdw(o, ti, c) * avdw(o, tj, c), bLJ = bvdw(o, ti, c) * bvdw(o, tj, c);
+                double Vel = qcrg(o, iq, s) * d->crg[j] * r;
+                if (c == 3) Vel *= d->el14_scale;
+                double Va = aLJ * r6 * r6, Vb = bLJ * r6;
+                double dv = r2 * (-Vel - 12.0 * Va + 6.0 * Vb) * d->lambda[s];
+                ADD_F(i, j, dv);
+                o->EQ[s].qp_el += Vel; o->EQ[s].qp_vdw += Va - Vb;
+            }
+        } else {
+            double r6 = r2 * r2 * r2;
+            r2 = 1.0 / r2;
+            double r = sqrt(r2);
+            for (int s = 0; s < o->S; ++s) {
+                int ti = d->qiac[iq * o->S + s];
+                double aLJ = d->qavdw[ti * 3 + qc - 1] * avdw(o, tj, c);
+                double bLJ = d->qbvdw[ti * 3 + qc - 1] * bvdw(o, tj, c);
+                double Vel = qcrg(o, iq, s) * d->crg[j] * r;
+                if (c == 3) Vel *= d->el14_scale;
+                double r6sc = r6 + d->sc_lookup[((size_t)iq * nt + tj) * o->S + s];
+                double Va = aLJ / (r6sc * r6sc), Vb = bLJ / r6sc;
+                double dv = r2 * (-Vel - (12.0 * Va - 6.0 * Vb) * (r6 / r6sc)) * d->lambda[s];
+                ADD_F(i, j, dv);
+                o->EQ[s].qp_el += Vel; o->EQ[s].qp_vdw += Va - Vb;
+            }
+        }
+    }
+}
+
+/* nonbond_ww_spc, src/md.f90:15021-15119: records walked in strides of 3,
+   i cycles through the solvent atoms of the i-water, j is its partner O. */
+static void nonbond_ww_spc(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    int ichg = 0;
+    for (int64_t k = 0; k < o->ww.n; k += 3) {
+        if (ichg > 2) ichg = 0;
+        int i = o->ww.a[k].i, j = o->ww.a[k].j;
+        double q1 = d->chg_solv[ichg];
+        for (int ip = 0; ip < 3; ++ip) {
+            int ja = j + ip;
+            double q2 = d->chg_solv[ip];
+            DX(i, ja);
+            double r2 = dx1 * dx1 + dx2 * dx2 + dx3 * dx3;
+            double r6 = r2 * r2 * r2;
+            r2 = 1.0 / r2;
+            double r = sqrt(r2);
+            double Vel = q1 * q2 * r;
+            o->E.ww_el += Vel;
+            double dv = r2 * (-Vel);
+            if (ichg == 0 && ip == 0) {
+                int c = ljcod(o, d->iac[i], d->iac[j]);
+                double a1 = d->aLJ_solv[0 * 2 + c - 1], a2 = d->aLJ_solv[ip * 2 + c - 1];
+                double b1 = d->bLJ_solv[0 * 2 + c - 1], b2 = d->bLJ_solv[ip * 2 + c - 1];
+                r6 = 1.0 / r6;
+                double Va = a1 * a2 * r6 * r6, Vb = b1 * b2 * r6;
+                o->E.ww_vdw += Va - Vb;
+                dv += r2 * (-12.0 * Va + 6.0 * Vb);
+            }
+            ADD_F(i, ja, dv);
+        }
+        ichg++;
+    }
+}
+
+/* nonbond_qw_spc, src/md.f90:14411-14570 */
+static void nonbond_qw_spc(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    int nt = d->natyps + d->nqat;
+    for (int64_t k = 0; k < o->qw.n; k += 3) {
+        int iq = o->qw.a[k].i, i = d->iqseq[iq], j = o->qw.a[k].j, c = o->qw.a[k].lj;
+        {
+            DX(i, j);
+            double r2 = dx1 * dx1 + dx2 * dx2 + dx3 * dx3;
+            double r6hc = r2 * r2 * r2;
+            r2 = 1.0 / r2;
+            double r = sqrt(r2), r6sc = r6hc, Va = 0, Vb = 0;
+            if (!d->qvdw_flag) {
+                double r6 = 1.0 / r6hc;
+                double aLJ = avdw(o, d->iac[i], c), bLJ = bvdw(o, d->iac[i], c);
+                Va = aLJ * d->aLJ_solv[0 * 2 + c - 1] * r6 * r6;
+                Vb = bLJ * d->bLJ_solv[0 * 2 + c - 1] * r6;
+            }
+            double dv = 0;
+            for (int s = 0; s < o->S; ++s) {
+                if (d->qvdw_flag) {
+                    int ti = d->qiac[iq * o->S + s];
+                    double aLJ = d->qavdw[ti * 3], bLJ = d->qbvdw[ti * 3];
+                    /* softcore indexed by the LJ code (quirk of src/md.f90:14492) */
+                    r6sc = r6hc + d->sc_lookup[((size_t)iq * nt + (c - 1)) * o->S + s];
+                    Va = aLJ * d->aLJ_solv[0 * 2 + c - 1] / (r6sc * r6sc);
+                    Vb = bLJ * d->bLJ_solv[0 * 2 + c - 1] / r6sc;
+                }
+                double Vel = d->chg_solv[0] * qcrg(o, iq, s) * r;
+                dv += r2 * (-Vel - ((12.0 * Va - 6.0 * Vb) * (r6hc / r6sc))) * d->lambda[s];
+                o->EQ[s].qw_el += Vel; o->EQ[s].qw_vdw += Va - Vb;
+            }
+            ADD_F(i, j, dv);
+        }
+        for (int ip = 1; ip < 3; ++ip) {
+            int ja = j + ip;
+            DX(i, ja);
+            double r2 = 1.0 / (dx1 * dx1 + dx2 * dx2 + dx3 * dx3), r = sqrt(r2), dv = 0;
+            for (int s = 0; s < o->S; ++s) {
+                double Vel = d->chg_solv[ip] * qcrg(o, iq, s) * r;
+                o->EQ[s].qw_el += Vel;
+                dv -= r2 * Vel * d->lambda[s];
+            }
+            ADD_F(i, ja, dv);
+        }
+    }
+}
+
+/* nonbond_qq, src/md.f90:13491-13636 */
+static void nonbond_qq(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    int nt = d->natyps + d->nqat, off = 0;
+    for (int s = 0; s < o->S; ++s) {
+        for (int k = 0; k < d->nbqq_count[s]; ++k) {
+            int p = off + k;
+            int iq = d->nbqq_iq[p], i = d->iqseq[iq], j = d->nbqq_j[p], jq = d->nbqq_jq[p], c = d->nbqq_ljcod[p];
+            double qi = qcrg(o, iq, s), qj, aLJ, bLJ;
+            double els = d->nbqq_elscale[p];
+            if (!d->qvdw_flag) {
+                int ti = d->iac[i], tj = d->iac[j];
+                aLJ = avdw(o, ti, c) * avdw(o, tj, c);
+                bLJ = bvdw(o, ti, c) * bvdw(o, tj, c);
+                qj = jq >= 0 ? qcrg(o, jq, s) : d->crg[j];
+            } else {
+                int ti = d->qiac[iq * o->S + s];
+                aLJ = d->qavdw[ti * 3 + c - 1];
+                bLJ = d->qbvdw[ti * 3 + c - 1];
+                if (jq >= 0) {
+                    int tj = d->qiac[jq * o->S + s];
+                    aLJ *= d->qavdw[tj * 3 + c - 1];
+                    bLJ *= d->qbvdw[tj * 3 + c - 1];
+                    qj = qcrg(o, jq, s);
+                } else {
+                    if (c == 2) { aLJ = d->qavdw[ti * 3]; bLJ = d->qbvdw[ti * 3]; }
+                    int tj = d->iac[j];
+                    aLJ *= avdw(o, tj, c);
+                    bLJ *= bvdw(o, tj, c);
+                    qj = d->crg[j];
+                }
+            }
+            DX(i, j);
+            double r2 = dx1 * dx1 + dx2 * dx2 + dx3 * dx3;
+            double r6hc = r2 * r2 * r2;
+            /* softcore column natyps+jq (1-based), natyps for jq = 0: src/md.f90:13561 */
+            int col = jq >= 0 ? d->natyps + jq : d->natyps - 1;
+            double r6 = r2 * r2 * r2 + d->sc_lookup[((size_t)iq * nt + col) * o->S + s];
+            r6 = 1.0 / r6;
+            double r12 = r6 * r6;
+            r2 = 1.0 / r2;
+            double r = sqrt(r2);
+            double Vel = qi * qj * r * els, Va, Vb, dv;
+            if (c == 3) Vel *= d->el14_scale;
+            if (d->qvdw_flag && jq >= 0 && c == 2) {
+                Va = aLJ * exp(-bLJ / r);
+                Vb = 0.0;
+                dv = r2 * (-Vel - bLJ * Va / r) * d->lambda[s];
+            } else {
+                Va = aLJ * r12;
+                Vb = bLJ * r6;
+                dv = r2 * (-Vel - (12.0 * Va - 6.0 * Vb) * r6hc * r6) * d->lambda[s];
+            }
+            ADD_F(i, j, dv);
+            if (jq >= 0) { o->EQ[s].qq_el += Vel; o->EQ[s].qq_vdw += Va - Vb; }
+            else         { o->EQ[s].qp_el += Vel; o->EQ[s].qp_vdw += Va - Vb; }
+        }
+        off += d->nbqq_count[s];
+    }
+}
+
+/* ------------------------------------------------------------ bonded */
+static inline const double *X(const oracle *o, int i) { return o->x + 3 * i; }
+
+/* qbond, src/md.f90:17196-17240 (Morse + harmonic) */
+static void qbond(oracle *o, int s) {
+    const qgpu_system_desc *d = &o->d;
+    int w = 2 + o->S;
+    for (int b = 0; b < d->nqbond; ++b) {
+        int ic = d->qbnd[b * w + 2 + s];
+        if (ic <= 0) continue;
+        const double *L = d->qbondlib + 4 * (ic - 1);
+        int i = d->qbnd[b * w], j = d->qbnd[b * w + 1];
+        double rij[3] = { X(o, j)[0] - X(o, i)[0], X(o, j)[1] - X(o, i)[1], X(o, j)[2] - X(o, i)[2] };
+        double bl = sqrt(rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2]);
+        double db = bl - L[2];
+        double fexp = exp(-L[1] * db);
+        double be = L[0] * (fexp * fexp - 2.0 * fexp) + 0.5 * L[3] * db * db;
+        o->EQ[s].q_bond += be;
+        double dv = (2.0 * L[0] * L[1] * (fexp - fexp * fexp) + L[3] * db) * d->lambda[s] / bl;
+        for (int a = 0; a < 3; ++a) { o->f[3 * j + a] += rij[a] * dv; o->f[3 * i + a] -= rij[a] * dv; }
+        if (b < 256) o->EMorseD[b] = db > 0 ? -(fexp * fexp - 2.0 * fexp) : 1.0;
+    }
+}
+
+/* shared angle geometry: qangle (src/md.f90:17022-17102), angle (1130-1232) */
+static double angle_term(oracle *o, int i, int j, int k, double fk, double ang0, double scale, double *pe) {
+    double rji[3], rjk[3];
+    for (int a = 0; a < 3; ++a) { rji[a] = X(o, i)[a] - X(o, j)[a]; rjk[a] = X(o, k)[a] - X(o, j)[a]; }
+    double bji = sqrt(rji[0] * rji[0] + rji[1] * rji[1] + rji[2] * rji[2]);
+    double bjk = sqrt(rjk[0] * rjk[0] + rjk[1] * rjk[1] + rjk[2] * rjk[2]);
+    double scp = (rji[0] * rjk[0] + rji[1] * rjk[1] + rji[2] * rjk[2]) / (bji * bjk);
+    if (scp > 1.0) scp = 1.0;
+    if (scp < -1.0) scp = -1.0;
+    double ang = acos(scp), da = ang - ang0;
+    *pe = 0.5 * fk * da * da;
+    double dv = fk * da * scale;
+    double f1 = sin(ang);
+    if (fabs(f1) < QREAL_EPS) f1 = QREAL_EPS;
+    f1 = -1.0 / f1;
+    for (int a = 0; a < 3; ++a) {
+        double di = f1 * (rjk[a] / (bji * bjk) - scp * rji[a] / (bji * bji));
+        double dk = f1 * (rji[a] / (bji * bjk) - scp * rjk[a] / (bjk * bjk));
+        o->f[3 * i + a] += dv * di;
+        o->f[3 * k + a] += dv * dk;
+        o->f[3 * j + a] -= dv * (di + dk);
+    }
+    return da;
+}
+
+static void qangle(oracle *o, int s) {
+    const qgpu_system_desc *d = &o->d;
+    int w = 3 + o->S;
+    for (int a = 0; a < d->nqangle; ++a) {
+        int ic = d->qang[a * w + 3 + s];
+        if (ic <= 0) continue;
+        const double *L = d->qanglib + 4 * (ic - 1);
+        double pe;
+        angle_term(o, d->qang[a * w], d->qang[a * w + 1], d->qang[a * w + 2], L[0], L[1], d->lambda[s], &pe);
+        o->EQ[s].q_angle += pe;
+    }
+}
+
+/* torsion geometry shared by qtorsion/qimproper (src/md.f90:17241-17538) and
+   torsion/improper/improper2 (17907-18054, 3130-3423).  Returns phi and writes
+   the 12 derivative components dp[] of phi w.r.t. the four atoms. */
+static double dihedral(const oracle *o, int i, int j, int k, int l, double dp[12]) {
+    double rji[3], rjk[3], rkl[3], rnj[3], rnk[3];
+    for (int a = 0; a < 3; ++a) {
+        rji[a] = X(o, i)[a] - X(o, j)[a];
+        rjk[a] = X(o, k)[a] - X(o, j)[a];
+        rkl[a] = X(o, l)[a] - X(o, k)[a];
+    }
+    rnj[0] = rji[1] * rjk[2] - rji[2] * rjk[1];
+    rnj[1] = rji[2] * rjk[0] - rji[0] * rjk[2];
+    rnj[2] = rji[0] * rjk[1] - rji[1] * rjk[0];
+    rnk[0] = -rjk[1] * rkl[2] + rjk[2] * rkl[1];
+    rnk[1] = -rjk[2] * rkl[0] + rjk[0] * rkl[2];
+    rnk[2] = -rjk[0] * rkl[1] + rjk[1] * rkl[0];
+    double bj = sqrt(rnj[0] * rnj[0] + rnj[1] * rnj[1] + rnj[2] * rnj[2]);
+    double bk = sqrt(rnk[0] * rnk[0] + rnk[1] * rnk[1] + rnk[2] * rnk[2]);
+    double scp = (rnj[0] * rnk[0] + rnj[1] * rnk[1] + rnj[2] * rnk[2]) / (bj * bk);
+    if (scp > 1.0) scp = 1.0;
+    if (scp < -1.0) scp = -1.0;
+    double phi = acos(scp);
+    double sgn = rjk[0] * (rnj[1] * rnk[2] - rnj[2] * rnk[1]) + rjk[1] * (rnj[2] * rnk[0] - rnj[0] * rnk[2]) +
+                 rjk[2] * (rnj[0] * rnk[1] - rnj[1] * rnk[0]);
+    if (sgn < 0) phi = -phi;
+    double f1 = sin(phi);
+    if (fabs(f1) < QREAL_EPS) f1 = QREAL_EPS;
+    f1 = -1.0 / f1;
+    double di[3], dl[3], rki[3], rlj[3];
+    for (int a = 0; a < 3; ++a) {
+        di[a] = f1 * (rnk[a] / (bj * bk) - scp * rnj[a] / (bj * bj));
+        dl[a] = f1 * (rnj[a] / (bj * bk) - scp * rnk[a] / (bk * bk));
+        rki[a] = rji[a] - rjk[a];
+        rlj[a] = -rjk[a] - rkl[a];
+    }
+    dp[0] = rjk[1] * di[2] - rjk[2] * di[1];
+    dp[1] = rjk[2] * di[0] - rjk[0] * di[2];
+    dp[2] = rjk[0] * di[1] - rjk[1] * di[0];
+    dp[3] = rki[1] * di[2] - rki[2] * di[1] + rkl[1] * dl[2] - rkl[2] * dl[1];
+    dp[4] = rki[2] * di[0] - rki[0] * di[2] + rkl[2] * dl[0] - rkl[0] * dl[2];
+    dp[5] = rki[0] * di[1] - rki[1] * di[0] + rkl[0] * dl[1] - rkl[1] * dl[0];
+    dp[6] = rlj[1] * dl[2] - rlj[2] * dl[1] - rji[1] * di[2] + rji[2] * di[1];
+    dp[7] = rlj[2] * dl[0] - rlj[0] * dl[2] - rji[2] * di[0] + rji[0] * di[2];
+    dp[8] = rlj[0] * dl[1] - rlj[1] * dl[0] - rji[0] * di[1] + rji[1] * di[0];
+    dp[9] = rjk[1] * dl[2] - rjk[2] * dl[1];
+    dp[10] = rjk[2] * dl[0] - rjk[0] * dl[2];
+    dp[11] = rjk[0] * dl[1] - rjk[1] * dl[0];
+    return phi;
+}
+static void apply_dp(oracle *o, int i, int j, int k, int l, double dv, const double dp[12]) {
+    int at[4] = { i, j, k, l };
+    for (int n = 0; n < 4; ++n)
+        for (int a = 0; a < 3; ++a) o->f[3 * at[n] + a] += dv * dp[3 * n + a];
+}
+
+static void qtorsion(oracle *o, int s) {
+    const qgpu_system_desc *d = &o->d;
+    int w = 4 + o->S;
+    for (int p = 0; p < d->nqtor; ++p) {
+        int ic = d->qtor[p * w + 4 + s];
+        if (ic <= 0) continue;
+        const double *L = d->qtorlib + 3 * (ic - 1);
+        const int32_t *t = d->qtor + p * w;
+        double dp[12];
+        double phi = dihedral(o, t[0], t[1], t[2], t[3], dp);
+        double arg = L[1] * phi - L[2];
+        o->EQ[s].q_torsion += L[0] * (1.0 + cos(arg));
+        double dv = -L[1] * L[0] * sin(arg) * d->lambda[s];
+        apply_dp(o, t[0], t[1], t[2], t[3], dv, dp);
+    }
+}
+
+static void qimproper(oracle *o, int s) {
+    const qgpu_system_desc *d = &o->d;
+    int w = 4 + o->S;
+    const double pi = 4.0 * atan(1.0);
+    for (int p = 0; p < d->nqimp; ++p) {
+        int ic = d->qimp[p * w + 4 + s];
+        if (ic <= 0) continue;
+        const double *L = d->qimplib + 2 * (ic - 1);
+        const int32_t *t = d->qimp + p * w;
+        double dp[12];
+        double phi = dihedral(o, t[0], t[1], t[2], t[3], dp);
+        double arg = phi - L[1];
+        arg = arg - 2.0 * pi * nearbyint(arg / (2.0 * pi));
+        double dv = L[0] * arg;
+        o->EQ[s].q_improper += 0.5 * dv * arg;
+        apply_dp(o, t[0], t[1], t[2], t[3], dv * d->lambda[s], dp);
+    }
+}
+
+/* bond, src/md.f90:1340-1405 */
+static double bonds(oracle *o, int b0, int b1) {
+    const qgpu_system_desc *d = &o->d;
+    double e = 0;
+    for (int b = b0; b < b1; ++b) {
+        int i = d->bnd[3 * b], j = d->bnd[3 * b + 1], c = d->bnd[3 * b + 2];
+        const double *L = d->bondlib + 2 * (c - 1);
+        double rij[3] = { X(o, j)[0] - X(o, i)[0], X(o, j)[1] - X(o, i)[1], X(o, j)[2] - X(o, i)[2] };
+        double bl = sqrt(rij[0] * rij[0] + rij[1] * rij[1] + rij[2] * rij[2]);
+        double db = bl - L[1];
+        e += 0.5 * L[0] * db * db;
+        double dv = L[0] * db / bl;
+        for (int a = 0; a < 3; ++a) { o->f[3 * j + a] += rij[a] * dv; o->f[3 * i + a] -= rij[a] * dv; }
+    }
+    return e;
+}
+static double angles(oracle *o, int a0, int a1) {
+    const qgpu_system_desc *d = &o->d;
+    double e = 0;
+    for (int a = a0; a < a1; ++a) {
+        const int32_t *t = d->ang + 4 * a;
+        const double *L = d->anglib + 4 * (t[3] - 1);
+        double pe;
+        angle_term(o, t[0], t[1], t[2], L[0], L[1], 1.0, &pe);
+        e += pe;
+    }
+    return e;
+}
+/* torsion, src/md.f90:17907-18054 (loop runs backwards as the reference) */
+static double torsions(oracle *o, int p0, int p1) {
+    const qgpu_system_desc *d = &o->d;
+    double e = 0;
+    for (int p = p1 - 1; p >= p0; --p) {
+        const int32_t *t = d->tor + 5 * p;
+        const float *L = d->torlib + 4 * (t[4] - 1);
+        double dp[12];
+        double phi = dihedral(o, t[0], t[1], t[2], t[3], dp);
+        double arg = (double)L[1] * phi - (double)L[2];
+        e += (double)L[0] * (1.0 + cos(arg)) * (double)L[3];
+        double dv = -(double)L[1] * (double)L[0] * sin(arg) * (double)L[3];
+        apply_dp(o, t[0], t[1], t[2], t[3], dv, dp);
+    }
+    return e;
+}
+/* improper (harmonic, src/md.f90:3130-3283) and improper2 (periodic, 3284-3423) */
+static double impropers(oracle *o, int p0, int p1) {
+    const qgpu_system_desc *d = &o->d;
+    const double pi = 4.0 * atan(1.0);
+    double e = 0;
+    for (int p = p1 - 1; p >= p0; --p) {
+        const int32_t *t = d->imp + 5 * p;
+        const float *L = d->implib + 2 * (t[4] - 1);
+        double dp[12];
+        double phi = dihedral(o, t[0], t[1], t[2], t[3], dp);
+        double dv;
+        if (d->ff_type == 2) {
+            double arg = 2.0 * phi - (double)L[1];
+            e += (double)L[0] * (1.0 + cos(arg));
+            dv = -2.0 * (double)L[0] * sin(arg);
+        } else {
+            double arg = phi - (double)L[1];
+            arg = arg - 2.0 * pi * nearbyint(arg / (2.0 * pi));
+            dv = (double)L[0] * arg;
+            e += 0.5 * dv * arg;
+        }
+        apply_dp(o, t[0], t[1], t[2], t[3], dv, dp);
+    }
+    return e;
+}
+
+/* --------------------------------------------------------- restraints */
+/* fix_shell, src/md.f90:2816-2864 (no freeze) */
+static void fix_shell(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    for (int i = 0; i < d->nat_solute; ++i) {
+        if (!(d->excl[i] || d->shell[i])) continue;
+        double fk = d->excl[i] ? d->fk_fix : d->fk_pshell;
+        double dr[3] = { o->x[3 * i] - d->xtop[3 * i], o->x[3 * i + 1] - d->xtop[3 * i + 1], o->x[3 * i + 2] - d->xtop[3 * i + 2] };
+        double e = 0.5 * fk * (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+        if (d->excl[i]) o->E.rst_fix += e;
+        if (d->shell[i]) o->E.rst_shell += e;
+        for (int a = 0; a < 3; ++a) o->f[3 * i + a] += fk * dr[a];
+    }
+}
+
+/* restrain_solvent, src/md.f90:18055-18102 */
+static void restrain_solvent(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    double shift = d->fk_wsphere != 0.0 ? sqrt(BOLTZ * o->Tfree / d->fk_wsphere) : 0.0;
+    for (int g = d->ncgp_solute; g < d->ncgp; ++g) {
+        int i = d->cgp_switch[g];
+        if (d->excl[i]) continue;
+        double dr[3] = { o->x[3 * i] - d->xwcent[0], o->x[3 * i + 1] - d->xwcent[1], o->x[3 * i + 2] - d->xwcent[2] };
+        double b = sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+        double db = b - (d->rwat - shift), erst, dv;
+        if (db > 0) {
+            erst = 0.5 * d->fk_wsphere * db * db - d->Dwmz;
+            dv = d->fk_wsphere * db / b;
+        } else if (b > 0.0) {
+            double fexp = exp(d->awmz * db);
+            erst = d->Dwmz * (fexp * fexp - 2.0 * fexp);
+            dv = -2.0 * d->Dwmz * d->awmz * (fexp - fexp * fexp) / b;
+        } else { erst = 0; dv = 0; }
+        o->E.rst_solvent_radial += erst;
+        for (int a = 0; a < 3; ++a) o->f[3 * i + a] += dv * dr[a];
+    }
+}
+
+/* offdiag, src/md.f90:15444-15470 */
+void oracle_offdiag(void *h, double *Hij_out, double *rkl_out) {
+    oracle *o = (oracle *)h;
+    const qgpu_system_desc *d = &o->d;
+    for (int k = 0; k < d->noffd; ++k) {
+        int a = d->iqseq[d->offd_kl[2 * k]], b = d->iqseq[d->offd_kl[2 * k + 1]];
+        double r = sqrt(dist2(o->x, b, a));
+        double H = d->offd_Amu[2 * k] * exp(-d->offd_Amu[2 * k + 1] * r);
+        o->Hij[d->offd_ij[2 * k]][d->offd_ij[2 * k + 1]] = H;
+        if (Hij_out) Hij_out[k] = H;
+        if (rkl_out) rkl_out[k] = r;
+    }
+}
+
+/* ------------------------------------------------------- pot_energy */
+/* pot_energy, src/md.f90:16015-16221, restricted to `terms` */
+void oracle_pot_energy(void *h, int terms, double *d_out, qgpu_energies *E_out, qgpu_qenergy *EQ_out) {
+    oracle *o = (oracle *)h;
+    const qgpu_system_desc *d = &o->d;
+    double kin = o->E.kinetic;
+    memset(&o->E, 0, sizeof(o->E));
+    o->E.kinetic = kin;
+    for (int s = 0; s < o->S; ++s) {
+        double lam = o->EQ[s].lambda;
+        memset(&o->EQ[s], 0, sizeof(qgpu_qenergy));
+        o->EQ[s].lambda = lam;
+    }
+    memset(o->f, 0, 3 * (size_t)o->N * sizeof(double));
+    if (terms & QGPU_TERMS_NONBOND) {
+        nonbond_pp(o);
+        nonbond_pw(o);
+        nonbond_qp(o);
+        if (d->natom > d->nat_solute) { nonbond_ww_spc(o); nonbond_qw_spc(o); }
+        if (d->use_LRF) lrf_taylor(o);
+    }
+    if (terms & QGPU_TERMS_BONDED) {
+        o->E.p_bond = bonds(o, 0, d->nbonds_solute);
+        o->E.w_bond = bonds(o, d->nbonds_solute, d->nbonds);
+        o->E.p_angle = angles(o, 0, d->nangles_solute);
+        o->E.w_angle = angles(o, d->nangles_solute, d->nangles);
+        o->E.p_torsion = torsions(o, 0, d->ntors_solute);
+        o->E.w_torsion = torsions(o, d->ntors_solute, d->ntors);
+        o->E.p_improper = impropers(o, 0, d->nimps_solute);
+        o->E.w_improper = impropers(o, d->nimps_solute, d->nimps);
+    }
+    if (terms & QGPU_TERMS_RESTRAINT) {
+        fix_shell(o);
+        if (d->nwat > 0) restrain_solvent(o);
+    }
+    if (terms & QGPU_TERMS_QQ) nonbond_qq(o);
+    if (terms & QGPU_TERMS_QBONDED)
+        for (int s = 0; s < o->S; ++s) { qbond(o, s); qangle(o, s); qtorsion(o, s); qimproper(o, s); }
+    for (int s = 0; s < o->S; ++s) {
+        qgpu_qenergy *q = &o->EQ[s];
+        q->qx_el = q->qq_el + q->qp_el + q->qw_el;
+        q->qx_vdw = q->qq_vdw + q->qp_vdw + q->qw_vdw;
+        q->total = q->q_bond + q->q_angle + q->q_torsion + q->q_improper + q->qx_el + q->qx_vdw + q->restraint;
+        o->E.q_bond += q->q_bond * q->lambda;
+        o->E.q_angle += q->q_angle * q->lambda;
+        o->E.q_torsion += q->q_torsion * q->lambda;
+        o->E.q_improper += q->q_improper * q->lambda;
+        o->E.qx_el += q->qx_el * q->lambda;
+        o->E.qx_vdw += q->qx_vdw * q->lambda;
+        o->E.rst_protein += q->restraint * q->lambda;
+    }
+    qgpu_energies *e = &o->E;
+    e->rst_total = e->rst_fix + e->rst_shell + e->rst_protein + e->rst_solvent_radial + e->rst_water_pol;
+    e->potential = e->p_bond + e->w_bond + e->p_angle + e->w_angle + e->p_torsion + e->p_improper + e->pp_el +
+                   e->pp_vdw + e->pw_el + e->pw_vdw + e->ww_el + e->ww_vdw + e->q_bond + e->q_angle +
+                   e->q_torsion + e->q_improper + e->qx_el + e->qx_vdw + e->rst_total + e->lrf;
+    if (d_out) memcpy(d_out, o->f, 3 * (size_t)o->N * sizeof(double));
+    if (E_out) *E_out = o->E;
+    if (EQ_out) memcpy(EQ_out, o->EQ, (size_t)o->S * sizeof(qgpu_qenergy));
+}
+
+/* ------------------------------------------------------------- SHAKE */
+/* shake, src/md.f90:17581-17679.  Returns average iterations per molecule
+   (the reference divides by nmol), or -1 when a molecule fails to converge. */
+int oracle_shake_arrays(void *h, const double *xx, double *x) {
+    oracle *o = (oracle *)h;
+    const qgpu_system_desc *d = &o->d;
+    int total = 0;
+    uint8_t ready[64];
+    for (int m = 0; m < d->shake_molecules; ++m) {
+        int c0 = d->shake_first[m], nc = d->shake_first[m + 1] - c0;
+        if (nc > 64) return -2;
+        memset(ready, 0, sizeof(ready));
+        int nits = 0;
+        for (;;) {
+            for (int c = 0; c < nc; ++c) {
+                if (ready[c]) continue;
+                int i = d->shake_i[c0 + c], j = d->shake_j[c0 + c];
+                double d2 = d->shake_dist2[c0 + c];
+                double xij[3], xxij[3];
+                for (int a = 0; a < 3; ++a) { xij[a] = x[3 * i + a] - x[3 * j + a]; xxij[a] = xx[3 * i + a] - xx[3 * j + a]; }
+                double xij2 = xij[0] * xij[0] + xij[1] * xij[1] + xij[2] * xij[2];
+                double diff = d2 - xij2;
+                if (fabs(diff) < SHAKE_TOL * d2) ready[c] = 1;
+                double scp = xij[0] * xxij[0] + xij[1] * xxij[1] + xij[2] * xxij[2];
+                double corr = diff / (2.0 * scp * (o->winv[i] + o->winv[j]));
+                for (int a = 0; a < 3; ++a) {
+                    x[3 * i + a] += xxij[a] * corr * o->winv[i];
+                    x[3 * j + a] -= xxij[a] * corr * o->winv[j];
+                }
+            }
+            nits++;
+            int all = 1;
+            for (int c = 0; c < nc; ++c) all &= ready[c];
+            if (all) break;
+            if (nits >= SHAKE_MAX_ITER) return -1;
+        }
+        total += nits;
+    }
+    return d->shake_molecules ? total / (d->shake_molecules) : 0;
+}
+
+/* ------------------------------------------------------ thermostat/MD */
+/* randm, src/md.f90:17543-17577 (multiplicative congruential generator) */
+static double randm(oracle *o, int32_t *ig) {
+    const int32_t m = 100000000, m1 = 10000, mult = 31415821;
+    if (!o->rand_new) { o->rand_new = 1; o->irand = abs(*ig) % m; }
+    int32_t ih = o->irand / m1, il = o->irand % m1, mh = mult / m1, ml = mult % m1;
+    o->irand = ((ih * ml + il * mh) % m1) * m1 + il * ml;
+    o->irand = (o->irand + 1) % m;
+    double r = (double)(o->irand / 10) * 10 / (double)m;
+    if (r <= 0.0 || r > 1.0) r = 0.0;
+    *ig = o->irand;
+    return r;
+}
+/* gauss, src/md.f90:2866-2882 */
+static double gauss(oracle *o, double am, double sd, int32_t *ig) {
+    double a = 0;
+    for (int i = 0; i < 12; ++i) a += randm(o, ig);
+    return (a - 6.0) * sd + am;
+}
+/* maxwell, src/md.f90:6075-6094 */
+void oracle_maxwell(void *h, double Tmaxw, int32_t seed) {
+    oracle *o = (oracle *)h;
+    double kT = BOLTZ * Tmaxw;
+    for (int i = 0; i < o->N; ++i) {
+        double sd = sqrt(kT / o->d.mass[o->d.iac[i]]);
+        for (int a = 0; a < 3; ++a) o->v[3 * i + a] = gauss(o, 0.0, sd, &seed);
+    }
+}
+/* initial_shaking, src/md.f90:4430-4450 */
+int oracle_initial_shaking(void *h) {
+    oracle *o = (oracle *)h;
+    size_t n3 = 3 * (size_t)o->N;
+    memcpy(o->xx, o->x, n3 * sizeof(double));
+    int r1 = oracle_shake_arrays(o, o->xx, o->x);
+    if (r1 < 0) return r1;
+    for (size_t k = 0; k < n3; ++k) o->xx[k] = o->x[k] - o->d.dt * o->v[k];
+    int r2 = oracle_shake_arrays(o, o->x, o->xx);
+    if (r2 < 0) return r2;
+    for (size_t k = 0; k < n3; ++k) o->v[k] = (o->x[k] - o->xx[k]) / o->d.dt;
+    return 0;
+}
+/* stop_cm_translation, src/md.f90:17784-17816 */
+void oracle_stop_cm_translation(void *h) {
+    oracle *o = (oracle *)h;
+    double tot = 0, vcm[3] = { 0, 0, 0 };
+    for (int i = 0; i < o->N; ++i) {
+        double m = o->d.mass[o->d.iac[i]];
+        tot += m;
+        for (int a = 0; a < 3; ++a) vcm[a] += m * o->v[3 * i + a];
+    }
+    for (int a = 0; a < 3; ++a) vcm[a] /= tot;
+    for (int i = 0; i < o->N; ++i)
+        for (int a = 0; a < 3; ++a) o->v[3 * i + a] -= vcm[a];
+}
+
+/* temperature, src/md.f90:6098-6190 (Berendsen scale factors) */
+void oracle_temperature(void *h, double *out4) {
+    oracle *o = (oracle *)h;
+    const qgpu_system_desc *d = &o->d;
+    double Tsu = 0, Tfsu = 0, Tsv = 0, Tfsv = 0;
+    for (int i = 0; i < o->N; ++i) {
+        const double *v = o->v + 3 * i;
+        double ek = 0.5 * d->mass[d->iac[i]] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        if (i < d->nat_solute) { Tsu += ek; if (!d->excl[i]) Tfsu += ek; }
+        else { Tsv += ek; if (!d->excl[i]) Tfsv += ek; }
+    }
+    double Tfree = Tfsv + Tfsu, Temp = Tsu + Tsv;
+    o->E.kinetic = Temp;
+    Temp = 2.0 * Temp / BOLTZ / (double)d->Ndegf;
+    Tfree = 2.0 * Tfree / BOLTZ / (double)d->Ndegfree;
+    if (d->detail_temps) {
+        Tfsu = 2.0 * Tfsu / BOLTZ / (double)d->Ndegfree_solute;
+        Tfsv = 2.0 * Tfsv / BOLTZ / (double)d->Ndegfree_solvent;
+    }
+    double ts = o->Tscale_solvent, tu = o->Tscale_solute;
+    if (d->separate_scaling) {
+        if (Tfsv != 0) ts = d->Temp0 / Tfsv - 1.0;
+        ts = sqrt(1 + d->dt / d->tau_T * ts);
+        if (Tfsu != 0) tu = d->Temp0 / Tfsu - 1.0;
+        tu = sqrt(1 + d->dt / d->tau_T * tu);
+    } else {
+        if (Tfree != 0) ts = d->Temp0 / Tfree - 1.0;
+        ts = sqrt(1 + d->dt / d->tau_T * ts);
+        tu = ts;
+    }
+    o->Temp = Temp; o->Tfree = Tfree; o->Tfree_solute = Tfsu; o->Tfree_solvent = Tfsv;
+    o->Tscale_solute = tu; o->Tscale_solvent = ts;
+    if (out4) { out4[0] = Temp; out4[1] = Tfree; out4[2] = tu; out4[3] = ts; }
+}
+
+/* newvel_ber, src/md.f90:6194-6223 (leap-frog) */
+static void newvel_ber(oracle *o, double step, double ts, int a0, int a1) {
+    const double dt = o->d.dt;
+    for (int i = a0; i < a1; ++i)
+        for (int a = 0; a < 3; ++a) {
+            int k = 3 * i + a;
+            o->v[k] = (o->v[k] - o->f[k] * o->winv[i] * step) * ts;
+            o->xx[k] = o->x[k];
+            o->x[k] = o->x[k] + o->v[k] * dt;
+        }
+}
+
+/* md_run, Berendsen leap-frog branch (src/md.f90:6471-6664), with the
+   terms selected by `terms`.  Energies of every step are written to
+   E_rows[nsteps] / EQ_rows[nsteps*nstates] when given.  Returns 0 or a
+   QGPU_E_* status. */
+int oracle_md_run(void *h, int32_t nsteps, int32_t terms, qgpu_energies *E_rows, qgpu_qenergy *EQ_rows,
+                  double *temps) {
+    oracle *o = (oracle *)h;
+    const qgpu_system_desc *d = &o->d;
+    size_t n3 = 3 * (size_t)o->N;
+    for (int step = 0; step < nsteps; ++step) {
+        if (step % d->NBcycle == 0) oracle_make_pair_lists(o);
+        oracle_pot_energy(o, terms, NULL, NULL, NULL);
+        if (d->noffd > 0) oracle_offdiag(o, NULL, NULL);
+        newvel_ber(o, d->dt, o->Tscale_solute, 0, d->nat_solute);
+        newvel_ber(o, d->dt, o->Tscale_solvent, d->nat_solute, d->natom);
+        if (d->shake_molecules > 0) {
+            if (oracle_shake_arrays(o, o->xx, o->x) < 0) return QGPU_E_SHAKE;
+            for (size_t k = 0; k < n3; ++k) o->v[k] = (o->x[k] - o->xx[k]) / d->dt;
+        }
+        oracle_temperature(o, NULL);
+        if (o->Temp != o->Temp) return QGPU_E_NAN;
+        if (E_rows) E_rows[step] = o->E;
+        if (EQ_rows) memcpy(EQ_rows + (size_t)step * o->S, o->EQ, (size_t)o->S * sizeof(qgpu_qenergy));
+        if (temps) temps[step] = o->Temp;
+    }
+    return 0;
+}
+
+/* -------------------------------------------------------- inspection */
+void oracle_get_energies(void *h, qgpu_energies *E, qgpu_qenergy *EQ) {
+    oracle *o = (oracle *)h;
+    if (E) *E = o->E;
+    if (EQ) memcpy(EQ, o->EQ, (size_t)o->S * sizeof(qgpu_qenergy));
+}
+int oracle_sizeof_desc(void) { return (int)sizeof(qgpu_system_desc); }
+int oracle_sizeof_energies(void) { return (int)sizeof(qgpu_energies); }
+int oracle_sizeof_qenergy(void) { return (int)sizeof(qgpu_qenergy); }
