@@ -251,6 +251,12 @@ int qgpu_shake(qgpu_handle *h, int32_t traj, const double *xx, double *x, int32_
 int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every,
              qgpu_ene_sink sink, void *user);
 
+/* Queues nsteps of the same device work as qgpu_run without waiting for it
+   (no energy sink); a failure surfaces at the next qgpu_sync or qgpu_run. */
+int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every);
+/* Waits for all queued work of the handle and returns its status. */
+int qgpu_sync(qgpu_handle *h);
+
 /* ---- inspection (tests and tools) --------------------------------------- */
 /* Near charge-group pairs of the last list build, one row per unordered pair
    (g1 < g2), with g1,g2 0-based group indices.  Returns the count in *npairs;
@@ -263,6 +269,17 @@ int qgpu_get_lrf(qgpu_handle *h, int32_t traj, double *lrf43);
 int qgpu_get_temperature(qgpu_handle *h, int32_t traj, double *out4);
 /* Kernel launches issued by the library since creation. */
 int64_t qgpu_kernel_launches(const qgpu_handle *h);
+/* The CUDA stream (cudaStream_t) all of this handle's work runs on, so a
+   caller can order its own work or record timing events against it. */
+void *qgpu_stream(qgpu_handle *h);
+/* Runs nsteps MD steps kernel by kernel with CUDA events around each launch;
+   per distinct kernel: name (64-char slots in names), total ms, launches. */
+int qgpu_profile(qgpu_handle *h, int32_t nsteps, char *names, double *ms, int64_t *counts, int32_t cap,
+                 int32_t *nkernels);
+/* Measured FP32 FMA throughput of the device in TFLOP/s (an FMA-chain kernel
+   over all SMs, timed with CUDA events); the roofline denominator of the
+   FP32-bound pair and LRF kernels. */
+int qgpu_fp32_peak(double *tflops);
 
 #ifdef __cplusplus
 }

@@ -19,7 +19,12 @@ _lib = None
 
 
 def build() -> str:
-    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile qoracle.c with the flags of oracle/Makefile (gcc, no make needed)."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    cc = os.environ.get("CC", "gcc")
+    subprocess.run([cc, "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c11",
+                    "-I" + os.path.join(os.path.dirname(_HERE), "include"), "-shared", "-o", LIB,
+                    os.path.join(_HERE, "qoracle.c"), "-lm"], check=True)
     return LIB
 
 

@@ -107,10 +107,15 @@ EXPORTS = {
     "qgpu_forces": (_i32, [C.c_void_p, _i32, _i32, _P, C.POINTER(Energies), C.POINTER(QEnergy)]),
     "qgpu_shake": (_i32, [C.c_void_p, _i32, _P, _P, C.POINTER(_i32)]),
     "qgpu_run": (_i32, [C.c_void_p, _i32, _i32, ENE_SINK, C.c_void_p]),
+    "qgpu_enqueue": (_i32, [C.c_void_p, _i32, _i32]),
+    "qgpu_sync": (_i32, [C.c_void_p]),
     "qgpu_get_group_pairs": (_i32, [C.c_void_p, _i32, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "qgpu_get_lrf": (_i32, [C.c_void_p, _i32, _P]),
     "qgpu_get_temperature": (_i32, [C.c_void_p, _i32, _P]),
     "qgpu_kernel_launches": (C.c_int64, [C.c_void_p]),
+    "qgpu_stream": (C.c_void_p, [C.c_void_p]),
+    "qgpu_profile": (_i32, [C.c_void_p, _i32, C.c_char_p, _P, _P, _i32, C.POINTER(_i32)]),
+    "qgpu_fp32_peak": (_i32, [C.POINTER(_f64)]),
 }
 
 _lib = None

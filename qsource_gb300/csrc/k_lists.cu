@@ -1,0 +1,220 @@
+// k_lists.cu -- charge-group centres, the fused pair-list + LRF scan, and the
+// Q-atom list membership (make_pair_lists, src/md.f90:5985-6071).
+#include "qgpu_internal.cuh"
+
+// float mirror of the FP64 master coordinates: hi = float(x - origin),
+// lo = float((x - origin) - hi); w = scaled charge.
+__global__ void k_mirror(DevSys S) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.natom) return;
+    const TrajInfo &T = S.traj[S.atraj[i]];
+    float4 h, l;
+    double r0 = S.x[3 * i] - T.origin[0], r1 = S.x[3 * i + 1] - T.origin[1], r2 = S.x[3 * i + 2] - T.origin[2];
+    h.x = (float)r0; h.y = (float)r1; h.z = (float)r2; h.w = S.pos[i].w;
+    l.x = (float)(r0 - (double)h.x); l.y = (float)(r1 - (double)h.y); l.z = (float)(r2 - (double)h.z); l.w = 0.f;
+    S.pos[i] = h;
+    S.poslo[i] = l;
+}
+
+// cgp_centers, src/md.f90:2253-2288: mean of the member coordinates (FP64).
+__global__ void k_centers(DevSys S) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= S.ngrp) return;
+    double c0 = 0, c1 = 0, c2 = 0;
+    int a0 = S.g_start[g], a1 = S.g_start[g + 1];
+    for (int k = a0; k < a1; ++k) {
+        int a = S.g_atoms[k];
+        c0 += S.x[3 * a]; c1 += S.x[3 * a + 1]; c2 += S.x[3 * a + 2];
+    }
+    double n = (double)(a1 - a0);
+    S.g_cent[3 * g] = c0 / n; S.g_cent[3 * g + 1] = c1 / n; S.g_cent[3 * g + 2] = c2 / n;
+}
+
+// Cut-off decision of the list builders (nbpplist_lrf :8083-8090,
+// nbpwlist_lrf :9382-9388, nbwwlist_lrf :10982-10986): FP32 prefilter on the
+// hi/lo representative-atom distance, exact FP64 recheck inside a 1e-5 band
+// so the decision equals the FP64 test `r2 <= rc**2` bit for bit.
+__device__ __forceinline__ bool within(float d2, float rc2, double drc2, const double *x, int a, int b) {
+    if (d2 < rc2 * (1.f - 1e-5f)) return true;
+    if (d2 > rc2 * (1.f + 1e-5f)) return false;
+    return dist2_exact(x, a, b) <= drc2;
+}
+
+// One thread per target charge group; the block walks all groups of its
+// trajectory in shared-memory tiles.  Near groups (inside the pp/pw/ww
+// cut-off) go to the target's neighbour list (both directions: a full list),
+// far groups inside RcLRF add their non-Q atoms to the target's multipole
+// expansion (lrf_update, src/md.f90:5896-5981), accumulated as 24 symmetric
+// sums in FP32 and folded into FP64 every 4 tiles.
+__global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, const int *blk_tn, const int *blk_traj) {
+    __shared__ float4 s_hi[QG_TILE_G], s_lo[QG_TILE_G];
+    __shared__ int s_meta[QG_TILE_G], s_rep[QG_TILE_G], s_aoff[QG_TILE_G + 1];
+    __shared__ float4 s_atom[QG_TILE_A];
+    const int b = blockIdx.x;
+    const TrajInfo &T = S.traj[blk_traj[b]];
+    const int tid = threadIdx.x;
+    const int t = blk_t0[b] + tid;
+    const bool valid = tid < blk_tn[b];
+    int kind_t = 0, rt = 0;
+    bool active = false;
+    float4 th = make_float4(0, 0, 0, 0), tl = th;
+    float cx = 0, cy = 0, cz = 0;
+    if (valid) {
+        kind_t = S.g_kind[t];
+        rt = S.g_switch[t];
+        active = !S.g_excl[t];
+        th = S.pos[rt]; tl = S.poslo[rt];
+        cx = (float)(S.g_cent[3 * t] - T.origin[0]);
+        cy = (float)(S.g_cent[3 * t + 1] - T.origin[1]);
+        cz = (float)(S.g_cent[3 * t + 2] - T.origin[2]);
+    }
+    float acc[QG_NLRF];
+    double accd[QG_NLRF];
+#pragma unroll
+    for (int k = 0; k < QG_NLRF; ++k) { acc[k] = 0.f; accd[k] = 0.0; }
+    int cnt = 0;
+    const int cap = S.nb_cap;
+    const float rc2_lrf = T.rc2_lrf;
+    const bool lrf = T.use_lrf != 0;
+    for (int it = 0; it < T.ntile; ++it) {
+        const int tile = T.tile0 + it;
+        const int g0 = S.tile_g0[tile], g1 = S.tile_g1[tile], ng = g1 - g0;
+        const int ab = S.g_start[g0], ae = S.g_start[g1];
+        __syncthreads();
+        for (int k = tid; k < ng; k += blockDim.x) {
+            int g = g0 + k, ra = S.g_switch[g];
+            s_hi[k] = S.pos[ra]; s_lo[k] = S.poslo[ra];
+            s_meta[k] = S.g_kind[g] | (S.g_excl[g] ? 2 : 0);
+            s_rep[k] = ra;
+            s_aoff[k] = S.g_start[g] - ab;
+            if (k == ng - 1) s_aoff[ng] = ae - ab;
+        }
+        for (int k = tid; k < ae - ab; k += blockDim.x) {
+            int a = S.g_atoms[ab + k];
+            float4 p = S.pos[a];
+            if (S.aq[a] >= 0) p.w = 0.f;   // Q atoms do not contribute to the LRF
+            s_atom[k] = p;
+        }
+        __syncthreads();
+        if (active) {
+            for (int s = 0; s < ng; ++s) {
+                const int g = g0 + s;
+                const int meta = s_meta[s];
+                if ((meta & 2) || g == t) continue;
+                const int kind_s = meta & 1;
+                float rc2; double drc2;
+                if (kind_t & kind_s) { rc2 = T.rc2_ww; drc2 = T.drc2_ww; }
+                else if (kind_t | kind_s) { rc2 = T.rc2_pw; drc2 = T.drc2_pw; }
+                else { rc2 = T.rc2_pp; drc2 = T.drc2_pp; }
+                float3 d = dpos(th, tl, s_hi[s], s_lo[s]);
+                float d2 = d.x * d.x + d.y * d.y + d.z * d.z;
+                if (within(d2, rc2, drc2, S.x, rt, s_rep[s])) {
+                    if (cnt < cap) S.nb_list[(size_t)t * cap + cnt] = g;
+                    cnt++;
+                } else if (lrf && within(d2, rc2_lrf, T.drc2_lrf, S.x, rt, s_rep[s])) {
+                    for (int k = s_aoff[s]; k < s_aoff[s + 1]; ++k) {
+                        const float4 p = s_atom[k];
+                        if (p.w == 0.f) continue;
+                        const float dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
+                        const float r2 = dx * dx + dy * dy + dz * dz;
+                        const float ri = rsqrtf(r2), ri2 = ri * ri;
+                        const float f0 = p.w * ri * ri2;
+                        const float f1 = 3.f * f0 * ri2;
+                        const float f2 = -f1 * ri2;
+                        acc[0] += p.w * ri;
+                        acc[1] += f0;
+                        acc[2] += f0 * dx; acc[3] += f0 * dy; acc[4] += f0 * dz;
+                        const float ux = f1 * dx, uy = f1 * dy, uz = f1 * dz;
+                        acc[5] += ux; acc[6] += uy; acc[7] += uz;
+                        acc[8] += ux * dx; acc[9] += uy * dy; acc[10] += uz * dz;
+                        acc[11] += ux * dy; acc[12] += ux * dz; acc[13] += uy * dz;
+                        const float vx = f2 * dx, vy = f2 * dy, vz = f2 * dz;
+                        const float wxx = vx * dx, wyy = vy * dy, wzz = vz * dz, wxy = vx * dy;
+                        acc[14] += wxx * dx; acc[15] += wyy * dy; acc[16] += wzz * dz;
+                        acc[17] += wxx * dy; acc[18] += wxx * dz; acc[19] += wyy * dx;
+                        acc[20] += wzz * dx; acc[21] += wyy * dz; acc[22] += wzz * dy;
+                        acc[23] += wxy * dz;
+                    }
+                }
+            }
+            if ((it & 3) == 3) {
+#pragma unroll
+                for (int k = 0; k < QG_NLRF; ++k) { accd[k] += (double)acc[k]; acc[k] = 0.f; }
+            }
+        }
+    }
+    if (!valid) return;
+#pragma unroll
+    for (int k = 0; k < QG_NLRF; ++k) accd[k] += (double)acc[k];
+    S.nb_count[t] = cnt < cap ? cnt : cap;
+    if (cnt > cap) atomicOr(S.status, ST_LIST_OVERFLOW);
+    double *ph = S.g_phi + (size_t)t * QG_NLRF;
+#pragma unroll
+    for (int k = 0; k < QG_NLRF; ++k) ph[k] = accd[k];
+    // symmetric Taylor coefficients
+    float *pf = S.g_phif + (size_t)t * QG_NPHI;
+    const double q1x = accd[5], q1y = accd[6], q1z = accd[7];
+    pf[0] = (float)accd[0];
+    pf[1] = (float)(-accd[2]); pf[2] = (float)(-accd[3]); pf[3] = (float)(-accd[4]);
+    pf[4] = (float)(accd[8] - accd[1]); pf[5] = (float)(accd[9] - accd[1]); pf[6] = (float)(accd[10] - accd[1]);
+    pf[7] = (float)accd[11]; pf[8] = (float)accd[12]; pf[9] = (float)accd[13];
+    pf[10] = (float)(5.0 * accd[14] + 3.0 * q1x);
+    pf[11] = (float)(5.0 * accd[15] + 3.0 * q1y);
+    pf[12] = (float)(5.0 * accd[16] + 3.0 * q1z);
+    pf[13] = (float)(5.0 * accd[17] + q1y);   // xxy
+    pf[14] = (float)(5.0 * accd[18] + q1z);   // xxz
+    pf[15] = (float)(5.0 * accd[19] + q1x);   // xyy
+    pf[16] = (float)(5.0 * accd[20] + q1x);   // xzz
+    pf[17] = (float)(5.0 * accd[21] + q1z);   // yyz
+    pf[18] = (float)(5.0 * accd[22] + q1y);   // yzz
+    pf[19] = (float)(5.0 * accd[23]);         // xyz
+}
+
+// Q-atom list membership (nbqplist src/md.f90:10215-10322, nbqwlist
+// :10464-10549): waters whose O and solute groups whose switch atom lie within
+// Rcq of the solute centre.  Built once when Rcq > rexcl_o, as the reference.
+__global__ void k_qmember(DevSys S, int first) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= S.ngrp) return;
+    const TrajInfo &T = S.traj[S.g_traj[g]];
+    if (!first && T.q_static) return;
+    if (T.nqat == 0) return;
+    int sw = S.g_switch[g];
+    double a = S.x[3 * sw] - T.xpcent[0], b = S.x[3 * sw + 1] - T.xpcent[1], c = S.x[3 * sw + 2] - T.xpcent[2];
+    bool in = !S.g_excl[g] && (a * a + b * b + c * c <= T.drcq2);
+    if (S.g_kind[g]) {
+        S.qw_member[sw] = in ? 1 : 0;
+    } else {
+        for (int k = S.g_start[g]; k < S.g_start[g + 1]; ++k) {
+            int at = S.g_atoms[k];
+            S.qp_member[at] = (in && !S.qp_skip[at]) ? 1 : 0;
+        }
+    }
+}
+
+static inline int nblk(int n, int b) { return (n + b - 1) / b; }
+
+void launch_mirror(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
+    prof_begin(L, "k_mirror");
+    k_mirror<<<nblk(S.natom, 256), 256, 0, L.stream>>>(S);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
+    prof_begin(L, "k_centers");
+    k_centers<<<nblk(S.ngrp, 256), 256, 0, L.stream>>>(S);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_scan(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
+    prof_begin(L, "k_scan");
+    k_scan<<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_qmember(const DevSys &S, const BlockTables &B, LaunchCtx &L, int first) {
+    prof_begin(L, "k_qmember");
+    k_qmember<<<nblk(S.ngrp, 256), 256, 0, L.stream>>>(S, first);
+    prof_end(L);
+    (*L.nlaunch)++;
+}

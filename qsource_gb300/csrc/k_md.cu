@@ -1,0 +1,284 @@
+// k_md.cu -- the FP64 update of the master coordinates: Berendsen leap-frog
+// (newvel_ber, src/md.f90:6194-6223), SHAKE (shake, 17581-17679), the
+// temperature / Berendsen scale (temperature, 6098-6190) and the per-step
+// energy summary (pot_energy's assembly, 16186-16218).
+#include <math.h>
+
+#include "qgpu_internal.cuh"
+
+#define BOLTZ 0.001986          // src/md.f90:54
+#define SHAKE_TOL 0.0001        // src/md.f90:460
+#define SHAKE_MAX_ITER 1000     // src/md.f90:461
+
+// v = (v - d*winv*dt)*Tscale; xx = x; x += v*dt.  Consumes and clears the
+// fixed-point gradient.
+__global__ void k_integrate(DevSys S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.natom) return;
+    const int tr = S.atraj[i];
+    const TrajInfo &T = S.traj[tr];
+    const TrajState &TS = S.tstate[tr];
+    const double ts = (i - T.atom0) < T.nat_solute ? TS.Tscale_solute : TS.Tscale_solvent;
+    const double wi = S.winv[i], dt = T.dt;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int k = 3 * i + c;
+        const double g = fx_get(S.fx[k]);
+        S.fx[k] = 0ull;
+        const double v = (S.v[k] - g * wi * dt) * ts;
+        S.v[k] = v;
+        S.xx[k] = S.x[k];
+        S.x[k] = S.x[k] + v * dt;
+    }
+}
+
+// One thread per molecule with constraints: Gauss-Seidel sweeps until every
+// |d0^2 - r^2| < SHAKE_TOL*d0^2, at most SHAKE_MAX_ITER sweeps (then the
+// status word reports the failure; the loop is always bounded).
+__global__ void k_shake(DevSys S, int traj_filter) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= S.nshk_mol) return;
+    const int tr = S.shk_traj[m];
+    if (traj_filter >= 0 && tr != traj_filter) return;
+    const int c0 = S.shk_first[m], nc = S.shk_first[m + 1] - c0;
+    const double *x0 = S.xx;
+    double *x = S.x;
+    unsigned long long ready = 0ull;
+    const unsigned long long all = nc >= 64 ? ~0ull : ((1ull << nc) - 1ull);
+    int nits = 0;
+    for (;;) {
+        for (int c = 0; c < nc; ++c) {
+            if (ready & (1ull << c)) continue;
+            const int i = S.shk_i[c0 + c], j = S.shk_j[c0 + c];
+            const double d2 = S.shk_d2[c0 + c];
+            double xij[3], xxij[3];
+            for (int a = 0; a < 3; ++a) { xij[a] = x[3 * i + a] - x[3 * j + a]; xxij[a] = x0[3 * i + a] - x0[3 * j + a]; }
+            const double xij2 = xij[0] * xij[0] + xij[1] * xij[1] + xij[2] * xij[2];
+            const double diff = d2 - xij2;
+            if (fabs(diff) < SHAKE_TOL * d2) ready |= (1ull << c);
+            const double scp = xij[0] * xxij[0] + xij[1] * xxij[1] + xij[2] * xxij[2];
+            const double wi = S.winv[i], wj = S.winv[j];
+            const double corr = diff / (2.0 * scp * (wi + wj));
+            for (int a = 0; a < 3; ++a) {
+                x[3 * i + a] += xxij[a] * corr * wi;
+                x[3 * j + a] -= xxij[a] * corr * wj;
+            }
+        }
+        nits++;
+        if (ready == all) break;
+        if (nits >= SHAKE_MAX_ITER) { atomicOr(S.status, ST_SHAKE); break; }
+    }
+    atomicAdd(&S.tstate[tr].shake_iters, nits);
+}
+
+// After SHAKE: v = (x - xx)/dt for every atom (md_run, src/md.f90:6596-6597),
+// refresh the float mirror, and per-block kinetic-energy partial sums
+// (solute, free solute, solvent, free solvent) in a fixed reduction order.
+__global__ void __launch_bounds__(QG_BLOCK) k_post(DevSys S, const int *aall, int shake_on) {
+    __shared__ double red[4][QG_BLOCK / 32];
+    const int i = aall[blockIdx.x * blockDim.x + threadIdx.x];
+    double ek[4] = {0, 0, 0, 0};
+    if (i >= 0) {
+        const int tr = S.atraj[i];
+        const TrajInfo &T = S.traj[tr];
+        const double dt = T.dt;
+        double vv = 0;
+        for (int c = 0; c < 3; ++c) {
+            const int k = 3 * i + c;
+            double v = S.v[k];
+            if (shake_on) { v = (S.x[k] - S.xx[k]) / dt; S.v[k] = v; }
+            vv += v * v;
+        }
+        const double e = 0.5 * S.mass[i] * vv;
+        const bool solute = (i - T.atom0) < T.nat_solute;
+        const bool fr = !S.aexcl[i];
+        if (solute) { ek[0] = e; ek[1] = fr ? e : 0; } else { ek[2] = e; ek[3] = fr ? e : 0; }
+        float4 h, l;
+        const double r0 = S.x[3 * i] - T.origin[0], r1 = S.x[3 * i + 1] - T.origin[1], r2 = S.x[3 * i + 2] - T.origin[2];
+        h.x = (float)r0; h.y = (float)r1; h.z = (float)r2; h.w = S.pos[i].w;
+        l.x = (float)(r0 - (double)h.x); l.y = (float)(r1 - (double)h.y); l.z = (float)(r2 - (double)h.z); l.w = 0.f;
+        S.pos[i] = h; S.poslo[i] = l;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int k = 0; k < 4; ++k) {
+        const double v = warp_sum_d(ek[k]);
+        if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
+        S.ekin_part[(size_t)blockIdx.x * 4 + threadIdx.x] = s;
+    }
+}
+
+// One block per trajectory: temperature() (optional) and the energy summary
+// of pot_energy; writes a record row and clears the energy accumulators.
+__global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_base, int k, int ene_every, int rec_cap) {
+    const int tr = blockIdx.x;
+    if (threadIdx.x != 0) return;
+    const TrajInfo &T = S.traj[tr];
+    TrajState &TS = S.tstate[tr];
+    if (do_temp) {
+        double e[4] = {0, 0, 0, 0};
+        for (int b = 0; b < T.ekin_nblk; ++b)
+            for (int c = 0; c < 4; ++c) e[c] += S.ekin_part[(size_t)(T.ekin_blk0 + b) * 4 + c];
+        double Tfsu = e[1], Tfsv = e[3];
+        double Tfree = Tfsv + Tfsu, Temp = e[0] + e[2];
+        TS.Ekin = Temp;
+        Temp = 2.0 * Temp / BOLTZ / (double)T.Ndegf;
+        Tfree = 2.0 * Tfree / BOLTZ / (double)T.Ndegfree;
+        if (T.detail_temps) {
+            Tfsu = 2.0 * Tfsu / BOLTZ / (double)T.Ndegfree_solute;
+            Tfsv = 2.0 * Tfsv / BOLTZ / (double)T.Ndegfree_solvent;
+        }
+        double ts = TS.Tscale_solvent, tu = TS.Tscale_solute;
+        if (T.separate_scaling) {
+            if (Tfsv != 0) ts = T.Temp0 / Tfsv - 1.0;
+            ts = sqrt(1 + T.dt / T.tau_T * ts);
+            if (Tfsu != 0) tu = T.Temp0 / Tfsu - 1.0;
+            tu = sqrt(1 + T.dt / T.tau_T * tu);
+        } else {
+            if (Tfree != 0) ts = T.Temp0 / Tfree - 1.0;
+            ts = sqrt(1 + T.dt / T.tau_T * ts);
+            tu = ts;
+        }
+        TS.Temp = Temp; TS.Tfree = Tfree; TS.Tscale_solute = tu; TS.Tscale_solvent = ts;
+        if (Temp != Temp) atomicOr(S.status, ST_NAN);
+    }
+    unsigned long long *ea = S.eacc + (size_t)tr * QG_NE;
+    double v[QG_NE];
+    for (int s = 0; s < QG_NE; ++s) { v[s] = fx_get(ea[s]); ea[s] = 0ull; }
+    if (!rec) return;
+    const int step = *rec_base + k;
+    if (ene_every <= 0 || step % ene_every != 0) return;
+    const int row = step / ene_every - rec_base[1];
+    if (row < 0 || row >= rec_cap) return;
+    double *R = rec + ((size_t)row * S.ntraj + tr) * QG_REC;
+    // Q energies per state
+    double qb = 0, qa = 0, qt = 0, qi = 0, qxe = 0, qxv = 0;
+    for (int s = 0; s < QG_MAXS; ++s) {
+        double *q = R + QG_REC_EQ + 15 * s;
+        for (int c = 0; c < 15; ++c) q[c] = 0;
+        if (s >= T.nstates) continue;
+        const double *w = v + EA_Q0 + EQ_N * s;
+        const double lam = T.lambda[s];
+        q[0] = lam;
+        q[1] = w[EQ_B]; q[2] = w[EQ_A]; q[3] = w[EQ_T]; q[4] = w[EQ_I];
+        q[5] = w[EQ_QQ_EL]; q[6] = w[EQ_QQ_VDW]; q[7] = w[EQ_QP_EL]; q[8] = w[EQ_QP_VDW];
+        q[9] = w[EQ_QW_EL]; q[10] = w[EQ_QW_VDW];
+        q[11] = q[5] + q[7] + q[9];
+        q[12] = q[6] + q[8] + q[10];
+        q[13] = 0.0;
+        q[14] = q[1] + q[2] + q[3] + q[4] + q[11] + q[12] + q[13];
+        qb += q[1] * lam; qa += q[2] * lam; qt += q[3] * lam; qi += q[4] * lam;
+        qxe += q[11] * lam; qxv += q[12] * lam;
+    }
+    double *E = R + QG_REC_E;
+    // field order of qgpu_energies
+    E[2] = v[EA_LRF];
+    E[3] = v[EA_P_BOND]; E[4] = v[EA_P_ANG]; E[5] = v[EA_P_TOR]; E[6] = v[EA_P_IMP];
+    E[7] = v[EA_W_BOND]; E[8] = v[EA_W_ANG]; E[9] = v[EA_W_TOR]; E[10] = v[EA_W_IMP];
+    E[11] = qb; E[12] = qa; E[13] = qt; E[14] = qi;
+    E[15] = v[EA_PP_EL]; E[16] = v[EA_PP_VDW]; E[17] = v[EA_PW_EL]; E[18] = v[EA_PW_VDW];
+    E[19] = v[EA_WW_EL]; E[20] = v[EA_WW_VDW]; E[21] = qxe; E[22] = qxv;
+    E[24] = v[EA_RST_FIX]; E[25] = v[EA_RST_SHELL]; E[26] = 0.0; E[27] = v[EA_RST_RAD]; E[28] = 0.0;
+    E[23] = E[24] + E[25] + E[26] + E[27] + E[28];
+    E[0] = E[3] + E[7] + E[4] + E[8] + E[5] + E[6] + E[15] + E[16] + E[17] + E[18] + E[19] + E[20] + E[11] + E[12] +
+           E[13] + E[14] + E[21] + E[22] + E[23] + E[2];
+    E[1] = TS.Ekin;
+    R[QG_REC_T] = TS.Temp;
+    R[QG_REC_T + 1] = TS.Tfree;
+    for (int c = 0; c < 2 * QG_MAXOD; ++c) R[QG_REC_OD + c] = S.od_out[(size_t)tr * QG_MAXOD * 2 + c];
+}
+
+__global__ void k_tick(int *rec_base, int n) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *rec_base += n;
+}
+
+__global__ void k_grad_to_double(DevSys S, double *out, int atom0, int n3) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n3) return;
+    out[k] = fx_get(S.fx[3 * atom0 + k]);
+}
+
+static inline int nblk(int n, int b) { return (n + b - 1) / b; }
+
+void launch_integrate(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
+    prof_begin(L, "k_integrate");
+    k_integrate<<<nblk(S.natom, 256), 256, 0, L.stream>>>(S);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_shake(const DevSys &S, const BlockTables &B, LaunchCtx &L, int traj_filter) {
+    if (!S.nshk_mol) return;
+    prof_begin(L, "k_shake");
+    k_shake<<<nblk(S.nshk_mol, 128), 128, 0, L.stream>>>(S, traj_filter);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_post(const DevSys &S, const BlockTables &B, LaunchCtx &L, int shake_on) {
+    prof_begin(L, "k_post");
+    k_post<<<B.naall / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.aall, shake_on);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *rec, const int *rec_base, int k,
+                     int ene_every, int rec_cap) {
+    prof_begin(L, "k_finalize");
+    k_finalize<<<S.ntraj, 32, 0, L.stream>>>(S, do_temperature, rec, rec_base, k, ene_every, rec_cap);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_tick(LaunchCtx &L, int *rec_base, int n) {
+    prof_begin(L, "k_tick");
+    k_tick<<<1, 32, 0, L.stream>>>(rec_base, n);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_grad_to_double(const DevSys &S, LaunchCtx &L, double *out, int atom0, int natom) {
+    prof_begin(L, "k_grad_to_double");
+    k_grad_to_double<<<nblk(3 * natom, 256), 256, 0, L.stream>>>(S, out, atom0, 3 * natom);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+
+// FP32 FMA throughput probe: 8 independent FMA chains per thread.
+__global__ void k_fma_peak(float *out, int iters, float a, float b) {
+    float r0 = threadIdx.x, r1 = r0 + 1, r2 = r0 + 2, r3 = r0 + 3, r4 = r0 + 4, r5 = r0 + 5, r6 = r0 + 6, r7 = r0 + 7;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            r0 = fmaf(r0, a, b); r1 = fmaf(r1, a, b); r2 = fmaf(r2, a, b); r3 = fmaf(r3, a, b);
+            r4 = fmaf(r4, a, b); r5 = fmaf(r5, a, b); r6 = fmaf(r6, a, b); r7 = fmaf(r7, a, b);
+        }
+    }
+    const float s = r0 + r1 + r2 + r3 + r4 + r5 + r6 + r7;
+    if (s == 12345.678f) out[0] = s;   // keeps the chains live
+}
+
+extern "C" int qgpu_fp32_peak(double *tflops) {
+    if (!tflops) return 1;
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 2;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    float *out = nullptr;
+    if (cudaMalloc(&out, sizeof(float)) != cudaSuccess) return 2;
+    const int threads = 256, blocks = nsm * 8, iters = 2048;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    k_fma_peak<<<blocks, threads>>>(out, 64, 0.999f, 0.001f);   // warm-up
+    cudaEventRecord(a);
+    k_fma_peak<<<blocks, threads>>>(out, iters, 0.999f, 0.001f);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    const double flops = 2.0 * 8 * 16 * (double)iters * threads * blocks;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}

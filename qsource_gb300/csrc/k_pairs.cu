@@ -1,0 +1,564 @@
+// k_pairs.cu -- the per-step pair loops of pot_energy_nonbonds
+// (src/md.f90:16261-16344), in gather form over the full neighbour lists that
+// k_scan builds: every thread owns the atoms of one target and sums all their
+// pair terms, so each pair is evaluated from both sides with bitwise opposite
+// results and no force atomics are needed inside the loop.  Pair distances come
+// from hi/lo float coordinates; energies are Kahan-summed per thread and
+// reduced in FP64; forces go to the int64 fixed-point gradient once per atom.
+#include "qgpu_internal.cuh"
+
+__device__ __forceinline__ int traj_of_entry(const DevSys &S, int e, bool group) {
+    if (e < 0) return -1 - e;
+    return group ? S.g_traj[e] : S.atraj[e];
+}
+
+// Block-wide FP64 sum of `v` into energy slot `slot` of trajectory `traj`.
+__device__ __forceinline__ void block_energy(const DevSys &S, int traj, int slot, double v, double *red) {
+    v = warp_sum_d(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
+        if (s != 0.0) fx_add(S.eacc + (size_t)traj * QG_NE + slot, s, S.status);
+    }
+}
+
+__device__ __forceinline__ int ljc(const DevSys &S, const TrajInfo &T, int ta, int tb) {
+    return S.ljcod[T.lj0 + (ta - T.type0) * T.natyps + (tb - T.type0)];
+}
+
+// lrf_taylor (src/md.f90:5824-5891) for one atom: potential and field of the
+// group's Taylor expansion at dr = centre - x.  Adds q*df to the gradient.
+__device__ __forceinline__ float lrf_atom(const float *ph, float dx, float dy, float dz, float q, float &gx, float &gy,
+                                          float &gz) {
+    const float p2x = ph[4] * dx + ph[7] * dy + ph[8] * dz;
+    const float p2y = ph[7] * dx + ph[5] * dy + ph[9] * dz;
+    const float p2z = ph[8] * dx + ph[9] * dy + ph[6] * dz;
+    const float V = ph[0] + ph[1] * dx + ph[2] * dy + ph[3] * dz + 0.5f * (p2x * dx + p2y * dy + p2z * dz);
+    const float xx = dx * dx, yy = dy * dy, zz = dz * dz, xy = dx * dy, xz = dx * dz, yz = dy * dz;
+    // phi3 order: xxx yyy zzz xxy xxz xyy xzz yyz yzz xyz
+    const float tx = ph[10] * xx + ph[15] * yy + ph[16] * zz + 2.f * (ph[13] * xy + ph[14] * xz + ph[19] * yz);
+    const float ty = ph[13] * xx + ph[11] * yy + ph[18] * zz + 2.f * (ph[15] * xy + ph[19] * xz + ph[17] * yz);
+    const float tz = ph[14] * xx + ph[17] * yy + ph[12] * zz + 2.f * (ph[19] * xy + ph[16] * xz + ph[18] * yz);
+    gx -= q * (ph[1] + p2x + 0.5f * tx);
+    gy -= q * (ph[2] + p2y + 0.5f * ty);
+    gz -= q * (ph[3] + p2z + 0.5f * tz);
+    return 0.5f * q * V;
+}
+
+// FP64 inverse distance from the master coordinates (accurate-energy mode)
+__device__ __forceinline__ double rinv_d(const double *x, int a, int b) {
+    const double dx = x[3 * b] - x[3 * a], dy = x[3 * b + 1] - x[3 * a + 1], dz = x[3 * b + 2] - x[3 * a + 2];
+    return rsqrt(dx * dx + dy * dy + dz * dz);
+}
+
+// Energy accumulator: Kahan-summed FP32 partials, or FP64 terms.
+template <bool D>
+struct EAcc;
+template <>
+struct EAcc<false> {
+    KSum k;
+    float part;
+    __device__ __forceinline__ void zero() { k.zero(); part = 0.f; }
+    __device__ __forceinline__ void term(float f, double) { part += f; }
+    __device__ __forceinline__ void flush() { k.add(part); part = 0.f; }
+    __device__ __forceinline__ double value() const { return k.value(); }
+};
+template <>
+struct EAcc<true> {
+    double s;
+    __device__ __forceinline__ void zero() { s = 0.0; }
+    __device__ __forceinline__ void term(float, double d) { s += d; }
+    __device__ __forceinline__ void flush() {}
+    __device__ __forceinline__ double value() const { return s; }
+};
+
+// --------------------------------------------------------------- waters
+// nonbond_ww_spc (src/md.f90:15021-15119), the water side of nonbond_pw
+// (13282-13365) and lrf_taylor for the three water atoms.
+template <bool EACC>
+__global__ void __launch_bounds__(QG_BLOCK) k_nb_water(DevSys S, const int *wgrp, int lrf) {
+    __shared__ double red[QG_BLOCK / 32];
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w = wgrp[idx];
+    const int traj = traj_of_entry(S, w, true);
+    const TrajInfo &T = S.traj[traj];
+    EAcc<EACC> eww_el, eww_vdw, epw_el, epw_vdw;
+    eww_el.zero(); eww_vdw.zero(); epw_el.zero(); epw_vdw.zero();
+    float elrf = 0.f;
+    if (w >= 0 && !S.g_excl[w]) {
+        const int a0 = S.g_atoms[S.g_start[w]];
+        float4 ah[3], al[3];
+        int ta[3];
+        double qd[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            ah[a] = S.pos[a0 + a]; al[a] = S.poslo[a0 + a]; ta[a] = S.atype[a0 + a];
+            if (EACC) qd[a] = S.crg_d[a0 + a];
+        }
+        float gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0}, gz[3] = {0, 0, 0};
+        const int n = S.nb_count[w];
+        const int *lst = S.nb_list + (size_t)w * S.nb_cap;
+        const float wwA = T.ww_A, wwB = T.ww_B;
+        for (int k = 0; k < n; ++k) {
+            const int g = lst[k];
+            const int b0 = S.g_atoms[S.g_start[g]];
+            if (S.g_kind[g]) {
+                float4 bh[3], bl[3];
+#pragma unroll
+                for (int b = 0; b < 3; ++b) { bh[b] = S.pos[b0 + b]; bl[b] = S.poslo[b0 + b]; }
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+#pragma unroll
+                    for (int b = 0; b < 3; ++b) {
+                        const float3 d = dpos(ah[a], al[a], bh[b], bl[b]);
+                        const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+                        const float ri = rsqrtf(r2), ri2 = ri * ri;
+                        const float Vel = ah[a].w * bh[b].w * ri;
+                        float dv = -Vel * ri2;
+                        double rid = 0.0;
+                        if (EACC) rid = rinv_d(S.x, a0 + a, b0 + b);
+                        if (a == 0 && b == 0) {
+                            const float r6 = ri2 * ri2 * ri2;
+                            const float Va = wwA * r6 * r6, Vb = wwB * r6;
+                            dv += ri2 * (-12.f * Va + 6.f * Vb);
+                            double ed = 0.0;
+                            if (EACC) {
+                                const double r6d = rid * rid * rid * rid * rid * rid;
+                                ed = T.ww_Ad * r6d * r6d - T.ww_Bd * r6d;
+                            }
+                            eww_vdw.term(Va - Vb, ed);
+                        }
+                        eww_el.term(Vel, EACC ? qd[a] * S.crg_d[b0 + b] * rid : 0.0);
+                        gx[a] -= dv * d.x; gy[a] -= dv * d.y; gz[a] -= dv * d.z;
+                    }
+                }
+                eww_el.flush(); eww_vdw.flush();
+            } else {
+                for (int kk = S.g_start[g]; kk < S.g_start[g + 1]; ++kk) {
+                    const int b = S.g_atoms[kk];
+                    if (S.aq[b] >= 0) continue;
+                    const float4 bh = S.pos[b], bl = S.poslo[b];
+                    const int tb = S.atype[b];
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const int c = ljc(S, T, ta[a], tb);
+                        const float A = S.avdw[ta[a] * 3 + c - 1] * S.avdw[tb * 3 + c - 1];
+                        const float B = S.bvdw[ta[a] * 3 + c - 1] * S.bvdw[tb * 3 + c - 1];
+                        const float3 d = dpos(ah[a], al[a], bh, bl);
+                        const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+                        const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
+                        const float Vel = ah[a].w * bh.w * ri, Va = A * r6 * r6, Vb = B * r6;
+                        const float dv = ri2 * (-Vel - 12.f * Va + 6.f * Vb);
+                        double eld = 0.0, evd = 0.0;
+                        if (EACC) {
+                            const double rid = rinv_d(S.x, a0 + a, b), r6d = rid * rid * rid * rid * rid * rid;
+                            eld = qd[a] * S.crg_d[b] * rid;
+                            evd = S.avdw_d[ta[a] * 3 + c - 1] * S.avdw_d[tb * 3 + c - 1] * r6d * r6d -
+                                  S.bvdw_d[ta[a] * 3 + c - 1] * S.bvdw_d[tb * 3 + c - 1] * r6d;
+                        }
+                        epw_el.term(Vel, eld); epw_vdw.term(Va - Vb, evd);
+                        gx[a] -= dv * d.x; gy[a] -= dv * d.y; gz[a] -= dv * d.z;
+                    }
+                }
+                epw_el.flush(); epw_vdw.flush();
+            }
+        }
+        if (lrf) {
+            const float *ph = S.g_phif + (size_t)w * QG_NPHI;
+            const float cx = (float)(S.g_cent[3 * w] - T.origin[0]);
+            const float cy = (float)(S.g_cent[3 * w + 1] - T.origin[1]);
+            const float cz = (float)(S.g_cent[3 * w + 2] - T.origin[2]);
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                elrf += lrf_atom(ph, (cx - ah[a].x) - al[a].x, (cy - ah[a].y) - al[a].y, (cz - ah[a].z) - al[a].z,
+                                 ah[a].w, gx[a], gy[a], gz[a]);
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            fx_add(S.fx + 3 * (a0 + a), gx[a], S.status);
+            fx_add(S.fx + 3 * (a0 + a) + 1, gy[a], S.status);
+            fx_add(S.fx + 3 * (a0 + a) + 2, gz[a], S.status);
+        }
+    }
+    block_energy(S, traj, EA_WW_EL, 0.5 * eww_el.value(), red);
+    block_energy(S, traj, EA_WW_VDW, 0.5 * eww_vdw.value(), red);
+    block_energy(S, traj, EA_PW_EL, 0.5 * epw_el.value(), red);
+    block_energy(S, traj, EA_PW_VDW, 0.5 * epw_vdw.value(), red);
+    if (lrf) block_energy(S, traj, EA_LRF, (double)elrf, red);
+}
+
+// ------------------------------------------------------- solute atoms
+struct PairFlags { bool excl, p14; };
+
+__device__ __forceinline__ PairFlags pair_flags(const DevSys &S, int i, int j) {
+    PairFlags f{false, false};
+    const int rel = j - i;
+    if (rel >= -32 && rel < 32) {
+        f.excl = (S.exmask[i] >> (rel + 32)) & 1ull;
+        f.p14 = (S.p14mask[i] >> (rel + 32)) & 1ull;
+    } else {
+        for (int k = S.exlong_first[i]; k < S.exlong_first[i + 1]; ++k)
+            if (S.exlong_j[k] == j) {
+                if (S.exlong_kind[k]) f.p14 = true; else f.excl = true;
+            }
+    }
+    return f;
+}
+
+// nonbond_pp (src/md.f90:13069-13155) and the solute side of nonbond_pw, plus
+// lrf_taylor, for one non-Q solute atom.
+template <bool EACC>
+__global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *satom, int lrf) {
+    __shared__ double red[QG_BLOCK / 32];
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = satom[idx];
+    const int traj = traj_of_entry(S, i, false);
+    const TrajInfo &T = S.traj[traj];
+    EAcc<EACC> epp_el, epp_vdw, epw_el, epw_vdw;
+    epp_el.zero(); epp_vdw.zero(); epw_el.zero(); epw_vdw.zero();
+    float elrf = 0.f;
+    if (i >= 0 && S.aq[i] < 0 && !S.g_excl[S.agrp[i]]) {
+        const int g = S.agrp[i];
+        const float4 ih = S.pos[i], il = S.poslo[i];
+        const int ti = S.atype[i];
+        const double qi = EACC ? S.crg_d[i] : 0.0;
+        float gx = 0.f, gy = 0.f, gz = 0.f;
+        const float el14 = T.el14;
+        // one pair term: LJ code c, el14 factor for 1-4 pairs (nonbond_pp :13102-13111)
+        auto pair = [&](int j, int c, EAcc<EACC> &e_el, EAcc<EACC> &e_vdw) {
+            const int tj = S.atype[j];
+            const float4 jh = S.pos[j], jl = S.poslo[j];
+            const float A = S.avdw[ti * 3 + c - 1] * S.avdw[tj * 3 + c - 1];
+            const float B = S.bvdw[ti * 3 + c - 1] * S.bvdw[tj * 3 + c - 1];
+            const float3 d = dpos(ih, il, jh, jl);
+            const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+            const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
+            float Vel = ih.w * jh.w * ri;
+            if (c == 3) Vel *= el14;
+            const float Va = A * r6 * r6, Vb = B * r6;
+            const float dv = ri2 * (-Vel - 12.f * Va + 6.f * Vb);
+            double eld = 0.0, evd = 0.0;
+            if (EACC) {
+                const double rid = rinv_d(S.x, i, j), r6d = rid * rid * rid * rid * rid * rid;
+                eld = qi * S.crg_d[j] * rid;
+                if (c == 3) eld *= (double)T.el14d;
+                evd = S.avdw_d[ti * 3 + c - 1] * S.avdw_d[tj * 3 + c - 1] * r6d * r6d -
+                      S.bvdw_d[ti * 3 + c - 1] * S.bvdw_d[tj * 3 + c - 1] * r6d;
+            }
+            e_el.term(Vel, eld); e_vdw.term(Va - Vb, evd);
+            gx -= dv * d.x; gy -= dv * d.y; gz -= dv * d.z;
+        };
+        // pp pair with exclusion / 1-4 handling (nbpplist_lrf :8108-8166)
+        auto pp = [&](int j) {
+            const PairFlags f = pair_flags(S, i, j);
+            if (f.excl) return;
+            pair(j, f.p14 ? 3 : ljc(S, T, ti, S.atype[j]), epp_el, epp_vdw);
+        };
+        for (int kk = S.g_start[g]; kk < S.g_start[g + 1]; ++kk) {
+            const int j = S.g_atoms[kk];
+            if (j == i || S.aq[j] >= 0) continue;
+            pp(j);
+        }
+        epp_el.flush(); epp_vdw.flush();
+        const int n = S.nb_count[g];
+        const int *lst = S.nb_list + (size_t)g * S.nb_cap;
+        for (int k = 0; k < n; ++k) {
+            const int h = lst[k];
+            if (S.g_kind[h]) {
+                const int b0 = S.g_atoms[S.g_start[h]];
+#pragma unroll
+                for (int b = 0; b < 3; ++b) pair(b0 + b, ljc(S, T, ti, S.atype[b0 + b]), epw_el, epw_vdw);
+                epw_el.flush(); epw_vdw.flush();
+            } else {
+                for (int kk = S.g_start[h]; kk < S.g_start[h + 1]; ++kk) {
+                    const int j = S.g_atoms[kk];
+                    if (S.aq[j] >= 0) continue;
+                    pp(j);
+                }
+                epp_el.flush(); epp_vdw.flush();
+            }
+        }
+        if (lrf) {
+            const float *ph = S.g_phif + (size_t)g * QG_NPHI;
+            const float cx = (float)(S.g_cent[3 * g] - T.origin[0]);
+            const float cy = (float)(S.g_cent[3 * g + 1] - T.origin[1]);
+            const float cz = (float)(S.g_cent[3 * g + 2] - T.origin[2]);
+            elrf = lrf_atom(ph, (cx - ih.x) - il.x, (cy - ih.y) - il.y, (cz - ih.z) - il.z, ih.w, gx, gy, gz);
+        }
+        fx_add(S.fx + 3 * i, gx, S.status);
+        fx_add(S.fx + 3 * i + 1, gy, S.status);
+        fx_add(S.fx + 3 * i + 2, gz, S.status);
+    }
+    block_energy(S, traj, EA_PP_EL, 0.5 * epp_el.value(), red);
+    block_energy(S, traj, EA_PP_VDW, 0.5 * epp_vdw.value(), red);
+    block_energy(S, traj, EA_PW_EL, 0.5 * epw_el.value(), red);
+    block_energy(S, traj, EA_PW_VDW, 0.5 * epw_vdw.value(), red);
+    if (lrf) block_energy(S, traj, EA_LRF, (double)elrf, red);
+}
+
+// ------------------------------------------------------- Q-atom loops
+// The Q atoms of a trajectory are iterated uniformly by the whole block, so
+// the force on each Q atom is reduced per warp (shuffles) and then across the
+// block's warps in a fixed order -- deterministic without float atomics.
+struct QShared {
+    float4 qh[QG_MAXQ], ql[QG_MAXQ];
+    float qf[QG_BLOCK / 32][QG_MAXQ][3];
+    double red[QG_BLOCK / 32];
+};
+
+__device__ __forceinline__ void q_reduce_store(QShared &sh, int iq, float fx, float fy, float fz) {
+    fx = warp_sum_f(fx); fy = warp_sum_f(fy); fz = warp_sum_f(fz);
+    if ((threadIdx.x & 31) == 0) {
+        const int w = threadIdx.x >> 5;
+        sh.qf[w][iq][0] = fx; sh.qf[w][iq][1] = fy; sh.qf[w][iq][2] = fz;
+    }
+}
+__device__ __forceinline__ void q_flush(const DevSys &S, const TrajInfo &T, QShared &sh) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < T.nqat * 3; k += blockDim.x) {
+        const int iq = k / 3, c = k % 3;
+        double s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += (double)sh.qf[w][iq][c];
+        if (s != 0.0) fx_add(S.fx + 3 * S.q_atom[T.q0 + iq] + c, s, S.status);
+    }
+}
+__device__ __forceinline__ void q_load(const DevSys &S, const TrajInfo &T, QShared &sh) {
+    for (int k = threadIdx.x; k < T.nqat; k += blockDim.x) {
+        const int a = S.q_atom[T.q0 + k];
+        sh.qh[k] = S.pos[a]; sh.ql[k] = S.poslo[a];
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ bool eacc_on(const EaccSel &e) {
+    if (e.mode == EACC_FP64) return true;
+    if (e.mode == EACC_RECORD) return e.ene_every > 0 && ((e.recctl[0] + e.k) % e.ene_every) == 0;
+    return false;
+}
+
+// per-state energy sums of one thread: Kahan FP32, or FP64 terms
+struct QE {
+    KSum k[QG_MAXS];
+    double d[QG_MAXS];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int s = 0; s < QG_MAXS; ++s) { k[s].zero(); d[s] = 0.0; }
+    }
+    __device__ __forceinline__ double value(int s, bool acc) const { return acc ? d[s] : k[s].value(); }
+};
+
+// nonbond_qw_spc, src/md.f90:14411-14570.  One thread per water.
+__global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, EaccSel esel) {
+    __shared__ QShared sh;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w = wgrp[idx];
+    const int traj = traj_of_entry(S, w, true);
+    const TrajInfo &T = S.traj[traj];
+    const bool acc = eacc_on(esel);
+    q_load(S, T, sh);
+    const int NS = T.nstates;
+    QE eel, evdw;
+    eel.zero(); evdw.zero();
+    int a0 = -1;
+    bool valid = false;
+    if (w >= 0) {
+        a0 = S.g_atoms[S.g_start[w]];
+        valid = S.qw_member[a0] != 0;
+    }
+    float4 ah[3] = {}, al[3] = {};
+    if (valid)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { ah[a] = S.pos[a0 + a]; al[a] = S.poslo[a0 + a]; }
+    float gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0}, gz[3] = {0, 0, 0};
+    float lam[QG_MAXS];
+#pragma unroll
+    for (int s = 0; s < QG_MAXS; ++s) lam[s] = (float)T.lambda[s];
+    const int ntq = T.natyps + T.nqat;
+    for (int iq = 0; iq < T.nqat; ++iq) {
+        float qfx = 0.f, qfy = 0.f, qfz = 0.f;
+        if (valid) {
+            const int q = T.q0 + iq;
+            const int qa = S.q_atom[q];
+            // O: Coulomb + LJ (softcore column = LJ code of the pair, src/md.f90:14492)
+            {
+                const float3 d = dpos(sh.qh[iq], sh.ql[iq], ah[0], al[0]);
+                const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+                const float r6hc = r2 * r2 * r2, ri = rsqrtf(r2), ri2 = ri * ri;
+                double rid = 0.0, r6hcd = 0.0;
+                if (acc) { rid = rinv_d(S.x, qa, a0); const double r2d = 1.0 / (rid * rid); r6hcd = r2d * r2d * r2d; }
+                float dv = 0.f;
+#pragma unroll
+                for (int s = 0; s < QG_MAXS; ++s) {
+                    if (s >= NS) break;
+                    const size_t sci = (size_t)T.sc0 + ((size_t)iq * ntq + (size_t)(S.qw_lj[q] - 1)) * QG_MAXS + s;
+                    const float A = S.qw_A[q * QG_MAXS + s], B = S.qw_B[q * QG_MAXS + s];
+                    const float r6s = T.qvdw ? r6hc + S.sc_f[sci] : r6hc;
+                    const float Va = A / (r6s * r6s), Vb = B / r6s;
+                    const float Vel = ah[0].w * S.qcrg_f[q * QG_MAXS + s] * ri;
+                    dv += lam[s] * ri2 * (-Vel - (12.f * Va - 6.f * Vb) * (r6hc / r6s));
+                    if (acc) {
+                        const double r6sd = T.qvdw ? r6hcd + S.sc_d[sci] : r6hcd;
+                        eel.d[s] += S.crg_d[a0] * S.qcrg_d[q * QG_MAXS + s] * rid;
+                        evdw.d[s] += S.qw_Ad[q * QG_MAXS + s] / (r6sd * r6sd) - S.qw_Bd[q * QG_MAXS + s] / r6sd;
+                    } else {
+                        eel.k[s].add(Vel); evdw.k[s].add(Va - Vb);
+                    }
+                }
+                gx[0] += dv * d.x; gy[0] += dv * d.y; gz[0] += dv * d.z;
+                qfx -= dv * d.x; qfy -= dv * d.y; qfz -= dv * d.z;
+            }
+#pragma unroll
+            for (int a = 1; a < 3; ++a) {
+                const float3 d = dpos(sh.qh[iq], sh.ql[iq], ah[a], al[a]);
+                const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+                const float ri = rsqrtf(r2), ri2 = ri * ri;
+                const double rid = acc ? rinv_d(S.x, qa, a0 + a) : 0.0;
+                float dv = 0.f;
+#pragma unroll
+                for (int s = 0; s < QG_MAXS; ++s) {
+                    if (s >= NS) break;
+                    const float Vel = ah[a].w * S.qcrg_f[q * QG_MAXS + s] * ri;
+                    if (acc) eel.d[s] += S.crg_d[a0 + a] * S.qcrg_d[q * QG_MAXS + s] * rid;
+                    else eel.k[s].add(Vel);
+                    dv -= lam[s] * ri2 * Vel;
+                }
+                gx[a] += dv * d.x; gy[a] += dv * d.y; gz[a] += dv * d.z;
+                qfx -= dv * d.x; qfy -= dv * d.y; qfz -= dv * d.z;
+            }
+        }
+        q_reduce_store(sh, iq, qfx, qfy, qfz);
+    }
+    if (valid)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            fx_add(S.fx + 3 * (a0 + a), gx[a], S.status);
+            fx_add(S.fx + 3 * (a0 + a) + 1, gy[a], S.status);
+            fx_add(S.fx + 3 * (a0 + a) + 2, gz[a], S.status);
+        }
+    q_flush(S, T, sh);
+    for (int s = 0; s < NS; ++s) {
+        block_energy(S, traj, EA_Q0 + EQ_N * s + EQ_QW_EL, eel.value(s, acc), sh.red);
+        block_energy(S, traj, EA_Q0 + EQ_N * s + EQ_QW_VDW, evdw.value(s, acc), sh.red);
+    }
+}
+
+// nonbond_qp (src/md.f90:13788-13921) / nonbond_qp_qvdw (14097-14230).
+// One thread per solute atom of the qp list.
+__global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, EaccSel esel) {
+    __shared__ QShared sh;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = satom[idx];
+    const int traj = traj_of_entry(S, j, false);
+    const TrajInfo &T = S.traj[traj];
+    const bool acc = eacc_on(esel);
+    q_load(S, T, sh);
+    const int NS = T.nstates;
+    QE eel, evdw;
+    eel.zero(); evdw.zero();
+    const bool valid = j >= 0 && S.qp_member[j];
+    float4 jh = {}, jl = {};
+    int tj = 0;
+    if (valid) { jh = S.pos[j]; jl = S.poslo[j]; tj = S.atype[j]; }
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    const int ntq = T.natyps + T.nqat;
+    for (int iq = 0; iq < T.nqat; ++iq) {
+        float qfx = 0.f, qfy = 0.f, qfz = 0.f;
+        if (valid) {
+            const int q = T.q0 + iq;
+            const int qa = S.q_atom[q];
+            const int tq = S.atype[qa];
+            int c = ljc(S, T, tj, tq);
+            for (int k = S.qp14_first[j]; k < S.qp14_first[j + 1]; ++k)
+                if (S.qp14_q[k] == q) c = 3;
+            const int qc = c == 2 ? 1 : c;
+            const float3 d = dpos(sh.qh[iq], sh.ql[iq], jh, jl);
+            const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+            const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = r2 * r2 * r2;
+            double rid = 0.0, r6d = 0.0;
+            if (acc) { rid = rinv_d(S.x, qa, j); const double r2d = 1.0 / (rid * rid); r6d = r2d * r2d * r2d; }
+            float dv = 0.f;
+#pragma unroll
+            for (int s = 0; s < QG_MAXS; ++s) {
+                if (s >= NS) break;
+                float A, B, r6s;
+                double Ad = 0, Bd = 0, r6sd = r6d;
+                if (!T.qvdw) {
+                    A = S.avdw[tq * 3 + c - 1] * S.avdw[tj * 3 + c - 1];
+                    B = S.bvdw[tq * 3 + c - 1] * S.bvdw[tj * 3 + c - 1];
+                    r6s = r6;
+                    if (acc) {
+                        Ad = S.avdw_d[tq * 3 + c - 1] * S.avdw_d[tj * 3 + c - 1];
+                        Bd = S.bvdw_d[tq * 3 + c - 1] * S.bvdw_d[tj * 3 + c - 1];
+                    }
+                } else {
+                    const int qt = S.qiac[q * QG_MAXS + s];
+                    const size_t sci = (size_t)T.sc0 + ((size_t)iq * ntq + (tj - T.type0)) * QG_MAXS + s;
+                    A = S.qavdw[qt * 3 + qc - 1] * S.avdw[tj * 3 + c - 1];
+                    B = S.qbvdw[qt * 3 + qc - 1] * S.bvdw[tj * 3 + c - 1];
+                    r6s = r6 + S.sc_f[sci];
+                    if (acc) {
+                        Ad = S.qavdw_d[qt * 3 + qc - 1] * S.avdw_d[tj * 3 + c - 1];
+                        Bd = S.qbvdw_d[qt * 3 + qc - 1] * S.bvdw_d[tj * 3 + c - 1];
+                        r6sd = r6d + S.sc_d[sci];
+                    }
+                }
+                float Vel = S.qcrg_f[q * QG_MAXS + s] * jh.w * ri;
+                if (c == 3) Vel *= T.el14;
+                const float Va = A / (r6s * r6s), Vb = B / r6s;
+                dv += (float)T.lambda[s] * ri2 * (-Vel - (12.f * Va - 6.f * Vb) * (r6 / r6s));
+                if (acc) {
+                    double Veld = S.qcrg_d[q * QG_MAXS + s] * S.crg_d[j] * rid;
+                    if (c == 3) Veld *= T.el14d;
+                    eel.d[s] += Veld;
+                    evdw.d[s] += Ad / (r6sd * r6sd) - Bd / r6sd;
+                } else {
+                    eel.k[s].add(Vel); evdw.k[s].add(Va - Vb);
+                }
+            }
+            gx += dv * d.x; gy += dv * d.y; gz += dv * d.z;
+            qfx -= dv * d.x; qfy -= dv * d.y; qfz -= dv * d.z;
+        }
+        q_reduce_store(sh, iq, qfx, qfy, qfz);
+    }
+    if (valid) {
+        fx_add(S.fx + 3 * j, gx, S.status);
+        fx_add(S.fx + 3 * j + 1, gy, S.status);
+        fx_add(S.fx + 3 * j + 2, gz, S.status);
+    }
+    q_flush(S, T, sh);
+    for (int s = 0; s < NS; ++s) {
+        block_energy(S, traj, EA_Q0 + EQ_N * s + EQ_QP_EL, eel.value(s, acc), sh.red);
+        block_energy(S, traj, EA_Q0 + EQ_N * s + EQ_QP_VDW, evdw.value(s, acc), sh.red);
+    }
+}
+
+void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
+    if (!B.nwgrp) return;
+    if (fp64_energy) { prof_begin(L, "k_nb_water"); k_nb_water<true><<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf); prof_end(L); }
+    else { prof_begin(L, "k_nb_water"); k_nb_water<false><<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf); prof_end(L); }
+    (*L.nlaunch)++;
+}
+void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
+    if (!B.nsatom) return;
+    if (fp64_energy) { prof_begin(L, "k_nb_solute"); k_nb_solute<true><<<B.nsatom / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); prof_end(L); }
+    else { prof_begin(L, "k_nb_solute"); k_nb_solute<false><<<B.nsatom / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); prof_end(L); }
+    (*L.nlaunch)++;
+}
+void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
+    if (!B.nwgrp) return;
+    prof_begin(L, "k_qw");
+    k_qw<<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_qp(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
+    if (!B.nsatom) return;
+    prof_begin(L, "k_qp");
+    k_qp<<<B.nsatom / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, e);
+    prof_end(L);
+    (*L.nlaunch)++;
+}

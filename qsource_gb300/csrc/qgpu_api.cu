@@ -1,0 +1,944 @@
+// qgpu_api.cu -- host side of the engine: descriptor validation, the batch
+// layout in device memory, work tables, and the C-ABI of include/qgpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "qgpu_internal.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                            \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) return fail(QGPU_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+int upload(std::vector<void *> &allocs, const std::vector<T> &h, T **d) {
+    size_t n = h.size() ? h.size() : 1;
+    CK(cudaMalloc((void **)d, n * sizeof(T)));
+    allocs.push_back(*d);
+    if (h.size()) CK(cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    else CK(cudaMemset(*d, 0, sizeof(T)));
+    return 0;
+}
+template <class T>
+int alloc0(std::vector<void *> &allocs, size_t n, T **d) {
+    if (!n) n = 1;
+    CK(cudaMalloc((void **)d, n * sizeof(T)));
+    allocs.push_back(*d);
+    CK(cudaMemset(*d, 0, n * sizeof(T)));
+    return 0;
+}
+
+// pad a per-trajectory segment of a work list to a multiple of QG_BLOCK
+void pad(std::vector<int> &v, size_t seg_start, int traj) {
+    while ((v.size() - seg_start) % QG_BLOCK) v.push_back(-1 - traj);
+}
+
+}  // namespace
+
+struct qgpu_handle {
+    int ntraj = 0;
+    std::vector<TrajInfo> info;
+    std::vector<int> nstates, natom, atom0, ncgp, grp0, nmol, nqat;
+    std::vector<std::vector<int>> offd_states;
+    DevSys S{};
+    BlockTables B{};
+    std::vector<void *> allocs;
+    cudaStream_t stream = nullptr;
+    long long nlaunch = 0;
+    int NBcycle = 10;
+    int lists_built = 0, temp_init = 0, any_shake = 0, any_wpol = 0;
+    long long step = 0;
+    cudaGraphExec_t graph = nullptr;
+    long long graph_nodes = 0;
+    int graph_ene_every = 0;
+    double *rec_d = nullptr;   // record rows
+    int *recctl_d = nullptr;   // [0] absolute step of the block start, [1] first row of the window
+    int rec_cap = 0;
+    double *ecur_d = nullptr;  // one record row per trajectory for qgpu_forces
+    int *zero_d = nullptr;
+    double *grad_d = nullptr;
+    int max_natom = 0;
+    int nqt = 0;
+};
+
+// ------------------------------------------------------------- profiler
+struct KernelProfiler {
+    struct Rec { std::string name; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    cudaEvent_t get() {
+        cudaEvent_t e;
+        if (!pool.empty()) { e = pool.back(); pool.pop_back(); }
+        else cudaEventCreate(&e);
+        return e;
+    }
+};
+void prof_begin(LaunchCtx &L, const char *name) {
+    if (!L.prof) return;
+    KernelProfiler::Rec r{name, L.prof->get(), L.prof->get()};
+    cudaEventRecord(r.a, L.stream);
+    L.prof->recs.push_back(r);
+}
+void prof_end(LaunchCtx &L) {
+    if (!L.prof || L.prof->recs.empty()) return;
+    cudaEventRecord(L.prof->recs.back().b, L.stream);
+}
+
+// ---------------------------------------------------------------- create
+static int validate(const qgpu_system_desc &d, int t) {
+    if (d.natom <= 0) return fail(QGPU_E_INVALID, "traj %d: natom must be > 0", t);
+    if (d.nat_solute < 0 || d.nat_solute > d.natom) return fail(QGPU_E_INVALID, "traj %d: bad nat_solute", t);
+    if (d.solv_atom != 3) return fail(QGPU_E_UNSUPPORTED, "traj %d: only 3-site solvent is supported", t);
+    if ((d.natom - d.nat_solute) % 3) return fail(QGPU_E_INVALID, "traj %d: solvent atoms not a multiple of 3", t);
+    if (d.ivdw_rule != 1) return fail(QGPU_E_UNSUPPORTED, "traj %d: only the geometric LJ rule is supported", t);
+    if (d.nstates < 1 || d.nstates > QG_MAXS)
+        return fail(QGPU_E_UNSUPPORTED, "traj %d: nstates %d outside 1..%d", t, d.nstates, QG_MAXS);
+    if (d.nqat < 0 || d.nqat > QG_MAXQ) return fail(QGPU_E_UNSUPPORTED, "traj %d: nqat %d > %d", t, d.nqat, QG_MAXQ);
+    if (d.noffd > QG_MAXOD) return fail(QGPU_E_UNSUPPORTED, "traj %d: noffd %d > %d", t, d.noffd, QG_MAXOD);
+    if (!d.x || !d.crg || !d.iac || !d.mass || !d.cgp_first) return fail(QGPU_E_INVALID, "traj %d: missing arrays", t);
+    if (d.NBcycle <= 0) return fail(QGPU_E_INVALID, "traj %d: NBcycle must be > 0", t);
+    for (int g = d.ncgp_solute; g < d.ncgp; ++g) {
+        int f = d.cgp_first[g], l = d.cgp_last[g];
+        if (l - f != 2) return fail(QGPU_E_INVALID, "traj %d: solvent group %d has %d atoms", t, g, l - f + 1);
+        int o = d.cgpatom[f];
+        if (d.cgpatom[f + 1] != o + 1 || d.cgpatom[f + 2] != o + 2 || d.cgp_switch[g] != o || o < d.nat_solute ||
+            (o - d.nat_solute) % 3)
+            return fail(QGPU_E_INVALID, "traj %d: solvent group %d is not (O,H,H) in order", t, g);
+    }
+    for (int m = 0; m < d.shake_molecules; ++m)
+        if (d.shake_first[m + 1] - d.shake_first[m] > 64)
+            return fail(QGPU_E_UNSUPPORTED, "traj %d: more than 64 constraints in one molecule", t);
+    for (int g = 0; g < d.ncgp; ++g)
+        if (d.cgp_last[g] - d.cgp_first[g] + 1 > QG_TILE_A)
+            return fail(QGPU_E_UNSUPPORTED, "traj %d: charge group %d too large", t, g);
+    return 0;
+}
+
+static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h) {
+    h->ntraj = ntraj;
+    std::vector<double> x, v, xtop, winv, mass_atom, crg_d;
+    std::vector<float4> pos;
+    std::vector<int> atype, aq, atraj, agrp;
+    std::vector<uint8_t> aexcl, ashell, qp_skip;
+    std::vector<unsigned long long> exmask, p14mask;
+    std::vector<int> exl_first{0}, exl_j, exl_kind;
+    std::vector<float> avdw, bvdw;
+    std::vector<double> avdw_d, bvdw_d;
+    std::vector<int8_t> ljcod;
+    std::vector<int> g_start{0}, g_atoms, g_switch, g_kind, g_traj, tile_g0, tile_g1;
+    std::vector<uint8_t> g_excl;
+    std::vector<int> q_atom, qiac, qw_lj, qp14_first{0}, qp14_q;
+    std::vector<float> qcrg_f, qavdw, qbvdw, sc_f, qw_A, qw_B;
+    std::vector<double> qw_Ad, qw_Bd;
+    std::vector<double> qcrg_d, qavdw_d, qbvdw_d, sc_d;
+    std::vector<int> qq_iq, qq_j, qq_jq;
+    std::vector<int8_t> qq_lj;
+    std::vector<double> qq_els;
+    std::vector<int> qt_atoms, qt_cod, qt_kind, qt_traj;
+    std::vector<double> qt_lib;
+    std::vector<int> bt_atoms, bt_cod, bt_kind, bt_blk_traj, bt_blk_slot;
+    std::vector<double> bt_lib;
+    std::vector<int> shk_first{0}, shk_i, shk_j, shk_traj;
+    std::vector<double> shk_d2;
+    std::vector<int> od_traj, od_ij, od_kl;
+    std::vector<double> od_Amu;
+    std::vector<int> wgrp, satom, scan_t0, scan_tn, scan_traj, aall, qqblk_traj, qqblk_s;
+    int type0 = 0, lj0 = 0, q0 = 0, qlib0 = 0, sc0 = 0, grp0 = 0, atom0 = 0, tile0 = 0;
+
+    for (int t = 0; t < ntraj; ++t) {
+        const qgpu_system_desc &d = descs[t];
+        if (int rc = validate(d, t)) return rc;
+        if (t > 0 && d.NBcycle != descs[0].NBcycle)
+            return fail(QGPU_E_UNSUPPORTED, "all trajectories of a batch must share NBcycle");
+        h->NBcycle = d.NBcycle;
+        const int N = d.natom, S = d.nstates, nq = d.nqat, nt = d.natyps;
+        TrajInfo T{};
+        T.atom0 = atom0; T.natom = N; T.nat_solute = d.nat_solute; T.nwat = d.nwat;
+        T.grp0 = grp0; T.ncgp = d.ncgp; T.ncgp_solute = d.ncgp_solute;
+        T.q0 = q0; T.nqat = nq; T.nstates = S;
+        T.type0 = type0; T.natyps = nt; T.lj0 = lj0;
+        T.qlib0 = qlib0; T.nqlib = d.nqlib; T.sc0 = sc0; T.qvdw = d.qvdw_flag;
+        T.use_lrf = d.use_LRF; T.q_static = d.Rcq > d.rexcl_o;
+        T.el14 = (float)d.el14_scale;
+        T.el14d = d.el14_scale;
+        T.rc2_pp = (float)(d.Rcpp * d.Rcpp); T.rc2_pw = (float)(d.Rcpw * d.Rcpw);
+        T.rc2_ww = (float)(d.Rcww * d.Rcww); T.rc2_lrf = (float)(d.RcLRF * d.RcLRF);
+        T.drc2_pp = d.Rcpp * d.Rcpp; T.drc2_pw = d.Rcpw * d.Rcpw; T.drc2_ww = d.Rcww * d.Rcww;
+        T.drc2_lrf = d.RcLRF * d.RcLRF; T.drcq2 = d.Rcq * d.Rcq;
+        for (int k = 0; k < 3; ++k) {
+            T.origin[k] = d.xwcent[k]; T.xpcent[k] = d.xpcent[k]; T.xwcent[k] = d.xwcent[k];
+            T.chg_solv[k] = (float)d.chg_solv[k];
+        }
+        T.rwat = d.rwat; T.fk_wsphere = d.fk_wsphere; T.Dwmz = d.Dwmz; T.awmz = d.awmz;
+        T.fk_pshell = d.fk_pshell; T.fk_fix = d.fk_fix;
+        for (int s = 0; s < QG_MAXS; ++s) T.lambda[s] = s < S ? d.lambda[s] : 0.0;
+        T.dt = d.dt; T.Temp0 = d.Temp0; T.tau_T = d.tau_T;
+        T.separate_scaling = d.separate_scaling; T.detail_temps = d.detail_temps;
+        T.Ndegf = d.Ndegf; T.Ndegfree = d.Ndegfree;
+        T.Ndegfree_solute = d.Ndegfree_solute; T.Ndegfree_solvent = d.Ndegfree_solvent;
+        T.ff_type = d.ff_type;
+        if (d.wpol_restr) h->any_wpol = 1;
+        // --- types
+        for (int a = 0; a < nt; ++a)
+            for (int c = 0; c < 3; ++c) {
+                avdw.push_back((float)d.avdw[a * 3 + c]); bvdw.push_back((float)d.bvdw[a * 3 + c]);
+                avdw_d.push_back(d.avdw[a * 3 + c]); bvdw_d.push_back(d.bvdw[a * 3 + c]);
+            }
+        for (int k = 0; k < nt * nt; ++k) ljcod.push_back(d.ljcod[k]);
+        // --- water LJ constants (nonbond_ww_spc uses aLJ_solv(1,iLJ)^2)
+        if (d.nwat > 0) {
+            int tO = d.iac[d.nat_solute];
+            int c = d.ljcod[tO * nt + tO];
+            T.ww_lj = c;
+            T.ww_A = (float)(d.aLJ_solv[c - 1] * d.aLJ_solv[c - 1]);
+            T.ww_B = (float)(d.bLJ_solv[c - 1] * d.bLJ_solv[c - 1]);
+            T.ww_Ad = d.aLJ_solv[c - 1] * d.aLJ_solv[c - 1];
+            T.ww_Bd = d.bLJ_solv[c - 1] * d.bLJ_solv[c - 1];
+        } else T.ww_lj = 1;
+        // --- atoms
+        std::vector<int> grp_of(N, 0);
+        for (int g = 0; g < d.ncgp; ++g)
+            for (int k = d.cgp_first[g]; k <= d.cgp_last[g]; ++k) grp_of[d.cgpatom[k]] = g;
+        for (int i = 0; i < N; ++i) {
+            for (int c = 0; c < 3; ++c) {
+                x.push_back(d.x[3 * i + c]);
+                v.push_back(d.v ? d.v[3 * i + c] : 0.0);
+                xtop.push_back(d.xtop ? d.xtop[3 * i + c] : d.x[3 * i + c]);
+            }
+            double m = d.mass[d.iac[i]];
+            winv.push_back(1.0 / m);
+            mass_atom.push_back(m);
+            crg_d.push_back(d.crg[i]);
+            pos.push_back(make_float4(0, 0, 0, (float)d.crg[i]));
+            atype.push_back(type0 + d.iac[i]);
+            aq.push_back(d.iqatom[i] >= 0 ? q0 + d.iqatom[i] : -1);
+            atraj.push_back(t);
+            agrp.push_back(grp0 + grp_of[i]);
+            aexcl.push_back(d.excl ? d.excl[i] : 0);
+            ashell.push_back(d.shell ? d.shell[i] : 0);
+            qp_skip.push_back(d.qp_skip ? d.qp_skip[i] : 0);
+        }
+        // exclusion masks (offset -32..31) and long pairs, both directions
+        std::vector<unsigned long long> em(N, 0ull), pm(N, 0ull);
+        std::vector<std::vector<std::pair<int, int>>> lng(N);
+        auto put = [&](const int32_t *pr, int np, int kind) {
+            for (int k = 0; k < np; ++k) {
+                int a = pr[2 * k], b = pr[2 * k + 1];
+                for (int dir = 0; dir < 2; ++dir) {
+                    int i = dir ? b : a, j = dir ? a : b, rel = j - i;
+                    if (rel >= -32 && rel < 32) (kind ? pm : em)[i] |= 1ull << (rel + 32);
+                    else lng[i].push_back({j, kind});
+                }
+            }
+        };
+        put(d.excl_pairs, d.nexcl, 0);
+        put(d.pairs14, d.n14, 1);
+        for (int i = 0; i < N; ++i) {
+            exmask.push_back(em[i]); p14mask.push_back(pm[i]);
+            for (auto &p : lng[i]) { exl_j.push_back(atom0 + p.first); exl_kind.push_back(p.second); }
+            exl_first.push_back((int)exl_j.size());
+        }
+        // --- groups and scan tiles
+        T.tile0 = tile0;
+        int tg0 = grp0, tat = 0, tng = 0;
+        for (int g = 0; g < d.ncgp; ++g) {
+            int na = d.cgp_last[g] - d.cgp_first[g] + 1;
+            if (tng == QG_TILE_G || tat + na > QG_TILE_A) {
+                tile_g0.push_back(tg0); tile_g1.push_back(grp0 + g); tile0++;
+                tg0 = grp0 + g; tat = 0; tng = 0;
+            }
+            tat += na; tng++;
+            for (int k = d.cgp_first[g]; k <= d.cgp_last[g]; ++k) g_atoms.push_back(atom0 + d.cgpatom[k]);
+            g_start.push_back((int)g_atoms.size());
+            g_switch.push_back(atom0 + d.cgp_switch[g]);
+            g_kind.push_back(g >= d.ncgp_solute ? 1 : 0);
+            g_excl.push_back(d.excl ? d.excl[d.cgp_switch[g]] : 0);
+            g_traj.push_back(t);
+        }
+        if (tng) { tile_g0.push_back(tg0); tile_g1.push_back(grp0 + d.ncgp); tile0++; }
+        T.ntile = tile0 - T.tile0;
+        for (int b = 0; b < d.ncgp; b += QG_BLOCK) {
+            scan_t0.push_back(grp0 + b); scan_tn.push_back(std::min(QG_BLOCK, d.ncgp - b)); scan_traj.push_back(t);
+        }
+        // --- work lists
+        size_t s0 = wgrp.size();
+        for (int g = d.ncgp_solute; g < d.ncgp; ++g) wgrp.push_back(grp0 + g);
+        pad(wgrp, s0, t);
+        s0 = satom.size();
+        for (int i = 0; i < d.nat_solute; ++i) satom.push_back(atom0 + i);
+        pad(satom, s0, t);
+        s0 = aall.size();
+        T.ekin_blk0 = (int)(aall.size() / QG_BLOCK);
+        for (int i = 0; i < N; ++i) aall.push_back(atom0 + i);
+        pad(aall, s0, t);
+        T.ekin_nblk = (int)((aall.size() - s0) / QG_BLOCK);
+        // --- Q atoms
+        int nql = d.nqlib;
+        for (int k = 0; k < nql; ++k)
+            for (int c = 0; c < 3; ++c) {
+                qavdw.push_back((float)d.qavdw[k * 3 + c]); qbvdw.push_back((float)d.qbvdw[k * 3 + c]);
+                qavdw_d.push_back(d.qavdw[k * 3 + c]); qbvdw_d.push_back(d.qbvdw[k * 3 + c]);
+            }
+        int tO = d.nwat > 0 ? d.iac[d.nat_solute] : 0;
+        for (int iq = 0; iq < nq; ++iq) {
+            int qa = d.iqseq[iq];
+            q_atom.push_back(atom0 + qa);
+            int tq = d.iac[qa];
+            int c = d.ljcod[tO * nt + tq];
+            qw_lj.push_back(c);
+            for (int s = 0; s < QG_MAXS; ++s) {
+                double qc = s < S ? d.qcrg[iq * S + s] : 0.0;
+                qcrg_d.push_back(qc); qcrg_f.push_back((float)qc);
+                int qt = s < S ? d.qiac[iq * S + s] : 0;
+                qiac.push_back(qlib0 + qt);
+                double A, B;
+                if (!d.qvdw_flag) {
+                    A = d.avdw[tq * 3 + c - 1] * d.aLJ_solv[c - 1];
+                    B = d.bvdw[tq * 3 + c - 1] * d.bLJ_solv[c - 1];
+                } else {
+                    A = d.qavdw[qt * 3] * d.aLJ_solv[c - 1];
+                    B = d.qbvdw[qt * 3] * d.bLJ_solv[c - 1];
+                }
+                qw_A.push_back((float)A); qw_B.push_back((float)B);
+                qw_Ad.push_back(A); qw_Bd.push_back(B);
+            }
+        }
+        int ntq = nt + nq;
+        for (int iq = 0; iq < nq; ++iq)
+            for (int col = 0; col < ntq; ++col)
+                for (int s = 0; s < QG_MAXS; ++s) {
+                    double sc = (s < S && d.sc_lookup) ? d.sc_lookup[((size_t)iq * ntq + col) * S + s] : 0.0;
+                    sc_d.push_back(sc); sc_f.push_back((float)sc);
+                }
+        {
+            std::vector<std::vector<int>> q14(N);
+            for (int k = 0; k < d.nqp14; ++k) q14[d.qp14_pairs[2 * k + 1]].push_back(q0 + d.qp14_pairs[2 * k]);
+            for (int i = 0; i < N; ++i) {
+                for (int q : q14[i]) qp14_q.push_back(q);
+                qp14_first.push_back((int)qp14_q.size());
+            }
+        }
+        // --- nbqq
+        int off = 0;
+        for (int s = 0; s < QG_MAXS; ++s) {
+            T.qq0[s] = (int)qq_iq.size();
+            int n = s < S ? d.nbqq_count[s] : 0;
+            T.nqq[s] = n;
+            for (int k = 0; k < n; ++k) {
+                int p = off + k;
+                qq_iq.push_back(q0 + d.nbqq_iq[p]);
+                qq_j.push_back(atom0 + d.nbqq_j[p]);
+                qq_jq.push_back(d.nbqq_jq[p] >= 0 ? q0 + d.nbqq_jq[p] : -1);
+                qq_lj.push_back(d.nbqq_ljcod[p]);
+                qq_els.push_back(d.nbqq_elscale[p]);
+            }
+            off += n;
+            if (n) { qqblk_traj.push_back(t); qqblk_s.push_back(s); }
+        }
+        // --- Q bonded terms
+        {
+            int lib_b = (int)(qt_lib.size() / 4);
+            for (int k = 0; k < d.nqbcod; ++k) for (int c = 0; c < 4; ++c) qt_lib.push_back(d.qbondlib[4 * k + c]);
+            int lib_a = (int)(qt_lib.size() / 4);
+            for (int k = 0; k < d.nqacod; ++k) for (int c = 0; c < 4; ++c) qt_lib.push_back(d.qanglib[4 * k + c]);
+            int lib_t = (int)(qt_lib.size() / 4);
+            for (int k = 0; k < d.nqtcod; ++k) { for (int c = 0; c < 3; ++c) qt_lib.push_back(d.qtorlib[3 * k + c]); qt_lib.push_back(0); }
+            int lib_i = (int)(qt_lib.size() / 4);
+            for (int k = 0; k < d.nqicod; ++k) { for (int c = 0; c < 2; ++c) qt_lib.push_back(d.qimplib[2 * k + c]); qt_lib.push_back(0); qt_lib.push_back(0); }
+            auto addq = [&](const int32_t *rows, int nrow, int nat, int kind, int libo) {
+                int w = nat + S;
+                for (int r = 0; r < nrow; ++r) {
+                    for (int a = 0; a < 4; ++a) qt_atoms.push_back(a < nat ? atom0 + rows[r * w + a] : atom0);
+                    for (int s = 0; s < QG_MAXS; ++s) {
+                        int c = s < S ? rows[r * w + nat + s] : 0;
+                        qt_cod.push_back(c > 0 ? libo + c : 0);
+                    }
+                    qt_kind.push_back(kind); qt_traj.push_back(t);
+                }
+            };
+            addq(d.qbnd, d.nqbond, 2, 0, lib_b);
+            addq(d.qang, d.nqangle, 3, 1, lib_a);
+            addq(d.qtor, d.nqtor, 4, 2, lib_t);
+            addq(d.qimp, d.nqimp, 4, 3, lib_i);
+        }
+        // --- classical bonded terms, one padded segment per energy slot
+        {
+            int lb = (int)(bt_lib.size() / 4);
+            for (int k = 0; k < d.nbndcod; ++k) { bt_lib.push_back(d.bondlib[2 * k]); bt_lib.push_back(d.bondlib[2 * k + 1]); bt_lib.push_back(0); bt_lib.push_back(0); }
+            int la = (int)(bt_lib.size() / 4);
+            for (int k = 0; k < d.nangcod; ++k) for (int c = 0; c < 4; ++c) bt_lib.push_back(d.anglib[4 * k + c]);
+            int lt = (int)(bt_lib.size() / 4);
+            for (int k = 0; k < d.ntorcod; ++k) for (int c = 0; c < 4; ++c) bt_lib.push_back((double)d.torlib[4 * k + c]);
+            int li = (int)(bt_lib.size() / 4);
+            for (int k = 0; k < d.nimpcod; ++k) { bt_lib.push_back((double)d.implib[2 * k]); bt_lib.push_back((double)d.implib[2 * k + 1]); bt_lib.push_back(0); bt_lib.push_back(0); }
+            auto seg = [&](const int32_t *rows, int r0, int r1, int nat, int w, int kind, int libo, int slot) {
+                if (r1 <= r0) return;
+                size_t st = bt_cod.size();
+                for (int r = r0; r < r1; ++r) {
+                    for (int a = 0; a < 4; ++a) bt_atoms.push_back(a < nat ? atom0 + rows[r * w + a] : atom0);
+                    bt_cod.push_back(libo + rows[r * w + nat] - 1);
+                    bt_kind.push_back(kind);
+                }
+                while ((bt_cod.size() - st) % QG_BLOCK) {
+                    for (int a = 0; a < 4; ++a) bt_atoms.push_back(0);
+                    bt_cod.push_back(-1); bt_kind.push_back(0);
+                }
+                for (size_t b = st / QG_BLOCK; b < bt_cod.size() / QG_BLOCK; ++b) { bt_blk_traj.push_back(t); bt_blk_slot.push_back(slot); }
+            };
+            seg(d.bnd, 0, d.nbonds_solute, 2, 3, 0, lb, EA_P_BOND);
+            seg(d.bnd, d.nbonds_solute, d.nbonds, 2, 3, 0, lb, EA_W_BOND);
+            seg(d.ang, 0, d.nangles_solute, 3, 4, 1, la, EA_P_ANG);
+            seg(d.ang, d.nangles_solute, d.nangles, 3, 4, 1, la, EA_W_ANG);
+            seg(d.tor, 0, d.ntors_solute, 4, 5, 2, lt, EA_P_TOR);
+            seg(d.tor, d.ntors_solute, d.ntors, 4, 5, 2, lt, EA_W_TOR);
+            int ik = d.ff_type == 2 ? 4 : 3;
+            seg(d.imp, 0, d.nimps_solute, 4, 5, ik, li, EA_P_IMP);
+            seg(d.imp, d.nimps_solute, d.nimps, 4, 5, ik, li, EA_W_IMP);
+        }
+        // --- SHAKE
+        T.shake_mol0 = (int)(shk_first.size() - 1);
+        T.nshake_mol = d.shake_molecules;
+        for (int m = 0; m < d.shake_molecules; ++m) {
+            for (int c = d.shake_first[m]; c < d.shake_first[m + 1]; ++c) {
+                shk_i.push_back(atom0 + d.shake_i[c]); shk_j.push_back(atom0 + d.shake_j[c]); shk_d2.push_back(d.shake_dist2[c]);
+            }
+            shk_first.push_back((int)shk_i.size());
+            shk_traj.push_back(t);
+        }
+        if (d.shake_molecules) h->any_shake = 1;
+        // --- off-diagonals
+        std::vector<int> ost;
+        for (int k = 0; k < d.noffd; ++k) {
+            od_traj.push_back(t); od_ij.push_back(k); od_ij.push_back(0);
+            od_kl.push_back(q0 + d.offd_kl[2 * k]); od_kl.push_back(q0 + d.offd_kl[2 * k + 1]);
+            od_Amu.push_back(d.offd_Amu[2 * k]); od_Amu.push_back(d.offd_Amu[2 * k + 1]);
+            ost.push_back(d.offd_ij[2 * k]); ost.push_back(d.offd_ij[2 * k + 1]);
+        }
+        h->offd_states.push_back(ost);
+        h->info.push_back(T);
+        h->nstates.push_back(S); h->natom.push_back(N); h->atom0.push_back(atom0);
+        h->ncgp.push_back(d.ncgp); h->grp0.push_back(grp0); h->nqat.push_back(nq);
+        h->nmol.push_back(0);
+        h->max_natom = std::max(h->max_natom, N);
+        atom0 += N; grp0 += d.ncgp; q0 += nq; type0 += nt; lj0 += nt * nt; qlib0 += nql; sc0 += nq * ntq * QG_MAXS;
+    }
+    // ---------------------------------------------------------- upload
+    std::vector<void *> &A = h->allocs;
+    DevSys &S = h->S;
+    S.ntraj = ntraj; S.natom = atom0; S.ngrp = grp0; S.nq = q0;
+    int gsz = 0;
+    for (int t = 0; t < ntraj; ++t) gsz = std::max(gsz, h->ncgp[t]);
+    S.nb_cap = 448;
+    if (const char *e = getenv("QGPU_NB_CAP")) {   // list capacity per charge group (tests force overflow)
+        int c = atoi(e);
+        if (c > 0) S.nb_cap = c;
+    }
+    TrajInfo *ti; TrajState *ts;
+    int rc;
+    if ((rc = upload(A, h->info, &ti))) return rc;
+    S.traj = ti;
+    std::vector<TrajState> tsh(ntraj);
+    for (auto &q : tsh) { q.Tscale_solute = q.Tscale_solvent = 1.0; q.Temp = q.Tfree = q.Ekin = 0; q.shake_iters = 0; }
+    if ((rc = upload(A, tsh, &ts))) return rc;
+    S.tstate = ts;
+#define UP(vec, field)                                            \
+    do {                                                          \
+        decltype(vec.data()) p_;                                  \
+        if ((rc = upload(A, vec, &p_))) return rc;                \
+        S.field = p_;                                             \
+    } while (0)
+    UP(x, x); UP(v, v); UP(xtop, xtop); UP(winv, winv); UP(mass_atom, mass); UP(crg_d, crg_d);
+    if ((rc = alloc0(A, (size_t)3 * atom0, &S.xx))) return rc;
+    UP(pos, pos);
+    if ((rc = alloc0(A, (size_t)atom0, &S.poslo))) return rc;
+    UP(atype, atype); UP(aq, aq); UP(aexcl, aexcl); UP(ashell, ashell); UP(atraj, atraj); UP(agrp, agrp);
+    if ((rc = alloc0(A, (size_t)3 * atom0, &S.fx))) return rc;
+    UP(exmask, exmask); UP(p14mask, p14mask); UP(exl_first, exlong_first); UP(exl_j, exlong_j); UP(exl_kind, exlong_kind);
+    UP(avdw, avdw); UP(bvdw, bvdw); UP(avdw_d, avdw_d); UP(bvdw_d, bvdw_d); UP(ljcod, ljcod);
+    UP(g_start, g_start); UP(g_atoms, g_atoms); UP(g_switch, g_switch); UP(g_kind, g_kind); UP(g_traj, g_traj);
+    UP(g_excl, g_excl); UP(tile_g0, tile_g0); UP(tile_g1, tile_g1);
+    if ((rc = alloc0(A, (size_t)3 * grp0, &S.g_cent))) return rc;
+    if ((rc = alloc0(A, (size_t)QG_NLRF * grp0, &S.g_phi))) return rc;
+    if ((rc = alloc0(A, (size_t)QG_NPHI * grp0, &S.g_phif))) return rc;
+    if ((rc = alloc0(A, (size_t)grp0, &S.nb_count))) return rc;
+    if ((rc = alloc0(A, (size_t)grp0 * S.nb_cap, &S.nb_list))) return rc;
+    UP(q_atom, q_atom); UP(qcrg_f, qcrg_f); UP(qcrg_d, qcrg_d); UP(qiac, qiac);
+    UP(qavdw, qavdw); UP(qbvdw, qbvdw); UP(qavdw_d, qavdw_d); UP(qbvdw_d, qbvdw_d); UP(sc_f, sc_f); UP(sc_d, sc_d);
+    {
+        float *p;
+        if ((rc = upload(A, qw_A, &p))) return rc; S.qw_A = p;
+        if ((rc = upload(A, qw_B, &p))) return rc; S.qw_B = p;
+    }
+    UP(qw_lj, qw_lj); UP(qw_Ad, qw_Ad); UP(qw_Bd, qw_Bd);
+    if ((rc = alloc0(A, (size_t)atom0, &S.qw_member))) return rc;
+    if ((rc = alloc0(A, (size_t)atom0, &S.qp_member))) return rc;
+    UP(qp_skip, qp_skip); UP(qp14_first, qp14_first); UP(qp14_q, qp14_q);
+    UP(qq_iq, qq_iq); UP(qq_j, qq_j); UP(qq_jq, qq_jq); UP(qq_lj, qq_lj); UP(qq_els, qq_els);
+    UP(qt_atoms, qt_atoms); UP(qt_cod, qt_cod); UP(qt_kind, qt_kind); UP(qt_traj, qt_traj); UP(qt_lib, qt_lib);
+    S.nqt = (int)qt_kind.size();
+    UP(bt_atoms, bt_atoms); UP(bt_cod, bt_cod); UP(bt_kind, bt_kind); UP(bt_lib, bt_lib);
+    UP(bt_blk_traj, bt_blk_traj); UP(bt_blk_slot, bt_blk_slot);
+    S.nbt = (int)bt_cod.size();
+    UP(od_traj, od_traj); UP(od_ij, od_ij); UP(od_kl, od_kl); UP(od_Amu, od_Amu);
+    S.nod = (int)od_traj.size();
+    if ((rc = alloc0(A, (size_t)ntraj * QG_MAXOD * 2, &S.od_out))) return rc;
+    UP(shk_first, shk_first); UP(shk_i, shk_i); UP(shk_j, shk_j); UP(shk_traj, shk_traj); UP(shk_d2, shk_d2);
+    S.nshk_mol = (int)shk_traj.size();
+    if ((rc = alloc0(A, (size_t)ntraj * QG_NE, &S.eacc))) return rc;
+    if ((rc = alloc0(A, (size_t)4 * (aall.size() / QG_BLOCK + 1), &S.ekin_part))) return rc;
+    if ((rc = alloc0(A, 1, &S.status))) return rc;
+    // block tables
+    BlockTables &B = h->B;
+    {
+        int *p;
+        if ((rc = upload(A, wgrp, &p))) return rc; B.wgrp = p; B.nwgrp = (int)wgrp.size();
+        if ((rc = upload(A, satom, &p))) return rc; B.satom = p; B.nsatom = (int)satom.size();
+        if ((rc = upload(A, scan_t0, &p))) return rc; B.scan_t0 = p;
+        if ((rc = upload(A, scan_tn, &p))) return rc; B.scan_tn = p;
+        if ((rc = upload(A, scan_traj, &p))) return rc; B.scan_traj = p; B.nscan = (int)scan_t0.size();
+        if ((rc = upload(A, aall, &p))) return rc; B.aall = p; B.naall = (int)aall.size();
+        if ((rc = upload(A, qqblk_traj, &p))) return rc; B.qqblk_traj = p;
+        if ((rc = upload(A, qqblk_s, &p))) return rc; B.qqblk_s = p; B.nqqblk = (int)qqblk_traj.size();
+    }
+    if ((rc = alloc0(A, (size_t)ntraj * QG_REC, &h->ecur_d))) return rc;
+    if ((rc = alloc0(A, 2, &h->zero_d))) return rc;
+    if ((rc = alloc0(A, (size_t)3 * h->max_natom, &h->grad_d))) return rc;
+    if ((rc = alloc0(A, 2, &h->recctl_d))) return rc;
+    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    // float mirror of the starting coordinates
+    LaunchCtx L{h->stream, &h->nlaunch};
+    launch_mirror(S, B, L);
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaGetLastError());
+    return 0;
+}
+
+static int check_status(qgpu_handle *h) {
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, h->S.status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaGetLastError());
+    if (!st) return 0;
+    int zero = 0;
+    CK(cudaMemcpy(h->S.status, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    if (st & ST_LIST_OVERFLOW) return fail(QGPU_E_LIST_OVERFLOW, "neighbour list capacity %d exceeded", h->S.nb_cap);
+    if (st & ST_SHAKE) return fail(QGPU_E_SHAKE, "shake failure: no convergence in 1000 iterations");
+    if (st & ST_NAN) return fail(QGPU_E_NAN, "a detected NaN in the temperature");
+    if (st & ST_FIXED) return fail(QGPU_E_FIXED_RANGE, "force or energy outside the fixed-point range");
+    return fail(QGPU_E_CUDA, "device status %d", st);
+}
+
+static void list_ops(qgpu_handle *h, LaunchCtx &L) {
+    launch_centers(h->S, h->B, L);
+    launch_scan(h->S, h->B, L);
+    launch_qmember(h->S, h->B, L, h->lists_built ? 0 : 1);
+}
+
+// fp64_energy: every pair energy in FP64 (drop-in call); otherwise FP32 pair
+// energies, with FP64 Q-atom energies on recorded steps (esel).
+static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, bool fp64_energy, EaccSel esel) {
+    if (terms & QGPU_TERMS_NONBOND) {
+        launch_nb_water(h->S, h->B, L, 1, fp64_energy);
+        launch_nb_solute(h->S, h->B, L, 1, fp64_energy);
+        launch_qw(h->S, h->B, L, esel);
+        launch_qp(h->S, h->B, L, esel);
+    }
+    if (terms & QGPU_TERMS_QQ) launch_qq(h->S, h->B, L);
+    if (terms & QGPU_TERMS_QBONDED) launch_qbonded(h->S, h->B, L, h->S.nqt);
+    if (terms & QGPU_TERMS_BONDED) launch_bonded(h->S, h->B, L);
+    if (terms & QGPU_TERMS_RESTRAINT) {
+        launch_fix_shell(h->S, h->B, L);
+        launch_restrain_solvent(h->S, h->B, L);
+    }
+    launch_offdiag(h->S, L);
+}
+
+static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every);
+
+// One NBcycle block (list build + NBcycle steps + record-counter tick),
+// captured once as a CUDA graph and replayed.
+static int replay_block(qgpu_handle *h, LaunchCtx &L, int ene_every) {
+    const int NB = h->NBcycle;
+    if (h->graph && h->graph_ene_every != ene_every) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    if (!h->graph) {
+        cudaGraph_t g;
+        long long before = h->nlaunch;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        list_ops(h, L);
+        for (int k = 0; k < NB; ++k) step_ops(h, L, k, ene_every);
+        launch_tick(L, h->recctl_d, NB);
+        CK(cudaStreamEndCapture(h->stream, &g));
+        CK(cudaGraphInstantiate(&h->graph, g, 0));
+        cudaGraphDestroy(g);
+        h->graph_nodes = h->nlaunch - before;
+        h->graph_ene_every = ene_every;
+        h->nlaunch = before;
+    }
+    CK(cudaGraphLaunch(h->graph, h->stream));
+    h->nlaunch += h->graph_nodes;
+    h->step += NB;
+    return 0;
+}
+
+static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every) {
+    EaccSel esel{EACC_RECORD, h->recctl_d, k, ene_every};
+    force_ops(h, L, QGPU_TERMS_ALL, false, esel);
+    launch_integrate(h->S, h->B, L);
+    launch_shake(h->S, h->B, L, -1);
+    launch_post(h->S, h->B, L, h->any_shake);
+    launch_finalize(h->S, L, 1, h->rec_d, h->recctl_d, k, ene_every, h->rec_cap);
+}
+
+// ------------------------------------------------------------------ C-ABI
+extern "C" {
+
+int qgpu_last_error(char *buf, int32_t len) {
+    if (!buf || len <= 0) return QGPU_E_INVALID;
+    snprintf(buf, (size_t)len, "%s", g_err.c_str());
+    return 0;
+}
+
+int qgpu_create(const qgpu_system_desc *descs, int32_t ntraj, qgpu_handle **out) {
+    if (!descs || ntraj <= 0 || !out) return fail(QGPU_E_INVALID, "qgpu_create: bad arguments");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(QGPU_E_CUDA, "no CUDA device");
+    qgpu_handle *h = new qgpu_handle();
+    int rc = create_impl(descs, ntraj, h);
+    if (rc) { qgpu_destroy(h); *out = nullptr; return rc; }
+    *out = h;
+    return 0;
+}
+
+int qgpu_destroy(qgpu_handle *h) {
+    if (!h) return 0;
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (void *p : h->allocs) cudaFree(p);
+    if (h->rec_d) cudaFree(h->rec_d);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return 0;
+}
+
+int qgpu_ntraj(const qgpu_handle *h) { return h ? h->ntraj : 0; }
+
+int64_t qgpu_kernel_launches(const qgpu_handle *h) { return h ? h->nlaunch : 0; }
+
+int qgpu_set_coords(qgpu_handle *h, int32_t traj, const double *x, const double *v) {
+    if (!h || traj < 0 || traj >= h->ntraj) return fail(QGPU_E_INVALID, "bad trajectory index");
+    size_t off = 3 * (size_t)h->atom0[traj], n = 3 * (size_t)h->natom[traj];
+    if (x) CK(cudaMemcpyAsync(h->S.x + off, x, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (v) CK(cudaMemcpyAsync(h->S.v + off, v, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    LaunchCtx L{h->stream, &h->nlaunch};
+    launch_mirror(h->S, h->B, L);
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int qgpu_get_coords(qgpu_handle *h, int32_t traj, double *x, double *v) {
+    if (!h || traj < 0 || traj >= h->ntraj) return fail(QGPU_E_INVALID, "bad trajectory index");
+    size_t off = 3 * (size_t)h->atom0[traj], n = 3 * (size_t)h->natom[traj];
+    if (x) CK(cudaMemcpyAsync(x, h->S.x + off, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (v) CK(cudaMemcpyAsync(v, h->S.v + off, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int qgpu_build_lists(qgpu_handle *h) {
+    if (!h) return fail(QGPU_E_INVALID, "null handle");
+    LaunchCtx L{h->stream, &h->nlaunch};
+    list_ops(h, L);
+    h->lists_built = 1;
+    return check_status(h);
+}
+
+static void unpack_row(const double *R, int S, qgpu_energies *E, qgpu_qenergy *EQ) {
+    if (E) memcpy(E, R + QG_REC_E, sizeof(qgpu_energies));
+    if (EQ)
+        for (int s = 0; s < S; ++s) memcpy(&EQ[s], R + QG_REC_EQ + 15 * s, sizeof(qgpu_qenergy));
+}
+
+int qgpu_forces(qgpu_handle *h, int32_t traj, int32_t terms, double *d, qgpu_energies *E, qgpu_qenergy *EQ) {
+    if (!h || traj < 0 || traj >= h->ntraj) return fail(QGPU_E_INVALID, "bad trajectory index");
+    if (!h->lists_built) return fail(QGPU_E_INVALID, "qgpu_forces before qgpu_build_lists");
+    LaunchCtx L{h->stream, &h->nlaunch};
+    CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
+    force_ops(h, L, terms, true, EaccSel{EACC_FP64, h->zero_d, 0, 1});
+    launch_finalize(h->S, L, 0, h->ecur_d, h->zero_d, 0, 1, 1);
+    std::vector<double> row(QG_REC);
+    CK(cudaMemcpyAsync(row.data(), h->ecur_d + (size_t)traj * QG_REC, QG_REC * sizeof(double), cudaMemcpyDeviceToHost,
+                       h->stream));
+    if (d) {
+        launch_grad_to_double(h->S, L, h->grad_d, h->atom0[traj], h->natom[traj]);
+        CK(cudaMemcpyAsync(d, h->grad_d, 3 * (size_t)h->natom[traj] * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    if (int rc = check_status(h)) return rc;
+    unpack_row(row.data(), h->nstates[traj], E, EQ);
+    return 0;
+}
+
+int qgpu_shake(qgpu_handle *h, int32_t traj, const double *xx, double *x, int32_t *niter) {
+    if (!h || traj < 0 || traj >= h->ntraj || !xx || !x) return fail(QGPU_E_INVALID, "bad arguments");
+    size_t off = 3 * (size_t)h->atom0[traj], n = 3 * (size_t)h->natom[traj];
+    CK(cudaMemcpyAsync(h->S.xx + off, xx, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->S.x + off, x, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(&h->S.tstate[traj].shake_iters, 0, sizeof(int), h->stream));
+    LaunchCtx L{h->stream, &h->nlaunch};
+    launch_shake(h->S, h->B, L, traj);
+    launch_mirror(h->S, h->B, L);
+    CK(cudaMemcpyAsync(x, h->S.x + off, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    int it = 0;
+    CK(cudaMemcpyAsync(&it, &h->S.tstate[traj].shake_iters, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    if (int rc = check_status(h)) return rc;
+    if (niter) *niter = h->info[traj].nshake_mol ? it / h->info[traj].nshake_mol : 0;
+    return 0;
+}
+
+int qgpu_get_temperature(qgpu_handle *h, int32_t traj, double *out4) {
+    if (!h || traj < 0 || traj >= h->ntraj || !out4) return fail(QGPU_E_INVALID, "bad arguments");
+    TrajState ts;
+    CK(cudaMemcpyAsync(&ts, h->S.tstate + traj, sizeof ts, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    out4[0] = ts.Temp; out4[1] = ts.Tfree; out4[2] = ts.Tscale_solute; out4[3] = ts.Tscale_solvent;
+    return 0;
+}
+
+int qgpu_get_group_pairs(qgpu_handle *h, int32_t traj, int32_t *pairs, int64_t cap, int64_t *npairs) {
+    if (!h || traj < 0 || traj >= h->ntraj) return fail(QGPU_E_INVALID, "bad trajectory index");
+    int G = h->ncgp[traj], g0 = h->grp0[traj], C = h->S.nb_cap;
+    std::vector<int> cnt(G), lst((size_t)G * C);
+    CK(cudaMemcpy(cnt.data(), h->S.nb_count + g0, G * sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(lst.data(), h->S.nb_list + (size_t)g0 * C, (size_t)G * C * sizeof(int), cudaMemcpyDeviceToHost));
+    int64_t n = 0;
+    for (int g = 0; g < G; ++g)
+        for (int k = 0; k < cnt[g]; ++k) {
+            int o = lst[(size_t)g * C + k] - g0;
+            if (o > g) {
+                if (pairs && n < cap) { pairs[2 * n] = g; pairs[2 * n + 1] = o; }
+                n++;
+            }
+        }
+    if (npairs) *npairs = n;
+    return 0;
+}
+
+int qgpu_get_lrf(qgpu_handle *h, int32_t traj, double *lrf43) {
+    if (!h || traj < 0 || traj >= h->ntraj || !lrf43) return fail(QGPU_E_INVALID, "bad arguments");
+    int G = h->ncgp[traj], g0 = h->grp0[traj];
+    std::vector<double> c(3 * (size_t)G), a((size_t)QG_NLRF * G);
+    CK(cudaMemcpy(c.data(), h->S.g_cent + 3 * (size_t)g0, c.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(a.data(), h->S.g_phi + (size_t)QG_NLRF * g0, a.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    // symmetric sums -> the 3 + 1 + 3 + 9 + 27 layout of LRF_TYPE (src/md.f90:444-450)
+    static const int p2[3][3] = {{8, 11, 12}, {11, 9, 13}, {12, 13, 10}};
+    for (int g = 0; g < G; ++g) {
+        const double *A = a.data() + (size_t)QG_NLRF * g;
+        double *o = lrf43 + 43 * (size_t)g;
+        for (int k = 0; k < 3; ++k) o[k] = c[3 * g + k];
+        o[3] = A[0];
+        for (int k = 0; k < 3; ++k) o[4 + k] = -A[2 + k];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) o[7 + 3 * i + j] = A[p2[i][j]] - (i == j ? A[1] : 0.0);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) {
+                    int s[3] = {i, j, k};
+                    std::sort(s, s + 3);
+                    int idx;
+                    if (s[0] == s[2]) idx = 14 + s[0];                       // xxx yyy zzz
+                    else if (s[0] == 0 && s[1] == 0) idx = s[2] == 1 ? 17 : 18; // xxy xxz
+                    else if (s[0] == 0 && s[1] == 1 && s[2] == 1) idx = 19;    // xyy
+                    else if (s[0] == 0 && s[1] == 2) idx = 20;                 // xzz
+                    else if (s[0] == 1 && s[1] == 1) idx = 21;                 // yyz
+                    else if (s[0] == 1 && s[1] == 2) idx = 22;                 // yzz
+                    else idx = 23;                                             // xyz
+                    double val = 5.0 * A[idx];
+                    if (i == j) val += A[5 + k];
+                    if (i == k) val += A[5 + j];
+                    if (j == k) val += A[5 + i];
+                    o[16 + 9 * i + 3 * j + k] = val;
+                }
+    }
+    return 0;
+}
+
+void *qgpu_stream(qgpu_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+// Runs nsteps MD steps launch by launch (no graph) with CUDA events around
+// every kernel and returns, per kernel name, total milliseconds and launches.
+int qgpu_profile(qgpu_handle *h, int32_t nsteps, char *names, double *ms, int64_t *counts, int32_t cap,
+                 int32_t *nkernels) {
+    if (!h || nsteps <= 0) return fail(QGPU_E_INVALID, "bad arguments");
+    if (h->any_wpol) return fail(QGPU_E_UNSUPPORTED, "water polarisation restraints are not run on the device");
+    KernelProfiler P;
+    LaunchCtx L{h->stream, &h->nlaunch, &P};
+    if (!h->rec_d) {
+        CK(cudaMalloc(&h->rec_d, (size_t)256 * h->ntraj * QG_REC * sizeof(double)));
+        h->rec_cap = 256;
+    }
+    const int ene_every = 1 << 30;
+    int ctl[2] = {(int)h->step, (int)((h->step + ene_every - 1) / ene_every)};
+    CK(cudaMemcpyAsync(h->recctl_d, ctl, sizeof ctl, cudaMemcpyHostToDevice, h->stream));
+    for (int k = 0; k < nsteps; ++k) {
+        if (h->step % h->NBcycle == 0) { list_ops(h, L); h->lists_built = 1; }
+        step_ops(h, L, 0, ene_every);
+        launch_tick(L, h->recctl_d, 1);
+        h->step += 1;
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    std::map<std::string, std::pair<double, long long>> acc;
+    for (auto &r : P.recs) {
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, r.a, r.b));
+        auto &a = acc[r.name];
+        a.first += t; a.second += 1;
+        cudaEventDestroy(r.a); cudaEventDestroy(r.b);
+    }
+    int n = 0;
+    for (auto &kv : acc) {
+        if (n < cap) {
+            if (names) snprintf(names + 64 * n, 64, "%s", kv.first.c_str());
+            if (ms) ms[n] = kv.second.first;
+            if (counts) counts[n] = kv.second.second;
+        }
+        n++;
+    }
+    if (nkernels) *nkernels = n;
+    return check_status(h);
+}
+
+// Enqueues nsteps of device work (graph replays where a whole NBcycle block
+// fits) without waiting; energies of every ene_every-th step go to the device
+// record buffer.  Errors surface at the next qgpu_sync / qgpu_run.
+int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every) {
+    if (!h || nsteps < 0) return fail(QGPU_E_INVALID, "bad arguments");
+    if (h->any_wpol)
+        return fail(QGPU_E_UNSUPPORTED, "water polarisation restraints are not run on the device (set polarisation off)");
+    if (ene_every <= 0) ene_every = 1 << 30;
+    if (h->graph && h->graph_ene_every != ene_every) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    LaunchCtx L{h->stream, &h->nlaunch};
+    if (!h->rec_d) {
+        CK(cudaMalloc(&h->rec_d, (size_t)256 * h->ntraj * QG_REC * sizeof(double)));
+        h->rec_cap = 256;
+    }
+    if (!h->temp_init) {
+        CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
+        CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
+        launch_post(h->S, h->B, L, 0);
+        launch_finalize(h->S, L, 1, nullptr, h->zero_d, 0, 1, 0);
+        h->temp_init = 1;
+    }
+    int ctl[2] = {(int)h->step, (int)((h->step + ene_every - 1) / ene_every)};
+    CK(cudaMemcpyAsync(h->recctl_d, ctl, sizeof ctl, cudaMemcpyHostToDevice, h->stream));
+    const int NB = h->NBcycle;
+    const long long end = h->step + nsteps;
+    while (h->step < end) {
+        if (h->step % NB == 0 && end - h->step >= NB && h->lists_built) {
+            if (int rc = replay_block(h, L, ene_every)) return rc;
+        } else {
+            if (h->step % NB == 0) { list_ops(h, L); h->lists_built = 1; }
+            step_ops(h, L, 0, ene_every);
+            launch_tick(L, h->recctl_d, 1);
+            h->step += 1;
+        }
+    }
+    return 0;
+}
+
+int qgpu_sync(qgpu_handle *h) {
+    if (!h) return fail(QGPU_E_INVALID, "null handle");
+    return check_status(h);
+}
+
+int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink sink, void *user) {
+    if (!h || nsteps < 0) return fail(QGPU_E_INVALID, "bad arguments");
+    if (h->any_wpol)
+        return fail(QGPU_E_UNSUPPORTED, "water polarisation restraints are not run on the device (set polarisation off)");
+    if (ene_every <= 0) ene_every = 1 << 30;
+    LaunchCtx L{h->stream, &h->nlaunch};
+    const int NB = h->NBcycle;
+    // record buffer: rows of ntraj records
+    int want_cap = 256;
+    if (!h->rec_d || h->rec_cap < want_cap) {
+        if (h->rec_d) cudaFree(h->rec_d);
+        CK(cudaMalloc(&h->rec_d, (size_t)want_cap * h->ntraj * QG_REC * sizeof(double)));
+        h->rec_cap = want_cap;
+        if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    }
+    int ctl[2] = {(int)h->step, (int)((h->step + ene_every - 1) / ene_every)};
+    CK(cudaMemcpyAsync(h->recctl_d, ctl, sizeof ctl, cudaMemcpyHostToDevice, h->stream));
+    int row0 = ctl[1];
+    CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
+    CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
+    if (!h->temp_init) {
+        // temperature() before the first step (md_run, src/md.f90:6395-6398)
+        launch_post(h->S, h->B, L, 0);
+        launch_finalize(h->S, L, 1, nullptr, h->zero_d, 0, 1, 0);
+        h->temp_init = 1;
+    }
+    auto flush = [&](long long upto_step) -> int {
+        long long rows = (upto_step + ene_every - 1) / ene_every - row0;
+        if (rows > h->rec_cap) rows = h->rec_cap;
+        if (rows > 0 && sink) {
+            std::vector<double> buf((size_t)rows * h->ntraj * QG_REC);
+            CK(cudaMemcpyAsync(buf.data(), h->rec_d, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            for (long long r = 0; r < rows; ++r)
+                for (int t = 0; t < h->ntraj; ++t) {
+                    const double *R = buf.data() + ((size_t)r * h->ntraj + t) * QG_REC;
+                    qgpu_energies E;
+                    qgpu_qenergy EQ[QG_MAXS];
+                    unpack_row(R, h->nstates[t], &E, EQ);
+                    sink(user, t, (int32_t)((row0 + r) * (long long)ene_every), EQ, h->nstates[t], &E);
+                }
+        }
+        return 0;
+    };
+    const long long end = h->step + nsteps;
+    while (h->step < end) {
+        const long long rows_needed = (h->step + NB + ene_every - 1) / ene_every - row0;
+        if (rows_needed > h->rec_cap) {
+            if (int rc = check_status(h)) return rc;
+            flush(h->step);
+            row0 = (int)((h->step + ene_every - 1) / ene_every);
+            int c2[2] = {(int)h->step, row0};
+            CK(cudaMemcpyAsync(h->recctl_d, c2, sizeof c2, cudaMemcpyHostToDevice, h->stream));
+        }
+        if (h->step % NB == 0 && end - h->step >= NB && h->lists_built) {
+            if (int rc = replay_block(h, L, ene_every)) return rc;
+        } else {
+            if (h->step % NB == 0) { list_ops(h, L); h->lists_built = 1; }
+            step_ops(h, L, 0, ene_every);
+            launch_tick(L, h->recctl_d, 1);
+            h->step += 1;
+        }
+    }
+    if (int rc = check_status(h)) return rc;
+    flush(h->step);
+    return check_status(h);
+}
+
+}  // extern "C"

@@ -1,0 +1,254 @@
+// qgpu_internal.cuh -- device-side data layout and helpers of the GB300 engine.
+//
+// Layout in HBM: every trajectory of a batch is concatenated.  Atoms, charge
+// groups and Q atoms carry global indices; TrajInfo holds each trajectory's
+// offsets and parameters.  Per-item work lists (water groups, solute atoms, ...)
+// are padded per trajectory to a multiple of QG_BLOCK with -1 so that a thread
+// block never spans two trajectories.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "qgpu.h"
+
+#define QG_BLOCK 128            // threads per block of the per-item kernels
+#define QG_MAXS 4               // states handled by the engine (<= QGPU_MAX_STATES)
+#define QG_MAXQ 128             // Q atoms per trajectory (reference max_qat = 100)
+#define QG_TILE_G 64            // source groups per scan tile
+#define QG_TILE_A 256           // source atoms per scan tile
+#define QG_MAXOD 6              // off-diagonal couplings recorded per trajectory
+#define QG_NLRF 24              // LRF accumulators per group (see k_scan)
+#define QG_NPHI 20              // symmetric LRF Taylor coefficients per group
+#define QG_FSCALE 4294967296.0  // fixed-point scale 2^32 for forces and energies
+#define QG_FMAX 1073741824.0    // |value| limit before the int64 accumulator (2^30)
+
+// energy accumulator slots (fixed point) per trajectory
+enum {
+    EA_PP_EL = 0, EA_PP_VDW, EA_PW_EL, EA_PW_VDW, EA_WW_EL, EA_WW_VDW, EA_LRF,
+    EA_P_BOND, EA_W_BOND, EA_P_ANG, EA_W_ANG, EA_P_TOR, EA_W_TOR, EA_P_IMP, EA_W_IMP,
+    EA_RST_FIX, EA_RST_SHELL, EA_RST_RAD,
+    EA_Q0  // then per state: QB QA QT QI QQ_EL QQ_VDW QP_EL QP_VDW QW_EL QW_VDW
+};
+enum { EQ_B = 0, EQ_A, EQ_T, EQ_I, EQ_QQ_EL, EQ_QQ_VDW, EQ_QP_EL, EQ_QP_VDW, EQ_QW_EL, EQ_QW_VDW, EQ_N };
+#define QG_NE (EA_Q0 + EQ_N * QG_MAXS)
+// energy record row: 29 ENERGIES + QG_MAXS*15 Q_ENERGIES + Temp, Tfree + QG_MAXOD*(Hij, rkl)
+#define QG_REC_E 0
+#define QG_REC_EQ 29
+#define QG_REC_T (29 + 15 * QG_MAXS)
+#define QG_REC_OD (QG_REC_T + 2)
+#define QG_REC (QG_REC_OD + 2 * QG_MAXOD)
+
+// status bits
+#define ST_LIST_OVERFLOW 1
+#define ST_SHAKE 2
+#define ST_FIXED 4
+#define ST_NAN 8
+
+struct TrajInfo {
+    int atom0, natom, nat_solute, nwat;
+    int grp0, ncgp, ncgp_solute;
+    int q0, nqat, nstates;
+    int type0, natyps, lj0;     // type table offset, ljcod matrix offset
+    int qlib0, nqlib, sc0;      // Q type table offset, sc_lookup offset
+    int qvdw;
+    int use_lrf, q_static;      // LRF on; qp/qw lists built once (Rcq > rexcl_o)
+    int tile0, ntile;           // scan tiles of this trajectory
+    int ww_lj;                  // ljcod of the water O pair
+    float ww_A, ww_B;           // O-O LJ products (aLJ_solv(1,c)^2, bLJ_solv(1,c)^2)
+    double ww_Ad, ww_Bd;
+    float chg_solv[3];
+    float el14;
+    double el14d;
+    float rc2_pp, rc2_pw, rc2_ww, rc2_lrf;   // float prefilter thresholds
+    double drc2_pp, drc2_pw, drc2_ww, drc2_lrf, drcq2;
+    double origin[3];           // float coordinates are relative to this point
+    double xpcent[3], xwcent[3];
+    double rwat, fk_wsphere, Dwmz, awmz, fk_pshell, fk_fix;
+    double lambda[QG_MAXS];
+    double dt, Temp0, tau_T;
+    int separate_scaling, detail_temps;
+    int Ndegf, Ndegfree, Ndegfree_solute, Ndegfree_solvent;
+    int shake_mol0, nshake_mol;
+    int nb0[6], nbn[6];         // bonded term ranges: p/w bonds, p/w angles... (see host)
+    int qq0[QG_MAXS], nqq[QG_MAXS];
+    int qterm0[4], nqterm[4];   // Q bond/angle/torsion/improper ranges
+    int ekin_blk0, ekin_nblk;   // Ekin partial slots of this trajectory
+    int ff_type;
+};
+
+// Per-trajectory dynamic state (device).
+struct TrajState {
+    double Tscale_solute, Tscale_solvent, Temp, Tfree;
+    double Ekin;
+    int shake_iters;
+    int pad;
+};
+
+struct DevSys {
+    int ntraj, natom, ngrp, nq;
+    int nb_cap;
+    const TrajInfo *traj;
+    TrajState *tstate;
+    // atoms
+    double *x, *v, *xx;
+    const double *xtop, *winv, *mass;
+    float4 *pos, *poslo;            // hi part + charge, lo part
+    const int *atype;               // global type index
+    const double *crg_d;            // scaled charges (FP64)
+    const int *aq;                  // global Q index or -1
+    const uint8_t *aexcl, *ashell;
+    const int *atraj, *agrp;
+    unsigned long long *fx;         // 3*natom fixed-point gradient
+    const unsigned long long *exmask, *p14mask;  // solute exclusion / 1-4 bits, offsets -32..31
+    const int *exlong_first, *exlong_j, *exlong_kind;
+    // types
+    const float *avdw, *bvdw;       // [type*3 + code-1]
+    const double *avdw_d, *bvdw_d;
+    const int8_t *ljcod;            // per-trajectory matrices at TrajInfo::lj0
+    // groups
+    const int *g_start, *g_atoms, *g_switch, *g_kind, *g_traj;
+    const uint8_t *g_excl;
+    double *g_cent;                 // 3*G
+    double *g_phi;                  // QG_NLRF*G accumulators
+    float *g_phif;                  // QG_NPHI*G Taylor coefficients
+    int *nb_count, *nb_list;
+    const int *tile_g0, *tile_g1;
+    // Q atoms
+    const int *q_atom;              // global atom of each global Q index
+    const float *qcrg_f;            // [q*QG_MAXS+s]
+    const double *qcrg_d;
+    const int *qiac;                // [q*QG_MAXS+s] global Q-type index
+    const float *qavdw, *qbvdw;     // [qtype*3 + code-1]
+    const double *qavdw_d, *qbvdw_d;
+    const float *sc_f;              // sc_lookup, [(q*(natyps+nqat)+col)*QG_MAXS+s] at TrajInfo::sc0
+    const double *sc_d;
+    float *qw_A, *qw_B;             // [q*QG_MAXS+s] water-O LJ products
+    const double *qw_Ad, *qw_Bd;
+    const int *qw_lj;               // [q] LJ code of the water-O / Q-atom pair
+    uint8_t *qw_member;             // per water (global water index) in the qw list
+    uint8_t *qp_member;             // per atom in the qp list
+    const uint8_t *qp_skip;
+    const int *qp14_first, *qp14_q; // per atom CSR of Q atoms with qconn == 4
+    // nbqq
+    const int *qq_iq, *qq_j, *qq_jq; const int8_t *qq_lj; const double *qq_els;
+    // Q bonded terms (flattened per kind, codes already per state)
+    const int *qt_atoms;            // 4 atoms per term
+    const int *qt_cod;              // [term*QG_MAXS+s] 1-based lib index (global) or 0
+    const int *qt_kind, *qt_traj;   // 0 bond 1 angle 2 torsion 3 improper
+    const double *qt_lib;           // 4 doubles per lib entry
+    int nqt;
+    // classical bonded terms
+    const int *bt_atoms;            // 4 atoms per term
+    const int *bt_cod;              // global lib index (0-based)
+    const double *bt_lib;           // 4 doubles per entry
+    const int *bt_kind;             // 0 bond 1 angle 2 torsion 3 harmonic improper 4 periodic improper
+    int nbt;                        // padded term list; blocks are single (trajectory, slot)
+    const int *bt_blk_traj, *bt_blk_slot;
+    // off-diagonal couplings
+    const int *od_traj, *od_ij, *od_kl; const double *od_Amu; int nod;
+    double *od_out;                 // [traj][QG_MAXOD][2]: Hij, rkl
+    // shake
+    const int *shk_first, *shk_i, *shk_j, *shk_traj;
+    const double *shk_d2;
+    int nshk_mol;
+    // energies and reductions
+    unsigned long long *eacc;       // QG_NE per trajectory
+    double *ekin_part;              // 4 per Ekin block
+    int *status;
+};
+
+// ------------------------------------------------------------- helpers
+__device__ __forceinline__ void fx_add(unsigned long long *p, double v, int *status) {
+    if (!(fabs(v) < QG_FMAX)) { atomicOr(status, ST_FIXED); return; }
+    long long q = __double2ll_rn(v * QG_FSCALE);
+    atomicAdd(p, (unsigned long long)q);
+}
+__device__ __forceinline__ double fx_get(unsigned long long u) { return (double)(long long)u * (1.0 / QG_FSCALE); }
+
+// compensated float accumulation (Kahan)
+struct KSum {
+    float s, c;
+    __device__ __forceinline__ void zero() { s = 0.f; c = 0.f; }
+    __device__ __forceinline__ void add(float v) {
+        float y = v - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum_f(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// hi/lo float difference: (b - a) with the rounding error of the absolute
+// coordinates removed
+__device__ __forceinline__ float3 dpos(const float4 ah, const float4 al, const float4 bh, const float4 bl) {
+    return make_float3((bh.x - ah.x) + (bl.x - al.x), (bh.y - ah.y) + (bl.y - al.y), (bh.z - ah.z) + (bl.z - al.z));
+}
+
+// exact FP64 squared distance in the reference's operation order (no FMA)
+__device__ __forceinline__ double dist2_exact(const double *x, int i, int j) {
+    double a = __dsub_rn(x[3 * i], x[3 * j]);
+    double b = __dsub_rn(x[3 * i + 1], x[3 * j + 1]);
+    double c = __dsub_rn(x[3 * i + 2], x[3 * j + 2]);
+    return __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
+}
+
+// ---------------------------------------------------------- launchers
+struct KernelProfiler;
+struct LaunchCtx {
+    cudaStream_t stream;
+    long long *nlaunch;
+    KernelProfiler *prof = nullptr;   // per-kernel CUDA-event timing when set
+};
+// bracket one launch with CUDA events on L.stream (no-ops without a profiler)
+void prof_begin(LaunchCtx &L, const char *name);
+void prof_end(LaunchCtx &L);
+struct BlockTables {
+    // per-item lists (padded per trajectory to QG_BLOCK)
+    const int *wgrp; int nwgrp;        // water groups
+    const int *satom; int nsatom;      // solute atoms (all, incl. Q/excluded -> skipped in kernels)
+    const int *scan_t0; const int *scan_tn; const int *scan_traj; int nscan;  // scan blocks
+    const int *gall; int ngall;        // all groups (centres)
+    const int *aall; int naall;        // all atoms, padded (Ekin blocks)
+    const int *qqblk_traj, *qqblk_s; int nqqblk;
+};
+
+void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L);
+void launch_scan(const DevSys &S, const BlockTables &B, LaunchCtx &L);
+void launch_qmember(const DevSys &S, const BlockTables &B, LaunchCtx &L, int first);
+// Energy accuracy: EACC_FP32 sums FP32 pair energies (Kahan + FP64 block
+// sums); EACC_FP64 evaluates every pair energy in FP64 from the master
+// coordinates (forces are FP32 in both); EACC_RECORD uses FP64 on the steps
+// whose energies are recorded (step = recctl[0] + k, step % ene_every == 0).
+enum { EACC_FP32 = 0, EACC_FP64 = 1, EACC_RECORD = 2 };
+struct EaccSel {
+    int mode;
+    const int *recctl;
+    int k, ene_every;
+};
+void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy);
+void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy);
+void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
+void launch_qp(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
+void launch_qq(const DevSys &S, const BlockTables &B, LaunchCtx &L);
+void launch_qbonded(const DevSys &S, const BlockTables &B, LaunchCtx &L, int nqterm_total);
+void launch_bonded(const DevSys &S, const BlockTables &B, LaunchCtx &L);
+void launch_integrate(const DevSys &S, const BlockTables &B, LaunchCtx &L);
+void launch_shake(const DevSys &S, const BlockTables &B, LaunchCtx &L, int traj_filter);
+void launch_post(const DevSys &S, const BlockTables &B, LaunchCtx &L, int shake_on);
+void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *rec, const int *rec_base, int k,
+                     int ene_every, int rec_cap);
+void launch_tick(LaunchCtx &L, int *rec_base, int n);
+void launch_offdiag(const DevSys &S, LaunchCtx &L);
+void launch_fix_shell(const DevSys &S, const BlockTables &B, LaunchCtx &L);
+void launch_restrain_solvent(const DevSys &S, const BlockTables &B, LaunchCtx &L);
+void launch_mirror(const DevSys &S, const BlockTables &B, LaunchCtx &L);
+void launch_grad_to_double(const DevSys &S, LaunchCtx &L, double *out, int atom0, int natom);

@@ -120,6 +120,49 @@ class System:
     def nwat(self) -> int:
         return (self.natom - self.nat_solute) // 3
 
+    # ------------------------------------------------------------ fixtures
+    def save_npz(self, path: str) -> None:
+        """Store every field (arrays, scalars, lists, the nbqq dict) in one npz."""
+        out = {}
+        for k, v in self.__dict__.items():
+            if k.startswith("_"):
+                continue
+            if isinstance(v, dict):
+                for kk, vv in v.items():
+                    out[f"dict:{k}:{kk}"] = np.asarray(vv)
+            elif isinstance(v, list) and v and isinstance(v[0], tuple):
+                out[f"tuples:{k}"] = np.asarray(v, dtype=np.float64).reshape(len(v), -1)
+            elif isinstance(v, list):
+                out[f"list:{k}"] = np.asarray(v)
+            elif v is None:
+                out[f"none:{k}"] = np.zeros(0)
+            else:
+                out[f"val:{k}"] = np.asarray(v)
+        np.savez_compressed(path, **out)
+
+    @classmethod
+    def load_npz(cls, path: str) -> "System":
+        kw: dict = {}
+        with np.load(path) as z:
+            for key in z.files:
+                kind, _, name = key.partition(":")
+                a = z[key]
+                if kind == "dict":
+                    d, _, sub = name.partition(":")
+                    kw.setdefault(d, {})[sub] = a
+                elif kind == "tuples":
+                    kw[name] = [tuple(r) for r in a.tolist()]
+                elif kind == "list":
+                    kw[name] = a.tolist()
+                elif kind == "none":
+                    kw[name] = None
+                else:
+                    kw[name] = a if a.ndim else a.item()
+        for k in ("offd",):
+            kw.setdefault(k, [])
+        kw["offd"] = [tuple(int(x) if i < 4 else x for i, x in enumerate(r)) for r in kw["offd"]]
+        return cls(**kw)
+
     # ----------------------------------------------------------- builders
     @classmethod
     def from_files(cls, top_text: str, fep_text: str | None, inp_text: str) -> "System":

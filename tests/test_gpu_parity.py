@@ -1,0 +1,219 @@
+"""GPU engine vs the FP64 oracle on identical inputs, through the C-ABI.
+
+Tolerances (pair terms run in FP32 with hi/lo coordinate differences, sums in
+FP64 / int64 fixed point):
+  * pair-list sets: exact (same (i, j, LJcod) records as the reference loops);
+  * forces: relative RMS  sqrt(sum|dF|^2 / sum|F|^2) <= 1e-5;
+  * energies: |dE| <= 1e-5 * (sum of |terms| scale) -- see ENERGY_TOL below;
+  * LRF multipoles: |d phi| <= 1e-5 * max|phi| per component family;
+  * SHAKE and the FP64 integrator: 1e-9 absolute on coordinates.
+"""
+from collections import Counter
+
+import numpy as np
+import pytest
+
+from conftest import golden_system
+from listcheck import expand, oracle_records
+
+pytestmark = pytest.mark.gpu
+
+FORCE_RTOL = 1e-5
+ENERGY_REL = 1e-5       # relative to |E| ...
+ENERGY_ABS = 2e-3       # ... or absolute kcal/mol for terms that nearly cancel
+
+
+def _engine(systems):
+    from qsource_gb300.engine import Engine
+    return Engine(systems)
+
+
+def _oracle(s):
+    from oracle.oracle import Oracle
+    return Oracle(s)
+
+
+@pytest.fixture(scope="module")
+def systems(engine_lib):
+    from qsource_gb300 import synth
+    out = {"cfg1": synth.config(1), "cfg2": synth.config(2), "cfg4": synth.config(4)}
+    g = golden_system("basic_sph")
+    o = _oracle(g)
+    o.maxwell(g.Tmaxw, int(g.seed))
+    assert o.initial_shaking() == 0
+    g.x, g.v = o.coords()
+    out["golden"] = g
+    return out
+
+
+def rel_rms(a, b):
+    return float(np.sqrt(np.sum((a - b) ** 2) / np.sum(b ** 2)))
+
+
+def energies_close(eg, eo, keys):
+    bad = []
+    for k in keys:
+        if abs(eg[k] - eo[k]) > max(ENERGY_REL * abs(eo[k]), ENERGY_ABS):
+            bad.append((k, eg[k], eo[k]))
+    return bad
+
+
+E_KEYS = ["pp_el", "pp_vdw", "pw_el", "pw_vdw", "ww_el", "ww_vdw", "lrf", "qx_el", "qx_vdw", "q_bond",
+          "q_angle", "q_torsion", "q_improper", "p_bond", "p_angle", "p_torsion", "p_improper", "rst_shell",
+          "rst_solvent_radial"]
+EQ_KEYS = ["qq_el", "qq_vdw", "qp_el", "qp_vdw", "qw_el", "qw_vdw", "q_bond", "q_angle", "q_torsion", "q_improper"]
+
+
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg4"])
+def test_pair_lists_exact(systems, name):
+    s = systems[name]
+    e = _engine(s)
+    e.make_pair_lists()
+    o = _oracle(s)
+    o.make_pair_lists()
+    ex = expand(s, e.group_pairs())
+    for lst in ("pp", "pw", "ww"):
+        assert Counter(ex[lst]) == Counter(oracle_records(o, lst)), lst
+
+
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2"])
+def test_lrf_multipoles(systems, name):
+    s = systems[name]
+    e = _engine(s)
+    e.make_pair_lists()
+    o = _oracle(s)
+    o.make_pair_lists()
+    g, r = e.lrf(), o.get_lrf()
+    assert np.allclose(g[:, :3], r[:, :3], rtol=0, atol=1e-12)
+    for lo, hi in ((3, 4), (4, 7), (7, 16), (16, 43)):
+        scale = np.abs(r[:, lo:hi]).max()
+        err = np.abs(g[:, lo:hi] - r[:, lo:hi]).max()
+        assert err <= 1e-5 * scale, (lo, err, scale)
+
+
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg4"])
+def test_forces_and_energies(systems, name):
+    s = systems[name]
+    e = _engine(s)
+    e.make_pair_lists()
+    d, E, EQ = e.pot_energy(0, terms=0x1F)
+    o = _oracle(s)
+    o.make_pair_lists()
+    do, Eo, EQo = o.pot_energy(0x1F)
+    assert rel_rms(d, do) <= FORCE_RTOL
+    assert not energies_close(E, Eo, E_KEYS)
+    for q, qo in zip(EQ, EQo):
+        assert not energies_close(q, qo, EQ_KEYS)
+
+
+def test_golden_columns_on_gpu(systems, golden):
+    """The GPU path reproduces the reference's printed step-0 values."""
+    s = systems["golden"]
+    e = _engine(s)
+    e.make_pair_lists()
+    _, E, EQ = e.pot_energy(0)
+    q = EQ[0]
+    got = {"QEL": q["qp_el"] + q["qw_el"], "QVdW": q["qp_vdw"] + q["qw_vdw"],
+           "EL": E["pp_el"] + E["pw_el"] + E["ww_el"], "VdW": E["pp_vdw"] + E["pw_vdw"] + E["ww_vdw"],
+           "QBND": q["q_bond"], "QANG": q["q_angle"], "QTOR": q["q_torsion"], "QIMP": q["q_improper"],
+           "BND": E["p_bond"], "ANG": E["p_angle"], "TOR": E["p_torsion"], "IMP": E["p_improper"]}
+    for col, want in golden["basic_sph"].items():
+        assert round(got[col], 2) == pytest.approx(want, abs=1e-9), (col, got[col], want)
+
+
+def test_shake_matches_oracle(systems):
+    s = systems["cfg1"]
+    e = _engine(s)
+    o = _oracle(s)
+    rng = np.random.default_rng(1)
+    xx = s.x.copy()
+    x = xx + rng.normal(0, 0.005, size=xx.shape)
+    xg, _ = e.shake(0, xx, x)
+    xo = x.copy()
+    assert o.shake(xx.copy(), xo) >= 1
+    assert np.abs(xg - xo).max() < 1e-9
+
+
+def test_short_md_matches_oracle(systems):
+    """20 Berendsen leap-frog steps with SHAKE and lists every 10 steps."""
+    s = systems["cfg1"]
+    e = _engine(s)
+    rows = e.run(20, ene_every=1)[0]
+    o = _oracle(s)
+    o.temperature()
+    rc, orows, oq, T = o.md_run(20)
+    assert rc == 0 and len(rows) == 20
+    for k in (0, 1, 10, 19):
+        pg, po = rows[k][1]["potential"], orows[k]["potential"]
+        assert abs(pg - po) <= 1e-4 * max(1.0, abs(po)), (k, pg, po)
+        kg, ko = rows[k][1]["kinetic"], orows[k]["kinetic"]
+        assert abs(kg - ko) <= 1e-4 * ko, (k, kg, ko)
+    x, _ = e.coords(0)
+    xo, _ = o.coords()
+    assert np.abs(x - xo).max() < 1e-4
+
+
+def test_run_is_bit_deterministic(systems):
+    s = systems["cfg2"]
+    a = _engine(s)
+    a.run(25)
+    b = _engine(s)
+    b.run(25)
+    xa, va = a.coords(0)
+    xb, vb = b.coords(0)
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+
+
+def test_batch_equals_single(systems):
+    """A trajectory gives bitwise the same result alone or inside a batch."""
+    s1, s2 = systems["cfg1"], systems["cfg2"]
+    batch = _engine([s1, s2])
+    batch.make_pair_lists()
+    single = _engine(s2)
+    single.make_pair_lists()
+    db, Eb, _ = batch.pot_energy(1)
+    ds, Es, _ = single.pot_energy(0)
+    assert np.array_equal(db, ds)
+    assert Eb == Es
+    batch.run(12)
+    single.run(12)
+    assert np.array_equal(batch.coords(1)[0], single.coords(0)[0])
+
+
+def test_shake_failure_is_reported(systems):
+    """Coincident reference positions make SHAKE diverge: the bounded
+    iteration stops at 1000 sweeps and the call returns QGPU_E_SHAKE."""
+    from qsource_gb300.engine import QgpuError
+    s = systems["cfg1"]
+    e = _engine(s)
+    xx = s.x.copy()
+    o = s.shake_i[0]
+    xx[3 * s.shake_j[0]:3 * s.shake_j[0] + 3] = xx[3 * o:3 * o + 3]
+    with pytest.raises(QgpuError) as ei:
+        e.shake(0, xx, s.x.copy())
+    assert ei.value.code == 4
+    # the context stays usable once the host hands it valid coordinates again
+    e.set_coords(0, s.x, s.v)
+    e.make_pair_lists()
+    d, _, _ = e.pot_energy(0)
+    assert np.isfinite(d).all()
+
+
+def test_list_overflow_is_reported(systems, monkeypatch):
+    from qsource_gb300.engine import QgpuError
+    monkeypatch.setenv("QGPU_NB_CAP", "8")
+    e = _engine(systems["cfg1"])
+    with pytest.raises(QgpuError) as ei:
+        e.make_pair_lists()
+    assert ei.value.code == 3
+
+
+def test_invalid_descriptor_is_rejected(systems):
+    from qsource_gb300.engine import QgpuError
+    import copy
+    s = copy.copy(systems["cfg1"])
+    s.nstates = 5
+    s.lambdas = [0.2] * 5 + [0.0] * 5
+    with pytest.raises(QgpuError) as ei:
+        _engine(s)
+    assert ei.value.code == 6
