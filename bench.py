@@ -299,6 +299,7 @@ def main():
     name, (kms, kcnt) = top
     fl = kernel_flops(name, wc)
     share = {k: round(v[0] / sum(x[0] for x in prof.values()), 4) for k, v in prof.items()}
+    us_per_step = {k: round(1e3 * v[0] / (2 * NB), 2) for k, v in prof.items()}
     roof = None
     if fl is not None:
         achieved = fl / (kms / kcnt * 1e-3) / 1e12
@@ -325,6 +326,7 @@ def main():
                        "energy sink, read back x,v (host wall clock)"},
         "roofline": roof,
         "kernel_share": share,
+        "kernel_us_per_step": us_per_step,
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None,
         "clocks": clk,
         "gpu_launches": int(launches),

@@ -40,18 +40,21 @@ __device__ __forceinline__ bool within(float d2, float rc2, double drc2, const d
     return dist2_exact(x, a, b) <= drc2;
 }
 
-// One thread per target charge group; the block walks all groups of its
-// trajectory in shared-memory tiles.  Near groups (inside the pp/pw/ww
-// cut-off) go to the target's neighbour list (both directions: a full list),
-// far groups inside RcLRF add their non-Q atoms to the target's multipole
+// Phase 1 of the scan: one thread per target charge group, one block per
+// (128 targets, source chunk of QG_TPC shared-memory tiles of the same
+// trajectory).  Near groups (inside the pp/pw/ww cut-off) go to the target's
+// chunk segment of near groups (a full list: both directions are found); far
+// groups inside RcLRF add their non-Q atoms to the target's multipole
 // expansion (lrf_update, src/md.f90:5896-5981), accumulated as 24 symmetric
-// sums in FP32 and folded into FP64 every 4 tiles.
-__global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, const int *blk_tn, const int *blk_traj) {
+// FP32 sums per chunk.
+__global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, const int *blk_tn, const int *blk_traj,
+                                                   const int *blk_chunk) {
     __shared__ float4 s_hi[QG_TILE_G], s_lo[QG_TILE_G];
     __shared__ int s_meta[QG_TILE_G], s_rep[QG_TILE_G], s_aoff[QG_TILE_G + 1];
     __shared__ float4 s_atom[QG_TILE_A];
     const int b = blockIdx.x;
     const TrajInfo &T = S.traj[blk_traj[b]];
+    const int chunk = blk_chunk[b];
     const int tid = threadIdx.x;
     const int t = blk_t0[b] + tid;
     const bool valid = tid < blk_tn[b];
@@ -68,15 +71,16 @@ __global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, 
         cy = (float)(S.g_cent[3 * t + 1] - T.origin[1]);
         cz = (float)(S.g_cent[3 * t + 2] - T.origin[2]);
     }
+    const long long slot = T.scr0 + (long long)chunk * T.ncgp + (t - T.grp0);
+    int *nbseg = S.scr_nb + (size_t)slot * QG_CAPC;
     float acc[QG_NLRF];
-    double accd[QG_NLRF];
 #pragma unroll
-    for (int k = 0; k < QG_NLRF; ++k) { acc[k] = 0.f; accd[k] = 0.0; }
-    int cnt = 0;
-    const int cap = S.nb_cap;
+    for (int k = 0; k < QG_NLRF; ++k) acc[k] = 0.f;
+    int cntw = 0, cnts = 0;
     const float rc2_lrf = T.rc2_lrf;
     const bool lrf = T.use_lrf != 0;
-    for (int it = 0; it < T.ntile; ++it) {
+    const int it0 = chunk * QG_TPC, it1 = min(T.ntile, it0 + QG_TPC);
+    for (int it = it0; it < it1; ++it) {
         const int tile = T.tile0 + it;
         const int g0 = S.tile_g0[tile], g1 = S.tile_g1[tile], ng = g1 - g0;
         const int ab = S.g_start[g0], ae = S.g_start[g1];
@@ -109,8 +113,10 @@ __global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, 
                 float3 d = dpos(th, tl, s_hi[s], s_lo[s]);
                 float d2 = d.x * d.x + d.y * d.y + d.z * d.z;
                 if (within(d2, rc2, drc2, S.x, rt, s_rep[s])) {
-                    if (cnt < cap) S.nb_list[(size_t)t * cap + cnt] = g;
-                    cnt++;
+                    // at most QG_CAPC groups per chunk: water neighbours (as
+                    // their O atom) from the front, solute groups from the back
+                    if (kind_s) nbseg[cntw++] = s_rep[s];
+                    else nbseg[QG_CAPC - 1 - cnts++] = g;
                 } else if (lrf && within(d2, rc2_lrf, T.drc2_lrf, S.x, rt, s_rep[s])) {
                     for (int k = s_aoff[s]; k < s_aoff[s + 1]; ++k) {
                         const float4 p = s_atom[k];
@@ -137,21 +143,55 @@ __global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, 
                     }
                 }
             }
-            if ((it & 3) == 3) {
-#pragma unroll
-                for (int k = 0; k < QG_NLRF; ++k) { accd[k] += (double)acc[k]; acc[k] = 0.f; }
-            }
         }
     }
     if (!valid) return;
+    S.scr_cnt[slot] = cntw | (cnts << 16);
+    float *ph = S.scr_phi + (size_t)slot * QG_NLRF;
 #pragma unroll
-    for (int k = 0; k < QG_NLRF; ++k) accd[k] += (double)acc[k];
+    for (int k = 0; k < QG_NLRF; ++k) ph[k] = acc[k];
+}
+
+// Phase 2: one warp per target group folds the chunks in order -- lane k
+// sums LRF component k in FP64, the lanes copy the chunks' near-group
+// segments into the neighbour list (water entries of every chunk first, then
+// solute entries) -- and lane 0 forms the symmetric Taylor coefficients.
+__global__ void k_scan_reduce(DevSys S) {
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (t >= S.ngrp) return;
+    const TrajInfo &T = S.traj[S.g_traj[t]];
+    const bool ex = S.g_excl[t];
+    double acc = 0.0;
+    const int cap = S.nb_cap;
+    int *lst = S.nb_list + (size_t)t * cap;
+    int cnt = 0;
+    for (int c = 0; c < T.nchunk; ++c) {
+        const long long slot = T.scr0 + (long long)c * T.ncgp + (t - T.grp0);
+        if (lane < QG_NLRF) acc += (double)S.scr_phi[(size_t)slot * QG_NLRF + lane];
+        const int nw = ex ? 0 : (S.scr_cnt[slot] & 0xffff);
+        const int *seg = S.scr_nb + (size_t)slot * QG_CAPC;
+        for (int k = lane; k < nw; k += 32)
+            if (cnt + k < cap) lst[cnt + k] = seg[k];
+        cnt += nw;
+    }
+    const int nwat = cnt;
+    for (int c = 0; c < T.nchunk; ++c) {
+        const long long slot = T.scr0 + (long long)c * T.ncgp + (t - T.grp0);
+        const int ns = ex ? 0 : (S.scr_cnt[slot] >> 16);
+        const int *seg = S.scr_nb + (size_t)slot * QG_CAPC;
+        for (int k = lane; k < ns; k += 32)
+            if (cnt + k < cap) lst[cnt + k] = seg[QG_CAPC - 1 - k];
+        cnt += ns;
+    }
+    double accd[QG_NLRF];
+#pragma unroll
+    for (int k = 0; k < QG_NLRF; ++k) accd[k] = __shfl_sync(0xffffffffu, acc, k);
+    if (lane < QG_NLRF) S.g_phi[(size_t)t * QG_NLRF + lane] = acc;
+    if (lane != 0) return;
+    S.nb_nw[t] = nwat < cap ? nwat : cap;
     S.nb_count[t] = cnt < cap ? cnt : cap;
     if (cnt > cap) atomicOr(S.status, ST_LIST_OVERFLOW);
-    double *ph = S.g_phi + (size_t)t * QG_NLRF;
-#pragma unroll
-    for (int k = 0; k < QG_NLRF; ++k) ph[k] = accd[k];
-    // symmetric Taylor coefficients
     float *pf = S.g_phif + (size_t)t * QG_NPHI;
     const double q1x = accd[5], q1y = accd[6], q1z = accd[7];
     pf[0] = (float)accd[0];
@@ -208,7 +248,11 @@ void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
 }
 void launch_scan(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
     prof_begin(L, "k_scan");
-    k_scan<<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj);
+    k_scan<<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
+    prof_end(L);
+    (*L.nlaunch)++;
+    prof_begin(L, "k_scan_reduce");
+    k_scan_reduce<<<nblk(S.ngrp * 32, 128), 128, 0, L.stream>>>(S);
     prof_end(L);
     (*L.nlaunch)++;
 }

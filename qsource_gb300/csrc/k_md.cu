@@ -58,7 +58,13 @@ __global__ void k_shake(DevSys S, int traj_filter) {
             if (fabs(diff) < SHAKE_TOL * d2) ready |= (1ull << c);
             const double scp = xij[0] * xxij[0] + xij[1] * xxij[1] + xij[2] * xxij[2];
             const double wi = S.winv[i], wj = S.winv[j];
-            const double corr = diff / (2.0 * scp * (wi + wj));
+            // diff / den with a Newton-refined reciprocal (two steps of
+            // y <- y (2 - den y) from a float seed reach FP64 precision)
+            const double den = 2.0 * scp * (wi + wj);
+            double y = (double)__fdividef(1.0f, (float)den);   // seed; refined below
+            y = y * (2.0 - den * y);
+            y = y * (2.0 - den * y);
+            const double corr = diff * y;
             for (int a = 0; a < 3; ++a) {
                 x[3 * i + a] += xxij[a] * corr * wi;
                 x[3 * j + a] -= xxij[a] * corr * wj;
@@ -71,33 +77,132 @@ __global__ void k_shake(DevSys S, int traj_filter) {
     atomicAdd(&S.tstate[tr].shake_iters, nits);
 }
 
-// After SHAKE: v = (x - xx)/dt for every atom (md_run, src/md.f90:6596-6597),
-// refresh the float mirror, and per-block kinetic-energy partial sums
-// (solute, free solute, solvent, free solvent) in a fixed reduction order.
-__global__ void __launch_bounds__(QG_BLOCK) k_post(DevSys S, const int *aall, int shake_on) {
-    __shared__ double red[4][QG_BLOCK / 32];
-    const int i = aall[blockIdx.x * blockDim.x + threadIdx.x];
-    double ek[4] = {0, 0, 0, 0};
-    if (i >= 0) {
-        const int tr = S.atraj[i];
-        const TrajInfo &T = S.traj[tr];
-        const double dt = T.dt;
-        double vv = 0;
-        for (int c = 0; c < 3; ++c) {
-            const int k = 3 * i + c;
-            double v = S.v[k];
-            if (shake_on) { v = (S.x[k] - S.xx[k]) / dt; S.v[k] = v; }
-            vv += v * v;
+// SHAKE of one water held in registers: the Gauss-Seidel sweeps of shake
+// (src/md.f90:17581-17679) over its constraints in topology order
+// O-H1, O-H2, H1-H2 (local atoms (0,1), (0,2), (1,2)).  Returns the sweep
+// count; sets *fail at SHAKE_MAX_ITER.
+template <int I, int J>
+__device__ __forceinline__ void shake_pair(double (&x)[3][3], const double (&xxij)[3], const double (&ua)[3],
+                                           const double (&ub)[3], double d2, double tol, double den0, unsigned &ready,
+                                           int c) {
+    if (ready & (1u << c)) return;
+    const double x0 = x[I][0] - x[J][0], x1 = x[I][1] - x[J][1], x2 = x[I][2] - x[J][2];
+    const double diff = d2 - (x0 * x0 + x1 * x1 + x2 * x2);
+    if (fabs(diff) < tol) ready |= 1u << c;
+    const double den = den0 * (x0 * xxij[0] + x1 * xxij[1] + x2 * xxij[2]);
+    // diff / den with a Newton-refined reciprocal of a float seed
+    double y = (double)__fdividef(1.0f, (float)den);   // seed; refined below
+    y = y * (2.0 - den * y);
+    y = y * (2.0 - den * y);
+    const double corr = diff * y;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        x[I][a] += ua[a] * corr;
+        x[J][a] -= ub[a] * corr;
+    }
+}
+
+__device__ int shake_water(double (&x)[3][3], const double (&xx)[3][3], const double (&w)[3], const double (&d2)[3],
+                           bool *fail) {
+    double xxij[3][3], ua[3][3], ub[3][3], den0[3], tol[3];
+    const int ci[3] = {0, 0, 1}, cj[3] = {1, 2, 2};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            xxij[c][a] = xx[ci[c]][a] - xx[cj[c]][a];
+            ua[c][a] = xxij[c][a] * w[ci[c]];
+            ub[c][a] = xxij[c][a] * w[cj[c]];
         }
-        const double e = 0.5 * S.mass[i] * vv;
-        const bool solute = (i - T.atom0) < T.nat_solute;
-        const bool fr = !S.aexcl[i];
-        if (solute) { ek[0] = e; ek[1] = fr ? e : 0; } else { ek[2] = e; ek[3] = fr ? e : 0; }
-        float4 h, l;
-        const double r0 = S.x[3 * i] - T.origin[0], r1 = S.x[3 * i + 1] - T.origin[1], r2 = S.x[3 * i + 2] - T.origin[2];
-        h.x = (float)r0; h.y = (float)r1; h.z = (float)r2; h.w = S.pos[i].w;
-        l.x = (float)(r0 - (double)h.x); l.y = (float)(r1 - (double)h.y); l.z = (float)(r2 - (double)h.z); l.w = 0.f;
-        S.pos[i] = h; S.poslo[i] = l;
+        den0[c] = 2.0 * (w[ci[c]] + w[cj[c]]);
+        tol[c] = SHAKE_TOL * d2[c];
+    }
+    unsigned ready = 0u;
+    int nits = 0;
+    for (;;) {
+        shake_pair<0, 1>(x, xxij[0], ua[0], ub[0], d2[0], tol[0], den0[0], ready, 0);
+        shake_pair<0, 2>(x, xxij[1], ua[1], ub[1], d2[1], tol[1], den0[1], ready, 1);
+        shake_pair<1, 2>(x, xxij[2], ua[2], ub[2], d2[2], tol[2], den0[2], ready, 2);
+        nits++;
+        if (ready == 7u) break;
+        if (nits >= SHAKE_MAX_ITER) { *fail = true; break; }
+    }
+    return nits;
+}
+
+// Per-step update over the trajectory's update items (atoms, or whole 3-atom
+// water molecules that carry SHAKE constraints):
+//   mode 0: kinetic energy + float mirror only (temperature before step 0);
+//   mode 1: leap-frog + Berendsen (newvel_ber), SHAKE of the molecule in
+//           registers, v = (x - xx)/dt (md_run :6596-6597), mirror, Ekin;
+//   mode 2: v = (x - xx)/dt after the separate SHAKE kernel, mirror, Ekin.
+// Ekin partials (solute, free solute, solvent, free solvent) per block.
+__global__ void __launch_bounds__(QG_BLOCK) k_update(DevSys S, const int *items, int mode) {
+    __shared__ double red[4][QG_BLOCK / 32];
+    const int it = items[blockIdx.x * blockDim.x + threadIdx.x];
+    double ek[4] = {0, 0, 0, 0};
+    if (it >= 0) {
+        const bool mol = (it >> 30) & 1;
+        const int m = it & 0x3fffffff;
+        const int a0 = mol ? S.shk_i[S.shk_first[m]] : m;   // first atom of the item
+        const int na = mol ? 3 : 1;
+        const int tr = S.atraj[a0];
+        const TrajInfo &T = S.traj[tr];
+        TrajState &TS = S.tstate[tr];
+        const double dt = T.dt;
+        double x[3][3], xx[3][3], v[3][3], w[3];
+        for (int k = 0; k < na; ++k) {
+            const int i = mol ? a0 + k : a0;
+            w[k] = S.winv[i];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) { x[k][a] = S.x[3 * i + a]; v[k][a] = S.v[3 * i + a]; xx[k][a] = S.xx[3 * i + a]; }
+            if (mode == 1) {
+                const double ts = (i - T.atom0) < T.nat_solute ? TS.Tscale_solute : TS.Tscale_solvent;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const double g = fx_get(S.fx[3 * i + a]);
+                    S.fx[3 * i + a] = 0ull;
+                    v[k][a] = (v[k][a] - g * w[k] * dt) * ts;
+                    xx[k][a] = x[k][a];
+                    x[k][a] = x[k][a] + v[k][a] * dt;
+                }
+            }
+        }
+        if (mode == 1 && mol) {
+            const int c0 = S.shk_first[m];
+            const double d2[3] = {S.shk_d2[c0], S.shk_d2[c0 + 1], S.shk_d2[c0 + 2]};
+            bool fail = false;
+            const int nits = shake_water(x, xx, w, d2, &fail);
+            if (fail) atomicOr(S.status, ST_SHAKE);
+            atomicAdd(&TS.shake_iters, nits);
+        }
+        const bool vfix = (mode == 1 && T.nshake_mol > 0) || mode == 2;
+        for (int k = 0; k < na; ++k) {
+            const int i = mol ? a0 + k : a0;
+            double vv = 0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                if (vfix) v[k][a] = (x[k][a] - xx[k][a]) * T.inv_dt;
+                vv += v[k][a] * v[k][a];
+            }
+            if (mode == 1) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) { S.x[3 * i + a] = x[k][a]; S.xx[3 * i + a] = xx[k][a]; }
+            }
+            if (mode != 0) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) S.v[3 * i + a] = v[k][a];
+            }
+            const double e = 0.5 * S.mass[i] * vv;
+            const bool fr = !S.aexcl[i];
+            if ((i - T.atom0) < T.nat_solute) { ek[0] += e; ek[1] += fr ? e : 0; }
+            else { ek[2] += e; ek[3] += fr ? e : 0; }
+            float4 h, l;
+            const double r0 = x[k][0] - T.origin[0], r1 = x[k][1] - T.origin[1], r2 = x[k][2] - T.origin[2];
+            h.x = (float)r0; h.y = (float)r1; h.z = (float)r2; h.w = S.pos[i].w;
+            l.x = (float)(r0 - (double)h.x); l.y = (float)(r1 - (double)h.y); l.z = (float)(r2 - (double)h.z); l.w = 0.f;
+            S.pos[i] = h; S.poslo[i] = l;
+        }
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int k = 0; k < 4; ++k) {
@@ -114,17 +219,30 @@ __global__ void __launch_bounds__(QG_BLOCK) k_post(DevSys S, const int *aall, in
 
 // One block per trajectory: temperature() (optional) and the energy summary
 // of pot_energy; writes a record row and clears the energy accumulators.
+// The Ekin partials are summed by the warp in a fixed order (strided lanes,
+// then a shuffle tree), the accumulator slots are read by all lanes.
 __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_base, int k, int ene_every, int rec_cap) {
+    __shared__ double v[QG_NE];
+    __shared__ double e4[4];
     const int tr = blockIdx.x;
-    if (threadIdx.x != 0) return;
+    const int lane = threadIdx.x;
     const TrajInfo &T = S.traj[tr];
     TrajState &TS = S.tstate[tr];
+    unsigned long long *ea = S.eacc + (size_t)tr * QG_NE;
+    for (int s = lane; s < QG_NE; s += 32) { v[s] = fx_get(ea[s]); ea[s] = 0ull; }
     if (do_temp) {
-        double e[4] = {0, 0, 0, 0};
-        for (int b = 0; b < T.ekin_nblk; ++b)
-            for (int c = 0; c < 4; ++c) e[c] += S.ekin_part[(size_t)(T.ekin_blk0 + b) * 4 + c];
-        double Tfsu = e[1], Tfsv = e[3];
-        double Tfree = Tfsv + Tfsu, Temp = e[0] + e[2];
+        for (int c = 0; c < 4; ++c) {
+            double p = 0;
+            for (int b = lane; b < T.ekin_nblk; b += 32) p += S.ekin_part[(size_t)(T.ekin_blk0 + b) * 4 + c];
+            p = warp_sum_d(p);
+            if (lane == 0) e4[c] = p;
+        }
+    }
+    __syncwarp();
+    if (lane != 0) return;
+    if (do_temp) {
+        double Tfsu = e4[1], Tfsv = e4[3];
+        double Tfree = Tfsv + Tfsu, Temp = e4[0] + e4[2];
         TS.Ekin = Temp;
         Temp = 2.0 * Temp / BOLTZ / (double)T.Ndegf;
         Tfree = 2.0 * Tfree / BOLTZ / (double)T.Ndegfree;
@@ -146,9 +264,6 @@ __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_ba
         TS.Temp = Temp; TS.Tfree = Tfree; TS.Tscale_solute = tu; TS.Tscale_solvent = ts;
         if (Temp != Temp) atomicOr(S.status, ST_NAN);
     }
-    unsigned long long *ea = S.eacc + (size_t)tr * QG_NE;
-    double v[QG_NE];
-    for (int s = 0; s < QG_NE; ++s) { v[s] = fx_get(ea[s]); ea[s] = 0ull; }
     if (!rec) return;
     const int step = *rec_base + k;
     if (ene_every <= 0 || step % ene_every != 0) return;
@@ -217,9 +332,9 @@ void launch_shake(const DevSys &S, const BlockTables &B, LaunchCtx &L, int traj_
     prof_end(L);
     (*L.nlaunch)++;
 }
-void launch_post(const DevSys &S, const BlockTables &B, LaunchCtx &L, int shake_on) {
-    prof_begin(L, "k_post");
-    k_post<<<B.naall / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.aall, shake_on);
+void launch_update(const DevSys &S, const BlockTables &B, LaunchCtx &L, int mode) {
+    prof_begin(L, "k_update");
+    k_update<<<B.nuitem / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.uitem, mode);
     prof_end(L);
     (*L.nlaunch)++;
 }

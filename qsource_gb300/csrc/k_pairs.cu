@@ -79,19 +79,25 @@ struct EAcc<true> {
 // --------------------------------------------------------------- waters
 // nonbond_ww_spc (src/md.f90:15021-15119), the water side of nonbond_pw
 // (13282-13365) and lrf_taylor for the three water atoms.
+// QG_LW lanes share one water: lane l takes neighbours l, l+QG_LW, ...; the
+// lanes' partial gradients are summed by an xor butterfly (fixed order).
 template <bool EACC>
 __global__ void __launch_bounds__(QG_BLOCK) k_nb_water(DevSys S, const int *wgrp, int lrf) {
     __shared__ double red[QG_BLOCK / 32];
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / QG_LW;
+    const int lane = threadIdx.x & (QG_LW - 1);
     const int w = wgrp[idx];
     const int traj = traj_of_entry(S, w, true);
     const TrajInfo &T = S.traj[traj];
     EAcc<EACC> eww_el, eww_vdw, epw_el, epw_vdw;
     eww_el.zero(); eww_vdw.zero(); epw_el.zero(); epw_vdw.zero();
     float elrf = 0.f;
-    if (w >= 0 && !S.g_excl[w]) {
-        const int a0 = S.g_atoms[S.g_start[w]];
-        float4 ah[3], al[3];
+    const bool valid = w >= 0 && !S.g_excl[w];
+    int a0 = 0;
+    float4 ah[3] = {}, al[3] = {};
+    float gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0}, gz[3] = {0, 0, 0};
+    if (valid) {
+        a0 = S.g_atoms[S.g_start[w]];
         int ta[3];
         double qd[3] = {0, 0, 0};
 #pragma unroll
@@ -99,89 +105,118 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_water(DevSys S, const int *wgrp
             ah[a] = S.pos[a0 + a]; al[a] = S.poslo[a0 + a]; ta[a] = S.atype[a0 + a];
             if (EACC) qd[a] = S.crg_d[a0 + a];
         }
-        float gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0}, gz[3] = {0, 0, 0};
-        const int n = S.nb_count[w];
+        const int n = S.nb_count[w], nw = S.nb_nw[w];
         const int *lst = S.nb_list + (size_t)w * S.nb_cap;
         const float wwA = T.ww_A, wwB = T.ww_B;
-        for (int k = 0; k < n; ++k) {
-            const int g = lst[k];
-            const int b0 = S.g_atoms[S.g_start[g]];
-            if (S.g_kind[g]) {
-                float4 bh[3], bl[3];
+        // water neighbours: 3x3 SPC pairs, LJ on O-O only (nonbond_ww_spc)
+        auto ww = [&](int b0, const float4 *bh, const float4 *bl) {
 #pragma unroll
-                for (int b = 0; b < 3; ++b) { bh[b] = S.pos[b0 + b]; bl[b] = S.poslo[b0 + b]; }
+            for (int a = 0; a < 3; ++a) {
+#pragma unroll
+                for (int b = 0; b < 3; ++b) {
+                    const float3 d = dpos(ah[a], al[a], bh[b], bl[b]);
+                    const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+                    const float ri = rsqrtf(r2), ri2 = ri * ri;
+                    const float Vel = ah[a].w * bh[b].w * ri;
+                    float dv = -Vel * ri2;
+                    double rid = 0.0;
+                    if (EACC) rid = rinv_d(S.x, a0 + a, b0 + b);
+                    if (a == 0 && b == 0) {
+                        const float r6 = ri2 * ri2 * ri2;
+                        const float Va = wwA * r6 * r6, Vb = wwB * r6;
+                        dv += ri2 * (-12.f * Va + 6.f * Vb);
+                        double ed = 0.0;
+                        if (EACC) {
+                            const double r6d = rid * rid * rid * rid * rid * rid;
+                            ed = T.ww_Ad * r6d * r6d - T.ww_Bd * r6d;
+                        }
+                        eww_vdw.term(Va - Vb, ed);
+                    }
+                    eww_el.term(Vel, EACC ? qd[a] * S.crg_d[b0 + b] * rid : 0.0);
+                    gx[a] -= dv * d.x; gy[a] -= dv * d.y; gz[a] -= dv * d.z;
+                }
+            }
+            eww_el.flush(); eww_vdw.flush();
+        };
+        // two neighbours per iteration keep two sets of loads in flight
+        int k = lane;
+        for (; k + QG_LW < nw; k += 2 * QG_LW) {
+            const int b0 = lst[k], b1 = lst[k + QG_LW];
+            float4 bh0[3], bl0[3], bh1[3], bl1[3];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                bh0[b] = S.pos[b0 + b]; bl0[b] = S.poslo[b0 + b];
+                bh1[b] = S.pos[b1 + b]; bl1[b] = S.poslo[b1 + b];
+            }
+            ww(b0, bh0, bl0);
+            ww(b1, bh1, bl1);
+        }
+        if (k < nw) {
+            const int b0 = lst[k];
+            float4 bh0[3], bl0[3];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) { bh0[b] = S.pos[b0 + b]; bl0[b] = S.poslo[b0 + b]; }
+            ww(b0, bh0, bl0);
+        }
+        // solute neighbours (the water side of nonbond_pw)
+        for (int kk = nw + lane; kk < n; kk += QG_LW) {
+            const int g = lst[kk];
+            for (int q = S.g_start[g]; q < S.g_start[g + 1]; ++q) {
+                const int b = S.g_atoms[q];
+                if (S.aq[b] >= 0) continue;
+                const float4 bh = S.pos[b], bl = S.poslo[b];
+                const int tb = S.atype[b];
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
-#pragma unroll
-                    for (int b = 0; b < 3; ++b) {
-                        const float3 d = dpos(ah[a], al[a], bh[b], bl[b]);
-                        const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
-                        const float ri = rsqrtf(r2), ri2 = ri * ri;
-                        const float Vel = ah[a].w * bh[b].w * ri;
-                        float dv = -Vel * ri2;
-                        double rid = 0.0;
-                        if (EACC) rid = rinv_d(S.x, a0 + a, b0 + b);
-                        if (a == 0 && b == 0) {
-                            const float r6 = ri2 * ri2 * ri2;
-                            const float Va = wwA * r6 * r6, Vb = wwB * r6;
-                            dv += ri2 * (-12.f * Va + 6.f * Vb);
-                            double ed = 0.0;
-                            if (EACC) {
-                                const double r6d = rid * rid * rid * rid * rid * rid;
-                                ed = T.ww_Ad * r6d * r6d - T.ww_Bd * r6d;
-                            }
-                            eww_vdw.term(Va - Vb, ed);
-                        }
-                        eww_el.term(Vel, EACC ? qd[a] * S.crg_d[b0 + b] * rid : 0.0);
-                        gx[a] -= dv * d.x; gy[a] -= dv * d.y; gz[a] -= dv * d.z;
+                    const int c = ljc(S, T, ta[a], tb);
+                    const float A = S.avdw[ta[a] * 3 + c - 1] * S.avdw[tb * 3 + c - 1];
+                    const float B = S.bvdw[ta[a] * 3 + c - 1] * S.bvdw[tb * 3 + c - 1];
+                    const float3 d = dpos(ah[a], al[a], bh, bl);
+                    const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+                    const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
+                    const float Vel = ah[a].w * bh.w * ri, Va = A * r6 * r6, Vb = B * r6;
+                    const float dv = ri2 * (-Vel - 12.f * Va + 6.f * Vb);
+                    double eld = 0.0, evd = 0.0;
+                    if (EACC) {
+                        const double rid = rinv_d(S.x, a0 + a, b), r6d = rid * rid * rid * rid * rid * rid;
+                        eld = qd[a] * S.crg_d[b] * rid;
+                        evd = S.avdw_d[ta[a] * 3 + c - 1] * S.avdw_d[tb * 3 + c - 1] * r6d * r6d -
+                              S.bvdw_d[ta[a] * 3 + c - 1] * S.bvdw_d[tb * 3 + c - 1] * r6d;
                     }
+                    epw_el.term(Vel, eld); epw_vdw.term(Va - Vb, evd);
+                    gx[a] -= dv * d.x; gy[a] -= dv * d.y; gz[a] -= dv * d.z;
                 }
-                eww_el.flush(); eww_vdw.flush();
-            } else {
-                for (int kk = S.g_start[g]; kk < S.g_start[g + 1]; ++kk) {
-                    const int b = S.g_atoms[kk];
-                    if (S.aq[b] >= 0) continue;
-                    const float4 bh = S.pos[b], bl = S.poslo[b];
-                    const int tb = S.atype[b];
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        const int c = ljc(S, T, ta[a], tb);
-                        const float A = S.avdw[ta[a] * 3 + c - 1] * S.avdw[tb * 3 + c - 1];
-                        const float B = S.bvdw[ta[a] * 3 + c - 1] * S.bvdw[tb * 3 + c - 1];
-                        const float3 d = dpos(ah[a], al[a], bh, bl);
-                        const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
-                        const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
-                        const float Vel = ah[a].w * bh.w * ri, Va = A * r6 * r6, Vb = B * r6;
-                        const float dv = ri2 * (-Vel - 12.f * Va + 6.f * Vb);
-                        double eld = 0.0, evd = 0.0;
-                        if (EACC) {
-                            const double rid = rinv_d(S.x, a0 + a, b), r6d = rid * rid * rid * rid * rid * rid;
-                            eld = qd[a] * S.crg_d[b] * rid;
-                            evd = S.avdw_d[ta[a] * 3 + c - 1] * S.avdw_d[tb * 3 + c - 1] * r6d * r6d -
-                                  S.bvdw_d[ta[a] * 3 + c - 1] * S.bvdw_d[tb * 3 + c - 1] * r6d;
-                        }
-                        epw_el.term(Vel, eld); epw_vdw.term(Va - Vb, evd);
-                        gx[a] -= dv * d.x; gy[a] -= dv * d.y; gz[a] -= dv * d.z;
-                    }
-                }
-                epw_el.flush(); epw_vdw.flush();
             }
+            epw_el.flush(); epw_vdw.flush();
         }
-        if (lrf) {
-            const float *ph = S.g_phif + (size_t)w * QG_NPHI;
-            const float cx = (float)(S.g_cent[3 * w] - T.origin[0]);
-            const float cy = (float)(S.g_cent[3 * w + 1] - T.origin[1]);
-            const float cz = (float)(S.g_cent[3 * w + 2] - T.origin[2]);
+    }
+    // every lane of the warp takes part in the butterfly (invalid lanes add 0)
 #pragma unroll
-            for (int a = 0; a < 3; ++a)
-                elrf += lrf_atom(ph, (cx - ah[a].x) - al[a].x, (cy - ah[a].y) - al[a].y, (cz - ah[a].z) - al[a].z,
-                                 ah[a].w, gx[a], gy[a], gz[a]);
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int o = QG_LW / 2; o > 0; o >>= 1) {
+            gx[a] += __shfl_xor_sync(S_GROUP_MASK, gx[a], o, QG_LW);
+            gy[a] += __shfl_xor_sync(S_GROUP_MASK, gy[a], o, QG_LW);
+            gz[a] += __shfl_xor_sync(S_GROUP_MASK, gz[a], o, QG_LW);
         }
+    {
+        if (valid && lane == 0) {
+            if (lrf) {
+                const float *ph = S.g_phif + (size_t)w * QG_NPHI;
+                const float cx = (float)(S.g_cent[3 * w] - T.origin[0]);
+                const float cy = (float)(S.g_cent[3 * w + 1] - T.origin[1]);
+                const float cz = (float)(S.g_cent[3 * w + 2] - T.origin[2]);
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            fx_add(S.fx + 3 * (a0 + a), gx[a], S.status);
-            fx_add(S.fx + 3 * (a0 + a) + 1, gy[a], S.status);
-            fx_add(S.fx + 3 * (a0 + a) + 2, gz[a], S.status);
+                for (int a = 0; a < 3; ++a)
+                    elrf += lrf_atom(ph, (cx - ah[a].x) - al[a].x, (cy - ah[a].y) - al[a].y,
+                                     (cz - ah[a].z) - al[a].z, ah[a].w, gx[a], gy[a], gz[a]);
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                fx_add(S.fx + 3 * (a0 + a), gx[a], S.status);
+                fx_add(S.fx + 3 * (a0 + a) + 1, gy[a], S.status);
+                fx_add(S.fx + 3 * (a0 + a) + 2, gz[a], S.status);
+            }
         }
     }
     block_energy(S, traj, EA_WW_EL, 0.5 * eww_el.value(), red);
@@ -214,19 +249,23 @@ __device__ __forceinline__ PairFlags pair_flags(const DevSys &S, int i, int j) {
 template <bool EACC>
 __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *satom, int lrf) {
     __shared__ double red[QG_BLOCK / 32];
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / QG_LW;
+    const int lane = threadIdx.x & (QG_LW - 1);
     const int i = satom[idx];
     const int traj = traj_of_entry(S, i, false);
     const TrajInfo &T = S.traj[traj];
     EAcc<EACC> epp_el, epp_vdw, epw_el, epw_vdw;
     epp_el.zero(); epp_vdw.zero(); epw_el.zero(); epw_vdw.zero();
     float elrf = 0.f;
-    if (i >= 0 && S.aq[i] < 0 && !S.g_excl[S.agrp[i]]) {
-        const int g = S.agrp[i];
-        const float4 ih = S.pos[i], il = S.poslo[i];
+    const bool valid = i >= 0 && S.aq[i] < 0 && !S.g_excl[S.agrp[i]];
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    int g = 0;
+    float4 ih = {}, il = {};
+    if (valid) {
+        g = S.agrp[i];
+        ih = S.pos[i]; il = S.poslo[i];
         const int ti = S.atype[i];
         const double qi = EACC ? S.crg_d[i] : 0.0;
-        float gx = 0.f, gy = 0.f, gz = 0.f;
         const float el14 = T.el14;
         // one pair term: LJ code c, el14 factor for 1-4 pairs (nonbond_pp :13102-13111)
         auto pair = [&](int j, int c, EAcc<EACC> &e_el, EAcc<EACC> &e_vdw) {
@@ -258,40 +297,49 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
             if (f.excl) return;
             pair(j, f.p14 ? 3 : ljc(S, T, ti, S.atype[j]), epp_el, epp_vdw);
         };
-        for (int kk = S.g_start[g]; kk < S.g_start[g + 1]; ++kk) {
+        for (int kk = S.g_start[g] + lane; kk < S.g_start[g + 1]; kk += QG_LW) {
             const int j = S.g_atoms[kk];
             if (j == i || S.aq[j] >= 0) continue;
             pp(j);
         }
         epp_el.flush(); epp_vdw.flush();
-        const int n = S.nb_count[g];
+        const int n = S.nb_count[g], nw = S.nb_nw[g];
         const int *lst = S.nb_list + (size_t)g * S.nb_cap;
-        for (int k = 0; k < n; ++k) {
-            const int h = lst[k];
-            if (S.g_kind[h]) {
-                const int b0 = S.g_atoms[S.g_start[h]];
+        for (int k = lane; k < nw; k += QG_LW) {
+            const int b0 = lst[k];
 #pragma unroll
-                for (int b = 0; b < 3; ++b) pair(b0 + b, ljc(S, T, ti, S.atype[b0 + b]), epw_el, epw_vdw);
-                epw_el.flush(); epw_vdw.flush();
-            } else {
-                for (int kk = S.g_start[h]; kk < S.g_start[h + 1]; ++kk) {
-                    const int j = S.g_atoms[kk];
-                    if (S.aq[j] >= 0) continue;
-                    pp(j);
-                }
-                epp_el.flush(); epp_vdw.flush();
+            for (int b = 0; b < 3; ++b) pair(b0 + b, ljc(S, T, ti, S.atype[b0 + b]), epw_el, epw_vdw);
+            epw_el.flush(); epw_vdw.flush();
+        }
+        for (int k = nw + lane; k < n; k += QG_LW) {
+            const int h = lst[k];
+            for (int kk = S.g_start[h]; kk < S.g_start[h + 1]; ++kk) {
+                const int j = S.g_atoms[kk];
+                if (S.aq[j] >= 0) continue;
+                pp(j);
             }
+            epp_el.flush(); epp_vdw.flush();
         }
-        if (lrf) {
-            const float *ph = S.g_phif + (size_t)g * QG_NPHI;
-            const float cx = (float)(S.g_cent[3 * g] - T.origin[0]);
-            const float cy = (float)(S.g_cent[3 * g + 1] - T.origin[1]);
-            const float cz = (float)(S.g_cent[3 * g + 2] - T.origin[2]);
-            elrf = lrf_atom(ph, (cx - ih.x) - il.x, (cy - ih.y) - il.y, (cz - ih.z) - il.z, ih.w, gx, gy, gz);
+    }
+#pragma unroll
+    for (int o = QG_LW / 2; o > 0; o >>= 1) {
+        gx += __shfl_xor_sync(S_GROUP_MASK, gx, o, QG_LW);
+        gy += __shfl_xor_sync(S_GROUP_MASK, gy, o, QG_LW);
+        gz += __shfl_xor_sync(S_GROUP_MASK, gz, o, QG_LW);
+    }
+    {
+        if (valid && lane == 0) {
+            if (lrf) {
+                const float *ph = S.g_phif + (size_t)g * QG_NPHI;
+                const float cx = (float)(S.g_cent[3 * g] - T.origin[0]);
+                const float cy = (float)(S.g_cent[3 * g + 1] - T.origin[1]);
+                const float cz = (float)(S.g_cent[3 * g + 2] - T.origin[2]);
+                elrf = lrf_atom(ph, (cx - ih.x) - il.x, (cy - ih.y) - il.y, (cz - ih.z) - il.z, ih.w, gx, gy, gz);
+            }
+            fx_add(S.fx + 3 * i, gx, S.status);
+            fx_add(S.fx + 3 * i + 1, gy, S.status);
+            fx_add(S.fx + 3 * i + 2, gz, S.status);
         }
-        fx_add(S.fx + 3 * i, gx, S.status);
-        fx_add(S.fx + 3 * i + 1, gy, S.status);
-        fx_add(S.fx + 3 * i + 2, gz, S.status);
     }
     block_energy(S, traj, EA_PP_EL, 0.5 * epp_el.value(), red);
     block_energy(S, traj, EA_PP_VDW, 0.5 * epp_vdw.value(), red);
@@ -538,14 +586,14 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
 
 void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
     if (!B.nwgrp) return;
-    if (fp64_energy) { prof_begin(L, "k_nb_water"); k_nb_water<true><<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf); prof_end(L); }
-    else { prof_begin(L, "k_nb_water"); k_nb_water<false><<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf); prof_end(L); }
+    if (fp64_energy) { prof_begin(L, "k_nb_water"); k_nb_water<true><<<B.nwgrp * QG_LW / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf); prof_end(L); }
+    else { prof_begin(L, "k_nb_water"); k_nb_water<false><<<B.nwgrp * QG_LW / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf); prof_end(L); }
     (*L.nlaunch)++;
 }
 void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
     if (!B.nsatom) return;
-    if (fp64_energy) { prof_begin(L, "k_nb_solute"); k_nb_solute<true><<<B.nsatom / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); prof_end(L); }
-    else { prof_begin(L, "k_nb_solute"); k_nb_solute<false><<<B.nsatom / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); prof_end(L); }
+    if (fp64_energy) { prof_begin(L, "k_nb_solute"); k_nb_solute<true><<<B.nsatom * QG_LW / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); prof_end(L); }
+    else { prof_begin(L, "k_nb_solute"); k_nb_solute<false><<<B.nsatom * QG_LW / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); prof_end(L); }
     (*L.nlaunch)++;
 }
 void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {

@@ -28,9 +28,8 @@ __device__ __forceinline__ void grad_add(const DevSys &S, int a, double gx, doub
 }
 
 // nonbond_qq, src/md.f90:13491-13636.  One block per (trajectory, state).
-__global__ void k_qq(DevSys S, const int *blk_traj, const int *blk_s) {
-    __shared__ double red[QG_BLOCK / 32];
-    const int traj = blk_traj[blockIdx.x], s = blk_s[blockIdx.x];
+__device__ void qq_block(const DevSys &S, int b, const int *blk_traj, const int *blk_s, double *red) {
+    const int traj = blk_traj[b], s = blk_s[b];
     const TrajInfo &T = S.traj[traj];
     const double lam = T.lambda[s];
     const int ntq = T.natyps + T.nqat;
@@ -169,8 +168,8 @@ __device__ __forceinline__ void apply_dp(const DevSys &S, const int *at, double 
 
 // qbond/qangle/qtorsion/qimproper (src/md.f90:17022-17538) without EVB
 // angle/torsion couplings.  One thread per (term, state).
-__global__ void k_qbonded(DevSys S) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ void qbonded_block(const DevSys &S, int b) {
+    const int id = b * blockDim.x + threadIdx.x;
     const int term = id / QG_MAXS, s = id % QG_MAXS;
     if (term >= S.nqt) return;
     const int traj = S.qt_traj[term];
@@ -225,10 +224,9 @@ __global__ void k_qbonded(DevSys S) {
 // bond/angle/torsion/improper(2), src/md.f90:1130-1405, 3130-3423,
 // 17907-18054.  Terms are grouped per (trajectory, energy slot) and padded to
 // whole blocks, so each block reduces into one slot.
-__global__ void __launch_bounds__(QG_BLOCK) k_bonded(DevSys S) {
-    __shared__ double red[QG_BLOCK / 32];
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    const int traj = S.bt_blk_traj[blockIdx.x], slot = S.bt_blk_slot[blockIdx.x];
+__device__ void bonded_block(const DevSys &S, int b, double *red) {
+    const int id = b * blockDim.x + threadIdx.x;
+    const int traj = S.bt_blk_traj[b], slot = S.bt_blk_slot[b];
     const int c = S.bt_cod[id];
     double e = 0;
     const double pi = 3.14159265358979323846;
@@ -276,9 +274,8 @@ __global__ void __launch_bounds__(QG_BLOCK) k_bonded(DevSys S) {
 }
 
 // fix_shell, src/md.f90:2816-2864 (no freeze).  One thread per solute atom.
-__global__ void __launch_bounds__(QG_BLOCK) k_fix_shell(DevSys S, const int *satom) {
-    __shared__ double red[QG_BLOCK / 32];
-    const int i = satom[blockIdx.x * blockDim.x + threadIdx.x];
+__device__ void fix_shell_block(const DevSys &S, int b, const int *satom, double *red) {
+    const int i = satom[b * blockDim.x + threadIdx.x];
     const int traj = i < 0 ? -1 - i : S.atraj[i];
     const TrajInfo &T = S.traj[traj];
     double efix = 0, eshell = 0;
@@ -295,9 +292,8 @@ __global__ void __launch_bounds__(QG_BLOCK) k_fix_shell(DevSys S, const int *sat
 }
 
 // restrain_solvent, src/md.f90:18055-18102.  One thread per water.
-__global__ void __launch_bounds__(QG_BLOCK) k_restrain_solvent(DevSys S, const int *wgrp) {
-    __shared__ double red[QG_BLOCK / 32];
-    const int w = wgrp[blockIdx.x * blockDim.x + threadIdx.x];
+__device__ void restrain_solvent_block(const DevSys &S, int b, const int *wgrp, double *red) {
+    const int w = wgrp[b * blockDim.x + threadIdx.x];
     const int traj = w < 0 ? -1 - w : S.g_traj[w];
     const TrajInfo &T = S.traj[traj];
     double erst = 0;
@@ -325,8 +321,8 @@ __global__ void __launch_bounds__(QG_BLOCK) k_restrain_solvent(DevSys S, const i
 }
 
 // offdiag, src/md.f90:15444-15470: Hij = A exp(-mu r_kl).
-__global__ void k_offdiag(DevSys S) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ void offdiag_block(const DevSys &S, int blk) {
+    const int k = blk * blockDim.x + threadIdx.x;
     if (k >= S.nod) return;
     const int traj = S.od_traj[k];
     const int a = S.q_atom[S.od_kl[2 * k]], b = S.q_atom[S.od_kl[2 * k + 1]];
@@ -338,47 +334,42 @@ __global__ void k_offdiag(DevSys S) {
     o[1] = r;
 }
 
+// The small terms share one launch: consecutive block ranges select the term.
+struct MiscPlan {
+    int nqq, nbt, nfix, nrad, nqb, nod;    // blocks per term
+};
+
+__global__ void __launch_bounds__(QG_BLOCK) k_misc(DevSys S, MiscPlan P, const int *qq_traj, const int *qq_s,
+                                                   const int *satom, const int *wgrp) {
+    __shared__ double red[QG_BLOCK / 32];
+    int b = blockIdx.x;
+    if (b < P.nqq) { qq_block(S, b, qq_traj, qq_s, red); return; }
+    b -= P.nqq;
+    if (b < P.nbt) { bonded_block(S, b, red); return; }
+    b -= P.nbt;
+    if (b < P.nfix) { fix_shell_block(S, b, satom, red); return; }
+    b -= P.nfix;
+    if (b < P.nrad) { restrain_solvent_block(S, b, wgrp, red); return; }
+    b -= P.nrad;
+    if (b < P.nqb) { qbonded_block(S, b); return; }
+    b -= P.nqb;
+    if (b < P.nod) { offdiag_block(S, b); return; }
+}
+
 static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
-void launch_qq(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
-    if (!B.nqqblk) return;
-    prof_begin(L, "k_qq");
-    k_qq<<<B.nqqblk, QG_BLOCK, 0, L.stream>>>(S, B.qqblk_traj, B.qqblk_s);
-    prof_end(L);
-    (*L.nlaunch)++;
-}
-void launch_qbonded(const DevSys &S, const BlockTables &B, LaunchCtx &L, int nqterm_total) {
-    if (!S.nqt) return;
-    prof_begin(L, "k_qbonded");
-    k_qbonded<<<nblk(S.nqt * QG_MAXS, 128), 128, 0, L.stream>>>(S);
-    prof_end(L);
-    (*L.nlaunch)++;
-}
-void launch_bonded(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
-    if (!S.nbt) return;
-    prof_begin(L, "k_bonded");
-    k_bonded<<<S.nbt / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S);
-    prof_end(L);
-    (*L.nlaunch)++;
-}
-void launch_fix_shell(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
-    if (!B.nsatom) return;
-    prof_begin(L, "k_fix_shell");
-    k_fix_shell<<<B.nsatom / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom);
-    prof_end(L);
-    (*L.nlaunch)++;
-}
-void launch_restrain_solvent(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
-    if (!B.nwgrp) return;
-    prof_begin(L, "k_restrain_solvent");
-    k_restrain_solvent<<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp);
-    prof_end(L);
-    (*L.nlaunch)++;
-}
-void launch_offdiag(const DevSys &S, LaunchCtx &L) {
-    if (!S.nod) return;
-    prof_begin(L, "k_offdiag");
-    k_offdiag<<<nblk(S.nod, 64), 64, 0, L.stream>>>(S);
+void launch_misc(const DevSys &S, const BlockTables &B, LaunchCtx &L, int terms) {
+    MiscPlan P{};
+    P.nqq = (terms & QGPU_TERMS_QQ) ? B.nqqblk : 0;
+    P.nbt = (terms & QGPU_TERMS_BONDED) ? S.nbt / QG_BLOCK : 0;
+    P.nfix = (terms & QGPU_TERMS_RESTRAINT) ? B.nsatom / QG_BLOCK : 0;
+    P.nrad = (terms & QGPU_TERMS_RESTRAINT) ? B.nwgrp / QG_BLOCK : 0;
+    P.nqb = (terms & QGPU_TERMS_QBONDED) ? nblk(S.nqt * QG_MAXS, QG_BLOCK) : 0;
+    P.nod = nblk(S.nod, QG_BLOCK);
+    const int nb = P.nqq + P.nbt + P.nfix + P.nrad + P.nqb + P.nod;
+    if (!nb) return;
+    prof_begin(L, "k_misc");
+    k_misc<<<nb, QG_BLOCK, 0, L.stream>>>(S, P, B.qqblk_traj, B.qqblk_s, B.satom, B.wgrp);
     prof_end(L);
     (*L.nlaunch)++;
 }

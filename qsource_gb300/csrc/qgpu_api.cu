@@ -71,6 +71,8 @@ struct qgpu_handle {
     long long nlaunch = 0;
     int NBcycle = 10;
     int lists_built = 0, temp_init = 0, any_shake = 0, any_wpol = 0;
+    std::vector<char> fused;   // per trajectory: SHAKE fused into the update kernel
+    bool all_fused = true;
     long long step = 0;
     cudaGraphExec_t graph = nullptr;
     long long graph_nodes = 0;
@@ -166,7 +168,8 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     std::vector<double> shk_d2;
     std::vector<int> od_traj, od_ij, od_kl;
     std::vector<double> od_Amu;
-    std::vector<int> wgrp, satom, scan_t0, scan_tn, scan_traj, aall, qqblk_traj, qqblk_s;
+    std::vector<int> wgrp, satom, scan_t0, scan_tn, scan_traj, scan_chunk, uitem, qqblk_traj, qqblk_s;
+    long long scr_slots = 0;
     int type0 = 0, lj0 = 0, q0 = 0, qlib0 = 0, sc0 = 0, grp0 = 0, atom0 = 0, tile0 = 0;
 
     for (int t = 0; t < ntraj; ++t) {
@@ -196,7 +199,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         T.rwat = d.rwat; T.fk_wsphere = d.fk_wsphere; T.Dwmz = d.Dwmz; T.awmz = d.awmz;
         T.fk_pshell = d.fk_pshell; T.fk_fix = d.fk_fix;
         for (int s = 0; s < QG_MAXS; ++s) T.lambda[s] = s < S ? d.lambda[s] : 0.0;
-        T.dt = d.dt; T.Temp0 = d.Temp0; T.tau_T = d.tau_T;
+        T.dt = d.dt; T.Temp0 = d.Temp0; T.tau_T = d.tau_T; T.inv_dt = 1.0 / d.dt;
         T.separate_scaling = d.separate_scaling; T.detail_temps = d.detail_temps;
         T.Ndegf = d.Ndegf; T.Ndegfree = d.Ndegfree;
         T.Ndegfree_solute = d.Ndegfree_solute; T.Ndegfree_solvent = d.Ndegfree_solvent;
@@ -281,9 +284,14 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         }
         if (tng) { tile_g0.push_back(tg0); tile_g1.push_back(grp0 + d.ncgp); tile0++; }
         T.ntile = tile0 - T.tile0;
-        for (int b = 0; b < d.ncgp; b += QG_BLOCK) {
-            scan_t0.push_back(grp0 + b); scan_tn.push_back(std::min(QG_BLOCK, d.ncgp - b)); scan_traj.push_back(t);
-        }
+        T.nchunk = (T.ntile + QG_TPC - 1) / QG_TPC;
+        T.scr0 = scr_slots;
+        scr_slots += (long long)T.nchunk * d.ncgp;
+        for (int b = 0; b < d.ncgp; b += QG_BLOCK)
+            for (int c = 0; c < T.nchunk; ++c) {
+                scan_t0.push_back(grp0 + b); scan_tn.push_back(std::min(QG_BLOCK, d.ncgp - b));
+                scan_traj.push_back(t); scan_chunk.push_back(c);
+            }
         // --- work lists
         size_t s0 = wgrp.size();
         for (int g = d.ncgp_solute; g < d.ncgp; ++g) wgrp.push_back(grp0 + g);
@@ -291,11 +299,45 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         s0 = satom.size();
         for (int i = 0; i < d.nat_solute; ++i) satom.push_back(atom0 + i);
         pad(satom, s0, t);
-        s0 = aall.size();
-        T.ekin_blk0 = (int)(aall.size() / QG_BLOCK);
-        for (int i = 0; i < N; ++i) aall.push_back(atom0 + i);
-        pad(aall, s0, t);
-        T.ekin_nblk = (int)((aall.size() - s0) / QG_BLOCK);
+        // update items: 3-atom molecules whose constraints stay inside (O,H,H)
+        // are updated and shaken by one thread; every other atom on its own
+        {
+            bool fuse = true;
+            for (int m = 0; m < d.shake_molecules && fuse; ++m) {
+                int c0 = d.shake_first[m], c1 = d.shake_first[m + 1];
+                int lo = d.natom, hi = -1;
+                for (int c = c0; c < c1; ++c) {
+                    lo = std::min(lo, std::min(d.shake_i[c], d.shake_j[c]));
+                    hi = std::max(hi, std::max(d.shake_i[c], d.shake_j[c]));
+                }
+                // fused only for the water pattern O-H1, O-H2, H1-H2 in this order
+                if (c1 - c0 != 3 || hi - lo != 2 ||
+                    d.shake_i[c0] != lo || d.shake_j[c0] != lo + 1 ||
+                    d.shake_i[c0 + 1] != lo || d.shake_j[c0 + 1] != lo + 2 ||
+                    d.shake_i[c0 + 2] != lo + 1 || d.shake_j[c0 + 2] != lo + 2)
+                    fuse = false;
+            }
+            std::vector<int> owner(N, -1);
+            if (fuse)
+                for (int m = 0; m < d.shake_molecules; ++m) {
+                    int lo = d.shake_i[d.shake_first[m]];
+                    for (int k = 0; k < 3 && lo + k < N; ++k) {
+                        if (owner[lo + k] >= 0) fuse = false;
+                        owner[lo + k] = m;
+                    }
+                }
+            h->fused.push_back(fuse);
+            s0 = uitem.size();
+            T.ekin_blk0 = (int)(uitem.size() / QG_BLOCK);
+            int shk_base = (int)(shk_first.size() - 1);
+            for (int i = 0; i < N; ++i) {
+                if (fuse && owner[i] >= 0) {
+                    if (d.shake_i[d.shake_first[owner[i]]] == i) uitem.push_back((1 << 30) | (shk_base + owner[i]));
+                } else uitem.push_back(atom0 + i);
+            }
+            pad(uitem, s0, t);
+            T.ekin_nblk = (int)((uitem.size() - s0) / QG_BLOCK);
+        }
         // --- Q atoms
         int nql = d.nqlib;
         for (int k = 0; k < nql; ++k)
@@ -485,6 +527,10 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     if ((rc = alloc0(A, (size_t)QG_NLRF * grp0, &S.g_phi))) return rc;
     if ((rc = alloc0(A, (size_t)QG_NPHI * grp0, &S.g_phif))) return rc;
     if ((rc = alloc0(A, (size_t)grp0, &S.nb_count))) return rc;
+    if ((rc = alloc0(A, (size_t)grp0, &S.nb_nw))) return rc;
+    if ((rc = alloc0(A, (size_t)scr_slots * QG_NLRF, &S.scr_phi))) return rc;
+    if ((rc = alloc0(A, (size_t)scr_slots, &S.scr_cnt))) return rc;
+    if ((rc = alloc0(A, (size_t)scr_slots * QG_CAPC, &S.scr_nb))) return rc;
     if ((rc = alloc0(A, (size_t)grp0 * S.nb_cap, &S.nb_list))) return rc;
     UP(q_atom, q_atom); UP(qcrg_f, qcrg_f); UP(qcrg_d, qcrg_d); UP(qiac, qiac);
     UP(qavdw, qavdw); UP(qbvdw, qbvdw); UP(qavdw_d, qavdw_d); UP(qbvdw_d, qbvdw_d); UP(sc_f, sc_f); UP(sc_d, sc_d);
@@ -509,7 +555,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     UP(shk_first, shk_first); UP(shk_i, shk_i); UP(shk_j, shk_j); UP(shk_traj, shk_traj); UP(shk_d2, shk_d2);
     S.nshk_mol = (int)shk_traj.size();
     if ((rc = alloc0(A, (size_t)ntraj * QG_NE, &S.eacc))) return rc;
-    if ((rc = alloc0(A, (size_t)4 * (aall.size() / QG_BLOCK + 1), &S.ekin_part))) return rc;
+    if ((rc = alloc0(A, (size_t)4 * (uitem.size() / QG_BLOCK + 1), &S.ekin_part))) return rc;
     if ((rc = alloc0(A, 1, &S.status))) return rc;
     // block tables
     BlockTables &B = h->B;
@@ -520,7 +566,8 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         if ((rc = upload(A, scan_t0, &p))) return rc; B.scan_t0 = p;
         if ((rc = upload(A, scan_tn, &p))) return rc; B.scan_tn = p;
         if ((rc = upload(A, scan_traj, &p))) return rc; B.scan_traj = p; B.nscan = (int)scan_t0.size();
-        if ((rc = upload(A, aall, &p))) return rc; B.aall = p; B.naall = (int)aall.size();
+        if ((rc = upload(A, scan_chunk, &p))) return rc; B.scan_chunk = p;
+        if ((rc = upload(A, uitem, &p))) return rc; B.uitem = p; B.nuitem = (int)uitem.size();
         if ((rc = upload(A, qqblk_traj, &p))) return rc; B.qqblk_traj = p;
         if ((rc = upload(A, qqblk_s, &p))) return rc; B.qqblk_s = p; B.nqqblk = (int)qqblk_traj.size();
     }
@@ -528,6 +575,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     if ((rc = alloc0(A, 2, &h->zero_d))) return rc;
     if ((rc = alloc0(A, (size_t)3 * h->max_natom, &h->grad_d))) return rc;
     if ((rc = alloc0(A, 2, &h->recctl_d))) return rc;
+    for (char f : h->fused) h->all_fused = h->all_fused && f;
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     // float mirror of the starting coordinates
     LaunchCtx L{h->stream, &h->nlaunch};
@@ -567,14 +615,7 @@ static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, bool fp64_energy,
         launch_qw(h->S, h->B, L, esel);
         launch_qp(h->S, h->B, L, esel);
     }
-    if (terms & QGPU_TERMS_QQ) launch_qq(h->S, h->B, L);
-    if (terms & QGPU_TERMS_QBONDED) launch_qbonded(h->S, h->B, L, h->S.nqt);
-    if (terms & QGPU_TERMS_BONDED) launch_bonded(h->S, h->B, L);
-    if (terms & QGPU_TERMS_RESTRAINT) {
-        launch_fix_shell(h->S, h->B, L);
-        launch_restrain_solvent(h->S, h->B, L);
-    }
-    launch_offdiag(h->S, L);
+    launch_misc(h->S, h->B, L, terms);
 }
 
 static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every);
@@ -607,9 +648,13 @@ static int replay_block(qgpu_handle *h, LaunchCtx &L, int ene_every) {
 static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every) {
     EaccSel esel{EACC_RECORD, h->recctl_d, k, ene_every};
     force_ops(h, L, QGPU_TERMS_ALL, false, esel);
-    launch_integrate(h->S, h->B, L);
-    launch_shake(h->S, h->B, L, -1);
-    launch_post(h->S, h->B, L, h->any_shake);
+    if (h->all_fused) {
+        launch_update(h->S, h->B, L, 1);
+    } else {
+        launch_integrate(h->S, h->B, L);
+        launch_shake(h->S, h->B, L, -1);
+        launch_update(h->S, h->B, L, 2);
+    }
     launch_finalize(h->S, L, 1, h->rec_d, h->recctl_d, k, ene_every, h->rec_cap);
 }
 
@@ -730,13 +775,17 @@ int qgpu_get_temperature(qgpu_handle *h, int32_t traj, double *out4) {
 int qgpu_get_group_pairs(qgpu_handle *h, int32_t traj, int32_t *pairs, int64_t cap, int64_t *npairs) {
     if (!h || traj < 0 || traj >= h->ntraj) return fail(QGPU_E_INVALID, "bad trajectory index");
     int G = h->ncgp[traj], g0 = h->grp0[traj], C = h->S.nb_cap;
-    std::vector<int> cnt(G), lst((size_t)G * C);
+    int N = h->natom[traj], a0 = h->atom0[traj];
+    std::vector<int> cnt(G), nw(G), lst((size_t)G * C), agrp(N);
     CK(cudaMemcpy(cnt.data(), h->S.nb_count + g0, G * sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(nw.data(), h->S.nb_nw + g0, G * sizeof(int), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(lst.data(), h->S.nb_list + (size_t)g0 * C, (size_t)G * C * sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(agrp.data(), h->S.agrp + a0, N * sizeof(int), cudaMemcpyDeviceToHost));
     int64_t n = 0;
     for (int g = 0; g < G; ++g)
         for (int k = 0; k < cnt[g]; ++k) {
-            int o = lst[(size_t)g * C + k] - g0;
+            int e = lst[(size_t)g * C + k];
+            int o = (k < nw[g] ? agrp[e - a0] : e) - g0;   // water entries hold the O atom
             if (o > g) {
                 if (pairs && n < cap) { pairs[2 * n] = g; pairs[2 * n + 1] = o; }
                 n++;
@@ -847,7 +896,7 @@ int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every) {
     if (!h->temp_init) {
         CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
         CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
-        launch_post(h->S, h->B, L, 0);
+        launch_update(h->S, h->B, L, 0);
         launch_finalize(h->S, L, 1, nullptr, h->zero_d, 0, 1, 0);
         h->temp_init = 1;
     }
@@ -895,7 +944,7 @@ int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink si
     CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
     if (!h->temp_init) {
         // temperature() before the first step (md_run, src/md.f90:6395-6398)
-        launch_post(h->S, h->B, L, 0);
+        launch_update(h->S, h->B, L, 0);
         launch_finalize(h->S, L, 1, nullptr, h->zero_d, 0, 1, 0);
         h->temp_init = 1;
     }

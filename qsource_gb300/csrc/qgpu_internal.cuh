@@ -12,10 +12,14 @@
 #include "qgpu.h"
 
 #define QG_BLOCK 128            // threads per block of the per-item kernels
+#define QG_LW 8                 // lanes that share one target in the pair kernels
+#define S_GROUP_MASK 0xffffffffu
 #define QG_MAXS 4               // states handled by the engine (<= QGPU_MAX_STATES)
 #define QG_MAXQ 128             // Q atoms per trajectory (reference max_qat = 100)
 #define QG_TILE_G 64            // source groups per scan tile
 #define QG_TILE_A 256           // source atoms per scan tile
+#define QG_TPC 4                // scan tiles per source chunk (one k_scan block)
+#define QG_CAPC (QG_TPC * QG_TILE_G)  // near groups a chunk can hold (= groups in a chunk)
 #define QG_MAXOD 6              // off-diagonal couplings recorded per trajectory
 #define QG_NLRF 24              // LRF accumulators per group (see k_scan)
 #define QG_NPHI 20              // symmetric LRF Taylor coefficients per group
@@ -53,6 +57,8 @@ struct TrajInfo {
     int qvdw;
     int use_lrf, q_static;      // LRF on; qp/qw lists built once (Rcq > rexcl_o)
     int tile0, ntile;           // scan tiles of this trajectory
+    int nchunk;                 // source chunks of QG_TPC tiles
+    long long scr0;             // first scan-scratch slot (slot = scr0 + chunk*ncgp + local group)
     int ww_lj;                  // ljcod of the water O pair
     float ww_A, ww_B;           // O-O LJ products (aLJ_solv(1,c)^2, bLJ_solv(1,c)^2)
     double ww_Ad, ww_Bd;
@@ -65,7 +71,7 @@ struct TrajInfo {
     double xpcent[3], xwcent[3];
     double rwat, fk_wsphere, Dwmz, awmz, fk_pshell, fk_fix;
     double lambda[QG_MAXS];
-    double dt, Temp0, tau_T;
+    double dt, Temp0, tau_T, inv_dt;
     int separate_scaling, detail_temps;
     int Ndegf, Ndegfree, Ndegfree_solute, Ndegfree_solvent;
     int shake_mol0, nshake_mol;
@@ -111,8 +117,15 @@ struct DevSys {
     double *g_cent;                 // 3*G
     double *g_phi;                  // QG_NLRF*G accumulators
     float *g_phif;                  // QG_NPHI*G Taylor coefficients
-    int *nb_count, *nb_list;
+    // neighbour list of a group: water neighbours first (as their O atom),
+    // then solute neighbours (as group index); nb_nw = number of water entries
+    int *nb_count, *nb_nw, *nb_list;
     const int *tile_g0, *tile_g1;
+    // scan scratch (per slot = (chunk, target group)): FP32 LRF partial sums,
+    // near-group count and near groups of the chunk
+    float *scr_phi;                 // QG_NLRF per slot
+    int *scr_cnt;                   // per slot
+    int *scr_nb;                    // QG_CAPC per slot
     // Q atoms
     const int *q_atom;              // global atom of each global Q index
     const float *qcrg_f;            // [q*QG_MAXS+s]
@@ -215,9 +228,9 @@ struct BlockTables {
     // per-item lists (padded per trajectory to QG_BLOCK)
     const int *wgrp; int nwgrp;        // water groups
     const int *satom; int nsatom;      // solute atoms (all, incl. Q/excluded -> skipped in kernels)
-    const int *scan_t0; const int *scan_tn; const int *scan_traj; int nscan;  // scan blocks
+    const int *scan_t0; const int *scan_tn; const int *scan_traj; const int *scan_chunk; int nscan;  // scan blocks
     const int *gall; int ngall;        // all groups (centres)
-    const int *aall; int naall;        // all atoms, padded (Ekin blocks)
+    const int *uitem; int nuitem;      // update items (atoms, or (1<<30)|shake molecule), padded
     const int *qqblk_traj, *qqblk_s; int nqqblk;
 };
 
@@ -238,17 +251,13 @@ void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lr
 void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy);
 void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
 void launch_qp(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
-void launch_qq(const DevSys &S, const BlockTables &B, LaunchCtx &L);
-void launch_qbonded(const DevSys &S, const BlockTables &B, LaunchCtx &L, int nqterm_total);
-void launch_bonded(const DevSys &S, const BlockTables &B, LaunchCtx &L);
+// nonbond_qq, Q bonded, classical bonded, restraints and off-diagonals in one launch
+void launch_misc(const DevSys &S, const BlockTables &B, LaunchCtx &L, int terms);
 void launch_integrate(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_shake(const DevSys &S, const BlockTables &B, LaunchCtx &L, int traj_filter);
-void launch_post(const DevSys &S, const BlockTables &B, LaunchCtx &L, int shake_on);
+void launch_update(const DevSys &S, const BlockTables &B, LaunchCtx &L, int mode);
 void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *rec, const int *rec_base, int k,
                      int ene_every, int rec_cap);
 void launch_tick(LaunchCtx &L, int *rec_base, int n);
-void launch_offdiag(const DevSys &S, LaunchCtx &L);
-void launch_fix_shell(const DevSys &S, const BlockTables &B, LaunchCtx &L);
-void launch_restrain_solvent(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_mirror(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_grad_to_double(const DevSys &S, LaunchCtx &L, double *out, int atom0, int natom);
