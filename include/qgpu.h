@@ -281,6 +281,35 @@ int qgpu_profile(qgpu_handle *h, int32_t nsteps, char *names, double *ms, int64_
    FP32-bound pair and LRF kernels. */
 int qgpu_fp32_peak(double *tflops);
 
+/* ---- allocation-free scan ----------------------------------------------- */
+/* Has no counterpart in the reference.  For callers that may not allocate
+   device memory -- a host program whose device memory belongs to its own
+   allocator or to a pool reserved once at start-up, or a time-step loop in
+   which a cudaMalloc (which can synchronise the device) is not allowed: the
+   charge-group scan of qgpu_build_lists for ONE system, on arrays the caller
+   already holds on the device, with no engine handle.  It allocates nothing:
+   its chunk partials live in a fixed 8 MiB device array of the library, held
+   by every device that loads it until the process exits.
+     inputs (device): x[3*natom] coordinates; crg[natom] scaled charges, 0 for
+       atoms that must not feed the multipoles (Q atoms); g_start[ngroup+1] and
+       g_atoms[] the members of each charge group (0-based atoms); g_switch
+       [ngroup] the switch atom; g_flags[ngroup] bit 0 = solvent group, bit 1 =
+       excluded group.  origin (host, 3 doubles): the point the float
+       coordinates are taken relative to (the solvent sphere centre).
+     cut-offs: rc_pp, rc_pw, rc_ww (near groups), rc_lrf (multipole range).
+     outputs (device): lrf43[ngroup*43] in the layout of qgpu_get_lrf;
+       near_count[ngroup] the number of groups inside the cut-off.
+   Limit: ngroup <= 65536; larger systems are refused with QGPU_E_INVALID.
+   The first call on each device resolves the array's device address (with
+   that device current); make it before any stream capture.  Work is queued on
+   `stream` (a cudaStream_t, NULL = legacy default stream) and the call returns
+   without waiting.  All calls share the one array: two calls whose work
+   overlaps on the GPU (other streams, other host threads) race on it. */
+int qgpu_lrf_scan_static(int32_t ngroup, const double *x, const double *crg, const int32_t *g_start,
+                         const int32_t *g_atoms, const int32_t *g_switch, const int32_t *g_flags,
+                         const double *origin, double rc_pp, double rc_pw, double rc_ww, double rc_lrf,
+                         double *lrf43, int32_t *near_count, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

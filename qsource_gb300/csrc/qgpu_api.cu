@@ -59,6 +59,17 @@ void pad(std::vector<int> &v, size_t seg_start, int traj) {
 
 }  // namespace
 
+// error reporting for the library's other translation units
+int qgpu_fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
 struct qgpu_handle {
     int ntraj = 0;
     std::vector<TrajInfo> info;

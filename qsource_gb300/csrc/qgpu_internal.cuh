@@ -82,6 +82,9 @@ struct TrajInfo {
     int ff_type;
 };
 
+// Records the message for qgpu_last_error and returns code (qgpu_api.cu).
+int qgpu_fail(int code, const char *fmt, ...);
+
 // Per-trajectory dynamic state (device).
 struct TrajState {
     double Tscale_solute, Tscale_solvent, Temp, Tfree;
