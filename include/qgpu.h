@@ -204,6 +204,10 @@ typedef struct qgpu_qenergy {
 #define QGPU_TERMS_BONDED    0x8   /* pot_energy_bonds                           */
 #define QGPU_TERMS_RESTRAINT 0x10  /* fix_shell + restrain_solvent               */
 #define QGPU_TERMS_ALL       0x1f
+/* Flag for qgpu_forces: evaluate with the precision of an MD step whose
+   energies are not recorded (FP32 throughout, energies from FP32 sums)
+   instead of the FP64 energies of the drop-in call. */
+#define QGPU_TERMS_STEP_PRECISION 0x100
 
 typedef struct qgpu_handle qgpu_handle;
 

@@ -19,6 +19,7 @@ QGPU_TERMS_QBONDED = 0x4
 QGPU_TERMS_BONDED = 0x8
 QGPU_TERMS_RESTRAINT = 0x10
 QGPU_TERMS_ALL = 0x1F
+QGPU_TERMS_STEP_PRECISION = 0x100
 
 STATUS = {0: "ok", 1: "invalid", 2: "cuda", 3: "list overflow", 4: "shake failure", 5: "nan",
           6: "unsupported", 7: "fixed-point range"}

@@ -2,8 +2,8 @@
 // Q-atom list membership (make_pair_lists, src/md.f90:5985-6071).
 #include "qgpu_internal.cuh"
 
-// float mirror of the FP64 master coordinates: hi = float(x - origin),
-// lo = float((x - origin) - hi); w = scaled charge.
+// float mirror of the FP64 coordinates: hi = float(x - origin),
+// lo = float((x - origin) - hi), w = scaled charge; float velocities.
 __global__ void k_mirror(DevSys S) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= S.natom) return;
@@ -14,9 +14,11 @@ __global__ void k_mirror(DevSys S) {
     l.x = (float)(r0 - (double)h.x); l.y = (float)(r1 - (double)h.y); l.z = (float)(r2 - (double)h.z); l.w = 0.f;
     S.pos[i] = h;
     S.poslo[i] = l;
+    S.velf[i] = make_float4((float)S.v[3 * i], (float)S.v[3 * i + 1], (float)S.v[3 * i + 2], 0.f);
 }
 
-// cgp_centers, src/md.f90:2253-2288: mean of the member coordinates (FP64).
+// cgp_centers, src/md.f90:2253-2288: mean of the member coordinates (FP64),
+// and its float offset from the trajectory origin for the per-step kernels.
 __global__ void k_centers(DevSys S) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= S.ngrp) return;
@@ -27,7 +29,10 @@ __global__ void k_centers(DevSys S) {
         c0 += S.x[3 * a]; c1 += S.x[3 * a + 1]; c2 += S.x[3 * a + 2];
     }
     double n = (double)(a1 - a0);
-    S.g_cent[3 * g] = c0 / n; S.g_cent[3 * g + 1] = c1 / n; S.g_cent[3 * g + 2] = c2 / n;
+    const double m0 = c0 / n, m1 = c1 / n, m2 = c2 / n;
+    S.g_cent[3 * g] = m0; S.g_cent[3 * g + 1] = m1; S.g_cent[3 * g + 2] = m2;
+    const TrajInfo &T = S.traj[S.g_traj[g]];
+    S.g_centf[g] = make_float4((float)(m0 - T.origin[0]), (float)(m1 - T.origin[1]), (float)(m2 - T.origin[2]), 0.f);
 }
 
 // Cut-off decision of the list builders (nbpplist_lrf :8083-8090,
@@ -67,9 +72,8 @@ __global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, 
         rt = S.g_switch[t];
         active = !S.g_excl[t];
         th = S.pos[rt]; tl = S.poslo[rt];
-        cx = (float)(S.g_cent[3 * t] - T.origin[0]);
-        cy = (float)(S.g_cent[3 * t + 1] - T.origin[1]);
-        cz = (float)(S.g_cent[3 * t + 2] - T.origin[2]);
+        const float4 c = S.g_centf[t];
+        cx = c.x; cy = c.y; cz = c.z;
     }
     const long long slot = T.scr0 + (long long)chunk * T.ncgp + (t - T.grp0);
     int *nbseg = S.scr_nb + (size_t)slot * QG_CAPC;

@@ -202,6 +202,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_update(DevSys S, const int *items,
             h.x = (float)r0; h.y = (float)r1; h.z = (float)r2; h.w = S.pos[i].w;
             l.x = (float)(r0 - (double)h.x); l.y = (float)(r1 - (double)h.y); l.z = (float)(r2 - (double)h.z); l.w = 0.f;
             S.pos[i] = h; S.poslo[i] = l;
+            S.velf[i] = make_float4((float)v[k][0], (float)v[k][1], (float)v[k][2], 0.f);
         }
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -215,6 +216,166 @@ __global__ void __launch_bounds__(QG_BLOCK) k_update(DevSys S, const int *items,
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
         S.ekin_part[(size_t)blockIdx.x * 4 + threadIdx.x] = s;
     }
+}
+
+// ------------------------------------------------ float-master fused step
+// SHAKE of one water in FP32 on relative vectors.  With D_a the displacement
+// of atom a in this step and r0 = x_i - x_j the constraint vector at the start
+// of the step (a double-float: r0h from the hi parts, r0l from the lo parts),
+// the residual of shake (src/md.f90:17620-17650) is
+//     diff = d0^2 - |r0 + D_i - D_j|^2 = base - (2 r0 + Dij).Dij,
+// base = d0^2 - |r0|^2 formed once per step with two-products / two-sums, so
+// the FP32 diff is accurate to about 1e-9 A^2 against the FP64 value and the
+// convergence test |diff| < 1e-4 d0^2 takes the same decisions except within
+// that distance of the threshold.  The correction follows the reference:
+// acor = diff / (2 (winv_i + winv_j) r.r0), x_i += r0 acor winv_i,
+// x_j -= r0 acor winv_j, Gauss-Seidel over O-H1, O-H2, H1-H2, constraints
+// that met the tolerance once are not revisited, at most SHAKE_MAX_ITER sweeps.
+template <int I, int J>
+__device__ __forceinline__ void shake_pair_f(float3 (&D)[3], const float3 &r0, const float3 &ua, const float3 &ub,
+                                             float base, float S0, float den0, float tol, unsigned &ready, int c) {
+    if (ready & (1u << c)) return;
+    const float dx = D[I].x - D[J].x, dy = D[I].y - D[J].y, dz = D[I].z - D[J].z;
+    const float diff = base - ((2.f * r0.x + dx) * dx + (2.f * r0.y + dy) * dy + (2.f * r0.z + dz) * dz);
+    if (fabsf(diff) < tol) ready |= 1u << c;
+    const float scp = S0 + (r0.x * dx + r0.y * dy + r0.z * dz);
+    const float corr = __fdividef(diff, den0 * scp);
+    D[I].x += ua.x * corr; D[I].y += ua.y * corr; D[I].z += ua.z * corr;
+    D[J].x -= ub.x * corr; D[J].y -= ub.y * corr; D[J].z -= ub.z * corr;
+}
+
+__device__ int shake_water_f(const float4 (&h)[3], const float4 (&l)[3], const float (&w)[3], const float2 (&d2)[3],
+                             float3 (&D)[3], bool *fail) {
+    const int ci[3] = {0, 0, 1}, cj[3] = {1, 2, 2};
+    float3 r0[3], ua[3], ub[3];
+    float base[3], S0[3], den0[3], tol[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int i = ci[c], j = cj[c];
+        const float hx = h[i].x - h[j].x, hy = h[i].y - h[j].y, hz = h[i].z - h[j].z;
+        const float lx = l[i].x - l[j].x, ly = l[i].y - l[j].y, lz = l[i].z - l[j].z;
+        r0[c] = make_float3(hx + lx, hy + ly, hz + lz);
+        // |r0h|^2 as an unevaluated sum sh + sl
+        float ex, ey, ez, e1, e2;
+        const float px = two_prod(hx, hx, ex), py = two_prod(hy, hy, ey), pz = two_prod(hz, hz, ez);
+        const float t = two_sum(px, py, e1);
+        const float sh = two_sum(t, pz, e2);
+        const float sl = ((e1 + e2) + (ex + ey + ez)) + 2.f * (hx * lx + hy * ly + hz * lz);
+        base[c] = (d2[c].x - sh) + (d2[c].y - sl);
+        S0[c] = sh;
+        ua[c] = make_float3(r0[c].x * w[i], r0[c].y * w[i], r0[c].z * w[i]);
+        ub[c] = make_float3(r0[c].x * w[j], r0[c].y * w[j], r0[c].z * w[j]);
+        den0[c] = 2.f * (w[i] + w[j]);
+        tol[c] = (float)SHAKE_TOL * d2[c].x;
+    }
+    unsigned ready = 0u;
+    int nits = 0;
+    for (;;) {
+        shake_pair_f<0, 1>(D, r0[0], ua[0], ub[0], base[0], S0[0], den0[0], tol[0], ready, 0);
+        shake_pair_f<0, 2>(D, r0[1], ua[1], ub[1], base[1], S0[1], den0[1], tol[1], ready, 1);
+        shake_pair_f<1, 2>(D, r0[2], ua[2], ub[2], base[2], S0[2], den0[2], tol[2], ready, 2);
+        nits++;
+        if (ready == 7u) break;
+        if (nits >= SHAKE_MAX_ITER) { *fail = true; break; }
+    }
+    return nits;
+}
+
+// x + D on a hi/lo pair, renormalised
+__device__ __forceinline__ void hilo_add(float &h, float &l, float d) {
+    float e;
+    const float s = two_sum(h, d, e);
+    h = fast_two_sum(s, l + e, l);
+}
+
+// One MD update (mode 1 of k_update) with the float master state: leap-frog
+// + Berendsen (newvel_ber), SHAKE of water items in registers, v = (x-xx)/dt,
+// Ekin partials.  No FP64 arithmetic except the x/v refresh (want_x).
+__global__ void __launch_bounds__(QG_BLOCK) k_update_f(DevSys S, const int *items, EaccSel esel, int nbcycle) {
+    __shared__ float red[4][QG_BLOCK / 32];
+    const int it = items[blockIdx.x * blockDim.x + threadIdx.x];
+    const int next = esel.recctl[0] + esel.k + 1;
+    const bool want_x = (next % nbcycle == 0) ||
+                        (esel.mode == EACC_RECORD && esel.ene_every > 0 && next % esel.ene_every == 0);
+    float ek[4] = {0.f, 0.f, 0.f, 0.f};
+    if (it >= 0) {
+        const bool mol = (it >> 30) & 1;
+        const int m = it & 0x3fffffff;
+        const int a0 = mol ? S.shk_i[S.shk_first[m]] : m;
+        const int na = mol ? 3 : 1;
+        const int tr = S.atraj[a0];
+        const TrajInfo &T = S.traj[tr];
+        TrajState &TS = S.tstate[tr];
+        const float dt = T.dtf;
+        float4 h[3], l[3];
+        float3 v[3], D[3];
+        float w[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (k >= na) { h[k] = l[k] = make_float4(0, 0, 0, 0); v[k] = D[k] = make_float3(0, 0, 0); w[k] = 0.f; continue; }
+            const int i = a0 + k;
+            h[k] = S.pos[i]; l[k] = S.poslo[i]; w[k] = S.winvf[i];
+            const float4 vi = S.velf[i];
+            const float ts = (i - T.atom0) < T.nat_solute ? TS.tsf_solute : TS.tsf_solvent;
+            const float gx = fx_getf(S.fx[3 * i]), gy = fx_getf(S.fx[3 * i + 1]), gz = fx_getf(S.fx[3 * i + 2]);
+            S.fx[3 * i] = 0ull; S.fx[3 * i + 1] = 0ull; S.fx[3 * i + 2] = 0ull;
+            const float wdt = w[k] * dt;
+            v[k] = make_float3((vi.x - gx * wdt) * ts, (vi.y - gy * wdt) * ts, (vi.z - gz * wdt) * ts);
+            D[k] = make_float3(v[k].x * dt, v[k].y * dt, v[k].z * dt);
+        }
+        if (mol) {
+            const int c0 = S.shk_first[m];
+            const float2 d2[3] = {S.shk_d2hl[c0], S.shk_d2hl[c0 + 1], S.shk_d2hl[c0 + 2]};
+            bool fail = false;
+            const int nits = shake_water_f(h, l, w, d2, D, &fail);
+            if (fail) atomicOr(S.status, ST_SHAKE);
+            atomicAdd(&TS.shake_iters, nits);
+        }
+        const bool vfix = T.nshake_mol > 0;
+        for (int k = 0; k < na; ++k) {
+            const int i = a0 + k;
+            if (vfix) v[k] = make_float3(D[k].x * T.inv_dtf, D[k].y * T.inv_dtf, D[k].z * T.inv_dtf);
+            hilo_add(h[k].x, l[k].x, D[k].x);
+            hilo_add(h[k].y, l[k].y, D[k].y);
+            hilo_add(h[k].z, l[k].z, D[k].z);
+            S.pos[i] = h[k]; S.poslo[i] = l[k];
+            S.velf[i] = make_float4(v[k].x, v[k].y, v[k].z, 0.f);
+            const float e = 0.5f * S.massf[i] * (v[k].x * v[k].x + v[k].y * v[k].y + v[k].z * v[k].z);
+            const bool fr = !S.aexcl[i];
+            if ((i - T.atom0) < T.nat_solute) { ek[0] += e; ek[1] += fr ? e : 0.f; }
+            else { ek[2] += e; ek[3] += fr ? e : 0.f; }
+            if (want_x) {
+                S.x[3 * i] = T.origin[0] + ((double)h[k].x + (double)l[k].x);
+                S.x[3 * i + 1] = T.origin[1] + ((double)h[k].y + (double)l[k].y);
+                S.x[3 * i + 2] = T.origin[2] + ((double)h[k].z + (double)l[k].z);
+                S.v[3 * i] = (double)v[k].x; S.v[3 * i + 1] = (double)v[k].y; S.v[3 * i + 2] = (double)v[k].z;
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float v = warp_sum_f(ek[k]);
+        if (lane == 0) red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        float s = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
+        S.ekin_part[(size_t)blockIdx.x * 4 + threadIdx.x] = (double)s;
+    }
+}
+
+// x = origin + (hi + lo), v = velf: the FP64 view of the float master.
+__global__ void k_sync_double(DevSys S) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.natom) return;
+    const TrajInfo &T = S.traj[S.atraj[i]];
+    const float4 h = S.pos[i], l = S.poslo[i], v = S.velf[i];
+    S.x[3 * i] = T.origin[0] + ((double)h.x + (double)l.x);
+    S.x[3 * i + 1] = T.origin[1] + ((double)h.y + (double)l.y);
+    S.x[3 * i + 2] = T.origin[2] + ((double)h.z + (double)l.z);
+    S.v[3 * i] = (double)v.x; S.v[3 * i + 1] = (double)v.y; S.v[3 * i + 2] = (double)v.z;
 }
 
 // One block per trajectory: temperature() (optional) and the energy summary
@@ -262,6 +423,9 @@ __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_ba
             tu = ts;
         }
         TS.Temp = Temp; TS.Tfree = Tfree; TS.Tscale_solute = tu; TS.Tscale_solvent = ts;
+        TS.tsf_solute = (float)tu; TS.tsf_solvent = (float)ts;
+        TS.wshift = T.fk_wsphere != 0.0 ? sqrt(BOLTZ * Tfree / T.fk_wsphere) : 0.0;
+        TS.wshiftf = (float)TS.wshift;
         if (Temp != Temp) atomicOr(S.status, ST_NAN);
     }
     if (!rec) return;
@@ -335,6 +499,18 @@ void launch_shake(const DevSys &S, const BlockTables &B, LaunchCtx &L, int traj_
 void launch_update(const DevSys &S, const BlockTables &B, LaunchCtx &L, int mode) {
     prof_begin(L, "k_update");
     k_update<<<B.nuitem / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.uitem, mode);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int nbcycle) {
+    prof_begin(L, "k_update_f");
+    k_update_f<<<B.nuitem / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.uitem, e, nbcycle);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_sync_double(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
+    prof_begin(L, "k_sync_double");
+    k_sync_double<<<nblk(S.natom, 256), 256, 0, L.stream>>>(S);
     prof_end(L);
     (*L.nlaunch)++;
 }

@@ -4,26 +4,14 @@
 // pair terms, so each pair is evaluated from both sides with bitwise opposite
 // results and no force atomics are needed inside the loop.  Pair distances come
 // from hi/lo float coordinates; energies are Kahan-summed per thread and
-// reduced in FP64; forces go to the int64 fixed-point gradient once per atom.
+// reduced as int64 fixed point; forces go to the int64 fixed-point gradient
+// once per atom.  Outside the accurate-energy variants (EACC) these kernels
+// execute no FP64 instruction: GB300 issues FP64 at 1/64 of the FP32 rate.
 #include "qgpu_internal.cuh"
 
 __device__ __forceinline__ int traj_of_entry(const DevSys &S, int e, bool group) {
     if (e < 0) return -1 - e;
     return group ? S.g_traj[e] : S.atraj[e];
-}
-
-// Block-wide FP64 sum of `v` into energy slot `slot` of trajectory `traj`.
-__device__ __forceinline__ void block_energy(const DevSys &S, int traj, int slot, double v, double *red) {
-    v = warp_sum_d(v);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
-        if (s != 0.0) fx_add(S.eacc + (size_t)traj * QG_NE + slot, s, S.status);
-    }
 }
 
 __device__ __forceinline__ int ljc(const DevSys &S, const TrajInfo &T, int ta, int tb) {
@@ -65,7 +53,7 @@ struct EAcc<false> {
     __device__ __forceinline__ void zero() { k.zero(); part = 0.f; }
     __device__ __forceinline__ void term(float f, double) { part += f; }
     __device__ __forceinline__ void flush() { k.add(part); part = 0.f; }
-    __device__ __forceinline__ double value() const { return k.value(); }
+    __device__ __forceinline__ long long fx(float scale, int *st) const { return k.fx(scale, st); }
 };
 template <>
 struct EAcc<true> {
@@ -73,7 +61,7 @@ struct EAcc<true> {
     __device__ __forceinline__ void zero() { s = 0.0; }
     __device__ __forceinline__ void term(float, double d) { s += d; }
     __device__ __forceinline__ void flush() {}
-    __device__ __forceinline__ double value() const { return s; }
+    __device__ __forceinline__ long long fx(float scale, int *st) const { return d2fx_chk(s * (double)scale, st); }
 };
 
 // --------------------------------------------------------------- waters
@@ -83,7 +71,7 @@ struct EAcc<true> {
 // lanes' partial gradients are summed by an xor butterfly (fixed order).
 template <bool EACC>
 __global__ void __launch_bounds__(QG_BLOCK) k_nb_water(DevSys S, const int *wgrp, int lrf) {
-    __shared__ double red[QG_BLOCK / 32];
+    __shared__ long long red[5][QG_BLOCK / 32];
     const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / QG_LW;
     const int lane = threadIdx.x & (QG_LW - 1);
     const int w = wgrp[idx];
@@ -203,27 +191,25 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_water(DevSys S, const int *wgrp
         if (valid && lane == 0) {
             if (lrf) {
                 const float *ph = S.g_phif + (size_t)w * QG_NPHI;
-                const float cx = (float)(S.g_cent[3 * w] - T.origin[0]);
-                const float cy = (float)(S.g_cent[3 * w + 1] - T.origin[1]);
-                const float cz = (float)(S.g_cent[3 * w + 2] - T.origin[2]);
+                const float4 c = S.g_centf[w];
 #pragma unroll
                 for (int a = 0; a < 3; ++a)
-                    elrf += lrf_atom(ph, (cx - ah[a].x) - al[a].x, (cy - ah[a].y) - al[a].y,
-                                     (cz - ah[a].z) - al[a].z, ah[a].w, gx[a], gy[a], gz[a]);
+                    elrf += lrf_atom(ph, (c.x - ah[a].x) - al[a].x, (c.y - ah[a].y) - al[a].y,
+                                     (c.z - ah[a].z) - al[a].z, ah[a].w, gx[a], gy[a], gz[a]);
             }
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                fx_add(S.fx + 3 * (a0 + a), gx[a], S.status);
-                fx_add(S.fx + 3 * (a0 + a) + 1, gy[a], S.status);
-                fx_add(S.fx + 3 * (a0 + a) + 2, gz[a], S.status);
+                fx_addf(S.fx + 3 * (a0 + a), gx[a], S.status);
+                fx_addf(S.fx + 3 * (a0 + a) + 1, gy[a], S.status);
+                fx_addf(S.fx + 3 * (a0 + a) + 2, gz[a], S.status);
             }
         }
     }
-    block_energy(S, traj, EA_WW_EL, 0.5 * eww_el.value(), red);
-    block_energy(S, traj, EA_WW_VDW, 0.5 * eww_vdw.value(), red);
-    block_energy(S, traj, EA_PW_EL, 0.5 * epw_el.value(), red);
-    block_energy(S, traj, EA_PW_VDW, 0.5 * epw_vdw.value(), red);
-    if (lrf) block_energy(S, traj, EA_LRF, (double)elrf, red);
+    // pair energies are summed from both sides: half of each thread's sum
+    const int slots[5] = {EA_WW_EL, EA_WW_VDW, EA_PW_EL, EA_PW_VDW, EA_LRF};
+    long long ev[5] = {eww_el.fx(0.5f, S.status), eww_vdw.fx(0.5f, S.status), epw_el.fx(0.5f, S.status),
+                       epw_vdw.fx(0.5f, S.status), f2fx_chk(elrf, S.status)};
+    block_energies_fx<5>(S.eacc + (size_t)traj * QG_NE, slots, ev, red);
 }
 
 // ------------------------------------------------------- solute atoms
@@ -248,7 +234,7 @@ __device__ __forceinline__ PairFlags pair_flags(const DevSys &S, int i, int j) {
 // lrf_taylor, for one non-Q solute atom.
 template <bool EACC>
 __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *satom, int lrf) {
-    __shared__ double red[QG_BLOCK / 32];
+    __shared__ long long red[5][QG_BLOCK / 32];
     const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / QG_LW;
     const int lane = threadIdx.x & (QG_LW - 1);
     const int i = satom[idx];
@@ -331,21 +317,18 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         if (valid && lane == 0) {
             if (lrf) {
                 const float *ph = S.g_phif + (size_t)g * QG_NPHI;
-                const float cx = (float)(S.g_cent[3 * g] - T.origin[0]);
-                const float cy = (float)(S.g_cent[3 * g + 1] - T.origin[1]);
-                const float cz = (float)(S.g_cent[3 * g + 2] - T.origin[2]);
-                elrf = lrf_atom(ph, (cx - ih.x) - il.x, (cy - ih.y) - il.y, (cz - ih.z) - il.z, ih.w, gx, gy, gz);
+                const float4 c = S.g_centf[g];
+                elrf = lrf_atom(ph, (c.x - ih.x) - il.x, (c.y - ih.y) - il.y, (c.z - ih.z) - il.z, ih.w, gx, gy, gz);
             }
-            fx_add(S.fx + 3 * i, gx, S.status);
-            fx_add(S.fx + 3 * i + 1, gy, S.status);
-            fx_add(S.fx + 3 * i + 2, gz, S.status);
+            fx_addf(S.fx + 3 * i, gx, S.status);
+            fx_addf(S.fx + 3 * i + 1, gy, S.status);
+            fx_addf(S.fx + 3 * i + 2, gz, S.status);
         }
     }
-    block_energy(S, traj, EA_PP_EL, 0.5 * epp_el.value(), red);
-    block_energy(S, traj, EA_PP_VDW, 0.5 * epp_vdw.value(), red);
-    block_energy(S, traj, EA_PW_EL, 0.5 * epw_el.value(), red);
-    block_energy(S, traj, EA_PW_VDW, 0.5 * epw_vdw.value(), red);
-    if (lrf) block_energy(S, traj, EA_LRF, (double)elrf, red);
+    const int slots[5] = {EA_PP_EL, EA_PP_VDW, EA_PW_EL, EA_PW_VDW, EA_LRF};
+    long long ev[5] = {epp_el.fx(0.5f, S.status), epp_vdw.fx(0.5f, S.status), epw_el.fx(0.5f, S.status),
+                       epw_vdw.fx(0.5f, S.status), f2fx_chk(elrf, S.status)};
+    block_energies_fx<5>(S.eacc + (size_t)traj * QG_NE, slots, ev, red);
 }
 
 // ------------------------------------------------------- Q-atom loops
@@ -355,7 +338,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
 struct QShared {
     float4 qh[QG_MAXQ], ql[QG_MAXQ];
     float qf[QG_BLOCK / 32][QG_MAXQ][3];
-    double red[QG_BLOCK / 32];
+    long long red[2 * QG_MAXS][QG_BLOCK / 32];
 };
 
 __device__ __forceinline__ void q_reduce_store(QShared &sh, int iq, float fx, float fy, float fz) {
@@ -369,9 +352,9 @@ __device__ __forceinline__ void q_flush(const DevSys &S, const TrajInfo &T, QSha
     __syncthreads();
     for (int k = threadIdx.x; k < T.nqat * 3; k += blockDim.x) {
         const int iq = k / 3, c = k % 3;
-        double s = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += (double)sh.qf[w][iq][c];
-        if (s != 0.0) fx_add(S.fx + 3 * S.q_atom[T.q0 + iq] + c, s, S.status);
+        float s = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh.qf[w][iq][c];
+        if (s != 0.f) fx_addf(S.fx + 3 * S.q_atom[T.q0 + iq] + c, s, S.status);
     }
 }
 __device__ __forceinline__ void q_load(const DevSys &S, const TrajInfo &T, QShared &sh) {
@@ -396,8 +379,26 @@ struct QE {
 #pragma unroll
         for (int s = 0; s < QG_MAXS; ++s) { k[s].zero(); d[s] = 0.0; }
     }
-    __device__ __forceinline__ double value(int s, bool acc) const { return acc ? d[s] : k[s].value(); }
+    __device__ __forceinline__ long long fx(int s, bool acc, int *st) const {
+        return acc ? d2fx_chk(d[s], st) : k[s].fx(1.f, st);
+    }
 };
+
+// the per-state el/vdW sums of a Q loop into slots base_el / base_vdw
+__device__ __forceinline__ void q_energies(const DevSys &S, int traj, int NS, const QE &eel, const QE &evdw, bool acc,
+                                           int e_el, int e_vdw, QShared &sh) {
+    int slots[2 * QG_MAXS];
+    long long v[2 * QG_MAXS];
+#pragma unroll
+    for (int s = 0; s < QG_MAXS; ++s) {
+        const bool on = s < NS;
+        slots[2 * s] = EA_Q0 + EQ_N * s + e_el;
+        slots[2 * s + 1] = EA_Q0 + EQ_N * s + e_vdw;
+        v[2 * s] = on ? eel.fx(s, acc, S.status) : 0;
+        v[2 * s + 1] = on ? evdw.fx(s, acc, S.status) : 0;
+    }
+    block_energies_fx<2 * QG_MAXS>(S.eacc + (size_t)traj * QG_NE, slots, v, sh.red);
+}
 
 // nonbond_qw_spc, src/md.f90:14411-14570.  One thread per water.
 __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, EaccSel esel) {
@@ -424,7 +425,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
     float gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0}, gz[3] = {0, 0, 0};
     float lam[QG_MAXS];
 #pragma unroll
-    for (int s = 0; s < QG_MAXS; ++s) lam[s] = (float)T.lambda[s];
+    for (int s = 0; s < QG_MAXS; ++s) lam[s] = T.lambdaf[s];
     const int ntq = T.natyps + T.nqat;
     for (int iq = 0; iq < T.nqat; ++iq) {
         float qfx = 0.f, qfy = 0.f, qfz = 0.f;
@@ -483,15 +484,12 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
     if (valid)
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            fx_add(S.fx + 3 * (a0 + a), gx[a], S.status);
-            fx_add(S.fx + 3 * (a0 + a) + 1, gy[a], S.status);
-            fx_add(S.fx + 3 * (a0 + a) + 2, gz[a], S.status);
+            fx_addf(S.fx + 3 * (a0 + a), gx[a], S.status);
+            fx_addf(S.fx + 3 * (a0 + a) + 1, gy[a], S.status);
+            fx_addf(S.fx + 3 * (a0 + a) + 2, gz[a], S.status);
         }
     q_flush(S, T, sh);
-    for (int s = 0; s < NS; ++s) {
-        block_energy(S, traj, EA_Q0 + EQ_N * s + EQ_QW_EL, eel.value(s, acc), sh.red);
-        block_energy(S, traj, EA_Q0 + EQ_N * s + EQ_QW_VDW, evdw.value(s, acc), sh.red);
-    }
+    q_energies(S, traj, NS, eel, evdw, acc, EQ_QW_EL, EQ_QW_VDW, sh);
 }
 
 // nonbond_qp (src/md.f90:13788-13921) / nonbond_qp_qvdw (14097-14230).
@@ -557,7 +555,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
                 float Vel = S.qcrg_f[q * QG_MAXS + s] * jh.w * ri;
                 if (c == 3) Vel *= T.el14;
                 const float Va = A / (r6s * r6s), Vb = B / r6s;
-                dv += (float)T.lambda[s] * ri2 * (-Vel - (12.f * Va - 6.f * Vb) * (r6 / r6s));
+                dv += T.lambdaf[s] * ri2 * (-Vel - (12.f * Va - 6.f * Vb) * (r6 / r6s));
                 if (acc) {
                     double Veld = S.qcrg_d[q * QG_MAXS + s] * S.crg_d[j] * rid;
                     if (c == 3) Veld *= T.el14d;
@@ -573,15 +571,12 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
         q_reduce_store(sh, iq, qfx, qfy, qfz);
     }
     if (valid) {
-        fx_add(S.fx + 3 * j, gx, S.status);
-        fx_add(S.fx + 3 * j + 1, gy, S.status);
-        fx_add(S.fx + 3 * j + 2, gz, S.status);
+        fx_addf(S.fx + 3 * j, gx, S.status);
+        fx_addf(S.fx + 3 * j + 1, gy, S.status);
+        fx_addf(S.fx + 3 * j + 2, gz, S.status);
     }
     q_flush(S, T, sh);
-    for (int s = 0; s < NS; ++s) {
-        block_energy(S, traj, EA_Q0 + EQ_N * s + EQ_QP_EL, eel.value(s, acc), sh.red);
-        block_energy(S, traj, EA_Q0 + EQ_N * s + EQ_QP_VDW, evdw.value(s, acc), sh.red);
-    }
+    q_energies(S, traj, NS, eel, evdw, acc, EQ_QP_EL, EQ_QP_VDW, sh);
 }
 
 void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {

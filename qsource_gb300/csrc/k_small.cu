@@ -1,152 +1,203 @@
-// k_small.cu -- the small FP64 terms of pot_energy (src/md.f90:16100-16150):
+// k_small.cu -- the small terms of pot_energy (src/md.f90:16100-16150):
 // nonbond_qq, the per-state Q bonded terms, classical bonded terms, the sphere
 // restraints and the EVB off-diagonal couplings.  These are O(Q^2) or O(N)
-// with little arithmetic, so they stay in FP64 like the reference.
+// with little arithmetic.  Each term is written once over a real type R:
+//   R = double on the steps whose energies are recorded and in the drop-in
+//          qgpu_forces call (coordinates from the FP64 x, FP64 parameters);
+//   R = float on every other MD step (relative vectors from the hi/lo float
+//          coordinates, float parameter copies), because GB300 issues FP64 at
+//          1/64 of the FP32 rate and these terms run every step.
 #include <math.h>
 
 #include "qgpu_internal.cuh"
 
 #define QREAL_EPS 1.0e-14   // src/sizes.f90:48
-#define BOLTZ 0.001986      // src/md.f90:54
 
-__device__ __forceinline__ void block_energy_d(const DevSys &S, int traj, int slot, double v, double *red) {
-    v = warp_sum_d(v);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
-        if (s != 0.0) fx_add(S.eacc + (size_t)traj * QG_NE + slot, s, S.status);
+template <typename R>
+struct V3 {
+    R x, y, z;
+};
+
+// b - a from the coordinates of the precision in use
+template <typename R>
+__device__ __forceinline__ V3<R> rel(const DevSys &S, int a, int b);
+template <>
+__device__ __forceinline__ V3<double> rel<double>(const DevSys &S, int a, int b) {
+    return {S.x[3 * b] - S.x[3 * a], S.x[3 * b + 1] - S.x[3 * a + 1], S.x[3 * b + 2] - S.x[3 * a + 2]};
+}
+template <>
+__device__ __forceinline__ V3<float> rel<float>(const DevSys &S, int a, int b) {
+    const float3 d = dpos(S.pos[a], S.poslo[a], S.pos[b], S.poslo[b]);
+    return {d.x, d.y, d.z};
+}
+
+// parameter access per precision
+template <typename R> struct P;
+template <>
+struct P<double> {
+    static __device__ __forceinline__ double crg(const DevSys &S, int i) { return S.crg_d[i]; }
+    static __device__ __forceinline__ double qcrg(const DevSys &S, int k) { return S.qcrg_d[k]; }
+    static __device__ __forceinline__ double avdw(const DevSys &S, int k) { return S.avdw_d[k]; }
+    static __device__ __forceinline__ double bvdw(const DevSys &S, int k) { return S.bvdw_d[k]; }
+    static __device__ __forceinline__ double qavdw(const DevSys &S, int k) { return S.qavdw_d[k]; }
+    static __device__ __forceinline__ double qbvdw(const DevSys &S, int k) { return S.qbvdw_d[k]; }
+    static __device__ __forceinline__ double sc(const DevSys &S, size_t k) { return S.sc_d[k]; }
+    static __device__ __forceinline__ double qq_els(const DevSys &S, int k) { return S.qq_els[k]; }
+    static __device__ __forceinline__ const double *qt_lib(const DevSys &S) { return S.qt_lib; }
+    static __device__ __forceinline__ const double *bt_lib(const DevSys &S) { return S.bt_lib; }
+    static __device__ __forceinline__ double lambda(const TrajInfo &T, int s) { return T.lambda[s]; }
+    static __device__ __forceinline__ double el14(const TrajInfo &T) { return T.el14d; }
+    static __device__ __forceinline__ void grad(const DevSys &S, int a, double gx, double gy, double gz) {
+        fx_add(S.fx + 3 * a, gx, S.status);
+        fx_add(S.fx + 3 * a + 1, gy, S.status);
+        fx_add(S.fx + 3 * a + 2, gz, S.status);
     }
-}
-__device__ __forceinline__ void grad_add(const DevSys &S, int a, double gx, double gy, double gz) {
-    fx_add(S.fx + 3 * a, gx, S.status);
-    fx_add(S.fx + 3 * a + 1, gy, S.status);
-    fx_add(S.fx + 3 * a + 2, gz, S.status);
-}
+    static __device__ __forceinline__ long long fx(double v, int *st) { return d2fx_chk(v, st); }
+};
+template <>
+struct P<float> {
+    static __device__ __forceinline__ float crg(const DevSys &S, int i) { return S.pos[i].w; }
+    static __device__ __forceinline__ float qcrg(const DevSys &S, int k) { return S.qcrg_f[k]; }
+    static __device__ __forceinline__ float avdw(const DevSys &S, int k) { return S.avdw[k]; }
+    static __device__ __forceinline__ float bvdw(const DevSys &S, int k) { return S.bvdw[k]; }
+    static __device__ __forceinline__ float qavdw(const DevSys &S, int k) { return S.qavdw[k]; }
+    static __device__ __forceinline__ float qbvdw(const DevSys &S, int k) { return S.qbvdw[k]; }
+    static __device__ __forceinline__ float sc(const DevSys &S, size_t k) { return S.sc_f[k]; }
+    static __device__ __forceinline__ float qq_els(const DevSys &S, int k) { return S.qq_elsf[k]; }
+    static __device__ __forceinline__ const float *qt_lib(const DevSys &S) { return S.qt_libf; }
+    static __device__ __forceinline__ const float *bt_lib(const DevSys &S) { return S.bt_libf; }
+    static __device__ __forceinline__ float lambda(const TrajInfo &T, int s) { return T.lambdaf[s]; }
+    static __device__ __forceinline__ float el14(const TrajInfo &T) { return T.el14; }
+    static __device__ __forceinline__ void grad(const DevSys &S, int a, float gx, float gy, float gz) {
+        fx_addf(S.fx + 3 * a, gx, S.status);
+        fx_addf(S.fx + 3 * a + 1, gy, S.status);
+        fx_addf(S.fx + 3 * a + 2, gz, S.status);
+    }
+    static __device__ __forceinline__ long long fx(float v, int *st) { return f2fx_chk(v, st); }
+};
+
+typedef long long Red[4][QG_BLOCK / 32];
 
 // nonbond_qq, src/md.f90:13491-13636.  One block per (trajectory, state).
-__device__ void qq_block(const DevSys &S, int b, const int *blk_traj, const int *blk_s, double *red) {
+template <typename R>
+__device__ void qq_block(const DevSys &S, int b, const int *blk_traj, const int *blk_s, Red &red) {
+    typedef P<R> p;
     const int traj = blk_traj[b], s = blk_s[b];
     const TrajInfo &T = S.traj[traj];
-    const double lam = T.lambda[s];
+    const R lam = p::lambda(T, s);
     const int ntq = T.natyps + T.nqat;
-    double eqq_el = 0, eqq_vdw = 0, eqp_el = 0, eqp_vdw = 0;
+    R eqq_el = 0, eqq_vdw = 0, eqp_el = 0, eqp_vdw = 0;
     for (int k = T.qq0[s] + threadIdx.x; k < T.qq0[s] + T.nqq[s]; k += blockDim.x) {
         const int q = S.qq_iq[k], i = S.q_atom[q], j = S.qq_j[k], jq = S.qq_jq[k], c = S.qq_lj[k];
         const int iql = q - T.q0;
-        const double qi = S.qcrg_d[q * QG_MAXS + s];
-        double qj, aLJ, bLJ;
+        const R qi = p::qcrg(S, q * QG_MAXS + s);
+        R qj, aLJ, bLJ;
         if (!T.qvdw) {
             const int ti = S.atype[i], tj = S.atype[j];
-            aLJ = S.avdw_d[ti * 3 + c - 1] * S.avdw_d[tj * 3 + c - 1];
-            bLJ = S.bvdw_d[ti * 3 + c - 1] * S.bvdw_d[tj * 3 + c - 1];
-            qj = jq >= 0 ? S.qcrg_d[jq * QG_MAXS + s] : S.crg_d[j];
+            aLJ = p::avdw(S, ti * 3 + c - 1) * p::avdw(S, tj * 3 + c - 1);
+            bLJ = p::bvdw(S, ti * 3 + c - 1) * p::bvdw(S, tj * 3 + c - 1);
+            qj = jq >= 0 ? p::qcrg(S, jq * QG_MAXS + s) : p::crg(S, j);
         } else {
             const int ti = S.qiac[q * QG_MAXS + s];
-            aLJ = S.qavdw_d[ti * 3 + c - 1];
-            bLJ = S.qbvdw_d[ti * 3 + c - 1];
+            aLJ = p::qavdw(S, ti * 3 + c - 1);
+            bLJ = p::qbvdw(S, ti * 3 + c - 1);
             if (jq >= 0) {
                 const int tj = S.qiac[jq * QG_MAXS + s];
-                aLJ *= S.qavdw_d[tj * 3 + c - 1];
-                bLJ *= S.qbvdw_d[tj * 3 + c - 1];
-                qj = S.qcrg_d[jq * QG_MAXS + s];
+                aLJ *= p::qavdw(S, tj * 3 + c - 1);
+                bLJ *= p::qbvdw(S, tj * 3 + c - 1);
+                qj = p::qcrg(S, jq * QG_MAXS + s);
             } else {
-                if (c == 2) { aLJ = S.qavdw_d[ti * 3]; bLJ = S.qbvdw_d[ti * 3]; }
+                if (c == 2) { aLJ = p::qavdw(S, ti * 3); bLJ = p::qbvdw(S, ti * 3); }
                 const int tj = S.atype[j];
-                aLJ *= S.avdw_d[tj * 3 + c - 1];
-                bLJ *= S.bvdw_d[tj * 3 + c - 1];
-                qj = S.crg_d[j];
+                aLJ *= p::avdw(S, tj * 3 + c - 1);
+                bLJ *= p::bvdw(S, tj * 3 + c - 1);
+                qj = p::crg(S, j);
             }
         }
-        const double dx = S.x[3 * j] - S.x[3 * i], dy = S.x[3 * j + 1] - S.x[3 * i + 1], dz = S.x[3 * j + 2] - S.x[3 * i + 2];
-        double r2 = dx * dx + dy * dy + dz * dz;
-        const double r6hc = r2 * r2 * r2;
+        const V3<R> d = rel<R>(S, i, j);
+        R r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+        const R r6hc = r2 * r2 * r2;
         // softcore column natyps+jq, natyps for a non-Q partner (src/md.f90:13561)
         const int col = jq >= 0 ? T.natyps + (jq - T.q0) : T.natyps - 1;
-        double r6 = r6hc + S.sc_d[(size_t)T.sc0 + ((size_t)iql * ntq + col) * QG_MAXS + s];
-        r6 = 1.0 / r6;
-        const double r12 = r6 * r6;
-        r2 = 1.0 / r2;
-        const double r = sqrt(r2);
-        double Vel = qi * qj * r * S.qq_els[k];
-        if (c == 3) Vel *= T.el14;
-        double Va, Vb, dv;
+        R r6 = r6hc + p::sc(S, (size_t)T.sc0 + ((size_t)iql * ntq + col) * QG_MAXS + s);
+        r6 = R(1) / r6;
+        const R r12 = r6 * r6;
+        r2 = R(1) / r2;
+        const R r = sqrt(r2);
+        R Vel = qi * qj * r * p::qq_els(S, k);
+        if (c == 3) Vel *= p::el14(T);
+        R Va, Vb, dv;
         if (T.qvdw && jq >= 0 && c == 2) {
             Va = aLJ * exp(-bLJ / r);
-            Vb = 0.0;
+            Vb = 0;
             dv = r2 * (-Vel - bLJ * Va / r) * lam;
         } else {
             Va = aLJ * r12;
             Vb = bLJ * r6;
-            dv = r2 * (-Vel - (12.0 * Va - 6.0 * Vb) * r6hc * r6) * lam;
+            dv = r2 * (-Vel - (R(12) * Va - R(6) * Vb) * r6hc * r6) * lam;
         }
-        grad_add(S, i, -dv * dx, -dv * dy, -dv * dz);
-        grad_add(S, j, dv * dx, dv * dy, dv * dz);
+        p::grad(S, i, -dv * d.x, -dv * d.y, -dv * d.z);
+        p::grad(S, j, dv * d.x, dv * d.y, dv * d.z);
         if (jq >= 0) { eqq_el += Vel; eqq_vdw += Va - Vb; }
         else { eqp_el += Vel; eqp_vdw += Va - Vb; }
     }
     const int base = EA_Q0 + EQ_N * s;
-    block_energy_d(S, traj, base + EQ_QQ_EL, eqq_el, red);
-    block_energy_d(S, traj, base + EQ_QQ_VDW, eqq_vdw, red);
-    block_energy_d(S, traj, base + EQ_QP_EL, eqp_el, red);
-    block_energy_d(S, traj, base + EQ_QP_VDW, eqp_vdw, red);
+    const int slots[4] = {base + EQ_QQ_EL, base + EQ_QQ_VDW, base + EQ_QP_EL, base + EQ_QP_VDW};
+    long long v[4] = {p::fx(eqq_el, S.status), p::fx(eqq_vdw, S.status), p::fx(eqp_el, S.status),
+                      p::fx(eqp_vdw, S.status)};
+    block_energies_fx<4>(S.eacc + (size_t)traj * QG_NE, slots, v, red);
 }
 
 // --------------------------------------------------- angle / dihedral
-__device__ double angle_grad(const DevSys &S, int i, int j, int k, double fk, double ang0, double scale, double gi[3],
-                             double gk[3]) {
-    double rji[3], rjk[3];
-    for (int a = 0; a < 3; ++a) { rji[a] = S.x[3 * i + a] - S.x[3 * j + a]; rjk[a] = S.x[3 * k + a] - S.x[3 * j + a]; }
-    const double bji = sqrt(rji[0] * rji[0] + rji[1] * rji[1] + rji[2] * rji[2]);
-    const double bjk = sqrt(rjk[0] * rjk[0] + rjk[1] * rjk[1] + rjk[2] * rjk[2]);
-    double scp = (rji[0] * rjk[0] + rji[1] * rjk[1] + rji[2] * rjk[2]) / (bji * bjk);
-    scp = fmin(1.0, fmax(-1.0, scp));
-    const double ang = acos(scp), da = ang - ang0;
-    const double dv = fk * da * scale;
-    double f1 = sin(ang);
-    if (fabs(f1) < QREAL_EPS) f1 = QREAL_EPS;
-    f1 = -1.0 / f1;
-    for (int a = 0; a < 3; ++a) {
-        gi[a] = dv * f1 * (rjk[a] / (bji * bjk) - scp * rji[a] / (bji * bji));
-        gk[a] = dv * f1 * (rji[a] / (bji * bjk) - scp * rjk[a] / (bjk * bjk));
+template <typename R>
+__device__ R angle_grad(const DevSys &S, int i, int j, int k, R fk, R ang0, R scale, R gi[3], R gk[3]) {
+    const V3<R> a = rel<R>(S, j, i), c = rel<R>(S, j, k);   // rji, rjk
+    const R rji[3] = {a.x, a.y, a.z}, rjk[3] = {c.x, c.y, c.z};
+    const R bji = sqrt(rji[0] * rji[0] + rji[1] * rji[1] + rji[2] * rji[2]);
+    const R bjk = sqrt(rjk[0] * rjk[0] + rjk[1] * rjk[1] + rjk[2] * rjk[2]);
+    R scp = (rji[0] * rjk[0] + rji[1] * rjk[1] + rji[2] * rjk[2]) / (bji * bjk);
+    scp = fmin(R(1), fmax(R(-1), scp));
+    const R ang = acos(scp), da = ang - ang0;
+    const R dv = fk * da * scale;
+    R f1 = sin(ang);
+    if (fabs(f1) < R(QREAL_EPS)) f1 = R(QREAL_EPS);
+    f1 = R(-1) / f1;
+    for (int q = 0; q < 3; ++q) {
+        gi[q] = dv * f1 * (rjk[q] / (bji * bjk) - scp * rji[q] / (bji * bji));
+        gk[q] = dv * f1 * (rji[q] / (bji * bjk) - scp * rjk[q] / (bjk * bjk));
     }
-    return 0.5 * fk * da * da;
+    return R(0.5) * fk * da * da;
 }
 
 // dihedral angle and its derivative components (src/md.f90:17241-17538)
-__device__ double dihedral(const DevSys &S, int i, int j, int k, int l, double dp[12]) {
-    double rji[3], rjk[3], rkl[3], rnj[3], rnk[3];
-    for (int a = 0; a < 3; ++a) {
-        rji[a] = S.x[3 * i + a] - S.x[3 * j + a];
-        rjk[a] = S.x[3 * k + a] - S.x[3 * j + a];
-        rkl[a] = S.x[3 * l + a] - S.x[3 * k + a];
-    }
+template <typename R>
+__device__ R dihedral(const DevSys &S, int i, int j, int k, int l, R dp[12]) {
+    const V3<R> a = rel<R>(S, j, i), b = rel<R>(S, j, k), c = rel<R>(S, k, l);
+    const R rji[3] = {a.x, a.y, a.z}, rjk[3] = {b.x, b.y, b.z}, rkl[3] = {c.x, c.y, c.z};
+    R rnj[3], rnk[3];
     rnj[0] = rji[1] * rjk[2] - rji[2] * rjk[1];
     rnj[1] = rji[2] * rjk[0] - rji[0] * rjk[2];
     rnj[2] = rji[0] * rjk[1] - rji[1] * rjk[0];
     rnk[0] = -rjk[1] * rkl[2] + rjk[2] * rkl[1];
     rnk[1] = -rjk[2] * rkl[0] + rjk[0] * rkl[2];
     rnk[2] = -rjk[0] * rkl[1] + rjk[1] * rkl[0];
-    const double bj = sqrt(rnj[0] * rnj[0] + rnj[1] * rnj[1] + rnj[2] * rnj[2]);
-    const double bk = sqrt(rnk[0] * rnk[0] + rnk[1] * rnk[1] + rnk[2] * rnk[2]);
-    double scp = (rnj[0] * rnk[0] + rnj[1] * rnk[1] + rnj[2] * rnk[2]) / (bj * bk);
-    scp = fmin(1.0, fmax(-1.0, scp));
-    double phi = acos(scp);
-    const double sgn = rjk[0] * (rnj[1] * rnk[2] - rnj[2] * rnk[1]) + rjk[1] * (rnj[2] * rnk[0] - rnj[0] * rnk[2]) +
-                       rjk[2] * (rnj[0] * rnk[1] - rnj[1] * rnk[0]);
+    const R bj = sqrt(rnj[0] * rnj[0] + rnj[1] * rnj[1] + rnj[2] * rnj[2]);
+    const R bk = sqrt(rnk[0] * rnk[0] + rnk[1] * rnk[1] + rnk[2] * rnk[2]);
+    R scp = (rnj[0] * rnk[0] + rnj[1] * rnk[1] + rnj[2] * rnk[2]) / (bj * bk);
+    scp = fmin(R(1), fmax(R(-1), scp));
+    R phi = acos(scp);
+    const R sgn = rjk[0] * (rnj[1] * rnk[2] - rnj[2] * rnk[1]) + rjk[1] * (rnj[2] * rnk[0] - rnj[0] * rnk[2]) +
+                  rjk[2] * (rnj[0] * rnk[1] - rnj[1] * rnk[0]);
     if (sgn < 0) phi = -phi;
-    double f1 = sin(phi);
-    if (fabs(f1) < QREAL_EPS) f1 = QREAL_EPS;
-    f1 = -1.0 / f1;
-    double di[3], dl[3], rki[3], rlj[3];
-    for (int a = 0; a < 3; ++a) {
-        di[a] = f1 * (rnk[a] / (bj * bk) - scp * rnj[a] / (bj * bj));
-        dl[a] = f1 * (rnj[a] / (bj * bk) - scp * rnk[a] / (bk * bk));
-        rki[a] = rji[a] - rjk[a];
-        rlj[a] = -rjk[a] - rkl[a];
+    R f1 = sin(phi);
+    if (fabs(f1) < R(QREAL_EPS)) f1 = R(QREAL_EPS);
+    f1 = R(-1) / f1;
+    R di[3], dl[3], rki[3], rlj[3];
+    for (int q = 0; q < 3; ++q) {
+        di[q] = f1 * (rnk[q] / (bj * bk) - scp * rnj[q] / (bj * bj));
+        dl[q] = f1 * (rnj[q] / (bj * bk) - scp * rnk[q] / (bk * bk));
+        rki[q] = rji[q] - rjk[q];
+        rlj[q] = -rjk[q] - rkl[q];
     }
     dp[0] = rjk[1] * di[2] - rjk[2] * di[1];
     dp[1] = rjk[2] * di[0] - rjk[0] * di[2];
@@ -162,13 +213,70 @@ __device__ double dihedral(const DevSys &S, int i, int j, int k, int l, double d
     dp[11] = rjk[0] * dl[1] - rjk[1] * dl[0];
     return phi;
 }
-__device__ __forceinline__ void apply_dp(const DevSys &S, const int *at, double dv, const double dp[12]) {
-    for (int n = 0; n < 4; ++n) grad_add(S, at[n], dv * dp[3 * n], dv * dp[3 * n + 1], dv * dp[3 * n + 2]);
+// FP32 forms of the two above.  The reference's expressions divide by
+// sin(angle) after cancelling terms of size 1 (the component of one normal
+// along the other), which in FP32 loses every digit for planar torsions and
+// impropers.  The float path takes the same angles from atan2 (the same
+// value and sign convention: phi < 0 when rjk.(rnj x rnk) < 0) and the
+// dihedral gradient in the cancellation-free form of Blondel & Karplus,
+// J. Comput. Chem. 17, 1132 (1996): with b1 = rji, b2 = rjk, b3 = rkl,
+// m = b1 x b2, n = b3 x b2,
+//   dphi/dri = |b2|/|m|^2 m,   dphi/drl = -|b2|/|n|^2 n,
+//   dphi/drj = -gi + (b1.b2/|b2|^2) gi + (b3.b2/|b2|^2) gl,
+//   dphi/drk = -gl - (b1.b2/|b2|^2) gi - (b3.b2/|b2|^2) gl.
+template <>
+__device__ float angle_grad<float>(const DevSys &S, int i, int j, int k, float fk, float ang0, float scale, float gi[3],
+                                   float gk[3]) {
+    const V3<float> a = rel<float>(S, j, i), c = rel<float>(S, j, k);
+    const float bji = sqrtf(a.x * a.x + a.y * a.y + a.z * a.z), bjk = sqrtf(c.x * c.x + c.y * c.y + c.z * c.z);
+    const float cx = a.y * c.z - a.z * c.y, cy = a.z * c.x - a.x * c.z, cz = a.x * c.y - a.y * c.x;
+    const float sn = sqrtf(cx * cx + cy * cy + cz * cz), cs = a.x * c.x + a.y * c.y + a.z * c.z;
+    const float ang = atan2f(sn, cs), da = ang - ang0;
+    const float inv = 1.f / (bji * bjk);
+    const float scp = cs * inv;
+    float f1 = sn * inv;
+    if (f1 < (float)QREAL_EPS) f1 = (float)QREAL_EPS;
+    const float dvf = -fk * da * scale / f1;
+    const float rji[3] = {a.x, a.y, a.z}, rjk[3] = {c.x, c.y, c.z};
+    for (int q = 0; q < 3; ++q) {
+        gi[q] = dvf * (rjk[q] * inv - scp * rji[q] / (bji * bji));
+        gk[q] = dvf * (rji[q] * inv - scp * rjk[q] / (bjk * bjk));
+    }
+    return 0.5f * fk * da * da;
+}
+template <>
+__device__ float dihedral<float>(const DevSys &S, int i, int j, int k, int l, float dp[12]) {
+    const V3<float> b1 = rel<float>(S, j, i), b2 = rel<float>(S, j, k), b3 = rel<float>(S, k, l);
+    const float mx = b1.y * b2.z - b1.z * b2.y, my = b1.z * b2.x - b1.x * b2.z, mz = b1.x * b2.y - b1.y * b2.x;
+    const float nx = b3.y * b2.z - b3.z * b2.y, ny = b3.z * b2.x - b3.x * b2.z, nz = b3.x * b2.y - b3.y * b2.x;
+    const float mm = mx * mx + my * my + mz * mz, nn = nx * nx + ny * ny + nz * nz;
+    const float b22 = b2.x * b2.x + b2.y * b2.y + b2.z * b2.z, b2n = sqrtf(b22);
+    const float c = mx * nx + my * ny + mz * nz;
+    const float s = (b2.x * (my * nz - mz * ny) + b2.y * (mz * nx - mx * nz) + b2.z * (mx * ny - my * nx)) / b2n;
+    const float phi = atan2f(s, c);
+    const float fi = b2n / mm, fl = -b2n / nn;
+    const float gi[3] = {fi * mx, fi * my, fi * mz}, gl[3] = {fl * nx, fl * ny, fl * nz};
+    const float P = (b1.x * b2.x + b1.y * b2.y + b1.z * b2.z) / b22;
+    const float Q = (b3.x * b2.x + b3.y * b2.y + b3.z * b2.z) / b22;
+    for (int q = 0; q < 3; ++q) {
+        dp[q] = gi[q];
+        dp[3 + q] = -gi[q] + P * gi[q] + Q * gl[q];
+        dp[6 + q] = -gl[q] - P * gi[q] - Q * gl[q];
+        dp[9 + q] = gl[q];
+    }
+    return phi;
+}
+
+template <typename R>
+__device__ __forceinline__ void apply_dp(const DevSys &S, const int *at, R dv, const R dp[12]) {
+    for (int n = 0; n < 4; ++n) P<R>::grad(S, at[n], dv * dp[3 * n], dv * dp[3 * n + 1], dv * dp[3 * n + 2]);
 }
 
 // qbond/qangle/qtorsion/qimproper (src/md.f90:17022-17538) without EVB
 // angle/torsion couplings.  One thread per (term, state).
+template <typename R>
 __device__ void qbonded_block(const DevSys &S, int b) {
+    typedef P<R> p;
     const int id = b * blockDim.x + threadIdx.x;
     const int term = id / QG_MAXS, s = id % QG_MAXS;
     if (term >= S.nqt) return;
@@ -177,157 +285,189 @@ __device__ void qbonded_block(const DevSys &S, int b) {
     if (s >= T.nstates) return;
     const int ic = S.qt_cod[term * QG_MAXS + s];
     if (ic <= 0) return;
-    const double *L = S.qt_lib + 4 * (ic - 1);
+    const auto *L = p::qt_lib(S) + 4 * (ic - 1);
     const int *at = S.qt_atoms + 4 * term;
-    const double lam = T.lambda[s];
+    const R lam = p::lambda(T, s);
     const int kind = S.qt_kind[term];
-    double e = 0;
+    R e = 0;
     int slot = EA_Q0 + EQ_N * s;
-    const double pi = 3.14159265358979323846;
+    const R pi = R(3.14159265358979323846);
     if (kind == 0) {
         const int i = at[0], j = at[1];
-        const double r0 = S.x[3 * j] - S.x[3 * i], r1 = S.x[3 * j + 1] - S.x[3 * i + 1], r2 = S.x[3 * j + 2] - S.x[3 * i + 2];
-        const double b = sqrt(r0 * r0 + r1 * r1 + r2 * r2), db = b - L[2];
-        const double fexp = exp(-L[1] * db);
-        e = L[0] * (fexp * fexp - 2.0 * fexp) + 0.5 * L[3] * db * db;
-        const double dv = (2.0 * L[0] * L[1] * (fexp - fexp * fexp) + L[3] * db) * lam / b;
-        grad_add(S, j, r0 * dv, r1 * dv, r2 * dv);
-        grad_add(S, i, -r0 * dv, -r1 * dv, -r2 * dv);
+        const V3<R> r = rel<R>(S, i, j);
+        const R bl = sqrt(r.x * r.x + r.y * r.y + r.z * r.z), db = bl - L[2];
+        const R fexp = exp(-L[1] * db);
+        e = L[0] * (fexp * fexp - R(2) * fexp) + R(0.5) * L[3] * db * db;
+        const R dv = (R(2) * L[0] * L[1] * (fexp - fexp * fexp) + L[3] * db) * lam / bl;
+        p::grad(S, j, r.x * dv, r.y * dv, r.z * dv);
+        p::grad(S, i, -r.x * dv, -r.y * dv, -r.z * dv);
         slot += EQ_B;
     } else if (kind == 1) {
-        double gi[3], gk[3];
-        e = angle_grad(S, at[0], at[1], at[2], L[0], L[1], lam, gi, gk);
-        grad_add(S, at[0], gi[0], gi[1], gi[2]);
-        grad_add(S, at[2], gk[0], gk[1], gk[2]);
-        grad_add(S, at[1], -(gi[0] + gk[0]), -(gi[1] + gk[1]), -(gi[2] + gk[2]));
+        R gi[3], gk[3];
+        e = angle_grad<R>(S, at[0], at[1], at[2], L[0], L[1], lam, gi, gk);
+        p::grad(S, at[0], gi[0], gi[1], gi[2]);
+        p::grad(S, at[2], gk[0], gk[1], gk[2]);
+        p::grad(S, at[1], -(gi[0] + gk[0]), -(gi[1] + gk[1]), -(gi[2] + gk[2]));
         slot += EQ_A;
     } else if (kind == 2) {
-        double dp[12];
-        const double phi = dihedral(S, at[0], at[1], at[2], at[3], dp);
-        const double arg = L[1] * phi - L[2];
-        e = L[0] * (1.0 + cos(arg));
-        apply_dp(S, at, -L[1] * L[0] * sin(arg) * lam, dp);
+        R dp[12];
+        const R phi = dihedral<R>(S, at[0], at[1], at[2], at[3], dp);
+        const R arg = L[1] * phi - L[2];
+        e = L[0] * (R(1) + cos(arg));
+        apply_dp<R>(S, at, -L[1] * L[0] * sin(arg) * lam, dp);
         slot += EQ_T;
     } else {
-        double dp[12];
-        const double phi = dihedral(S, at[0], at[1], at[2], at[3], dp);
-        double arg = phi - L[1];
-        arg = arg - 2.0 * pi * rint(arg / (2.0 * pi));
-        const double dv = L[0] * arg;
-        e = 0.5 * dv * arg;
-        apply_dp(S, at, dv * lam, dp);
+        R dp[12];
+        const R phi = dihedral<R>(S, at[0], at[1], at[2], at[3], dp);
+        R arg = phi - L[1];
+        arg = arg - R(2) * pi * rint(arg / (R(2) * pi));
+        const R dv = L[0] * arg;
+        e = R(0.5) * dv * arg;
+        apply_dp<R>(S, at, dv * lam, dp);
         slot += EQ_I;
     }
-    fx_add(S.eacc + (size_t)traj * QG_NE + slot, e, S.status);
+    const long long q = p::fx(e, S.status);
+    if (q) atomicAdd(S.eacc + (size_t)traj * QG_NE + slot, (unsigned long long)q);
 }
 
 // bond/angle/torsion/improper(2), src/md.f90:1130-1405, 3130-3423,
 // 17907-18054.  Terms are grouped per (trajectory, energy slot) and padded to
 // whole blocks, so each block reduces into one slot.
-__device__ void bonded_block(const DevSys &S, int b, double *red) {
+template <typename R>
+__device__ void bonded_block(const DevSys &S, int b, Red &red) {
+    typedef P<R> p;
     const int id = b * blockDim.x + threadIdx.x;
-    const int traj = S.bt_blk_traj[b], slot = S.bt_blk_slot[b];
+    const int traj = S.bt_blk_traj[b];
     const int c = S.bt_cod[id];
-    double e = 0;
-    const double pi = 3.14159265358979323846;
+    R e = 0;
+    const R pi = R(3.14159265358979323846);
     if (c >= 0) {
         const int *at = S.bt_atoms + 4 * id;
-        const double *L = S.bt_lib + 4 * c;
+        const auto *L = p::bt_lib(S) + 4 * c;
         const int kind = S.bt_kind[id];
         if (kind == 0) {
             const int i = at[0], j = at[1];
-            const double r0 = S.x[3 * j] - S.x[3 * i], r1 = S.x[3 * j + 1] - S.x[3 * i + 1], r2 = S.x[3 * j + 2] - S.x[3 * i + 2];
-            const double b = sqrt(r0 * r0 + r1 * r1 + r2 * r2), db = b - L[1];
-            e = 0.5 * L[0] * db * db;
-            const double dv = L[0] * db / b;
-            grad_add(S, j, r0 * dv, r1 * dv, r2 * dv);
-            grad_add(S, i, -r0 * dv, -r1 * dv, -r2 * dv);
+            const V3<R> r = rel<R>(S, i, j);
+            const R bl = sqrt(r.x * r.x + r.y * r.y + r.z * r.z), db = bl - L[1];
+            e = R(0.5) * L[0] * db * db;
+            const R dv = L[0] * db / bl;
+            p::grad(S, j, r.x * dv, r.y * dv, r.z * dv);
+            p::grad(S, i, -r.x * dv, -r.y * dv, -r.z * dv);
         } else if (kind == 1) {
-            double gi[3], gk[3];
-            e = angle_grad(S, at[0], at[1], at[2], L[0], L[1], 1.0, gi, gk);
-            grad_add(S, at[0], gi[0], gi[1], gi[2]);
-            grad_add(S, at[2], gk[0], gk[1], gk[2]);
-            grad_add(S, at[1], -(gi[0] + gk[0]), -(gi[1] + gk[1]), -(gi[2] + gk[2]));
+            R gi[3], gk[3];
+            e = angle_grad<R>(S, at[0], at[1], at[2], L[0], L[1], R(1), gi, gk);
+            p::grad(S, at[0], gi[0], gi[1], gi[2]);
+            p::grad(S, at[2], gk[0], gk[1], gk[2]);
+            p::grad(S, at[1], -(gi[0] + gk[0]), -(gi[1] + gk[1]), -(gi[2] + gk[2]));
         } else if (kind == 2) {
-            double dp[12];
-            const double phi = dihedral(S, at[0], at[1], at[2], at[3], dp);
-            const double arg = L[1] * phi - L[2];
-            e = L[0] * (1.0 + cos(arg)) * L[3];
-            apply_dp(S, at, -L[1] * L[0] * sin(arg) * L[3], dp);
+            R dp[12];
+            const R phi = dihedral<R>(S, at[0], at[1], at[2], at[3], dp);
+            const R arg = L[1] * phi - L[2];
+            e = L[0] * (R(1) + cos(arg)) * L[3];
+            apply_dp<R>(S, at, -L[1] * L[0] * sin(arg) * L[3], dp);
         } else if (kind == 3) {
-            double dp[12];
-            const double phi = dihedral(S, at[0], at[1], at[2], at[3], dp);
-            double arg = phi - L[1];
-            arg = arg - 2.0 * pi * rint(arg / (2.0 * pi));
-            const double dv = L[0] * arg;
-            e = 0.5 * dv * arg;
-            apply_dp(S, at, dv, dp);
+            R dp[12];
+            const R phi = dihedral<R>(S, at[0], at[1], at[2], at[3], dp);
+            R arg = phi - L[1];
+            arg = arg - R(2) * pi * rint(arg / (R(2) * pi));
+            const R dv = L[0] * arg;
+            e = R(0.5) * dv * arg;
+            apply_dp<R>(S, at, dv, dp);
         } else {
-            double dp[12];
-            const double phi = dihedral(S, at[0], at[1], at[2], at[3], dp);
-            const double arg = 2.0 * phi - L[1];
-            e = L[0] * (1.0 + cos(arg));
-            apply_dp(S, at, -2.0 * L[0] * sin(arg), dp);
+            R dp[12];
+            const R phi = dihedral<R>(S, at[0], at[1], at[2], at[3], dp);
+            const R arg = R(2) * phi - L[1];
+            e = L[0] * (R(1) + cos(arg));
+            apply_dp<R>(S, at, R(-2) * L[0] * sin(arg), dp);
         }
     }
-    block_energy_d(S, traj, slot, e, red);
+    const int slots[1] = {S.bt_blk_slot[b]};
+    long long v[1] = {p::fx(e, S.status)};
+    block_energies_fx<1>(S.eacc + (size_t)traj * QG_NE, slots, v, red);
 }
 
 // fix_shell, src/md.f90:2816-2864 (no freeze).  One thread per solute atom.
-__device__ void fix_shell_block(const DevSys &S, int b, const int *satom, double *red) {
+template <typename R>
+__device__ void fix_shell_block(const DevSys &S, int b, const int *satom, Red &red) {
+    typedef P<R> p;
     const int i = satom[b * blockDim.x + threadIdx.x];
     const int traj = i < 0 ? -1 - i : S.atraj[i];
     const TrajInfo &T = S.traj[traj];
-    double efix = 0, eshell = 0;
+    R efix = 0, eshell = 0;
     if (i >= 0 && (S.aexcl[i] || S.ashell[i])) {
-        const double fk = S.aexcl[i] ? T.fk_fix : T.fk_pshell;
-        const double d0 = S.x[3 * i] - S.xtop[3 * i], d1 = S.x[3 * i + 1] - S.xtop[3 * i + 1], d2 = S.x[3 * i + 2] - S.xtop[3 * i + 2];
-        const double e = 0.5 * fk * (d0 * d0 + d1 * d1 + d2 * d2);
+        R fk, d0, d1, d2;
+        if (sizeof(R) == 8) {
+            fk = S.aexcl[i] ? R(T.fk_fix) : R(T.fk_pshell);
+            d0 = R(S.x[3 * i] - S.xtop[3 * i]); d1 = R(S.x[3 * i + 1] - S.xtop[3 * i + 1]);
+            d2 = R(S.x[3 * i + 2] - S.xtop[3 * i + 2]);
+        } else {
+            fk = S.aexcl[i] ? R(T.fk_fixf) : R(T.fk_pshellf);
+            const float3 d = dpos(S.xtoph[i], S.xtopl[i], S.pos[i], S.poslo[i]);
+            d0 = R(d.x); d1 = R(d.y); d2 = R(d.z);
+        }
+        const R e = R(0.5) * fk * (d0 * d0 + d1 * d1 + d2 * d2);
         if (S.aexcl[i]) efix = e;
         if (S.ashell[i]) eshell = e;
-        grad_add(S, i, fk * d0, fk * d1, fk * d2);
+        p::grad(S, i, fk * d0, fk * d1, fk * d2);
     }
-    block_energy_d(S, traj, EA_RST_FIX, efix, red);
-    block_energy_d(S, traj, EA_RST_SHELL, eshell, red);
+    const int slots[2] = {EA_RST_FIX, EA_RST_SHELL};
+    long long v[2] = {p::fx(efix, S.status), p::fx(eshell, S.status)};
+    block_energies_fx<2>(S.eacc + (size_t)traj * QG_NE, slots, v, red);
 }
 
-// restrain_solvent, src/md.f90:18055-18102.  One thread per water.
-__device__ void restrain_solvent_block(const DevSys &S, int b, const int *wgrp, double *red) {
+// restrain_solvent, src/md.f90:18055-18102.  One thread per water.  The shift
+// sqrt(Boltz*Tfree/fk_wsphere) is formed by k_finalize with the temperature.
+template <typename R>
+__device__ void restrain_solvent_block(const DevSys &S, int b, const int *wgrp, Red &red) {
+    typedef P<R> p;
     const int w = wgrp[b * blockDim.x + threadIdx.x];
     const int traj = w < 0 ? -1 - w : S.g_traj[w];
     const TrajInfo &T = S.traj[traj];
-    double erst = 0;
+    R erst = 0;
     if (w >= 0) {
         const int i = S.g_switch[w];
         if (!S.aexcl[i]) {
-            const double Tfree = S.tstate[traj].Tfree;
-            const double shift = T.fk_wsphere != 0.0 ? sqrt(BOLTZ * Tfree / T.fk_wsphere) : 0.0;
-            const double d0 = S.x[3 * i] - T.xwcent[0], d1 = S.x[3 * i + 1] - T.xwcent[1], d2 = S.x[3 * i + 2] - T.xwcent[2];
-            const double b = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-            const double db = b - (T.rwat - shift);
-            double dv;
+            R d0, d1, d2, fk, rwat, Dwmz, awmz, shift;
+            if (sizeof(R) == 8) {
+                d0 = R(S.x[3 * i] - T.xwcent[0]); d1 = R(S.x[3 * i + 1] - T.xwcent[1]);
+                d2 = R(S.x[3 * i + 2] - T.xwcent[2]);
+                fk = R(T.fk_wsphere); rwat = R(T.rwat); Dwmz = R(T.Dwmz); awmz = R(T.awmz);
+                shift = R(S.tstate[traj].wshift);
+            } else {
+                // the float coordinates are relative to the origin, which is xwcent
+                const float4 h = S.pos[i], l = S.poslo[i];
+                d0 = R(h.x + l.x); d1 = R(h.y + l.y); d2 = R(h.z + l.z);
+                fk = R(T.fk_wspheref); rwat = R(T.rwatf); Dwmz = R(T.Dwmzf); awmz = R(T.awmzf);
+                shift = R(S.tstate[traj].wshiftf);
+            }
+            const R bl = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+            const R db = bl - (rwat - shift);
+            R dv;
             if (db > 0) {
-                erst = 0.5 * T.fk_wsphere * db * db - T.Dwmz;
-                dv = T.fk_wsphere * db / b;
-            } else if (b > 0.0) {
-                const double fexp = exp(T.awmz * db);
-                erst = T.Dwmz * (fexp * fexp - 2.0 * fexp);
-                dv = -2.0 * T.Dwmz * T.awmz * (fexp - fexp * fexp) / b;
+                erst = R(0.5) * fk * db * db - Dwmz;
+                dv = fk * db / bl;
+            } else if (bl > R(0)) {
+                const R fexp = exp(awmz * db);
+                erst = Dwmz * (fexp * fexp - R(2) * fexp);
+                dv = R(-2) * Dwmz * awmz * (fexp - fexp * fexp) / bl;
             } else { dv = 0; erst = 0; }
-            grad_add(S, i, dv * d0, dv * d1, dv * d2);
+            p::grad(S, i, dv * d0, dv * d1, dv * d2);
         }
     }
-    block_energy_d(S, traj, EA_RST_RAD, erst, red);
+    const int slots[1] = {EA_RST_RAD};
+    long long v[1] = {p::fx(erst, S.status)};
+    block_energies_fx<1>(S.eacc + (size_t)traj * QG_NE, slots, v, red);
 }
 
-// offdiag, src/md.f90:15444-15470: Hij = A exp(-mu r_kl).
+// offdiag, src/md.f90:15444-15470: Hij = A exp(-mu r_kl).  Its only consumer is
+// the energy record, so it runs on the FP64 (recorded / drop-in) evaluations.
 __device__ void offdiag_block(const DevSys &S, int blk) {
     const int k = blk * blockDim.x + threadIdx.x;
     if (k >= S.nod) return;
     const int traj = S.od_traj[k];
     const int a = S.q_atom[S.od_kl[2 * k]], b = S.q_atom[S.od_kl[2 * k + 1]];
-    const double d0 = S.x[3 * b] - S.x[3 * a], d1 = S.x[3 * b + 1] - S.x[3 * a + 1], d2 = S.x[3 * b + 2] - S.x[3 * a + 2];
-    const double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    const V3<double> d = rel<double>(S, a, b);
+    const double r = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
     const int slot = S.od_ij[2 * k];   // index of the coupling within its trajectory
     double *o = S.od_out + ((size_t)traj * QG_MAXOD + slot) * 2;
     o[0] = S.od_Amu[2 * k] * exp(-S.od_Amu[2 * k + 1] * r);
@@ -339,26 +479,35 @@ struct MiscPlan {
     int nqq, nbt, nfix, nrad, nqb, nod;    // blocks per term
 };
 
-__global__ void __launch_bounds__(QG_BLOCK) k_misc(DevSys S, MiscPlan P, const int *qq_traj, const int *qq_s,
-                                                   const int *satom, const int *wgrp) {
-    __shared__ double red[QG_BLOCK / 32];
+template <typename R>
+__device__ __forceinline__ void misc_body(const DevSys &S, const MiscPlan &P, const int *qq_traj, const int *qq_s,
+                                          const int *satom, const int *wgrp, Red &red) {
     int b = blockIdx.x;
-    if (b < P.nqq) { qq_block(S, b, qq_traj, qq_s, red); return; }
+    if (b < P.nqq) { qq_block<R>(S, b, qq_traj, qq_s, red); return; }
     b -= P.nqq;
-    if (b < P.nbt) { bonded_block(S, b, red); return; }
+    if (b < P.nbt) { bonded_block<R>(S, b, red); return; }
     b -= P.nbt;
-    if (b < P.nfix) { fix_shell_block(S, b, satom, red); return; }
+    if (b < P.nfix) { fix_shell_block<R>(S, b, satom, red); return; }
     b -= P.nfix;
-    if (b < P.nrad) { restrain_solvent_block(S, b, wgrp, red); return; }
+    if (b < P.nrad) { restrain_solvent_block<R>(S, b, wgrp, red); return; }
     b -= P.nrad;
-    if (b < P.nqb) { qbonded_block(S, b); return; }
+    if (b < P.nqb) { qbonded_block<R>(S, b); return; }
     b -= P.nqb;
-    if (b < P.nod) { offdiag_block(S, b); return; }
+    if (sizeof(R) == 8 && b < P.nod) offdiag_block(S, b);
+}
+
+__global__ void __launch_bounds__(QG_BLOCK) k_misc(DevSys S, MiscPlan P, const int *qq_traj, const int *qq_s,
+                                                   const int *satom, const int *wgrp, EaccSel esel) {
+    __shared__ Red red;
+    bool acc = esel.mode == EACC_FP64;
+    if (esel.mode == EACC_RECORD) acc = esel.ene_every > 0 && ((esel.recctl[0] + esel.k) % esel.ene_every) == 0;
+    if (acc) misc_body<double>(S, P, qq_traj, qq_s, satom, wgrp, red);
+    else misc_body<float>(S, P, qq_traj, qq_s, satom, wgrp, red);
 }
 
 static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
-void launch_misc(const DevSys &S, const BlockTables &B, LaunchCtx &L, int terms) {
+void launch_misc(const DevSys &S, const BlockTables &B, LaunchCtx &L, int terms, EaccSel e) {
     MiscPlan P{};
     P.nqq = (terms & QGPU_TERMS_QQ) ? B.nqqblk : 0;
     P.nbt = (terms & QGPU_TERMS_BONDED) ? S.nbt / QG_BLOCK : 0;
@@ -369,7 +518,7 @@ void launch_misc(const DevSys &S, const BlockTables &B, LaunchCtx &L, int terms)
     const int nb = P.nqq + P.nbt + P.nfix + P.nrad + P.nqb + P.nod;
     if (!nb) return;
     prof_begin(L, "k_misc");
-    k_misc<<<nb, QG_BLOCK, 0, L.stream>>>(S, P, B.qqblk_traj, B.qqblk_s, B.satom, B.wgrp);
+    k_misc<<<nb, QG_BLOCK, 0, L.stream>>>(S, P, B.qqblk_traj, B.qqblk_s, B.satom, B.wgrp, e);
     prof_end(L);
     (*L.nlaunch)++;
 }

@@ -84,6 +84,9 @@ struct qgpu_handle {
     int lists_built = 0, temp_init = 0, any_shake = 0, any_wpol = 0;
     std::vector<char> fused;   // per trajectory: SHAKE fused into the update kernel
     bool all_fused = true;
+    // 0: x/v and the float coordinates agree; 1: the float master (fused
+    // steps) is newer than x/v
+    int master = 0;
     long long step = 0;
     cudaGraphExec_t graph = nullptr;
     long long graph_nodes = 0;
@@ -209,8 +212,12 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         }
         T.rwat = d.rwat; T.fk_wsphere = d.fk_wsphere; T.Dwmz = d.Dwmz; T.awmz = d.awmz;
         T.fk_pshell = d.fk_pshell; T.fk_fix = d.fk_fix;
+        T.fk_wspheref = (float)d.fk_wsphere; T.rwatf = (float)d.rwat; T.Dwmzf = (float)d.Dwmz; T.awmzf = (float)d.awmz;
+        T.fk_pshellf = (float)d.fk_pshell; T.fk_fixf = (float)d.fk_fix;
         for (int s = 0; s < QG_MAXS; ++s) T.lambda[s] = s < S ? d.lambda[s] : 0.0;
+        for (int s = 0; s < QG_MAXS; ++s) T.lambdaf[s] = (float)T.lambda[s];
         T.dt = d.dt; T.Temp0 = d.Temp0; T.tau_T = d.tau_T; T.inv_dt = 1.0 / d.dt;
+        T.dtf = (float)T.dt; T.inv_dtf = (float)T.inv_dt;
         T.separate_scaling = d.separate_scaling; T.detail_temps = d.detail_temps;
         T.Ndegf = d.Ndegf; T.Ndegfree = d.Ndegfree;
         T.Ndegfree_solute = d.Ndegfree_solute; T.Ndegfree_solvent = d.Ndegfree_solvent;
@@ -515,7 +522,10 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     if ((rc = upload(A, h->info, &ti))) return rc;
     S.traj = ti;
     std::vector<TrajState> tsh(ntraj);
-    for (auto &q : tsh) { q.Tscale_solute = q.Tscale_solvent = 1.0; q.Temp = q.Tfree = q.Ekin = 0; q.shake_iters = 0; }
+    for (auto &q : tsh) {
+        q.Tscale_solute = q.Tscale_solvent = 1.0; q.Temp = q.Tfree = q.Ekin = 0; q.shake_iters = 0;
+        q.tsf_solute = q.tsf_solvent = 1.f; q.wshift = 0.0; q.wshiftf = 0.f;
+    }
     if ((rc = upload(A, tsh, &ts))) return rc;
     S.tstate = ts;
 #define UP(vec, field)                                            \
@@ -528,6 +538,34 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     if ((rc = alloc0(A, (size_t)3 * atom0, &S.xx))) return rc;
     UP(pos, pos);
     if ((rc = alloc0(A, (size_t)atom0, &S.poslo))) return rc;
+    if ((rc = alloc0(A, (size_t)atom0, &S.velf))) return rc;
+    {
+        // float copies for the per-step kernels; topology coordinates as hi/lo
+        // offsets from each trajectory's origin
+        std::vector<float> winvf(winv.begin(), winv.end()), massf(mass_atom.begin(), mass_atom.end());
+        std::vector<float4> xth(atom0), xtl(atom0);
+        for (int t = 0; t < ntraj; ++t)
+            for (int i = h->atom0[t]; i < h->atom0[t] + h->natom[t]; ++i) {
+                float r[3], e[3];
+                for (int c = 0; c < 3; ++c) {
+                    const double d = xtop[3 * (size_t)i + c] - h->info[t].origin[c];
+                    r[c] = (float)d;
+                    e[c] = (float)(d - (double)r[c]);
+                }
+                xth[i] = make_float4(r[0], r[1], r[2], 0.f);
+                xtl[i] = make_float4(e[0], e[1], e[2], 0.f);
+            }
+        UP(winvf, winvf); UP(massf, massf); UP(xth, xtoph); UP(xtl, xtopl);
+        std::vector<float2> d2hl(shk_d2.size());
+        for (size_t c = 0; c < shk_d2.size(); ++c) {
+            const float hi = (float)shk_d2[c];
+            d2hl[c] = make_float2(hi, (float)(shk_d2[c] - (double)hi));
+        }
+        UP(d2hl, shk_d2hl);
+        std::vector<float> qq_elsf(qq_els.begin(), qq_els.end()), qt_libf(qt_lib.begin(), qt_lib.end()),
+            bt_libf(bt_lib.begin(), bt_lib.end());
+        UP(qq_elsf, qq_elsf); UP(qt_libf, qt_libf); UP(bt_libf, bt_libf);
+    }
     UP(atype, atype); UP(aq, aq); UP(aexcl, aexcl); UP(ashell, ashell); UP(atraj, atraj); UP(agrp, agrp);
     if ((rc = alloc0(A, (size_t)3 * atom0, &S.fx))) return rc;
     UP(exmask, exmask); UP(p14mask, p14mask); UP(exl_first, exlong_first); UP(exl_j, exlong_j); UP(exl_kind, exlong_kind);
@@ -535,6 +573,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     UP(g_start, g_start); UP(g_atoms, g_atoms); UP(g_switch, g_switch); UP(g_kind, g_kind); UP(g_traj, g_traj);
     UP(g_excl, g_excl); UP(tile_g0, tile_g0); UP(tile_g1, tile_g1);
     if ((rc = alloc0(A, (size_t)3 * grp0, &S.g_cent))) return rc;
+    if ((rc = alloc0(A, (size_t)grp0, &S.g_centf))) return rc;
     if ((rc = alloc0(A, (size_t)QG_NLRF * grp0, &S.g_phi))) return rc;
     if ((rc = alloc0(A, (size_t)QG_NPHI * grp0, &S.g_phif))) return rc;
     if ((rc = alloc0(A, (size_t)grp0, &S.nb_count))) return rc;
@@ -611,6 +650,14 @@ static int check_status(qgpu_handle *h) {
     return fail(QGPU_E_CUDA, "device status %d", st);
 }
 
+// Refreshes x/v from the float master after fused steps (API reads, list
+// builds and FP64 evaluations read x/v).
+static void ensure_double(qgpu_handle *h, LaunchCtx &L) {
+    if (h->master == 1) launch_sync_double(h->S, h->B, L);
+    h->master = 0;
+}
+static void after_steps(qgpu_handle *h) { h->master = h->all_fused ? 1 : 0; }
+
 static void list_ops(qgpu_handle *h, LaunchCtx &L) {
     launch_centers(h->S, h->B, L);
     launch_scan(h->S, h->B, L);
@@ -626,7 +673,7 @@ static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, bool fp64_energy,
         launch_qw(h->S, h->B, L, esel);
         launch_qp(h->S, h->B, L, esel);
     }
-    launch_misc(h->S, h->B, L, terms);
+    launch_misc(h->S, h->B, L, terms, esel);
 }
 
 static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every);
@@ -660,7 +707,7 @@ static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every) {
     EaccSel esel{EACC_RECORD, h->recctl_d, k, ene_every};
     force_ops(h, L, QGPU_TERMS_ALL, false, esel);
     if (h->all_fused) {
-        launch_update(h->S, h->B, L, 1);
+        launch_update_f(h->S, h->B, L, esel, h->NBcycle);
     } else {
         launch_integrate(h->S, h->B, L);
         launch_shake(h->S, h->B, L, -1);
@@ -707,9 +754,10 @@ int64_t qgpu_kernel_launches(const qgpu_handle *h) { return h ? h->nlaunch : 0; 
 int qgpu_set_coords(qgpu_handle *h, int32_t traj, const double *x, const double *v) {
     if (!h || traj < 0 || traj >= h->ntraj) return fail(QGPU_E_INVALID, "bad trajectory index");
     size_t off = 3 * (size_t)h->atom0[traj], n = 3 * (size_t)h->natom[traj];
+    LaunchCtx L{h->stream, &h->nlaunch};
+    ensure_double(h, L);
     if (x) CK(cudaMemcpyAsync(h->S.x + off, x, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (v) CK(cudaMemcpyAsync(h->S.v + off, v, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    LaunchCtx L{h->stream, &h->nlaunch};
     launch_mirror(h->S, h->B, L);
     CK(cudaStreamSynchronize(h->stream));
     return 0;
@@ -718,6 +766,8 @@ int qgpu_set_coords(qgpu_handle *h, int32_t traj, const double *x, const double 
 int qgpu_get_coords(qgpu_handle *h, int32_t traj, double *x, double *v) {
     if (!h || traj < 0 || traj >= h->ntraj) return fail(QGPU_E_INVALID, "bad trajectory index");
     size_t off = 3 * (size_t)h->atom0[traj], n = 3 * (size_t)h->natom[traj];
+    LaunchCtx L{h->stream, &h->nlaunch};
+    ensure_double(h, L);
     if (x) CK(cudaMemcpyAsync(x, h->S.x + off, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     if (v) CK(cudaMemcpyAsync(v, h->S.v + off, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -727,6 +777,7 @@ int qgpu_get_coords(qgpu_handle *h, int32_t traj, double *x, double *v) {
 int qgpu_build_lists(qgpu_handle *h) {
     if (!h) return fail(QGPU_E_INVALID, "null handle");
     LaunchCtx L{h->stream, &h->nlaunch};
+    ensure_double(h, L);
     list_ops(h, L);
     h->lists_built = 1;
     return check_status(h);
@@ -742,8 +793,12 @@ int qgpu_forces(qgpu_handle *h, int32_t traj, int32_t terms, double *d, qgpu_ene
     if (!h || traj < 0 || traj >= h->ntraj) return fail(QGPU_E_INVALID, "bad trajectory index");
     if (!h->lists_built) return fail(QGPU_E_INVALID, "qgpu_forces before qgpu_build_lists");
     LaunchCtx L{h->stream, &h->nlaunch};
+    ensure_double(h, L);
     CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
-    force_ops(h, L, terms, true, EaccSel{EACC_FP64, h->zero_d, 0, 1});
+    if (terms & QGPU_TERMS_STEP_PRECISION)
+        force_ops(h, L, terms, false, EaccSel{EACC_FP32, h->zero_d, 0, 1});
+    else
+        force_ops(h, L, terms, true, EaccSel{EACC_FP64, h->zero_d, 0, 1});
     launch_finalize(h->S, L, 0, h->ecur_d, h->zero_d, 0, 1, 1);
     std::vector<double> row(QG_REC);
     CK(cudaMemcpyAsync(row.data(), h->ecur_d + (size_t)traj * QG_REC, QG_REC * sizeof(double), cudaMemcpyDeviceToHost,
@@ -760,10 +815,11 @@ int qgpu_forces(qgpu_handle *h, int32_t traj, int32_t terms, double *d, qgpu_ene
 int qgpu_shake(qgpu_handle *h, int32_t traj, const double *xx, double *x, int32_t *niter) {
     if (!h || traj < 0 || traj >= h->ntraj || !xx || !x) return fail(QGPU_E_INVALID, "bad arguments");
     size_t off = 3 * (size_t)h->atom0[traj], n = 3 * (size_t)h->natom[traj];
+    LaunchCtx L{h->stream, &h->nlaunch};
+    ensure_double(h, L);
     CK(cudaMemcpyAsync(h->S.xx + off, xx, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->S.x + off, x, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemsetAsync(&h->S.tstate[traj].shake_iters, 0, sizeof(int), h->stream));
-    LaunchCtx L{h->stream, &h->nlaunch};
     launch_shake(h->S, h->B, L, traj);
     launch_mirror(h->S, h->B, L);
     CK(cudaMemcpyAsync(x, h->S.x + off, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -862,12 +918,14 @@ int qgpu_profile(qgpu_handle *h, int32_t nsteps, char *names, double *ms, int64_
     const int ene_every = 1 << 30;
     int ctl[2] = {(int)h->step, (int)((h->step + ene_every - 1) / ene_every)};
     CK(cudaMemcpyAsync(h->recctl_d, ctl, sizeof ctl, cudaMemcpyHostToDevice, h->stream));
+    ensure_double(h, L);
     for (int k = 0; k < nsteps; ++k) {
         if (h->step % h->NBcycle == 0) { list_ops(h, L); h->lists_built = 1; }
         step_ops(h, L, 0, ene_every);
         launch_tick(L, h->recctl_d, 1);
         h->step += 1;
     }
+    after_steps(h);
     CK(cudaStreamSynchronize(h->stream));
     std::map<std::string, std::pair<double, long long>> acc;
     for (auto &r : P.recs) {
@@ -904,6 +962,7 @@ int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every) {
         CK(cudaMalloc(&h->rec_d, (size_t)256 * h->ntraj * QG_REC * sizeof(double)));
         h->rec_cap = 256;
     }
+    ensure_double(h, L);
     if (!h->temp_init) {
         CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
         CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
@@ -925,6 +984,7 @@ int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every) {
             h->step += 1;
         }
     }
+    after_steps(h);
     return 0;
 }
 
@@ -953,6 +1013,7 @@ int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink si
     int row0 = ctl[1];
     CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
     CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
+    ensure_double(h, L);
     if (!h->temp_init) {
         // temperature() before the first step (md_run, src/md.f90:6395-6398)
         launch_update(h->S, h->B, L, 0);
@@ -996,6 +1057,7 @@ int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink si
             h->step += 1;
         }
     }
+    after_steps(h);
     if (int rc = check_status(h)) return rc;
     flush(h->step);
     return check_status(h);

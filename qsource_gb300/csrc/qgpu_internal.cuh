@@ -71,7 +71,11 @@ struct TrajInfo {
     double xpcent[3], xwcent[3];
     double rwat, fk_wsphere, Dwmz, awmz, fk_pshell, fk_fix;
     double lambda[QG_MAXS];
+    float lambdaf[QG_MAXS];
     double dt, Temp0, tau_T, inv_dt;
+    float dtf, inv_dtf;
+    // float copies of the restraint parameters for the per-step kernels
+    float fk_wspheref, rwatf, Dwmzf, awmzf, fk_pshellf, fk_fixf;
     int separate_scaling, detail_temps;
     int Ndegf, Ndegfree, Ndegfree_solute, Ndegfree_solvent;
     int shake_mol0, nshake_mol;
@@ -90,7 +94,9 @@ struct TrajState {
     double Tscale_solute, Tscale_solvent, Temp, Tfree;
     double Ekin;
     int shake_iters;
-    int pad;
+    float tsf_solute, tsf_solvent;  // float copies of the Berendsen scales
+    float wshiftf;                  // sqrt(Boltz*Tfree/fk_wsphere), restrain_solvent
+    double wshift;
 };
 
 struct DevSys {
@@ -102,6 +108,13 @@ struct DevSys {
     double *x, *v, *xx;
     const double *xtop, *winv, *mass;
     float4 *pos, *poslo;            // hi part + charge, lo part
+    // The fused MD path keeps its master state in float: pos/poslo as a
+    // double-float (about 48 significant bits) relative to the trajectory
+    // origin, and float velocities.  x/v are refreshed from it when a step
+    // or an API call reads them (see k_update_f and k_sync_double).
+    float4 *velf;
+    const float *winvf, *massf;
+    const float4 *xtoph, *xtopl;    // topology coordinates relative to the origin, hi/lo
     const int *atype;               // global type index
     const double *crg_d;            // scaled charges (FP64)
     const int *aq;                  // global Q index or -1
@@ -118,6 +131,7 @@ struct DevSys {
     const int *g_start, *g_atoms, *g_switch, *g_kind, *g_traj;
     const uint8_t *g_excl;
     double *g_cent;                 // 3*G
+    float4 *g_centf;                // centre - origin in float (per list build)
     double *g_phi;                  // QG_NLRF*G accumulators
     float *g_phif;                  // QG_NPHI*G Taylor coefficients
     // neighbour list of a group: water neighbours first (as their O atom),
@@ -146,17 +160,19 @@ struct DevSys {
     const uint8_t *qp_skip;
     const int *qp14_first, *qp14_q; // per atom CSR of Q atoms with qconn == 4
     // nbqq
-    const int *qq_iq, *qq_j, *qq_jq; const int8_t *qq_lj; const double *qq_els;
+    const int *qq_iq, *qq_j, *qq_jq; const int8_t *qq_lj; const double *qq_els; const float *qq_elsf;
     // Q bonded terms (flattened per kind, codes already per state)
     const int *qt_atoms;            // 4 atoms per term
     const int *qt_cod;              // [term*QG_MAXS+s] 1-based lib index (global) or 0
     const int *qt_kind, *qt_traj;   // 0 bond 1 angle 2 torsion 3 improper
     const double *qt_lib;           // 4 doubles per lib entry
+    const float *qt_libf;
     int nqt;
     // classical bonded terms
     const int *bt_atoms;            // 4 atoms per term
     const int *bt_cod;              // global lib index (0-based)
     const double *bt_lib;           // 4 doubles per entry
+    const float *bt_libf;
     const int *bt_kind;             // 0 bond 1 angle 2 torsion 3 harmonic improper 4 periodic improper
     int nbt;                        // padded term list; blocks are single (trajectory, slot)
     const int *bt_blk_traj, *bt_blk_slot;
@@ -166,6 +182,7 @@ struct DevSys {
     // shake
     const int *shk_first, *shk_i, *shk_j, *shk_traj;
     const double *shk_d2;
+    const float2 *shk_d2hl;         // d0^2 as a float pair (hi, lo)
     int nshk_mol;
     // energies and reductions
     unsigned long long *eacc;       // QG_NE per trajectory
@@ -181,6 +198,44 @@ __device__ __forceinline__ void fx_add(unsigned long long *p, double v, int *sta
 }
 __device__ __forceinline__ double fx_get(unsigned long long u) { return (double)(long long)u * (1.0 / QG_FSCALE); }
 
+// round(v * 2^32) as an int64 from the float's bits, with integer
+// instructions only: on GB300 the FP64 pipe (which also converts to and from
+// double) issues at 1/64 of the FP32 rate, so per-atom epilogues avoid it.
+// Ties round away from zero.  Callers keep |v| < 2^30.
+__device__ __forceinline__ long long f2fx(float v) {
+    const unsigned u = __float_as_uint(v);
+    const int e = (int)((u >> 23) & 0xffu);
+    if (e == 0) return 0;                                       // zero / subnormal
+    const unsigned long long m = (u & 0x7fffffu) | 0x800000u;   // |v| = m * 2^(e-150)
+    int sh = e - 118;                                           // |v| * 2^32 = m * 2^sh
+    if (sh > 38) sh = 38;
+    unsigned long long r;
+    if (sh >= 0) r = m << sh;
+    else if (sh >= -24) r = (m + (1ull << (-sh - 1))) >> (-sh);
+    else r = 0;
+    return (u >> 31) ? -(long long)r : (long long)r;
+}
+// the fixed-point gradient from a float (no FP64 instruction)
+__device__ __forceinline__ void fx_addf(unsigned long long *p, float v, int *status) {
+    if (!(fabsf(v) < 1073741824.f)) { atomicOr(status, ST_FIXED); return; }
+    atomicAdd(p, (unsigned long long)f2fx(v));
+}
+// fixed-point value of a float with the range check
+__device__ __forceinline__ long long f2fx_chk(float v, int *status) {
+    if (!(fabsf(v) < 1073741824.f)) { atomicOr(status, ST_FIXED); return 0; }
+    return f2fx(v);
+}
+__device__ __forceinline__ long long d2fx_chk(double v, int *status) {
+    if (!(fabs(v) < QG_FMAX)) { atomicOr(status, ST_FIXED); return 0; }
+    return __double2ll_rn(v * QG_FSCALE);
+}
+// float value of a fixed-point accumulator without FP64: the high word holds
+// the integer part, the low word 2^-32 units
+__device__ __forceinline__ float fx_getf(unsigned long long u) {
+    const long long q = (long long)u;
+    return (float)(int)(q >> 32) + (float)(unsigned)(q & 0xffffffffull) * 2.3283064365386963e-10f;
+}
+
 // compensated float accumulation (Kahan)
 struct KSum {
     float s, c;
@@ -192,11 +247,57 @@ struct KSum {
         s = t;
     }
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+    // fixed-point value of scale * (s - c)
+    __device__ __forceinline__ long long fx(float scale, int *status) const {
+        return f2fx_chk(s * scale, status) - f2fx_chk(c * scale, status);
+    }
 };
+
+// Block sums of N int64 fixed-point energies into the slots of one
+// trajectory: warp shuffles, then warp 0 adds the warps' partials in order.
+// Every thread of the block must call it.
+template <int N>
+__device__ __forceinline__ void block_energies_fx(unsigned long long *eacc, const int (&slot)[N], long long (&v)[N],
+                                                  long long (*red)[QG_BLOCK / 32]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < N; ++k) red[k][warp] = v[k];
+    __syncthreads();
+    if (threadIdx.x < N) {
+        long long s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
+        int sl = 0;
+#pragma unroll
+        for (int k = 0; k < N; ++k) sl = (k == (int)threadIdx.x) ? slot[k] : sl;   // no local-memory indexing
+        if (s) atomicAdd(eacc + sl, (unsigned long long)s);
+    }
+}
 
 __device__ __forceinline__ double warp_sum_d(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
+}
+// Error-free transformations (Knuth two-sum, Dekker fast two-sum; FMA two-product)
+__device__ __forceinline__ float two_sum(float a, float b, float &err) {
+    const float s = a + b, bb = s - a;
+    err = (a - (s - bb)) + (b - bb);
+    return s;
+}
+__device__ __forceinline__ float fast_two_sum(float a, float b, float &err) {   // |a| >= |b|
+    const float s = a + b;
+    err = b - (s - a);
+    return s;
+}
+__device__ __forceinline__ float two_prod(float a, float b, float &err) {
+    const float p = a * b;
+    err = fmaf(a, b, -p);
+    return p;
 }
 __device__ __forceinline__ float warp_sum_f(float v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -255,10 +356,17 @@ void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int l
 void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
 void launch_qp(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
 // nonbond_qq, Q bonded, classical bonded, restraints and off-diagonals in one launch
-void launch_misc(const DevSys &S, const BlockTables &B, LaunchCtx &L, int terms);
+// On each launch the kernel evaluates in FP64 from x when eacc_on(e), else in
+// FP32 from the float coordinates.
+void launch_misc(const DevSys &S, const BlockTables &B, LaunchCtx &L, int terms, EaccSel e);
 void launch_integrate(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_shake(const DevSys &S, const BlockTables &B, LaunchCtx &L, int traj_filter);
 void launch_update(const DevSys &S, const BlockTables &B, LaunchCtx &L, int mode);
+// the fused step with the float master; writes x/v as well when the next
+// step lists or records (e: the record selector of this step, nbcycle)
+void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int nbcycle);
+// x = origin + hi + lo, v = velf for every atom
+void launch_sync_double(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *rec, const int *rec_base, int k,
                      int ene_every, int rec_cap);
 void launch_tick(LaunchCtx &L, int *rec_base, int n);

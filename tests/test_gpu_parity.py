@@ -6,7 +6,10 @@ FP64 / int64 fixed point):
   * forces: relative RMS  sqrt(sum|dF|^2 / sum|F|^2) <= 1e-5;
   * energies: |dE| <= 1e-5 * (sum of |terms| scale) -- see ENERGY_TOL below;
   * LRF multipoles: |d phi| <= 1e-5 * max|phi| per component family;
-  * SHAKE and the FP64 integrator: 1e-9 absolute on coordinates.
+  * SHAKE (drop-in, FP64): 1e-9 absolute on coordinates;
+  * MD (float master state, FP32 SHAKE on unrecorded steps): recorded
+    potential and kinetic energies 1e-4 relative, coordinates 1e-4 A after
+    20 steps.
 """
 from collections import Counter
 
@@ -21,6 +24,7 @@ pytestmark = pytest.mark.gpu
 FORCE_RTOL = 1e-5
 ENERGY_REL = 1e-5       # relative to |E| ...
 ENERGY_ABS = 2e-3       # ... or absolute kcal/mol for terms that nearly cancel
+STEP_PAIR_ENERGY_ABS = 0.05   # FP32 pair-energy sums, see test_step_precision_forces
 
 
 def _engine(systems):
@@ -134,23 +138,52 @@ def test_shake_matches_oracle(systems):
     assert np.abs(xg - xo).max() < 1e-9
 
 
-def test_short_md_matches_oracle(systems):
-    """20 Berendsen leap-frog steps with SHAKE and lists every 10 steps."""
+@pytest.mark.parametrize("ene_every", [1, 5])
+def test_short_md_matches_oracle(systems, ene_every):
+    """20 Berendsen leap-frog steps with SHAKE and lists every 10 steps.  With
+    ene_every=5 the unrecorded steps run the FP32 path (float master state,
+    FP32 SHAKE and bonded terms); recorded steps evaluate energies in FP64."""
     s = systems["cfg1"]
     e = _engine(s)
-    rows = e.run(20, ene_every=1)[0]
+    rows = e.run(20, ene_every=ene_every)[0]
     o = _oracle(s)
     o.temperature()
     rc, orows, oq, T = o.md_run(20)
-    assert rc == 0 and len(rows) == 20
-    for k in (0, 1, 10, 19):
-        pg, po = rows[k][1]["potential"], orows[k]["potential"]
+    assert rc == 0 and len(rows) == 20 // ene_every
+    for r in rows:
+        k = r[0]
+        pg, po = r[1]["potential"], orows[k]["potential"]
         assert abs(pg - po) <= 1e-4 * max(1.0, abs(po)), (k, pg, po)
-        kg, ko = rows[k][1]["kinetic"], orows[k]["kinetic"]
+        kg, ko = r[1]["kinetic"], orows[k]["kinetic"]
         assert abs(kg - ko) <= 1e-4 * ko, (k, kg, ko)
     x, _ = e.coords(0)
     xo, _ = o.coords()
     assert np.abs(x - xo).max() < 1e-4
+
+
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg4"])
+def test_step_precision_forces(systems, name):
+    """The precision of an unrecorded MD step (QGPU_TERMS_STEP_PRECISION: FP32
+    bonded, restraint and Q terms from the float coordinates, FP32 energy sums)
+    against the FP64 oracle, with the force and energy tolerances above."""
+    from qsource_gb300.abi import QGPU_TERMS_STEP_PRECISION
+    s = systems[name]
+    e = _engine(s)
+    e.make_pair_lists()
+    d, E, EQ = e.pot_energy(0, terms=0x1F | QGPU_TERMS_STEP_PRECISION)
+    o = _oracle(s)
+    o.make_pair_lists()
+    do, Eo, EQo = o.pot_energy(terms=0x1F)
+    assert rel_rms(d, do) <= FORCE_RTOL
+    # FP32 pair energies (pp/pw/ww, the FP32 path of every unrecorded step) carry
+    # the rounding of each term: about 1e-8 of the sum of |terms|, which for the
+    # water sphere of the golden system (ww_el = -7.3 from |terms| summing to
+    # 7.7e6 kcal/mol) is 0.02 kcal/mol.
+    pair = ["pp_el", "pp_vdw", "pw_el", "pw_vdw", "ww_el", "ww_vdw"]
+    assert all(abs(E[k] - Eo[k]) <= max(ENERGY_REL * abs(Eo[k]), STEP_PAIR_ENERGY_ABS) for k in pair)
+    assert not energies_close(E, Eo, [k for k in E_KEYS if k not in pair])
+    for s_ in range(s.nstates):
+        assert not energies_close(EQ[s_], EQo[s_], EQ_KEYS)
 
 
 def test_run_is_bit_deterministic(systems):
