@@ -157,22 +157,23 @@ __global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, 
 }
 
 // Phase 2: one warp per target group folds the chunks in order -- lane k
-// sums LRF component k in FP64, the lanes copy the chunks' near-group
-// segments into the neighbour list (water entries of every chunk first, then
-// solute entries) -- and lane 0 forms the symmetric Taylor coefficients.
+// sums LRF component k (FP32; at most a few tens of chunk partials), the
+// lanes copy the chunks' near-group segments into the neighbour list (water
+// entries of every chunk first, then solute entries) -- and lane 0 forms the
+// symmetric Taylor coefficients.  No FP64: this runs over every group.
 __global__ void k_scan_reduce(DevSys S) {
     const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (t >= S.ngrp) return;
     const TrajInfo &T = S.traj[S.g_traj[t]];
     const bool ex = S.g_excl[t];
-    double acc = 0.0;
+    float acc = 0.f;
     const int cap = S.nb_cap;
     int *lst = S.nb_list + (size_t)t * cap;
     int cnt = 0;
     for (int c = 0; c < T.nchunk; ++c) {
         const long long slot = T.scr0 + (long long)c * T.ncgp + (t - T.grp0);
-        if (lane < QG_NLRF) acc += (double)S.scr_phi[(size_t)slot * QG_NLRF + lane];
+        if (lane < QG_NLRF) acc += S.scr_phi[(size_t)slot * QG_NLRF + lane];
         const int nw = ex ? 0 : (S.scr_cnt[slot] & 0xffff);
         const int *seg = S.scr_nb + (size_t)slot * QG_CAPC;
         for (int k = lane; k < nw; k += 32)
@@ -188,30 +189,30 @@ __global__ void k_scan_reduce(DevSys S) {
             if (cnt + k < cap) lst[cnt + k] = seg[QG_CAPC - 1 - k];
         cnt += ns;
     }
-    double accd[QG_NLRF];
+    float a[QG_NLRF];
 #pragma unroll
-    for (int k = 0; k < QG_NLRF; ++k) accd[k] = __shfl_sync(0xffffffffu, acc, k);
+    for (int k = 0; k < QG_NLRF; ++k) a[k] = __shfl_sync(0xffffffffu, acc, k);
     if (lane < QG_NLRF) S.g_phi[(size_t)t * QG_NLRF + lane] = acc;
     if (lane != 0) return;
     S.nb_nw[t] = nwat < cap ? nwat : cap;
     S.nb_count[t] = cnt < cap ? cnt : cap;
     if (cnt > cap) atomicOr(S.status, ST_LIST_OVERFLOW);
     float *pf = S.g_phif + (size_t)t * QG_NPHI;
-    const double q1x = accd[5], q1y = accd[6], q1z = accd[7];
-    pf[0] = (float)accd[0];
-    pf[1] = (float)(-accd[2]); pf[2] = (float)(-accd[3]); pf[3] = (float)(-accd[4]);
-    pf[4] = (float)(accd[8] - accd[1]); pf[5] = (float)(accd[9] - accd[1]); pf[6] = (float)(accd[10] - accd[1]);
-    pf[7] = (float)accd[11]; pf[8] = (float)accd[12]; pf[9] = (float)accd[13];
-    pf[10] = (float)(5.0 * accd[14] + 3.0 * q1x);
-    pf[11] = (float)(5.0 * accd[15] + 3.0 * q1y);
-    pf[12] = (float)(5.0 * accd[16] + 3.0 * q1z);
-    pf[13] = (float)(5.0 * accd[17] + q1y);   // xxy
-    pf[14] = (float)(5.0 * accd[18] + q1z);   // xxz
-    pf[15] = (float)(5.0 * accd[19] + q1x);   // xyy
-    pf[16] = (float)(5.0 * accd[20] + q1x);   // xzz
-    pf[17] = (float)(5.0 * accd[21] + q1z);   // yyz
-    pf[18] = (float)(5.0 * accd[22] + q1y);   // yzz
-    pf[19] = (float)(5.0 * accd[23]);         // xyz
+    const float q1x = a[5], q1y = a[6], q1z = a[7];
+    pf[0] = a[0];
+    pf[1] = -a[2]; pf[2] = -a[3]; pf[3] = -a[4];
+    pf[4] = a[8] - a[1]; pf[5] = a[9] - a[1]; pf[6] = a[10] - a[1];
+    pf[7] = a[11]; pf[8] = a[12]; pf[9] = a[13];
+    pf[10] = 5.f * a[14] + 3.f * q1x;
+    pf[11] = 5.f * a[15] + 3.f * q1y;
+    pf[12] = 5.f * a[16] + 3.f * q1z;
+    pf[13] = 5.f * a[17] + q1y;   // xxy
+    pf[14] = 5.f * a[18] + q1z;   // xxz
+    pf[15] = 5.f * a[19] + q1x;   // xyy
+    pf[16] = 5.f * a[20] + q1x;   // xzz
+    pf[17] = 5.f * a[21] + q1z;   // yyz
+    pf[18] = 5.f * a[22] + q1y;   // yzz
+    pf[19] = 5.f * a[23];         // xyz
 }
 
 // Q-atom list membership (nbqplist src/md.f90:10215-10322, nbqwlist

@@ -18,7 +18,7 @@ __global__ void k_integrate(DevSys S) {
     const int tr = S.atraj[i];
     const TrajInfo &T = S.traj[tr];
     const TrajState &TS = S.tstate[tr];
-    const double ts = (i - T.atom0) < T.nat_solute ? TS.Tscale_solute : TS.Tscale_solvent;
+    const double ts = (i - T.atom0) < T.nat_solute ? TS.tsf_solute : TS.tsf_solvent;
     const double wi = S.winv[i], dt = T.dt;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -77,65 +77,11 @@ __global__ void k_shake(DevSys S, int traj_filter) {
     atomicAdd(&S.tstate[tr].shake_iters, nits);
 }
 
-// SHAKE of one water held in registers: the Gauss-Seidel sweeps of shake
-// (src/md.f90:17581-17679) over its constraints in topology order
-// O-H1, O-H2, H1-H2 (local atoms (0,1), (0,2), (1,2)).  Returns the sweep
-// count; sets *fail at SHAKE_MAX_ITER.
-template <int I, int J>
-__device__ __forceinline__ void shake_pair(double (&x)[3][3], const double (&xxij)[3], const double (&ua)[3],
-                                           const double (&ub)[3], double d2, double tol, double den0, unsigned &ready,
-                                           int c) {
-    if (ready & (1u << c)) return;
-    const double x0 = x[I][0] - x[J][0], x1 = x[I][1] - x[J][1], x2 = x[I][2] - x[J][2];
-    const double diff = d2 - (x0 * x0 + x1 * x1 + x2 * x2);
-    if (fabs(diff) < tol) ready |= 1u << c;
-    const double den = den0 * (x0 * xxij[0] + x1 * xxij[1] + x2 * xxij[2]);
-    // diff / den with a Newton-refined reciprocal of a float seed
-    double y = (double)__fdividef(1.0f, (float)den);   // seed; refined below
-    y = y * (2.0 - den * y);
-    y = y * (2.0 - den * y);
-    const double corr = diff * y;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        x[I][a] += ua[a] * corr;
-        x[J][a] -= ub[a] * corr;
-    }
-}
-
-__device__ int shake_water(double (&x)[3][3], const double (&xx)[3][3], const double (&w)[3], const double (&d2)[3],
-                           bool *fail) {
-    double xxij[3][3], ua[3][3], ub[3][3], den0[3], tol[3];
-    const int ci[3] = {0, 0, 1}, cj[3] = {1, 2, 2};
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            xxij[c][a] = xx[ci[c]][a] - xx[cj[c]][a];
-            ua[c][a] = xxij[c][a] * w[ci[c]];
-            ub[c][a] = xxij[c][a] * w[cj[c]];
-        }
-        den0[c] = 2.0 * (w[ci[c]] + w[cj[c]]);
-        tol[c] = SHAKE_TOL * d2[c];
-    }
-    unsigned ready = 0u;
-    int nits = 0;
-    for (;;) {
-        shake_pair<0, 1>(x, xxij[0], ua[0], ub[0], d2[0], tol[0], den0[0], ready, 0);
-        shake_pair<0, 2>(x, xxij[1], ua[1], ub[1], d2[1], tol[1], den0[1], ready, 1);
-        shake_pair<1, 2>(x, xxij[2], ua[2], ub[2], d2[2], tol[2], den0[2], ready, 2);
-        nits++;
-        if (ready == 7u) break;
-        if (nits >= SHAKE_MAX_ITER) { *fail = true; break; }
-    }
-    return nits;
-}
-
-// Per-step update over the trajectory's update items (atoms, or whole 3-atom
-// water molecules that carry SHAKE constraints):
+// Per-step update of the FP64 path, over the update items (atoms, or whole
+// molecules that carry SHAKE constraints):
 //   mode 0: kinetic energy + float mirror only (temperature before step 0);
-//   mode 1: leap-frog + Berendsen (newvel_ber), SHAKE of the molecule in
-//           registers, v = (x - xx)/dt (md_run :6596-6597), mirror, Ekin;
-//   mode 2: v = (x - xx)/dt after the separate SHAKE kernel, mirror, Ekin.
+//   mode 2: v = (x - xx)/dt after k_integrate + k_shake (md_run
+//           :6596-6597), mirror, Ekin.
 // Ekin partials (solute, free solute, solvent, free solvent) per block.
 __global__ void __launch_bounds__(QG_BLOCK) k_update(DevSys S, const int *items, int mode) {
     __shared__ double red[4][QG_BLOCK / 32];
@@ -148,61 +94,26 @@ __global__ void __launch_bounds__(QG_BLOCK) k_update(DevSys S, const int *items,
         const int na = mol ? 3 : 1;
         const int tr = S.atraj[a0];
         const TrajInfo &T = S.traj[tr];
-        TrajState &TS = S.tstate[tr];
-        const double dt = T.dt;
-        double x[3][3], xx[3][3], v[3][3], w[3];
         for (int k = 0; k < na; ++k) {
             const int i = mol ? a0 + k : a0;
-            w[k] = S.winv[i];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) { x[k][a] = S.x[3 * i + a]; v[k][a] = S.v[3 * i + a]; xx[k][a] = S.xx[3 * i + a]; }
-            if (mode == 1) {
-                const double ts = (i - T.atom0) < T.nat_solute ? TS.Tscale_solute : TS.Tscale_solvent;
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    const double g = fx_get(S.fx[3 * i + a]);
-                    S.fx[3 * i + a] = 0ull;
-                    v[k][a] = (v[k][a] - g * w[k] * dt) * ts;
-                    xx[k][a] = x[k][a];
-                    x[k][a] = x[k][a] + v[k][a] * dt;
-                }
-            }
-        }
-        if (mode == 1 && mol) {
-            const int c0 = S.shk_first[m];
-            const double d2[3] = {S.shk_d2[c0], S.shk_d2[c0 + 1], S.shk_d2[c0 + 2]};
-            bool fail = false;
-            const int nits = shake_water(x, xx, w, d2, &fail);
-            if (fail) atomicOr(S.status, ST_SHAKE);
-            atomicAdd(&TS.shake_iters, nits);
-        }
-        const bool vfix = (mode == 1 && T.nshake_mol > 0) || mode == 2;
-        for (int k = 0; k < na; ++k) {
-            const int i = mol ? a0 + k : a0;
-            double vv = 0;
+            double x[3], v[3], vv = 0;
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                if (vfix) v[k][a] = (x[k][a] - xx[k][a]) * T.inv_dt;
-                vv += v[k][a] * v[k][a];
-            }
-            if (mode == 1) {
-#pragma unroll
-                for (int a = 0; a < 3; ++a) { S.x[3 * i + a] = x[k][a]; S.xx[3 * i + a] = xx[k][a]; }
-            }
-            if (mode != 0) {
-#pragma unroll
-                for (int a = 0; a < 3; ++a) S.v[3 * i + a] = v[k][a];
+                x[a] = S.x[3 * i + a];
+                v[a] = S.v[3 * i + a];
+                if (mode == 2) { v[a] = (x[a] - S.xx[3 * i + a]) * T.inv_dt; S.v[3 * i + a] = v[a]; }
+                vv += v[a] * v[a];
             }
             const double e = 0.5 * S.mass[i] * vv;
             const bool fr = !S.aexcl[i];
             if ((i - T.atom0) < T.nat_solute) { ek[0] += e; ek[1] += fr ? e : 0; }
             else { ek[2] += e; ek[3] += fr ? e : 0; }
             float4 h, l;
-            const double r0 = x[k][0] - T.origin[0], r1 = x[k][1] - T.origin[1], r2 = x[k][2] - T.origin[2];
+            const double r0 = x[0] - T.origin[0], r1 = x[1] - T.origin[1], r2 = x[2] - T.origin[2];
             h.x = (float)r0; h.y = (float)r1; h.z = (float)r2; h.w = S.pos[i].w;
             l.x = (float)(r0 - (double)h.x); l.y = (float)(r1 - (double)h.y); l.z = (float)(r2 - (double)h.z); l.w = 0.f;
             S.pos[i] = h; S.poslo[i] = l;
-            S.velf[i] = make_float4((float)v[k][0], (float)v[k][1], (float)v[k][2], 0.f);
+            S.velf[i] = make_float4((float)v[0], (float)v[1], (float)v[2], 0.f);
         }
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -214,7 +125,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_update(DevSys S, const int *items,
     if (threadIdx.x < 4) {
         double s = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
-        S.ekin_part[(size_t)blockIdx.x * 4 + threadIdx.x] = s;
+        S.ekin_part[(size_t)blockIdx.x * 4 + threadIdx.x] = (float)s;
     }
 }
 
@@ -288,81 +199,113 @@ __device__ __forceinline__ void hilo_add(float &h, float &l, float d) {
     h = fast_two_sum(s, l + e, l);
 }
 
-// One MD update (mode 1 of k_update) with the float master state: leap-frog
-// + Berendsen (newvel_ber), SHAKE of water items in registers, v = (x-xx)/dt,
+// One MD update with the float master state, one thread per atom in blocks
+// of QG_UBLK atoms: leap-frog + Berendsen (newvel_ber, src/md.f90:6194-6223)
+// per atom; in blocks of 32 waters, warp 0 then runs the SHAKE of one water
+// per lane on the displacements held in shared memory; then per atom
+// v = (x - xx)/dt (md_run :6596-6597), the hi/lo position update and the
 // Ekin partials.  No FP64 arithmetic except the x/v refresh (want_x).
-__global__ void __launch_bounds__(QG_BLOCK) k_update_f(DevSys S, const int *items, EaccSel esel, int nbcycle) {
-    __shared__ float red[4][QG_BLOCK / 32];
-    const int it = items[blockIdx.x * blockDim.x + threadIdx.x];
+// ekin_only: temperature before the first step (Ekin of the current velf).
+__global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom, const int *ucon,
+                                                      const uint8_t *ublk_water, EaccSel esel, int nbcycle,
+                                                      int ekin_only) {
+    __shared__ float4 s_h[QG_UBLK], s_l[QG_UBLK];
+    __shared__ float s_D[3][QG_UBLK];
+    __shared__ float s_w[QG_UBLK];
+    __shared__ float red[4][QG_UBLK / 32];
+    const int t = threadIdx.x;
+    const int a = uatom[blockIdx.x * QG_UBLK + t];
+    const bool water_blk = ublk_water[blockIdx.x] != 0;
     const int next = esel.recctl[0] + esel.k + 1;
-    const bool want_x = (next % nbcycle == 0) ||
-                        (esel.mode == EACC_RECORD && esel.ene_every > 0 && next % esel.ene_every == 0);
-    float ek[4] = {0.f, 0.f, 0.f, 0.f};
-    if (it >= 0) {
-        const bool mol = (it >> 30) & 1;
-        const int m = it & 0x3fffffff;
-        const int a0 = mol ? S.shk_i[S.shk_first[m]] : m;
-        const int na = mol ? 3 : 1;
-        const int tr = S.atraj[a0];
-        const TrajInfo &T = S.traj[tr];
-        TrajState &TS = S.tstate[tr];
-        const float dt = T.dtf;
-        float4 h[3], l[3];
-        float3 v[3], D[3];
-        float w[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            if (k >= na) { h[k] = l[k] = make_float4(0, 0, 0, 0); v[k] = D[k] = make_float3(0, 0, 0); w[k] = 0.f; continue; }
-            const int i = a0 + k;
-            h[k] = S.pos[i]; l[k] = S.poslo[i]; w[k] = S.winvf[i];
-            const float4 vi = S.velf[i];
-            const float ts = (i - T.atom0) < T.nat_solute ? TS.tsf_solute : TS.tsf_solvent;
-            const float gx = fx_getf(S.fx[3 * i]), gy = fx_getf(S.fx[3 * i + 1]), gz = fx_getf(S.fx[3 * i + 2]);
-            S.fx[3 * i] = 0ull; S.fx[3 * i + 1] = 0ull; S.fx[3 * i + 2] = 0ull;
-            const float wdt = w[k] * dt;
-            v[k] = make_float3((vi.x - gx * wdt) * ts, (vi.y - gy * wdt) * ts, (vi.z - gz * wdt) * ts);
-            D[k] = make_float3(v[k].x * dt, v[k].y * dt, v[k].z * dt);
-        }
-        if (mol) {
-            const int c0 = S.shk_first[m];
-            const float2 d2[3] = {S.shk_d2hl[c0], S.shk_d2hl[c0 + 1], S.shk_d2hl[c0 + 2]};
-            bool fail = false;
-            const int nits = shake_water_f(h, l, w, d2, D, &fail);
-            if (fail) atomicOr(S.status, ST_SHAKE);
-            atomicAdd(&TS.shake_iters, nits);
-        }
-        const bool vfix = T.nshake_mol > 0;
-        for (int k = 0; k < na; ++k) {
-            const int i = a0 + k;
-            if (vfix) v[k] = make_float3(D[k].x * T.inv_dtf, D[k].y * T.inv_dtf, D[k].z * T.inv_dtf);
-            hilo_add(h[k].x, l[k].x, D[k].x);
-            hilo_add(h[k].y, l[k].y, D[k].y);
-            hilo_add(h[k].z, l[k].z, D[k].z);
-            S.pos[i] = h[k]; S.poslo[i] = l[k];
-            S.velf[i] = make_float4(v[k].x, v[k].y, v[k].z, 0.f);
-            const float e = 0.5f * S.massf[i] * (v[k].x * v[k].x + v[k].y * v[k].y + v[k].z * v[k].z);
-            const bool fr = !S.aexcl[i];
-            if ((i - T.atom0) < T.nat_solute) { ek[0] += e; ek[1] += fr ? e : 0.f; }
-            else { ek[2] += e; ek[3] += fr ? e : 0.f; }
-            if (want_x) {
-                S.x[3 * i] = T.origin[0] + ((double)h[k].x + (double)l[k].x);
-                S.x[3 * i + 1] = T.origin[1] + ((double)h[k].y + (double)l[k].y);
-                S.x[3 * i + 2] = T.origin[2] + ((double)h[k].z + (double)l[k].z);
-                S.v[3 * i] = (double)v[k].x; S.v[3 * i + 1] = (double)v[k].y; S.v[3 * i + 2] = (double)v[k].z;
+    const bool want_x = !ekin_only && ((next % nbcycle == 0) ||
+                        (esel.mode == EACC_RECORD && esel.ene_every > 0 && next % esel.ene_every == 0));
+    const int tr = a >= 0 ? S.atraj[a] : -1 - a;
+    const TrajInfo &T = S.traj[tr];
+    float4 h = make_float4(0, 0, 0, 0), l = h;
+    float3 v = make_float3(0, 0, 0), D = v;
+    if (a >= 0) {
+        const float4 vi = S.velf[a];
+        v = make_float3(vi.x, vi.y, vi.z);
+        if (!ekin_only) {
+            const TrajState &TS = S.tstate[tr];
+            h = S.pos[a]; l = S.poslo[a];
+            const float w = S.winvf[a], dt = T.dtf;
+            const float ts = (a - T.atom0) < T.nat_solute ? TS.tsf_solute : TS.tsf_solvent;
+            const float gx = fx_getf(S.fx[3 * a]), gy = fx_getf(S.fx[3 * a + 1]), gz = fx_getf(S.fx[3 * a + 2]);
+            S.fx[3 * a] = 0ull; S.fx[3 * a + 1] = 0ull; S.fx[3 * a + 2] = 0ull;
+            const float wdt = w * dt;
+            v = make_float3((v.x - gx * wdt) * ts, (v.y - gy * wdt) * ts, (v.z - gz * wdt) * ts);
+            D = make_float3(v.x * dt, v.y * dt, v.z * dt);
+            if (water_blk) {
+                s_h[t] = h; s_l[t] = l; s_w[t] = w;
+                s_D[0][t] = D.x; s_D[1][t] = D.y; s_D[2][t] = D.z;
             }
         }
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (water_blk && !ekin_only) {
+        __syncthreads();
+        if (t < 32) {
+            const int c0 = ucon[blockIdx.x * QG_UBLK + 3 * t];
+            int nits = 0;
+            if (c0 >= 0) {
+                float4 wh[3], wl[3];
+                float ww[3];
+                float3 wD[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int q = 3 * t + k;
+                    wh[k] = s_h[q]; wl[k] = s_l[q]; ww[k] = s_w[q];
+                    wD[k] = make_float3(s_D[0][q], s_D[1][q], s_D[2][q]);
+                }
+                const float2 d2[3] = {S.shk_d2hl[c0], S.shk_d2hl[c0 + 1], S.shk_d2hl[c0 + 2]};
+                bool fail = false;
+                nits = shake_water_f(wh, wl, ww, d2, wD, &fail);
+                if (fail) atomicOr(S.status, ST_SHAKE);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int q = 3 * t + k;
+                    s_D[0][q] = wD[k].x; s_D[1][q] = wD[k].y; s_D[2][q] = wD[k].z;
+                }
+            }
+            // a block holds one trajectory: one counter update per block
+            for (int o = 16; o > 0; o >>= 1) nits += __shfl_down_sync(0xffffffffu, nits, o);
+            if (t == 0 && nits) atomicAdd(&S.tstate[tr].shake_iters, nits);
+        }
+        __syncthreads();
+        if (a >= 0) D = make_float3(s_D[0][t], s_D[1][t], s_D[2][t]);
+    }
+    float ek[4] = {0.f, 0.f, 0.f, 0.f};
+    if (a >= 0) {
+        if (!ekin_only) {
+            if (T.nshake_mol > 0) v = make_float3(D.x * T.inv_dtf, D.y * T.inv_dtf, D.z * T.inv_dtf);
+            hilo_add(h.x, l.x, D.x);
+            hilo_add(h.y, l.y, D.y);
+            hilo_add(h.z, l.z, D.z);
+            S.pos[a] = h; S.poslo[a] = l;
+            S.velf[a] = make_float4(v.x, v.y, v.z, 0.f);
+            if (want_x) {
+                S.x[3 * a] = T.origin[0] + ((double)h.x + (double)l.x);
+                S.x[3 * a + 1] = T.origin[1] + ((double)h.y + (double)l.y);
+                S.x[3 * a + 2] = T.origin[2] + ((double)h.z + (double)l.z);
+                S.v[3 * a] = (double)v.x; S.v[3 * a + 1] = (double)v.y; S.v[3 * a + 2] = (double)v.z;
+            }
+        }
+        const float e = 0.5f * S.massf[a] * (v.x * v.x + v.y * v.y + v.z * v.z);
+        const bool fr = !S.aexcl[a];
+        if ((a - T.atom0) < T.nat_solute) { ek[0] = e; ek[1] = fr ? e : 0.f; }
+        else { ek[2] = e; ek[3] = fr ? e : 0.f; }
+    }
+    const int lane = t & 31, warp = t >> 5;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const float v = warp_sum_f(ek[k]);
-        if (lane == 0) red[k][warp] = v;
+        const float r = warp_sum_f(ek[k]);
+        if (lane == 0) red[k][warp] = r;
     }
     __syncthreads();
-    if (threadIdx.x < 4) {
+    if (t < 4) {
         float s = 0.f;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
-        S.ekin_part[(size_t)blockIdx.x * 4 + threadIdx.x] = (double)s;
+        for (int w = 0; w < QG_UBLK / 32; ++w) s += red[t][w];
+        S.ekin_part[(size_t)blockIdx.x * 4 + t] = s;
     }
 }
 
@@ -378,61 +321,63 @@ __global__ void k_sync_double(DevSys S) {
     S.v[3 * i] = (double)v.x; S.v[3 * i + 1] = (double)v.y; S.v[3 * i + 2] = (double)v.z;
 }
 
-// One block per trajectory: temperature() (optional) and the energy summary
-// of pot_energy; writes a record row and clears the energy accumulators.
-// The Ekin partials are summed by the warp in a fixed order (strided lanes,
-// then a shuffle tree), the accumulator slots are read by all lanes.
+// One warp per trajectory: temperature() (optional, every step) and, on the
+// steps whose energies are recorded, the energy summary of pot_energy into a
+// record row; clears the energy accumulators.  The per-step part is FP32:
+// T = Ekin * 2/(Boltz*Ndegf) with the constants formed on the host, the
+// Berendsen scale sqrt(1 + dt/tau_T (T0/T - 1)) (src/md.f90:6160-6180).
+// FP64 is used for the record rows only.
 __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_base, int k, int ene_every, int rec_cap) {
     __shared__ double v[QG_NE];
-    __shared__ double e4[4];
     const int tr = blockIdx.x;
     const int lane = threadIdx.x;
     const TrajInfo &T = S.traj[tr];
     TrajState &TS = S.tstate[tr];
     unsigned long long *ea = S.eacc + (size_t)tr * QG_NE;
-    for (int s = lane; s < QG_NE; s += 32) { v[s] = fx_get(ea[s]); ea[s] = 0ull; }
+    int row = -1;
+    if (rec) {
+        const int step = rec_base[0] + k;
+        if (ene_every > 0 && step % ene_every == 0) {
+            row = step / ene_every - rec_base[1];
+            if (row >= rec_cap) row = -1;
+        }
+    }
+    for (int s = lane; s < QG_NE; s += 32) {
+        if (row >= 0) v[s] = fx_get(ea[s]);
+        ea[s] = 0ull;
+    }
     if (do_temp) {
+        float e4[4];
+#pragma unroll
         for (int c = 0; c < 4; ++c) {
-            double p = 0;
+            float p = 0.f;
             for (int b = lane; b < T.ekin_nblk; b += 32) p += S.ekin_part[(size_t)(T.ekin_blk0 + b) * 4 + c];
-            p = warp_sum_d(p);
-            if (lane == 0) e4[c] = p;
+            e4[c] = warp_sum_f(p);
+        }
+        if (lane == 0) {
+            float Tfsu = e4[1], Tfsv = e4[3];
+            const float Ekin = e4[0] + e4[2];
+            const float Temp = Ekin * T.cT, Tfree = (e4[1] + e4[3]) * T.cTfree;
+            if (T.detail_temps) { Tfsu *= T.cTfsu; Tfsv *= T.cTfsv; }
+            float ts = TS.tsf_solvent, tu = TS.tsf_solute;
+            if (T.separate_scaling) {
+                if (Tfsv != 0.f) ts = T.Temp0f / Tfsv - 1.f;
+                ts = sqrtf(1.f + T.dt_tau * ts);
+                if (Tfsu != 0.f) tu = T.Temp0f / Tfsu - 1.f;
+                tu = sqrtf(1.f + T.dt_tau * tu);
+            } else {
+                if (Tfree != 0.f) ts = T.Temp0f / Tfree - 1.f;
+                ts = sqrtf(1.f + T.dt_tau * ts);
+                tu = ts;
+            }
+            TS.Ekin = Ekin; TS.Temp = Temp; TS.Tfree = Tfree;
+            TS.tsf_solute = tu; TS.tsf_solvent = ts;
+            TS.wshiftf = T.fk_wspheref != 0.f ? sqrtf(0.001986f * Tfree / T.fk_wspheref) : 0.f;
+            if (Temp != Temp) atomicOr(S.status, ST_NAN);
         }
     }
     __syncwarp();
-    if (lane != 0) return;
-    if (do_temp) {
-        double Tfsu = e4[1], Tfsv = e4[3];
-        double Tfree = Tfsv + Tfsu, Temp = e4[0] + e4[2];
-        TS.Ekin = Temp;
-        Temp = 2.0 * Temp / BOLTZ / (double)T.Ndegf;
-        Tfree = 2.0 * Tfree / BOLTZ / (double)T.Ndegfree;
-        if (T.detail_temps) {
-            Tfsu = 2.0 * Tfsu / BOLTZ / (double)T.Ndegfree_solute;
-            Tfsv = 2.0 * Tfsv / BOLTZ / (double)T.Ndegfree_solvent;
-        }
-        double ts = TS.Tscale_solvent, tu = TS.Tscale_solute;
-        if (T.separate_scaling) {
-            if (Tfsv != 0) ts = T.Temp0 / Tfsv - 1.0;
-            ts = sqrt(1 + T.dt / T.tau_T * ts);
-            if (Tfsu != 0) tu = T.Temp0 / Tfsu - 1.0;
-            tu = sqrt(1 + T.dt / T.tau_T * tu);
-        } else {
-            if (Tfree != 0) ts = T.Temp0 / Tfree - 1.0;
-            ts = sqrt(1 + T.dt / T.tau_T * ts);
-            tu = ts;
-        }
-        TS.Temp = Temp; TS.Tfree = Tfree; TS.Tscale_solute = tu; TS.Tscale_solvent = ts;
-        TS.tsf_solute = (float)tu; TS.tsf_solvent = (float)ts;
-        TS.wshift = T.fk_wsphere != 0.0 ? sqrt(BOLTZ * Tfree / T.fk_wsphere) : 0.0;
-        TS.wshiftf = (float)TS.wshift;
-        if (Temp != Temp) atomicOr(S.status, ST_NAN);
-    }
-    if (!rec) return;
-    const int step = *rec_base + k;
-    if (ene_every <= 0 || step % ene_every != 0) return;
-    const int row = step / ene_every - rec_base[1];
-    if (row < 0 || row >= rec_cap) return;
+    if (lane != 0 || row < 0) return;
     double *R = rec + ((size_t)row * S.ntraj + tr) * QG_REC;
     // Q energies per state
     double qb = 0, qa = 0, qt = 0, qi = 0, qxe = 0, qxv = 0;
@@ -465,9 +410,9 @@ __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_ba
     E[23] = E[24] + E[25] + E[26] + E[27] + E[28];
     E[0] = E[3] + E[7] + E[4] + E[8] + E[5] + E[6] + E[15] + E[16] + E[17] + E[18] + E[19] + E[20] + E[11] + E[12] +
            E[13] + E[14] + E[21] + E[22] + E[23] + E[2];
-    E[1] = TS.Ekin;
-    R[QG_REC_T] = TS.Temp;
-    R[QG_REC_T + 1] = TS.Tfree;
+    E[1] = (double)TS.Ekin;
+    R[QG_REC_T] = (double)TS.Temp;
+    R[QG_REC_T + 1] = (double)TS.Tfree;
     for (int c = 0; c < 2 * QG_MAXOD; ++c) R[QG_REC_OD + c] = S.od_out[(size_t)tr * QG_MAXOD * 2 + c];
 }
 
@@ -502,9 +447,9 @@ void launch_update(const DevSys &S, const BlockTables &B, LaunchCtx &L, int mode
     prof_end(L);
     (*L.nlaunch)++;
 }
-void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int nbcycle) {
+void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int nbcycle, int ekin_only) {
     prof_begin(L, "k_update_f");
-    k_update_f<<<B.nuitem / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.uitem, e, nbcycle);
+    k_update_f<<<B.nuatom / QG_UBLK, QG_UBLK, 0, L.stream>>>(S, B.uatom, B.ucon, B.ublk_water, e, nbcycle, ekin_only);
     prof_end(L);
     (*L.nlaunch)++;
 }

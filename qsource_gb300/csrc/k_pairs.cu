@@ -332,18 +332,28 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
 }
 
 // ------------------------------------------------------- Q-atom loops
-// The Q atoms of a trajectory are iterated uniformly by the whole block, so
-// the force on each Q atom is reduced per warp (shuffles) and then across the
-// block's warps in a fixed order -- deterministic without float atomics.
+// LG lanes share one water (k_qw) or one solute atom (k_qp); lane l takes the
+// Q atoms l, l+LG, ...  In each round the lanes of a warp with the same l hold
+// partial forces on the same Q atom: an xor butterfly over the groups sums
+// them in a fixed order, the warp's sums go to shared memory and the block
+// adds its warps in order -- deterministic without float atomics.  LG is
+// chosen per launch: more lanes when the Q atoms are many or the items few.
 struct QShared {
     float4 qh[QG_MAXQ], ql[QG_MAXQ];
     float qf[QG_BLOCK / 32][QG_MAXQ][3];
     long long red[2 * QG_MAXS][QG_BLOCK / 32];
 };
 
-__device__ __forceinline__ void q_reduce_store(QShared &sh, int iq, float fx, float fy, float fz) {
-    fx = warp_sum_f(fx); fy = warp_sum_f(fy); fz = warp_sum_f(fz);
-    if ((threadIdx.x & 31) == 0) {
+// sum over the warp's groups of the force on Q atom iq (all lanes call it)
+template <int LG>
+__device__ __forceinline__ void q_reduce_store(QShared &sh, int iq, bool on, float fx, float fy, float fz) {
+#pragma unroll
+    for (int o = LG; o < 32; o <<= 1) {
+        fx += __shfl_xor_sync(0xffffffffu, fx, o);
+        fy += __shfl_xor_sync(0xffffffffu, fy, o);
+        fz += __shfl_xor_sync(0xffffffffu, fz, o);
+    }
+    if ((threadIdx.x & 31) < LG && on) {
         const int w = threadIdx.x >> 5;
         sh.qf[w][iq][0] = fx; sh.qf[w][iq][1] = fy; sh.qf[w][iq][2] = fz;
     }
@@ -363,6 +373,13 @@ __device__ __forceinline__ void q_load(const DevSys &S, const TrajInfo &T, QShar
         sh.qh[k] = S.pos[a]; sh.ql[k] = S.poslo[a];
     }
     __syncthreads();
+}
+// sum of a lane group's partial forces on its own atom
+template <int LG>
+__device__ __forceinline__ float group_sum(float v) {
+#pragma unroll
+    for (int o = LG / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 
 __device__ __forceinline__ bool eacc_on(const EaccSel &e) {
@@ -400,10 +417,12 @@ __device__ __forceinline__ void q_energies(const DevSys &S, int traj, int NS, co
     block_energies_fx<2 * QG_MAXS>(S.eacc + (size_t)traj * QG_NE, slots, v, sh.red);
 }
 
-// nonbond_qw_spc, src/md.f90:14411-14570.  One thread per water.
+// nonbond_qw_spc, src/md.f90:14411-14570.  LG lanes per water.
+template <int LG>
 __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, EaccSel esel) {
     __shared__ QShared sh;
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LG;
+    const int lane = threadIdx.x & (LG - 1);
     const int w = wgrp[idx];
     const int traj = traj_of_entry(S, w, true);
     const TrajInfo &T = S.traj[traj];
@@ -427,9 +446,11 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
 #pragma unroll
     for (int s = 0; s < QG_MAXS; ++s) lam[s] = T.lambdaf[s];
     const int ntq = T.natyps + T.nqat;
-    for (int iq = 0; iq < T.nqat; ++iq) {
+    for (int iq0 = 0; iq0 < T.nqat; iq0 += LG) {
+        const int iq = iq0 + lane;
+        const bool on = iq < T.nqat;
         float qfx = 0.f, qfy = 0.f, qfz = 0.f;
-        if (valid) {
+        if (valid && on) {
             const int q = T.q0 + iq;
             const int qa = S.q_atom[q];
             // O: Coulomb + LJ (softcore column = LJ code of the pair, src/md.f90:14492)
@@ -446,9 +467,10 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
                     const size_t sci = (size_t)T.sc0 + ((size_t)iq * ntq + (size_t)(S.qw_lj[q] - 1)) * QG_MAXS + s;
                     const float A = S.qw_A[q * QG_MAXS + s], B = S.qw_B[q * QG_MAXS + s];
                     const float r6s = T.qvdw ? r6hc + S.sc_f[sci] : r6hc;
-                    const float Va = A / (r6s * r6s), Vb = B / r6s;
+                    const float ir6 = __frcp_rn(r6s);
+                    const float Va = A * ir6 * ir6, Vb = B * ir6;
                     const float Vel = ah[0].w * S.qcrg_f[q * QG_MAXS + s] * ri;
-                    dv += lam[s] * ri2 * (-Vel - (12.f * Va - 6.f * Vb) * (r6hc / r6s));
+                    dv += lam[s] * ri2 * (-Vel - (12.f * Va - 6.f * Vb) * (r6hc * ir6));
                     if (acc) {
                         const double r6sd = T.qvdw ? r6hcd + S.sc_d[sci] : r6hcd;
                         eel.d[s] += S.crg_d[a0] * S.qcrg_d[q * QG_MAXS + s] * rid;
@@ -479,9 +501,11 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
                 qfx -= dv * d.x; qfy -= dv * d.y; qfz -= dv * d.z;
             }
         }
-        q_reduce_store(sh, iq, qfx, qfy, qfz);
+        q_reduce_store<LG>(sh, iq, on, qfx, qfy, qfz);
     }
-    if (valid)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { gx[a] = group_sum<LG>(gx[a]); gy[a] = group_sum<LG>(gy[a]); gz[a] = group_sum<LG>(gz[a]); }
+    if (valid && lane == 0)
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             fx_addf(S.fx + 3 * (a0 + a), gx[a], S.status);
@@ -493,10 +517,12 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
 }
 
 // nonbond_qp (src/md.f90:13788-13921) / nonbond_qp_qvdw (14097-14230).
-// One thread per solute atom of the qp list.
+// LG lanes per solute atom of the qp list.
+template <int LG>
 __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, EaccSel esel) {
     __shared__ QShared sh;
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LG;
+    const int lane = threadIdx.x & (LG - 1);
     const int j = satom[idx];
     const int traj = traj_of_entry(S, j, false);
     const TrajInfo &T = S.traj[traj];
@@ -511,9 +537,11 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
     if (valid) { jh = S.pos[j]; jl = S.poslo[j]; tj = S.atype[j]; }
     float gx = 0.f, gy = 0.f, gz = 0.f;
     const int ntq = T.natyps + T.nqat;
-    for (int iq = 0; iq < T.nqat; ++iq) {
+    for (int iq0 = 0; iq0 < T.nqat; iq0 += LG) {
+        const int iq = iq0 + lane;
+        const bool on = iq < T.nqat;
         float qfx = 0.f, qfy = 0.f, qfz = 0.f;
-        if (valid) {
+        if (valid && on) {
             const int q = T.q0 + iq;
             const int qa = S.q_atom[q];
             const int tq = S.atype[qa];
@@ -554,8 +582,9 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
                 }
                 float Vel = S.qcrg_f[q * QG_MAXS + s] * jh.w * ri;
                 if (c == 3) Vel *= T.el14;
-                const float Va = A / (r6s * r6s), Vb = B / r6s;
-                dv += T.lambdaf[s] * ri2 * (-Vel - (12.f * Va - 6.f * Vb) * (r6 / r6s));
+                const float ir6 = __frcp_rn(r6s);
+                const float Va = A * ir6 * ir6, Vb = B * ir6;
+                dv += T.lambdaf[s] * ri2 * (-Vel - (12.f * Va - 6.f * Vb) * (r6 * ir6));
                 if (acc) {
                     double Veld = S.qcrg_d[q * QG_MAXS + s] * S.crg_d[j] * rid;
                     if (c == 3) Veld *= T.el14d;
@@ -568,9 +597,10 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
             gx += dv * d.x; gy += dv * d.y; gz += dv * d.z;
             qfx -= dv * d.x; qfy -= dv * d.y; qfz -= dv * d.z;
         }
-        q_reduce_store(sh, iq, qfx, qfy, qfz);
+        q_reduce_store<LG>(sh, iq, on, qfx, qfy, qfz);
     }
-    if (valid) {
+    gx = group_sum<LG>(gx); gy = group_sum<LG>(gy); gz = group_sum<LG>(gz);
+    if (valid && lane == 0) {
         fx_addf(S.fx + 3 * j, gx, S.status);
         fx_addf(S.fx + 3 * j + 1, gy, S.status);
         fx_addf(S.fx + 3 * j + 2, gz, S.status);
@@ -591,17 +621,25 @@ void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int l
     else { prof_begin(L, "k_nb_solute"); k_nb_solute<false><<<B.nsatom * QG_LW / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); prof_end(L); }
     (*L.nlaunch)++;
 }
+// Lanes per item of the Q loops: one per water while each trajectory has
+// few Q atoms (the per-item set-up then dominates), more for larger Q sets;
+// the qp items (solute atoms) are fewer and always take four.
+static int qw_lanes(const BlockTables &B) { return B.max_nqat <= 16 ? 1 : (B.max_nqat <= 48 ? 2 : 4); }
+
 void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
     if (!B.nwgrp) return;
     prof_begin(L, "k_qw");
-    k_qw<<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+    const int lg = qw_lanes(B);
+    if (lg == 1) k_qw<1><<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+    else if (lg == 2) k_qw<2><<<B.nwgrp * 2 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+    else k_qw<4><<<B.nwgrp * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
     prof_end(L);
     (*L.nlaunch)++;
 }
 void launch_qp(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
     if (!B.nsatom) return;
     prof_begin(L, "k_qp");
-    k_qp<<<B.nsatom / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, e);
+    k_qp<4><<<B.nsatom * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, e);
     prof_end(L);
     (*L.nlaunch)++;
 }

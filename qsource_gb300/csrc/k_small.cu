@@ -432,7 +432,7 @@ __device__ void restrain_solvent_block(const DevSys &S, int b, const int *wgrp, 
                 d0 = R(S.x[3 * i] - T.xwcent[0]); d1 = R(S.x[3 * i + 1] - T.xwcent[1]);
                 d2 = R(S.x[3 * i + 2] - T.xwcent[2]);
                 fk = R(T.fk_wsphere); rwat = R(T.rwat); Dwmz = R(T.Dwmz); awmz = R(T.awmz);
-                shift = R(S.tstate[traj].wshift);
+                shift = R(S.tstate[traj].wshiftf);
             } else {
                 // the float coordinates are relative to the origin, which is xwcent
                 const float4 h = S.pos[i], l = S.poslo[i];

@@ -183,6 +183,9 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     std::vector<int> od_traj, od_ij, od_kl;
     std::vector<double> od_Amu;
     std::vector<int> wgrp, satom, scan_t0, scan_tn, scan_traj, scan_chunk, uitem, qqblk_traj, qqblk_s;
+    std::vector<int> uatom, ucon;
+    std::vector<uint8_t> ublk_water;
+    std::vector<int> ek_u0, ek_un, ek_a0, ek_an;   // Ekin block ranges of the two update layouts
     long long scr_slots = 0;
     int type0 = 0, lj0 = 0, q0 = 0, qlib0 = 0, sc0 = 0, grp0 = 0, atom0 = 0, tile0 = 0;
 
@@ -218,6 +221,13 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         for (int s = 0; s < QG_MAXS; ++s) T.lambdaf[s] = (float)T.lambda[s];
         T.dt = d.dt; T.Temp0 = d.Temp0; T.tau_T = d.tau_T; T.inv_dt = 1.0 / d.dt;
         T.dtf = (float)T.dt; T.inv_dtf = (float)T.inv_dt;
+        {
+            const double boltz = 0.001986;   // src/md.f90:54
+            auto c = [&](int n) { return n > 0 ? (float)(2.0 / boltz / (double)n) : 0.f; };
+            T.cT = c(d.Ndegf); T.cTfree = c(d.Ndegfree);
+            T.cTfsu = c(d.Ndegfree_solute); T.cTfsv = c(d.Ndegfree_solvent);
+            T.dt_tau = (float)(d.dt / d.tau_T); T.Temp0f = (float)d.Temp0;
+        }
         T.separate_scaling = d.separate_scaling; T.detail_temps = d.detail_temps;
         T.Ndegf = d.Ndegf; T.Ndegfree = d.Ndegfree;
         T.Ndegfree_solute = d.Ndegfree_solute; T.Ndegfree_solvent = d.Ndegfree_solvent;
@@ -355,6 +365,30 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
             }
             pad(uitem, s0, t);
             T.ekin_nblk = (int)((uitem.size() - s0) / QG_BLOCK);
+            ek_u0.push_back(T.ekin_blk0); ek_un.push_back(T.ekin_nblk);
+            // atom layout of the fused update
+            const size_t u0 = uatom.size();
+            auto upad = [&]() {
+                while ((uatom.size() - u0) % QG_UBLK) { uatom.push_back(-1 - t); ucon.push_back(-1); }
+            };
+            for (int i = 0; i < N; ++i)
+                if (!(fuse && owner[i] >= 0)) { uatom.push_back(atom0 + i); ucon.push_back(-1); }
+            upad();
+            const size_t nb_plain = (uatom.size() - u0) / QG_UBLK;
+            if (fuse) {
+                const int cbase = (int)shk_i.size();   // this trajectory's constraints come next
+                for (int m = 0; m < d.shake_molecules; ++m) {
+                    const int lo = d.shake_i[d.shake_first[m]];
+                    for (int k = 0; k < 3; ++k) {
+                        uatom.push_back(atom0 + lo + k);
+                        ucon.push_back(k == 0 ? cbase + d.shake_first[m] : -1);
+                    }
+                }
+                upad();
+            }
+            const size_t nb_all = (uatom.size() - u0) / QG_UBLK;
+            for (size_t b = 0; b < nb_all; ++b) ublk_water.push_back(b >= nb_plain ? 1 : 0);
+            ek_a0.push_back((int)(u0 / QG_UBLK)); ek_an.push_back((int)nb_all);
         }
         // --- Q atoms
         int nql = d.nqlib;
@@ -523,8 +557,8 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     S.traj = ti;
     std::vector<TrajState> tsh(ntraj);
     for (auto &q : tsh) {
-        q.Tscale_solute = q.Tscale_solvent = 1.0; q.Temp = q.Tfree = q.Ekin = 0; q.shake_iters = 0;
-        q.tsf_solute = q.tsf_solvent = 1.f; q.wshift = 0.0; q.wshiftf = 0.f;
+        q.Temp = q.Tfree = q.Ekin = 0.f; q.shake_iters = 0;
+        q.tsf_solute = q.tsf_solvent = 1.f; q.wshiftf = 0.f; q.pad = 0;
     }
     if ((rc = upload(A, tsh, &ts))) return rc;
     S.tstate = ts;
@@ -605,7 +639,17 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     UP(shk_first, shk_first); UP(shk_i, shk_i); UP(shk_j, shk_j); UP(shk_traj, shk_traj); UP(shk_d2, shk_d2);
     S.nshk_mol = (int)shk_traj.size();
     if ((rc = alloc0(A, (size_t)ntraj * QG_NE, &S.eacc))) return rc;
-    if ((rc = alloc0(A, (size_t)4 * (uitem.size() / QG_BLOCK + 1), &S.ekin_part))) return rc;
+    for (char f : h->fused) h->all_fused = h->all_fused && f;
+    {
+        const size_t nblk_ek = std::max(uitem.size() / QG_BLOCK, uatom.size() / QG_UBLK) + 1;
+        if ((rc = alloc0(A, (size_t)4 * nblk_ek, &S.ekin_part))) return rc;
+    }
+    // the Ekin partials follow the update kernel in use (fused: atom layout)
+    for (int t = 0; t < ntraj; ++t) {
+        h->info[t].ekin_blk0 = h->all_fused ? ek_a0[t] : ek_u0[t];
+        h->info[t].ekin_nblk = h->all_fused ? ek_an[t] : ek_un[t];
+    }
+    CK(cudaMemcpy((void *)S.traj, h->info.data(), h->info.size() * sizeof(TrajInfo), cudaMemcpyHostToDevice));
     if ((rc = alloc0(A, 1, &S.status))) return rc;
     // block tables
     BlockTables &B = h->B;
@@ -618,14 +662,19 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         if ((rc = upload(A, scan_traj, &p))) return rc; B.scan_traj = p; B.nscan = (int)scan_t0.size();
         if ((rc = upload(A, scan_chunk, &p))) return rc; B.scan_chunk = p;
         if ((rc = upload(A, uitem, &p))) return rc; B.uitem = p; B.nuitem = (int)uitem.size();
+        if ((rc = upload(A, uatom, &p))) return rc; B.uatom = p; B.nuatom = (int)uatom.size();
+        if ((rc = upload(A, ucon, &p))) return rc; B.ucon = p;
+        uint8_t *pb;
+        if ((rc = upload(A, ublk_water, &pb))) return rc; B.ublk_water = pb;
         if ((rc = upload(A, qqblk_traj, &p))) return rc; B.qqblk_traj = p;
         if ((rc = upload(A, qqblk_s, &p))) return rc; B.qqblk_s = p; B.nqqblk = (int)qqblk_traj.size();
+        B.max_nqat = 0;
+        for (int t = 0; t < ntraj; ++t) B.max_nqat = std::max(B.max_nqat, h->info[t].nqat);
     }
     if ((rc = alloc0(A, (size_t)ntraj * QG_REC, &h->ecur_d))) return rc;
     if ((rc = alloc0(A, 2, &h->zero_d))) return rc;
     if ((rc = alloc0(A, (size_t)3 * h->max_natom, &h->grad_d))) return rc;
     if ((rc = alloc0(A, 2, &h->recctl_d))) return rc;
-    for (char f : h->fused) h->all_fused = h->all_fused && f;
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     // float mirror of the starting coordinates
     LaunchCtx L{h->stream, &h->nlaunch};
@@ -657,6 +706,13 @@ static void ensure_double(qgpu_handle *h, LaunchCtx &L) {
     h->master = 0;
 }
 static void after_steps(qgpu_handle *h) { h->master = h->all_fused ? 1 : 0; }
+
+// temperature() before the first step (md_run, src/md.f90:6395-6398): the
+// Ekin partials of the update layout in use
+static void temperature_init(qgpu_handle *h, LaunchCtx &L) {
+    if (h->all_fused) launch_update_f(h->S, h->B, L, EaccSel{EACC_FP32, h->zero_d, 0, 1}, h->NBcycle, 1);
+    else launch_update(h->S, h->B, L, 0);
+}
 
 static void list_ops(qgpu_handle *h, LaunchCtx &L) {
     launch_centers(h->S, h->B, L);
@@ -707,7 +763,7 @@ static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every) {
     EaccSel esel{EACC_RECORD, h->recctl_d, k, ene_every};
     force_ops(h, L, QGPU_TERMS_ALL, false, esel);
     if (h->all_fused) {
-        launch_update_f(h->S, h->B, L, esel, h->NBcycle);
+        launch_update_f(h->S, h->B, L, esel, h->NBcycle, 0);
     } else {
         launch_integrate(h->S, h->B, L);
         launch_shake(h->S, h->B, L, -1);
@@ -835,7 +891,7 @@ int qgpu_get_temperature(qgpu_handle *h, int32_t traj, double *out4) {
     TrajState ts;
     CK(cudaMemcpyAsync(&ts, h->S.tstate + traj, sizeof ts, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    out4[0] = ts.Temp; out4[1] = ts.Tfree; out4[2] = ts.Tscale_solute; out4[3] = ts.Tscale_solvent;
+    out4[0] = ts.Temp; out4[1] = ts.Tfree; out4[2] = ts.tsf_solute; out4[3] = ts.tsf_solvent;
     return 0;
 }
 
@@ -866,8 +922,10 @@ int qgpu_get_lrf(qgpu_handle *h, int32_t traj, double *lrf43) {
     if (!h || traj < 0 || traj >= h->ntraj || !lrf43) return fail(QGPU_E_INVALID, "bad arguments");
     int G = h->ncgp[traj], g0 = h->grp0[traj];
     std::vector<double> c(3 * (size_t)G), a((size_t)QG_NLRF * G);
+    std::vector<float> af((size_t)QG_NLRF * G);
     CK(cudaMemcpy(c.data(), h->S.g_cent + 3 * (size_t)g0, c.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(a.data(), h->S.g_phi + (size_t)QG_NLRF * g0, a.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(af.data(), h->S.g_phi + (size_t)QG_NLRF * g0, af.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < af.size(); ++k) a[k] = af[k];
     // symmetric sums -> the 3 + 1 + 3 + 9 + 27 layout of LRF_TYPE (src/md.f90:444-450)
     static const int p2[3][3] = {{8, 11, 12}, {11, 9, 13}, {12, 13, 10}};
     for (int g = 0; g < G; ++g) {
@@ -966,7 +1024,7 @@ int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every) {
     if (!h->temp_init) {
         CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
         CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
-        launch_update(h->S, h->B, L, 0);
+        temperature_init(h, L);
         launch_finalize(h->S, L, 1, nullptr, h->zero_d, 0, 1, 0);
         h->temp_init = 1;
     }
@@ -1016,7 +1074,7 @@ int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink si
     ensure_double(h, L);
     if (!h->temp_init) {
         // temperature() before the first step (md_run, src/md.f90:6395-6398)
-        launch_update(h->S, h->B, L, 0);
+        temperature_init(h, L);
         launch_finalize(h->S, L, 1, nullptr, h->zero_d, 0, 1, 0);
         h->temp_init = 1;
     }

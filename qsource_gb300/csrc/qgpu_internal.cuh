@@ -12,6 +12,7 @@
 #include "qgpu.h"
 
 #define QG_BLOCK 128            // threads per block of the per-item kernels
+#define QG_UBLK 96              // threads per block of the fused update (32 waters)
 #define QG_LW 8                 // lanes that share one target in the pair kernels
 #define S_GROUP_MASK 0xffffffffu
 #define QG_MAXS 4               // states handled by the engine (<= QGPU_MAX_STATES)
@@ -74,6 +75,8 @@ struct TrajInfo {
     float lambdaf[QG_MAXS];
     double dt, Temp0, tau_T, inv_dt;
     float dtf, inv_dtf;
+    // temperature(): T = Ekin * c, c = 2/(Boltz*Ndegf...); dt/tau_T; Temp0
+    float cT, cTfree, cTfsu, cTfsv, dt_tau, Temp0f;
     // float copies of the restraint parameters for the per-step kernels
     float fk_wspheref, rwatf, Dwmzf, awmzf, fk_pshellf, fk_fixf;
     int separate_scaling, detail_temps;
@@ -82,7 +85,7 @@ struct TrajInfo {
     int nb0[6], nbn[6];         // bonded term ranges: p/w bonds, p/w angles... (see host)
     int qq0[QG_MAXS], nqq[QG_MAXS];
     int qterm0[4], nqterm[4];   // Q bond/angle/torsion/improper ranges
-    int ekin_blk0, ekin_nblk;   // Ekin partial slots of this trajectory
+    int ekin_blk0, ekin_nblk;   // Ekin partial slots of this trajectory (update blocks)
     int ff_type;
 };
 
@@ -90,13 +93,15 @@ struct TrajInfo {
 int qgpu_fail(int code, const char *fmt, ...);
 
 // Per-trajectory dynamic state (device).
+// Per-trajectory dynamic state (device), in FP32: it is updated every step by
+// a one-warp kernel, where each FP64 instruction would hold the FP64 pipe for
+// ~64 cycles of a serial chain.
 struct TrajState {
-    double Tscale_solute, Tscale_solvent, Temp, Tfree;
-    double Ekin;
-    int shake_iters;
-    float tsf_solute, tsf_solvent;  // float copies of the Berendsen scales
+    float Temp, Tfree, Ekin;
+    float tsf_solute, tsf_solvent;  // Berendsen scales of the next step
     float wshiftf;                  // sqrt(Boltz*Tfree/fk_wsphere), restrain_solvent
-    double wshift;
+    int shake_iters;
+    int pad;
 };
 
 struct DevSys {
@@ -132,7 +137,7 @@ struct DevSys {
     const uint8_t *g_excl;
     double *g_cent;                 // 3*G
     float4 *g_centf;                // centre - origin in float (per list build)
-    double *g_phi;                  // QG_NLRF*G accumulators
+    float *g_phi;                   // QG_NLRF*G accumulators
     float *g_phif;                  // QG_NPHI*G Taylor coefficients
     // neighbour list of a group: water neighbours first (as their O atom),
     // then solute neighbours (as group index); nb_nw = number of water entries
@@ -186,7 +191,7 @@ struct DevSys {
     int nshk_mol;
     // energies and reductions
     unsigned long long *eacc;       // QG_NE per trajectory
-    double *ekin_part;              // 4 per Ekin block
+    float *ekin_part;               // 4 per Ekin block
     int *status;
 };
 
@@ -335,7 +340,12 @@ struct BlockTables {
     const int *scan_t0; const int *scan_tn; const int *scan_traj; const int *scan_chunk; int nscan;  // scan blocks
     const int *gall; int ngall;        // all groups (centres)
     const int *uitem; int nuitem;      // update items (atoms, or (1<<30)|shake molecule), padded
+    // fused update, one thread per atom in blocks of QG_UBLK: unconstrained
+    // atoms first, then 32 waters (96 atoms) per block; ucon = first
+    // constraint of the water whose first atom is in that slot, else -1
+    const int *uatom, *ucon; const uint8_t *ublk_water; int nuatom;
     const int *qqblk_traj, *qqblk_s; int nqqblk;
+    int max_nqat;                      // largest Q-atom count of a trajectory
 };
 
 void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L);
@@ -364,7 +374,7 @@ void launch_shake(const DevSys &S, const BlockTables &B, LaunchCtx &L, int traj_
 void launch_update(const DevSys &S, const BlockTables &B, LaunchCtx &L, int mode);
 // the fused step with the float master; writes x/v as well when the next
 // step lists or records (e: the record selector of this step, nbcycle)
-void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int nbcycle);
+void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int nbcycle, int ekin_only);
 // x = origin + hi + lo, v = velf for every atom
 void launch_sync_double(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *rec, const int *rec_base, int k,
