@@ -38,58 +38,68 @@ WORKLOAD = ("lambda-window batch: 21 windows of the 18 A droplet (8 Q atoms, 2 s
 
 
 # ------------------------------------------------------------ CPU arm
-def _cpu_sample(args):
-    """One oracle trajectory sample: a list build + nsteps MD steps (FP64 C
-    restatement of the reference, one core).  Returns seconds per step."""
-    kind, rank, nsteps = args
+NTRAJ = 32
+
+
+def _cpu_traj(args):
+    """One trajectory of the batch on one host core with the FP64 C
+    restatement of the reference: `warm` untimed steps, then `nsteps` timed
+    steps (lists every 10 steps, Berendsen leap-frog, SHAKE).  Returns the
+    timed seconds."""
+    i, warm, nsteps = args
     sys.path.insert(0, ROOT)
     from qsource_gb300 import synth
     from oracle.oracle import Oracle
-    s = _representatives(rank)[kind]
-    o = Oracle(s)
+    o = Oracle(synth.lambda_batch_member(i))
     o.temperature()
+    if warm:
+        o.md_run(warm)
     t0 = time.perf_counter()
     rc, _, _, _ = o.md_run(nsteps)
     dt = time.perf_counter() - t0
-    return kind, dt / nsteps, rc
+    if rc:
+        raise RuntimeError(f"oracle trajectory {i}: status {rc}")
+    return i, dt
 
 
-def _representatives(rank=0):
-    from qsource_gb300 import synth
-    import numpy as np
-    qa = synth.neutral_charges(np.random.default_rng(1000), 8, 0.4)
-    reps = {"window": synth.config(1, window=10, replica=rank)}
-    for R, ns in ((20.0, 800), (25.0, 1500), (30.0, 2000)):
-        reps[f"R{int(R)}"] = synth.synthetic(R, ns, 8, np.stack([qa, np.zeros(8)], 1), (0.5, 0.5), 3000 + rank)
-    return reps
+def _makespan(times, cores):
+    """Wall time of running the given per-trajectory times on `cores` cores,
+    longest first, each trajectory on the first free core."""
+    free = [0.0] * cores
+    for t in sorted(times, reverse=True):
+        k = free.index(min(free))
+        free[k] += t
+    return max(free)
 
 
-def _batch_kinds():
-    """Which representative stands for each of the 32 trajectories."""
-    kinds = ["window"] * 21
-    radii = (20, 25, 30)
-    for r in range(11):
-        kinds.append(f"R{radii[r % 3]}")
-    return kinds
+def cpu_pool():
+    """Process pool over every host core; started with spawn before any CUDA
+    call of the parent process."""
+    return mp.get_context("spawn").Pool(os.cpu_count() or 1)
 
 
-def cpu_baseline(pool, nsteps: int, rank: int = 0):
-    """Aggregate ns/day of the oracle on all host cores: every core runs one
-    trajectory at a time; the batch step costs sum(t_traj) / cores."""
-    cores = os.cpu_count() or 1
-    jobs = [(k, rank, nsteps) for k in ("window", "R20", "R25", "R30")]
+def cpu_baseline(pool, nsteps: int, warm: int = 0):
+    """Aggregate ns/day of the 32-trajectory batch on the host cores: every
+    trajectory is timed on its own core (all cores busy at once); the batch
+    wall time is the makespan of those times on the pool's cores."""
+    cores = pool._processes
+    jobs = [(i, warm, nsteps) for i in range(NTRAJ)]
+    # longest trajectories (the replicas) first
+    jobs.sort(key=lambda j: -j[0])
     t0 = time.perf_counter()
-    res = pool.map(_cpu_sample, jobs)
+    res = dict(pool.map(_cpu_traj, jobs, chunksize=1))
     wall = time.perf_counter() - t0
-    per = {k: t for k, t, rc in res}
-    step_cpu = sum(per[k] for k in _batch_kinds())
-    batch_step = step_cpu / cores
-    nsday = len(_batch_kinds()) * FS_PER_STEP * 1e-6 * 86400.0 / batch_step
-    sample = (f"oracle (FP64 C restatement) on {cores} host cores: one list build + {nsteps} Berendsen/SHAKE steps "
-              f"of the 18 A window and of 20/25/30 A replicas, extrapolated to the 32-trajectory batch "
-              f"({', '.join(f'{k} {v * 1e3:.1f} ms/step' for k, v in per.items())}; sample wall {wall:.1f} s)")
+    times = [res[i] for i in range(NTRAJ)]
+    span = _makespan(times, cores)
+    batch_step = span / nsteps
+    nsday = NTRAJ * FS_PER_STEP * 1e-6 * 86400.0 / batch_step
+    sample = (f"oracle (FP64 C restatement of the reference loops) on {cores} host cores, one trajectory per core: "
+              f"all {NTRAJ} trajectories of the batch, {warm} untimed + {nsteps} timed Berendsen/SHAKE steps each "
+              f"(lists every {NB} steps); batch step = makespan of the per-trajectory times on {cores} cores "
+              f"({span:.2f} s for {nsteps} steps; single-core sum {sum(times):.2f} s; pool wall incl. set-up "
+              f"{wall:.1f} s)")
     return {"value": round(nsday, 4), "unit": "ns/day", "cores": cores, "kind": "port", "sample": sample,
-            "ms_per_batch_step": batch_step * 1e3}
+            "ms_per_batch_step": batch_step * 1e3, "single_core_ms_per_batch_step": 1e3 * sum(times) / nsteps}
 
 
 # --------------------------------------------------------- clocks
@@ -105,7 +115,7 @@ class Clocks:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -187,10 +197,11 @@ def kernel_flops(name, wc):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=10)
+    ap.add_argument("--cpu-steps", type=int, default=20, help="timed oracle steps of the CPU baseline")
+    ap.add_argument("--ref-max-steps", type=int, default=100, help="cap on the reference arm's timed steps")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -202,26 +213,23 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        ctx = mp.get_context("spawn")
-        with ctx.Pool(min(4, os.cpu_count() or 1)) as pool:
-            per_step = []
-            base = None
-            for _ in range(max(1, min(3, args.steps // 100))):
-                base = cpu_baseline(pool, args.cpu_steps)
-                per_step.append(base["ms_per_batch_step"])
-        ms = sum(per_step) / len(per_step)
+        # the whole K-step run of the batch, capped so that it ends in minutes
+        ksteps = min(steps, args.ref_max_steps)
+        with cpu_pool() as pool:
+            base = cpu_baseline(pool, ksteps, warm=min(warm, NB))
         out = {"metric": METRIC, "value": base["value"], "unit": "ns/day", "impl": "reference", "n_gpus": args.gpus,
-               "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
-               "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-               "config": {"workload": WORKLOAD, "trajectories": 32, "dt_fs": 1.0, "nbcycle": NB,
-                          "parallelism": "host cores, one trajectory per core"},
+               "steps": ksteps, "warmup": min(warm, NB), "ms_per_step": round(base["ms_per_batch_step"], 3),
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+               "data": "synthetic (seeded water spheres, random-init)",
+               "config": {"workload": WORKLOAD, "trajectories": NTRAJ, "dt_fs": FS_PER_STEP, "nbcycle": NB,
+                          "parallelism": f"host cores ({base['cores']}), one trajectory per core"},
                "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
                "e2e": {"value": base["value"], "unit": "ns/day", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
         return
 
     # the CPU-baseline pool is started before the first CUDA call
-    pool = mp.get_context("spawn").Pool(min(4, os.cpu_count() or 1)) if rank == 0 and not args.no_cpu else None
+    pool = cpu_pool() if rank == 0 and not args.no_cpu else None
     import numpy as np
     import torch
     dist = None

@@ -17,6 +17,18 @@ __global__ void k_mirror(DevSys S) {
     S.velf[i] = make_float4((float)S.v[3 * i], (float)S.v[3 * i + 1], (float)S.v[3 * i + 2], 0.f);
 }
 
+__global__ void k_wrec(DevSys S, const int *wgrp, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int w = wgrp[k];
+    if (w < 0) return;
+    const int a0 = S.g_atoms[S.g_start[w]];
+    float4 h[3], l[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { h[a] = S.pos[a0 + a]; l[a] = S.poslo[a0 + a]; }
+    put_wrec(S.wrec + a0, h, l);
+}
+
 // cgp_centers, src/md.f90:2253-2288: mean of the member coordinates (FP64),
 // and its float offset from the trajectory origin for the per-step kernels.
 __global__ void k_centers(DevSys S) {
@@ -239,11 +251,19 @@ __global__ void k_qmember(DevSys S, int first) {
 
 static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 
+void launch_wrec(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
+    if (!B.nwgrp) return;
+    prof_begin(L, "k_wrec");
+    k_wrec<<<nblk(B.nwgrp, 256), 256, 0, L.stream>>>(S, B.wgrp, B.nwgrp);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
 void launch_mirror(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
     prof_begin(L, "k_mirror");
     k_mirror<<<nblk(S.natom, 256), 256, 0, L.stream>>>(S);
     prof_end(L);
     (*L.nlaunch)++;
+    launch_wrec(S, B, L);
 }
 void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
     prof_begin(L, "k_centers");

@@ -283,6 +283,7 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
             hilo_add(h.z, l.z, D.z);
             S.pos[a] = h; S.poslo[a] = l;
             S.velf[a] = make_float4(v.x, v.y, v.z, 0.f);
+            if (water_blk) { s_h[t] = h; s_l[t] = l; }
             if (want_x) {
                 S.x[3 * a] = T.origin[0] + ((double)h.x + (double)l.x);
                 S.x[3 * a + 1] = T.origin[1] + ((double)h.y + (double)l.y);
@@ -294,6 +295,18 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
         const bool fr = !S.aexcl[a];
         if ((a - T.atom0) < T.nat_solute) { ek[0] = e; ek[1] = fr ? e : 0.f; }
         else { ek[2] = e; ek[3] = fr ? e : 0.f; }
+    }
+    if (water_blk && !ekin_only) {
+        // packed water records of the new positions
+        __syncthreads();
+        if (t < 32) {
+            const int c0 = ucon[blockIdx.x * QG_UBLK + 3 * t];
+            if (c0 >= 0) {
+                const float4 wh[3] = {s_h[3 * t], s_h[3 * t + 1], s_h[3 * t + 2]};
+                const float4 wl[3] = {s_l[3 * t], s_l[3 * t + 1], s_l[3 * t + 2]};
+                put_wrec(S.wrec + uatom[blockIdx.x * QG_UBLK + 3 * t], wh, wl);
+            }
+        }
     }
     const int lane = t & 31, warp = t >> 5;
 #pragma unroll

@@ -96,16 +96,30 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_water(DevSys S, const int *wgrp
         const int n = S.nb_count[w], nw = S.nb_nw[w];
         const int *lst = S.nb_list + (size_t)w * S.nb_cap;
         const float wwA = T.ww_A, wwB = T.ww_B;
-        // water neighbours: 3x3 SPC pairs, LJ on O-O only (nonbond_ww_spc)
-        auto ww = [&](int b0, const float4 *bh, const float4 *bl) {
+        // water neighbours: 3x3 SPC pairs with the charge products of the
+        // solvent table, LJ on O-O only (nonbond_ww_spc).  Both waters come
+        // from their packed records: O as hi/lo, H as float offsets from O.
+        // d = dO + (db - da) is formed so that the opposite side of the pair
+        // computes exactly -d.
+        float qq[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) qq[c] = T.wwqq[c];
+        const float4 r0 = S.wrec[a0], r1 = S.wrec[a0 + 1], r2 = S.wrec[a0 + 2];
+        const float3 da[3] = {make_float3(0.f, 0.f, 0.f), make_float3(r0.w, r1.w, r2.x), make_float3(r2.y, r2.z, r2.w)};
+        auto ww = [&](int b0, const float4 q0, const float4 q1, const float4 q2) {
+            const float3 dO = make_float3((q0.x - r0.x) + (q1.x - r1.x), (q0.y - r0.y) + (q1.y - r1.y),
+                                          (q0.z - r0.z) + (q1.z - r1.z));
+            const float3 db[3] = {make_float3(0.f, 0.f, 0.f), make_float3(q0.w, q1.w, q2.x),
+                                  make_float3(q2.y, q2.z, q2.w)};
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
 #pragma unroll
                 for (int b = 0; b < 3; ++b) {
-                    const float3 d = dpos(ah[a], al[a], bh[b], bl[b]);
+                    const float3 d = make_float3(dO.x + (db[b].x - da[a].x), dO.y + (db[b].y - da[a].y),
+                                                 dO.z + (db[b].z - da[a].z));
                     const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
                     const float ri = rsqrtf(r2), ri2 = ri * ri;
-                    const float Vel = ah[a].w * bh[b].w * ri;
+                    const float Vel = qq[3 * a + b] * ri;
                     float dv = -Vel * ri2;
                     double rid = 0.0;
                     if (EACC) rid = rinv_d(S.x, a0 + a, b0 + b);
@@ -130,21 +144,14 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_water(DevSys S, const int *wgrp
         int k = lane;
         for (; k + QG_LW < nw; k += 2 * QG_LW) {
             const int b0 = lst[k], b1 = lst[k + QG_LW];
-            float4 bh0[3], bl0[3], bh1[3], bl1[3];
-#pragma unroll
-            for (int b = 0; b < 3; ++b) {
-                bh0[b] = S.pos[b0 + b]; bl0[b] = S.poslo[b0 + b];
-                bh1[b] = S.pos[b1 + b]; bl1[b] = S.poslo[b1 + b];
-            }
-            ww(b0, bh0, bl0);
-            ww(b1, bh1, bl1);
+            const float4 p0 = S.wrec[b0], p1 = S.wrec[b0 + 1], p2 = S.wrec[b0 + 2];
+            const float4 s0 = S.wrec[b1], s1 = S.wrec[b1 + 1], s2 = S.wrec[b1 + 2];
+            ww(b0, p0, p1, p2);
+            ww(b1, s0, s1, s2);
         }
         if (k < nw) {
             const int b0 = lst[k];
-            float4 bh0[3], bl0[3];
-#pragma unroll
-            for (int b = 0; b < 3; ++b) { bh0[b] = S.pos[b0 + b]; bl0[b] = S.poslo[b0 + b]; }
-            ww(b0, bh0, bl0);
+            ww(b0, S.wrec[b0], S.wrec[b0 + 1], S.wrec[b0 + 2]);
         }
         // solute neighbours (the water side of nonbond_pw)
         for (int kk = nw + lane; kk < n; kk += QG_LW) {

@@ -213,6 +213,8 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
             T.origin[k] = d.xwcent[k]; T.xpcent[k] = d.xpcent[k]; T.xwcent[k] = d.xwcent[k];
             T.chg_solv[k] = (float)d.chg_solv[k];
         }
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) T.wwqq[3 * a + b] = (float)(d.chg_solv[a] * d.chg_solv[b]);
         T.rwat = d.rwat; T.fk_wsphere = d.fk_wsphere; T.Dwmz = d.Dwmz; T.awmz = d.awmz;
         T.fk_pshell = d.fk_pshell; T.fk_fix = d.fk_fix;
         T.fk_wspheref = (float)d.fk_wsphere; T.rwatf = (float)d.rwat; T.Dwmzf = (float)d.Dwmz; T.awmzf = (float)d.awmz;
@@ -354,6 +356,11 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
                         owner[lo + k] = m;
                     }
                 }
+            // the fused update writes the packed water records only in its
+            // water blocks: every water must be one of them
+            if (fuse)
+                for (int i = d.nat_solute; i < N; ++i)
+                    if (owner[i] < 0) fuse = false;
             h->fused.push_back(fuse);
             s0 = uitem.size();
             T.ekin_blk0 = (int)(uitem.size() / QG_BLOCK);
@@ -573,6 +580,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     UP(pos, pos);
     if ((rc = alloc0(A, (size_t)atom0, &S.poslo))) return rc;
     if ((rc = alloc0(A, (size_t)atom0, &S.velf))) return rc;
+    if ((rc = alloc0(A, (size_t)atom0, &S.wrec))) return rc;
     {
         // float copies for the per-step kernels; topology coordinates as hi/lo
         // offsets from each trajectory's origin
@@ -711,7 +719,7 @@ static void after_steps(qgpu_handle *h) { h->master = h->all_fused ? 1 : 0; }
 // Ekin partials of the update layout in use
 static void temperature_init(qgpu_handle *h, LaunchCtx &L) {
     if (h->all_fused) launch_update_f(h->S, h->B, L, EaccSel{EACC_FP32, h->zero_d, 0, 1}, h->NBcycle, 1);
-    else launch_update(h->S, h->B, L, 0);
+    else { launch_update(h->S, h->B, L, 0); launch_wrec(h->S, h->B, L); }
 }
 
 static void list_ops(qgpu_handle *h, LaunchCtx &L) {
@@ -768,6 +776,7 @@ static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every) {
         launch_integrate(h->S, h->B, L);
         launch_shake(h->S, h->B, L, -1);
         launch_update(h->S, h->B, L, 2);
+        launch_wrec(h->S, h->B, L);
     }
     launch_finalize(h->S, L, 1, h->rec_d, h->recctl_d, k, ene_every, h->rec_cap);
 }

@@ -64,6 +64,7 @@ struct TrajInfo {
     float ww_A, ww_B;           // O-O LJ products (aLJ_solv(1,c)^2, bLJ_solv(1,c)^2)
     double ww_Ad, ww_Bd;
     float chg_solv[3];
+    float wwqq[9];              // chg_solv(a)*chg_solv(b), nonbond_ww_spc charge products
     float el14;
     double el14d;
     float rc2_pp, rc2_pw, rc2_ww, rc2_lrf;   // float prefilter thresholds
@@ -120,6 +121,10 @@ struct DevSys {
     float4 *velf;
     const float *winvf, *massf;
     const float4 *xtoph, *xtopl;    // topology coordinates relative to the origin, hi/lo
+    // packed water record at the slots of each water's 3 atoms (O first):
+    //   [O] = (O_hi.xyz, d1.x)  [O+1] = (O_lo.xyz, d1.y)  [O+2] = (d1.z, d2.xyz)
+    // with dk = H_k - O in float: a neighbour water is 3 float4 loads.
+    float4 *wrec;
     const int *atype;               // global type index
     const double *crg_d;            // scaled charges (FP64)
     const int *aq;                  // global Q index or -1
@@ -315,6 +320,19 @@ __device__ __forceinline__ float3 dpos(const float4 ah, const float4 al, const f
     return make_float3((bh.x - ah.x) + (bl.x - al.x), (bh.y - ah.y) + (bl.y - al.y), (bh.z - ah.z) + (bl.z - al.z));
 }
 
+// Packed record of one water (see DevSys::wrec) from its hi/lo coordinates.
+__device__ __forceinline__ void put_wrec(float4 *wr, const float4 (&h)[3], const float4 (&l)[3]) {
+    float d[2][3];
+#pragma unroll
+    for (int k = 1; k < 3; ++k) {
+        d[k - 1][0] = (h[k].x - h[0].x) + (l[k].x - l[0].x);
+        d[k - 1][1] = (h[k].y - h[0].y) + (l[k].y - l[0].y);
+        d[k - 1][2] = (h[k].z - h[0].z) + (l[k].z - l[0].z);
+    }
+    wr[0] = make_float4(h[0].x, h[0].y, h[0].z, d[0][0]);
+    wr[1] = make_float4(l[0].x, l[0].y, l[0].z, d[0][1]);
+    wr[2] = make_float4(d[0][2], d[1][0], d[1][1], d[1][2]);
+}
 // exact FP64 squared distance in the reference's operation order (no FMA)
 __device__ __forceinline__ double dist2_exact(const double *x, int i, int j) {
     double a = __dsub_rn(x[3 * i], x[3 * j]);
@@ -380,5 +398,6 @@ void launch_sync_double(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *rec, const int *rec_base, int k,
                      int ene_every, int rec_cap);
 void launch_tick(LaunchCtx &L, int *rec_base, int n);
-void launch_mirror(const DevSys &S, const BlockTables &B, LaunchCtx &L);
+void launch_mirror(const DevSys &S, const BlockTables &B, LaunchCtx &L);   // also refreshes wrec
+void launch_wrec(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_grad_to_double(const DevSys &S, LaunchCtx &L, double *out, int atom0, int natom);
