@@ -203,6 +203,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=20, help="timed oracle steps of the CPU baseline")
     ap.add_argument("--ref-max-steps", type=int, default=100, help="cap on the reference arm's timed steps")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                    help="MD step precision (qgpu_set_precision): double-float master / FP64 master")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -247,6 +249,9 @@ def main():
     ntraj = len(systems)
     natoms = sum(s.natom for s in systems)
     eng = Engine(systems)
+    if args.precision == "fp64":
+        from qsource_gb300.abi import QGPU_PRECISION_FP64
+        eng.set_precision(QGPU_PRECISION_FP64)
     eng.enqueue(warm, 0)
     eng.sync()
 
@@ -328,7 +333,8 @@ def main():
         "config": {"workload": WORKLOAD, "trajectories": ntraj, "atoms": natoms, "dt_fs": FS_PER_STEP, "nbcycle": NB,
                    "timed": f"{nblk} blocks of {NB} steps, each one CUDA-graph replay",
                    "l2": "flushed before every timed 10-step block (256 MB write on the engine stream)",
-                   "parallelism": "replicas" if world > 1 else "single GPU, one handle"},
+                   "parallelism": "replicas" if world > 1 else "single GPU, one handle",
+                   "precision": args.precision},
         "e2e": {"value": round(e2e, 3), "unit": "ns/day", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "how": "per 10-step block: upload x,v of all 32 trajectories from pinned memory, qgpu_run with an "
                        "energy sink, read back x,v (host wall clock)"},

@@ -174,6 +174,12 @@ typedef struct qgpu_system_desc {
     int32_t NBcycle;
     int32_t Ndegf, Ndegfree, Ndegf_solvent, Ndegfree_solvent;
     int32_t Ndegf_solute, Ndegfree_solute, detail_temps;
+
+    /* list variant: 0 = switch-atom cut-off (topology flag iuse_switch_atom = 1,
+       nbpplist_lrf/nbpwlist_lrf/nbqplist); 1 = any-atom cut-off for solute
+       groups (iuse_switch_atom = 0, nbpplis2_lrf src/md.f90:7441,
+       nbpwlis2_lrf :8902, nbqplis2 :9946) */
+    int32_t any_atom_lists;
 } qgpu_system_desc;
 
 /* Energies, the ENERGIES record of src/nrgy.f90:48-54 (sphere subset). */
@@ -255,6 +261,21 @@ int qgpu_shake(qgpu_handle *h, int32_t traj, const double *xx, double *x, int32_
 int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every,
              qgpu_ene_sink sink, void *user);
 
+/* Precision of the persistent MD step (qgpu_run / qgpu_enqueue).
+   QGPU_PRECISION_MIXED (the default): master positions as a double-float
+     (about 48 significant bits), FP32 velocities, SHAKE of 3-site waters in
+     FP32 on relative vectors, FP32 bonded/restraint terms on unrecorded steps;
+     FP64 energies on recorded steps.  Used when every trajectory's
+     constraints are 3-site waters (O-H, O-H, H-H), else the FP64 form runs.
+   QGPU_PRECISION_FP64: FP64 master x and v with the reference's FP64
+     leap-frog (newvel_ber, src/md.f90:6194-6223) and FP64 SHAKE
+     (src/md.f90:17581-17679) every step.
+   Pair terms are FP32 with int64 fixed-point sums in both.  Switching keeps
+   the current coordinates and velocities. */
+#define QGPU_PRECISION_MIXED 0
+#define QGPU_PRECISION_FP64  1
+int qgpu_set_precision(qgpu_handle *h, int32_t mode);
+
 /* Queues nsteps of the same device work as qgpu_run without waiting for it
    (no energy sink); a failure surfaces at the next qgpu_sync or qgpu_run. */
 int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every);
@@ -290,7 +311,8 @@ int qgpu_fp32_peak(double *tflops);
    device memory -- a host program whose device memory belongs to its own
    allocator or to a pool reserved once at start-up, or a time-step loop in
    which a cudaMalloc (which can synchronise the device) is not allowed: the
-   charge-group scan of qgpu_build_lists for ONE system, on arrays the caller
+   charge-group scan of qgpu_build_lists (switch-atom cut-off, topology flag
+   iuse_switch_atom = 1) for ONE system, on arrays the caller
    already holds on the device, with no engine handle.  It allocates nothing:
    its chunk partials live in a fixed 8 MiB device array of the library, held
    by every device that loads it until the process exits.

@@ -303,6 +303,92 @@ static void nbpwlist_lrf(oracle *o) {
     }
 }
 
+/* Any-atom cut-off of a solute group pair (nbpplis2_lrf, src/md.f90:7518-7545):
+   inside when some atom pair of the two groups (Q atoms included) lies within
+   the cut-off.  *r2_last is the last distance the reference's loop computed:
+   the pair (last atom of ig, last atom of jg) when no pair is inside. */
+static int any_atom_inside(const oracle *o, int ig, int jg, double rc2, double *r2_last) {
+    const qgpu_system_desc *d = &o->d;
+    double r2 = 0.0;
+    for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig]; ++ka)
+        for (int kb = d->cgp_first[jg]; kb <= d->cgp_last[jg]; ++kb) {
+            r2 = dist2(o->x, d->cgpatom[ka], d->cgpatom[kb]);
+            if (r2 <= rc2) { *r2_last = r2; return 1; }
+        }
+    *r2_last = r2;
+    return 0;
+}
+
+/* nbpplis2_lrf, src/md.f90:7441-7627 (iuse_switch_atom = 0) */
+static void nbpplis2_lrf(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    double rc2 = d->Rcpp * d->Rcpp, rl2 = d->RcLRF * d->RcLRF;
+    o->pp.n = 0;
+    for (int ig = 0; ig < d->ncgp_solute; ++ig) {
+        if (d->excl[d->cgp_switch[ig]]) continue;
+        for (int jg = 0; jg < d->ncgp_solute; ++jg) {
+            if (parity_skip(ig, jg)) continue;
+            if (d->excl[d->cgp_switch[jg]]) continue;
+            double r2;
+            if (any_atom_inside(o, ig, jg, rc2, &r2)) {
+                for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig]; ++ka) {
+                    int i = d->cgpatom[ka];
+                    if (is_q(o, i)) continue;
+                    for (int kb = d->cgp_first[jg]; kb <= d->cgp_last[jg]; ++kb) {
+                        int j = d->cgpatom[kb];
+                        if (is_q(o, j)) continue;
+                        if (ig == jg && i >= j) continue;
+                        if (excluded(o, i, j)) continue;
+                        int lj = ljcod(o, d->iac[i], d->iac[j]);
+                        if (is14(o, i, j)) lj = 3;
+                        nb_push(&o->pp, i, j, lj, lj);
+                    }
+                }
+            } else if (d->use_LRF && r2 <= rl2) {
+                lrf_update(o, ig, jg);
+                lrf_update(o, jg, ig);
+            }
+        }
+    }
+}
+
+/* nbpwlis2_lrf, src/md.f90:8902-9043 (iuse_switch_atom = 0): a solute group
+   and a water are inside when some atom of the group lies within Rcpw of the
+   water O; otherwise the LRF test uses the group's last atom. */
+static void nbpwlis2_lrf(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    double rc2 = d->Rcpw * d->Rcpw, rl2 = d->RcLRF * d->RcLRF;
+    o->pw.n = 0;
+    for (int ig = 0; ig < d->ncgp_solute; ++ig) {
+        if (d->excl[d->cgp_switch[ig]]) continue;
+        for (int jw = 0; jw < d->nwat; ++jw) {
+            int ja = d->nat_solute + 3 * jw;
+            if (d->excl[ja]) continue;
+            int jg = o->iwhich[ja];
+            int inside = 0;
+            double r2 = 0.0;
+            for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig] && !inside; ++ka) {
+                r2 = dist2(o->x, d->cgpatom[ka], ja);
+                if (r2 <= rc2) inside = 1;
+            }
+            if (inside) {
+                for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig]; ++ka) {
+                    int i = d->cgpatom[ka];
+                    if (is_q(o, i)) continue;
+                    for (int s = 0; s < 3; ++s) {
+                        int j = ja + s;
+                        if (all_zero(o, i, j)) continue;
+                        nb_push(&o->pw, i, j, ljcod(o, d->iac[i], d->iac[j]), 0);
+                    }
+                }
+            } else if (d->use_LRF && r2 <= rl2) {
+                lrf_update(o, ig, jg);
+                lrf_update(o, jg, ig);
+            }
+        }
+    }
+}
+
 /* nbqplist, src/md.f90:10215-10322 (built once when Rcq > rexcl_o) */
 static void nbqplist(oracle *o) {
     const qgpu_system_desc *d = &o->d;
@@ -313,8 +399,19 @@ static void nbqplist(oracle *o) {
     for (int ig = 0; ig < d->ncgp_solute; ++ig) {
         int ia = d->cgp_switch[ig];
         if (d->excl[ia]) continue;
-        double a = o->x[3 * ia] - d->xpcent[0], b = o->x[3 * ia + 1] - d->xpcent[1], c = o->x[3 * ia + 2] - d->xpcent[2];
-        if (a * a + b * b + c * c > rc2) continue;
+        int inside = 0;
+        if (d->any_atom_lists) {
+            /* nbqplis2, src/md.f90:9946-10071: any atom of the group within Rcq */
+            for (int k = d->cgp_first[ig]; k <= d->cgp_last[ig] && !inside; ++k) {
+                int i = d->cgpatom[k];
+                double a = o->x[3 * i] - d->xpcent[0], b = o->x[3 * i + 1] - d->xpcent[1], c = o->x[3 * i + 2] - d->xpcent[2];
+                inside = a * a + b * b + c * c <= rc2;
+            }
+        } else {
+            double a = o->x[3 * ia] - d->xpcent[0], b = o->x[3 * ia + 1] - d->xpcent[1], c = o->x[3 * ia + 2] - d->xpcent[2];
+            inside = a * a + b * b + c * c <= rc2;
+        }
+        if (!inside) continue;
         for (int k = d->cgp_first[ig]; k <= d->cgp_last[ig]; ++k) {
             int i = d->cgpatom[k];
             if (d->qp_skip[i]) continue;
@@ -378,12 +475,17 @@ static void nbqwlist(oracle *o) {
     o->qw_done = 1;
 }
 
-/* make_pair_lists, sphere + LRF + switch atoms branch, src/md.f90:6043-6058 */
+/* make_pair_lists, sphere + LRF branch, src/md.f90:6043-6058 (switch-atom or any-atom lists) */
 void oracle_make_pair_lists(void *h) {
     oracle *o = (oracle *)h;
     if (o->d.use_LRF) cgp_centers(o);
-    nbpplist_lrf(o);
-    nbpwlist_lrf(o);
+    if (o->d.any_atom_lists) {
+        nbpplis2_lrf(o);
+        nbpwlis2_lrf(o);
+    } else {
+        nbpplist_lrf(o);
+        nbpwlist_lrf(o);
+    }
     nbqplist(o);
     nbwwlist_lrf(o);
     nbqwlist(o);

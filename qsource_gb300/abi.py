@@ -20,6 +20,8 @@ QGPU_TERMS_BONDED = 0x8
 QGPU_TERMS_RESTRAINT = 0x10
 QGPU_TERMS_ALL = 0x1F
 QGPU_TERMS_STEP_PRECISION = 0x100
+QGPU_PRECISION_MIXED = 0
+QGPU_PRECISION_FP64 = 1
 
 STATUS = {0: "ok", 1: "invalid", 2: "cuda", 3: "list overflow", 4: "shake failure", 5: "nan",
           6: "unsupported", 7: "fixed-point range"}
@@ -64,6 +66,7 @@ class SystemDesc(C.Structure):
         ("dt", _f64), ("Temp0", _f64), ("tau_T", _f64), ("separate_scaling", _i32), ("NBcycle", _i32),
         ("Ndegf", _i32), ("Ndegfree", _i32), ("Ndegf_solvent", _i32), ("Ndegfree_solvent", _i32),
         ("Ndegf_solute", _i32), ("Ndegfree_solute", _i32), ("detail_temps", _i32),
+        ("any_atom_lists", _i32),
     ]
 
 
@@ -109,6 +112,7 @@ EXPORTS = {
     "qgpu_shake": (_i32, [C.c_void_p, _i32, _P, _P, C.POINTER(_i32)]),
     "qgpu_run": (_i32, [C.c_void_p, _i32, _i32, ENE_SINK, C.c_void_p]),
     "qgpu_enqueue": (_i32, [C.c_void_p, _i32, _i32]),
+    "qgpu_set_precision": (_i32, [C.c_void_p, _i32]),
     "qgpu_sync": (_i32, [C.c_void_p]),
     "qgpu_get_group_pairs": (_i32, [C.c_void_p, _i32, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "qgpu_get_lrf": (_i32, [C.c_void_p, _i32, _P]),

@@ -44,7 +44,17 @@ __global__ void k_centers(DevSys S) {
     const double m0 = c0 / n, m1 = c1 / n, m2 = c2 / n;
     S.g_cent[3 * g] = m0; S.g_cent[3 * g + 1] = m1; S.g_cent[3 * g + 2] = m2;
     const TrajInfo &T = S.traj[S.g_traj[g]];
-    S.g_centf[g] = make_float4((float)(m0 - T.origin[0]), (float)(m1 - T.origin[1]), (float)(m2 - T.origin[2]), 0.f);
+    // .w: distance from the switch atom to the farthest member (rounded up),
+    // the bound of the any-atom cut-off test (nb*lis2*)
+    const int sw = S.g_switch[g];
+    double e2 = 0.0;
+    for (int k = a0; k < a1; ++k) {
+        const int a = S.g_atoms[k];
+        const double dx = S.x[3 * a] - S.x[3 * sw], dy = S.x[3 * a + 1] - S.x[3 * sw + 1], dz = S.x[3 * a + 2] - S.x[3 * sw + 2];
+        e2 = fmax(e2, dx * dx + dy * dy + dz * dz);
+    }
+    const float ext = (float)sqrt(e2) * (1.f + 1e-5f) + 1e-4f;
+    S.g_centf[g] = make_float4((float)(m0 - T.origin[0]), (float)(m1 - T.origin[1]), (float)(m2 - T.origin[2]), ext);
 }
 
 // Cut-off decision of the list builders (nbpplist_lrf :8083-8090,
@@ -56,6 +66,16 @@ __device__ __forceinline__ bool within(float d2, float rc2, double drc2, const d
     if (d2 > rc2 * (1.f + 1e-5f)) return false;
     return dist2_exact(x, a, b) <= drc2;
 }
+// the same with a 1e-4 band, for distances from hi-only float coordinates
+__device__ __forceinline__ bool within_hi(float d2, float rc2, double drc2, const double *x, int a, int b) {
+    if (d2 < rc2 * (1.f - 1e-4f)) return true;
+    if (d2 > rc2 * (1.f + 1e-4f)) return false;
+    return dist2_exact(x, a, b) <= drc2;
+}
+__device__ __forceinline__ float d2hi(const float4 a, const float4 b) {
+    const float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+    return dx * dx + dy * dy + dz * dz;
+}
 
 // Phase 1 of the scan: one thread per target charge group, one block per
 // (128 targets, source chunk of QG_TPC shared-memory tiles of the same
@@ -64,11 +84,13 @@ __device__ __forceinline__ bool within(float d2, float rc2, double drc2, const d
 // groups inside RcLRF add their non-Q atoms to the target's multipole
 // expansion (lrf_update, src/md.f90:5896-5981), accumulated as 24 symmetric
 // FP32 sums per chunk.
+template <bool ANY>
 __global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, const int *blk_tn, const int *blk_traj,
                                                    const int *blk_chunk) {
     __shared__ float4 s_hi[QG_TILE_G], s_lo[QG_TILE_G];
     __shared__ int s_meta[QG_TILE_G], s_rep[QG_TILE_G], s_aoff[QG_TILE_G + 1];
     __shared__ float4 s_atom[QG_TILE_A];
+    __shared__ float s_ext[QG_TILE_G];
     const int b = blockIdx.x;
     const TrajInfo &T = S.traj[blk_traj[b]];
     const int chunk = blk_chunk[b];
@@ -79,13 +101,32 @@ __global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, 
     bool active = false;
     float4 th = make_float4(0, 0, 0, 0), tl = th;
     float cx = 0, cy = 0, cz = 0;
+    float ext_t = 0.f;
+    int ta0 = 0, ta1 = 0;
+    const bool any_atom = ANY && T.any_atom != 0;
+    // any-atom test: the target's first QG_TREG atoms in registers (a water
+    // target takes part by its O only); tlast = the group's last atom
+    // (per-thread slots in shared memory keep them out of the registers)
+    __shared__ float4 s_tp[ANY ? QG_TREG + 1 : 1][QG_BLOCK];
+    __shared__ int s_ti[ANY ? QG_TREG + 1 : 1][QG_BLOCK];
+    int ntreg = 0;
     if (valid) {
         kind_t = S.g_kind[t];
         rt = S.g_switch[t];
         active = !S.g_excl[t];
         th = S.pos[rt]; tl = S.poslo[rt];
         const float4 c = S.g_centf[t];
-        cx = c.x; cy = c.y; cz = c.z;
+        cx = c.x; cy = c.y; cz = c.z; ext_t = c.w;
+        ta0 = S.g_start[t]; ta1 = kind_t ? ta0 + 1 : S.g_start[t + 1];
+        if (any_atom) {
+            ntreg = min(ta1 - ta0, QG_TREG);
+            for (int k = 0; k < ntreg; ++k) {
+                const int a = S.g_atoms[ta0 + k];
+                s_ti[k][tid] = a; s_tp[k][tid] = S.pos[a];
+            }
+            const int la = kind_t ? rt : S.g_atoms[S.g_start[t + 1] - 1];
+            s_ti[ANY ? QG_TREG : 0][tid] = la; s_tp[ANY ? QG_TREG : 0][tid] = S.pos[la];
+        }
     }
     const long long slot = T.scr0 + (long long)chunk * T.ncgp + (t - T.grp0);
     int *nbseg = S.scr_nb + (size_t)slot * QG_CAPC;
@@ -104,6 +145,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, 
         for (int k = tid; k < ng; k += blockDim.x) {
             int g = g0 + k, ra = S.g_switch[g];
             s_hi[k] = S.pos[ra]; s_lo[k] = S.poslo[ra];
+            s_ext[k] = S.g_centf[g].w;
             s_meta[k] = S.g_kind[g] | (S.g_excl[g] ? 2 : 0);
             s_rep[k] = ra;
             s_aoff[k] = S.g_start[g] - ab;
@@ -128,12 +170,45 @@ __global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, 
                 else { rc2 = T.rc2_pp; drc2 = T.drc2_pp; }
                 float3 d = dpos(th, tl, s_hi[s], s_lo[s]);
                 float d2 = d.x * d.x + d.y * d.y + d.z * d.z;
-                if (within(d2, rc2, drc2, S.x, rt, s_rep[s])) {
+                bool near_, far_lrf;
+                if (any_atom && !(kind_t & kind_s)) {
+                    // nbpplis2_lrf (src/md.f90:7518-7545) / nbpwlis2_lrf
+                    // (:8970-8985): inside when any atom pair is within the
+                    // cut-off (a water counts by its O); else the LRF test
+                    // on the last atom pair the reference's loop computed
+                    const int sa0 = ab + s_aoff[s], sa1 = ab + s_aoff[s + 1];
+                    const int sb1 = kind_s ? sa0 + 1 : sa1;   // a water source: its O only
+                    near_ = false;
+                    const float reach = sqrtf(rc2) + (kind_t ? 0.f : ext_t) + (kind_s ? 0.f : s_ext[s]);
+                    if (d2 <= reach * reach * (1.f + 1e-4f)) {
+                        for (int kb = sa0; kb < sb1 && !near_; ++kb) {
+                            const float4 pb = s_atom[kb - ab];
+                            const int jb = S.g_atoms[kb];
+                            for (int k = 0; k < ntreg && !near_; ++k)
+                                near_ = within_hi(d2hi(s_tp[k][tid], pb), rc2, drc2, S.x, s_ti[k][tid], jb);
+                            for (int ka = ta0 + QG_TREG; ka < ta1 && !near_; ++ka) {
+                                const int ia = S.g_atoms[ka];
+                                near_ = within_hi(d2hi(S.pos[ia], pb), rc2, drc2, S.x, ia, jb);
+                            }
+                        }
+                    }
+                    far_lrf = false;
+                    if (!near_ && lrf) {
+                        const int lk = kind_s ? sa0 : sa1 - 1;
+                        const int lt = ANY ? QG_TREG : 0;
+                        far_lrf = within_hi(d2hi(s_tp[lt][tid], s_atom[lk - ab]), rc2_lrf, T.drc2_lrf, S.x,
+                                            s_ti[lt][tid], S.g_atoms[lk]);
+                    }
+                } else {
+                    near_ = within(d2, rc2, drc2, S.x, rt, s_rep[s]);
+                    far_lrf = !near_ && lrf && within(d2, rc2_lrf, T.drc2_lrf, S.x, rt, s_rep[s]);
+                }
+                if (near_) {
                     // at most QG_CAPC groups per chunk: water neighbours (as
                     // their O atom) from the front, solute groups from the back
                     if (kind_s) nbseg[cntw++] = s_rep[s];
                     else nbseg[QG_CAPC - 1 - cnts++] = g;
-                } else if (lrf && within(d2, rc2_lrf, T.drc2_lrf, S.x, rt, s_rep[s])) {
+                } else if (far_lrf) {
                     for (int k = s_aoff[s]; k < s_aoff[s + 1]; ++k) {
                         const float4 p = s_atom[k];
                         if (p.w == 0.f) continue;
@@ -239,6 +314,15 @@ __global__ void k_qmember(DevSys S, int first) {
     int sw = S.g_switch[g];
     double a = S.x[3 * sw] - T.xpcent[0], b = S.x[3 * sw + 1] - T.xpcent[1], c = S.x[3 * sw + 2] - T.xpcent[2];
     bool in = !S.g_excl[g] && (a * a + b * b + c * c <= T.drcq2);
+    if (T.any_atom && !S.g_kind[g] && !S.g_excl[g]) {
+        // nbqplis2, src/md.f90:9946-10071: any atom of the group within Rcq
+        in = false;
+        for (int k = S.g_start[g]; k < S.g_start[g + 1] && !in; ++k) {
+            const int at = S.g_atoms[k];
+            a = S.x[3 * at] - T.xpcent[0]; b = S.x[3 * at + 1] - T.xpcent[1]; c = S.x[3 * at + 2] - T.xpcent[2];
+            in = a * a + b * b + c * c <= T.drcq2;
+        }
+    }
     if (S.g_kind[g]) {
         S.qw_member[sw] = in ? 1 : 0;
     } else {
@@ -273,7 +357,10 @@ void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
 }
 void launch_scan(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
     prof_begin(L, "k_scan");
-    k_scan<<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
+    if (B.any_atom)
+        k_scan<true><<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
+    else
+        k_scan<false><<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
     prof_end(L);
     (*L.nlaunch)++;
     prof_begin(L, "k_scan_reduce");

@@ -72,7 +72,7 @@ __global__ void k_shake(DevSys S, int traj_filter) {
         }
         nits++;
         if (ready == all) break;
-        if (nits >= SHAKE_MAX_ITER) { atomicOr(S.status, ST_SHAKE); break; }
+        if (nits >= SHAKE_MAX_ITER) { atomicOr(S.status, ST_SHAKE); atomicCAS(S.status + 1, 0, tr + 1); break; }
     }
     atomicAdd(&S.tstate[tr].shake_iters, nits);
 }
@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
                 const float2 d2[3] = {S.shk_d2hl[c0], S.shk_d2hl[c0 + 1], S.shk_d2hl[c0 + 2]};
                 bool fail = false;
                 nits = shake_water_f(wh, wl, ww, d2, wD, &fail);
-                if (fail) atomicOr(S.status, ST_SHAKE);
+                if (fail) { atomicOr(S.status, ST_SHAKE); atomicCAS(S.status + 1, 0, tr + 1); }
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const int q = 3 * t + k;
@@ -297,15 +297,14 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
         else { ek[2] = e; ek[3] = fr ? e : 0.f; }
     }
     if (water_blk && !ekin_only) {
-        // packed water records of the new positions
+        // packed water records of the new positions: thread t writes float4
+        // t % 3 of the record of water t / 3
         __syncthreads();
-        if (t < 32) {
-            const int c0 = ucon[blockIdx.x * QG_UBLK + 3 * t];
-            if (c0 >= 0) {
-                const float4 wh[3] = {s_h[3 * t], s_h[3 * t + 1], s_h[3 * t + 2]};
-                const float4 wl[3] = {s_l[3 * t], s_l[3 * t + 1], s_l[3 * t + 2]};
-                put_wrec(S.wrec + uatom[blockIdx.x * QG_UBLK + 3 * t], wh, wl);
-            }
+        const int w3 = t - t % 3;
+        if (ucon[blockIdx.x * QG_UBLK + w3] >= 0) {
+            const float4 wh[3] = {s_h[w3], s_h[w3 + 1], s_h[w3 + 2]};
+            const float4 wl[3] = {s_l[w3], s_l[w3 + 1], s_l[w3 + 2]};
+            S.wrec[uatom[blockIdx.x * QG_UBLK + w3] + t % 3] = wrec_part(wh, wl, t % 3);
         }
     }
     const int lane = t & 31, warp = t >> 5;

@@ -79,11 +79,17 @@ struct qgpu_handle {
     BlockTables B{};
     std::vector<void *> allocs;
     cudaStream_t stream = nullptr;
+    // side streams of the per-step force kernels, which are independent of
+    // one another (each adds into the fixed-point gradient and energies)
+    cudaStream_t side[QG_NSIDE] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[QG_NSIDE] = {};
     long long nlaunch = 0;
     int NBcycle = 10;
     int lists_built = 0, temp_init = 0, any_shake = 0, any_wpol = 0;
     std::vector<char> fused;   // per trajectory: SHAKE fused into the update kernel
     bool all_fused = true;
+    bool can_fuse = true;      // every trajectory's constraints allow the fused update
+    std::vector<int> ek_u0, ek_un, ek_a0, ek_an;   // Ekin block ranges of the two update layouts
     // 0: x/v and the float coordinates agree; 1: the float master (fused
     // steps) is newer than x/v
     int master = 0;
@@ -231,6 +237,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
             T.dt_tau = (float)(d.dt / d.tau_T); T.Temp0f = (float)d.Temp0;
         }
         T.separate_scaling = d.separate_scaling; T.detail_temps = d.detail_temps;
+        T.any_atom = d.any_atom_lists ? 1 : 0;
         T.Ndegf = d.Ndegf; T.Ndegfree = d.Ndegfree;
         T.Ndegfree_solute = d.Ndegfree_solute; T.Ndegfree_solvent = d.Ndegfree_solvent;
         T.ff_type = d.ff_type;
@@ -648,6 +655,8 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     S.nshk_mol = (int)shk_traj.size();
     if ((rc = alloc0(A, (size_t)ntraj * QG_NE, &S.eacc))) return rc;
     for (char f : h->fused) h->all_fused = h->all_fused && f;
+    h->can_fuse = h->all_fused;
+    h->ek_u0 = ek_u0; h->ek_un = ek_un; h->ek_a0 = ek_a0; h->ek_an = ek_an;
     {
         const size_t nblk_ek = std::max(uitem.size() / QG_BLOCK, uatom.size() / QG_UBLK) + 1;
         if ((rc = alloc0(A, (size_t)4 * nblk_ek, &S.ekin_part))) return rc;
@@ -658,7 +667,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         h->info[t].ekin_nblk = h->all_fused ? ek_an[t] : ek_un[t];
     }
     CK(cudaMemcpy((void *)S.traj, h->info.data(), h->info.size() * sizeof(TrajInfo), cudaMemcpyHostToDevice));
-    if ((rc = alloc0(A, 1, &S.status))) return rc;
+    if ((rc = alloc0(A, 2, &S.status))) return rc;   // [0] status bits, [1] 1 + trajectory of a SHAKE failure
     // block tables
     BlockTables &B = h->B;
     {
@@ -678,12 +687,18 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         if ((rc = upload(A, qqblk_s, &p))) return rc; B.qqblk_s = p; B.nqqblk = (int)qqblk_traj.size();
         B.max_nqat = 0;
         for (int t = 0; t < ntraj; ++t) B.max_nqat = std::max(B.max_nqat, h->info[t].nqat);
+        for (int t = 0; t < ntraj; ++t) B.any_atom |= h->info[t].any_atom;
     }
     if ((rc = alloc0(A, (size_t)ntraj * QG_REC, &h->ecur_d))) return rc;
     if ((rc = alloc0(A, 2, &h->zero_d))) return rc;
     if ((rc = alloc0(A, (size_t)3 * h->max_natom, &h->grad_d))) return rc;
     if ((rc = alloc0(A, 2, &h->recctl_d))) return rc;
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    for (int k = 0; k < QG_NSIDE; ++k) {
+        CK(cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->ev_join[k], cudaEventDisableTiming));
+    }
     // float mirror of the starting coordinates
     LaunchCtx L{h->stream, &h->nlaunch};
     launch_mirror(S, B, L);
@@ -693,15 +708,17 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
 }
 
 static int check_status(qgpu_handle *h) {
-    int st = 0;
-    CK(cudaMemcpyAsync(&st, h->S.status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    int stw[2] = {0, 0};
+    CK(cudaMemcpyAsync(stw, h->S.status, sizeof stw, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());
+    const int st = stw[0];
     if (!st) return 0;
-    int zero = 0;
-    CK(cudaMemcpy(h->S.status, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    const int zero[2] = {0, 0};
+    CK(cudaMemcpy(h->S.status, zero, sizeof zero, cudaMemcpyHostToDevice));
     if (st & ST_LIST_OVERFLOW) return fail(QGPU_E_LIST_OVERFLOW, "neighbour list capacity %d exceeded", h->S.nb_cap);
-    if (st & ST_SHAKE) return fail(QGPU_E_SHAKE, "shake failure: no convergence in 1000 iterations");
+    if (st & ST_SHAKE)
+        return fail(QGPU_E_SHAKE, "shake failure: no convergence in 1000 iterations (trajectory %d)", stw[1] - 1);
     if (st & ST_NAN) return fail(QGPU_E_NAN, "a detected NaN in the temperature");
     if (st & ST_FIXED) return fail(QGPU_E_FIXED_RANGE, "force or energy outside the fixed-point range");
     return fail(QGPU_E_CUDA, "device status %d", st);
@@ -730,14 +747,39 @@ static void list_ops(qgpu_handle *h, LaunchCtx &L) {
 
 // fp64_energy: every pair energy in FP64 (drop-in call); otherwise FP32 pair
 // energies, with FP64 Q-atom energies on recorded steps (esel).
+// The force kernels only read coordinates and tables and add into the
+// fixed-point gradient and energy accumulators (integer adds, so the result
+// does not depend on their order): they run concurrently on side streams that
+// fork from and join back into the handle's stream (also inside graph
+// capture).  The per-kernel profiler keeps them in one stream.
 static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, bool fp64_energy, EaccSel esel) {
-    if (terms & QGPU_TERMS_NONBOND) {
+    if (!(terms & QGPU_TERMS_NONBOND)) {
+        launch_misc(h->S, h->B, L, terms, esel);
+        return;
+    }
+    if (L.prof || !h->ev_fork) {
         launch_nb_water(h->S, h->B, L, 1, fp64_energy);
         launch_nb_solute(h->S, h->B, L, 1, fp64_energy);
         launch_qw(h->S, h->B, L, esel);
         launch_qp(h->S, h->B, L, esel);
+        launch_misc(h->S, h->B, L, terms, esel);
+        return;
     }
-    launch_misc(h->S, h->B, L, terms, esel);
+    cudaEventRecord(h->ev_fork, L.stream);
+    LaunchCtx Ls[QG_NSIDE];
+    for (int k = 0; k < QG_NSIDE; ++k) {
+        cudaStreamWaitEvent(h->side[k], h->ev_fork, 0);
+        Ls[k] = LaunchCtx{h->side[k], L.nlaunch};
+    }
+    launch_nb_water(h->S, h->B, L, 1, fp64_energy);
+    launch_nb_solute(h->S, h->B, Ls[0], 1, fp64_energy);
+    launch_qw(h->S, h->B, Ls[1], esel);
+    launch_qp(h->S, h->B, Ls[2], esel);
+    launch_misc(h->S, h->B, Ls[2], terms, esel);
+    for (int k = 0; k < QG_NSIDE; ++k) {
+        cudaEventRecord(h->ev_join[k], h->side[k]);
+        cudaStreamWaitEvent(L.stream, h->ev_join[k], 0);
+    }
 }
 
 static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every);
@@ -807,6 +849,11 @@ int qgpu_destroy(qgpu_handle *h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (void *p : h->allocs) cudaFree(p);
     if (h->rec_d) cudaFree(h->rec_d);
+    for (int k = 0; k < QG_NSIDE; ++k) {
+        if (h->side[k]) { cudaStreamSynchronize(h->side[k]); cudaStreamDestroy(h->side[k]); }
+        if (h->ev_join[k]) cudaEventDestroy(h->ev_join[k]);
+    }
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return 0;
@@ -1058,6 +1105,26 @@ int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every) {
 int qgpu_sync(qgpu_handle *h) {
     if (!h) return fail(QGPU_E_INVALID, "null handle");
     return check_status(h);
+}
+
+int qgpu_set_precision(qgpu_handle *h, int32_t mode) {
+    if (!h || (mode != QGPU_PRECISION_MIXED && mode != QGPU_PRECISION_FP64))
+        return fail(QGPU_E_INVALID, "qgpu_set_precision: bad arguments");
+    const bool fused = mode == QGPU_PRECISION_MIXED && h->can_fuse;
+    if (fused == h->all_fused) return 0;
+    LaunchCtx L{h->stream, &h->nlaunch};
+    ensure_double(h, L);          // x/v from the float master before leaving it
+    CK(cudaStreamSynchronize(h->stream));
+    h->all_fused = fused;
+    for (int t = 0; t < h->ntraj; ++t) {
+        h->info[t].ekin_blk0 = fused ? h->ek_a0[t] : h->ek_u0[t];
+        h->info[t].ekin_nblk = fused ? h->ek_an[t] : h->ek_un[t];
+    }
+    CK(cudaMemcpy((void *)h->S.traj, h->info.data(), h->info.size() * sizeof(TrajInfo), cudaMemcpyHostToDevice));
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    // the Ekin partials of the new layout are formed again before the next step
+    h->temp_init = 0;
+    return 0;
 }
 
 int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink sink, void *user) {

@@ -14,6 +14,8 @@
 #define QG_BLOCK 128            // threads per block of the per-item kernels
 #define QG_UBLK 96              // threads per block of the fused update (32 waters)
 #define QG_LW 8                 // lanes that share one target in the pair kernels
+#define QG_NSIDE 3              // side streams of the concurrent force kernels
+#define QG_TREG 4               // target-group atoms held in registers by the any-atom scan test
 #define S_GROUP_MASK 0xffffffffu
 #define QG_MAXS 4               // states handled by the engine (<= QGPU_MAX_STATES)
 #define QG_MAXQ 128             // Q atoms per trajectory (reference max_qat = 100)
@@ -57,6 +59,7 @@ struct TrajInfo {
     int qlib0, nqlib, sc0;      // Q type table offset, sc_lookup offset
     int qvdw;
     int use_lrf, q_static;      // LRF on; qp/qw lists built once (Rcq > rexcl_o)
+    int any_atom;               // any-atom cut-off for solute groups (iuse_switch_atom = 0)
     int tile0, ntile;           // scan tiles of this trajectory
     int nchunk;                 // source chunks of QG_TPC tiles
     long long scr0;             // first scan-scratch slot (slot = scr0 + chunk*ncgp + local group)
@@ -320,18 +323,23 @@ __device__ __forceinline__ float3 dpos(const float4 ah, const float4 al, const f
     return make_float3((bh.x - ah.x) + (bl.x - al.x), (bh.y - ah.y) + (bl.y - al.y), (bh.z - ah.z) + (bl.z - al.z));
 }
 
-// Packed record of one water (see DevSys::wrec) from its hi/lo coordinates.
-__device__ __forceinline__ void put_wrec(float4 *wr, const float4 (&h)[3], const float4 (&l)[3]) {
+// Packed record of one water (see DevSys::wrec) from its hi/lo coordinates:
+// float4 number k (0..2) of the record.
+__device__ __forceinline__ float4 wrec_part(const float4 (&h)[3], const float4 (&l)[3], int k) {
     float d[2][3];
 #pragma unroll
-    for (int k = 1; k < 3; ++k) {
-        d[k - 1][0] = (h[k].x - h[0].x) + (l[k].x - l[0].x);
-        d[k - 1][1] = (h[k].y - h[0].y) + (l[k].y - l[0].y);
-        d[k - 1][2] = (h[k].z - h[0].z) + (l[k].z - l[0].z);
+    for (int m = 1; m < 3; ++m) {
+        d[m - 1][0] = (h[m].x - h[0].x) + (l[m].x - l[0].x);
+        d[m - 1][1] = (h[m].y - h[0].y) + (l[m].y - l[0].y);
+        d[m - 1][2] = (h[m].z - h[0].z) + (l[m].z - l[0].z);
     }
-    wr[0] = make_float4(h[0].x, h[0].y, h[0].z, d[0][0]);
-    wr[1] = make_float4(l[0].x, l[0].y, l[0].z, d[0][1]);
-    wr[2] = make_float4(d[0][2], d[1][0], d[1][1], d[1][2]);
+    if (k == 0) return make_float4(h[0].x, h[0].y, h[0].z, d[0][0]);
+    if (k == 1) return make_float4(l[0].x, l[0].y, l[0].z, d[0][1]);
+    return make_float4(d[0][2], d[1][0], d[1][1], d[1][2]);
+}
+__device__ __forceinline__ void put_wrec(float4 *wr, const float4 (&h)[3], const float4 (&l)[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) wr[k] = wrec_part(h, l, k);
 }
 // exact FP64 squared distance in the reference's operation order (no FMA)
 __device__ __forceinline__ double dist2_exact(const double *x, int i, int j) {
@@ -364,6 +372,7 @@ struct BlockTables {
     const int *uatom, *ucon; const uint8_t *ublk_water; int nuatom;
     const int *qqblk_traj, *qqblk_s; int nqqblk;
     int max_nqat;                      // largest Q-atom count of a trajectory
+    int any_atom;                      // some trajectory uses the any-atom cut-off
 };
 
 void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L);

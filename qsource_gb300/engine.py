@@ -110,6 +110,11 @@ class Engine:
         self._check(self.lib.qgpu_get_lrf(self.h, traj, abi.ptr(out)))
         return out
 
+    def set_precision(self, mode: int):
+        """QGPU_PRECISION_MIXED (default) or QGPU_PRECISION_FP64 for the MD
+        step (see qgpu_set_precision)."""
+        self._check(self.lib.qgpu_set_precision(self.h, mode))
+
     def enqueue(self, nsteps: int, ene_every: int = 0):
         """Queue nsteps of device work without waiting (see qgpu_enqueue)."""
         self._check(self.lib.qgpu_enqueue(self.h, nsteps, ene_every))

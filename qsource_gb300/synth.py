@@ -100,9 +100,17 @@ def _waters(R: float, solute: np.ndarray, rng: np.random.Generator) -> np.ndarra
 
 def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, seed: int, *,
               solute_sigma: float = 0.3, T: float = 300.0, stepsize: float = 1.0, tau_T: float = 100.0,
-              NBcycle: int = 10, Rc: float = 10.0, offdiag=None, initial_velocities: bool = True) -> System:
+              NBcycle: int = 10, Rc: float = 10.0, offdiag=None, initial_velocities: bool = True,
+              any_atom: bool = False) -> System:
     """Water sphere of radius R around a solute chain of n_solute atoms whose
-    first nq atoms are Q atoms with per-state charges qcharges[nq, nstates]."""
+    first nq atoms are Q atoms with per-state charges qcharges[nq, nstates].
+
+    any_atom selects the any-atom cut-off for the solute charge groups
+    (topology flag iuse_switch_atom = 0).  The chain's groups are 4
+    consecutive atoms with no angle terms, so two atoms of groups whose
+    switch atoms lie beyond the cut-off can come within 2 A of each other with
+    no LJ repulsion between them under the switch-atom cut-off; the solute
+    systems of the benchmark use the any-atom cut-off for that reason."""
     rng = np.random.default_rng(seed)
     S = qcharges.shape[1]
     n_solute = max(n_solute, nq)
@@ -146,7 +154,7 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
         "nangles_solute": 0, "ang": np.zeros((0, 4), np.int32), "anglib": np.zeros((0, 4)),
         "ntors_solute": 0, "tor": np.zeros((0, 5), np.int32), "torlib": np.zeros((0, 4)),
         "nimps_solute": 0, "imp": np.zeros((0, 5), np.int32), "imp_type": 2, "implib": np.zeros((0, 2)),
-        "crg": crg, "ncgp_solute": ncgp_solute, "iuse_switch_atom": 1,
+        "crg": crg, "ncgp_solute": ncgp_solute, "iuse_switch_atom": 0 if any_atom else 1,
         "cgp_first": np.array(first, np.int32), "cgp_last": np.array(last, np.int32),
         "cgp_switch": np.array(sw, np.int32), "cgpatom": np.array(atoms, np.int32),
         "ivdw_rule": 1, "el14_scale": 0.5, "coulomb_constant": 332.0,
@@ -203,6 +211,7 @@ def config(cfg: int, replica: int = 0, window: int = 0, nwindows: int = 21, **kw
         qa = neutral_charges(qrng, 8, 0.4)
         lam = kw.pop("lambdas", (0.5, 0.5))
         return synthetic(18.0, 8, 8, np.stack([qa, np.zeros(8)], 1), lam, seed, **kw)
+    kw.setdefault("any_atom", True)
     if cfg == 2:
         qa = neutral_charges(qrng, 50, 0.4)
         lam = kw.pop("lambdas", (0.5, 0.5))
@@ -231,6 +240,7 @@ def lambda_batch_member(i: int, nwindows: int = 21, replicas: int = 11, **kw) ->
     qa = neutral_charges(np.random.default_rng(1000), 8, 0.4)
     ns = 500 + int(round(1500 * r / max(replicas - 1, 1)))
     ns = min(ns, {20.0: 800, 25.0: 1500, 30.0: 2000}[R])
+    kw.setdefault("any_atom", True)
     return synthetic(R, ns, 8, np.stack([qa, np.zeros(8)], 1), (0.5, 0.5), 3000 + 100 * r, **kw)
 
 

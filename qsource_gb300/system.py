@@ -114,6 +114,7 @@ class System:
         for k in ("Ndegf", "Ndegfree", "Ndegf_solvent", "Ndegfree_solvent", "Ndegf_solute", "Ndegfree_solute"):
             setattr(d, k, int(getattr(self, k)))
         d.detail_temps = int(self.detail_temps)
+        d.any_atom_lists = int(getattr(self, "any_atom_lists", 0))
         return d
 
     @property
@@ -480,6 +481,7 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
         tau_T=TIME_UNIT * inp["bath_coupling"], separate_scaling=separate_scaling, NBcycle=inp["non_bond"],
         Ndegf=Ndegf, Ndegfree=Ndegfree, Ndegf_solvent=Ndegf_solvent, Ndegfree_solvent=Ndegfree_solvent,
         Ndegf_solute=Ndegf_solute, Ndegfree_solute=Ndegfree_solute, detail_temps=detail,
+        any_atom_lists=0 if int(top.get("iuse_switch_atom", 1)) == 1 else 1,
         Tmaxw=inp["initial_temperature"], seed=inp["random_seed"], nsteps=inp["steps"],
     )
 

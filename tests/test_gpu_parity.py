@@ -40,7 +40,10 @@ def _oracle(s):
 @pytest.fixture(scope="module")
 def systems(engine_lib):
     from qsource_gb300 import synth
-    out = {"cfg1": synth.config(1), "cfg2": synth.config(2), "cfg4": synth.config(4)}
+    # cfg2/cfg4 use the any-atom cut-off (nb*lis2*); cfg2sw is cfg2 with the
+    # switch-atom cut-off, which the reference's own golden systems also use
+    out = {"cfg1": synth.config(1), "cfg2": synth.config(2), "cfg4": synth.config(4),
+           "cfg2sw": synth.config(2, any_atom=False)}
     g = golden_system("basic_sph")
     o = _oracle(g)
     o.maxwell(g.Tmaxw, int(g.seed))
@@ -68,7 +71,7 @@ E_KEYS = ["pp_el", "pp_vdw", "pw_el", "pw_vdw", "ww_el", "ww_vdw", "lrf", "qx_el
 EQ_KEYS = ["qq_el", "qq_vdw", "qp_el", "qp_vdw", "qw_el", "qw_vdw", "q_bond", "q_angle", "q_torsion", "q_improper"]
 
 
-@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg4"])
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg2sw", "cfg4"])
 def test_pair_lists_exact(systems, name):
     s = systems[name]
     e = _engine(s)
@@ -80,7 +83,7 @@ def test_pair_lists_exact(systems, name):
         assert Counter(ex[lst]) == Counter(oracle_records(o, lst)), lst
 
 
-@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2"])
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg2sw"])
 def test_lrf_multipoles(systems, name):
     s = systems[name]
     e = _engine(s)
@@ -95,7 +98,7 @@ def test_lrf_multipoles(systems, name):
         assert err <= 1e-5 * scale, (lo, err, scale)
 
 
-@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg4"])
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg2sw", "cfg4"])
 def test_forces_and_energies(systems, name):
     s = systems[name]
     e = _engine(s)

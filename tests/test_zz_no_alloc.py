@@ -85,7 +85,8 @@ def _check(got_lrf, got_near, ref_lrf, ref_near):
 @pytest.mark.gpu
 def test_static_scan_matches_engine_on_two_calls(engine_lib):
     from qsource_gb300 import synth
-    big, small = synth.config(2), synth.config(1)
+    # the scan applies the switch-atom cut-off (iuse_switch_atom = 1)
+    big, small = synth.config(2, any_atom=False), synth.config(1)
     assert big.use_LRF and small.use_LRF
     assert len(big.cgp_first) > len(small.cgp_first)
     first = _scan_static(engine_lib, big, _device_inputs(big))
