@@ -282,22 +282,22 @@ def main():
         ms = float(t.item())
     ns_per_day = world * ntraj * steps * FS_PER_STEP * 1e-6 * 86400.0 / (ms * 1e-3)
 
-    # --- end to end through the public API with host buffers
-    xs = [torch.empty(3 * s.natom, dtype=torch.float64).pin_memory().numpy() for s in systems]
-    vs = [torch.empty(3 * s.natom, dtype=torch.float64).pin_memory().numpy() for s in systems]
-    for t in range(ntraj):
-        xs[t][:], vs[t][:] = eng.coords(t)
-    e2e_blocks = max(2, nblk // 2)
+    # --- end to end through the public API with host buffers: per block the
+    # coordinates and velocities of the whole batch go up from pinned memory,
+    # the block runs with an energy sink, and x, v come back
+    n3 = 3 * natoms
+    xs = torch.empty(n3, dtype=torch.float64).pin_memory().numpy()
+    vs = torch.empty(n3, dtype=torch.float64).pin_memory().numpy()
+    eng.coords_all(xs, vs)
+    e2e_blocks = max(2, min(nblk // 2, 100))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     nrows = 0
     for b in range(e2e_blocks):
-        for t in range(ntraj):
-            eng.set_coords(t, xs[t], vs[t])
+        eng.set_coords_all(xs, vs)
         rows = eng.run(NB, ene_every=NB)
         nrows += sum(len(r) for r in rows)
-        for t in range(ntraj):
-            xs[t][:], vs[t][:] = eng.coords(t)
+        eng.coords_all(xs, vs)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e = world * ntraj * e2e_blocks * NB * FS_PER_STEP * 1e-6 * 86400.0 / e2e_s
@@ -336,8 +336,8 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU, one handle",
                    "precision": args.precision},
         "e2e": {"value": round(e2e, 3), "unit": "ns/day", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "how": "per 10-step block: upload x,v of all 32 trajectories from pinned memory, qgpu_run with an "
-                       "energy sink, read back x,v (host wall clock)"},
+                "how": "per 10-step block: qgpu_set_coords_all of x,v of all 32 trajectories from pinned memory, "
+                       "qgpu_run with an energy sink, qgpu_get_coords_all (host wall clock)"},
         "roofline": roof,
         "kernel_share": share,
         "kernel_us_per_step": us_per_step,

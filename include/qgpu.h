@@ -180,6 +180,34 @@ typedef struct qgpu_system_desc {
        groups (iuse_switch_atom = 0, nbpplis2_lrf src/md.f90:7441,
        nbpwlis2_lrf :8902, nbqplis2 :9946) */
     int32_t any_atom_lists;
+
+    /* sequence restraints ([sequence_restraints], p_restrain src/md.f90:15484-15576) */
+    int32_t nrstr_seq;
+    const int32_t *rstseq_ij;     /* 2*n: first, last atom (inclusive)                */
+    const double  *rstseq_fk;     /* n: force constant                                */
+    const int32_t *rstseq_flags;  /* 2*n: ih (1 = hydrogens too), to_centre (0 each   */
+                                  /*      atom, 1 geometric centre, 2 mass centre)    */
+    const uint8_t *heavy;         /* natom: mass >= 4 (topo.f90:871-880)              */
+    int32_t excluded_freeze;      /* [sphere] excluded_freeze                         */
+
+    /* water polarisation restraint (watpol src/md.f90:18372-18541; the shells of
+       wat_shells :18185-18368, used when wpol_restr != 0) */
+    double fkwpol;
+    int32_t nwpolr_shell;
+    const double *wshell_rout;    /* nwpolr_shell: outer radius                       */
+    const double *wshell_dr;      /* nwpolr_shell: width                              */
+    const double *wshell_cstb;    /* nwpolr_shell: Born term                          */
+    const double *wshell_theta_corr; /* nwpolr_shell: starting theta_corr (restart) */
+    int32_t itdis_update;         /* theta_corr update interval (100)                 */
+
+    /* thermostat and integrator ([MD], md_run src/md.f90:6440-6460, 6577-6606) */
+    int32_t thermostat;           /* 0 Berendsen, 1 Langevin, 2 Nose-Hoover           */
+    int32_t integrator;           /* 0 leap-frog, 1 velocity-verlet                   */
+    double friction;              /* Langevin friction (internal time units^-1)       */
+    int32_t langevin_gauss;       /* Langevin random forces: 0 uniform, 1 Gaussian    */
+    int32_t rand_state;           /* randm state (iseed) when the run starts           */
+    int32_t nhchains;             /* Nose-Hoover chain length                         */
+    double nhq;                   /* Nose-Hoover mass                                 */
 } qgpu_system_desc;
 
 /* Energies, the ENERGIES record of src/nrgy.f90:48-54 (sphere subset). */
@@ -235,6 +263,11 @@ int qgpu_ntraj(const qgpu_handle *h);
 /* ---- state transfer ----------------------------------------------------- */
 int qgpu_set_coords(qgpu_handle *h, int32_t traj, const double *x, const double *v);
 int qgpu_get_coords(qgpu_handle *h, int32_t traj, double *x, double *v);
+/* The same for every trajectory of the batch at once: x and v hold the
+   trajectories' 3*natom arrays back to back in trajectory order (one copy
+   each way instead of one per trajectory). */
+int qgpu_set_coords_all(qgpu_handle *h, const double *x, const double *v);
+int qgpu_get_coords_all(qgpu_handle *h, double *x, double *v);
 
 /* ---- drop-in call points ------------------------------------------------ */
 /* make_pair_lists (src/md.f90:5985-6071): group centres, pp/pw/ww lists with

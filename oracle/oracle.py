@@ -57,6 +57,7 @@ def lib() -> C.CDLL:
         L.oracle_md_run.restype = C.c_int
         L.oracle_md_run.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(Energies), C.POINTER(QEnergy), vp]
         L.oracle_get_energies.argtypes = [vp, C.POINTER(Energies), C.POINTER(QEnergy)]
+        L.oracle_final_energy.argtypes = [vp, C.c_int, C.POINTER(Energies), C.POINTER(QEnergy)]
         L.oracle_sizeof_desc.restype = C.c_int
         _lib = L
     return _lib
@@ -140,6 +141,13 @@ class Oracle:
         H = np.zeros(max(n, 1)); r = np.zeros(max(n, 1))
         self.L.oracle_offdiag(self.h, _p(H), _p(r))
         return H[:n], r[:n]
+
+    def final_energy(self, terms: int = 0x1F):
+        """Lists and energies after an MD run (the reference's FINAL report)."""
+        E = Energies()
+        EQ = (QEnergy * max(self.S, 1))()
+        self.L.oracle_final_energy(self.h, terms, C.byref(E), EQ)
+        return E.as_dict(), [EQ[s].as_dict() for s in range(self.S)]
 
     def md_run(self, nsteps: int, terms: int = 0x1F):
         E = (Energies * nsteps)()

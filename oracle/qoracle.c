@@ -48,7 +48,16 @@ typedef struct oracle {
     /* temperature state */
     double Temp, Tfree, Tfree_solute, Tfree_solvent, Tscale_solute, Tscale_solvent;
     int32_t irand, rand_new;
+    int32_t iseed;              /* the argument the reference passes to randm */
     int status;
+    int istep;                  /* md_run step counter (watpol's itdis_update) */
+    /* water polarisation shells (wshell, src/md.f90:18185-18368) */
+    double *theta_corr, *avtheta, *avn_insh;
+    double *theta, *tdum, *theta0;
+    int32_t *list_sh, *nsort, *n_insh;
+    /* Langevin random-force amplitudes and Nose-Hoover chain */
+    double *randva, *randfa;
+    double xnh[64], vnh[64], qnh[64], Gnh[64];
 } oracle;
 
 /* ------------------------------------------------------------------ utils */
@@ -127,6 +136,32 @@ void *oracle_create(const qgpu_system_desc *in) {
     build_pair_csr(N, in->n14, in->pairs14, &o->p14_first, &o->p14_j);
     for (int s = 0; s < o->S; ++s) o->EQ[s].lambda = in->lambda[s];
     o->Tscale_solute = o->Tscale_solvent = 1.0;
+    /* copy the variable-length inputs the new terms keep referring to */
+    o->d.rstseq_ij = (const int32_t *)dupbuf(in->rstseq_ij, 2 * (size_t)in->nrstr_seq * sizeof(int32_t));
+    o->d.rstseq_fk = (const double *)dupbuf(in->rstseq_fk, (size_t)in->nrstr_seq * sizeof(double));
+    o->d.rstseq_flags = (const int32_t *)dupbuf(in->rstseq_flags, 2 * (size_t)in->nrstr_seq * sizeof(int32_t));
+    o->d.heavy = (const uint8_t *)dupbuf(in->heavy, in->heavy ? (size_t)N : 0);
+    int ns = in->wpol_restr ? in->nwpolr_shell : 0;
+    o->d.nwpolr_shell = ns;
+    o->theta_corr = (double *)xmalloc((size_t)(ns + 1) * sizeof(double));
+    o->avtheta = (double *)xmalloc((size_t)(ns + 1) * sizeof(double));
+    o->avn_insh = (double *)xmalloc((size_t)(ns + 1) * sizeof(double));
+    o->n_insh = (int32_t *)xmalloc((size_t)(ns + 1) * sizeof(int32_t));
+    for (int k = 0; k < ns; ++k) o->theta_corr[k] = in->wshell_theta_corr ? in->wshell_theta_corr[k] : 0.0;
+    int nw = (N - in->nat_solute) / 3;
+    o->theta = (double *)xmalloc((size_t)(nw + 1) * sizeof(double));
+    o->tdum = (double *)xmalloc((size_t)(nw + 1) * sizeof(double));
+    o->theta0 = (double *)xmalloc((size_t)(nw + 1) * sizeof(double));
+    o->list_sh = (int32_t *)xmalloc((size_t)(nw + 1) * (ns + 1) * sizeof(int32_t));
+    o->nsort = (int32_t *)xmalloc((size_t)(nw + 1) * (ns + 1) * sizeof(int32_t));
+    o->randva = (double *)xmalloc((size_t)N * sizeof(double));
+    o->randfa = (double *)xmalloc(3 * (size_t)N * sizeof(double));
+    o->iseed = in->rand_state;
+    /* Nose-Hoover chain start (init_shake tail, src/md.f90:4415-4424) */
+    int nc = in->nhchains > 0 ? (in->nhchains < 64 ? in->nhchains : 64) : 0;
+    for (int k = 0; k < nc; ++k) { o->qnh[k] = in->nhq; o->vnh[k] = 0; o->xnh[k] = 0; }
+    if (nc) o->qnh[0] = in->Ndegf * in->nhq;
+    o->d.nhchains = nc;
     return o;
 }
 
@@ -136,6 +171,11 @@ void oracle_destroy(void *h) {
     free(o->x); free(o->v); free(o->xx); free(o->f); free(o->winv); free(o->iwhich); free(o->lrf);
     free(o->pp.a); free(o->pw.a); free(o->ww.a); free(o->qp.a); free(o->qw.a);
     free(o->ex_first); free(o->ex_j); free(o->p14_first); free(o->p14_j);
+    free((void *)o->d.rstseq_ij); free((void *)o->d.rstseq_fk); free((void *)o->d.rstseq_flags);
+    free((void *)o->d.heavy);
+    free(o->theta_corr); free(o->avtheta); free(o->avn_insh); free(o->n_insh);
+    free(o->theta); free(o->tdum); free(o->theta0); free(o->list_sh); free(o->nsort);
+    free(o->randva); free(o->randfa);
     free(o);
 }
 
@@ -993,6 +1033,150 @@ static void restrain_solvent(oracle *o) {
     }
 }
 
+/* p_restrain, sequence restraints, src/md.f90:15484-15576.  An atom takes
+   part when heavy, or when the H flag is set and it is not a frozen
+   excluded atom (the reference's .and. binds before .or.). */
+static void p_restrain_seq(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    for (int ir = 0; ir < d->nrstr_seq; ++ir) {
+        const int i0 = d->rstseq_ij[2 * ir], i1 = d->rstseq_ij[2 * ir + 1];
+        const double fk = d->rstseq_fk[ir];
+        const int ih = d->rstseq_flags[2 * ir], tc = d->rstseq_flags[2 * ir + 1];
+#define SEQ_SEL(i) ((d->heavy && d->heavy[i]) || (ih == 1 && !(d->excl[i] && d->excluded_freeze)))
+        if (tc == 1 || tc == 2) {
+            double dr[3] = { 0, 0, 0 }, w = 0.0;
+            for (int i = i0; i <= i1; ++i) {
+                if (!SEQ_SEL(i)) continue;
+                double m = tc == 2 ? d->mass[d->iac[i]] : 1.0;
+                w += m;
+                for (int a = 0; a < 3; ++a) dr[a] += (o->x[3 * i + a] - d->xtop[3 * i + a]) * (tc == 2 ? m : 1.0);
+            }
+            if (w > 0) {
+                for (int a = 0; a < 3; ++a) dr[a] /= w;
+                double r2 = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+                o->E.rst_protein += 0.5 * fk * r2;
+                for (int i = i0; i <= i1; ++i) {
+                    if (!SEQ_SEL(i)) continue;
+                    double s = tc == 1 ? d->mass[d->iac[i]] / 12.010 : 1.0;
+                    for (int a = 0; a < 3; ++a) o->f[3 * i + a] += tc == 1 ? fk * dr[a] * s : fk * dr[a];
+                }
+            }
+        } else {
+            for (int i = i0; i <= i1; ++i) {
+                if (!SEQ_SEL(i)) continue;
+                double dr[3] = { o->x[3 * i] - d->xtop[3 * i], o->x[3 * i + 1] - d->xtop[3 * i + 1],
+                                 o->x[3 * i + 2] - d->xtop[3 * i + 2] };
+                o->E.rst_protein += 0.5 * fk * (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+                for (int a = 0; a < 3; ++a) o->f[3 * i + a] += fk * dr[a];
+            }
+        }
+#undef SEQ_SEL
+    }
+}
+
+/* water dipole / radial unit vectors and the angle between them (watpol) */
+static double wat_angle(const oracle *o, int i, double rmu[3], double rcu[3], double *rm, double *rc, double *scp) {
+    const double *x = o->x + 3 * i;
+    const double *c = o->d.xwcent;
+    for (int a = 0; a < 3; ++a) rmu[a] = x[3 + a] + x[6 + a] - 2.0 * x[a];
+    *rm = sqrt(rmu[0] * rmu[0] + rmu[1] * rmu[1] + rmu[2] * rmu[2]);
+    for (int a = 0; a < 3; ++a) rmu[a] /= *rm;
+    for (int a = 0; a < 3; ++a) rcu[a] = x[a] - c[a];
+    *rc = sqrt(rcu[0] * rcu[0] + rcu[1] * rcu[1] + rcu[2] * rcu[2]);
+    for (int a = 0; a < 3; ++a) rcu[a] /= *rc;
+    double s = rmu[0] * rcu[0] + rmu[1] * rcu[1] + rmu[2] * rcu[2];
+    if (s > 1.0) s = 1.0;
+    if (s < -1.0) s = -1.0;
+    *scp = s;
+    return acos(s);
+}
+
+/* watpol, src/md.f90:18372-18541: radial polarisation restraint of the
+   waters in the outer shells.  Shell k is 0-based here (is = k + 1). */
+static void watpol(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    const int ns = d->nwpolr_shell, nw = d->nwat, stride = nw + 1;
+    const double pi = 4.0 * atan(1.0);
+    if (ns <= 0) return;
+    for (int k = 0; k < ns; ++k) o->n_insh[k] = 0;
+    for (int iw = 0; iw < nw; ++iw) {
+        o->theta[iw] = 0; o->theta0[iw] = 0;
+        int i = d->nat_solute + 3 * iw;
+        if (d->excl[i]) continue;
+        double rmu[3], rcu[3], rm, rc, scp;
+        o->theta[iw] = wat_angle(o, i, rmu, rcu, &rm, &rc, &scp);
+        o->tdum[iw] = o->theta[iw];
+        if (rc > d->wshell_rout[ns - 1] - d->wshell_dr[ns - 1]) {
+            int is;
+            for (is = ns; is >= 2; --is)
+                if (rc <= d->wshell_rout[is - 1]) break;
+            if (is < 2) is = 1;
+            int k = is - 1;
+            o->list_sh[k * stride + o->n_insh[k]++] = iw;
+        }
+    }
+    /* selection sort by theta; ties keep the list (water index) order */
+    for (int k = 0; k < ns; ++k) {
+        int n = o->n_insh[k];
+        for (int il = 0; il < n; ++il) {
+            double tmin = 2.0 * pi;
+            int jmin = -1;
+            for (int jl = 0; jl < n; ++jl) {
+                int jw = o->list_sh[k * stride + jl];
+                if (o->tdum[jw] < tmin) { jmin = jw; tmin = o->theta[jw]; }
+            }
+            o->nsort[k * stride + il] = jmin;
+            if (jmin >= 0) o->tdum[jmin] = 99999.0;
+        }
+    }
+    if (o->istep != 0 && d->itdis_update > 0 && o->istep % d->itdis_update == 0) {
+        for (int k = 0; k < ns; ++k) {
+            o->avtheta[k] /= (double)d->itdis_update;
+            o->avn_insh[k] /= (double)d->itdis_update;
+            o->theta_corr[k] = o->theta_corr[k] + o->avtheta[k] - acos(d->wshell_cstb[k]);
+            o->avtheta[k] = 0;
+            o->avn_insh[k] = 0;
+        }
+    }
+    for (int k = 0; k < ns; ++k) {
+        int n = o->n_insh[k];
+        if (n == 0) continue;
+        double avtdum = 0;
+        for (int il = 1; il <= n; ++il) {
+            int iw = o->nsort[k * stride + il - 1];
+            double arg = 1.0 + (1.0 - 2.0 * (double)il) / (double)n;
+            double t0 = acos(arg);
+            t0 = t0 - 3.0 * sin(t0) * d->wshell_cstb[k] / 2.0;
+            if (t0 < 0) t0 = 0;
+            if (t0 > pi) t0 = pi;
+            o->theta0[il - 1] = t0;
+            avtdum += o->theta[iw];
+            double dth = o->theta[iw] - t0 + o->theta_corr[k];
+            o->E.rst_water_pol += 0.5 * d->fkwpol * dth * dth;
+            double dv = d->fkwpol * dth;
+            int i = d->nat_solute + 3 * iw;
+            double rmu[3], rcu[3], rm, rc, scp;
+            wat_angle(o, i, rmu, rcu, &rm, &rc, &scp);
+            double f0 = sin(acos(scp));
+            if (fabs(f0) < 1e-14) f0 = 1e-14;
+            f0 = -1.0 / f0;
+            f0 = dv * f0;
+            double f1[3], f2[3];
+            for (int a = 0; a < 3; ++a) {
+                f1[a] = (rcu[a] - rmu[a] * scp) / rm;
+                f2[a] = (rmu[a] - rcu[a] * scp) / rc;
+            }
+            for (int a = 0; a < 3; ++a) {
+                o->f[3 * i + a] += f0 * (-2.0 * f1[a] + f2[a]);
+                o->f[3 * i + 3 + a] += f0 * f1[a];
+                o->f[3 * i + 6 + a] += f0 * f1[a];
+            }
+        }
+        o->avtheta[k] += avtdum / (double)n;
+        o->avn_insh[k] += n;
+    }
+}
+
 /* offdiag, src/md.f90:15444-15470 */
 void oracle_offdiag(void *h, double *Hij_out, double *rkl_out) {
     oracle *o = (oracle *)h;
@@ -1039,8 +1223,13 @@ void oracle_pot_energy(void *h, int terms, double *d_out, qgpu_energies *E_out, 
         o->E.w_improper = impropers(o, d->nimps_solute, d->nimps);
     }
     if (terms & QGPU_TERMS_RESTRAINT) {
+        /* pot_energy order, src/md.f90:16113-16125 */
         fix_shell(o);
-        if (d->nwat > 0) restrain_solvent(o);
+        p_restrain_seq(o);
+        if (d->nwat > 0) {
+            restrain_solvent(o);
+            if (d->wpol_restr) watpol(o);
+        }
     }
     if (terms & QGPU_TERMS_QQ) nonbond_qq(o);
     if (terms & QGPU_TERMS_QBONDED)
@@ -1184,7 +1373,9 @@ void oracle_temperature(void *h, double *out4) {
         Tfsv = 2.0 * Tfsv / BOLTZ / (double)d->Ndegfree_solvent;
     }
     double ts = o->Tscale_solvent, tu = o->Tscale_solute;
-    if (d->separate_scaling) {
+    if (d->thermostat != 0) {
+        /* only the Berendsen thermostat scales (src/md.f90:6166) */
+    } else if (d->separate_scaling) {
         if (Tfsv != 0) ts = d->Temp0 / Tfsv - 1.0;
         ts = sqrt(1 + d->dt / d->tau_T * ts);
         if (Tfsu != 0) tu = d->Temp0 / Tfsu - 1.0;
@@ -1199,20 +1390,90 @@ void oracle_temperature(void *h, double *out4) {
     if (out4) { out4[0] = Temp; out4[1] = Tfree; out4[2] = tu; out4[3] = ts; }
 }
 
-/* newvel_ber, src/md.f90:6194-6223 (leap-frog) */
+/* newvel_ber, src/md.f90:6194-6223; with velocity-verlet the velocity update
+   is applied a second time after the position update */
 static void newvel_ber(oracle *o, double step, double ts, int a0, int a1) {
     const double dt = o->d.dt;
+    const int vv = o->d.integrator == 1;
     for (int i = a0; i < a1; ++i)
         for (int a = 0; a < 3; ++a) {
             int k = 3 * i + a;
             o->v[k] = (o->v[k] - o->f[k] * o->winv[i] * step) * ts;
             o->xx[k] = o->x[k];
             o->x[k] = o->x[k] + o->v[k] * dt;
+            if (vv) o->v[k] = (o->v[k] - o->f[k] * o->winv[i] * step) * ts;
         }
 }
 
-/* md_run, Berendsen leap-frog branch (src/md.f90:6471-6664), with the
-   terms selected by `terms`.  Energies of every step are written to
+/* newvel_lan, src/md.f90:6225-6270: random forces for every atom first
+   (uniform: randva*(r - 1/2); Gaussian: gauss(0, randva)), then the update */
+static void newvel_lan(oracle *o, double step, double lfriction) {
+    const double dt = o->d.dt;
+    const int vv = o->d.integrator == 1;
+    for (int i = 0; i < o->N; ++i)
+        for (int a = 0; a < 3; ++a)
+            o->randfa[3 * i + a] = o->d.langevin_gauss ? gauss(o, 0.0, o->randva[i], &o->iseed)
+                                                       : o->randva[i] * (randm(o, &o->iseed) - 0.5);
+    for (int i = 0; i < o->N; ++i)
+        for (int a = 0; a < 3; ++a) {
+            int k = 3 * i + a;
+            o->v[k] = (o->v[k] * lfriction) - (o->f[k] - o->randfa[k]) * o->winv[i] * step;
+            o->xx[k] = o->x[k];
+            o->x[k] = o->x[k] + o->v[k] * dt;
+            if (vv) o->v[k] = (o->v[k] * lfriction) - (o->f[k] - o->randfa[k]) * o->winv[i] * step;
+        }
+}
+
+/* newvel_nos, src/md.f90:6272-6298 */
+static void newvel_nos(oracle *o, double step) {
+    const double dt = o->d.dt;
+    const int vv = o->d.integrator == 1;
+    for (int i = 0; i < o->N; ++i)
+        for (int a = 0; a < 3; ++a) {
+            int k = 3 * i + a;
+            o->v[k] = o->v[k] - o->f[k] * o->winv[i] * step;
+            o->xx[k] = o->x[k];
+            o->x[k] = o->x[k] + o->v[k] * dt;
+            if (vv) o->v[k] = o->v[k] - o->f[k] * o->winv[i] * step;
+        }
+}
+
+/* nh_prop, src/md.f90:6300-6345 (chain index k = i - 1) */
+static void nh_prop(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    const int nc = d->nhchains;
+    if (nc < 1) return;
+    const double dt2 = 0.5 * d->dt, dt4 = 0.5 * dt2, dt8 = 0.5 * dt4;
+    const double kbT = BOLTZ * d->Temp0;
+    double expf = 1.0, sc;
+    o->Gnh[0] = d->Ndegf * BOLTZ * (o->Temp - d->Temp0) / o->qnh[0];
+    for (int i = 1; i < nc; ++i) o->Gnh[i] = (o->qnh[i - 1] * o->vnh[i - 1] * o->vnh[i - 1] - kbT) / o->qnh[i];
+    o->vnh[nc - 1] = o->vnh[nc - 1] + o->Gnh[nc - 1] * dt4;
+    o->xnh[nc - 1] = o->xnh[nc - 1] + o->vnh[nc - 1] * dt2;
+    for (int i = nc - 2; i >= 0; --i) {
+        expf = exp(-dt8 * o->vnh[i + 1]);
+        o->vnh[i] = (o->vnh[i] * expf + o->Gnh[i] * dt4) * expf;
+        o->xnh[i] = o->xnh[i] + o->vnh[i] * dt2;
+    }
+    sc = exp(-o->vnh[0] * dt2);
+    for (size_t k = 0; k < 3 * (size_t)o->N; ++k) o->v[k] = o->v[k] * sc;
+    o->Gnh[0] = d->Ndegf * BOLTZ * (sc * sc * o->Temp - d->Temp0) / o->qnh[0];
+    o->vnh[0] = (o->vnh[0] * expf + o->Gnh[0] * dt4) * expf;
+    for (int i = 1; i < nc - 1; ++i) {
+        expf = exp(-dt8 * o->vnh[i + 1]);
+        o->Gnh[i] = (o->qnh[i - 1] * o->vnh[i - 1] * o->vnh[i - 1] - kbT) / o->qnh[i];
+        o->vnh[i] = (o->vnh[i] * expf + o->Gnh[i] * dt4) * expf;
+    }
+    if (nc > 1) {
+        o->Gnh[nc - 1] = (o->qnh[nc - 2] * o->vnh[nc - 2] * o->vnh[nc - 2] - kbT) / o->qnh[nc - 1];
+        o->vnh[nc - 1] = o->vnh[nc - 1] + o->Gnh[nc - 1] * dt4;
+    }
+}
+
+/* md_run, src/md.f90:6440-6664: thermostat constants before the loop, then
+   per step lists (every NBcycle steps), pot_energy, offdiag, the thermostat's
+   velocity/position update, SHAKE (+ a second nh_prop), temperature.  The step
+   counter continues across calls.  Energies of every step are written to
    E_rows[nsteps] / EQ_rows[nsteps*nstates] when given.  Returns 0 or a
    QGPU_E_* status. */
 int oracle_md_run(void *h, int32_t nsteps, int32_t terms, qgpu_energies *E_rows, qgpu_qenergy *EQ_rows,
@@ -1220,15 +1481,30 @@ int oracle_md_run(void *h, int32_t nsteps, int32_t terms, qgpu_energies *E_rows,
     oracle *o = (oracle *)h;
     const qgpu_system_desc *d = &o->d;
     size_t n3 = 3 * (size_t)o->N;
-    for (int step = 0; step < nsteps; ++step) {
-        if (step % d->NBcycle == 0) oracle_make_pair_lists(o);
+    const double dv_mod = d->integrator == 1 ? 0.5 * d->dt : d->dt;
+    double dv_friction = 1.0;
+    if (d->thermostat == 1) {
+        dv_friction = 1.0 - d->friction * dv_mod;
+        double gkT = (d->langevin_gauss ? 2.0 : 24.0) * d->friction * BOLTZ * d->Temp0 / dv_mod;
+        for (int i = 0; i < o->N; ++i) o->randva[i] = sqrt(gkT / o->winv[i]);
+    }
+    for (int step = 0; step < nsteps; ++step, ++o->istep) {
+        if (o->istep % d->NBcycle == 0) oracle_make_pair_lists(o);
         oracle_pot_energy(o, terms, NULL, NULL, NULL);
         if (d->noffd > 0) oracle_offdiag(o, NULL, NULL);
-        newvel_ber(o, d->dt, o->Tscale_solute, 0, d->nat_solute);
-        newvel_ber(o, d->dt, o->Tscale_solvent, d->nat_solute, d->natom);
+        if (d->thermostat == 1) {
+            newvel_lan(o, dv_mod, dv_friction);
+        } else if (d->thermostat == 2) {
+            nh_prop(o);
+            newvel_nos(o, dv_mod);
+        } else {
+            newvel_ber(o, dv_mod, o->Tscale_solute, 0, d->nat_solute);
+            newvel_ber(o, dv_mod, o->Tscale_solvent, d->nat_solute, d->natom);
+        }
         if (d->shake_molecules > 0) {
             if (oracle_shake_arrays(o, o->xx, o->x) < 0) return QGPU_E_SHAKE;
             for (size_t k = 0; k < n3; ++k) o->v[k] = (o->x[k] - o->xx[k]) / d->dt;
+            if (d->thermostat == 2) nh_prop(o);
         }
         oracle_temperature(o, NULL);
         if (o->Temp != o->Temp) return QGPU_E_NAN;
@@ -1237,6 +1513,14 @@ int oracle_md_run(void *h, int32_t nsteps, int32_t terms, qgpu_energies *E_rows,
         if (temps) temps[step] = o->Temp;
     }
     return 0;
+}
+
+/* The energies after the MD loop (src/md.f90:6687-6693): lists and
+   pot_energy at the final coordinates, with the step counter at nsteps. */
+void oracle_final_energy(void *h, int terms, qgpu_energies *E, qgpu_qenergy *EQ) {
+    oracle *o = (oracle *)h;
+    oracle_make_pair_lists(o);
+    oracle_pot_energy(o, terms, NULL, E, EQ);
 }
 
 /* -------------------------------------------------------- inspection */

@@ -67,6 +67,12 @@ class SystemDesc(C.Structure):
         ("Ndegf", _i32), ("Ndegfree", _i32), ("Ndegf_solvent", _i32), ("Ndegfree_solvent", _i32),
         ("Ndegf_solute", _i32), ("Ndegfree_solute", _i32), ("detail_temps", _i32),
         ("any_atom_lists", _i32),
+        ("nrstr_seq", _i32), ("rstseq_ij", _P), ("rstseq_fk", _P), ("rstseq_flags", _P), ("heavy", _P),
+        ("excluded_freeze", _i32),
+        ("fkwpol", _f64), ("nwpolr_shell", _i32), ("wshell_rout", _P), ("wshell_dr", _P), ("wshell_cstb", _P),
+        ("wshell_theta_corr", _P), ("itdis_update", _i32),
+        ("thermostat", _i32), ("integrator", _i32), ("friction", _f64), ("langevin_gauss", _i32),
+        ("rand_state", _i32), ("nhchains", _i32), ("nhq", _f64),
     ]
 
 
@@ -107,6 +113,8 @@ EXPORTS = {
     "qgpu_ntraj": (_i32, [C.c_void_p]),
     "qgpu_set_coords": (_i32, [C.c_void_p, _i32, _P, _P]),
     "qgpu_get_coords": (_i32, [C.c_void_p, _i32, _P, _P]),
+    "qgpu_set_coords_all": (_i32, [C.c_void_p, _P, _P]),
+    "qgpu_get_coords_all": (_i32, [C.c_void_p, _P, _P]),
     "qgpu_build_lists": (_i32, [C.c_void_p]),
     "qgpu_forces": (_i32, [C.c_void_p, _i32, _i32, _P, C.POINTER(Energies), C.POINTER(QEnergy)]),
     "qgpu_shake": (_i32, [C.c_void_p, _i32, _P, _P, C.POINTER(_i32)]),

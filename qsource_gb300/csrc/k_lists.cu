@@ -17,6 +17,27 @@ __global__ void k_mirror(DevSys S) {
     S.velf[i] = make_float4((float)S.v[3 * i], (float)S.v[3 * i + 1], (float)S.v[3 * i + 2], 0.f);
 }
 
+// k_mirror over atoms [a0, a0 + n) of one trajectory, with the packed
+// records of its waters (each water's O thread forms them from x).
+__global__ void k_mirror_range(DevSys S, int a0, int n) {
+    const int i = a0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a0 + n) return;
+    const TrajInfo &T = S.traj[S.atraj[i]];
+    float4 h[3], l[3];
+    const int na = S.g_kind[S.agrp[i]] && S.g_atoms[S.g_start[S.agrp[i]]] == i ? 3 : 1;
+    for (int k = 0; k < na; ++k) {
+        const int a = i + k;
+        const double r0 = S.x[3 * a] - T.origin[0], r1 = S.x[3 * a + 1] - T.origin[1], r2 = S.x[3 * a + 2] - T.origin[2];
+        h[k].x = (float)r0; h[k].y = (float)r1; h[k].z = (float)r2; h[k].w = S.pos[a].w;
+        l[k].x = (float)(r0 - (double)h[k].x); l[k].y = (float)(r1 - (double)h[k].y); l[k].z = (float)(r2 - (double)h[k].z);
+        l[k].w = 0.f;
+    }
+    S.pos[i] = h[0];
+    S.poslo[i] = l[0];
+    S.velf[i] = make_float4((float)S.v[3 * i], (float)S.v[3 * i + 1], (float)S.v[3 * i + 2], 0.f);
+    if (na == 3) put_wrec(S.wrec + i, h, l);
+}
+
 __global__ void k_wrec(DevSys S, const int *wgrp, int n) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
@@ -339,6 +360,13 @@ void launch_wrec(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
     if (!B.nwgrp) return;
     prof_begin(L, "k_wrec");
     k_wrec<<<nblk(B.nwgrp, 256), 256, 0, L.stream>>>(S, B.wgrp, B.nwgrp);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_mirror_range(const DevSys &S, LaunchCtx &L, int a0, int n) {
+    if (n <= 0) return;
+    prof_begin(L, "k_mirror_range");
+    k_mirror_range<<<nblk(n, 256), 256, 0, L.stream>>>(S, a0, n);
     prof_end(L);
     (*L.nlaunch)++;
 }

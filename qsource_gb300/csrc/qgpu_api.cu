@@ -870,7 +870,30 @@ int qgpu_set_coords(qgpu_handle *h, int32_t traj, const double *x, const double 
     ensure_double(h, L);
     if (x) CK(cudaMemcpyAsync(h->S.x + off, x, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (v) CK(cudaMemcpyAsync(h->S.v + off, v, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    launch_mirror(h->S, h->B, L);
+    launch_mirror_range(h->S, L, h->atom0[traj], h->natom[traj]);
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int qgpu_set_coords_all(qgpu_handle *h, const double *x, const double *v) {
+    if (!h) return fail(QGPU_E_INVALID, "null handle");
+    const size_t n = 3 * (size_t)h->S.natom;
+    LaunchCtx L{h->stream, &h->nlaunch};
+    ensure_double(h, L);
+    if (x) CK(cudaMemcpyAsync(h->S.x, x, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (v) CK(cudaMemcpyAsync(h->S.v, v, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    launch_mirror_range(h->S, L, 0, h->S.natom);
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+int qgpu_get_coords_all(qgpu_handle *h, double *x, double *v) {
+    if (!h) return fail(QGPU_E_INVALID, "null handle");
+    const size_t n = 3 * (size_t)h->S.natom;
+    LaunchCtx L{h->stream, &h->nlaunch};
+    ensure_double(h, L);
+    if (x) CK(cudaMemcpyAsync(x, h->S.x, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (v) CK(cudaMemcpyAsync(v, h->S.v, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return 0;
 }

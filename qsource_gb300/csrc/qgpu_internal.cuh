@@ -409,4 +409,5 @@ void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *
 void launch_tick(LaunchCtx &L, int *rec_base, int n);
 void launch_mirror(const DevSys &S, const BlockTables &B, LaunchCtx &L);   // also refreshes wrec
 void launch_wrec(const DevSys &S, const BlockTables &B, LaunchCtx &L);
+void launch_mirror_range(const DevSys &S, LaunchCtx &L, int a0, int n);   // one trajectory's atoms
 void launch_grad_to_double(const DevSys &S, LaunchCtx &L, double *out, int atom0, int natom);

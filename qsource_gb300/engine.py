@@ -74,6 +74,22 @@ class Engine:
         self._check(self.lib.qgpu_get_coords(self.h, traj, abi.ptr(x), abi.ptr(v)))
         return x, v
 
+    def set_coords_all(self, x=None, v=None):
+        """Coordinates / velocities of every trajectory, back to back in
+        trajectory order (qgpu_set_coords_all)."""
+        xa = None if x is None else np.ascontiguousarray(x, np.float64)
+        va = None if v is None else np.ascontiguousarray(v, np.float64)
+        self._check(self.lib.qgpu_set_coords_all(self.h, abi.ptr(xa), abi.ptr(va)))
+
+    def coords_all(self, x=None, v=None):
+        """Every trajectory's x and v back to back (qgpu_get_coords_all); fills
+        the given arrays (e.g. pinned host buffers) or new ones."""
+        n = 3 * sum(s.natom for s in self.systems)
+        x = np.zeros(n) if x is None else x
+        v = np.zeros(n) if v is None else v
+        self._check(self.lib.qgpu_get_coords_all(self.h, abi.ptr(x), abi.ptr(v)))
+        return x, v
+
     # ----------------------------------------------------------- call points
     def make_pair_lists(self):
         self._check(self.lib.qgpu_build_lists(self.h))

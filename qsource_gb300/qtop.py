@@ -279,6 +279,19 @@ def read_inp(text: str) -> dict:
     lam = []
     for ln in secs.get("lambdas", []):
         lam.extend(float(x) for x in ln.split())
+    # [sequence_restraints]: atom_i atom_j fc H-flag to_centre (initialize,
+    # src/md.f90:5215-5233; to_centre defaults to 0)
+    rstseq = []
+    for ln in secs.get("sequence_restraints", []):
+        t = ln.split()
+        if len(t) >= 3:
+            rstseq.append((int(t[0]), int(t[1]), float(t[2]), int(t[3]) if len(t) > 3 else 0,
+                           int(t[4]) if len(t) > 4 else 0))
+
+    def real(d, key, default=None):
+        return float(d[key]) if key in d else default
+
+    wpol = onoff(solv.get("polarisation"), True)
     return {
         "steps": int(md.get("steps", 0)),
         "stepsize": float(md.get("stepsize", 1.0)),
@@ -303,7 +316,15 @@ def read_inp(text: str) -> dict:
         "excluded_force": float(sph.get("excluded_force", 200.0)),
         "solvent_radius": float(solv["radius"]) if "radius" in solv else None,
         "radial_force": float(solv["radial_force"]) if "radial_force" in solv else -1.0,
-        "polarisation": onoff(solv.get("polarisation"), True),
+        "polarisation": wpol,
+        "charge_correction": onoff(solv.get("charge_correction"), wpol),
+        "polarisation_force": real(solv, "polarisation_force", -1.0),
+        "excluded_freeze": onoff(sph.get("excluded_freeze"), False),
+        "sequence_restraints": rstseq,
+        "langevin_friction": real(md, "langevin_friction"),
+        "langevin_random": onoff(md.get("langevin_random"), False),
+        "nhchains": int(md["nhchains"]) if "nhchains" in md else 10,
+        "nose_hoover_mass": real(md, "nose-hoover_mass"),
         "morse_depth": float(solv.get("morse_depth", -1.0)),
         "morse_width": float(solv.get("morse_width", -1.0)),
         "non_bond": int(inter.get("non_bond", 10)),

@@ -115,6 +115,32 @@ class System:
             setattr(d, k, int(getattr(self, k)))
         d.detail_temps = int(self.detail_temps)
         d.any_atom_lists = int(getattr(self, "any_atom_lists", 0))
+        g = lambda k, dflt: getattr(self, k, dflt)
+        rij = np.asarray(g("rstseq_ij", np.zeros((0, 2), np.int32)), dtype=np.int32).reshape(-1, 2)
+        d.nrstr_seq = len(rij)
+        d.rstseq_ij = arr(rij, np.int32)
+        d.rstseq_fk = arr(np.asarray(g("rstseq_fk", np.zeros(0))), np.float64)
+        d.rstseq_flags = arr(np.asarray(g("rstseq_flags", np.zeros((0, 2), np.int32))).reshape(-1, 2), np.int32)
+        heavy = g("heavy", None)
+        if heavy is None:
+            heavy = (np.asarray(self.mass)[np.asarray(self.iac)] >= 4.0).astype(np.uint8)
+        d.heavy = arr(np.asarray(heavy), np.uint8)
+        d.excluded_freeze = int(g("excluded_freeze", 0))
+        wsh = np.asarray(g("wshell", np.zeros((0, 4))), dtype=np.float64).reshape(-1, 4)
+        d.fkwpol = float(g("fkwpol", 20.0))
+        d.nwpolr_shell = len(wsh)
+        d.wshell_rout = arr(wsh[:, 0], np.float64)
+        d.wshell_dr = arr(wsh[:, 1], np.float64)
+        d.wshell_cstb = arr(wsh[:, 2], np.float64)
+        d.wshell_theta_corr = arr(wsh[:, 3], np.float64)
+        d.itdis_update = int(g("itdis_update", 100))
+        d.thermostat = int(g("thermostat", 0))
+        d.integrator = int(g("integrator", 0))
+        d.friction = float(g("friction", 1.0 / self.tau_T))
+        d.langevin_gauss = int(g("langevin_gauss", 0))
+        d.rand_state = int(g("rand_state", 1))
+        d.nhchains = int(g("nhchains", 10))
+        d.nhq = float(g("nhq", 0.001986 * self.Temp0 / (self.tau_T * self.tau_T)))
         return d
 
     @property
@@ -456,6 +482,52 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
     aLJ_solv = np.array([avdw[iac[ns + k], 0:2] for k in range(3)])
     bLJ_solv = np.array([bvdw[iac[ns + k], 0:2] for k in range(3)])
     x = xtop.copy()
+
+    # --- thermostat / integrator ([MD], initialize src/md.f90:4648-4705)
+    thermo = {"berendsen": 0, "langevin": 1, "nose-hoover": 2}.get(str(inp["thermostat"]).lower())
+    if thermo is None:
+        raise ValueError(f"unknown thermostat {inp['thermostat']}")
+    integ = {"leap-frog": 0, "velocity-verlet": 1}.get(str(inp["integrator"]).lower())
+    if integ is None:
+        raise ValueError(f"unknown integrator {inp['integrator']}")
+    tau_T = TIME_UNIT * inp["bath_coupling"]
+    friction = inp["langevin_friction"] if inp["langevin_friction"] is not None else 1.0 / tau_T
+    kbT = BOLTZ * inp["temperature"]
+    nhq = inp["nose_hoover_mass"] if inp["nose_hoover_mass"] is not None else kbT / (tau_T * tau_T)
+
+    # --- sequence restraints (0-based atoms)
+    rs = inp["sequence_restraints"]
+    rstseq_ij = np.array([(a - 1, b - 1) for a, b, _, _, _ in rs], dtype=np.int32).reshape(-1, 2)
+    rstseq_fk = np.array([fk for _, _, fk, _, _ in rs], dtype=np.float64)
+    rstseq_flags = np.array([(ih, tc) for _, _, _, ih, tc in rs], dtype=np.int32).reshape(-1, 2)
+
+    # --- water polarisation shells (wat_sphere / wat_shells, src/md.f90:18106-18368)
+    wpol = bool(inp["polarisation"]) and natom > nsol
+    fkwpol = inp["polarisation_force"] if inp["polarisation_force"] != -1.0 else 20.0
+    wshell = np.zeros((0, 4))
+    if wpol:
+        crgQtot = 0.0
+        if inp["charge_correction"]:
+            for iq in range(nq):
+                for s_ in range(S):
+                    crgQtot += qcrg[iq, s_] / sq * lam[s_]
+        # the water dipole from the last bond and angle of the topology
+        bcod = int(top["bnd"][-1][2]) - 1
+        acod = int(top["ang"][-1][3]) - 1
+        mu_w = -(crg[nsol] / sq) * top["bondlib"][bcod][1] * math.cos(top["anglib"][acod][1] * DEG2RAD / 2.0)
+        drs = 3.0001 / 0.5
+        nsh = int(-0.5 + math.sqrt(2.0 * drs + 0.25))
+        rows = []
+        rout = rwat
+        pi = 4.0 * math.atan(1.0)
+        for k in range(1, nsh + 1):
+            dr = 0.5 * k
+            ri = rout - dr
+            rshell = (0.5 * (rout ** 3 + ri ** 3)) ** (1.0 / 3.0)
+            cstb = crgQtot * 0.98750 / (0.0335 * mu_w * 4.0 * pi * rshell ** 2)
+            rows.append((rout, dr, cstb, 0.0))
+            rout = rout - dr
+        wshell = np.array(rows, dtype=np.float64).reshape(-1, 4)
     return System(
         natom=natom, nat_solute=nsol, natyps=natyps, ncgp_solute=ncgp_solute, nqat=nq, nstates=S,
         x=x, v=np.zeros(3 * natom), xtop=xtop, crg=crg, iac=iac, excl=excl, shell=shell, iqatom=iqatom,
@@ -475,10 +547,14 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
         shake_first=shake_first, shake_i=shake_i, shake_j=shake_j, shake_dist2=shake_d2,
         offd=offd, xpcent=top["xpcent"], xwcent=top["xwcent"], rexcl_o=rexcl_o, rwat=rwat,
         fk_wsphere=fk_wsphere, Dwmz=Dwmz, awmz=awmz, fk_pshell=inp["shell_force"], fk_fix=fk_fix,
-        wpol_restr=inp["polarisation"],
+        wpol_restr=wpol, fkwpol=fkwpol, wshell=wshell, itdis_update=100,
+        rstseq_ij=rstseq_ij, rstseq_fk=rstseq_fk, rstseq_flags=rstseq_flags, heavy=heavy.astype(np.uint8),
+        excluded_freeze=int(inp["excluded_freeze"]),
+        thermostat=thermo, integrator=integ, friction=friction, langevin_gauss=int(inp["langevin_random"]),
+        rand_state=int(inp["random_seed"]), nhchains=int(inp["nhchains"]), nhq=nhq,
         Rcpp=inp["Rcpp"], Rcww=inp["Rcww"], Rcpw=inp["Rcpw"], Rcq=inp["Rcq"], RcLRF=inp["RcLRF"],
         use_LRF=inp["lrf"], dt=TIME_UNIT * inp["stepsize"], Temp0=inp["temperature"],
-        tau_T=TIME_UNIT * inp["bath_coupling"], separate_scaling=separate_scaling, NBcycle=inp["non_bond"],
+        tau_T=tau_T, separate_scaling=separate_scaling, NBcycle=inp["non_bond"],
         Ndegf=Ndegf, Ndegfree=Ndegfree, Ndegf_solvent=Ndegf_solvent, Ndegfree_solvent=Ndegfree_solvent,
         Ndegf_solute=Ndegf_solute, Ndegfree_solute=Ndegfree_solute, detail_temps=detail,
         any_atom_lists=0 if int(top.get("iuse_switch_atom", 1)) == 1 else 1,

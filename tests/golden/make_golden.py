@@ -15,6 +15,9 @@ reference's published step-0 values for the same systems:
              tests/basic_tests/run_test.sh:171-176
   test2:     tests/test2/eval_test.sh:67  "Q-surr. 1 1.0000 3.12 139.43"
   test3:     tests/test3/eval_test.sh:67  "Q-surr. 1 1.0000 -14.07 3.11"
+  basic_sph_dynamics: rows 1-3 (step 0, step 50, final after 100 steps) of
+             tests/basic_tests/SPH_{leap-frog,velocity-verlet}_{berendsen,
+             langevin,nose-hoover}_benchmark.en
 """
 import json
 import os
@@ -58,8 +61,31 @@ def parse_benchmark_row1(path: str) -> dict:
     raise ValueError(path)
 
 
+def parse_benchmark_rows(path: str, nrows: int = 3) -> list:
+    """Rows 1..nrows of a basic_tests band file: per row, the 15 columns
+    QEL QVdW EL VdW QBND QANG QTOR QIMP BND ANG TOR IMP TOT KIN POT as
+    [lower, upper] pairs."""
+    cols = "QEL QVdW EL VdW QBND QANG QTOR QIMP BND ANG TOR IMP TOT KIN POT".split()
+    out = []
+    with open(path) as f:
+        for line in f:
+            if not line[:1].isdigit():
+                continue
+            v = [float(x) for x in line.split()[1:]]
+            out.append({c: [v[2 * k], v[2 * k + 1]] for k, c in enumerate(cols)})
+            if len(out) == nrows:
+                break
+    return out
+
+
 def main(ref: str):
     gold = {}
+    # rows 1-3 of the six sphere band files: step 0, step 50 and the final
+    # energies after 100 steps of tests/basic_tests/eq1.inp
+    gold["basic_sph_dynamics"] = {
+        f"{integ}/{thermo}": parse_benchmark_rows(
+            os.path.join(ref, f"tests/basic_tests/SPH_{integ}_{thermo}_benchmark.en"))
+        for integ in ("leap-frog", "velocity-verlet") for thermo in ("berendsen", "langevin", "nose-hoover")}
     for name, (top, fep, inp) in systems(ref):
         s = System.from_files(top, fep, inp)
         s.save_npz(os.path.join(HERE, f"{name}.npz"))

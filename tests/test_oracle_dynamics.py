@@ -1,0 +1,85 @@
+"""The FP64 oracle's MD loop against the reference's own dynamics bands.
+
+tests/basic_tests/SPH_<integrator>_<thermostat>_benchmark.en of the reference
+hold, per output row, the lower and upper value of 15 energy columns over the
+reference's benchmark runs of tests/basic_tests/eq1.inp (3,397-atom water
+sphere with the 46-atom ligand, 0.1 fs steps, T0 = 0.1 K, tau_T = 1 fs,
+sequence restraint on atoms 1-46, shell, radial and polarisation restraints).
+Rows 1-3 are step 0, step 50 and the final energies after 100 steps
+(tests/golden/golden.json, written by tests/golden/make_golden.py).
+
+Tolerances:
+  * row 1, the 12 energy columns: equal to the band after rounding to the
+    reference's printed 2 decimals (an exact pin);
+  * row 1, KIN / TOT / POT: within the band +- 0.5 kcal/mol.  Step 0's
+    velocities come from initial shaking of Maxwell velocities divided by
+    dt = 0.1 fs, which amplifies the SHAKE residuals; the reference runs
+    themselves spread by 0.2-0.5 kcal/mol here;
+  * rows 2 and 3: within [lo - tol, hi + tol] with
+    tol = 2 (hi - lo) + 0.005 |mid| + 0.05 kcal/mol, the band widened by twice
+    its own spread plus 0.5 % for the chaotic growth of last-digit
+    differences over 100 steps;
+  * Nose-Hoover row 3 (after the thermostat has driven the system from 35 K
+    to about 380 K): KIN and TOT to 2 % of the band centre.
+"""
+import pytest
+
+from conftest import golden_system
+
+COLS = "QEL QVdW EL VdW QBND QANG QTOR QIMP BND ANG TOR IMP TOT KIN POT".split()
+THERMO = {"berendsen": 0, "langevin": 1, "nose-hoover": 2}
+INTEG = {"leap-frog": 0, "velocity-verlet": 1}
+
+
+def columns(E, EQ):
+    q = EQ[0]
+    return {
+        "QEL": q["qp_el"] + q["qw_el"], "QVdW": q["qp_vdw"] + q["qw_vdw"],
+        "EL": E["pp_el"] + E["pw_el"] + E["ww_el"], "VdW": E["pp_vdw"] + E["pw_vdw"] + E["ww_vdw"],
+        "QBND": q["q_bond"], "QANG": q["q_angle"], "QTOR": q["q_torsion"], "QIMP": q["q_improper"],
+        "BND": E["p_bond"], "ANG": E["p_angle"], "TOR": E["p_torsion"], "IMP": E["p_improper"],
+        "TOT": E["kinetic"] + E["potential"], "KIN": E["kinetic"], "POT": E["potential"],
+    }
+
+
+def run_eq1(integrator: str, thermostat: str):
+    """qdyn's start-up (maxwell, initial shaking, stop_cm_translation,
+    temperature) and 100 steps of eq1.inp with the oracle; rows 1-3."""
+    from oracle.oracle import Oracle
+    s = golden_system("basic_sph")
+    s.thermostat = THERMO[thermostat]
+    s.integrator = INTEG[integrator]
+    o = Oracle(s)
+    o.maxwell(s.Tmaxw, int(s.seed))
+    assert o.initial_shaking() == 0
+    o.stop_cm_translation()
+    o.temperature()
+    rc, rows, qrows, _ = o.md_run(100)
+    assert rc == 0
+    Ef, EQf = o.final_energy()
+    return [columns(rows[0], qrows[0]), columns(rows[50], qrows[50]), columns(Ef, EQf)]
+
+
+@pytest.mark.parametrize("integrator", list(INTEG))
+@pytest.mark.parametrize("thermostat", list(THERMO))
+def test_md_rows_match_reference_bands(golden, integrator, thermostat):
+    bands = golden["basic_sph_dynamics"][f"{integrator}/{thermostat}"]
+    got = run_eq1(integrator, thermostat)
+    bad = []
+    for r in range(3):
+        for c in COLS:
+            lo, hi = bands[r][c]
+            g = got[r][c]
+            mid = 0.5 * (lo + hi)
+            if r == 0 and c not in ("TOT", "KIN", "POT"):
+                ok = round(g, 2) == pytest.approx(round(mid, 2), abs=1e-9)
+            elif r == 0:
+                ok = lo - 0.5 <= g <= hi + 0.5
+            elif r == 2 and thermostat == "nose-hoover" and c in ("KIN", "TOT"):
+                ok = abs(g - mid) <= 0.02 * abs(mid)
+            else:
+                tol = 2.0 * (hi - lo) + 0.005 * abs(mid) + 0.05
+                ok = lo - tol <= g <= hi + tol
+            if not ok:
+                bad.append((r + 1, c, round(g, 4), lo, hi))
+    assert not bad, bad
