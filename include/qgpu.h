@@ -294,6 +294,12 @@ int qgpu_shake(qgpu_handle *h, int32_t traj, const double *xx, double *x, int32_
 int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every,
              qgpu_ene_sink sink, void *user);
 
+/* Sets the step counter istep (md_run's loop index).  The water polarisation
+   restraint updates its theta_corr when istep is a nonzero multiple of
+   itdis_update (src/md.f90:18451); qgpu_run advances the counter itself, a
+   drop-in host that calls qgpu_forces once per step sets it before each call. */
+int qgpu_set_step(qgpu_handle *h, int64_t istep);
+
 /* Precision of the persistent MD step (qgpu_run / qgpu_enqueue).
    QGPU_PRECISION_MIXED (the default): master positions as a double-float
      (about 48 significant bits), FP32 velocities, SHAKE of 3-site waters in

@@ -58,6 +58,8 @@ def lib() -> C.CDLL:
         L.oracle_md_run.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(Energies), C.POINTER(QEnergy), vp]
         L.oracle_get_energies.argtypes = [vp, C.POINTER(Energies), C.POINTER(QEnergy)]
         L.oracle_final_energy.argtypes = [vp, C.c_int, C.POINTER(Energies), C.POINTER(QEnergy)]
+        L.oracle_rand_state.restype = C.c_int32
+        L.oracle_rand_state.argtypes = [vp]
         L.oracle_sizeof_desc.restype = C.c_int
         _lib = L
     return _lib
@@ -141,6 +143,10 @@ class Oracle:
         H = np.zeros(max(n, 1)); r = np.zeros(max(n, 1))
         self.L.oracle_offdiag(self.h, _p(H), _p(r))
         return H[:n], r[:n]
+
+    def rand_state(self) -> int:
+        """The randm state the next random number continues from."""
+        return int(self.L.oracle_rand_state(self.h))
 
     def final_energy(self, terms: int = 0x1F):
         """Lists and energies after an MD run (the reference's FINAL report)."""

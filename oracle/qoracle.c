@@ -1529,6 +1529,12 @@ void oracle_get_energies(void *h, qgpu_energies *E, qgpu_qenergy *EQ) {
     if (E) *E = o->E;
     if (EQ) memcpy(EQ, o->EQ, (size_t)o->S * sizeof(qgpu_qenergy));
 }
+/* the randm state the next random number continues from (the reference's
+   iseed after its last randm call) */
+int32_t oracle_rand_state(void *h) {
+    oracle *o = (oracle *)h;
+    return o->rand_new ? o->irand : abs(o->iseed) % 100000000;
+}
 int oracle_sizeof_desc(void) { return (int)sizeof(qgpu_system_desc); }
 int oracle_sizeof_energies(void) { return (int)sizeof(qgpu_energies); }
 int oracle_sizeof_qenergy(void) { return (int)sizeof(qgpu_qenergy); }

@@ -121,6 +121,7 @@ EXPORTS = {
     "qgpu_run": (_i32, [C.c_void_p, _i32, _i32, ENE_SINK, C.c_void_p]),
     "qgpu_enqueue": (_i32, [C.c_void_p, _i32, _i32]),
     "qgpu_set_precision": (_i32, [C.c_void_p, _i32]),
+    "qgpu_set_step": (_i32, [C.c_void_p, C.c_int64]),
     "qgpu_sync": (_i32, [C.c_void_p]),
     "qgpu_get_group_pairs": (_i32, [C.c_void_p, _i32, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "qgpu_get_lrf": (_i32, [C.c_void_p, _i32, _P]),

@@ -10,8 +10,12 @@
 #define SHAKE_TOL 0.0001        // src/md.f90:460
 #define SHAKE_MAX_ITER 1000     // src/md.f90:461
 
-// v = (v - d*winv*dt)*Tscale; xx = x; x += v*dt.  Consumes and clears the
-// fixed-point gradient.
+// The thermostat's velocity and position update of one atom (md_run
+// :6577-6590): Berendsen newvel_ber (v = (v - d winv dv)*Tscale), Langevin
+// newvel_lan (v = v*(1 - friction dv) - (d - F_rand) winv dv), Nose-Hoover
+// nh_prop scale + newvel_nos; xx = x, x += v dt; with velocity-verlet
+// (dv = dt/2) the velocity update is applied again after the position update.
+// Consumes and clears the fixed-point gradient.
 __global__ void k_integrate(DevSys S) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= S.natom) return;
@@ -19,16 +23,26 @@ __global__ void k_integrate(DevSys S) {
     const TrajInfo &T = S.traj[tr];
     const TrajState &TS = S.tstate[tr];
     const double ts = (i - T.atom0) < T.nat_solute ? TS.tsf_solute : TS.tsf_solvent;
-    const double wi = S.winv[i], dt = T.dt;
+    const double wi = S.winv[i], dt = T.dt, dvm = T.dvm;
+    double rf[3] = {0.0, 0.0, 0.0};
+    if (T.thermostat == 1) langevin_force<double>(S, T, TS.rnd, i, rf);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const int k = 3 * i + c;
         const double g = fx_get(S.fx[k]);
         S.fx[k] = 0ull;
-        const double v = (S.v[k] - g * wi * dt) * ts;
-        S.v[k] = v;
+        double v = S.v[k];
+        if (T.thermostat == 1) v = v * T.lfric - (g - rf[c]) * wi * dvm;
+        else if (T.thermostat == 2) v = v * TS.nh_s1 - g * wi * dvm;
+        else v = (v - g * wi * dvm) * ts;
         S.xx[k] = S.x[k];
         S.x[k] = S.x[k] + v * dt;
+        if (T.integrator == 1) {
+            if (T.thermostat == 1) v = v * T.lfric - (g - rf[c]) * wi * dvm;
+            else if (T.thermostat == 2) v = v - g * wi * dvm;
+            else v = (v - g * wi * dvm) * ts;
+        }
+        S.v[k] = v;
     }
 }
 
@@ -101,7 +115,13 @@ __global__ void __launch_bounds__(QG_BLOCK) k_update(DevSys S, const int *items,
             for (int a = 0; a < 3; ++a) {
                 x[a] = S.x[3 * i + a];
                 v[a] = S.v[3 * i + a];
-                if (mode == 2) { v[a] = (x[a] - S.xx[3 * i + a]) * T.inv_dt; S.v[3 * i + a] = v[a]; }
+                if (mode == 2 && T.nshake_mol > 0) {
+                    // v = (x - xx)/dt after SHAKE (md_run :6596-6600), then the
+                    // Nose-Hoover second scale
+                    v[a] = (x[a] - S.xx[3 * i + a]) * T.inv_dt;
+                    if (T.thermostat == 2) v[a] *= S.tstate[tr].nh_s2;
+                    S.v[3 * i + a] = v[a];
+                }
                 vv += v[a] * v[a];
             }
             const double e = 0.5 * S.mass[i] * vv;
@@ -233,9 +253,21 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
             const float ts = (a - T.atom0) < T.nat_solute ? TS.tsf_solute : TS.tsf_solvent;
             const float gx = fx_getf(S.fx[3 * a]), gy = fx_getf(S.fx[3 * a + 1]), gz = fx_getf(S.fx[3 * a + 2]);
             S.fx[3 * a] = 0ull; S.fx[3 * a + 1] = 0ull; S.fx[3 * a + 2] = 0ull;
-            const float wdt = w * dt;
-            v = make_float3((v.x - gx * wdt) * ts, (v.y - gy * wdt) * ts, (v.z - gz * wdt) * ts);
+            // the thermostat's update (see k_integrate), in FP32
+            const float wdv = w * T.dvmf;
+            float rf[3] = {0.f, 0.f, 0.f};
+            if (T.thermostat == 1) langevin_force<float>(S, T, TS.rnd, a, rf);
+            const float s1 = T.thermostat == 2 ? (float)TS.nh_s1 : 1.f;
+            auto kick = [&](float3 u, float fs) {
+                if (T.thermostat == 1)
+                    return make_float3(u.x * T.lfricf - (gx - rf[0]) * wdv, u.y * T.lfricf - (gy - rf[1]) * wdv,
+                                       u.z * T.lfricf - (gz - rf[2]) * wdv);
+                if (T.thermostat == 2) return make_float3(u.x * fs - gx * wdv, u.y * fs - gy * wdv, u.z * fs - gz * wdv);
+                return make_float3((u.x - gx * wdv) * ts, (u.y - gy * wdv) * ts, (u.z - gz * wdv) * ts);
+            };
+            v = kick(v, s1);
             D = make_float3(v.x * dt, v.y * dt, v.z * dt);
+            if (T.integrator == 1) v = kick(v, 1.f);
             if (water_blk) {
                 s_h[t] = h; s_l[t] = l; s_w[t] = w;
                 s_D[0][t] = D.x; s_D[1][t] = D.y; s_D[2][t] = D.z;
@@ -277,7 +309,13 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
     float ek[4] = {0.f, 0.f, 0.f, 0.f};
     if (a >= 0) {
         if (!ekin_only) {
-            if (T.nshake_mol > 0) v = make_float3(D.x * T.inv_dtf, D.y * T.inv_dtf, D.z * T.inv_dtf);
+            if (T.nshake_mol > 0) {
+                v = make_float3(D.x * T.inv_dtf, D.y * T.inv_dtf, D.z * T.inv_dtf);
+                if (T.thermostat == 2) {
+                    const float s2 = (float)S.tstate[tr].nh_s2;
+                    v = make_float3(v.x * s2, v.y * s2, v.z * s2);
+                }
+            }
             hilo_add(h.x, l.x, D.x);
             hilo_add(h.y, l.y, D.y);
             hilo_add(h.z, l.z, D.z);
@@ -339,6 +377,39 @@ __global__ void k_sync_double(DevSys S) {
 // T = Ekin * 2/(Boltz*Ndegf) with the constants formed on the host, the
 // Berendsen scale sqrt(1 + dt/tau_T (T0/T - 1)) (src/md.f90:6160-6180).
 // FP64 is used for the record rows only.
+// nh_prop, src/md.f90:6300-6345: Nose-Hoover chain propagation by dt/2;
+// returns the velocity scale s (chain index i = reference i - 1).
+__device__ double nh_prop(const TrajInfo &T, double *vnh, double *xnh, double Temp) {
+    const int nc = T.nhc;
+    if (nc < 1) return 1.0;
+    const double dt2 = 0.5 * T.dt, dt4 = 0.5 * dt2, dt8 = 0.5 * dt4, kbT = T.kbT;
+    double G[QG_MAXNH];
+    double expf = 1.0;
+    G[0] = T.Ndegf * BOLTZ * (Temp - T.Temp0) / T.qnh[0];
+    for (int i = 1; i < nc; ++i) G[i] = (T.qnh[i - 1] * vnh[i - 1] * vnh[i - 1] - kbT) / T.qnh[i];
+    vnh[nc - 1] = vnh[nc - 1] + G[nc - 1] * dt4;
+    xnh[nc - 1] = xnh[nc - 1] + vnh[nc - 1] * dt2;
+    for (int i = nc - 2; i >= 0; --i) {
+        expf = exp(-dt8 * vnh[i + 1]);
+        vnh[i] = (vnh[i] * expf + G[i] * dt4) * expf;
+        xnh[i] = xnh[i] + vnh[i] * dt2;
+    }
+    const double sc = exp(-vnh[0] * dt2);
+    G[0] = T.Ndegf * BOLTZ * (sc * sc * Temp - T.Temp0) / T.qnh[0];
+    vnh[0] = (vnh[0] * expf + G[0] * dt4) * expf;
+    for (int i = 1; i < nc - 1; ++i) {
+        expf = exp(-dt8 * vnh[i + 1]);
+        G[i] = (T.qnh[i - 1] * vnh[i - 1] * vnh[i - 1] - kbT) / T.qnh[i];
+        vnh[i] = (vnh[i] * expf + G[i] * dt4) * expf;
+    }
+    if (nc > 1) {
+        G[nc - 1] = (T.qnh[nc - 2] * vnh[nc - 2] * vnh[nc - 2] - kbT) / T.qnh[nc - 1];
+        vnh[nc - 1] = vnh[nc - 1] + G[nc - 1] * dt4;
+    }
+    return sc;
+}
+
+// do_temp: FIN_* flags
 __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_base, int k, int ene_every, int rec_cap) {
     __shared__ double v[QG_NE];
     const int tr = blockIdx.x;
@@ -372,7 +443,9 @@ __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_ba
             const float Temp = Ekin * T.cT, Tfree = (e4[1] + e4[3]) * T.cTfree;
             if (T.detail_temps) { Tfsu *= T.cTfsu; Tfsv *= T.cTfsv; }
             float ts = TS.tsf_solvent, tu = TS.tsf_solute;
-            if (T.separate_scaling) {
+            if (T.thermostat != 0) {
+                ts = 1.f; tu = 1.f;   // only the Berendsen thermostat scales (md.f90:6166)
+            } else if (T.separate_scaling) {
                 if (Tfsv != 0.f) ts = T.Temp0f / Tfsv - 1.f;
                 ts = sqrtf(1.f + T.dt_tau * ts);
                 if (Tfsu != 0.f) tu = T.Temp0f / Tfsu - 1.f;
@@ -386,6 +459,15 @@ __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_ba
             TS.tsf_solute = tu; TS.tsf_solvent = ts;
             TS.wshiftf = T.fk_wspheref != 0.f ? sqrtf(0.001986f * Tfree / T.fk_wspheref) : 0.f;
             if (Temp != Temp) atomicOr(S.status, ST_NAN);
+            if (T.thermostat == 1 && (do_temp & FIN_STEP))
+                TS.rnd = (unsigned)((T.lcgA * TS.rnd + T.lcgC) % QG_LCG_M);
+            if (T.thermostat == 2 && (do_temp & FIN_NH)) {
+                // the two nh_prop calls of the next step (before the update and
+                // after SHAKE, md_run :6584-6600) both read this temperature
+                double *vnh = S.nh_state + (size_t)tr * 2 * QG_MAXNH, *xnh = vnh + QG_MAXNH;
+                TS.nh_s1 = nh_prop(T, vnh, xnh, (double)Temp);
+                TS.nh_s2 = T.nshake_mol > 0 ? nh_prop(T, vnh, xnh, (double)Temp) : 1.0;
+            }
         }
     }
     __syncwarp();
@@ -418,7 +500,8 @@ __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_ba
     E[11] = qb; E[12] = qa; E[13] = qt; E[14] = qi;
     E[15] = v[EA_PP_EL]; E[16] = v[EA_PP_VDW]; E[17] = v[EA_PW_EL]; E[18] = v[EA_PW_VDW];
     E[19] = v[EA_WW_EL]; E[20] = v[EA_WW_VDW]; E[21] = qxe; E[22] = qxv;
-    E[24] = v[EA_RST_FIX]; E[25] = v[EA_RST_SHELL]; E[26] = 0.0; E[27] = v[EA_RST_RAD]; E[28] = 0.0;
+    E[24] = v[EA_RST_FIX]; E[25] = v[EA_RST_SHELL]; E[26] = v[EA_RST_PROT]; E[27] = v[EA_RST_RAD];
+    E[28] = v[EA_RST_WPOL];
     E[23] = E[24] + E[25] + E[26] + E[27] + E[28];
     E[0] = E[3] + E[7] + E[4] + E[8] + E[5] + E[6] + E[15] + E[16] + E[17] + E[18] + E[19] + E[20] + E[11] + E[12] +
            E[13] + E[14] + E[21] + E[22] + E[23] + E[2];

@@ -459,6 +459,76 @@ __device__ void restrain_solvent_block(const DevSys &S, int b, const int *wgrp, 
     block_energies_fx<1>(S.eacc + (size_t)traj * QG_NE, slots, v, red);
 }
 
+// p_restrain's sequence restraints, src/md.f90:15484-15576.  One block per
+// restraint; an atom of the range takes part when heavy, or when the H flag
+// is set and it is not a frozen excluded atom.  to_centre 1 / 2 restrain the
+// (mass-weighted) mean displacement from the topology and apply fk*dr
+// (x mass/12.010 for the geometric centre) to every taking part atom;
+// to_centre 0 restrains each atom.
+template <typename R>
+__device__ void seqrst_block(const DevSys &S, int b, Red &red) {
+    typedef P<R> p;
+    __shared__ R sw[4][QG_BLOCK / 32];
+    __shared__ R tot[4];
+    const int i0 = S.rs_i0[b], i1 = S.rs_i1[b], ih = S.rs_ih[b], tc = S.rs_tc[b], traj = S.rs_traj[b];
+    const TrajInfo &T = S.traj[traj];
+    const R fk = R(S.rs_fk[b]);
+    auto sel = [&](int i) { return S.aheavy[i] || (ih == 1 && !(S.aexcl[i] && T.freeze)); };
+    auto disp = [&](int i, R &d0, R &d1, R &d2) {
+        if (sizeof(R) == 8) {
+            d0 = R(S.x[3 * i] - S.xtop[3 * i]); d1 = R(S.x[3 * i + 1] - S.xtop[3 * i + 1]);
+            d2 = R(S.x[3 * i + 2] - S.xtop[3 * i + 2]);
+        } else {
+            const float3 d = dpos(S.xtoph[i], S.xtopl[i], S.pos[i], S.poslo[i]);
+            d0 = R(d.x); d1 = R(d.y); d2 = R(d.z);
+        }
+    };
+    R e = 0;
+    if (tc == 1 || tc == 2) {
+        R acc[4] = {0, 0, 0, 0};
+        for (int i = i0 + (int)threadIdx.x; i <= i1; i += blockDim.x) {
+            if (!sel(i)) continue;
+            R d0, d1, d2;
+            disp(i, d0, d1, d2);
+            const R m = tc == 2 ? R(S.mass[i]) : R(1);
+            acc[0] += d0 * m; acc[1] += d1 * m; acc[2] += d2 * m; acc[3] += m;
+        }
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+            if (lane == 0) sw[c][warp] = acc[c];
+        }
+        __syncthreads();
+        if (threadIdx.x < 4) {
+            R t = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sw[threadIdx.x][w];
+            tot[threadIdx.x] = t;
+        }
+        __syncthreads();
+        if (tot[3] > R(0)) {
+            const R dr0 = tot[0] / tot[3], dr1 = tot[1] / tot[3], dr2 = tot[2] / tot[3];
+            if (threadIdx.x == 0) e = R(0.5) * fk * (dr0 * dr0 + dr1 * dr1 + dr2 * dr2);
+            for (int i = i0 + (int)threadIdx.x; i <= i1; i += blockDim.x) {
+                if (!sel(i)) continue;
+                const R sc = tc == 1 ? R(S.mass[i]) / R(12.010) : R(1);
+                p::grad(S, i, fk * dr0 * sc, fk * dr1 * sc, fk * dr2 * sc);
+            }
+        }
+    } else {
+        for (int i = i0 + (int)threadIdx.x; i <= i1; i += blockDim.x) {
+            if (!sel(i)) continue;
+            R d0, d1, d2;
+            disp(i, d0, d1, d2);
+            e += R(0.5) * fk * (d0 * d0 + d1 * d1 + d2 * d2);
+            p::grad(S, i, fk * d0, fk * d1, fk * d2);
+        }
+    }
+    const int slots[1] = {EA_RST_PROT};
+    long long v[1] = {p::fx(e, S.status)};
+    block_energies_fx<1>(S.eacc + (size_t)traj * QG_NE, slots, v, red);
+}
+
 // offdiag, src/md.f90:15444-15470: Hij = A exp(-mu r_kl).  Its only consumer is
 // the energy record, so it runs on the FP64 (recorded / drop-in) evaluations.
 __device__ void offdiag_block(const DevSys &S, int blk) {
@@ -476,7 +546,7 @@ __device__ void offdiag_block(const DevSys &S, int blk) {
 
 // The small terms share one launch: consecutive block ranges select the term.
 struct MiscPlan {
-    int nqq, nbt, nfix, nrad, nqb, nod;    // blocks per term
+    int nqq, nbt, nfix, nrad, nqb, nod, nrs;    // blocks per term
 };
 
 template <typename R>
@@ -493,6 +563,8 @@ __device__ __forceinline__ void misc_body(const DevSys &S, const MiscPlan &P, co
     b -= P.nrad;
     if (b < P.nqb) { qbonded_block<R>(S, b); return; }
     b -= P.nqb;
+    if (b < P.nrs) { seqrst_block<R>(S, b, red); return; }
+    b -= P.nrs;
     if (sizeof(R) == 8 && b < P.nod) offdiag_block(S, b);
 }
 
@@ -515,10 +587,165 @@ void launch_misc(const DevSys &S, const BlockTables &B, LaunchCtx &L, int terms,
     P.nrad = (terms & QGPU_TERMS_RESTRAINT) ? B.nwgrp / QG_BLOCK : 0;
     P.nqb = (terms & QGPU_TERMS_QBONDED) ? nblk(S.nqt * QG_MAXS, QG_BLOCK) : 0;
     P.nod = nblk(S.nod, QG_BLOCK);
-    const int nb = P.nqq + P.nbt + P.nfix + P.nrad + P.nqb + P.nod;
+    P.nrs = (terms & QGPU_TERMS_RESTRAINT) ? S.nrs : 0;
+    const int nb = P.nqq + P.nbt + P.nfix + P.nrad + P.nqb + P.nod + P.nrs;
     if (!nb) return;
     prof_begin(L, "k_misc");
     k_misc<<<nb, QG_BLOCK, 0, L.stream>>>(S, P, B.qqblk_traj, B.qqblk_s, B.satom, B.wgrp, e);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+
+// ------------------------------------------------------------------ watpol
+// watpol, src/md.f90:18372-18541: radial polarisation restraint of the waters
+// in the outer shells, one block per trajectory with the restraint on, FP64
+// throughout.  Coordinates are the origin-relative hi + lo floats (always
+// current; the origin is the solvent centre).  The reference's selection
+// sort by theta (ties in water order) is a rank: the number of shell members
+// with a smaller (theta, water) key.  Per-trajectory scratch (e_th, e_iw,
+// e_sh, e_rank, srt) lives in wp_scr at TrajInfo::wp_scr0.
+struct WpWater {
+    double rmu[3], rcu[3], rm, rc, scp, theta;
+};
+__device__ __forceinline__ void wp_water(const DevSys &S, int o, WpWater &w) {
+    double x[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float4 h = S.pos[o + k], l = S.poslo[o + k];
+        x[k][0] = (double)h.x + (double)l.x; x[k][1] = (double)h.y + (double)l.y; x[k][2] = (double)h.z + (double)l.z;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { w.rmu[a] = x[1][a] + x[2][a] - 2.0 * x[0][a]; w.rcu[a] = x[0][a]; }
+    w.rm = sqrt(w.rmu[0] * w.rmu[0] + w.rmu[1] * w.rmu[1] + w.rmu[2] * w.rmu[2]);
+    w.rc = sqrt(w.rcu[0] * w.rcu[0] + w.rcu[1] * w.rcu[1] + w.rcu[2] * w.rcu[2]);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { w.rmu[a] /= w.rm; w.rcu[a] /= w.rc; }
+    double sc = w.rmu[0] * w.rcu[0] + w.rmu[1] * w.rcu[1] + w.rmu[2] * w.rcu[2];
+    sc = fmin(1.0, fmax(-1.0, sc));
+    w.scp = sc;
+    w.theta = acos(sc);
+}
+
+__global__ void __launch_bounds__(QG_WPBLK) k_watpol(DevSys S, const int *wp_traj, double *scr, const int *wp_scr0,
+                                                     const int *step_base, int k) {
+    __shared__ int cnt[QG_MAXSHELL], tot;
+    __shared__ double sred[QG_WPBLK / 32];
+    const int tr = wp_traj[blockIdx.x];
+    const TrajInfo &T = S.traj[tr];
+    const int ns = T.nshell, nw = T.nwat, w0 = T.atom0 + T.nat_solute;
+    double *e_th = scr + wp_scr0[blockIdx.x];
+    int *e_iw = (int *)(e_th + nw);
+    int *e_sh = e_iw + nw;
+    int *e_rank = e_sh + nw;
+    double *srt = (double *)(e_rank + nw + (nw & 1));
+    double *st = S.wp_state + 3 * (size_t)T.wp0;   // per shell: theta_corr, avtheta, avn_insh
+    const int tid = threadIdx.x;
+    if (tid < QG_MAXSHELL) cnt[tid] = 0;
+    if (tid == 0) tot = 0;
+    __syncthreads();
+    // theta of each water and its shell
+    for (int iw = tid; iw < nw; iw += blockDim.x) {
+        const int o = w0 + 3 * iw;
+        if (S.aexcl[o]) continue;
+        WpWater w;
+        wp_water(S, o, w);
+        if (w.rc > T.wp_rlayer) {
+            int is;
+            for (is = ns; is >= 2; --is)
+                if (w.rc <= T.sh_rout[is - 1]) break;
+            if (is < 2) is = 1;
+            const int e = atomicAdd(&tot, 1);
+            atomicAdd(&cnt[is - 1], 1);
+            e_th[e] = w.theta; e_iw[e] = iw; e_sh[e] = is - 1;
+        }
+    }
+    __syncthreads();
+    const int ne = tot;
+    // rank inside the shell: (theta, water index) order
+    for (int e = tid; e < ne; e += blockDim.x) {
+        const double t = e_th[e];
+        const int iw = e_iw[e], sh = e_sh[e];
+        int r = 0;
+        for (int f = 0; f < ne; ++f) {
+            const double u = e_th[f];
+            r += (e_sh[f] == sh) && (u < t || (u == t && e_iw[f] < iw));
+        }
+        e_rank[e] = r;
+        int off = 0;
+        for (int q = 0; q < sh; ++q) off += cnt[q];
+        srt[off + r] = t;
+    }
+    // theta_corr update every itdis_update steps (md.f90:18451-18465)
+    const int istep = step_base[0] + k;
+    if (tid == 0 && istep != 0 && T.itdis_update > 0 && istep % T.itdis_update == 0)
+        for (int q = 0; q < ns; ++q) {
+            double *sq = st + 3 * q;
+            sq[1] /= (double)T.itdis_update;
+            sq[2] /= (double)T.itdis_update;
+            sq[0] = sq[0] + sq[1] - T.sh_acos_cstb[q];
+            sq[1] = 0.0; sq[2] = 0.0;
+        }
+    __syncthreads();
+    // energy and forces
+    double esum = 0.0;
+    const double pi = 3.141592653589793;
+    for (int e = tid; e < ne; e += blockDim.x) {
+        const int sh = e_sh[e], n = cnt[sh];
+        const int il = e_rank[e] + 1;
+        const double arg = 1.0 + (1.0 - 2.0 * (double)il) / (double)n;
+        double t0 = acos(arg);
+        t0 = t0 - 3.0 * sin(t0) * T.sh_cstb[sh] / 2.0;
+        t0 = fmin(pi, fmax(0.0, t0));
+        const double dth = e_th[e] - t0 + st[3 * sh];
+        esum += 0.5 * T.fkwpol * dth * dth;
+        const double dv = T.fkwpol * dth;
+        const int o = w0 + 3 * e_iw[e];
+        WpWater w;
+        wp_water(S, o, w);
+        double f0 = sin(acos(w.scp));
+        if (fabs(f0) < 1e-14) f0 = 1e-14;
+        f0 = dv * (-1.0 / f0);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double f1 = (w.rcu[a] - w.rmu[a] * w.scp) / w.rm;
+            const double f2 = (w.rmu[a] - w.rcu[a] * w.scp) / w.rc;
+            fx_add(S.fx + 3 * o + a, f0 * (-2.0 * f1 + f2), S.status);
+            fx_add(S.fx + 3 * (o + 1) + a, f0 * f1, S.status);
+            fx_add(S.fx + 3 * (o + 2) + a, f0 * f1, S.status);
+        }
+    }
+    // energy: fixed-point block sum
+    long long q = d2fx_chk(esum, S.status);
+    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+    __shared__ long long qred[QG_WPBLK / 32];
+    if ((tid & 31) == 0) qred[tid >> 5] = q;
+    __syncthreads();
+    if (tid == 0) {
+        long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += qred[w];
+        if (t) atomicAdd(S.eacc + (size_t)tr * QG_NE + EA_RST_WPOL, (unsigned long long)t);
+    }
+    // shell averages of theta, summed in rank order by one warp per shell
+    const int warp = tid >> 5, lane = tid & 31;
+    if (warp < ns) {
+        int off = 0;
+        for (int q2 = 0; q2 < warp; ++q2) off += cnt[q2];
+        const int n = cnt[warp];
+        double a = 0.0;
+        for (int r = lane; r < n; r += 32) a += srt[off + r];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0 && n > 0) {
+            st[3 * warp + 1] += a / (double)n;
+            st[3 * warp + 2] += (double)n;
+        }
+    }
+    (void)sred;
+}
+
+void launch_watpol(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
+    if (!B.nwp) return;
+    prof_begin(L, "k_watpol");
+    k_watpol<<<B.nwp, QG_WPBLK, 0, L.stream>>>(S, B.wp_traj, B.wp_scr, B.wp_scr0, e.recctl, e.k);
     prof_end(L);
     (*L.nlaunch)++;
 }

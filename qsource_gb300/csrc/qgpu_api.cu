@@ -86,6 +86,7 @@ struct qgpu_handle {
     long long nlaunch = 0;
     int NBcycle = 10;
     int lists_built = 0, temp_init = 0, any_shake = 0, any_wpol = 0;
+    int nh_ready = 0;          // Nose-Hoover scales of the next step are formed
     std::vector<char> fused;   // per trajectory: SHAKE fused into the update kernel
     bool all_fused = true;
     bool can_fuse = true;      // every trajectory's constraints allow the fused update
@@ -189,6 +190,14 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     std::vector<int> od_traj, od_ij, od_kl;
     std::vector<double> od_Amu;
     std::vector<int> wgrp, satom, scan_t0, scan_tn, scan_traj, scan_chunk, uitem, qqblk_traj, qqblk_s;
+    // sequence restraints, water polarisation
+    std::vector<int> rs_i0, rs_i1, rs_ih, rs_tc, rs_traj, wp_traj, wp_scr0;
+    std::vector<double> rs_fk, wp_state;
+    std::vector<uint8_t> aheavy;
+    long long wp_scr_n = 0;
+    // thermostats: Langevin amplitudes and randm skip-ahead per atom
+    std::vector<double> randva;
+    std::vector<unsigned> lcg_a, lcg_c, rnd0;
     std::vector<int> uatom, ucon;
     std::vector<uint8_t> ublk_water;
     std::vector<int> ek_u0, ek_un, ek_a0, ek_an;   // Ekin block ranges of the two update layouts
@@ -241,7 +250,67 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         T.Ndegf = d.Ndegf; T.Ndegfree = d.Ndegfree;
         T.Ndegfree_solute = d.Ndegfree_solute; T.Ndegfree_solvent = d.Ndegfree_solvent;
         T.ff_type = d.ff_type;
-        if (d.wpol_restr) h->any_wpol = 1;
+        // --- sequence restraints (p_restrain, src/md.f90:15484-15576)
+        for (int r = 0; r < d.nrstr_seq; ++r) {
+            const int a = d.rstseq_ij[2 * r], b = d.rstseq_ij[2 * r + 1];
+            if (a < 0 || b >= N || a > b) return fail(QGPU_E_INVALID, "trajectory %d: sequence restraint %d atoms", t, r);
+            rs_i0.push_back(atom0 + a); rs_i1.push_back(atom0 + b);
+            rs_fk.push_back(d.rstseq_fk[r]); rs_ih.push_back(d.rstseq_flags[2 * r]);
+            rs_tc.push_back(d.rstseq_flags[2 * r + 1]); rs_traj.push_back(t);
+        }
+        for (int i = 0; i < N; ++i)
+            aheavy.push_back(d.heavy ? d.heavy[i] : (uint8_t)(d.mass[d.iac[i]] >= 4.0));
+        T.freeze = d.excluded_freeze;
+        // --- thermostat / integrator (md_run :6440-6460)
+        if (d.thermostat < 0 || d.thermostat > 2 || d.integrator < 0 || d.integrator > 1)
+            return fail(QGPU_E_INVALID, "trajectory %d: thermostat %d / integrator %d", t, d.thermostat, d.integrator);
+        if (d.thermostat == 2 && (d.nhchains < 1 || d.nhchains > QG_MAXNH))
+            return fail(QGPU_E_UNSUPPORTED, "trajectory %d: Nose-Hoover chain of %d (1..%d)", t, d.nhchains, QG_MAXNH);
+        T.thermostat = d.thermostat; T.integrator = d.integrator; T.lgauss = d.langevin_gauss ? 1 : 0;
+        T.dvm = d.integrator == 1 ? 0.5 * d.dt : d.dt;
+        T.dvmf = (float)T.dvm;
+        T.lfric = 1.0 - d.friction * T.dvm;
+        T.lfricf = (float)T.lfric;
+        T.kbT = 0.001986 * d.Temp0;
+        T.nhc = d.thermostat == 2 ? d.nhchains : 0;
+        for (int c = 0; c < T.nhc; ++c) T.qnh[c] = c == 0 ? d.Ndegf * d.nhq : d.nhq;
+        {
+            // x_{n+k} = A_k x_n + C_k (mod 10^8) for the randm stream
+            const unsigned long long m = QG_LCG_M;
+            auto comp = [&](unsigned long long a1, unsigned long long c1, unsigned long long &a, unsigned long long &c) {
+                c = (a1 * c + c1) % m;   // apply (a1, c1) after (a, c)
+                a = (a1 * a) % m;
+            };
+            const int per = d.langevin_gauss ? 36 : 3;
+            unsigned long long ap = 1, cp = 0;
+            for (int q = 0; q < per; ++q) comp(QG_LCG_MULT, 1, ap, cp);
+            unsigned long long a = 1, c = 0;
+            const double gk = (d.langevin_gauss ? 2.0 : 24.0) * d.friction * 0.001986 * d.Temp0 / T.dvm;
+            for (int i = 0; i < N; ++i) {
+                lcg_a.push_back((unsigned)a); lcg_c.push_back((unsigned)c);
+                randva.push_back(d.thermostat == 1 ? sqrt(gk * d.mass[d.iac[i]]) : 0.0);
+                comp(ap, cp, a, c);
+            }
+            T.lcgA = a; T.lcgC = c;
+            rnd0.push_back((unsigned)(std::abs((long long)d.rand_state) % (long long)m));
+        }
+        // --- water polarisation shells (watpol, wat_shells)
+        T.wp0 = (int)(wp_state.size() / 3);
+        if (d.wpol_restr && d.nwat > 0 && d.nwpolr_shell > 0) {
+            if (d.nwpolr_shell > QG_MAXSHELL)
+                return fail(QGPU_E_UNSUPPORTED, "trajectory %d: %d polarisation shells (max %d)", t, d.nwpolr_shell,
+                            QG_MAXSHELL);
+            T.wpol = 1; T.nshell = d.nwpolr_shell; T.fkwpol = d.fkwpol; T.itdis_update = d.itdis_update;
+            for (int k = 0; k < d.nwpolr_shell; ++k) {
+                T.sh_rout[k] = d.wshell_rout[k]; T.sh_cstb[k] = d.wshell_cstb[k];
+                T.sh_acos_cstb[k] = acos(d.wshell_cstb[k]);
+                wp_state.push_back(d.wshell_theta_corr ? d.wshell_theta_corr[k] : 0.0);
+                wp_state.push_back(0.0); wp_state.push_back(0.0);
+            }
+            T.wp_rlayer = d.wshell_rout[d.nwpolr_shell - 1] - d.wshell_dr[d.nwpolr_shell - 1];
+            wp_traj.push_back(t); wp_scr0.push_back((int)wp_scr_n);
+            wp_scr_n += (28LL * d.nwat + 4) / 8 + 2;
+        }
         // --- types
         for (int a = 0; a < nt; ++a)
             for (int c = 0; c < 3; ++c) {
@@ -572,7 +641,8 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     std::vector<TrajState> tsh(ntraj);
     for (auto &q : tsh) {
         q.Temp = q.Tfree = q.Ekin = 0.f; q.shake_iters = 0;
-        q.tsf_solute = q.tsf_solvent = 1.f; q.wshiftf = 0.f; q.pad = 0;
+        q.tsf_solute = q.tsf_solvent = 1.f; q.wshiftf = 0.f;
+        q.rnd = rnd0[&q - tsh.data()]; q.nh_s1 = q.nh_s2 = 1.0;
     }
     if ((rc = upload(A, tsh, &ts))) return rc;
     S.tstate = ts;
@@ -654,6 +724,16 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     UP(shk_first, shk_first); UP(shk_i, shk_i); UP(shk_j, shk_j); UP(shk_traj, shk_traj); UP(shk_d2, shk_d2);
     S.nshk_mol = (int)shk_traj.size();
     if ((rc = alloc0(A, (size_t)ntraj * QG_NE, &S.eacc))) return rc;
+    UP(rs_i0, rs_i0); UP(rs_i1, rs_i1); UP(rs_ih, rs_ih); UP(rs_tc, rs_tc); UP(rs_traj, rs_traj); UP(rs_fk, rs_fk);
+    S.nrs = (int)rs_i0.size();
+    UP(aheavy, aheavy);
+    UP(randva, randva); UP(lcg_a, lcg_a); UP(lcg_c, lcg_c);
+    {
+        std::vector<float> rvf(randva.begin(), randva.end());
+        UP(rvf, randvaf);
+    }
+    if ((rc = alloc0(A, (size_t)ntraj * 2 * QG_MAXNH, &S.nh_state))) return rc;
+    if (!wp_state.empty()) { double *p_; if ((rc = upload(A, wp_state, &p_))) return rc; S.wp_state = p_; }
     for (char f : h->fused) h->all_fused = h->all_fused && f;
     h->can_fuse = h->all_fused;
     h->ek_u0 = ek_u0; h->ek_un = ek_un; h->ek_a0 = ek_a0; h->ek_an = ek_an;
@@ -688,6 +768,14 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         B.max_nqat = 0;
         for (int t = 0; t < ntraj; ++t) B.max_nqat = std::max(B.max_nqat, h->info[t].nqat);
         for (int t = 0; t < ntraj; ++t) B.any_atom |= h->info[t].any_atom;
+        B.nwp = (int)wp_traj.size();
+        if (B.nwp) {
+            int *p_;
+            if ((rc = upload(A, wp_traj, &p_))) return rc; B.wp_traj = p_;
+            if ((rc = upload(A, wp_scr0, &p_))) return rc; B.wp_scr0 = p_;
+            double *q_;
+            if ((rc = alloc0(A, (size_t)wp_scr_n, &q_))) return rc; B.wp_scr = q_;
+        }
     }
     if ((rc = alloc0(A, (size_t)ntraj * QG_REC, &h->ecur_d))) return rc;
     if ((rc = alloc0(A, 2, &h->zero_d))) return rc;
@@ -753,8 +841,10 @@ static void list_ops(qgpu_handle *h, LaunchCtx &L) {
 // fork from and join back into the handle's stream (also inside graph
 // capture).  The per-kernel profiler keeps them in one stream.
 static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, bool fp64_energy, EaccSel esel) {
+    const bool wpol = (terms & QGPU_TERMS_RESTRAINT) != 0;
     if (!(terms & QGPU_TERMS_NONBOND)) {
         launch_misc(h->S, h->B, L, terms, esel);
+        if (wpol) launch_watpol(h->S, h->B, L, esel);
         return;
     }
     if (L.prof || !h->ev_fork) {
@@ -763,6 +853,7 @@ static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, bool fp64_energy,
         launch_qw(h->S, h->B, L, esel);
         launch_qp(h->S, h->B, L, esel);
         launch_misc(h->S, h->B, L, terms, esel);
+        if (wpol) launch_watpol(h->S, h->B, L, esel);
         return;
     }
     cudaEventRecord(h->ev_fork, L.stream);
@@ -776,6 +867,7 @@ static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, bool fp64_energy,
     launch_qw(h->S, h->B, Ls[1], esel);
     launch_qp(h->S, h->B, Ls[2], esel);
     launch_misc(h->S, h->B, Ls[2], terms, esel);
+    if (wpol) launch_watpol(h->S, h->B, Ls[1], esel);
     for (int k = 0; k < QG_NSIDE; ++k) {
         cudaEventRecord(h->ev_join[k], h->side[k]);
         cudaStreamWaitEvent(L.stream, h->ev_join[k], 0);
@@ -820,7 +912,7 @@ static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every) {
         launch_update(h->S, h->B, L, 2);
         launch_wrec(h->S, h->B, L);
     }
-    launch_finalize(h->S, L, 1, h->rec_d, h->recctl_d, k, ene_every, h->rec_cap);
+    launch_finalize(h->S, L, FIN_TEMP | FIN_STEP | FIN_NH, h->rec_d, h->recctl_d, k, ene_every, h->rec_cap);
 }
 
 // ------------------------------------------------------------------ C-ABI
@@ -931,9 +1023,9 @@ int qgpu_forces(qgpu_handle *h, int32_t traj, int32_t terms, double *d, qgpu_ene
     ensure_double(h, L);
     CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
     if (terms & QGPU_TERMS_STEP_PRECISION)
-        force_ops(h, L, terms, false, EaccSel{EACC_FP32, h->zero_d, 0, 1});
+        force_ops(h, L, terms, false, EaccSel{EACC_FP32, h->recctl_d, 0, 1});
     else
-        force_ops(h, L, terms, true, EaccSel{EACC_FP64, h->zero_d, 0, 1});
+        force_ops(h, L, terms, true, EaccSel{EACC_FP64, h->recctl_d, 0, 1});
     launch_finalize(h->S, L, 0, h->ecur_d, h->zero_d, 0, 1, 1);
     std::vector<double> row(QG_REC);
     CK(cudaMemcpyAsync(row.data(), h->ecur_d + (size_t)traj * QG_REC, QG_REC * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1045,7 +1137,6 @@ void *qgpu_stream(qgpu_handle *h) { return h ? (void *)h->stream : nullptr; }
 int qgpu_profile(qgpu_handle *h, int32_t nsteps, char *names, double *ms, int64_t *counts, int32_t cap,
                  int32_t *nkernels) {
     if (!h || nsteps <= 0) return fail(QGPU_E_INVALID, "bad arguments");
-    if (h->any_wpol) return fail(QGPU_E_UNSUPPORTED, "water polarisation restraints are not run on the device");
     KernelProfiler P;
     LaunchCtx L{h->stream, &h->nlaunch, &P};
     if (!h->rec_d) {
@@ -1090,8 +1181,6 @@ int qgpu_profile(qgpu_handle *h, int32_t nsteps, char *names, double *ms, int64_
 // record buffer.  Errors surface at the next qgpu_sync / qgpu_run.
 int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every) {
     if (!h || nsteps < 0) return fail(QGPU_E_INVALID, "bad arguments");
-    if (h->any_wpol)
-        return fail(QGPU_E_UNSUPPORTED, "water polarisation restraints are not run on the device (set polarisation off)");
     if (ene_every <= 0) ene_every = 1 << 30;
     if (h->graph && h->graph_ene_every != ene_every) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     LaunchCtx L{h->stream, &h->nlaunch};
@@ -1104,7 +1193,8 @@ int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every) {
         CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
         CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
         temperature_init(h, L);
-        launch_finalize(h->S, L, 1, nullptr, h->zero_d, 0, 1, 0);
+        launch_finalize(h->S, L, FIN_TEMP | (h->nh_ready ? 0 : FIN_NH), nullptr, h->zero_d, 0, 1, 0);
+        h->nh_ready = 1;
         h->temp_init = 1;
     }
     int ctl[2] = {(int)h->step, (int)((h->step + ene_every - 1) / ene_every)};
@@ -1130,6 +1220,15 @@ int qgpu_sync(qgpu_handle *h) {
     return check_status(h);
 }
 
+int qgpu_set_step(qgpu_handle *h, int64_t istep) {
+    if (!h || istep < 0 || istep > 2000000000LL) return fail(QGPU_E_INVALID, "qgpu_set_step: bad arguments");
+    h->step = istep;
+    const int ctl = (int)istep;
+    CK(cudaMemcpyAsync(h->recctl_d, &ctl, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
 int qgpu_set_precision(qgpu_handle *h, int32_t mode) {
     if (!h || (mode != QGPU_PRECISION_MIXED && mode != QGPU_PRECISION_FP64))
         return fail(QGPU_E_INVALID, "qgpu_set_precision: bad arguments");
@@ -1152,8 +1251,6 @@ int qgpu_set_precision(qgpu_handle *h, int32_t mode) {
 
 int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink sink, void *user) {
     if (!h || nsteps < 0) return fail(QGPU_E_INVALID, "bad arguments");
-    if (h->any_wpol)
-        return fail(QGPU_E_UNSUPPORTED, "water polarisation restraints are not run on the device (set polarisation off)");
     if (ene_every <= 0) ene_every = 1 << 30;
     LaunchCtx L{h->stream, &h->nlaunch};
     const int NB = h->NBcycle;
@@ -1174,7 +1271,8 @@ int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink si
     if (!h->temp_init) {
         // temperature() before the first step (md_run, src/md.f90:6395-6398)
         temperature_init(h, L);
-        launch_finalize(h->S, L, 1, nullptr, h->zero_d, 0, 1, 0);
+        launch_finalize(h->S, L, FIN_TEMP | (h->nh_ready ? 0 : FIN_NH), nullptr, h->zero_d, 0, 1, 0);
+        h->nh_ready = 1;
         h->temp_init = 1;
     }
     auto flush = [&](long long upto_step) -> int {

@@ -16,6 +16,15 @@
 #define QG_LW 8                 // lanes that share one target in the pair kernels
 #define QG_NSIDE 3              // side streams of the concurrent force kernels
 #define QG_TREG 4               // target-group atoms held in registers by the any-atom scan test
+#define QG_MAXSHELL 8           // water polarisation shells per trajectory
+#define QG_MAXNH 16             // Nose-Hoover chain length
+#define QG_LCG_M 100000000ull   // randm modulus, multiplier (src/md.f90:17549-17551)
+#define QG_LCG_MULT 31415821ull
+// k_finalize flags
+#define FIN_TEMP 1              // temperature() and the Berendsen scales
+#define FIN_STEP 2              // a step has been taken: advance the Langevin random stream
+#define FIN_NH 4                // propagate the Nose-Hoover chain for the next step
+#define QG_WPBLK 512            // threads of the water polarisation kernel (one block per trajectory)
 #define S_GROUP_MASK 0xffffffffu
 #define QG_MAXS 4               // states handled by the engine (<= QGPU_MAX_STATES)
 #define QG_MAXQ 128             // Q atoms per trajectory (reference max_qat = 100)
@@ -33,7 +42,7 @@
 enum {
     EA_PP_EL = 0, EA_PP_VDW, EA_PW_EL, EA_PW_VDW, EA_WW_EL, EA_WW_VDW, EA_LRF,
     EA_P_BOND, EA_W_BOND, EA_P_ANG, EA_W_ANG, EA_P_TOR, EA_W_TOR, EA_P_IMP, EA_W_IMP,
-    EA_RST_FIX, EA_RST_SHELL, EA_RST_RAD,
+    EA_RST_FIX, EA_RST_SHELL, EA_RST_RAD, EA_RST_PROT, EA_RST_WPOL,
     EA_Q0  // then per state: QB QA QT QI QQ_EL QQ_VDW QP_EL QP_VDW QW_EL QW_VDW
 };
 enum { EQ_B = 0, EQ_A, EQ_T, EQ_I, EQ_QQ_EL, EQ_QQ_VDW, EQ_QP_EL, EQ_QP_VDW, EQ_QW_EL, EQ_QW_VDW, EQ_N };
@@ -91,6 +100,19 @@ struct TrajInfo {
     int qterm0[4], nqterm[4];   // Q bond/angle/torsion/improper ranges
     int ekin_blk0, ekin_nblk;   // Ekin partial slots of this trajectory (update blocks)
     int ff_type;
+    // water polarisation restraint (watpol): shells, layer bound, first of
+    // this trajectory's wpol state slots (-1 when off)
+    int wpol, nshell, wp0, freeze;
+    double fkwpol, wp_rlayer;
+    double sh_rout[QG_MAXSHELL], sh_cstb[QG_MAXSHELL], sh_acos_cstb[QG_MAXSHELL];
+    int itdis_update;
+    // thermostat (0 Berendsen, 1 Langevin, 2 Nose-Hoover) and integrator
+    // (0 leap-frog, 1 velocity-verlet); dv_mod = dt or dt/2 (md_run :6440-6460)
+    int thermostat, integrator, lgauss, nhc;
+    double dvm, lfric, kbT;
+    float dvmf, lfricf;
+    unsigned long long lcgA, lcgC;   // randm stream advance of one step (3N or 36N numbers)
+    double qnh[QG_MAXNH];
 };
 
 // Records the message for qgpu_last_error and returns code (qgpu_api.cu).
@@ -105,7 +127,8 @@ struct TrajState {
     float tsf_solute, tsf_solvent;  // Berendsen scales of the next step
     float wshiftf;                  // sqrt(Boltz*Tfree/fk_wsphere), restrain_solvent
     int shake_iters;
-    int pad;
+    unsigned rnd;                   // randm state before the next step's random forces
+    double nh_s1, nh_s2;            // Nose-Hoover velocity scales of the next step
 };
 
 struct DevSys {
@@ -197,6 +220,21 @@ struct DevSys {
     const double *shk_d2;
     const float2 *shk_d2hl;         // d0^2 as a float pair (hi, lo)
     int nshk_mol;
+    // sequence restraints (p_restrain): atom range [rs_i0, rs_i1], force
+    // constant, H flag, to_centre, trajectory
+    const int *rs_i0, *rs_i1, *rs_ih, *rs_tc, *rs_traj;
+    const double *rs_fk;
+    int nrs;
+    const uint8_t *aheavy;
+    // Langevin: random-force amplitude sqrt(gkT/winv) per atom; skip-ahead of
+    // the randm stream to each atom's first number: x_atom = (A x + C) mod m
+    const double *randva;
+    const float *randvaf;
+    const unsigned *lcg_a, *lcg_c;
+    double *nh_state;               // per trajectory: vnh[QG_MAXNH], xnh[QG_MAXNH]
+    // water polarisation state per (trajectory, shell): theta_corr, avtheta,
+    // avn_insh (slot = TrajInfo::wp0 + shell)
+    double *wp_state;               // 3 doubles per slot
     // energies and reductions
     unsigned long long *eacc;       // QG_NE per trajectory
     float *ekin_part;               // 4 per Ekin block
@@ -341,6 +379,34 @@ __device__ __forceinline__ void put_wrec(float4 *wr, const float4 (&h)[3], const
 #pragma unroll
     for (int k = 0; k < 3; ++k) wr[k] = wrec_part(h, l, k);
 }
+// randm (src/md.f90:17543-17577): irand <- (irand*31415821 + 1) mod 10^8,
+// r = 10*(irand/10)/10^8
+__device__ __forceinline__ unsigned lcg_next(unsigned x) {
+    return (unsigned)(((unsigned long long)x * QG_LCG_MULT + 1ull) % QG_LCG_M);
+}
+__device__ __forceinline__ double lcg_real(unsigned x) {
+    const double r = (double)(x / 10u) * 10.0 / 100000000.0;
+    return (r <= 0.0 || r > 1.0) ? 0.0 : r;
+}
+// Langevin random force of atom a for this step (newvel_lan, src/md.f90:
+// 6232-6247): uniform randva*(r - 1/2) or Gaussian gauss(0, randva), from the
+// atom's own position in the step's stream.
+template <typename R>
+__device__ __forceinline__ void langevin_force(const DevSys &S, const TrajInfo &T, unsigned base, int a, R (&f)[3]) {
+    unsigned x = (unsigned)(((unsigned long long)S.lcg_a[a] * base + S.lcg_c[a]) % QG_LCG_M);
+    const R amp = sizeof(R) == 8 ? R(S.randva[a]) : R(S.randvaf[a]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        if (!T.lgauss) {
+            x = lcg_next(x);
+            f[j] = amp * (R(lcg_real(x)) - R(0.5));
+        } else {
+            double s = 0.0;
+            for (int q = 0; q < 12; ++q) { x = lcg_next(x); s += lcg_real(x); }
+            f[j] = R(s - 6.0) * amp;
+        }
+    }
+}
 // exact FP64 squared distance in the reference's operation order (no FMA)
 __device__ __forceinline__ double dist2_exact(const double *x, int i, int j) {
     double a = __dsub_rn(x[3 * i], x[3 * j]);
@@ -372,6 +438,8 @@ struct BlockTables {
     const int *uatom, *ucon; const uint8_t *ublk_water; int nuatom;
     const int *qqblk_traj, *qqblk_s; int nqqblk;
     int max_nqat;                      // largest Q-atom count of a trajectory
+    // water polarisation: trajectories with the restraint, their scratch
+    const int *wp_traj, *wp_scr0; double *wp_scr; int nwp;
     int any_atom;                      // some trajectory uses the any-atom cut-off
 };
 
@@ -396,6 +464,7 @@ void launch_qp(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
 // On each launch the kernel evaluates in FP64 from x when eacc_on(e), else in
 // FP32 from the float coordinates.
 void launch_misc(const DevSys &S, const BlockTables &B, LaunchCtx &L, int terms, EaccSel e);
+void launch_watpol(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
 void launch_integrate(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_shake(const DevSys &S, const BlockTables &B, LaunchCtx &L, int traj_filter);
 void launch_update(const DevSys &S, const BlockTables &B, LaunchCtx &L, int mode);

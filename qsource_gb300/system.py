@@ -491,23 +491,23 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
     if integ is None:
         raise ValueError(f"unknown integrator {inp['integrator']}")
     tau_T = TIME_UNIT * inp["bath_coupling"]
-    friction = inp["langevin_friction"] if inp["langevin_friction"] is not None else 1.0 / tau_T
+    friction = inp.get("langevin_friction") if inp.get("langevin_friction") is not None else 1.0 / tau_T
     kbT = BOLTZ * inp["temperature"]
-    nhq = inp["nose_hoover_mass"] if inp["nose_hoover_mass"] is not None else kbT / (tau_T * tau_T)
+    nhq = inp.get("nose_hoover_mass") if inp.get("nose_hoover_mass") is not None else kbT / (tau_T * tau_T)
 
     # --- sequence restraints (0-based atoms)
-    rs = inp["sequence_restraints"]
+    rs = inp.get("sequence_restraints", [])
     rstseq_ij = np.array([(a - 1, b - 1) for a, b, _, _, _ in rs], dtype=np.int32).reshape(-1, 2)
     rstseq_fk = np.array([fk for _, _, fk, _, _ in rs], dtype=np.float64)
     rstseq_flags = np.array([(ih, tc) for _, _, _, ih, tc in rs], dtype=np.int32).reshape(-1, 2)
 
     # --- water polarisation shells (wat_sphere / wat_shells, src/md.f90:18106-18368)
     wpol = bool(inp["polarisation"]) and natom > nsol
-    fkwpol = inp["polarisation_force"] if inp["polarisation_force"] != -1.0 else 20.0
+    fkwpol = inp.get("polarisation_force", -1.0) if inp.get("polarisation_force", -1.0) != -1.0 else 20.0
     wshell = np.zeros((0, 4))
     if wpol:
         crgQtot = 0.0
-        if inp["charge_correction"]:
+        if inp.get("charge_correction", inp["polarisation"]):
             for iq in range(nq):
                 for s_ in range(S):
                     crgQtot += qcrg[iq, s_] / sq * lam[s_]
@@ -549,9 +549,9 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
         fk_wsphere=fk_wsphere, Dwmz=Dwmz, awmz=awmz, fk_pshell=inp["shell_force"], fk_fix=fk_fix,
         wpol_restr=wpol, fkwpol=fkwpol, wshell=wshell, itdis_update=100,
         rstseq_ij=rstseq_ij, rstseq_fk=rstseq_fk, rstseq_flags=rstseq_flags, heavy=heavy.astype(np.uint8),
-        excluded_freeze=int(inp["excluded_freeze"]),
-        thermostat=thermo, integrator=integ, friction=friction, langevin_gauss=int(inp["langevin_random"]),
-        rand_state=int(inp["random_seed"]), nhchains=int(inp["nhchains"]), nhq=nhq,
+        excluded_freeze=int(inp.get("excluded_freeze", False)),
+        thermostat=thermo, integrator=integ, friction=friction, langevin_gauss=int(inp.get("langevin_random", False)),
+        rand_state=int(inp["random_seed"]), nhchains=int(inp.get("nhchains", 10)), nhq=nhq,
         Rcpp=inp["Rcpp"], Rcww=inp["Rcww"], Rcpw=inp["Rcpw"], Rcq=inp["Rcq"], RcLRF=inp["RcLRF"],
         use_LRF=inp["lrf"], dt=TIME_UNIT * inp["stepsize"], Temp0=inp["temperature"],
         tau_T=tau_T, separate_scaling=separate_scaling, NBcycle=inp["non_bond"],

@@ -48,7 +48,9 @@ def systems(engine_lib):
     o = _oracle(g)
     o.maxwell(g.Tmaxw, int(g.seed))
     assert o.initial_shaking() == 0
+    o.stop_cm_translation()
     g.x, g.v = o.coords()
+    g.rand_state = o.rand_state()   # the random stream continues after maxwell
     out["golden"] = g
     return out
 
@@ -67,7 +69,7 @@ def energies_close(eg, eo, keys):
 
 E_KEYS = ["pp_el", "pp_vdw", "pw_el", "pw_vdw", "ww_el", "ww_vdw", "lrf", "qx_el", "qx_vdw", "q_bond",
           "q_angle", "q_torsion", "q_improper", "p_bond", "p_angle", "p_torsion", "p_improper", "rst_shell",
-          "rst_solvent_radial"]
+          "rst_solvent_radial", "rst_protein", "rst_water_pol"]
 EQ_KEYS = ["qq_el", "qq_vdw", "qp_el", "qp_vdw", "qw_el", "qw_vdw", "q_bond", "q_angle", "q_torsion", "q_improper"]
 
 
@@ -162,6 +164,38 @@ def test_short_md_matches_oracle(systems, ene_every):
     x, _ = e.coords(0)
     xo, _ = o.coords()
     assert np.abs(x - xo).max() < 1e-4
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("integrator", [0, 1])
+@pytest.mark.parametrize("thermostat", [0, 1, 2])
+def test_thermostats_match_oracle(systems, thermostat, integrator, precision):
+    """The reference's sphere test system (water polarisation, sequence,
+    shell and radial restraints; 0.1 fs steps) for 20 steps with each
+    thermostat (Berendsen, Langevin with the reference's random stream,
+    Nose-Hoover chain) and integrator (leap-frog, velocity-verlet), against
+    the FP64 oracle from the same start: recorded potential and kinetic
+    energies to 1e-4 relative, coordinates to 1e-4 A."""
+    import copy
+    from qsource_gb300.abi import QGPU_PRECISION_FP64
+    s = copy.copy(systems["golden"])
+    s.thermostat, s.integrator = thermostat, integrator
+    e = _engine(s)
+    if precision == "fp64":
+        e.set_precision(QGPU_PRECISION_FP64)
+    rows = e.run(20, ene_every=5)[0]
+    o = _oracle(s)
+    o.temperature()
+    rc, orows, _, _ = o.md_run(20)
+    assert rc == 0 and len(rows) == 4
+    for r in rows:
+        k = r[0]
+        for key in ("potential", "kinetic"):
+            g_, w_ = r[1][key], orows[k][key]
+            assert abs(g_ - w_) <= 1e-4 * max(1.0, abs(w_)), (k, key, g_, w_)
+    x, _ = e.coords(0)
+    xo, _ = o.coords()
+    assert abs(x - xo).max() < 1e-4
 
 
 @pytest.mark.parametrize("name", ["golden", "cfg1", "cfg4"])
