@@ -321,6 +321,33 @@ int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every);
 /* Waits for all queued work of the handle and returns its status. */
 int qgpu_sync(qgpu_handle *h);
 
+/* ---- energy files and free energies ------------------------------------- */
+/* Attaches a Q energy file (.en, the layout of put_ene, src/nrgy.f90:94-123,
+   with the header of src/md.f90:17011-17015; arrays = 1) to trajectory traj:
+   writes the header now and, during qgpu_run, one frame for every recorded
+   step > 0, as qdyn does every iene_cycle steps (md_run :6630-6633).  qfep
+   reads these files unchanged. */
+int qgpu_ene_open(qgpu_handle *h, int32_t traj, const char *path);
+int qgpu_ene_close(qgpu_handle *h, int32_t traj);
+/* Writes a whole energy file from host rows: nframes frames of nstates
+   qgpu_qenergy each, with noffd couplings per frame (offd_ij: 1-based state
+   pairs, offd_Hr: nframes*noffd (Hij, rkl)).  No device involved. */
+int qgpu_enefile_write(const char *path, int32_t nframes, int32_t nstates, const qgpu_qenergy *frames,
+                       int32_t noffd, const int32_t *offd_ij, const double *offd_Hr);
+/* Free-energy perturbation over a chain of lambda windows, accumulated on
+   the device from every recorded frame with a nonzero step (qfep Part 1,
+   src/qfep.f90:609-661): window w = trajectory chain[w]; per frame
+   dv = sum_s lambda_{w+-1,s} V_s - sum_s lambda_{w,s} V_s with V_s the state
+   total, and the sums of exp(-dv/kT) (FP64, in frame order) and of dv, dv^2,
+   dv^3 per direction; the first nskip frames of each window are skipped.
+   Starting clears the sums. */
+int qgpu_fep_start(qgpu_handle *h, int32_t nwin, const int32_t *chain, double kT, int32_t nskip);
+/* qfep's dgf(w) = -kT ln<exp(-dv_f/kT)> (w < nwin-1), dgr(w) (w > 0) and
+   dG(w) = dG(w-1) + (dgf(w-1) - dgr(w))/2, dG(0) = 0, each nwin long; stats
+   (may be NULL) gets 7 values per window: frames, mean / variance / skew of
+   dv forward, and of dv backward. */
+int qgpu_fep_result(qgpu_handle *h, double *dgf, double *dgr, double *dg, double *stats);
+
 /* ---- inspection (tests and tools) --------------------------------------- */
 /* Near charge-group pairs of the last list build, one row per unordered pair
    (g1 < g2), with g1,g2 0-based group indices.  Returns the count in *npairs;

@@ -60,6 +60,8 @@ def lib() -> C.CDLL:
         L.oracle_final_energy.argtypes = [vp, C.c_int, C.POINTER(Energies), C.POINTER(QEnergy)]
         L.oracle_rand_state.restype = C.c_int32
         L.oracle_rand_state.argtypes = [vp]
+        L.oracle_qfep_fep.restype = C.c_int
+        L.oracle_qfep_fep.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_int, C.c_double, C.c_int, vp, vp, vp, vp]
         L.oracle_sizeof_desc.restype = C.c_int
         _lib = L
     return _lib
@@ -163,3 +165,15 @@ class Oracle:
         rows = [E[k].as_dict() for k in range(nsteps)]
         qrows = [[EQ[k * self.S + s].as_dict() for s in range(self.S)] for k in range(nsteps)]
         return rc, rows, qrows, T
+
+
+def qfep_fep(paths, nstates: int, kT: float, nskip: int = 0):
+    """qfep Part 1 on energy files in lambda order: (dgf, dgr, dG, npts)."""
+    n = len(paths)
+    arr = (C.c_char_p * n)(*[p.encode() for p in paths])
+    dgf, dgr, dg = np.zeros(n), np.zeros(n), np.zeros(n)
+    npts = np.zeros(n, dtype=np.int32)
+    rc = lib().oracle_qfep_fep(n, arr, nstates, kT, nskip, _p(dgf), _p(dgr), _p(dg), _p(npts))
+    if rc:
+        raise RuntimeError("qfep: cannot read the energy files")
+    return dgf, dgr, dg, npts

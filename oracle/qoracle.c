@@ -19,6 +19,8 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <stdio.h>
+
 #include "qgpu.h"
 
 #define BOLTZ 0.001986          /* src/md.f90:54 */
@@ -1538,3 +1540,104 @@ int32_t oracle_rand_state(void *h) {
 int oracle_sizeof_desc(void) { return (int)sizeof(qgpu_system_desc); }
 int oracle_sizeof_energies(void) { return (int)sizeof(qgpu_energies); }
 int oracle_sizeof_qenergy(void) { return (int)sizeof(qgpu_qenergy); }
+
+/* ------------------------------------------------------------- qfep */
+/* One Fortran unformatted sequential record (4-byte length markers before
+   and after the payload).  Returns the payload length, -1 at end of file,
+   -2 on a malformed record; the payload is copied when it fits in cap. */
+static long read_record(FILE *f, unsigned char *buf, long cap) {
+    int32_t n, m;
+    if (fread(&n, 4, 1, f) != 1) return -1;
+    if (n < 0) return -2;
+    if (n <= cap) {
+        if (n && fread(buf, 1, (size_t)n, f) != (size_t)n) return -2;
+    } else if (fseek(f, n, SEEK_CUR) != 0) return -2;
+    if (fread(&m, 4, 1, f) != 1 || m != n) return -2;
+    return n;
+}
+
+/* qfep Part 1 (src/qfep.f90:247-661) on nfiles energy files in lambda order:
+   reads each file's header (canary 1337) and frames (get_ene, src/nrgy.f90:
+   147-188: nstates state records, then the OFFD record), takes lambda of the
+   window from the state records, V = EQ(s)%total, skips nskip points, and
+   forms dgf / dgr / dG exactly as qfep.  npts[nfiles] gets the frame counts.
+   Returns 0, or -1 when a file cannot be read. */
+int oracle_qfep_fep(int nfiles, const char **paths, int nstates, double rt, int nskip, double *dgf_out,
+                    double *dgr_out, double *dg_out, int *npts) {
+    if (nfiles < 1 || nstates < 1 || nstates > QGPU_MAX_STATES) return -1;
+    double **V = (double **)xmalloc((size_t)nfiles * sizeof(double *));
+    double *lam = (double *)xmalloc((size_t)nfiles * nstates * sizeof(double));
+    int rc = 0;
+    unsigned char buf[4096];
+    for (int fi = 0; fi < nfiles && !rc; ++fi) {
+        FILE *f = fopen(paths[fi], "rb");
+        if (!f) { rc = -1; break; }
+        long n = read_record(f, buf, sizeof buf);
+        int32_t canary = 0;
+        if (n >= 4) memcpy(&canary, buf, 4);
+        if (n < 4 || canary != 1337) { fclose(f); rc = -1; break; }
+        size_t cap = 64, np = 0;
+        V[fi] = (double *)xmalloc(cap * nstates * sizeof(double));
+        for (;;) {
+            double row[QGPU_MAX_STATES];
+            int s;
+            for (s = 0; s < nstates; ++s) {
+                n = read_record(f, buf, sizeof buf);
+                if (n < 4 + 8 * 15) break;
+                double lm, tot;
+                memcpy(&lm, buf + 4, 8);
+                memcpy(&tot, buf + 12, 8);
+                if (np == 0) lam[(size_t)fi * nstates + s] = lm;
+                row[s] = tot;
+            }
+            if (s < nstates) break;
+            if (read_record(f, buf, sizeof buf) < 0) break;   /* OFFD */
+            if (np == cap) { cap *= 2; V[fi] = (double *)realloc(V[fi], cap * nstates * sizeof(double)); }
+            memcpy(V[fi] + np * nstates, row, (size_t)nstates * sizeof(double));
+            ++np;
+        }
+        fclose(f);
+        npts[fi] = (int)np;
+    }
+    if (!rc) {
+        double *dgf = (double *)xmalloc((size_t)(nfiles + 2) * sizeof(double));
+        double *dgr = (double *)xmalloc((size_t)(nfiles + 2) * sizeof(double));
+        for (int fi = 0; fi + 1 < nfiles; ++fi) {
+            double sum = 0.0;
+            for (int p = nskip; p < npts[fi]; ++p) {
+                double v1 = 0.0, v2 = 0.0;
+                for (int s = 0; s < nstates; ++s) {
+                    v1 += lam[(size_t)fi * nstates + s] * V[fi][(size_t)p * nstates + s];
+                    v2 += lam[(size_t)(fi + 1) * nstates + s] * V[fi][(size_t)p * nstates + s];
+                }
+                sum += exp(-(v2 - v1) / rt);
+            }
+            sum /= (double)(npts[fi] - nskip);
+            dgf[fi] = -rt * log(sum);
+        }
+        for (int fi = nfiles - 1; fi >= 1; --fi) {
+            double sum = 0.0;
+            for (int p = nskip; p < npts[fi]; ++p) {
+                double v1 = 0.0, v2 = 0.0;
+                for (int s = 0; s < nstates; ++s) {
+                    v1 += lam[(size_t)fi * nstates + s] * V[fi][(size_t)p * nstates + s];
+                    v2 += lam[(size_t)(fi - 1) * nstates + s] * V[fi][(size_t)p * nstates + s];
+                }
+                sum += exp(-(v2 - v1) / rt);
+            }
+            sum /= (double)(npts[fi] - nskip);
+            dgr[fi] = -rt * log(sum);
+        }
+        double g = 0.0;
+        for (int fi = 0; fi < nfiles; ++fi) {
+            if (fi > 0) g = g + 0.5 * (dgf[fi - 1] - dgr[fi]);
+            if (dg_out) dg_out[fi] = g;
+            if (dgf_out) dgf_out[fi] = fi + 1 < nfiles ? dgf[fi] : 0.0;
+            if (dgr_out) dgr_out[fi] = fi > 0 ? dgr[fi] : 0.0;
+        }
+        free(dgf); free(dgr);
+    }
+    for (int fi = 0; fi < nfiles; ++fi) free(V[fi]);
+    free(V); free(lam);
+    return rc;
+}

@@ -122,6 +122,11 @@ EXPORTS = {
     "qgpu_enqueue": (_i32, [C.c_void_p, _i32, _i32]),
     "qgpu_set_precision": (_i32, [C.c_void_p, _i32]),
     "qgpu_set_step": (_i32, [C.c_void_p, C.c_int64]),
+    "qgpu_ene_open": (_i32, [C.c_void_p, _i32, C.c_char_p]),
+    "qgpu_ene_close": (_i32, [C.c_void_p, _i32]),
+    "qgpu_enefile_write": (_i32, [C.c_char_p, _i32, _i32, C.POINTER(QEnergy), _i32, _P, _P]),
+    "qgpu_fep_start": (_i32, [C.c_void_p, _i32, _P, _f64, _i32]),
+    "qgpu_fep_result": (_i32, [C.c_void_p, _P, _P, _P, _P]),
     "qgpu_sync": (_i32, [C.c_void_p]),
     "qgpu_get_group_pairs": (_i32, [C.c_void_p, _i32, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "qgpu_get_lrf": (_i32, [C.c_void_p, _i32, _P]),

@@ -418,16 +418,41 @@ __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_ba
     TrajState &TS = S.tstate[tr];
     unsigned long long *ea = S.eacc + (size_t)tr * QG_NE;
     int row = -1;
-    if (rec) {
-        const int step = rec_base[0] + k;
-        if (ene_every > 0 && step % ene_every == 0) {
-            row = step / ene_every - rec_base[1];
-            if (row >= rec_cap) row = -1;
-        }
+    const int fstep = rec_base[0] + k;
+    const bool rec_step = rec && ene_every > 0 && fstep % ene_every == 0;
+    if (rec_step) {
+        row = fstep / ene_every - rec_base[1];
+        if (row >= rec_cap) row = -1;
     }
+    // FEP frames: qdyn writes energy frames at nonzero recorded steps only
+    const bool fep = rec_step && T.fep_on && fstep > 0;
     for (int s = lane; s < QG_NE; s += 32) {
-        if (row >= 0) v[s] = fx_get(ea[s]);
+        if (row >= 0 || fep) v[s] = fx_get(ea[s]);
         ea[s] = 0ull;
+    }
+    __syncwarp();
+    if (fep && lane == 0 && ++TS.fep_n > T.fep_nskip) {
+        // qfep Part 1 (src/qfep.f90:609-655): dv = veff2 - veff1 in qfep's
+        // operation order, sums in frame order; V_s = EQ(s)%total
+        double *A = S.fep_acc + (size_t)tr * QG_NFEP;
+        double ve = 0.0, vf = 0.0, vr = 0.0;
+        for (int s = 0; s < T.nstates; ++s) {
+            const double *w = v + EA_Q0 + EQ_N * s;
+            const double Vs = w[EQ_B] + w[EQ_A] + w[EQ_T] + w[EQ_I] + (w[EQ_QQ_EL] + w[EQ_QP_EL] + w[EQ_QW_EL]) +
+                              (w[EQ_QQ_VDW] + w[EQ_QP_VDW] + w[EQ_QW_VDW]) + 0.0;
+            ve += T.lambda[s] * Vs;
+            vf += T.fep_lamf[s] * Vs;
+            vr += T.fep_lamr[s] * Vs;
+        }
+        A[0] += 1.0;
+        if (T.fep_has_f) {
+            const double dv = vf - ve;
+            A[1] += exp(-dv / T.fep_kT); A[2] += dv; A[3] += dv * dv; A[4] += dv * dv * dv;
+        }
+        if (T.fep_has_r) {
+            const double dv = vr - ve;
+            A[5] += exp(-dv / T.fep_kT); A[6] += dv; A[7] += dv * dv; A[8] += dv * dv * dv;
+        }
     }
     if (do_temp) {
         float e4[4];

@@ -87,6 +87,10 @@ struct qgpu_handle {
     int NBcycle = 10;
     int lists_built = 0, temp_init = 0, any_shake = 0, any_wpol = 0;
     int nh_ready = 0;          // Nose-Hoover scales of the next step are formed
+    std::vector<FILE *> ene_files;   // attached .en files per trajectory (or null)
+    std::vector<int> fep_chain;      // trajectories of the FEP window chain
+    double fep_kT = 0;
+    int fep_nskip = 0;
     std::vector<char> fused;   // per trajectory: SHAKE fused into the update kernel
     bool all_fused = true;
     bool can_fuse = true;      // every trajectory's constraints allow the fused update
@@ -733,6 +737,8 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         UP(rvf, randvaf);
     }
     if ((rc = alloc0(A, (size_t)ntraj * 2 * QG_MAXNH, &S.nh_state))) return rc;
+    if ((rc = alloc0(A, (size_t)ntraj * QG_NFEP, &S.fep_acc))) return rc;
+    h->ene_files.assign(ntraj, nullptr);
     if (!wp_state.empty()) { double *p_; if ((rc = upload(A, wp_state, &p_))) return rc; S.wp_state = p_; }
     for (char f : h->fused) h->all_fused = h->all_fused && f;
     h->can_fuse = h->all_fused;
@@ -946,6 +952,8 @@ int qgpu_destroy(qgpu_handle *h) {
         if (h->ev_join[k]) cudaEventDestroy(h->ev_join[k]);
     }
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    for (FILE *f : h->ene_files)
+        if (f) fclose(f);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return 0;
@@ -1249,6 +1257,91 @@ int qgpu_set_precision(qgpu_handle *h, int32_t mode) {
     return 0;
 }
 
+int qgpu_ene_open(qgpu_handle *h, int32_t traj, const char *path) {
+    if (!h || traj < 0 || traj >= h->ntraj || !path) return fail(QGPU_E_INVALID, "qgpu_ene_open: bad arguments");
+    if (h->ene_files[traj]) fclose(h->ene_files[traj]);
+    h->ene_files[traj] = fopen(path, "wb");
+    if (!h->ene_files[traj]) return fail(QGPU_E_INVALID, "qgpu_ene_open: cannot open %s", path);
+    if (qgpu_ene_write_header(h->ene_files[traj], "5.06 (qsource_gb300)"))
+        return fail(QGPU_E_INVALID, "qgpu_ene_open: cannot write %s", path);
+    return 0;
+}
+
+int qgpu_ene_close(qgpu_handle *h, int32_t traj) {
+    if (!h || traj < 0 || traj >= h->ntraj) return fail(QGPU_E_INVALID, "qgpu_ene_close: bad arguments");
+    if (h->ene_files[traj] && fclose(h->ene_files[traj]) != 0) {
+        h->ene_files[traj] = nullptr;
+        return fail(QGPU_E_INVALID, "qgpu_ene_close: write failed");
+    }
+    h->ene_files[traj] = nullptr;
+    return 0;
+}
+
+int qgpu_fep_start(qgpu_handle *h, int32_t nwin, const int32_t *chain, double kT, int32_t nskip) {
+    if (!h || nwin < 2 || !chain || !(kT > 0) || nskip < 0) return fail(QGPU_E_INVALID, "qgpu_fep_start: bad arguments");
+    std::vector<char> seen(h->ntraj, 0);
+    for (int w = 0; w < nwin; ++w) {
+        const int t = chain[w];
+        if (t < 0 || t >= h->ntraj || seen[t]) return fail(QGPU_E_INVALID, "qgpu_fep_start: bad chain entry %d", w);
+        if (h->nstates[t] != h->nstates[chain[0]])
+            return fail(QGPU_E_INVALID, "qgpu_fep_start: windows with different state counts");
+        seen[t] = 1;
+    }
+    LaunchCtx L{h->stream, &h->nlaunch};
+    CK(cudaStreamSynchronize(h->stream));
+    for (int t = 0; t < h->ntraj; ++t) h->info[t].fep_on = 0;
+    for (int w = 0; w < nwin; ++w) {
+        TrajInfo &T = h->info[chain[w]];
+        T.fep_on = 1; T.fep_kT = kT; T.fep_nskip = nskip;
+        T.fep_has_f = w + 1 < nwin; T.fep_has_r = w > 0;
+        for (int s = 0; s < QG_MAXS; ++s) {
+            T.fep_lamf[s] = T.fep_has_f ? h->info[chain[w + 1]].lambda[s] : 0.0;
+            T.fep_lamr[s] = T.fep_has_r ? h->info[chain[w - 1]].lambda[s] : 0.0;
+        }
+    }
+    CK(cudaMemcpy((void *)h->S.traj, h->info.data(), h->info.size() * sizeof(TrajInfo), cudaMemcpyHostToDevice));
+    CK(cudaMemset(h->S.fep_acc, 0, (size_t)h->ntraj * QG_NFEP * sizeof(double)));
+    for (int t = 0; t < h->ntraj; ++t) CK(cudaMemset(&h->S.tstate[t].fep_n, 0, sizeof(int)));
+    h->fep_chain.assign(chain, chain + nwin);
+    h->fep_kT = kT; h->fep_nskip = nskip;
+    (void)L;
+    return 0;
+}
+
+int qgpu_fep_result(qgpu_handle *h, double *dgf, double *dgr, double *dg, double *stats) {
+    if (!h || h->fep_chain.empty()) return fail(QGPU_E_INVALID, "qgpu_fep_result: no FEP chain (qgpu_fep_start)");
+    CK(cudaStreamSynchronize(h->stream));
+    const int nw = (int)h->fep_chain.size();
+    std::vector<double> A((size_t)h->ntraj * QG_NFEP);
+    CK(cudaMemcpy(A.data(), h->S.fep_acc, A.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    const double rt = h->fep_kT;
+    std::vector<double> f(nw, 0.0), r(nw, 0.0), g(nw, 0.0);
+    for (int w = 0; w < nw; ++w) {
+        const double *a = A.data() + (size_t)h->fep_chain[w] * QG_NFEP;
+        const double n = a[0];
+        if (w + 1 < nw) f[w] = n > 0 ? -rt * log(a[1] / n) : 0.0;
+        if (w > 0) r[w] = n > 0 ? -rt * log(a[5] / n) : 0.0;
+        if (stats) {
+            double *o = stats + (size_t)w * 7;
+            o[0] = n;
+            for (int d = 0; d < 2; ++d) {
+                const double s1 = a[2 + 4 * d], s2 = a[3 + 4 * d], s3 = a[4 + 4 * d];
+                const double mu = n > 0 ? s1 / n : 0.0, var = n > 0 ? s2 / n - mu * mu : 0.0;
+                const double m3 = n > 0 ? s3 / n - 3.0 * mu * s2 / n + 2.0 * mu * mu * mu : 0.0;
+                o[1 + 3 * d] = mu;
+                o[2 + 3 * d] = var;
+                o[3 + 3 * d] = var > 0 ? m3 / pow(var, 1.5) : 0.0;
+            }
+        }
+    }
+    // dG(1) = 0, dG(i) = dG(i-1) + (dgf(i-1) - dgr(i))/2 (src/qfep.f90:658-661)
+    for (int w = 1; w < nw; ++w) g[w] = g[w - 1] + 0.5 * (f[w - 1] - r[w]);
+    if (dgf) memcpy(dgf, f.data(), nw * sizeof(double));
+    if (dgr) memcpy(dgr, r.data(), nw * sizeof(double));
+    if (dg) memcpy(dg, g.data(), nw * sizeof(double));
+    return 0;
+}
+
 int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink sink, void *user) {
     if (!h || nsteps < 0) return fail(QGPU_E_INVALID, "bad arguments");
     if (ene_every <= 0) ene_every = 1 << 30;
@@ -1275,20 +1368,31 @@ int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink si
         h->nh_ready = 1;
         h->temp_init = 1;
     }
+    bool any_file = false;
+    for (FILE *f : h->ene_files) any_file = any_file || f;
     auto flush = [&](long long upto_step) -> int {
         long long rows = (upto_step + ene_every - 1) / ene_every - row0;
         if (rows > h->rec_cap) rows = h->rec_cap;
-        if (rows > 0 && sink) {
+        if (rows > 0 && (sink || any_file)) {
             std::vector<double> buf((size_t)rows * h->ntraj * QG_REC);
             CK(cudaMemcpyAsync(buf.data(), h->rec_d, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
             CK(cudaStreamSynchronize(h->stream));
             for (long long r = 0; r < rows; ++r)
                 for (int t = 0; t < h->ntraj; ++t) {
                     const double *R = buf.data() + ((size_t)r * h->ntraj + t) * QG_REC;
+                    const long long step = (row0 + r) * (long long)ene_every;
                     qgpu_energies E;
                     qgpu_qenergy EQ[QG_MAXS];
                     unpack_row(R, h->nstates[t], &E, EQ);
-                    sink(user, t, (int32_t)((row0 + r) * (long long)ene_every), EQ, h->nstates[t], &E);
+                    if (sink) sink(user, t, (int32_t)step, EQ, h->nstates[t], &E);
+                    // qdyn writes energy frames at nonzero steps (md_run :6630)
+                    if (h->ene_files[t] && step > 0) {
+                        const int nod = (int)h->offd_states[t].size() / 2;
+                        std::vector<int32_t> ij(2 * nod);
+                        for (int q = 0; q < 2 * nod; ++q) ij[q] = h->offd_states[t][q] + 1;
+                        if (qgpu_ene_write_frame(h->ene_files[t], h->nstates[t], EQ, nod, ij.data(), R + QG_REC_OD))
+                            return fail(QGPU_E_INVALID, "writing the energy file of trajectory %d failed", t);
+                    }
                 }
         }
         return 0;

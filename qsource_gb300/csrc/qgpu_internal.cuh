@@ -8,6 +8,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdio.h>
 
 #include "qgpu.h"
 
@@ -113,10 +114,21 @@ struct TrajInfo {
     float dvmf, lfricf;
     unsigned long long lcgA, lcgC;   // randm stream advance of one step (3N or 36N numbers)
     double qnh[QG_MAXNH];
+    // free-energy perturbation (qfep Part 1) on the device: this trajectory's
+    // window has neighbours (has_f / has_r) with lambdas lamf / lamr
+    int fep_on, fep_has_f, fep_has_r, fep_nskip;
+    double fep_kT, fep_lamf[QG_MAXS], fep_lamr[QG_MAXS];
 };
+#define QG_NFEP 9                // FEP accumulators per trajectory (see k_finalize)
 
 // Records the message for qgpu_last_error and returns code (qgpu_api.cu).
 int qgpu_fail(int code, const char *fmt, ...);
+// Q energy-file records (qgpu_ene.cu): header, and one frame (nstates
+// state records + the OFFD record; offd_ij 1-based state pairs, offd_Hr
+// (Hij, rkl) per coupling)
+int qgpu_ene_write_header(FILE *f, const char *version);
+int qgpu_ene_write_frame(FILE *f, int32_t nstates, const qgpu_qenergy *EQ, int32_t noffd, const int32_t *offd_ij,
+                         const double *offd_Hr);
 
 // Per-trajectory dynamic state (device).
 // Per-trajectory dynamic state (device), in FP32: it is updated every step by
@@ -128,6 +140,7 @@ struct TrajState {
     float wshiftf;                  // sqrt(Boltz*Tfree/fk_wsphere), restrain_solvent
     int shake_iters;
     unsigned rnd;                   // randm state before the next step's random forces
+    int fep_n;                      // recorded frames seen by the FEP accumulation
     double nh_s1, nh_s2;            // Nose-Hoover velocity scales of the next step
 };
 
@@ -232,6 +245,7 @@ struct DevSys {
     const float *randvaf;
     const unsigned *lcg_a, *lcg_c;
     double *nh_state;               // per trajectory: vnh[QG_MAXNH], xnh[QG_MAXNH]
+    double *fep_acc;                // per trajectory: QG_NFEP sums (k_finalize)
     // water polarisation state per (trajectory, shell): theta_corr, avtheta,
     // avn_insh (slot = TrajInfo::wp0 + shell)
     double *wp_state;               // 3 doubles per slot

@@ -126,6 +126,31 @@ class Engine:
         self._check(self.lib.qgpu_get_lrf(self.h, traj, abi.ptr(out)))
         return out
 
+    # ---------------------------------------------------- energy files, FEP
+    def ene_open(self, traj: int, path: str):
+        """Attach a Q energy file to trajectory traj (qgpu_ene_open)."""
+        self._check(self.lib.qgpu_ene_open(self.h, traj, path.encode()))
+
+    def ene_close(self, traj: int):
+        self._check(self.lib.qgpu_ene_close(self.h, traj))
+
+    def fep_start(self, chain, kT: float, nskip: int = 0):
+        """Start the device FEP sums over the window chain (trajectories in
+        lambda order, qgpu_fep_start)."""
+        c = np.ascontiguousarray(chain, dtype=np.int32)
+        self._fep_n = len(c)
+        self._check(self.lib.qgpu_fep_start(self.h, len(c), abi.ptr(c), kT, nskip))
+
+    def fep_result(self):
+        """(dgf, dgr, dG, stats[nwin, 7]) of qfep Part 1 from the device sums."""
+        n = self._fep_n
+        dgf, dgr, dg, st = np.zeros(n), np.zeros(n), np.zeros(n), np.zeros((n, 7))
+        self._check(self.lib.qgpu_fep_result(self.h, abi.ptr(dgf), abi.ptr(dgr), abi.ptr(dg), abi.ptr(st)))
+        return dgf, dgr, dg, st
+
+    def set_step(self, istep: int):
+        self._check(self.lib.qgpu_set_step(self.h, istep))
+
     def set_precision(self, mode: int):
         """QGPU_PRECISION_MIXED (default) or QGPU_PRECISION_FP64 for the MD
         step (see qgpu_set_precision)."""

@@ -287,3 +287,27 @@ def test_invalid_descriptor_is_rejected(systems):
     with pytest.raises(QgpuError) as ei:
         _engine(s)
     assert ei.value.code == 6
+
+
+def test_fep_sums_match_qfep_on_engine_files(engine_lib, tmp_path):
+    """Five lambda windows of the 18 A droplet run as one batch with energy
+    files attached: the device's streaming FEP sums give qfep's dgf / dgr / dG
+    of the files the engine wrote (the oracle's qfep restatement), to 1e-9."""
+    from oracle.oracle import qfep_fep
+    from qsource_gb300 import synth
+    nw, kT, nskip = 5, 0.596163, 2
+    systems = [synth.config(1, window=w, lambdas=(1 - w / (nw - 1), w / (nw - 1))) for w in range(nw)]
+    e = _engine(systems)
+    paths = [str(tmp_path / f"w{w}.en") for w in range(nw)]
+    for w, p in enumerate(paths):
+        e.ene_open(w, p)
+    e.fep_start(list(range(nw)), kT, nskip)
+    e.run(200, ene_every=10)
+    for w in range(nw):
+        e.ene_close(w)
+    dgf, dgr, dg, st = e.fep_result()
+    of, orr, og, npts = qfep_fep(paths, 2, kT, nskip)
+    assert list(npts) == [19] * nw            # frames at steps 10 ... 190
+    assert np.all(st[:, 0] == 19 - nskip)
+    for a, b in ((dgf, of), (dgr, orr), (dg, og)):
+        assert np.allclose(a, b, rtol=1e-9, atol=1e-9), (a, b)
