@@ -228,24 +228,26 @@ def config(cfg: int, replica: int = 0, window: int = 0, nwindows: int = 21, **kw
     raise ValueError(f"unknown config {cfg}")
 
 
-def lambda_batch_member(i: int, nwindows: int = 21, replicas: int = 11, **kw) -> System:
-    """Trajectory i of lambda_batch(nwindows, replicas), built alone."""
+def lambda_batch_member(i: int, nwindows: int = 21, replicas: int = 11, rank: int = 0, **kw) -> System:
+    """Trajectory i of lambda_batch(nwindows, replicas, rank), built alone.
+    Different ranks (GPUs of a multi-GPU run) get the same recipe with their
+    own seeds: independent replicas."""
     if not 0 <= i < nwindows + replicas:
         raise IndexError(i)
     if i < nwindows:
         la = 1.0 - i / (nwindows - 1) if nwindows > 1 else 0.5
-        return config(1, window=i, lambdas=(la, 1.0 - la), **kw)
+        return config(1, window=i, replica=rank, lambdas=(la, 1.0 - la), **kw)
     r = i - nwindows
     R = (20.0, 25.0, 30.0)[r % 3]
     qa = neutral_charges(np.random.default_rng(1000), 8, 0.4)
     ns = 500 + int(round(1500 * r / max(replicas - 1, 1)))
     ns = min(ns, {20.0: 800, 25.0: 1500, 30.0: 2000}[R])
     kw.setdefault("any_atom", True)
-    return synthetic(R, ns, 8, np.stack([qa, np.zeros(8)], 1), (0.5, 0.5), 3000 + 100 * r, **kw)
+    return synthetic(R, ns, 8, np.stack([qa, np.zeros(8)], 1), (0.5, 0.5), 3000 + 100 * r + 50000 * rank, **kw)
 
 
-def lambda_batch(nwindows: int = 21, replicas: int = 11, **kw) -> list[System]:
+def lambda_batch(nwindows: int = 21, replicas: int = 11, rank: int = 0, **kw) -> list[System]:
     """The lambda-window batch: nwindows windows (lambda_A from 1 to 0) of the
     18 A droplet plus uneven replicas (spheres of 20/25/30 A with 500- to
     2,000-atom solutes, 8 Q atoms at lambda 0.5)."""
-    return [lambda_batch_member(i, nwindows, replicas, **kw) for i in range(nwindows + replicas)]
+    return [lambda_batch_member(i, nwindows, replicas, rank, **kw) for i in range(nwindows + replicas)]
