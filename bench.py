@@ -203,6 +203,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=20, help="timed oracle steps of the CPU baseline")
     ap.add_argument("--ref-max-steps", type=int, default=100, help="cap on the reference arm's timed steps")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
+    ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                     help="MD step precision (qgpu_set_precision): double-float master / FP64 master")
     args = ap.parse_args()
@@ -243,11 +244,12 @@ def main():
     from qsource_gb300.engine import Engine
 
     # weak scaling: every rank runs its own batch of independent replicas
-    # (same shapes, own seeds); no data-path collective
+    # (same recipe, own seeds); no data-path collective
     systems = synth.lambda_batch(rank=rank)
     ntraj = len(systems)
     natoms = sum(s.natom for s in systems)
     eng = Engine(systems)
+    tuning = eng.autotune() if not args.no_tune else None
     if args.precision == "fp64":
         from qsource_gb300.abi import QGPU_PRECISION_FP64
         eng.set_precision(QGPU_PRECISION_FP64)
@@ -331,7 +333,9 @@ def main():
                    "timed": f"{nblk} blocks of {NB} steps, each one CUDA-graph replay",
                    "l2": "flushed before every timed 10-step block (256 MB write on the engine stream)",
                    "parallelism": "replicas" if world > 1 else "single GPU, one handle",
-                   "precision": args.precision},
+                   "precision": args.precision,
+                   "launch_shapes": ({"lanes_water": tuning[0], "min_blocks_water": tuning[1],
+                                      "lanes_solute": tuning[2], "lanes_qw": tuning[3]} if tuning else "default")},
         "e2e": {"value": round(e2e, 3), "unit": "ns/day", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "how": "per 10-step block: qgpu_set_coords_all of x,v of all 32 trajectories from pinned memory, "
                        "qgpu_run with an energy sink, qgpu_get_coords_all (host wall clock)"},

@@ -122,6 +122,8 @@ EXPORTS = {
     "qgpu_enqueue": (_i32, [C.c_void_p, _i32, _i32]),
     "qgpu_set_precision": (_i32, [C.c_void_p, _i32]),
     "qgpu_set_step": (_i32, [C.c_void_p, C.c_int64]),
+    "qgpu_autotune": (_i32, [C.c_void_p, _P]),
+    "qgpu_set_tuning": (_i32, [C.c_void_p, _P]),
     "qgpu_ene_open": (_i32, [C.c_void_p, _i32, C.c_char_p]),
     "qgpu_ene_close": (_i32, [C.c_void_p, _i32]),
     "qgpu_enefile_write": (_i32, [C.c_char_p, _i32, _i32, C.POINTER(QEnergy), _i32, _P, _P]),

@@ -67,13 +67,13 @@ struct EAcc<true> {
 // --------------------------------------------------------------- waters
 // nonbond_ww_spc (src/md.f90:15021-15119), the water side of nonbond_pw
 // (13282-13365) and lrf_taylor for the three water atoms.
-// QG_LW lanes share one water: lane l takes neighbours l, l+QG_LW, ...; the
+// LW lanes share one water: lane l takes neighbours l, l+LW, ...; the
 // lanes' partial gradients are summed by an xor butterfly (fixed order).
-template <bool EACC>
-__global__ void __launch_bounds__(QG_BLOCK) k_nb_water(DevSys S, const int *wgrp, int lrf) {
+template <bool EACC, int LW, int MINB>
+__global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int *wgrp, int lrf) {
     __shared__ long long red[5][QG_BLOCK / 32];
-    const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / QG_LW;
-    const int lane = threadIdx.x & (QG_LW - 1);
+    const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LW;
+    const int lane = threadIdx.x & (LW - 1);
     const int w = wgrp[idx];
     const int traj = traj_of_entry(S, w, true);
     const TrajInfo &T = S.traj[traj];
@@ -142,8 +142,8 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_water(DevSys S, const int *wgrp
         };
         // two neighbours per iteration keep two sets of loads in flight
         int k = lane;
-        for (; k + QG_LW < nw; k += 2 * QG_LW) {
-            const int b0 = lst[k], b1 = lst[k + QG_LW];
+        for (; k + LW < nw; k += 2 * LW) {
+            const int b0 = lst[k], b1 = lst[k + LW];
             const float4 p0 = S.wrec[b0], p1 = S.wrec[b0 + 1], p2 = S.wrec[b0 + 2];
             const float4 s0 = S.wrec[b1], s1 = S.wrec[b1 + 1], s2 = S.wrec[b1 + 2];
             ww(b0, p0, p1, p2);
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_water(DevSys S, const int *wgrp
             ww(b0, S.wrec[b0], S.wrec[b0 + 1], S.wrec[b0 + 2]);
         }
         // solute neighbours (the water side of nonbond_pw)
-        for (int kk = nw + lane; kk < n; kk += QG_LW) {
+        for (int kk = nw + lane; kk < n; kk += LW) {
             const int g = lst[kk];
             for (int q = S.g_start[g]; q < S.g_start[g + 1]; ++q) {
                 const int b = S.g_atoms[q];
@@ -189,10 +189,10 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_water(DevSys S, const int *wgrp
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int o = QG_LW / 2; o > 0; o >>= 1) {
-            gx[a] += __shfl_xor_sync(S_GROUP_MASK, gx[a], o, QG_LW);
-            gy[a] += __shfl_xor_sync(S_GROUP_MASK, gy[a], o, QG_LW);
-            gz[a] += __shfl_xor_sync(S_GROUP_MASK, gz[a], o, QG_LW);
+        for (int o = LW / 2; o > 0; o >>= 1) {
+            gx[a] += __shfl_xor_sync(S_GROUP_MASK, gx[a], o, LW);
+            gy[a] += __shfl_xor_sync(S_GROUP_MASK, gy[a], o, LW);
+            gz[a] += __shfl_xor_sync(S_GROUP_MASK, gz[a], o, LW);
         }
     {
         if (valid && lane == 0) {
@@ -239,11 +239,11 @@ __device__ __forceinline__ PairFlags pair_flags(const DevSys &S, int i, int j) {
 
 // nonbond_pp (src/md.f90:13069-13155) and the solute side of nonbond_pw, plus
 // lrf_taylor, for one non-Q solute atom.
-template <bool EACC>
+template <bool EACC, int LW>
 __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *satom, int lrf) {
     __shared__ long long red[5][QG_BLOCK / 32];
-    const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / QG_LW;
-    const int lane = threadIdx.x & (QG_LW - 1);
+    const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LW;
+    const int lane = threadIdx.x & (LW - 1);
     const int i = satom[idx];
     const int traj = traj_of_entry(S, i, false);
     const TrajInfo &T = S.traj[traj];
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
             if (f.excl) return;
             pair(j, f.p14 ? 3 : ljc(S, T, ti, S.atype[j]), epp_el, epp_vdw);
         };
-        for (int kk = S.g_start[g] + lane; kk < S.g_start[g + 1]; kk += QG_LW) {
+        for (int kk = S.g_start[g] + lane; kk < S.g_start[g + 1]; kk += LW) {
             const int j = S.g_atoms[kk];
             if (j == i || S.aq[j] >= 0) continue;
             pp(j);
@@ -298,13 +298,13 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         epp_el.flush(); epp_vdw.flush();
         const int n = S.nb_count[g], nw = S.nb_nw[g];
         const int *lst = S.nb_list + (size_t)g * S.nb_cap;
-        for (int k = lane; k < nw; k += QG_LW) {
+        for (int k = lane; k < nw; k += LW) {
             const int b0 = lst[k];
 #pragma unroll
             for (int b = 0; b < 3; ++b) pair(b0 + b, ljc(S, T, ti, S.atype[b0 + b]), epw_el, epw_vdw);
             epw_el.flush(); epw_vdw.flush();
         }
-        for (int k = nw + lane; k < n; k += QG_LW) {
+        for (int k = nw + lane; k < n; k += LW) {
             const int h = lst[k];
             for (int kk = S.g_start[h]; kk < S.g_start[h + 1]; ++kk) {
                 const int j = S.g_atoms[kk];
@@ -315,10 +315,10 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         }
     }
 #pragma unroll
-    for (int o = QG_LW / 2; o > 0; o >>= 1) {
-        gx += __shfl_xor_sync(S_GROUP_MASK, gx, o, QG_LW);
-        gy += __shfl_xor_sync(S_GROUP_MASK, gy, o, QG_LW);
-        gz += __shfl_xor_sync(S_GROUP_MASK, gz, o, QG_LW);
+    for (int o = LW / 2; o > 0; o >>= 1) {
+        gx += __shfl_xor_sync(S_GROUP_MASK, gx, o, LW);
+        gy += __shfl_xor_sync(S_GROUP_MASK, gy, o, LW);
+        gz += __shfl_xor_sync(S_GROUP_MASK, gz, o, LW);
     }
     {
         if (valid && lane == 0) {
@@ -616,22 +616,53 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
     q_energies(S, traj, NS, eel, evdw, acc, EQ_QP_EL, EQ_QP_VDW, sh);
 }
 
+// Launch shapes (the autotuner's choice, BlockTables::tune): lanes per water
+// LW (4/8/16/32) and the register bound of the water kernel (minimum
+// resident blocks 1 or 6); lanes per solute atom (4/8/16).  The FP64-energy
+// variants (drop-in calls) use 8 lanes.
+template <int LW, int MINB>
+static void water_fp32(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf) {
+    k_nb_water<false, LW, MINB><<<B.nwgrp * LW / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+}
 void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
     if (!B.nwgrp) return;
-    if (fp64_energy) { prof_begin(L, "k_nb_water"); k_nb_water<true><<<B.nwgrp * QG_LW / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf); prof_end(L); }
-    else { prof_begin(L, "k_nb_water"); k_nb_water<false><<<B.nwgrp * QG_LW / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf); prof_end(L); }
+    prof_begin(L, "k_nb_water");
+    if (fp64_energy) {
+        k_nb_water<true, 8, 1><<<B.nwgrp * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    } else {
+        const bool m6 = B.tune.minb_water == 6;
+        switch (B.tune.lw_water) {
+        case 4: m6 ? water_fp32<4, 6>(S, B, L, lrf) : water_fp32<4, 1>(S, B, L, lrf); break;
+        case 16: m6 ? water_fp32<16, 6>(S, B, L, lrf) : water_fp32<16, 1>(S, B, L, lrf); break;
+        case 32: m6 ? water_fp32<32, 6>(S, B, L, lrf) : water_fp32<32, 1>(S, B, L, lrf); break;
+        default: m6 ? water_fp32<8, 6>(S, B, L, lrf) : water_fp32<8, 1>(S, B, L, lrf); break;
+        }
+    }
+    prof_end(L);
     (*L.nlaunch)++;
 }
 void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
     if (!B.nsatom) return;
-    if (fp64_energy) { prof_begin(L, "k_nb_solute"); k_nb_solute<true><<<B.nsatom * QG_LW / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); prof_end(L); }
-    else { prof_begin(L, "k_nb_solute"); k_nb_solute<false><<<B.nsatom * QG_LW / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); prof_end(L); }
+    prof_begin(L, "k_nb_solute");
+    if (fp64_energy) {
+        k_nb_solute<true, 8><<<B.nsatom * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf);
+    } else {
+        switch (B.tune.lw_solute) {
+        case 4: k_nb_solute<false, 4><<<B.nsatom * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
+        case 16: k_nb_solute<false, 16><<<B.nsatom * 16 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
+        default: k_nb_solute<false, 8><<<B.nsatom * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
+        }
+    }
+    prof_end(L);
     (*L.nlaunch)++;
 }
 // Lanes per item of the Q loops: one per water while each trajectory has
 // few Q atoms (the per-item set-up then dominates), more for larger Q sets;
 // the qp items (solute atoms) are fewer and always take four.
-static int qw_lanes(const BlockTables &B) { return B.max_nqat <= 16 ? 1 : (B.max_nqat <= 48 ? 2 : 4); }
+static int qw_lanes(const BlockTables &B) {
+    if (B.tune.lg_qw == 1 || B.tune.lg_qw == 2 || B.tune.lg_qw == 4) return B.tune.lg_qw;
+    return B.max_nqat <= 16 ? 1 : (B.max_nqat <= 48 ? 2 : 4);
+}
 
 void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
     if (!B.nwgrp) return;

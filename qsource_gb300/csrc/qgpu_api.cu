@@ -1228,6 +1228,118 @@ int qgpu_sync(qgpu_handle *h) {
     return check_status(h);
 }
 
+// ------------------------------------------------------------ autotuner
+// Chooses the launch shapes of the pair kernels by timing every variant on
+// this handle's own lists (CUDA events on the handle's stream, median of 7
+// launches after 2 warm-up launches).  The choice is kept per device and
+// system size for the later handles of the process.
+static std::map<std::string, Tuning> g_tune_cache;
+
+static std::string tune_key(const qgpu_handle *h) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp p{};
+    cudaGetDeviceProperties(&p, dev);
+    char buf[256];
+    snprintf(buf, sizeof buf, "%s/%d/%d/%d/%d/%d", p.name, p.multiProcessorCount, h->ntraj, h->S.natom, h->B.nwgrp,
+             h->B.nsatom);
+    return buf;
+}
+
+static int time_variant(qgpu_handle *h, LaunchCtx &L, void (*launch)(qgpu_handle *, LaunchCtx &), float *ms) {
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    for (int w = 0; w < 2; ++w) launch(h, L);
+    std::vector<float> t;
+    for (int r = 0; r < 7; ++r) {
+        CK(cudaEventRecord(a, h->stream));
+        launch(h, L);
+        CK(cudaEventRecord(b, h->stream));
+        CK(cudaEventSynchronize(b));
+        float x = 0.f;
+        CK(cudaEventElapsedTime(&x, a, b));
+        t.push_back(x);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    std::sort(t.begin(), t.end());
+    *ms = t[t.size() / 2];
+    return 0;
+}
+
+static void tune_water(qgpu_handle *h, LaunchCtx &L) { launch_nb_water(h->S, h->B, L, 1, false); }
+static void tune_solute(qgpu_handle *h, LaunchCtx &L) { launch_nb_solute(h->S, h->B, L, 1, false); }
+static void tune_qw(qgpu_handle *h, LaunchCtx &L) {
+    launch_qw(h->S, h->B, L, EaccSel{EACC_FP32, h->zero_d, 0, 1});
+}
+
+int qgpu_set_tuning(qgpu_handle *h, const int32_t *tuning) {
+    if (!h || !tuning) return fail(QGPU_E_INVALID, "qgpu_set_tuning: bad arguments");
+    const int lw = tuning[0], mb = tuning[1], ls = tuning[2], lq = tuning[3];
+    if ((lw != 4 && lw != 8 && lw != 16 && lw != 32) || (mb != 1 && mb != 6) || (ls != 4 && ls != 8 && ls != 16) ||
+        (lq != 0 && lq != 1 && lq != 2 && lq != 4))
+        return fail(QGPU_E_INVALID, "qgpu_set_tuning: unsupported shape");
+    CK(cudaStreamSynchronize(h->stream));
+    h->B.tune.lw_water = lw; h->B.tune.minb_water = mb; h->B.tune.lw_solute = ls; h->B.tune.lg_qw = lq;
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    return 0;
+}
+
+int qgpu_autotune(qgpu_handle *h, int32_t *tuning) {
+    if (!h) return fail(QGPU_E_INVALID, "null handle");
+    const std::string key = tune_key(h);
+    auto it = g_tune_cache.find(key);
+    if (it == g_tune_cache.end()) {
+        if (!h->lists_built)
+            if (int rc = qgpu_build_lists(h)) return rc;
+        LaunchCtx L{h->stream, &h->nlaunch};
+        ensure_double(h, L);
+        CK(cudaStreamSynchronize(h->stream));
+        Tuning best = h->B.tune;
+        float t, tb = 1e30f;
+        if (h->B.nwgrp) {
+            for (int lw : {4, 8, 16, 32})
+                for (int mb : {1, 6}) {
+                    h->B.tune.lw_water = lw; h->B.tune.minb_water = mb;
+                    if (int rc = time_variant(h, L, tune_water, &t)) return rc;
+                    if (t < tb) { tb = t; best.lw_water = lw; best.minb_water = mb; }
+                }
+            h->B.tune.lw_water = best.lw_water; h->B.tune.minb_water = best.minb_water;
+            tb = 1e30f;
+            for (int lq : {1, 2, 4}) {
+                h->B.tune.lg_qw = lq;
+                if (int rc = time_variant(h, L, tune_qw, &t)) return rc;
+                if (t < tb) { tb = t; best.lg_qw = lq; }
+            }
+            h->B.tune.lg_qw = best.lg_qw;
+        }
+        if (h->B.nsatom) {
+            tb = 1e30f;
+            for (int ls : {4, 8, 16}) {
+                h->B.tune.lw_solute = ls;
+                if (int rc = time_variant(h, L, tune_solute, &t)) return rc;
+                if (t < tb) { tb = t; best.lw_solute = ls; }
+            }
+        }
+        h->B.tune = best;
+        // the timing launches added into the gradient and energies
+        CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
+        CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (int rc = check_status(h)) return rc;
+        g_tune_cache[key] = best;
+    } else {
+        h->B.tune = it->second;
+    }
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    if (tuning) {
+        tuning[0] = h->B.tune.lw_water; tuning[1] = h->B.tune.minb_water;
+        tuning[2] = h->B.tune.lw_solute; tuning[3] = h->B.tune.lg_qw;
+    }
+    return 0;
+}
+
 int qgpu_set_step(qgpu_handle *h, int64_t istep) {
     if (!h || istep < 0 || istep > 2000000000LL) return fail(QGPU_E_INVALID, "qgpu_set_step: bad arguments");
     h->step = istep;

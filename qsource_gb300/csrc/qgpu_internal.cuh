@@ -439,7 +439,13 @@ struct LaunchCtx {
 // bracket one launch with CUDA events on L.stream (no-ops without a profiler)
 void prof_begin(LaunchCtx &L, const char *name);
 void prof_end(LaunchCtx &L);
+// Launch-shape choices of the pair kernels (the autotuner's parameters);
+// 0 = default.
+struct Tuning {
+    int lw_water = 8, minb_water = 1, lw_solute = 8, lg_qw = 0;
+};
 struct BlockTables {
+    Tuning tune;
     // per-item lists (padded per trajectory to QG_BLOCK)
     const int *wgrp; int nwgrp;        // water groups
     const int *satom; int nsatom;      // solute atoms (all, incl. Q/excluded -> skipped in kernels)

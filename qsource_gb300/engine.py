@@ -148,6 +148,18 @@ class Engine:
         self._check(self.lib.qgpu_fep_result(self.h, abi.ptr(dgf), abi.ptr(dgr), abi.ptr(dg), abi.ptr(st)))
         return dgf, dgr, dg, st
 
+    def autotune(self) -> list:
+        """Time the pair-kernel launch shapes and keep the fastest
+        (qgpu_autotune); returns [lanes_water, min_blocks_water,
+        lanes_solute, lanes_qw]."""
+        t = np.zeros(4, dtype=np.int32)
+        self._check(self.lib.qgpu_autotune(self.h, abi.ptr(t)))
+        return [int(v) for v in t]
+
+    def set_tuning(self, tuning):
+        t = np.ascontiguousarray(tuning, dtype=np.int32)
+        self._check(self.lib.qgpu_set_tuning(self.h, abi.ptr(t)))
+
     def set_step(self, istep: int):
         self._check(self.lib.qgpu_set_step(self.h, istep))
 

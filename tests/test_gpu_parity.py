@@ -311,3 +311,35 @@ def test_fep_sums_match_qfep_on_engine_files(engine_lib, tmp_path):
     assert np.all(st[:, 0] == 19 - nskip)
     for a, b in ((dgf, of), (dgr, orr), (dg, og)):
         assert np.allclose(a, b, rtol=1e-9, atol=1e-9), (a, b)
+
+
+@pytest.mark.parametrize("shape", [[4, 1, 4, 1], [8, 6, 8, 2], [16, 1, 16, 4], [32, 6, 8, 0]])
+def test_every_launch_shape_matches_oracle(systems, shape):
+    """Each launch shape the autotuner may pick (lanes per water / register
+    bound / lanes per solute atom / lanes per Q-water item) gives the oracle's
+    forces and energies with the step-precision tolerances."""
+    from qsource_gb300.abi import QGPU_TERMS_STEP_PRECISION
+    s = systems["cfg2"]
+    e = _engine(s)
+    e.set_tuning(shape)
+    e.make_pair_lists()
+    d, E, EQ = e.pot_energy(0, terms=0x1F | QGPU_TERMS_STEP_PRECISION)
+    o = _oracle(s)
+    o.make_pair_lists()
+    do, Eo, EQo = o.pot_energy(terms=0x1F)
+    assert rel_rms(d, do) <= FORCE_RTOL
+    pair = ["pp_el", "pp_vdw", "pw_el", "pw_vdw", "ww_el", "ww_vdw"]
+    assert all(abs(E[k] - Eo[k]) <= max(ENERGY_REL * abs(Eo[k]), STEP_PAIR_ENERGY_ABS) for k in pair)
+    for s_ in range(s.nstates):
+        assert not energies_close(EQ[s_], EQo[s_], EQ_KEYS)
+
+
+def test_autotune_picks_a_valid_shape_and_is_cached(systems):
+    s = systems["cfg1"]
+    a = _engine(s)
+    t1 = a.autotune()
+    assert t1[0] in (4, 8, 16, 32) and t1[1] in (1, 6) and t1[2] in (4, 8, 16) and t1[3] in (1, 2, 4)
+    b = _engine(s)
+    assert b.autotune() == t1            # same device and size: the cached choice
+    rows = b.run(10, ene_every=5)[0]
+    assert len(rows) == 2 and all(np.isfinite(r[1]["potential"]) for r in rows)
