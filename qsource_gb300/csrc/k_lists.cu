@@ -106,7 +106,7 @@ __device__ __forceinline__ float d2hi(const float4 a, const float4 b) {
 // expansion (lrf_update, src/md.f90:5896-5981), accumulated as 24 symmetric
 // FP32 sums per chunk.
 template <bool ANY>
-__global__ void __launch_bounds__(QG_BLOCK) k_scan(DevSys S, const int *blk_t0, const int *blk_tn, const int *blk_traj,
+__global__ void __launch_bounds__(QG_BLOCK, QG_SCAN_MINB) k_scan(DevSys S, const int *blk_t0, const int *blk_tn, const int *blk_traj,
                                                    const int *blk_chunk) {
     __shared__ float4 s_hi[QG_TILE_G], s_lo[QG_TILE_G];
     __shared__ int s_meta[QG_TILE_G], s_rep[QG_TILE_G], s_aoff[QG_TILE_G + 1];

@@ -82,15 +82,16 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
     float elrf = 0.f;
     const bool valid = w >= 0 && !S.g_excl[w];
     int a0 = 0;
-    float4 ah[3] = {}, al[3] = {};
     float gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0}, gz[3] = {0, 0, 0};
+    // the water's own packed record: O hi/lo and the H offsets
+    float4 r0 = make_float4(0, 0, 0, 0), r1 = r0, r2 = r0;
     if (valid) {
         a0 = S.g_atoms[S.g_start[w]];
         int ta[3];
         double qd[3] = {0, 0, 0};
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            ah[a] = S.pos[a0 + a]; al[a] = S.poslo[a0 + a]; ta[a] = S.atype[a0 + a];
+            ta[a] = S.atype[a0 + a];
             if (EACC) qd[a] = S.crg_d[a0 + a];
         }
         const int n = S.nb_count[w], nw = S.nb_nw[w];
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
         float qq[9];
 #pragma unroll
         for (int c = 0; c < 9; ++c) qq[c] = T.wwqq[c];
-        const float4 r0 = S.wrec[a0], r1 = S.wrec[a0 + 1], r2 = S.wrec[a0 + 2];
+        r0 = S.wrec[a0]; r1 = S.wrec[a0 + 1]; r2 = S.wrec[a0 + 2];
         const float3 da[3] = {make_float3(0.f, 0.f, 0.f), make_float3(r0.w, r1.w, r2.x), make_float3(r2.y, r2.z, r2.w)};
         auto ww = [&](int b0, const float4 q0, const float4 q1, const float4 q2) {
             const float3 dO = make_float3((q0.x - r0.x) + (q1.x - r1.x), (q0.y - r0.y) + (q1.y - r1.y),
@@ -153,7 +154,9 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
             const int b0 = lst[k];
             ww(b0, S.wrec[b0], S.wrec[b0 + 1], S.wrec[b0 + 2]);
         }
-        // solute neighbours (the water side of nonbond_pw)
+        // solute neighbours (the water side of nonbond_pw).  d = dpos(O, j) - d_a
+        // is the exact negative of the solute side's dpos(j, O) + d_a.
+        const float4 oh = make_float4(r0.x, r0.y, r0.z, 0.f), ol = make_float4(r1.x, r1.y, r1.z, 0.f);
         for (int kk = nw + lane; kk < n; kk += LW) {
             const int g = lst[kk];
             for (int q = S.g_start[g]; q < S.g_start[g + 1]; ++q) {
@@ -161,15 +164,16 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
                 if (S.aq[b] >= 0) continue;
                 const float4 bh = S.pos[b], bl = S.poslo[b];
                 const int tb = S.atype[b];
+                const float3 dO = dpos(oh, ol, bh, bl);
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
                     const int c = ljc(S, T, ta[a], tb);
                     const float A = S.avdw[ta[a] * 3 + c - 1] * S.avdw[tb * 3 + c - 1];
                     const float B = S.bvdw[ta[a] * 3 + c - 1] * S.bvdw[tb * 3 + c - 1];
-                    const float3 d = dpos(ah[a], al[a], bh, bl);
+                    const float3 d = make_float3(dO.x - da[a].x, dO.y - da[a].y, dO.z - da[a].z);
                     const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
                     const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
-                    const float Vel = ah[a].w * bh.w * ri, Va = A * r6 * r6, Vb = B * r6;
+                    const float Vel = T.chg_solv[a] * bh.w * ri, Va = A * r6 * r6, Vb = B * r6;
                     const float dv = ri2 * (-Vel - 12.f * Va + 6.f * Vb);
                     double eld = 0.0, evd = 0.0;
                     if (EACC) {
@@ -201,8 +205,13 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
                 const float4 c = S.g_centf[w];
 #pragma unroll
                 for (int a = 0; a < 3; ++a)
-                    elrf += lrf_atom(ph, (c.x - ah[a].x) - al[a].x, (c.y - ah[a].y) - al[a].y,
-                                     (c.z - ah[a].z) - al[a].z, ah[a].w, gx[a], gy[a], gz[a]);
+                {
+                    // centre - x_a = ((c - O_hi) - O_lo) - d_a
+                    const float3 da = a == 0 ? make_float3(0.f, 0.f, 0.f)
+                                             : (a == 1 ? make_float3(r0.w, r1.w, r2.x) : make_float3(r2.y, r2.z, r2.w));
+                    elrf += lrf_atom(ph, ((c.x - r0.x) - r1.x) - da.x, ((c.y - r0.y) - r1.y) - da.y,
+                                     ((c.z - r0.z) - r1.z) - da.z, T.chg_solv[a], gx[a], gy[a], gz[a]);
+                }
             }
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
@@ -298,10 +307,42 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         epp_el.flush(); epp_vdw.flush();
         const int n = S.nb_count[g], nw = S.nb_nw[g];
         const int *lst = S.nb_list + (size_t)g * S.nb_cap;
+        // water neighbours from their packed records: d = dpos(i, O) + d_k;
+        // LJ products and charge products of the three water atoms formed once
+        // (all waters of a trajectory share types and charges)
+        float Aw[3], Bw[3], qw[3];
+        int cw[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int tw = S.atype[T.atom0 + T.nat_solute + k];
+            cw[k] = ljc(S, T, ti, tw);
+            Aw[k] = S.avdw[ti * 3 + cw[k] - 1] * S.avdw[tw * 3 + cw[k] - 1];
+            Bw[k] = S.bvdw[ti * 3 + cw[k] - 1] * S.bvdw[tw * 3 + cw[k] - 1];
+            qw[k] = ih.w * T.chg_solv[k];
+        }
         for (int k = lane; k < nw; k += LW) {
             const int b0 = lst[k];
+            const float4 w0 = S.wrec[b0], w1 = S.wrec[b0 + 1], w2 = S.wrec[b0 + 2];
+            const float3 dO = dpos(ih, il, make_float4(w0.x, w0.y, w0.z, 0.f), make_float4(w1.x, w1.y, w1.z, 0.f));
+            const float3 dk[3] = {make_float3(0.f, 0.f, 0.f), make_float3(w0.w, w1.w, w2.x), make_float3(w2.y, w2.z, w2.w)};
 #pragma unroll
-            for (int b = 0; b < 3; ++b) pair(b0 + b, ljc(S, T, ti, S.atype[b0 + b]), epw_el, epw_vdw);
+            for (int b = 0; b < 3; ++b) {
+                const float3 d = make_float3(dO.x + dk[b].x, dO.y + dk[b].y, dO.z + dk[b].z);
+                const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+                const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
+                const float Vel = qw[b] * ri, Va = Aw[b] * r6 * r6, Vb = Bw[b] * r6;
+                const float dv = ri2 * (-Vel - 12.f * Va + 6.f * Vb);
+                double eld = 0.0, evd = 0.0;
+                if (EACC) {
+                    const int j = b0 + b, tj = S.atype[j];
+                    const double rid = rinv_d(S.x, i, j), r6d = rid * rid * rid * rid * rid * rid;
+                    eld = qi * S.crg_d[j] * rid;
+                    evd = S.avdw_d[ti * 3 + cw[b] - 1] * S.avdw_d[tj * 3 + cw[b] - 1] * r6d * r6d -
+                          S.bvdw_d[ti * 3 + cw[b] - 1] * S.bvdw_d[tj * 3 + cw[b] - 1] * r6d;
+                }
+                epw_el.term(Vel, eld); epw_vdw.term(Va - Vb, evd);
+                gx -= dv * d.x; gy -= dv * d.y; gz -= dv * d.z;
+            }
             epw_el.flush(); epw_vdw.flush();
         }
         for (int k = nw + lane; k < n; k += LW) {

@@ -31,7 +31,12 @@
 #define QG_MAXQ 128             // Q atoms per trajectory (reference max_qat = 100)
 #define QG_TILE_G 64            // source groups per scan tile
 #define QG_TILE_A 256           // source atoms per scan tile
-#define QG_TPC 4                // scan tiles per source chunk (one k_scan block)
+#ifndef QG_TPC
+#define QG_TPC 1                // scan tiles per source chunk (one k_scan block)
+#endif
+#ifndef QG_SCAN_MINB
+#define QG_SCAN_MINB 6          // k_scan register bound (minimum resident blocks)
+#endif
 #define QG_CAPC (QG_TPC * QG_TILE_G)  // near groups a chunk can hold (= groups in a chunk)
 #define QG_MAXOD 6              // off-diagonal couplings recorded per trajectory
 #define QG_NLRF 24              // LRF accumulators per group (see k_scan)
