@@ -335,7 +335,8 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU, one handle",
                    "precision": args.precision,
                    "launch_shapes": ({"lanes_water": tuning[0], "min_blocks_water": tuning[1],
-                                      "lanes_solute": tuning[2], "lanes_qw": tuning[3]} if tuning else "default")},
+                                      "lanes_solute": tuning[2], "lanes_qw": tuning[3], "unroll_water": tuning[4]}
+                                     if tuning else "default")},
         "e2e": {"value": round(e2e, 3), "unit": "ns/day", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "how": "per 10-step block: qgpu_set_coords_all of x,v of all 32 trajectories from pinned memory, "
                        "qgpu_run with an energy sink, qgpu_get_coords_all (host wall clock)"},

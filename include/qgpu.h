@@ -295,12 +295,12 @@ int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every,
              qgpu_ene_sink sink, void *user);
 
 /* Autotuner.  Times every launch shape of the pair kernels on this handle's
-   own lists -- lanes per target water (4/8/16/32) and the water kernel's
-   register bound (1 or 6 resident blocks), lanes per Q-water item (1/2/4),
-   lanes per solute atom (4/8/16) -- keeps the fastest, and caches the choice
-   per device and system size for later handles of the process.
-   tuning[4] (may be NULL) receives {lanes_water, min_blocks_water,
-   lanes_solute, lanes_qw}.  Results are deterministic for a given choice;
+   own lists -- lanes per target water (4/8/16), the water kernel's register
+   bound (1 or 6 resident blocks) and neighbours per loop iteration (1/2/4),
+   lanes per Q-water item (1/2/4), lanes per solute atom (4/8/16) -- keeps the
+   fastest, and caches the choice per device and system size for later
+   handles of the process.  tuning[5] (may be NULL) receives {lanes_water,
+   min_blocks_water, lanes_solute, lanes_qw, unroll_water}.  Results are deterministic for a given choice;
    different choices sum the float pair terms in a different order. */
 int qgpu_autotune(qgpu_handle *h, int32_t *tuning);
 /* Pins a choice (the values qgpu_autotune reports; lanes_qw 0 = by Q count). */

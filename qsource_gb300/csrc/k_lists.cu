@@ -98,6 +98,30 @@ __device__ __forceinline__ float d2hi(const float4 a, const float4 b) {
     return dx * dx + dy * dy + dz * dz;
 }
 
+// lrf_update (src/md.f90:5896-5981) of one source atom p (charge in .w) at
+// the target centre c: the 24 symmetric FP32 sums of the multipole expansion.
+__device__ __forceinline__ void lrf_acc(float (&acc)[QG_NLRF], const float4 p, float cx, float cy, float cz) {
+    const float dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float ri = rsqrtf(r2), ri2 = ri * ri;
+    const float f0 = p.w * ri * ri2;
+    const float f1 = 3.f * f0 * ri2;
+    const float f2 = -f1 * ri2;
+    acc[0] += p.w * ri;
+    acc[1] += f0;
+    acc[2] += f0 * dx; acc[3] += f0 * dy; acc[4] += f0 * dz;
+    const float ux = f1 * dx, uy = f1 * dy, uz = f1 * dz;
+    acc[5] += ux; acc[6] += uy; acc[7] += uz;
+    acc[8] += ux * dx; acc[9] += uy * dy; acc[10] += uz * dz;
+    acc[11] += ux * dy; acc[12] += ux * dz; acc[13] += uy * dz;
+    const float vx = f2 * dx, vy = f2 * dy, vz = f2 * dz;
+    const float wxx = vx * dx, wyy = vy * dy, wzz = vz * dz, wxy = vx * dy;
+    acc[14] += wxx * dx; acc[15] += wyy * dy; acc[16] += wzz * dz;
+    acc[17] += wxx * dy; acc[18] += wxx * dz; acc[19] += wyy * dx;
+    acc[20] += wzz * dx; acc[21] += wyy * dz; acc[22] += wzz * dy;
+    acc[23] += wxy * dz;
+}
+
 // Phase 1 of the scan: one thread per target charge group, one block per
 // (128 targets, source chunk of QG_TPC shared-memory tiles of the same
 // trajectory).  Near groups (inside the pp/pw/ww cut-off) go to the target's
@@ -230,28 +254,20 @@ __global__ void __launch_bounds__(QG_BLOCK, QG_SCAN_MINB) k_scan(DevSys S, const
                     if (kind_s) nbseg[cntw++] = s_rep[s];
                     else nbseg[QG_CAPC - 1 - cnts++] = g;
                 } else if (far_lrf) {
-                    for (int k = s_aoff[s]; k < s_aoff[s + 1]; ++k) {
-                        const float4 p = s_atom[k];
-                        if (p.w == 0.f) continue;
-                        const float dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
-                        const float r2 = dx * dx + dy * dy + dz * dz;
-                        const float ri = rsqrtf(r2), ri2 = ri * ri;
-                        const float f0 = p.w * ri * ri2;
-                        const float f1 = 3.f * f0 * ri2;
-                        const float f2 = -f1 * ri2;
-                        acc[0] += p.w * ri;
-                        acc[1] += f0;
-                        acc[2] += f0 * dx; acc[3] += f0 * dy; acc[4] += f0 * dz;
-                        const float ux = f1 * dx, uy = f1 * dy, uz = f1 * dz;
-                        acc[5] += ux; acc[6] += uy; acc[7] += uz;
-                        acc[8] += ux * dx; acc[9] += uy * dy; acc[10] += uz * dz;
-                        acc[11] += ux * dy; acc[12] += ux * dz; acc[13] += uy * dz;
-                        const float vx = f2 * dx, vy = f2 * dy, vz = f2 * dz;
-                        const float wxx = vx * dx, wyy = vy * dy, wzz = vz * dz, wxy = vx * dy;
-                        acc[14] += wxx * dx; acc[15] += wyy * dy; acc[16] += wzz * dz;
-                        acc[17] += wxx * dy; acc[18] += wxx * dz; acc[19] += wyy * dx;
-                        acc[20] += wzz * dx; acc[21] += wyy * dz; acc[22] += wzz * dy;
-                        acc[23] += wxy * dz;
+                    const int k0 = s_aoff[s];
+                    if (kind_s) {
+                        // a water: its three (charged) atoms unrolled, so their
+                        // independent rsqrt chains overlap; same order of sums
+                        const float4 p0 = s_atom[k0], p1 = s_atom[k0 + 1], p2 = s_atom[k0 + 2];
+                        lrf_acc(acc, p0, cx, cy, cz);
+                        lrf_acc(acc, p1, cx, cy, cz);
+                        lrf_acc(acc, p2, cx, cy, cz);
+                    } else {
+                        for (int k = k0; k < s_aoff[s + 1]; ++k) {
+                            const float4 p = s_atom[k];
+                            if (p.w == 0.f) continue;
+                            lrf_acc(acc, p, cx, cy, cz);
+                        }
                     }
                 }
             }

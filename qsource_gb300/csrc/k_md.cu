@@ -226,9 +226,14 @@ __device__ __forceinline__ void hilo_add(float &h, float &l, float d) {
 // v = (x - xx)/dt (md_run :6596-6597), the hi/lo position update and the
 // Ekin partials.  No FP64 arithmetic except the x/v refresh (want_x).
 // ekin_only: temperature before the first step (Ekin of the current velf).
+__device__ void finalize_traj(const DevSys &S, int tr, int lane, double *v, int do_temp, double *rec,
+                              const int *rec_base, int k, int ene_every, int rec_cap);
+
+// fin: FIN_* flags of the step's end (temperature, thermostat state, energy
+// record), run by the last block of each trajectory (0: none)
 __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom, const int *ucon,
                                                       const uint8_t *ublk_water, EaccSel esel, int nbcycle,
-                                                      int ekin_only) {
+                                                      int ekin_only, int fin, double *rec, int rec_cap) {
     __shared__ float4 s_h[QG_UBLK], s_l[QG_UBLK];
     __shared__ float s_D[3][QG_UBLK];
     __shared__ float s_w[QG_UBLK];
@@ -356,7 +361,19 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
         float s = 0.f;
         for (int w = 0; w < QG_UBLK / 32; ++w) s += red[t][w];
         S.ekin_part[(size_t)blockIdx.x * 4 + t] = s;
+        __threadfence();
     }
+    if (!fin) return;
+    // the last block of the trajectory to finish runs the step's end
+    __shared__ int s_last;
+    __shared__ double s_fin[QG_NE];
+    __syncthreads();
+    if (t == 0) s_last = atomicAdd(S.fin_cnt + tr, 1) == T.ekin_nblk - 1;
+    __syncthreads();
+    if (!s_last || t >= 32) return;
+    __threadfence();
+    finalize_traj(S, tr, t, s_fin, fin, rec, esel.recctl, esel.k, esel.ene_every, rec_cap);
+    if (t == 0) S.fin_cnt[tr] = 0;
 }
 
 // x = origin + (hi + lo), v = velf: the FP64 view of the float master.
@@ -409,11 +426,14 @@ __device__ double nh_prop(const TrajInfo &T, double *vnh, double *xnh, double Te
     return sc;
 }
 
-// do_temp: FIN_* flags
-__global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_base, int k, int ene_every, int rec_cap) {
-    __shared__ double v[QG_NE];
-    const int tr = blockIdx.x;
-    const int lane = threadIdx.x;
+// The end of a step for trajectory tr, run by one warp (lane = 0..31; v a
+// shared QG_NE scratch): energy accumulators into the record row on recorded
+// steps (and cleared), FEP sums, temperature and thermostat state.
+// do_temp: FIN_* flags.  Ekin partials and accumulators are read with
+// ld.global.cg: in the fused update the last block of a trajectory runs this
+// after the other blocks' writes (made visible by __threadfence).
+__device__ void finalize_traj(const DevSys &S, int tr, int lane, double *v, int do_temp, double *rec,
+                              const int *rec_base, int k, int ene_every, int rec_cap) {
     const TrajInfo &T = S.traj[tr];
     TrajState &TS = S.tstate[tr];
     unsigned long long *ea = S.eacc + (size_t)tr * QG_NE;
@@ -427,7 +447,7 @@ __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_ba
     // FEP frames: qdyn writes energy frames at nonzero recorded steps only
     const bool fep = rec_step && T.fep_on && fstep > 0;
     for (int s = lane; s < QG_NE; s += 32) {
-        if (row >= 0 || fep) v[s] = fx_get(ea[s]);
+        if (row >= 0 || fep) v[s] = fx_get(__ldcg(ea + s));
         ea[s] = 0ull;
     }
     __syncwarp();
@@ -459,7 +479,7 @@ __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_ba
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             float p = 0.f;
-            for (int b = lane; b < T.ekin_nblk; b += 32) p += S.ekin_part[(size_t)(T.ekin_blk0 + b) * 4 + c];
+            for (int b = lane; b < T.ekin_nblk; b += 32) p += __ldcg(S.ekin_part + (size_t)(T.ekin_blk0 + b) * 4 + c);
             e4[c] = warp_sum_f(p);
         }
         if (lane == 0) {
@@ -536,6 +556,13 @@ __global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_ba
     for (int c = 0; c < 2 * QG_MAXOD; ++c) R[QG_REC_OD + c] = S.od_out[(size_t)tr * QG_MAXOD * 2 + c];
 }
 
+// One warp per trajectory (the FP64 path, temperature before the first step,
+// drop-in energy calls).
+__global__ void k_finalize(DevSys S, int do_temp, double *rec, const int *rec_base, int k, int ene_every, int rec_cap) {
+    __shared__ double v[QG_NE];
+    finalize_traj(S, blockIdx.x, threadIdx.x, v, do_temp, rec, rec_base, k, ene_every, rec_cap);
+}
+
 __global__ void k_tick(int *rec_base, int n) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *rec_base += n;
 }
@@ -567,9 +594,11 @@ void launch_update(const DevSys &S, const BlockTables &B, LaunchCtx &L, int mode
     prof_end(L);
     (*L.nlaunch)++;
 }
-void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int nbcycle, int ekin_only) {
+void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int nbcycle, int ekin_only,
+                     int fin, double *rec, int rec_cap) {
     prof_begin(L, "k_update_f");
-    k_update_f<<<B.nuatom / QG_UBLK, QG_UBLK, 0, L.stream>>>(S, B.uatom, B.ucon, B.ublk_water, e, nbcycle, ekin_only);
+    k_update_f<<<B.nuatom / QG_UBLK, QG_UBLK, 0, L.stream>>>(S, B.uatom, B.ucon, B.ublk_water, e, nbcycle, ekin_only,
+                                                             fin, rec, rec_cap);
     prof_end(L);
     (*L.nlaunch)++;
 }

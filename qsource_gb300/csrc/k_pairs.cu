@@ -69,7 +69,7 @@ struct EAcc<true> {
 // (13282-13365) and lrf_taylor for the three water atoms.
 // LW lanes share one water: lane l takes neighbours l, l+LW, ...; the
 // lanes' partial gradients are summed by an xor butterfly (fixed order).
-template <bool EACC, int LW, int MINB>
+template <bool EACC, int LW, int MINB, int U>
 __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int *wgrp, int lrf) {
     __shared__ long long red[5][QG_BLOCK / 32];
     const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LW;
@@ -141,16 +141,19 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
             }
             eww_el.flush(); eww_vdw.flush();
         };
-        // two neighbours per iteration keep two sets of loads in flight
+        // U neighbours per iteration keep U sets of loads in flight
         int k = lane;
-        for (; k + LW < nw; k += 2 * LW) {
-            const int b0 = lst[k], b1 = lst[k + LW];
-            const float4 p0 = S.wrec[b0], p1 = S.wrec[b0 + 1], p2 = S.wrec[b0 + 2];
-            const float4 s0 = S.wrec[b1], s1 = S.wrec[b1 + 1], s2 = S.wrec[b1 + 2];
-            ww(b0, p0, p1, p2);
-            ww(b1, s0, s1, s2);
+        for (; k + (U - 1) * LW < nw; k += U * LW) {
+            int bb[U];
+            float4 p[U][3];
+#pragma unroll
+            for (int u = 0; u < U; ++u) bb[u] = lst[k + u * LW];
+#pragma unroll
+            for (int u = 0; u < U; ++u) { p[u][0] = S.wrec[bb[u]]; p[u][1] = S.wrec[bb[u] + 1]; p[u][2] = S.wrec[bb[u] + 2]; }
+#pragma unroll
+            for (int u = 0; u < U; ++u) ww(bb[u], p[u][0], p[u][1], p[u][2]);
         }
-        if (k < nw) {
+        for (; k < nw; k += LW) {
             const int b0 = lst[k];
             ww(b0, S.wrec[b0], S.wrec[b0 + 1], S.wrec[b0 + 2]);
         }
@@ -658,24 +661,27 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
 }
 
 // Launch shapes (the autotuner's choice, BlockTables::tune): lanes per water
-// LW (4/8/16/32) and the register bound of the water kernel (minimum
-// resident blocks 1 or 6); lanes per solute atom (4/8/16).  The FP64-energy
+// LW (4/8/16), the register bound of the water kernel (minimum resident
+// blocks 1 or 6) and its neighbours per loop iteration (1/2/4); lanes per
+// solute atom (4/8/16).  The FP64-energy
 // variants (drop-in calls) use 8 lanes.
 template <int LW, int MINB>
 static void water_fp32(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf) {
-    k_nb_water<false, LW, MINB><<<B.nwgrp * LW / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    const int nb = B.nwgrp * LW / QG_BLOCK;
+    if (B.tune.unroll_water == 1) k_nb_water<false, LW, MINB, 1><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    else if (B.tune.unroll_water == 4) k_nb_water<false, LW, MINB, 4><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    else k_nb_water<false, LW, MINB, 2><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
 }
 void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
     if (!B.nwgrp) return;
     prof_begin(L, "k_nb_water");
     if (fp64_energy) {
-        k_nb_water<true, 8, 1><<<B.nwgrp * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+        k_nb_water<true, 8, 1, 2><<<B.nwgrp * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
     } else {
         const bool m6 = B.tune.minb_water == 6;
         switch (B.tune.lw_water) {
         case 4: m6 ? water_fp32<4, 6>(S, B, L, lrf) : water_fp32<4, 1>(S, B, L, lrf); break;
         case 16: m6 ? water_fp32<16, 6>(S, B, L, lrf) : water_fp32<16, 1>(S, B, L, lrf); break;
-        case 32: m6 ? water_fp32<32, 6>(S, B, L, lrf) : water_fp32<32, 1>(S, B, L, lrf); break;
         default: m6 ? water_fp32<8, 6>(S, B, L, lrf) : water_fp32<8, 1>(S, B, L, lrf); break;
         }
     }

@@ -404,7 +404,26 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
             }
         // --- work lists
         size_t s0 = wgrp.size();
-        for (int g = d.ncgp_solute; g < d.ncgp; ++g) wgrp.push_back(grp0 + g);
+        {
+            // water work order: by 1 A shells of the distance from the solvent
+            // centre, inner first (neighbour counts fall towards the surface,
+            // so a warp's lane groups get similar loads), topology order inside
+            // a shell.  The order changes no result: each water sums its own
+            // pairs and the block sums are fixed point.
+            std::vector<std::pair<int, int>> key;
+            for (int g = d.ncgp_solute; g < d.ncgp; ++g) {
+                const int o = d.cgp_switch[g];
+                double r2 = 0;
+                for (int c = 0; c < 3; ++c) {
+                    const double dx = d.x[3 * o + c] - d.xwcent[c];
+                    r2 += dx * dx;
+                }
+                key.push_back({(int)std::sqrt(r2), g});
+            }
+            std::stable_sort(key.begin(), key.end(),
+                             [](const std::pair<int, int> &a, const std::pair<int, int> &b) { return a.first < b.first; });
+            for (const auto &k : key) wgrp.push_back(grp0 + k.second);
+        }
         pad(wgrp, s0, t);
         s0 = satom.size();
         for (int i = 0; i < d.nat_solute; ++i) satom.push_back(atom0 + i);
@@ -738,6 +757,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     }
     if ((rc = alloc0(A, (size_t)ntraj * 2 * QG_MAXNH, &S.nh_state))) return rc;
     if ((rc = alloc0(A, (size_t)ntraj * QG_NFEP, &S.fep_acc))) return rc;
+    if ((rc = alloc0(A, (size_t)ntraj, &S.fin_cnt))) return rc;
     h->ene_files.assign(ntraj, nullptr);
     if (!wp_state.empty()) { double *p_; if ((rc = upload(A, wp_state, &p_))) return rc; S.wp_state = p_; }
     for (char f : h->fused) h->all_fused = h->all_fused && f;
@@ -911,14 +931,15 @@ static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every) {
     EaccSel esel{EACC_RECORD, h->recctl_d, k, ene_every};
     force_ops(h, L, QGPU_TERMS_ALL, false, esel);
     if (h->all_fused) {
-        launch_update_f(h->S, h->B, L, esel, h->NBcycle, 0);
+        // the update's last block per trajectory ends the step
+        launch_update_f(h->S, h->B, L, esel, h->NBcycle, 0, FIN_TEMP | FIN_STEP | FIN_NH, h->rec_d, h->rec_cap);
     } else {
         launch_integrate(h->S, h->B, L);
         launch_shake(h->S, h->B, L, -1);
         launch_update(h->S, h->B, L, 2);
         launch_wrec(h->S, h->B, L);
+        launch_finalize(h->S, L, FIN_TEMP | FIN_STEP | FIN_NH, h->rec_d, h->recctl_d, k, ene_every, h->rec_cap);
     }
-    launch_finalize(h->S, L, FIN_TEMP | FIN_STEP | FIN_NH, h->rec_d, h->recctl_d, k, ene_every, h->rec_cap);
 }
 
 // ------------------------------------------------------------------ C-ABI
@@ -1276,12 +1297,13 @@ static void tune_qw(qgpu_handle *h, LaunchCtx &L) {
 
 int qgpu_set_tuning(qgpu_handle *h, const int32_t *tuning) {
     if (!h || !tuning) return fail(QGPU_E_INVALID, "qgpu_set_tuning: bad arguments");
-    const int lw = tuning[0], mb = tuning[1], ls = tuning[2], lq = tuning[3];
-    if ((lw != 4 && lw != 8 && lw != 16 && lw != 32) || (mb != 1 && mb != 6) || (ls != 4 && ls != 8 && ls != 16) ||
-        (lq != 0 && lq != 1 && lq != 2 && lq != 4))
+    const int lw = tuning[0], mb = tuning[1], ls = tuning[2], lq = tuning[3], uw = tuning[4];
+    if ((lw != 4 && lw != 8 && lw != 16) || (mb != 1 && mb != 6) || (ls != 4 && ls != 8 && ls != 16) ||
+        (lq != 0 && lq != 1 && lq != 2 && lq != 4) || (uw != 1 && uw != 2 && uw != 4))
         return fail(QGPU_E_INVALID, "qgpu_set_tuning: unsupported shape");
     CK(cudaStreamSynchronize(h->stream));
     h->B.tune.lw_water = lw; h->B.tune.minb_water = mb; h->B.tune.lw_solute = ls; h->B.tune.lg_qw = lq;
+    h->B.tune.unroll_water = uw;
     if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     return 0;
 }
@@ -1299,13 +1321,15 @@ int qgpu_autotune(qgpu_handle *h, int32_t *tuning) {
         Tuning best = h->B.tune;
         float t, tb = 1e30f;
         if (h->B.nwgrp) {
-            for (int lw : {4, 8, 16, 32})
-                for (int mb : {1, 6}) {
-                    h->B.tune.lw_water = lw; h->B.tune.minb_water = mb;
-                    if (int rc = time_variant(h, L, tune_water, &t)) return rc;
-                    if (t < tb) { tb = t; best.lw_water = lw; best.minb_water = mb; }
-                }
+            for (int lw : {4, 8, 16})
+                for (int mb : {1, 6})
+                    for (int uw : {1, 2, 4}) {
+                        h->B.tune.lw_water = lw; h->B.tune.minb_water = mb; h->B.tune.unroll_water = uw;
+                        if (int rc = time_variant(h, L, tune_water, &t)) return rc;
+                        if (t < tb) { tb = t; best.lw_water = lw; best.minb_water = mb; best.unroll_water = uw; }
+                    }
             h->B.tune.lw_water = best.lw_water; h->B.tune.minb_water = best.minb_water;
+            h->B.tune.unroll_water = best.unroll_water;
             tb = 1e30f;
             for (int lq : {1, 2, 4}) {
                 h->B.tune.lg_qw = lq;
@@ -1335,7 +1359,7 @@ int qgpu_autotune(qgpu_handle *h, int32_t *tuning) {
     if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     if (tuning) {
         tuning[0] = h->B.tune.lw_water; tuning[1] = h->B.tune.minb_water;
-        tuning[2] = h->B.tune.lw_solute; tuning[3] = h->B.tune.lg_qw;
+        tuning[2] = h->B.tune.lw_solute; tuning[3] = h->B.tune.lg_qw; tuning[4] = h->B.tune.unroll_water;
     }
     return 0;
 }

@@ -251,6 +251,7 @@ struct DevSys {
     const unsigned *lcg_a, *lcg_c;
     double *nh_state;               // per trajectory: vnh[QG_MAXNH], xnh[QG_MAXNH]
     double *fep_acc;                // per trajectory: QG_NFEP sums (k_finalize)
+    int *fin_cnt;                   // per trajectory: update blocks done this step (fused step end)
     // water polarisation state per (trajectory, shell): theta_corr, avtheta,
     // avn_insh (slot = TrajInfo::wp0 + shell)
     double *wp_state;               // 3 doubles per slot
@@ -447,7 +448,7 @@ void prof_end(LaunchCtx &L);
 // Launch-shape choices of the pair kernels (the autotuner's parameters);
 // 0 = default.
 struct Tuning {
-    int lw_water = 8, minb_water = 1, lw_solute = 8, lg_qw = 0;
+    int lw_water = 8, minb_water = 1, lw_solute = 8, lg_qw = 0, unroll_water = 2;
 };
 struct BlockTables {
     Tuning tune;
@@ -495,7 +496,8 @@ void launch_shake(const DevSys &S, const BlockTables &B, LaunchCtx &L, int traj_
 void launch_update(const DevSys &S, const BlockTables &B, LaunchCtx &L, int mode);
 // the fused step with the float master; writes x/v as well when the next
 // step lists or records (e: the record selector of this step, nbcycle)
-void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int nbcycle, int ekin_only);
+void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int nbcycle, int ekin_only,
+                     int fin = 0, double *rec = nullptr, int rec_cap = 0);
 // x = origin + hi + lo, v = velf for every atom
 void launch_sync_double(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *rec, const int *rec_base, int k,

@@ -151,8 +151,8 @@ class Engine:
     def autotune(self) -> list:
         """Time the pair-kernel launch shapes and keep the fastest
         (qgpu_autotune); returns [lanes_water, min_blocks_water,
-        lanes_solute, lanes_qw]."""
-        t = np.zeros(4, dtype=np.int32)
+        lanes_solute, lanes_qw, unroll_water]."""
+        t = np.zeros(5, dtype=np.int32)
         self._check(self.lib.qgpu_autotune(self.h, abi.ptr(t)))
         return [int(v) for v in t]
 
