@@ -360,6 +360,24 @@ int qgpu_fep_start(qgpu_handle *h, int32_t nwin, const int32_t *chain, double kT
    dv forward, and of dv backward. */
 int qgpu_fep_result(qgpu_handle *h, double *dgf, double *dgr, double *dg, double *stats);
 
+/* ---- learned lambda schedule: the MLP ----------------------------------- */
+/* Has no counterpart in the reference (qdyn runs lambda windows one after
+   another on a fixed schedule).  A 3-layer MLP, 16 inputs (zero-padded) ->
+   tanh 128 -> tanh 128 -> 1, run by hand-written one-block kernels whose
+   layer products use BF16 tensor-core mma with FP32 accumulation; FP32 master
+   parameters, Adam moments.  Parameter layout (floats): W1[128][16], b1[128],
+   W2[128][128], b2[128], W3[16][128] (row 0 used), b3[16] (entry 0 used);
+   qgpu_mlp_nparams() floats in all.  Batches hold 1..64 rows of 16 features. */
+int qgpu_mlp_nparams(void);
+/* out[n] = network(X[n][16]) */
+int qgpu_mlp_predict(const float *params, const float *X, int32_t n, float *out);
+/* iters full-batch Adam steps (lr; beta 0.9/0.999) on the mean squared error
+   to Y[n], deterministic; params, adam_m, adam_v updated in place; step0 =
+   Adam steps already taken; loss_out[iters] (may be NULL) the loss before each
+   step; grad_out[nparams] (may be NULL) the gradient of the last step. */
+int qgpu_mlp_train(float *params, float *adam_m, float *adam_v, const float *X, const float *Y, int32_t n,
+                   int32_t iters, float lr, int32_t step0, float *loss_out, float *grad_out);
+
 /* ---- inspection (tests and tools) --------------------------------------- */
 /* Near charge-group pairs of the last list build, one row per unordered pair
    (g1 < g2), with g1,g2 0-based group indices.  Returns the count in *npairs;

@@ -123,6 +123,9 @@ EXPORTS = {
     "qgpu_set_precision": (_i32, [C.c_void_p, _i32]),
     "qgpu_set_step": (_i32, [C.c_void_p, C.c_int64]),
     "qgpu_autotune": (_i32, [C.c_void_p, _P]),
+    "qgpu_mlp_nparams": (_i32, []),
+    "qgpu_mlp_predict": (_i32, [_P, _P, _i32, _P]),
+    "qgpu_mlp_train": (_i32, [_P, _P, _P, _P, _P, _i32, _i32, C.c_float, _i32, _P, _P]),
     "qgpu_set_tuning": (_i32, [C.c_void_p, _P]),
     "qgpu_ene_open": (_i32, [C.c_void_p, _i32, C.c_char_p]),
     "qgpu_ene_close": (_i32, [C.c_void_p, _i32]),

@@ -343,3 +343,71 @@ def test_autotune_picks_a_valid_shape_and_is_cached(systems):
     assert b.autotune() == t1            # same device and size: the cached choice
     rows = b.run(10, ene_every=5)[0]
     assert len(rows) == 2 and all(np.isfinite(r[1]["potential"]) for r in rows)
+
+
+# ------------------------------------------------------------- schedule MLP
+def _mlp_data(seed, ncurves, kT=0.596, npilot=11, nsamp=20):
+    """Pilot statistics of random FEP spread curves (Gaussian model) and the
+    true log-spread at the pilot windows."""
+    from mlp_ref import pilot_stats, s_curve
+    from qsource_gb300.schedule import features
+    rng = np.random.default_rng(seed)
+    lam = np.linspace(0.0, 1.0, npilot)
+    X, Y, curves = [], [], []
+    for _ in range(ncurves):
+        s = s_curve(rng)
+        st = pilot_stats(rng, s, lam, kT, nsamp)
+        X.append(features(lam, st, kT))
+        Y.append(np.log([s(x) for x in lam]))
+        curves.append((s, st))
+    return lam, np.concatenate(X), np.concatenate(Y).astype(np.float32), curves
+
+
+def test_mlp_kernels_match_cpu_reference(engine_lib):
+    """One training step of the library's kernels (forward, backward through
+    BF16 tensor-core products with FP32 sums) against the CPU reference with
+    the same BF16 roundings: loss to 1e-4, each layer's gradient to 1e-2 of its
+    norm, predictions to 1e-3."""
+    from mlp_ref import forward, loss_and_grad
+    from qsource_gb300.schedule import MLP
+    rng = np.random.default_rng(11)
+    net = MLP(seed=5)
+    X = rng.normal(0, 1, (40, 16)).astype(np.float32)
+    Y = rng.normal(0, 1, 40).astype(np.float32)
+    p0 = net.params.copy()
+    ref_loss, ref_grad = loss_and_grad(p0, X, Y)
+    pred = net.predict(X)
+    assert np.allclose(pred, forward(p0, X)[3][:, 0], rtol=1e-3, atol=1e-3)
+    loss, grad = net.train(X, Y, iters=1, lr=0.0)
+    assert np.array_equal(net.params, p0)            # lr 0 leaves the parameters
+    assert abs(loss[0] - ref_loss) <= 1e-4 * ref_loss
+    o = 0
+    for n in (128 * 16, 128, 128 * 128, 128, 16 * 128, 16):
+        gg, gr = grad[o:o + n].astype(np.float64), ref_grad[o:o + n]
+        assert np.linalg.norm(gg - gr) <= 1e-2 * max(np.linalg.norm(gr), 1e-12), o
+        o += n
+
+
+def test_learned_schedule_beats_uniform(engine_lib):
+    """Trained on the GPU (the library's kernels) on pilot statistics of
+    random spread curves, the network's placement halves (median) the
+    expected FEP error of uniform windows on held-out curves (Gaussian gap
+    model, 21 windows, equal sampling per window), and does no worse than
+    placing by the pilot's own short-run spread."""
+    from mlp_ref import schedule_mse
+    from qsource_gb300.schedule import MLP, learned_schedule, place
+    kT = 0.596
+    lam, X, Y, _ = _mlp_data(1, 5)
+    net = MLP(seed=2)
+    loss, _ = net.train(X, Y, iters=2000, lr=3e-3)
+    assert loss[-1] < 0.05 * loss[0]
+    lam, _, _, test = _mlp_data(99, 10)
+    uni, lrn, raw = [], [], []
+    for s, st in test:
+        w, _ = learned_schedule(net, lam, st, kT, 21)
+        pilot_s = np.sqrt(np.maximum(st[:, 2], st[:, 5])) / (lam[1] - lam[0])
+        uni.append(schedule_mse(s, np.linspace(0, 1, 21), kT, 200))
+        lrn.append(schedule_mse(s, w, kT, 200))
+        raw.append(schedule_mse(s, place(lam, pilot_s, 21), kT, 200))
+    assert np.median(np.array(lrn) / np.array(uni)) < 0.5
+    assert np.median(np.array(lrn) / np.array(raw)) < 1.05
