@@ -312,6 +312,14 @@ def main():
     fl = kernel_flops(name, wc)
     share = {k: round(v[0] / sum(x[0] for x in prof.values()), 4) for k, v in prof.items()}
     us_per_step = {k: round(1e3 * v[0] / (2 * NB), 2) for k, v in prof.items()}
+    # every kernel with an algorithmic count: its own roofline fraction
+    per_kernel = {}
+    for kname, (kms_k, kcnt_k) in prof.items():
+        fk = kernel_flops(kname, wc)
+        if fk is not None and kcnt_k:
+            ach = fk / (kms_k / kcnt_k * 1e-3) / 1e12
+            per_kernel[kname] = {"achieved_tflops": round(ach, 3), "frac": round(ach / peak, 4),
+                                 "us_per_launch": round(1e3 * kms_k / kcnt_k, 2)}
     roof = None
     if fl is not None:
         achieved = fl / (kms / kcnt * 1e-3) / 1e12
@@ -342,6 +350,7 @@ def main():
                        "qgpu_run with an energy sink, qgpu_get_coords_all (host wall clock)"},
         "roofline": roof,
         "kernel_share": share,
+        "kernel_roofline": per_kernel,
         "kernel_us_per_step": us_per_step,
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None,
         "clocks": clk,
