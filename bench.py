@@ -12,8 +12,10 @@ Printed: one JSON line (rank 0).  `value` = aggregate ns/day from CUDA events
 on the engine's stream around the timed 10-step blocks (L2 flushed with a
 256 MB write before each block); `e2e` = the same through the public API with
 host buffers (coordinates and velocities uploaded from pinned memory and read
-back, energies read back every block).  --impl reference times the FP64 CPU
-restatement of the reference (oracle/) on all host cores instead.
+back, energies read back every block); `plain_form` = the same trajectories
+run one at a time, each alone in its own handle (the unbatched GPU form), and
+`batched_over_plain` = value / plain_form.  --impl reference times the FP64
+CPU restatement of the reference (oracle/) on all host cores instead.
 """
 from __future__ import annotations
 
@@ -193,6 +195,44 @@ def kernel_flops(name, wc):
     return None
 
 
+def plain_form(systems, flush, nblk: int, world: int) -> dict:
+    """The same trajectories on the same GPU kernels, one trajectory per
+    handle and one after another (the uniform-window form without batching):
+    each trajectory gets its own handle with the default launch shapes, one
+    untimed block, then nblk timed 10-step graph replays with the L2 flushed
+    before each.  Aggregate ns/day = all simulated time / the summed device
+    time, the throughput of running the windows one by one."""
+    import torch
+    from qsource_gb300.engine import Engine
+    ms_total = 0.0
+    per = []
+    for s in systems:
+        e = Engine([s])
+        e.enqueue(NB, 0)
+        e.sync()
+        ext = torch.cuda.ExternalStream(e.stream())
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nblk)]
+        torch.cuda.synchronize()
+        with torch.cuda.stream(ext):
+            for b in range(nblk):
+                flush.fill_(float(b))
+                ev[b][0].record(ext)
+                e.enqueue(NB, NB)
+                ev[b][1].record(ext)
+        e.sync()
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+        ms_total += ms
+        per.append(ms / (nblk * NB))
+        e.close()
+    value = aggregate_ns_per_day(world, len(systems), nblk * NB, ms_total)
+    return {"value": round(value, 3), "unit": "ns/day",
+            "ms_per_step_min": round(min(per), 5), "ms_per_step_max": round(max(per), 5),
+            "how": f"each of the {len(systems)} trajectories alone in its own handle (default launch shapes), "
+                   f"one after another: 1 untimed + {nblk} timed 10-step CUDA-graph blocks each, L2 flushed "
+                   f"before every block; aggregate = simulated ns / summed device time"}
+
+
 # ------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -206,6 +246,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                     help="MD step precision (qgpu_set_precision): double-float master / FP64 master")
+    ap.add_argument("--no-plain", action="store_true", help="skip the one-trajectory-at-a-time GPU form")
+    ap.add_argument("--plain-blocks", type=int, default=20, help="timed 10-step blocks per trajectory, plain form")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -327,6 +369,7 @@ def main():
                 "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": committed_traffic(name),
                 "peak_source": "measured in this run: FP32 FMA-chain kernel over all SMs (qgpu_fp32_peak)",
                 "avg_launch_ms": round(kms / kcnt, 5), "flops_per_launch": fl}
+    plain = None if args.no_plain else plain_form(systems, flush, args.plain_blocks, world)
     if rank != 0:
         return
     cpu = cpu_baseline(pool, args.cpu_steps) if pool else None
@@ -353,6 +396,8 @@ def main():
         "kernel_roofline": per_kernel,
         "kernel_us_per_step": us_per_step,
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None,
+        "plain_form": plain,
+        "batched_over_plain": round(ns_per_day / plain["value"], 3) if plain else None,
         "clocks": clk,
         "gpu_launches": int(launches),
         "work": wc,

@@ -208,6 +208,24 @@ typedef struct qgpu_system_desc {
     int32_t rand_state;           /* randm state (iseed) when the run starts           */
     int32_t nhchains;             /* Nose-Hoover chain length                         */
     double nhq;                   /* Nose-Hoover mass                                 */
+
+    /* periodic box: topology boundary record "PBC" (topo_read src/topo.f90:
+       1022-1031), [PBC] of the input (initialize src/md.f90:4514-4590) and of
+       the FEP file (switching_atom, src/qatom.f90:672-687).  use_pbc = 0 is the
+       simulation sphere and the fields below are ignored.  With use_pbc = 1
+       the lists and pair loops take minimum images (make_pair_lists box branch
+       src/md.f90:6003-6029, pot_energy_nonbonds :16266-16300); the sphere
+       restraints (fix_shell, restrain_solvent, watpol) are off (:16114-16124). */
+    int32_t use_pbc;
+    double boxlength[3];
+    double boxcentre[3];
+    int32_t qswitch;              /* Q-atom switching atom, 0-based (PBC with Q atoms) */
+    int32_t put_solute_back;      /* put_back_in_box of solute molecules              */
+    int32_t put_solvent_back;     /* put_back_in_box of solvent molecules             */
+    int32_t rigid_box_centre;     /* 0: box centre follows the solute (put_back_in_box)*/
+    int32_t nmol;                 /* molecules                                        */
+    const int32_t *istart_mol;    /* nmol: first atom of each molecule, 0-based       */
+    int32_t nsolute_mol;          /* the first nsolute_mol molecules are solute       */
 } qgpu_system_desc;
 
 /* Energies, the ENERGIES record of src/nrgy.f90:48-54 (sphere subset). */

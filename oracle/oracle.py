@@ -60,6 +60,7 @@ def lib() -> C.CDLL:
         L.oracle_final_energy.argtypes = [vp, C.c_int, C.POINTER(Energies), C.POINTER(QEnergy)]
         L.oracle_rand_state.restype = C.c_int32
         L.oracle_rand_state.argtypes = [vp]
+        L.oracle_put_back_in_box.argtypes = [vp]
         L.oracle_qfep_fep.restype = C.c_int
         L.oracle_qfep_fep.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_int, C.c_double, C.c_int, vp, vp, vp, vp]
         L.oracle_sizeof_desc.restype = C.c_int
@@ -145,6 +146,9 @@ class Oracle:
         H = np.zeros(max(n, 1)); r = np.zeros(max(n, 1))
         self.L.oracle_offdiag(self.h, _p(H), _p(r))
         return H[:n], r[:n]
+
+    def put_back_in_box(self):
+        self.L.oracle_put_back_in_box(self.h)
 
     def rand_state(self) -> int:
         """The randm state the next random number continues from."""

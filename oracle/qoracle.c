@@ -29,7 +29,10 @@
 #define QREAL_EPS 1.0e-14       /* src/sizes.f90:48 (double build) */
 #define NLRF 43                 /* cent[3] phi0 phi1[3] phi2[9] phi3[27] */
 
-typedef struct { int32_t i, j; int8_t lj, qlj; } nbrec;
+/* si, sj: the atoms whose difference x[sj] - x[si] gives the periodic shift
+   of the pair in a box (the switch atoms of the charge-group pair, the two
+   water O, the Q switching atom and a solute / water atom); -1 in a sphere */
+typedef struct { int32_t i, j; int8_t lj, qlj; int32_t si, sj; } nbrec;
 
 typedef struct { nbrec *a; int64_t n, cap; } nblist;
 
@@ -60,6 +63,9 @@ typedef struct oracle {
     /* Langevin random-force amplitudes and Nose-Hoover chain */
     double *randva, *randfa;
     double xnh[64], vnh[64], qnh[64], Gnh[64];
+    /* periodic box: 1/boxlength and the box centre put_back_in_box moves */
+    double ibox[3], boxc[3];
+    int32_t *istart_mol;
 } oracle;
 
 /* ------------------------------------------------------------------ utils */
@@ -69,12 +75,13 @@ static void *dupbuf(const void *src, size_t n) {
     if (src && n) memcpy(p, src, n);
     return p;
 }
-static void nb_push(nblist *l, int32_t i, int32_t j, int lj, int qlj) {
+static void nb_push_s(nblist *l, int32_t i, int32_t j, int lj, int qlj, int32_t si, int32_t sj) {
     if (l->n == l->cap) {
         l->cap = l->cap ? 2 * l->cap : 1024;
         l->a = (nbrec *)realloc(l->a, (size_t)l->cap * sizeof(nbrec));
     }
     l->a[l->n].i = i; l->a[l->n].j = j; l->a[l->n].lj = (int8_t)lj; l->a[l->n].qlj = (int8_t)qlj;
+    l->a[l->n].si = si; l->a[l->n].sj = sj;
     l->n++;
 }
 static inline int ljcod(const oracle *o, int ti, int tj) { return o->d.ljcod[ti * o->d.natyps + tj]; }
@@ -164,6 +171,13 @@ void *oracle_create(const qgpu_system_desc *in) {
     for (int k = 0; k < nc; ++k) { o->qnh[k] = in->nhq; o->vnh[k] = 0; o->xnh[k] = 0; }
     if (nc) o->qnh[0] = in->Ndegf * in->nhq;
     o->d.nhchains = nc;
+    /* periodic box (inv_boxl = 1/boxlength, prep_sim) */
+    for (int k = 0; k < 3; ++k) {
+        o->ibox[k] = in->use_pbc ? 1.0 / in->boxlength[k] : 0.0;
+        o->boxc[k] = in->boxcentre[k];
+    }
+    o->istart_mol = (int32_t *)dupbuf(in->istart_mol, in->use_pbc ? (size_t)in->nmol * sizeof(int32_t) : 0);
+    o->d.istart_mol = o->istart_mol;
     return o;
 }
 
@@ -194,6 +208,27 @@ void oracle_get_coords(void *h, double *x, double *v) {
 
 /* ------------------------------------------------------------------ LRF */
 /* cgp_centers, src/md.f90:2253-2288 */
+/* ----------------------------------------------------------- periodic box */
+/* boxlength(k)*nint(d*inv_boxl(k)), the periodic shift of one component as
+   every box routine of the reference writes it (Fortran nint rounds halves
+   away from zero, as round() does) */
+static inline double pbc_shift(const oracle *o, int k, double dk) {
+    return o->d.boxlength[k] * round(dk * o->ibox[k]);
+}
+/* |x_i - x_j|^2, the minimum image in a box (dx = dx - boxlength*nint(dx*inv_boxl),
+   r2 = dx**2 + dy**2 + dz**2: nbpplist_box_lrf src/md.f90:8282-8288 and the
+   other box list builders); the plain distance in a sphere */
+static inline double dist2m(const oracle *o, int i, int j) {
+    const double *x = o->x;
+    double a = x[3 * i] - x[3 * j], b = x[3 * i + 1] - x[3 * j + 1], c = x[3 * i + 2] - x[3 * j + 2];
+    if (o->d.use_pbc) {
+        a = a - pbc_shift(o, 0, a);
+        b = b - pbc_shift(o, 1, b);
+        c = c - pbc_shift(o, 2, c);
+    }
+    return a * a + b * b + c * c;
+}
+
 static void cgp_centers(oracle *o) {
     const qgpu_system_desc *d = &o->d;
     for (int g = 0; g < d->ncgp; ++g) {
@@ -208,17 +243,24 @@ static void cgp_centers(oracle *o) {
     }
 }
 
-/* lrf_update(group1, group2), src/md.f90:5896-5981 (sphere: no shift).
-   Multipoles of the non-Q atoms of group1 expanded about the centre of group2.
+/* lrf_update(group1, group2), src/md.f90:5896-5981.
+   Multipoles of the non-Q atoms of group1 expanded about the centre of group2;
+   in a box shifted by the periodic image of group1's switch atom relative to
+   that centre (:5905-5917).
    phi2(a,b) and phi3(a,b,c) are stored row-major, index (a*3+b) and (a*9+b*3+c). */
 static void lrf_update(oracle *o, int g1, int g2) {
     const qgpu_system_desc *d = &o->d;
     double *r = o->lrf + (size_t)g2 * NLRF;
     double *phi1 = r + 4, *phi2 = r + 7, *phi3 = r + 16;
+    double sh[3] = { 0.0, 0.0, 0.0 };
+    if (d->use_pbc) {
+        const int sw = d->cgp_switch[g1];
+        for (int a = 0; a < 3; ++a) sh[a] = pbc_shift(o, a, o->x[3 * sw + a] - r[a]);
+    }
     for (int k = d->cgp_first[g1]; k <= d->cgp_last[g1]; ++k) {
         int i = d->cgpatom[k];
         if (is_q(o, i)) continue;
-        double dr[3] = { o->x[3 * i] - r[0], o->x[3 * i + 1] - r[1], o->x[3 * i + 2] - r[2] };
+        double dr[3] = { o->x[3 * i] - r[0] - sh[0], o->x[3 * i + 1] - r[1] - sh[1], o->x[3 * i + 2] - r[2] - sh[2] };
         double r2 = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
         double f0 = d->crg[i] / (r2 * sqrt(r2));
         double f1 = 3.0 * f0 / r2;
@@ -290,7 +332,7 @@ static void nbpplist_lrf(oracle *o) {
             if (parity_skip(ig, jg)) continue;
             int js = d->cgp_switch[jg];
             if (d->excl[js]) continue;
-            double r2 = dist2(o->x, is, js);
+            double r2 = dist2m(o, is, js);
             if (r2 <= rc2) {
                 for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig]; ++ka) {
                     int i = d->cgpatom[ka];
@@ -303,7 +345,7 @@ static void nbpplist_lrf(oracle *o) {
                         if (excluded(o, i, j)) continue;
                         int lj = ljcod(o, d->iac[i], d->iac[j]);
                         if (is14(o, i, j)) lj = 3;
-                        nb_push(&o->pp, i, j, lj, lj);
+                        nb_push_s(&o->pp, i, j, lj, lj, is, js);
                     }
                 }
             } else if (d->use_LRF && r2 <= rl2) {
@@ -326,7 +368,7 @@ static void nbpwlist_lrf(oracle *o) {
             int ja = d->nat_solute + 3 * jw;
             int jg = o->iwhich[ja];
             if (d->excl[ja]) continue;
-            double r2 = dist2(o->x, is, ja);
+            double r2 = dist2m(o, is, ja);
             if (r2 <= rc2) {
                 for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig]; ++ka) {
                     int i = d->cgpatom[ka];
@@ -334,7 +376,7 @@ static void nbpwlist_lrf(oracle *o) {
                     for (int s = 0; s < 3; ++s) {
                         int j = ja + s;
                         if (all_zero(o, i, j)) continue;
-                        nb_push(&o->pw, i, j, ljcod(o, d->iac[i], d->iac[j]), 0);
+                        nb_push_s(&o->pw, i, j, ljcod(o, d->iac[i], d->iac[j]), 0, is, ja);
                     }
                 }
             } else if (d->use_LRF && r2 <= rl2) {
@@ -383,7 +425,7 @@ static void nbpplis2_lrf(oracle *o) {
                         if (excluded(o, i, j)) continue;
                         int lj = ljcod(o, d->iac[i], d->iac[j]);
                         if (is14(o, i, j)) lj = 3;
-                        nb_push(&o->pp, i, j, lj, lj);
+                        nb_push_s(&o->pp, i, j, lj, lj, -1, -1);
                     }
                 }
             } else if (d->use_LRF && r2 <= rl2) {
@@ -420,7 +462,7 @@ static void nbpwlis2_lrf(oracle *o) {
                     for (int s = 0; s < 3; ++s) {
                         int j = ja + s;
                         if (all_zero(o, i, j)) continue;
-                        nb_push(&o->pw, i, j, ljcod(o, d->iac[i], d->iac[j]), 0);
+                        nb_push_s(&o->pw, i, j, ljcod(o, d->iac[i], d->iac[j]), 0, -1, -1);
                     }
                 }
             } else if (d->use_LRF && r2 <= rl2) {
@@ -432,8 +474,52 @@ static void nbpwlis2_lrf(oracle *o) {
 }
 
 /* nbqplist, src/md.f90:10215-10322 (built once when Rcq > rexcl_o) */
+/* nbqplist_box, src/md.f90:10327-10459: rebuilt at every list update; a
+   solute group is inside when one of its atoms lies within Rcq of the Q
+   switching atom (minimum image); that atom fixes the group's periodic shift */
+static void nbqplist_box(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    o->qp.n = 0;
+    if (d->nqat == 0) return;
+    double rc2 = d->Rcq * d->Rcq;
+    for (int ig = 0; ig < d->ncgp_solute; ++ig) {
+        int inside = -1;
+        for (int k = d->cgp_first[ig]; k <= d->cgp_last[ig] && inside < 0; ++k)
+            if (dist2m(o, d->cgpatom[k], d->qswitch) <= rc2) inside = d->cgpatom[k];
+        if (inside < 0) continue;
+        for (int k = d->cgp_first[ig]; k <= d->cgp_last[ig]; ++k) {
+            int i = d->cgpatom[k];
+            if (d->qp_skip[i]) continue;
+            for (int iq = 0; iq < d->nqat; ++iq) {
+                int lj = ljcod(o, d->iac[i], d->iac[d->iqseq[iq]]);
+                for (int p = 0; p < d->nqp14; ++p)
+                    if (d->qp14_pairs[2 * p] == iq && d->qp14_pairs[2 * p + 1] == i) lj = 3;
+                nb_push_s(&o->qp, iq, i, lj, lj == 2 ? 1 : lj, d->qswitch, inside);
+            }
+        }
+    }
+}
+
+/* nbqwlist_box, src/md.f90:10554-10618: waters whose O lies within Rcq of
+   the Q switching atom (minimum image), rebuilt at every list update */
+static void nbqwlist_box(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    o->qw.n = 0;
+    if (d->nqat == 0) return;
+    double rc2 = d->Rcq * d->Rcq;
+    int ns = d->nat_solute;
+    for (int w = 0; w < d->nwat; ++w) {
+        int ia = ns + 3 * w;
+        if (dist2m(o, ia, d->qswitch) <= rc2)
+            for (int iq = 0; iq < d->nqat; ++iq)
+                for (int s = 0; s < 3; ++s)
+                    nb_push_s(&o->qw, iq, ia + s, ljcod(o, d->iac[ns + s], d->iac[d->iqseq[iq]]), 0, d->qswitch, ia);
+    }
+}
+
 static void nbqplist(oracle *o) {
     const qgpu_system_desc *d = &o->d;
+    if (d->use_pbc) { nbqplist_box(o); return; }
     if (o->qp_done && d->Rcq > d->rexcl_o) return;
     o->qp.n = 0;
     double rc2 = d->Rcq * d->Rcq;
@@ -462,7 +548,7 @@ static void nbqplist(oracle *o) {
                 for (int p = 0; p < d->nqp14; ++p)
                     if (d->qp14_pairs[2 * p] == iq && d->qp14_pairs[2 * p + 1] == i) lj = 3;
                 int qlj = lj == 2 ? 1 : lj;
-                nb_push(&o->qp, iq, i, lj, qlj);
+                nb_push_s(&o->qp, iq, i, lj, qlj, -1, -1);
             }
         }
     }
@@ -484,11 +570,11 @@ static void nbwwlist_lrf(oracle *o) {
             if (d->excl[ja]) continue;
             int jg = o->iwhich[ja];
             if (parity_skip(iw, jw) || iw == jw) continue;
-            double r2 = dist2(o->x, is, ja);
+            double r2 = dist2m(o, is, ja);
             if (r2 <= rc2) {
                 for (int la = 0; la < 3; ++la)
                     for (int ka = 0; ka < 3; ++ka)
-                        nb_push(&o->ww, is + la, ja + ka, ljcod(o, d->iac[ns + la], d->iac[ns + ka]), 0);
+                        nb_push_s(&o->ww, is + la, ja + ka, ljcod(o, d->iac[ns + la], d->iac[ns + ka]), 0, is, ja);
             } else if (d->use_LRF && r2 <= rl2) {
                 lrf_update(o, ig, jg);
                 lrf_update(o, jg, ig);
@@ -500,6 +586,7 @@ static void nbwwlist_lrf(oracle *o) {
 /* nbqwlist, src/md.f90:10464-10549 (built once when Rcq > rexcl_o) */
 static void nbqwlist(oracle *o) {
     const qgpu_system_desc *d = &o->d;
+    if (d->use_pbc) { nbqwlist_box(o); return; }
     if (o->qw_done && d->Rcq > d->rexcl_o) return;
     o->qw.n = 0;
     if (d->nqat == 0) return;
@@ -512,12 +599,13 @@ static void nbqwlist(oracle *o) {
         if (a * a + b * b + c * c <= rc2)
             for (int iq = 0; iq < d->nqat; ++iq)
                 for (int s = 0; s < 3; ++s)
-                    nb_push(&o->qw, iq, ia + s, ljcod(o, d->iac[ns + s], d->iac[d->iqseq[iq]]), 0);
+                    nb_push_s(&o->qw, iq, ia + s, ljcod(o, d->iac[ns + s], d->iac[d->iqseq[iq]]), 0, -1, -1);
     }
     o->qw_done = 1;
 }
 
-/* make_pair_lists, sphere + LRF branch, src/md.f90:6043-6058 (switch-atom or any-atom lists) */
+/* make_pair_lists, LRF branches, src/md.f90:6003-6058: sphere (switch-atom or
+   any-atom lists) or periodic box (switch-atom lists, minimum images) */
 void oracle_make_pair_lists(void *h) {
     oracle *o = (oracle *)h;
     if (o->d.use_LRF) cgp_centers(o);
@@ -551,6 +639,14 @@ void oracle_get_lrf(void *h, double *out) {
 /* ---------------------------------------------------------- nonbonds */
 #define DX(i, j) double dx1 = o->x[3 * (j)] - o->x[3 * (i)], dx2 = o->x[3 * (j) + 1] - o->x[3 * (i) + 1], \
                         dx3 = o->x[3 * (j) + 2] - o->x[3 * (i) + 2]
+/* dx = dx - shift of the record's pair in a box (nonbond_pp_box :13226-13228,
+   nonbond_pw_box, nonbond_ww_spc_box :15187-15193, nonbond_qp_box :13989-13991,
+   nonbond_qw_spc_box :14627-14633) with shift = boxlength*nint((x[sj]-x[si])*inv_boxl) */
+#define BOX_SHIFT(rec) do { if (o->d.use_pbc) { const double *X_ = o->x; \
+    const int si_ = (rec).si, sj_ = (rec).sj; \
+    dx1 = dx1 - pbc_shift(o, 0, X_[3 * sj_] - X_[3 * si_]); \
+    dx2 = dx2 - pbc_shift(o, 1, X_[3 * sj_ + 1] - X_[3 * si_ + 1]); \
+    dx3 = dx3 - pbc_shift(o, 2, X_[3 * sj_ + 2] - X_[3 * si_ + 2]); } } while (0)
 #define ADD_F(i, j, dv) do { double *F = o->f; \
     F[3*(i)] -= (dv)*dx1; F[3*(i)+1] -= (dv)*dx2; F[3*(i)+2] -= (dv)*dx3; \
     F[3*(j)] += (dv)*dx1; F[3*(j)+1] += (dv)*dx2; F[3*(j)+2] += (dv)*dx3; } while (0)
@@ -561,6 +657,7 @@ static void nonbond_pp(oracle *o) {
     for (int64_t k = 0; k < o->pp.n; ++k) {
         int i = o->pp.a[k].i, j = o->pp.a[k].j, c = o->pp.a[k].lj;
         DX(i, j);
+        BOX_SHIFT(o->pp.a[k]);
         double r2 = 1.0 / (dx1 * dx1 + dx2 * dx2 + dx3 * dx3), r = sqrt(r2), r6 = r2 * r2 * r2;
         double Vel = d->crg[i] * d->crg[j] * r;
         if (c == 3) Vel *= d->el14_scale;
@@ -580,6 +677,7 @@ static void nonbond_pw(oracle *o) {
         double aLJ = avdw(o, d->iac[i], c) * avdw(o, d->iac[j], c);
         double bLJ = bvdw(o, d->iac[i], c) * bvdw(o, d->iac[j], c);
         DX(i, j);
+        BOX_SHIFT(o->pw.a[k]);
         double r2 = 1.0 / (dx1 * dx1 + dx2 * dx2 + dx3 * dx3), r = sqrt(r2), r6 = r2 * r2 * r2;
         double Vel = d->crg[i] * d->crg[j] * r, Va = aLJ * r6 * r6, Vb = bLJ * r6;
         double dv = r2 * (-Vel - 12.0 * Va + 6.0 * Vb);
@@ -596,6 +694,7 @@ static void nonbond_qp(oracle *o) {
         int iq = o->qp.a[k].i, i = d->iqseq[iq], j = o->qp.a[k].j, c = o->qp.a[k].lj, qc = o->qp.a[k].qlj;
         int tj = d->iac[j];
         DX(i, j);
+        BOX_SHIFT(o->qp.a[k]);
         double r2 = dx1 * dx1 + dx2 * dx2 + dx3 * dx3;
         if (!d->qvdw_flag) {
             r2 = 1.0 / r2;
@@ -643,6 +742,7 @@ static void nonbond_ww_spc(oracle *o) {
             int ja = j + ip;
             double q2 = d->chg_solv[ip];
             DX(i, ja);
+            BOX_SHIFT(o->ww.a[k]);
             double r2 = dx1 * dx1 + dx2 * dx2 + dx3 * dx3;
             double r6 = r2 * r2 * r2;
             r2 = 1.0 / r2;
@@ -673,6 +773,7 @@ static void nonbond_qw_spc(oracle *o) {
         int iq = o->qw.a[k].i, i = d->iqseq[iq], j = o->qw.a[k].j, c = o->qw.a[k].lj;
         {
             DX(i, j);
+            BOX_SHIFT(o->qw.a[k]);
             double r2 = dx1 * dx1 + dx2 * dx2 + dx3 * dx3;
             double r6hc = r2 * r2 * r2;
             r2 = 1.0 / r2;
@@ -702,6 +803,7 @@ static void nonbond_qw_spc(oracle *o) {
         for (int ip = 1; ip < 3; ++ip) {
             int ja = j + ip;
             DX(i, ja);
+            BOX_SHIFT(o->qw.a[k]);
             double r2 = 1.0 / (dx1 * dx1 + dx2 * dx2 + dx3 * dx3), r = sqrt(r2), dv = 0;
             for (int s = 0; s < o->S; ++s) {
                 double Vel = d->chg_solv[ip] * qcrg(o, iq, s) * r;
@@ -1068,6 +1170,9 @@ static void p_restrain_seq(oracle *o) {
                 if (!SEQ_SEL(i)) continue;
                 double dr[3] = { o->x[3 * i] - d->xtop[3 * i], o->x[3 * i + 1] - d->xtop[3 * i + 1],
                                  o->x[3 * i + 2] - d->xtop[3 * i + 2] };
+                /* the periodically minimal distance (:15561-15565) */
+                if (d->use_pbc)
+                    for (int a = 0; a < 3; ++a) dr[a] = dr[a] - pbc_shift(o, a, dr[a]);
                 o->E.rst_protein += 0.5 * fk * (dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
                 for (int a = 0; a < 3; ++a) o->f[3 * i + a] += fk * dr[a];
             }
@@ -1225,10 +1330,10 @@ void oracle_pot_energy(void *h, int terms, double *d_out, qgpu_energies *E_out, 
         o->E.w_improper = impropers(o, d->nimps_solute, d->nimps);
     }
     if (terms & QGPU_TERMS_RESTRAINT) {
-        /* pot_energy order, src/md.f90:16113-16125 */
-        fix_shell(o);
+        /* pot_energy order, src/md.f90:16113-16125; no sphere restraints in a box */
+        if (!d->use_pbc) fix_shell(o);
         p_restrain_seq(o);
-        if (d->nwat > 0) {
+        if (d->nwat > 0 && !d->use_pbc) {
             restrain_solvent(o);
             if (d->wpol_restr) watpol(o);
         }
@@ -1472,6 +1577,42 @@ static void nh_prop(oracle *o) {
     }
 }
 
+/* put_back_in_box, src/md.f90:18740-18857: the box centre follows the mean
+   solute position unless rigid_box_centre; every molecule of the selected
+   kind whose mass centre lies outside the box moves by one box length per
+   axis. */
+static void put_back_in_box(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    if (!d->rigid_box_centre) {
+        const int n = d->nat_solute > 0 ? d->nat_solute : d->natom;
+        double c[3] = { 0.0, 0.0, 0.0 };
+        for (int i = 0; i < n; ++i)
+            for (int a = 0; a < 3; ++a) c[a] += o->x[3 * i + a];
+        for (int a = 0; a < 3; ++a) o->boxc[a] = c[a] / n;
+    }
+    double hi[3], lo[3];
+    for (int a = 0; a < 3; ++a) {
+        hi[a] = o->boxc[a] + d->boxlength[a] / 2;
+        lo[a] = o->boxc[a] - d->boxlength[a] / 2;
+    }
+    const int m0 = d->put_solute_back ? 0 : d->nsolute_mol;
+    const int m1 = d->put_solvent_back ? d->nmol : d->nsolute_mol;
+    for (int m = m0; m < m1; ++m) {
+        const int a0 = o->istart_mol[m], a1 = m + 1 < d->nmol ? o->istart_mol[m + 1] : d->natom;
+        double cm[3] = { 0.0, 0.0, 0.0 }, mt = 0.0;
+        for (int j = a0; j < a1; ++j) mt += d->mass[d->iac[j]];
+        for (int j = a0; j < a1; ++j)
+            for (int a = 0; a < 3; ++a) cm[a] += o->x[3 * j + a] * d->mass[d->iac[j]];
+        for (int a = 0; a < 3; ++a) {
+            cm[a] = cm[a] * (1.0 / mt);
+            double mv = cm[a] > hi[a] ? -d->boxlength[a] : (cm[a] < lo[a] ? d->boxlength[a] : 0.0);
+            if (mv != 0.0)
+                for (int j = a0; j < a1; ++j) o->x[3 * j + a] = o->x[3 * j + a] + mv;
+        }
+    }
+}
+void oracle_put_back_in_box(void *h) { put_back_in_box((oracle *)h); }
+
 /* md_run, src/md.f90:6440-6664: thermostat constants before the loop, then
    per step lists (every NBcycle steps), pot_energy, offdiag, the thermostat's
    velocity/position update, SHAKE (+ a second nh_prop), temperature.  The step
@@ -1491,7 +1632,10 @@ int oracle_md_run(void *h, int32_t nsteps, int32_t terms, qgpu_energies *E_rows,
         for (int i = 0; i < o->N; ++i) o->randva[i] = sqrt(gkT / o->winv[i]);
     }
     for (int step = 0; step < nsteps; ++step, ++o->istep) {
-        if (o->istep % d->NBcycle == 0) oracle_make_pair_lists(o);
+        if (o->istep % d->NBcycle == 0) {
+            if (d->use_pbc && (d->put_solute_back || d->put_solvent_back)) put_back_in_box(o);
+            oracle_make_pair_lists(o);
+        }
         oracle_pot_energy(o, terms, NULL, NULL, NULL);
         if (d->noffd > 0) oracle_offdiag(o, NULL, NULL);
         if (d->thermostat == 1) {

@@ -73,6 +73,9 @@ class SystemDesc(C.Structure):
         ("wshell_theta_corr", _P), ("itdis_update", _i32),
         ("thermostat", _i32), ("integrator", _i32), ("friction", _f64), ("langevin_gauss", _i32),
         ("rand_state", _i32), ("nhchains", _i32), ("nhq", _f64),
+        ("use_pbc", _i32), ("boxlength", _f64 * 3), ("boxcentre", _f64 * 3), ("qswitch", _i32),
+        ("put_solute_back", _i32), ("put_solvent_back", _i32), ("rigid_box_centre", _i32),
+        ("nmol", _i32), ("istart_mol", _P), ("nsolute_mol", _i32),
     ]
 
 

@@ -142,6 +142,7 @@ static int validate(const qgpu_system_desc &d, int t) {
     if (d.solv_atom != 3) return fail(QGPU_E_UNSUPPORTED, "traj %d: only 3-site solvent is supported", t);
     if ((d.natom - d.nat_solute) % 3) return fail(QGPU_E_INVALID, "traj %d: solvent atoms not a multiple of 3", t);
     if (d.ivdw_rule != 1) return fail(QGPU_E_UNSUPPORTED, "traj %d: only the geometric LJ rule is supported", t);
+    if (d.use_pbc) return fail(QGPU_E_UNSUPPORTED, "traj %d: periodic box not supported by this build", t);
     if (d.nstates < 1 || d.nstates > QG_MAXS)
         return fail(QGPU_E_UNSUPPORTED, "traj %d: nstates %d outside 1..%d", t, d.nstates, QG_MAXS);
     if (d.nqat < 0 || d.nqat > QG_MAXQ) return fail(QGPU_E_UNSUPPORTED, "traj %d: nqat %d > %d", t, d.nqat, QG_MAXQ);

@@ -201,6 +201,10 @@ def read_top(text: str) -> dict:
     if ln.strip() == "":
         ln = r.line()
     nres = int(ln.split()[0])
+    # "nres nres_solute" (the second number only when some residues are solvent)
+    p2 = ln.split()
+    t["nres"] = nres
+    t["nres_solute"] = int(p2[1]) if len(p2) > 1 and re.fullmatch(r"\d+", p2[1]) else nres
     r.values(nres, int)
     r.skip()
     r.skip((nres + 15) // 16)
@@ -212,8 +216,18 @@ def read_top(text: str) -> dict:
     r.skip((natyps + 12) // 13)
     t["solvent_type"] = r.values(1, int)[0]
     ln = r.line().split()
-    if ln[0] == "PBC":
-        raise ValueError("periodic-box topologies are not supported (sphere only)")
+    t["use_pbc"] = ln[0] == "PBC"
+    if t["use_pbc"]:
+        # periodic box (src/topo.f90:1023-1031): box edges and centre; no
+        # excluded atoms and no sphere
+        t["boxlength"] = np.array(r.values(3, _f))
+        t["boxcentre"] = np.array(r.values(3, _f))
+        t["rexcl_o"], t["rwat"] = 0.0, 0.0
+        t["xpcent"] = t["boxcentre"].copy()
+        t["xwcent"] = t["boxcentre"].copy()
+        t["nexats"], t["nexwat"] = 0, 0
+        t["excl"] = np.zeros(nat, dtype=np.uint8)
+        return t
     if t["version"] < 5.01:
         t["rexcl_o"], t["rexcl_i_top"], t["rwat"] = _f(ln[0]), _f(ln[1]), _f(ln[2])
     else:
@@ -292,7 +306,14 @@ def read_inp(text: str) -> dict:
         return float(d[key]) if key in d else default
 
     wpol = onoff(solv.get("polarisation"), True)
+    # [PBC] (initialize, src/md.f90:4514-4590); constant pressure is not supported
+    pbc = kv("pbc")
     return {
+        "pbc": "pbc" in secs,
+        "put_solute_back_in_box": onoff(pbc.get("put_solute_back_in_box"), False),
+        "put_solvent_back_in_box": onoff(pbc.get("put_solvent_back_in_box"), False),
+        "rigid_box_centre": onoff(pbc.get("rigid_box_centre"), False),
+        "constant_pressure": onoff(pbc.get("constant_pressure"), False),
         "steps": int(md.get("steps", 0)),
         "stepsize": float(md.get("stepsize", 1.0)),
         "temperature": float(md.get("temperature", 300.0)),
@@ -332,7 +353,7 @@ def read_inp(text: str) -> dict:
         "topology": files.get("topology"),
         "fep": files.get("fep"),
         "unsupported": [s for s in secs if s in ("distance_restraints", "angle_restraints", "wall_restraints",
-                                                  "group_contribution", "pbc")],
+                                                  "group_contribution")],
     }
 
 
@@ -343,6 +364,10 @@ def read_fep(text: str) -> dict:
     kv = {ln.split(None, 1)[0].lower(): ln.split(None, 1)[1] for ln in secs.get("fep", []) if len(ln.split()) > 1}
     fep["nstates"] = int(kv.get("states", 1))
     offset = int(kv.get("offset", 0))
+    # [PBC] switching_atom: the atom the Q-atom lists are centred on in a
+    # periodic box (qatom_load_fep, src/qatom.f90:672-687)
+    pb = {ln.split(None, 1)[0].lower(): ln.split(None, 1)[1] for ln in secs.get("pbc", []) if len(ln.split()) > 1}
+    fep["qswitch"] = int(pb["switching_atom"]) + offset if "switching_atom" in pb else None
     if "offset_name" in kv or "offset_residue" in kv:
         raise ValueError("[FEP] offset_name/offset_residue are not supported")
     atoms = {}

@@ -141,6 +141,18 @@ class System:
         d.rand_state = int(g("rand_state", 1))
         d.nhchains = int(g("nhchains", 10))
         d.nhq = float(g("nhq", 0.001986 * self.Temp0 / (self.tau_T * self.tau_T)))
+        d.use_pbc = int(g("use_pbc", 0))
+        for k in range(3):
+            d.boxlength[k] = float(np.asarray(g("boxlength", np.zeros(3)))[k])
+            d.boxcentre[k] = float(np.asarray(g("boxcentre", np.zeros(3)))[k])
+        d.qswitch = int(g("qswitch", -1))
+        d.put_solute_back = int(g("put_solute_back", 0))
+        d.put_solvent_back = int(g("put_solvent_back", 0))
+        d.rigid_box_centre = int(g("rigid_box_centre", 0))
+        im = np.asarray(g("istart_mol", np.zeros(0, np.int32)), dtype=np.int32)
+        d.nmol = len(im)
+        d.istart_mol = arr(im, np.int32)
+        d.nsolute_mol = int(g("nsolute_mol", 0))
         return d
 
     @property
@@ -206,6 +218,13 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
     if inp["unsupported"]:
         raise ValueError(f"unsupported input sections: {inp['unsupported']}")
     natom, nsol = top["natom"], top["nat_solute"]
+    # periodic box: the topology's boundary and the input's [PBC] must agree
+    # (src/md.f90:17869-17872)
+    use_pbc = bool(top.get("use_pbc", False))
+    if use_pbc != bool(inp.get("pbc", False)):
+        raise ValueError("the boundary of the topology (sphere / PBC) and of the input must match")
+    if use_pbc and inp.get("constant_pressure"):
+        raise ValueError("[PBC] constant_pressure is not supported")
     natyps = len(top["mass"])
     cc = top["coulomb_constant"]
     sq = math.sqrt(cc)
@@ -228,7 +247,7 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
         rexcl_i *= rexcl_o
     shell = np.zeros(natom, dtype=np.uint8)
     xp = top["xpcent"]
-    for g in range(ncgp_solute):
+    for g in range(0 if use_pbc else ncgp_solute):
         s = cgp_switch[g]
         if not excl[s] and heavy[s]:
             if np.sum((xtop[3 * s:3 * s + 3] - xp) ** 2) > rexcl_i ** 2:
@@ -502,7 +521,7 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
     rstseq_flags = np.array([(ih, tc) for _, _, _, ih, tc in rs], dtype=np.int32).reshape(-1, 2)
 
     # --- water polarisation shells (wat_sphere / wat_shells, src/md.f90:18106-18368)
-    wpol = bool(inp["polarisation"]) and natom > nsol
+    wpol = bool(inp["polarisation"]) and natom > nsol and not use_pbc
     fkwpol = inp.get("polarisation_force", -1.0) if inp.get("polarisation_force", -1.0) != -1.0 else 20.0
     wshell = np.zeros((0, 4))
     if wpol:
@@ -528,7 +547,23 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
             rows.append((rout, dr, cstb, 0.0))
             rout = rout - dr
         wshell = np.array(rows, dtype=np.float64).reshape(-1, 4)
+    # --- periodic box: Q-atom switching atom and the molecules put_back_in_box moves
+    qswitch = -1
+    if use_pbc and nq:
+        if fep is None or fep.get("qswitch") is None:
+            raise ValueError("a periodic box with Q atoms needs [PBC] switching_atom in the FEP file")
+        qswitch = int(fep["qswitch"]) - 1
+    if use_pbc and inp["Rcq"] < 0:
+        raise ValueError("q_atom < 0 (all atoms on the Q lists) is not supported in a periodic box")
+    nsolvent_mol = int(top.get("nres", 0)) - int(top.get("nres_solute", top.get("nres", 0)))
+    box = dict(use_pbc=int(use_pbc), boxlength=np.asarray(top.get("boxlength", np.zeros(3)), dtype=np.float64),
+               boxcentre=np.asarray(top.get("boxcentre", np.zeros(3)), dtype=np.float64), qswitch=qswitch,
+               put_solute_back=int(inp.get("put_solute_back_in_box", False)),
+               put_solvent_back=int(inp.get("put_solvent_back_in_box", False)),
+               rigid_box_centre=int(inp.get("rigid_box_centre", False)),
+               istart_mol=np.asarray(istart[:-1], dtype=np.int32), nsolute_mol=nmol - nsolvent_mol)
     return System(
+        **box,
         natom=natom, nat_solute=nsol, natyps=natyps, ncgp_solute=ncgp_solute, nqat=nq, nstates=S,
         x=x, v=np.zeros(3 * natom), xtop=xtop, crg=crg, iac=iac, excl=excl, shell=shell, iqatom=iqatom,
         mass=mass, avdw=avdw, bvdw=bvdw, ljcod=ljcod, el14_scale=top["el14_scale"], ff_type=top["ff_type"],

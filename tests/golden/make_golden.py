@@ -18,6 +18,11 @@ reference's published step-0 values for the same systems:
   basic_sph_dynamics: rows 1-3 (step 0, step 50, final after 100 steps) of
              tests/basic_tests/SPH_{leap-frog,velocity-verlet}_{berendsen,
              langevin,nose-hoover}_benchmark.en
+  basic_pbc: tests/basic_tests/PBC_leap-frog_berendsen_benchmark.en row 1 with
+             tests/basic_tests/prep_PBC inputs and the PBC substitutions of
+             tests/basic_tests/run_test.sh:177-181 (periodic box, q_atom 24,
+             lrf 24)
+  basic_pbc_dynamics: rows 1-3 of the six PBC_*_benchmark.en band files
 """
 import json
 import os
@@ -41,11 +46,21 @@ def sph_inp(text: str) -> str:
             .replace("invalid-integrator", "leap-frog").replace("invalid-thermostat", "berendsen"))
 
 
+def pbc_inp(text: str, integrator: str = "leap-frog", thermostat: str = "berendsen") -> str:
+    """The substitutions run_test.sh applies for the PBC cases."""
+    return (text.replace("invalid-boundary", "[PBC]\nput_solvent_back_in_box\ton\nput_solute_back_in_box\toff")
+            .replace("invalid-qatom", "q_atom\t24").replace("invalid-lrf", "lrf\t24")
+            .replace("invalid-integrator", integrator).replace("invalid-thermostat", thermostat))
+
+
 def systems(ref: str):
     t = os.path.join(ref, "tests")
     yield "basic_sph", (_read(os.path.join(t, "basic_tests/prep_SPH/lig_w.top")),
                         _read(os.path.join(t, "basic_tests/prep_SPH/lig_w.fep")),
                         sph_inp(_read(os.path.join(t, "basic_tests/eq1.inp"))))
+    yield "basic_pbc", (_read(os.path.join(t, "basic_tests/prep_PBC/lig_w.top")),
+                        _read(os.path.join(t, "basic_tests/prep_PBC/lig_w.fep")),
+                        pbc_inp(_read(os.path.join(t, "basic_tests/eq1.inp"))))
     for name in ("test2", "test3"):
         yield name, (_read(os.path.join(t, name, "prep/lig_w.top")), _read(os.path.join(t, name, "prep/lig_w.fep")),
                      _read(os.path.join(t, name, "eq1.inp")))
@@ -86,6 +101,11 @@ def main(ref: str):
         f"{integ}/{thermo}": parse_benchmark_rows(
             os.path.join(ref, f"tests/basic_tests/SPH_{integ}_{thermo}_benchmark.en"))
         for integ in ("leap-frog", "velocity-verlet") for thermo in ("berendsen", "langevin", "nose-hoover")}
+    gold["basic_pbc_dynamics"] = {
+        f"{integ}/{thermo}": parse_benchmark_rows(
+            os.path.join(ref, f"tests/basic_tests/PBC_{integ}_{thermo}_benchmark.en"))
+        for integ in ("leap-frog", "velocity-verlet") for thermo in ("berendsen", "langevin", "nose-hoover")}
+    gold["basic_pbc"] = parse_benchmark_row1(os.path.join(ref, "tests/basic_tests/PBC_leap-frog_berendsen_benchmark.en"))
     for name, (top, fep, inp) in systems(ref):
         s = System.from_files(top, fep, inp)
         s.save_npz(os.path.join(HERE, f"{name}.npz"))

@@ -1,10 +1,12 @@
 """The FP64 oracle's MD loop against the reference's own dynamics bands.
 
-tests/basic_tests/SPH_<integrator>_<thermostat>_benchmark.en of the reference
-hold, per output row, the lower and upper value of 15 energy columns over the
-reference's benchmark runs of tests/basic_tests/eq1.inp (3,397-atom water
-sphere with the 46-atom ligand, 0.1 fs steps, T0 = 0.1 K, tau_T = 1 fs,
-sequence restraint on atoms 1-46, shell, radial and polarisation restraints).
+tests/basic_tests/{SPH,PBC}_<integrator>_<thermostat>_benchmark.en of the
+reference hold, per output row, the lower and upper value of 15 energy columns
+over the reference's benchmark runs of tests/basic_tests/eq1.inp (0.1 fs
+steps, T0 = 0.1 K, tau_T = 1 fs, sequence restraint on atoms 1-46): SPH is the
+3,397-atom water sphere with the 46-atom ligand (shell, radial and
+polarisation restraints); PBC the 12,262-atom periodic box (49.6 A, q_atom and
+lrf cut-offs 24 A, solvent put back in the box every list update).
 Rows 1-3 are step 0, step 50 and the final energies after 100 steps
 (tests/golden/golden.json, written by tests/golden/make_golden.py).
 
@@ -42,11 +44,11 @@ def columns(E, EQ):
     }
 
 
-def run_eq1(integrator: str, thermostat: str):
+def run_eq1(integrator: str, thermostat: str, boundary: str = "sph"):
     """qdyn's start-up (maxwell, initial shaking, stop_cm_translation,
     temperature) and 100 steps of eq1.inp with the oracle; rows 1-3."""
     from oracle.oracle import Oracle
-    s = golden_system("basic_sph")
+    s = golden_system(f"basic_{boundary}")
     s.thermostat = THERMO[thermostat]
     s.integrator = INTEG[integrator]
     o = Oracle(s)
@@ -62,9 +64,10 @@ def run_eq1(integrator: str, thermostat: str):
 
 @pytest.mark.parametrize("integrator", list(INTEG))
 @pytest.mark.parametrize("thermostat", list(THERMO))
-def test_md_rows_match_reference_bands(golden, integrator, thermostat):
-    bands = golden["basic_sph_dynamics"][f"{integrator}/{thermostat}"]
-    got = run_eq1(integrator, thermostat)
+@pytest.mark.parametrize("boundary", ["sph", "pbc"])
+def test_md_rows_match_reference_bands(golden, integrator, thermostat, boundary):
+    bands = golden[f"basic_{boundary}_dynamics"][f"{integrator}/{thermostat}"]
+    got = run_eq1(integrator, thermostat, boundary)
     bad = []
     for r in range(3):
         for c in COLS:

@@ -4,10 +4,13 @@ Pins (tests/golden/golden.json, written by tests/golden/make_golden.py):
   * tests/basic_tests/SPH_leap-frog_berendsen_benchmark.en row 1 of the
     reference: QEL QVdW EL VdW QBND QANG QTOR QIMP BND ANG TOR IMP (lower ==
     upper bound, printed to 0.01 kcal/mol);
+  * tests/basic_tests/PBC_leap-frog_berendsen_benchmark.en row 1: the same
+    12 columns for the periodic box (prep_PBC inputs, q_atom 24, lrf 24);
   * tests/test2/eval_test.sh:67 and tests/test3/eval_test.sh:67: the step-0
     "Q-surr." el/vdW line.
 Step 0 follows qdyn's start-up (src/qdyn.f90:126-132): maxwell, initial
-shaking, stop_cm_translation, then make_pair_lists and pot_energy.
+shaking, stop_cm_translation, then (in a box) put_back_in_box,
+make_pair_lists and pot_energy.
 """
 import os
 
@@ -24,6 +27,8 @@ def step0(system):
     o.maxwell(system.Tmaxw, int(system.seed))
     assert o.initial_shaking() == 0
     o.stop_cm_translation()
+    if getattr(system, "use_pbc", 0):
+        o.put_back_in_box()
     o.make_pair_lists()
     d, E, EQ = o.pot_energy()
     return o, d, E, EQ
@@ -39,7 +44,7 @@ def columns(E, EQ):
     }
 
 
-@pytest.mark.parametrize("name", ["basic_sph", "test2", "test3"])
+@pytest.mark.parametrize("name", ["basic_sph", "basic_pbc", "test2", "test3"])
 def test_step0_matches_reference_golden(name, golden):
     s = golden_system(name)
     _, _, E, EQ = step0(s)
