@@ -87,6 +87,13 @@ __device__ __forceinline__ bool within(float d2, float rc2, double drc2, const d
     if (d2 > rc2 * (1.f + 1e-5f)) return false;
     return dist2_exact(x, a, b) <= drc2;
 }
+// the same for a minimum-image distance in a periodic box
+__device__ __forceinline__ bool within_box(float d2, float rc2, double drc2, const double *x, int a, int b,
+                                           const TrajInfo &T) {
+    if (d2 < rc2 * (1.f - 1e-5f)) return true;
+    if (d2 > rc2 * (1.f + 1e-5f)) return false;
+    return dist2_exact_box(x, a, b, T) <= drc2;
+}
 // the same with a 1e-4 band, for distances from hi-only float coordinates
 __device__ __forceinline__ bool within_hi(float d2, float rc2, double drc2, const double *x, int a, int b) {
     if (d2 < rc2 * (1.f - 1e-4f)) return true;
@@ -122,6 +129,26 @@ __device__ __forceinline__ void lrf_acc(float (&acc)[QG_NLRF], const float4 p, f
     acc[23] += wxy * dz;
 }
 
+// lrf_update's periodic shift L*nint((x_sw - cent)/L) of a far source group
+// (switch atom sw at hi/lo sh/sl) about the target centre c (float offsets);
+// recomputed from the FP64 coordinates and centre when the float quotient is
+// within 1e-4 of a half-integer, where float rounding could pick the other image.
+__device__ __forceinline__ float3 lrf_box_shift(const DevSys &S, const TrajInfo &T, const float4 sh, const float4 sl,
+                                                float cx, float cy, float cz, int sw, int t) {
+    const float u[3] = {((sh.x - cx) + sl.x) * T.iboxf[0], ((sh.y - cy) + sl.y) * T.iboxf[1],
+                        ((sh.z - cz) + sl.z) * T.iboxf[2]};
+    float o[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float a = fabsf(u[k]);
+        float n = rintf(u[k]);
+        if (fabsf(a - floorf(a) - 0.5f) < 1e-4f)
+            n = (float)round((S.x[3 * sw + k] - S.g_cent[3 * t + k]) * T.ibox[k]);
+        o[k] = T.boxf[k] * n;
+    }
+    return make_float3(o[0], o[1], o[2]);
+}
+
 // Phase 1 of the scan: one thread per target charge group, one block per
 // (128 targets, source chunk of QG_TPC shared-memory tiles of the same
 // trajectory).  Near groups (inside the pp/pw/ww cut-off) go to the target's
@@ -129,7 +156,11 @@ __device__ __forceinline__ void lrf_acc(float (&acc)[QG_NLRF], const float4 p, f
 // groups inside RcLRF add their non-Q atoms to the target's multipole
 // expansion (lrf_update, src/md.f90:5896-5981), accumulated as 24 symmetric
 // FP32 sums per chunk.
-template <bool ANY>
+// PBC: the periodic-box form (nbpplist_box_lrf :8190, nbpwlist_box_lrf :9431,
+// nbwwlist_box_lrf :11023): minimum-image switch-atom distances, and each far
+// group's atoms shifted by the periodic image of its switch atom relative to
+// the target centre (lrf_update :5905-5917).
+template <bool ANY, bool PBC>
 __global__ void __launch_bounds__(QG_BLOCK, QG_SCAN_MINB) k_scan(DevSys S, const int *blk_t0, const int *blk_tn, const int *blk_traj,
                                                    const int *blk_chunk) {
     __shared__ float4 s_hi[QG_TILE_G], s_lo[QG_TILE_G];
@@ -214,6 +245,7 @@ __global__ void __launch_bounds__(QG_BLOCK, QG_SCAN_MINB) k_scan(DevSys S, const
                 else if (kind_t | kind_s) { rc2 = T.rc2_pw; drc2 = T.drc2_pw; }
                 else { rc2 = T.rc2_pp; drc2 = T.drc2_pp; }
                 float3 d = dpos(th, tl, s_hi[s], s_lo[s]);
+                if (PBC) d = f3sub(d, box_shift(T, d));
                 float d2 = d.x * d.x + d.y * d.y + d.z * d.z;
                 bool near_, far_lrf;
                 if (any_atom && !(kind_t & kind_s)) {
@@ -244,6 +276,9 @@ __global__ void __launch_bounds__(QG_BLOCK, QG_SCAN_MINB) k_scan(DevSys S, const
                         far_lrf = within_hi(d2hi(s_tp[lt][tid], s_atom[lk - ab]), rc2_lrf, T.drc2_lrf, S.x,
                                             s_ti[lt][tid], S.g_atoms[lk]);
                     }
+                } else if (PBC) {
+                    near_ = within_box(d2, rc2, drc2, S.x, rt, s_rep[s], T);
+                    far_lrf = !near_ && lrf && within_box(d2, rc2_lrf, T.drc2_lrf, S.x, rt, s_rep[s], T);
                 } else {
                     near_ = within(d2, rc2, drc2, S.x, rt, s_rep[s]);
                     far_lrf = !near_ && lrf && within(d2, rc2_lrf, T.drc2_lrf, S.x, rt, s_rep[s]);
@@ -255,18 +290,25 @@ __global__ void __launch_bounds__(QG_BLOCK, QG_SCAN_MINB) k_scan(DevSys S, const
                     else nbseg[QG_CAPC - 1 - cnts++] = g;
                 } else if (far_lrf) {
                     const int k0 = s_aoff[s];
+                    // in a box the expansion centre moves by the periodic
+                    // image of the source's switch atom (lrf_update :5905-5917)
+                    float ex = cx, ey = cy, ez = cz;
+                    if (PBC) {
+                        const float3 sh = lrf_box_shift(S, T, s_hi[s], s_lo[s], cx, cy, cz, s_rep[s], t);
+                        ex = cx + sh.x; ey = cy + sh.y; ez = cz + sh.z;
+                    }
                     if (kind_s) {
                         // a water: its three (charged) atoms unrolled, so their
                         // independent rsqrt chains overlap; same order of sums
                         const float4 p0 = s_atom[k0], p1 = s_atom[k0 + 1], p2 = s_atom[k0 + 2];
-                        lrf_acc(acc, p0, cx, cy, cz);
-                        lrf_acc(acc, p1, cx, cy, cz);
-                        lrf_acc(acc, p2, cx, cy, cz);
+                        lrf_acc(acc, p0, ex, ey, ez);
+                        lrf_acc(acc, p1, ex, ey, ez);
+                        lrf_acc(acc, p2, ex, ey, ez);
                     } else {
                         for (int k = k0; k < s_aoff[s + 1]; ++k) {
                             const float4 p = s_atom[k];
                             if (p.w == 0.f) continue;
-                            lrf_acc(acc, p, cx, cy, cz);
+                            lrf_acc(acc, p, ex, ey, ez);
                         }
                     }
                 }
@@ -349,6 +391,26 @@ __global__ void k_qmember(DevSys S, int first) {
     if (!first && T.q_static) return;
     if (T.nqat == 0) return;
     int sw = S.g_switch[g];
+    if (T.pbc) {
+        // nbqwlist_box :10554 / nbqplist_box :10327: within Rcq of the Q
+        // switching atom (minimum image); a solute group by any of its atoms,
+        // the first such atom fixing the group's periodic shift
+        const int q = T.qswitch;
+        int in_at = -1;
+        if (S.g_kind[g]) {
+            if (dist2_exact_box(S.x, sw, q, T) <= T.drcq2) in_at = sw;
+            S.qw_member[sw] = in_at >= 0 ? 1 : 0;
+        } else {
+            for (int k = S.g_start[g]; k < S.g_start[g + 1] && in_at < 0; ++k)
+                if (dist2_exact_box(S.x, S.g_atoms[k], q, T) <= T.drcq2) in_at = S.g_atoms[k];
+            S.g_qin[g] = in_at;
+            for (int k = S.g_start[g]; k < S.g_start[g + 1]; ++k) {
+                const int at = S.g_atoms[k];
+                S.qp_member[at] = (in_at >= 0 && !S.qp_skip[at]) ? 1 : 0;
+            }
+        }
+        return;
+    }
     double a = S.x[3 * sw] - T.xpcent[0], b = S.x[3 * sw + 1] - T.xpcent[1], c = S.x[3 * sw + 2] - T.xpcent[2];
     bool in = !S.g_excl[g] && (a * a + b * b + c * c <= T.drcq2);
     if (T.any_atom && !S.g_kind[g] && !S.g_excl[g]) {
@@ -370,7 +432,83 @@ __global__ void k_qmember(DevSys S, int first) {
     }
 }
 
+// put_back_in_box, src/md.f90:18740-18857: one block per box trajectory.  The
+// box centre follows the mean solute position (all atoms without solute)
+// unless rigid_box_centre; every selected molecule whose mass centre lies
+// outside the box moves by one box length per axis, in FP64 on x, and its
+// float coordinates (and water record) are re-formed.
+__global__ void k_put_back(DevSys S, const int *pb_traj) {
+    const int traj = pb_traj[blockIdx.x];
+    const TrajInfo &T = S.traj[traj];
+    __shared__ double red[3][256];
+    __shared__ double bc[3];
+    const int tid = threadIdx.x;
+    if (!T.rigid_box) {
+        const int n = T.nat_solute > 0 ? T.nat_solute : T.natom;
+        double c[3] = {0.0, 0.0, 0.0};
+        for (int i = tid; i < n; i += blockDim.x)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) c[a] += S.x[3 * (T.atom0 + i) + a];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) red[a][tid] = c[a];
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if (tid < w)
+#pragma unroll
+                for (int a = 0; a < 3; ++a) red[a][tid] += red[a][tid + w];
+            __syncthreads();
+        }
+        if (tid < 3) S.boxc[3 * traj + tid] = red[tid][0] / n;
+        __syncthreads();
+    }
+    if (tid < 3) bc[tid] = S.boxc[3 * traj + tid];
+    __syncthreads();
+    const int m0 = T.put_solute ? 0 : T.nsolute_mol, m1 = T.put_solvent ? T.nmol : T.nsolute_mol;
+    for (int m = m0 + tid; m < m1; m += blockDim.x) {
+        const int a0 = S.mol_start[T.mol0 + m], a1 = S.mol_start[T.mol0 + m + 1];
+        double cm[3] = {0.0, 0.0, 0.0}, mt = 0.0;
+        for (int j = a0; j < a1; ++j) mt += S.mass[j];
+        for (int j = a0; j < a1; ++j)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) cm[a] = __dadd_rn(cm[a], __dmul_rn(S.x[3 * j + a], S.mass[j]));
+        bool moved = false;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double c = __dmul_rn(cm[a], 1.0 / mt);
+            const double hi = bc[a] + T.box[a] / 2, lo = bc[a] - T.box[a] / 2;
+            const double mv = c > hi ? -T.box[a] : (c < lo ? T.box[a] : 0.0);
+            if (mv != 0.0) {
+                moved = true;
+                for (int j = a0; j < a1; ++j) S.x[3 * j + a] = S.x[3 * j + a] + mv;
+            }
+        }
+        if (!moved) continue;
+        for (int j = a0; j < a1; ++j) {
+            const double r0 = S.x[3 * j] - T.origin[0], r1 = S.x[3 * j + 1] - T.origin[1], r2 = S.x[3 * j + 2] - T.origin[2];
+            float4 h, l;
+            h.x = (float)r0; h.y = (float)r1; h.z = (float)r2; h.w = S.pos[j].w;
+            l.x = (float)(r0 - (double)h.x); l.y = (float)(r1 - (double)h.y); l.z = (float)(r2 - (double)h.z); l.w = 0.f;
+            S.pos[j] = h;
+            S.poslo[j] = l;
+        }
+        if (a1 - a0 == 3 && a0 >= T.atom0 + T.nat_solute) {
+            float4 h[3], l[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { h[k] = S.pos[a0 + k]; l[k] = S.poslo[a0 + k]; }
+            put_wrec(S.wrec + a0, h, l);
+        }
+    }
+}
+
 static inline int nblk(int n, int b) { return (n + b - 1) / b; }
+
+void launch_put_back(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
+    if (!B.npb) return;
+    prof_begin(L, "k_put_back");
+    k_put_back<<<B.npb, 256, 0, L.stream>>>(S, B.pb_traj);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
 
 void launch_wrec(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
     if (!B.nwgrp) return;
@@ -401,10 +539,13 @@ void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
 }
 void launch_scan(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
     prof_begin(L, "k_scan");
+    // a batch mixes no any-atom and box trajectories (refused at creation)
     if (B.any_atom)
-        k_scan<true><<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
+        k_scan<true, false><<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
+    else if (B.pbc)
+        k_scan<false, true><<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
     else
-        k_scan<false><<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
+        k_scan<false, false><<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
     prof_end(L);
     (*L.nlaunch)++;
     prof_begin(L, "k_scan_reduce");

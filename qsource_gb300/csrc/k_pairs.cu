@@ -37,11 +37,14 @@ __device__ __forceinline__ float lrf_atom(const float *ph, float dx, float dy, f
     return 0.5f * q * V;
 }
 
-// FP64 inverse distance from the master coordinates (accurate-energy mode)
-__device__ __forceinline__ double rinv_d(const double *x, int a, int b) {
-    const double dx = x[3 * b] - x[3 * a], dy = x[3 * b + 1] - x[3 * a + 1], dz = x[3 * b + 2] - x[3 * a + 2];
+// FP64 inverse distance from the master coordinates (accurate-energy mode),
+// of the difference x_b - x_a less the pair's periodic shift s (zero in a sphere)
+__device__ __forceinline__ double rinv_d(const double *x, int a, int b, const double3 s) {
+    const double dx = (x[3 * b] - x[3 * a]) - s.x, dy = (x[3 * b + 1] - x[3 * a + 1]) - s.y,
+                 dz = (x[3 * b + 2] - x[3 * a + 2]) - s.z;
     return rsqrt(dx * dx + dy * dy + dz * dz);
 }
+__device__ __forceinline__ double3 dzero3() { return make_double3(0.0, 0.0, 0.0); }
 
 // Energy accumulator: Kahan-summed FP32 partials, or FP64 terms.
 template <bool D>
@@ -107,9 +110,16 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
         for (int c = 0; c < 9; ++c) qq[c] = T.wwqq[c];
         r0 = S.wrec[a0]; r1 = S.wrec[a0 + 1]; r2 = S.wrec[a0 + 2];
         const float3 da[3] = {make_float3(0.f, 0.f, 0.f), make_float3(r0.w, r1.w, r2.x), make_float3(r2.y, r2.z, r2.w)};
+        const bool pbc = T.pbc != 0;
         auto ww = [&](int b0, const float4 q0, const float4 q1, const float4 q2) {
-            const float3 dO = make_float3((q0.x - r0.x) + (q1.x - r1.x), (q0.y - r0.y) + (q1.y - r1.y),
-                                          (q0.z - r0.z) + (q1.z - r1.z));
+            float3 dO = make_float3((q0.x - r0.x) + (q1.x - r1.x), (q0.y - r0.y) + (q1.y - r1.y),
+                                    (q0.z - r0.z) + (q1.z - r1.z));
+            // box: the O-O image fixes all nine pairs (nonbond_ww_spc_box :15187-15193)
+            double3 shd = dzero3();
+            if (pbc) {
+                dO = f3sub(dO, box_shift(T, dO));
+                if (EACC) shd = box_shift_d(T, S.x, a0, b0);
+            }
             const float3 db[3] = {make_float3(0.f, 0.f, 0.f), make_float3(q0.w, q1.w, q2.x),
                                   make_float3(q2.y, q2.z, q2.w)};
 #pragma unroll
@@ -123,7 +133,7 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
                     const float Vel = qq[3 * a + b] * ri;
                     float dv = -Vel * ri2;
                     double rid = 0.0;
-                    if (EACC) rid = rinv_d(S.x, a0 + a, b0 + b);
+                    if (EACC) rid = rinv_d(S.x, a0 + a, b0 + b, shd);
                     if (a == 0 && b == 0) {
                         const float r6 = ri2 * ri2 * ri2;
                         const float Va = wwA * r6 * r6, Vb = wwB * r6;
@@ -162,12 +172,21 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
         const float4 oh = make_float4(r0.x, r0.y, r0.z, 0.f), ol = make_float4(r1.x, r1.y, r1.z, 0.f);
         for (int kk = nw + lane; kk < n; kk += LW) {
             const int g = lst[kk];
+            // box: the image of the group's switch atom relative to this O
+            // (nonbond_pw_box :13395-13405)
+            float3 sg = make_float3(0.f, 0.f, 0.f);
+            double3 sgd = dzero3();
+            if (pbc) {
+                const int sw = S.g_switch[g];
+                sg = box_shift(T, dpos(oh, ol, S.pos[sw], S.poslo[sw]));
+                if (EACC) sgd = box_shift_d(T, S.x, a0, sw);
+            }
             for (int q = S.g_start[g]; q < S.g_start[g + 1]; ++q) {
                 const int b = S.g_atoms[q];
                 if (S.aq[b] >= 0) continue;
                 const float4 bh = S.pos[b], bl = S.poslo[b];
                 const int tb = S.atype[b];
-                const float3 dO = dpos(oh, ol, bh, bl);
+                const float3 dO = f3sub(dpos(oh, ol, bh, bl), sg);
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
                     const int c = ljc(S, T, ta[a], tb);
@@ -180,7 +199,7 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
                     const float dv = ri2 * (-Vel - 12.f * Va + 6.f * Vb);
                     double eld = 0.0, evd = 0.0;
                     if (EACC) {
-                        const double rid = rinv_d(S.x, a0 + a, b), r6d = rid * rid * rid * rid * rid * rid;
+                        const double rid = rinv_d(S.x, a0 + a, b, sgd), r6d = rid * rid * rid * rid * rid * rid;
                         eld = qd[a] * S.crg_d[b] * rid;
                         evd = S.avdw_d[ta[a] * 3 + c - 1] * S.avdw_d[tb * 3 + c - 1] * r6d * r6d -
                               S.bvdw_d[ta[a] * 3 + c - 1] * S.bvdw_d[tb * 3 + c - 1] * r6d;
@@ -272,13 +291,17 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         const int ti = S.atype[i];
         const double qi = EACC ? S.crg_d[i] : 0.0;
         const float el14 = T.el14;
-        // one pair term: LJ code c, el14 factor for 1-4 pairs (nonbond_pp :13102-13111)
-        auto pair = [&](int j, int c, EAcc<EACC> &e_el, EAcc<EACC> &e_vdw) {
+        const bool pbc = T.pbc != 0;
+        const int swg = S.g_switch[g];
+        const float4 swh = S.pos[swg], swl = S.poslo[swg];
+        // one pair term: LJ code c, el14 factor for 1-4 pairs (nonbond_pp :13102-13111),
+        // periodic shift (sf, sd) of the group pair (nonbond_pp_box :13226-13228)
+        auto pair = [&](int j, int c, EAcc<EACC> &e_el, EAcc<EACC> &e_vdw, const float3 sf, const double3 sd) {
             const int tj = S.atype[j];
             const float4 jh = S.pos[j], jl = S.poslo[j];
             const float A = S.avdw[ti * 3 + c - 1] * S.avdw[tj * 3 + c - 1];
             const float B = S.bvdw[ti * 3 + c - 1] * S.bvdw[tj * 3 + c - 1];
-            const float3 d = dpos(ih, il, jh, jl);
+            const float3 d = f3sub(dpos(ih, il, jh, jl), sf);
             const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
             const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
             float Vel = ih.w * jh.w * ri;
@@ -287,7 +310,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
             const float dv = ri2 * (-Vel - 12.f * Va + 6.f * Vb);
             double eld = 0.0, evd = 0.0;
             if (EACC) {
-                const double rid = rinv_d(S.x, i, j), r6d = rid * rid * rid * rid * rid * rid;
+                const double rid = rinv_d(S.x, i, j, sd), r6d = rid * rid * rid * rid * rid * rid;
                 eld = qi * S.crg_d[j] * rid;
                 if (c == 3) eld *= (double)T.el14d;
                 evd = S.avdw_d[ti * 3 + c - 1] * S.avdw_d[tj * 3 + c - 1] * r6d * r6d -
@@ -297,15 +320,16 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
             gx -= dv * d.x; gy -= dv * d.y; gz -= dv * d.z;
         };
         // pp pair with exclusion / 1-4 handling (nbpplist_lrf :8108-8166)
-        auto pp = [&](int j) {
+        auto pp = [&](int j, const float3 sf, const double3 sd) {
             const PairFlags f = pair_flags(S, i, j);
             if (f.excl) return;
-            pair(j, f.p14 ? 3 : ljc(S, T, ti, S.atype[j]), epp_el, epp_vdw);
+            pair(j, f.p14 ? 3 : ljc(S, T, ti, S.atype[j]), epp_el, epp_vdw, sf, sd);
         };
+        const float3 zf = make_float3(0.f, 0.f, 0.f);
         for (int kk = S.g_start[g] + lane; kk < S.g_start[g + 1]; kk += LW) {
             const int j = S.g_atoms[kk];
             if (j == i || S.aq[j] >= 0) continue;
-            pp(j);
+            pp(j, zf, dzero3());
         }
         epp_el.flush(); epp_vdw.flush();
         const int n = S.nb_count[g], nw = S.nb_nw[g];
@@ -326,7 +350,14 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         for (int k = lane; k < nw; k += LW) {
             const int b0 = lst[k];
             const float4 w0 = S.wrec[b0], w1 = S.wrec[b0 + 1], w2 = S.wrec[b0 + 2];
-            const float3 dO = dpos(ih, il, make_float4(w0.x, w0.y, w0.z, 0.f), make_float4(w1.x, w1.y, w1.z, 0.f));
+            const float4 oh = make_float4(w0.x, w0.y, w0.z, 0.f), ol = make_float4(w1.x, w1.y, w1.z, 0.f);
+            float3 dO = dpos(ih, il, oh, ol);
+            // box: the O image relative to this group's switch atom (nonbond_pw_box)
+            double3 sgd = dzero3();
+            if (pbc) {
+                dO = f3sub(dO, box_shift(T, dpos(swh, swl, oh, ol)));
+                if (EACC) sgd = box_shift_d(T, S.x, swg, b0);
+            }
             const float3 dk[3] = {make_float3(0.f, 0.f, 0.f), make_float3(w0.w, w1.w, w2.x), make_float3(w2.y, w2.z, w2.w)};
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
@@ -338,7 +369,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
                 double eld = 0.0, evd = 0.0;
                 if (EACC) {
                     const int j = b0 + b, tj = S.atype[j];
-                    const double rid = rinv_d(S.x, i, j), r6d = rid * rid * rid * rid * rid * rid;
+                    const double rid = rinv_d(S.x, i, j, sgd), r6d = rid * rid * rid * rid * rid * rid;
                     eld = qi * S.crg_d[j] * rid;
                     evd = S.avdw_d[ti * 3 + cw[b] - 1] * S.avdw_d[tj * 3 + cw[b] - 1] * r6d * r6d -
                           S.bvdw_d[ti * 3 + cw[b] - 1] * S.bvdw_d[tj * 3 + cw[b] - 1] * r6d;
@@ -350,10 +381,17 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         }
         for (int k = nw + lane; k < n; k += LW) {
             const int h = lst[k];
+            float3 sf = zf;
+            double3 sd = dzero3();
+            if (pbc) {
+                const int swn = S.g_switch[h];
+                sf = box_shift(T, dpos(swh, swl, S.pos[swn], S.poslo[swn]));
+                if (EACC) sd = box_shift_d(T, S.x, swg, swn);
+            }
             for (int kk = S.g_start[h]; kk < S.g_start[h + 1]; ++kk) {
                 const int j = S.g_atoms[kk];
                 if (S.aq[j] >= 0) continue;
-                pp(j);
+                pp(j, sf, sd);
             }
             epp_el.flush(); epp_vdw.flush();
         }
@@ -492,6 +530,13 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
     if (valid)
 #pragma unroll
         for (int a = 0; a < 3; ++a) { ah[a] = S.pos[a0 + a]; al[a] = S.poslo[a0 + a]; }
+    // box: the O image relative to the Q switching atom (nonbond_qw_spc_box :14612-14618)
+    float3 sw = make_float3(0.f, 0.f, 0.f);
+    double3 swd = dzero3();
+    if (valid && T.pbc) {
+        sw = box_shift(T, dpos(S.pos[T.qswitch], S.poslo[T.qswitch], ah[0], al[0]));
+        if (acc) swd = box_shift_d(T, S.x, T.qswitch, a0);
+    }
     float gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0}, gz[3] = {0, 0, 0};
     float lam[QG_MAXS];
 #pragma unroll
@@ -506,11 +551,11 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
             const int qa = S.q_atom[q];
             // O: Coulomb + LJ (softcore column = LJ code of the pair, src/md.f90:14492)
             {
-                const float3 d = dpos(sh.qh[iq], sh.ql[iq], ah[0], al[0]);
+                const float3 d = f3sub(dpos(sh.qh[iq], sh.ql[iq], ah[0], al[0]), sw);
                 const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
                 const float r6hc = r2 * r2 * r2, ri = rsqrtf(r2), ri2 = ri * ri;
                 double rid = 0.0, r6hcd = 0.0;
-                if (acc) { rid = rinv_d(S.x, qa, a0); const double r2d = 1.0 / (rid * rid); r6hcd = r2d * r2d * r2d; }
+                if (acc) { rid = rinv_d(S.x, qa, a0, swd); const double r2d = 1.0 / (rid * rid); r6hcd = r2d * r2d * r2d; }
                 float dv = 0.f;
 #pragma unroll
                 for (int s = 0; s < QG_MAXS; ++s) {
@@ -535,10 +580,10 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
             }
 #pragma unroll
             for (int a = 1; a < 3; ++a) {
-                const float3 d = dpos(sh.qh[iq], sh.ql[iq], ah[a], al[a]);
+                const float3 d = f3sub(dpos(sh.qh[iq], sh.ql[iq], ah[a], al[a]), sw);
                 const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
                 const float ri = rsqrtf(r2), ri2 = ri * ri;
-                const double rid = acc ? rinv_d(S.x, qa, a0 + a) : 0.0;
+                const double rid = acc ? rinv_d(S.x, qa, a0 + a, swd) : 0.0;
                 float dv = 0.f;
 #pragma unroll
                 for (int s = 0; s < QG_MAXS; ++s) {
@@ -586,6 +631,15 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
     float4 jh = {}, jl = {};
     int tj = 0;
     if (valid) { jh = S.pos[j]; jl = S.poslo[j]; tj = S.atype[j]; }
+    // box: the image of the atom that put this group on the list, relative to
+    // the Q switching atom (nonbond_qp_box :13960-13969)
+    float3 sq = make_float3(0.f, 0.f, 0.f);
+    double3 sqd = dzero3();
+    if (valid && T.pbc) {
+        const int in = S.g_qin[S.agrp[j]];
+        sq = box_shift(T, dpos(S.pos[T.qswitch], S.poslo[T.qswitch], S.pos[in], S.poslo[in]));
+        if (acc) sqd = box_shift_d(T, S.x, T.qswitch, in);
+    }
     float gx = 0.f, gy = 0.f, gz = 0.f;
     const int ntq = T.natyps + T.nqat;
     for (int iq0 = 0; iq0 < T.nqat; iq0 += LG) {
@@ -600,11 +654,11 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
             for (int k = S.qp14_first[j]; k < S.qp14_first[j + 1]; ++k)
                 if (S.qp14_q[k] == q) c = 3;
             const int qc = c == 2 ? 1 : c;
-            const float3 d = dpos(sh.qh[iq], sh.ql[iq], jh, jl);
+            const float3 d = f3sub(dpos(sh.qh[iq], sh.ql[iq], jh, jl), sq);
             const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
             const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = r2 * r2 * r2;
             double rid = 0.0, r6d = 0.0;
-            if (acc) { rid = rinv_d(S.x, qa, j); const double r2d = 1.0 / (rid * rid); r6d = r2d * r2d * r2d; }
+            if (acc) { rid = rinv_d(S.x, qa, j, sqd); const double r2d = 1.0 / (rid * rid); r6d = r2d * r2d * r2d; }
             float dv = 0.f;
 #pragma unroll
             for (int s = 0; s < QG_MAXS; ++s) {

@@ -394,7 +394,8 @@ __device__ void fix_shell_block(const DevSys &S, int b, const int *satom, Red &r
     const int traj = i < 0 ? -1 - i : S.atraj[i];
     const TrajInfo &T = S.traj[traj];
     R efix = 0, eshell = 0;
-    if (i >= 0 && (S.aexcl[i] || S.ashell[i])) {
+    // sphere only (pot_energy :16114-16116)
+    if (i >= 0 && !T.pbc && (S.aexcl[i] || S.ashell[i])) {
         R fk, d0, d1, d2;
         if (sizeof(R) == 8) {
             fk = S.aexcl[i] ? R(T.fk_fix) : R(T.fk_pshell);
@@ -424,7 +425,8 @@ __device__ void restrain_solvent_block(const DevSys &S, int b, const int *wgrp, 
     const int traj = w < 0 ? -1 - w : S.g_traj[w];
     const TrajInfo &T = S.traj[traj];
     R erst = 0;
-    if (w >= 0) {
+    // sphere only (pot_energy :16120-16124)
+    if (w >= 0 && !T.pbc) {
         const int i = S.g_switch[w];
         if (!S.aexcl[i]) {
             R d0, d1, d2, fk, rwat, Dwmz, awmz, shift;
@@ -520,6 +522,18 @@ __device__ void seqrst_block(const DevSys &S, int b, Red &red) {
             if (!sel(i)) continue;
             R d0, d1, d2;
             disp(i, d0, d1, d2);
+            if (T.pbc) {
+                // the periodically minimal distance (:15561-15565)
+                if (sizeof(R) == 8) {
+                    d0 = d0 - R(T.box[0] * round(double(d0) * T.ibox[0]));
+                    d1 = d1 - R(T.box[1] * round(double(d1) * T.ibox[1]));
+                    d2 = d2 - R(T.box[2] * round(double(d2) * T.ibox[2]));
+                } else {
+                    d0 = d0 - R(T.boxf[0] * rintf(float(d0) * T.iboxf[0]));
+                    d1 = d1 - R(T.boxf[1] * rintf(float(d1) * T.iboxf[1]));
+                    d2 = d2 - R(T.boxf[2] * rintf(float(d2) * T.iboxf[2]));
+                }
+            }
             e += R(0.5) * fk * (d0 * d0 + d1 * d1 + d2 * d2);
             p::grad(S, i, fk * d0, fk * d1, fk * d2);
         }

@@ -142,7 +142,23 @@ static int validate(const qgpu_system_desc &d, int t) {
     if (d.solv_atom != 3) return fail(QGPU_E_UNSUPPORTED, "traj %d: only 3-site solvent is supported", t);
     if ((d.natom - d.nat_solute) % 3) return fail(QGPU_E_INVALID, "traj %d: solvent atoms not a multiple of 3", t);
     if (d.ivdw_rule != 1) return fail(QGPU_E_UNSUPPORTED, "traj %d: only the geometric LJ rule is supported", t);
-    if (d.use_pbc) return fail(QGPU_E_UNSUPPORTED, "traj %d: periodic box not supported by this build", t);
+    if (d.use_pbc) {
+        // the box forms cover the switch-atom lists (nb*list_box*); the
+        // any-atom box lists of the reference shift by a different atom pair
+        if (d.any_atom_lists)
+            return fail(QGPU_E_UNSUPPORTED, "traj %d: periodic box with any-atom lists (iuse_switch_atom = 0)", t);
+        for (int k = 0; k < 3; ++k)
+            if (!(d.boxlength[k] > 0.0)) return fail(QGPU_E_INVALID, "traj %d: box length %d not > 0", t, k);
+        if (d.nqat > 0 && (d.qswitch < 0 || d.qswitch >= d.natom))
+            return fail(QGPU_E_INVALID, "traj %d: Q switching atom %d outside the system", t, d.qswitch);
+        if (d.Rcq < 0.0) return fail(QGPU_E_UNSUPPORTED, "traj %d: q_atom cut-off < 0 in a periodic box", t);
+        if ((d.put_solute_back || d.put_solvent_back) &&
+            (d.nmol < 1 || !d.istart_mol || d.nsolute_mol < 0 || d.nsolute_mol > d.nmol))
+            return fail(QGPU_E_INVALID, "traj %d: molecules needed to put them back in the box", t);
+        for (int m = 0; (d.put_solute_back || d.put_solvent_back) && m < d.nmol; ++m)
+            if (d.istart_mol[m] < 0 || d.istart_mol[m] >= d.natom || (m && d.istart_mol[m] <= d.istart_mol[m - 1]))
+                return fail(QGPU_E_INVALID, "traj %d: molecule %d start", t, m);
+    }
     if (d.nstates < 1 || d.nstates > QG_MAXS)
         return fail(QGPU_E_UNSUPPORTED, "traj %d: nstates %d outside 1..%d", t, d.nstates, QG_MAXS);
     if (d.nqat < 0 || d.nqat > QG_MAXQ) return fail(QGPU_E_UNSUPPORTED, "traj %d: nqat %d > %d", t, d.nqat, QG_MAXQ);
@@ -197,6 +213,8 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     std::vector<int> wgrp, satom, scan_t0, scan_tn, scan_traj, scan_chunk, uitem, qqblk_traj, qqblk_s;
     // sequence restraints, water polarisation
     std::vector<int> rs_i0, rs_i1, rs_ih, rs_tc, rs_traj, wp_traj, wp_scr0;
+    std::vector<int> mol_start, pb_traj;     // periodic box: molecules, put_back_in_box trajectories
+    std::vector<double> boxc0;
     std::vector<double> rs_fk, wp_state;
     std::vector<uint8_t> aheavy;
     long long wp_scr_n = 0;
@@ -252,6 +270,24 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         }
         T.separate_scaling = d.separate_scaling; T.detail_temps = d.detail_temps;
         T.any_atom = d.any_atom_lists ? 1 : 0;
+        // --- periodic box (the Q lists follow the switching atom: rebuilt with every list)
+        for (int k = 0; k < 3; ++k) boxc0.push_back(d.use_pbc ? d.boxcentre[k] : 0.0);
+        if (d.use_pbc) {
+            T.pbc = 1; T.q_static = 0;
+            T.qswitch = nq > 0 ? atom0 + d.qswitch : -1;
+            for (int k = 0; k < 3; ++k) {
+                T.box[k] = d.boxlength[k]; T.ibox[k] = 1.0 / d.boxlength[k];
+                T.boxf[k] = (float)T.box[k]; T.iboxf[k] = (float)T.ibox[k];
+            }
+            T.put_solute = d.put_solute_back; T.put_solvent = d.put_solvent_back;
+            T.rigid_box = d.rigid_box_centre;
+            if (d.put_solute_back || d.put_solvent_back) {
+                T.mol0 = (int)mol_start.size(); T.nmol = d.nmol; T.nsolute_mol = d.nsolute_mol;
+                for (int m = 0; m < d.nmol; ++m) mol_start.push_back(atom0 + d.istart_mol[m]);
+                mol_start.push_back(atom0 + N);
+                pb_traj.push_back(t);
+            }
+        }
         T.Ndegf = d.Ndegf; T.Ndegfree = d.Ndegfree;
         T.Ndegfree_solute = d.Ndegfree_solute; T.Ndegfree_solvent = d.Ndegfree_solvent;
         T.ff_type = d.ff_type;
@@ -735,6 +771,12 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     UP(qw_lj, qw_lj); UP(qw_Ad, qw_Ad); UP(qw_Bd, qw_Bd);
     if ((rc = alloc0(A, (size_t)atom0, &S.qw_member))) return rc;
     if ((rc = alloc0(A, (size_t)atom0, &S.qp_member))) return rc;
+    {
+        std::vector<int> gq(grp0, -1);
+        UP(gq, g_qin);
+        UP(mol_start, mol_start);
+        UP(boxc0, boxc);
+    }
     UP(qp_skip, qp_skip); UP(qp14_first, qp14_first); UP(qp14_q, qp14_q);
     UP(qq_iq, qq_iq); UP(qq_j, qq_j); UP(qq_jq, qq_jq); UP(qq_lj, qq_lj); UP(qq_els, qq_els);
     UP(qt_atoms, qt_atoms); UP(qt_cod, qt_cod); UP(qt_kind, qt_kind); UP(qt_traj, qt_traj); UP(qt_lib, qt_lib);
@@ -795,6 +837,14 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         B.max_nqat = 0;
         for (int t = 0; t < ntraj; ++t) B.max_nqat = std::max(B.max_nqat, h->info[t].nqat);
         for (int t = 0; t < ntraj; ++t) B.any_atom |= h->info[t].any_atom;
+        for (int t = 0; t < ntraj; ++t) B.pbc |= h->info[t].pbc;
+        if (B.any_atom && B.pbc)
+            return fail(QGPU_E_UNSUPPORTED, "a batch cannot mix any-atom lists and periodic boxes");
+        B.npb = (int)pb_traj.size();
+        if (B.npb) {
+            int *p_;
+            if ((rc = upload(A, pb_traj, &p_))) return rc; B.pb_traj = p_;
+        }
         B.nwp = (int)wp_traj.size();
         if (B.nwp) {
             int *p_;
@@ -854,7 +904,10 @@ static void temperature_init(qgpu_handle *h, LaunchCtx &L) {
     else { launch_update(h->S, h->B, L, 0); launch_wrec(h->S, h->B, L); }
 }
 
-static void list_ops(qgpu_handle *h, LaunchCtx &L) {
+// md: a list build of the MD loop, which first puts molecules back in the box
+// (md_run :6483-6485); qgpu_build_lists alone is make_pair_lists.
+static void list_ops(qgpu_handle *h, LaunchCtx &L, bool md = true) {
+    if (md) launch_put_back(h->S, h->B, L);
     launch_centers(h->S, h->B, L);
     launch_scan(h->S, h->B, L);
     launch_qmember(h->S, h->B, L, h->lists_built ? 0 : 1);
@@ -1035,7 +1088,7 @@ int qgpu_build_lists(qgpu_handle *h) {
     if (!h) return fail(QGPU_E_INVALID, "null handle");
     LaunchCtx L{h->stream, &h->nlaunch};
     ensure_double(h, L);
-    list_ops(h, L);
+    list_ops(h, L, false);
     h->lists_built = 1;
     return check_status(h);
 }

@@ -123,6 +123,13 @@ struct TrajInfo {
     // window has neighbours (has_f / has_r) with lambdas lamf / lamr
     int fep_on, fep_has_f, fep_has_r, fep_nskip;
     double fep_kT, fep_lamf[QG_MAXS], fep_lamr[QG_MAXS];
+    // periodic box (use_pbc): edges and inverse edges, the Q switching atom
+    // (global index), the molecules put_back_in_box may move (DevSys::mol_start
+    // from mol0, nmol of them, the first nsolute_mol solute) and which kinds
+    int pbc, qswitch, put_solute, put_solvent, rigid_box;
+    int mol0, nmol, nsolute_mol;
+    float boxf[3], iboxf[3];
+    double box[3], ibox[3];
 };
 #define QG_NFEP 9                // FEP accumulators per trajectory (see k_finalize)
 
@@ -211,6 +218,9 @@ struct DevSys {
     const int *qw_lj;               // [q] LJ code of the water-O / Q-atom pair
     uint8_t *qw_member;             // per water (global water index) in the qw list
     uint8_t *qp_member;             // per atom in the qp list
+    int *g_qin;                     // per solute group in a box: the atom that put it on the qp list (its shift)
+    const int *mol_start;           // molecules of the box trajectories: first atom (global); TrajInfo::mol0
+    double *boxc;                   // per trajectory: box centre (put_back_in_box)
     const uint8_t *qp_skip;
     const int *qp14_first, *qp14_q; // per atom CSR of Q atoms with qconn == 4
     // nbqq
@@ -427,6 +437,37 @@ __device__ __forceinline__ void langevin_force(const DevSys &S, const TrajInfo &
         }
     }
 }
+// Periodic box.  The shift of a difference d is L*nint(d/L) per component
+// (boxlength*nint(d*inv_boxl), every box routine of src/md.f90); the float
+// form rounds to nearest-even, which differs from nint only at exact
+// half-integers (components of exactly half a box, far outside every cut-off).
+__device__ __forceinline__ float3 box_shift(const TrajInfo &T, const float3 d) {
+    return make_float3(T.boxf[0] * rintf(d.x * T.iboxf[0]), T.boxf[1] * rintf(d.y * T.iboxf[1]),
+                       T.boxf[2] * rintf(d.z * T.iboxf[2]));
+}
+__device__ __forceinline__ float3 f3sub(const float3 a, const float3 b) {
+    return make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
+}
+// FP64 shift of x[b] - x[a] in the reference's operation order
+__device__ __forceinline__ double3 box_shift_d(const TrajInfo &T, const double *x, int a, int b) {
+    double3 s;
+    s.x = __dmul_rn(T.box[0], round(__dmul_rn(__dsub_rn(x[3 * b], x[3 * a]), T.ibox[0])));
+    s.y = __dmul_rn(T.box[1], round(__dmul_rn(__dsub_rn(x[3 * b + 1], x[3 * a + 1]), T.ibox[1])));
+    s.z = __dmul_rn(T.box[2], round(__dmul_rn(__dsub_rn(x[3 * b + 2], x[3 * a + 2]), T.ibox[2])));
+    return s;
+}
+// exact FP64 minimum-image squared distance (nbpplist_box_lrf src/md.f90:
+// 8282-8288: dx = dx - boxlength*nint(dx*inv_boxl), r2 = dx**2+dy**2+dz**2)
+__device__ __forceinline__ double dist2_exact_box(const double *x, int i, int j, const TrajInfo &T) {
+    double c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double a = __dsub_rn(x[3 * i + k], x[3 * j + k]);
+        c[k] = __dsub_rn(a, __dmul_rn(T.box[k], round(__dmul_rn(a, T.ibox[k]))));
+    }
+    return __dadd_rn(__dadd_rn(__dmul_rn(c[0], c[0]), __dmul_rn(c[1], c[1])), __dmul_rn(c[2], c[2]));
+}
+
 // exact FP64 squared distance in the reference's operation order (no FMA)
 __device__ __forceinline__ double dist2_exact(const double *x, int i, int j) {
     double a = __dsub_rn(x[3 * i], x[3 * j]);
@@ -467,11 +508,16 @@ struct BlockTables {
     // water polarisation: trajectories with the restraint, their scratch
     const int *wp_traj, *wp_scr0; double *wp_scr; int nwp;
     int any_atom;                      // some trajectory uses the any-atom cut-off
+    int pbc;                           // some trajectory is a periodic box
+    // put_back_in_box: one block per trajectory that moves molecules
+    const int *pb_traj; int npb;
 };
 
 void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_scan(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_qmember(const DevSys &S, const BlockTables &B, LaunchCtx &L, int first);
+// put_back_in_box (src/md.f90:18740-18857) of the box trajectories, before a list build of the MD loop
+void launch_put_back(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 // Energy accuracy: EACC_FP32 sums FP32 pair energies (Kahan + FP64 block
 // sums); EACC_FP64 evaluates every pair energy in FP64 from the master
 // coordinates (forces are FP32 in both); EACC_RECORD uses FP64 on the steps
