@@ -72,7 +72,9 @@ struct EAcc<true> {
 // (13282-13365) and lrf_taylor for the three water atoms.
 // LW lanes share one water: lane l takes neighbours l, l+LW, ...; the
 // lanes' partial gradients are summed by an xor butterfly (fixed order).
-template <bool EACC, int LW, int MINB, int U>
+// BOX: some trajectory of the batch is a periodic box (its kernels subtract
+// the pair shifts; sphere trajectories of the batch have a zero box).
+template <bool EACC, int LW, int MINB, int U, bool BOX>
 __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int *wgrp, int lrf) {
     __shared__ long long red[5][QG_BLOCK / 32];
     const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LW;
@@ -110,7 +112,7 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
         for (int c = 0; c < 9; ++c) qq[c] = T.wwqq[c];
         r0 = S.wrec[a0]; r1 = S.wrec[a0 + 1]; r2 = S.wrec[a0 + 2];
         const float3 da[3] = {make_float3(0.f, 0.f, 0.f), make_float3(r0.w, r1.w, r2.x), make_float3(r2.y, r2.z, r2.w)};
-        const bool pbc = T.pbc != 0;
+        const bool pbc = BOX && T.pbc != 0;
         auto ww = [&](int b0, const float4 q0, const float4 q1, const float4 q2) {
             float3 dO = make_float3((q0.x - r0.x) + (q1.x - r1.x), (q0.y - r0.y) + (q1.y - r1.y),
                                     (q0.z - r0.z) + (q1.z - r1.z));
@@ -270,7 +272,7 @@ __device__ __forceinline__ PairFlags pair_flags(const DevSys &S, int i, int j) {
 
 // nonbond_pp (src/md.f90:13069-13155) and the solute side of nonbond_pw, plus
 // lrf_taylor, for one non-Q solute atom.
-template <bool EACC, int LW>
+template <bool EACC, int LW, bool BOX>
 __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *satom, int lrf) {
     __shared__ long long red[5][QG_BLOCK / 32];
     const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LW;
@@ -291,9 +293,10 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         const int ti = S.atype[i];
         const double qi = EACC ? S.crg_d[i] : 0.0;
         const float el14 = T.el14;
-        const bool pbc = T.pbc != 0;
+        const bool pbc = BOX && T.pbc != 0;
         const int swg = S.g_switch[g];
-        const float4 swh = S.pos[swg], swl = S.poslo[swg];
+        float4 swh = {}, swl = {};
+        if (pbc) { swh = S.pos[swg]; swl = S.poslo[swg]; }
         // one pair term: LJ code c, el14 factor for 1-4 pairs (nonbond_pp :13102-13111),
         // periodic shift (sf, sd) of the group pair (nonbond_pp_box :13226-13228)
         auto pair = [&](int j, int c, EAcc<EACC> &e_el, EAcc<EACC> &e_vdw, const float3 sf, const double3 sd) {
@@ -719,41 +722,51 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
 // blocks 1 or 6) and its neighbours per loop iteration (1/2/4); lanes per
 // solute atom (4/8/16).  The FP64-energy
 // variants (drop-in calls) use 8 lanes.
-template <int LW, int MINB>
+template <int LW, int MINB, bool BOX>
 static void water_fp32(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf) {
     const int nb = B.nwgrp * LW / QG_BLOCK;
-    if (B.tune.unroll_water == 1) k_nb_water<false, LW, MINB, 1><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
-    else if (B.tune.unroll_water == 4) k_nb_water<false, LW, MINB, 4><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
-    else k_nb_water<false, LW, MINB, 2><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    if (B.tune.unroll_water == 1) k_nb_water<false, LW, MINB, 1, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    else if (B.tune.unroll_water == 4) k_nb_water<false, LW, MINB, 4, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    else k_nb_water<false, LW, MINB, 2, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+}
+template <bool BOX>
+static void water_launch(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
+    if (fp64_energy) {
+        k_nb_water<true, 8, 1, 2, BOX><<<B.nwgrp * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    } else {
+        const bool m6 = B.tune.minb_water == 6;
+        switch (B.tune.lw_water) {
+        case 4: m6 ? water_fp32<4, 6, BOX>(S, B, L, lrf) : water_fp32<4, 1, BOX>(S, B, L, lrf); break;
+        case 16: m6 ? water_fp32<16, 6, BOX>(S, B, L, lrf) : water_fp32<16, 1, BOX>(S, B, L, lrf); break;
+        default: m6 ? water_fp32<8, 6, BOX>(S, B, L, lrf) : water_fp32<8, 1, BOX>(S, B, L, lrf); break;
+        }
+    }
 }
 void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
     if (!B.nwgrp) return;
     prof_begin(L, "k_nb_water");
-    if (fp64_energy) {
-        k_nb_water<true, 8, 1, 2><<<B.nwgrp * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
-    } else {
-        const bool m6 = B.tune.minb_water == 6;
-        switch (B.tune.lw_water) {
-        case 4: m6 ? water_fp32<4, 6>(S, B, L, lrf) : water_fp32<4, 1>(S, B, L, lrf); break;
-        case 16: m6 ? water_fp32<16, 6>(S, B, L, lrf) : water_fp32<16, 1>(S, B, L, lrf); break;
-        default: m6 ? water_fp32<8, 6>(S, B, L, lrf) : water_fp32<8, 1>(S, B, L, lrf); break;
-        }
-    }
+    if (B.pbc) water_launch<true>(S, B, L, lrf, fp64_energy);
+    else water_launch<false>(S, B, L, lrf, fp64_energy);
     prof_end(L);
     (*L.nlaunch)++;
+}
+template <bool BOX>
+static void solute_launch(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
+    if (fp64_energy) {
+        k_nb_solute<true, 8, BOX><<<B.nsatom * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf);
+    } else {
+        switch (B.tune.lw_solute) {
+        case 4: k_nb_solute<false, 4, BOX><<<B.nsatom * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
+        case 16: k_nb_solute<false, 16, BOX><<<B.nsatom * 16 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
+        default: k_nb_solute<false, 8, BOX><<<B.nsatom * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
+        }
+    }
 }
 void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
     if (!B.nsatom) return;
     prof_begin(L, "k_nb_solute");
-    if (fp64_energy) {
-        k_nb_solute<true, 8><<<B.nsatom * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf);
-    } else {
-        switch (B.tune.lw_solute) {
-        case 4: k_nb_solute<false, 4><<<B.nsatom * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
-        case 16: k_nb_solute<false, 16><<<B.nsatom * 16 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
-        default: k_nb_solute<false, 8><<<B.nsatom * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
-        }
-    }
+    if (B.pbc) solute_launch<true>(S, B, L, lrf, fp64_energy);
+    else solute_launch<false>(S, B, L, lrf, fp64_energy);
     prof_end(L);
     (*L.nlaunch)++;
 }
