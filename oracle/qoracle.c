@@ -651,7 +651,20 @@ void oracle_get_lrf(void *h, double *out) {
     F[3*(i)] -= (dv)*dx1; F[3*(i)+1] -= (dv)*dx2; F[3*(i)+2] -= (dv)*dx3; \
     F[3*(j)] += (dv)*dx1; F[3*(j)+1] += (dv)*dx2; F[3*(j)+2] += (dv)*dx3; } while (0)
 
-/* nonbond_pp, src/md.f90:13069-13155 */
+/* Arithmetic combination rule (ivdw_rule 2; nonbon2_*, src/md.f90:11354-13068):
+   aLJ = (a_i + a_j)^6 and bLJ = b_i b_j, V_a = bLJ aLJ^2 / r^12,
+   V_b = 2 bLJ aLJ / r^6.  A = bLJ*aLJ*aLJ and B = 2*bLJ*aLJ in the
+   reference's association. */
+static inline void arith_AB(double ai, double aj, double bi, double bj, double *A, double *B) {
+    double a = ai + aj;
+    a = a * a;
+    a = a * a * a;
+    const double b = bi * bj;
+    *A = b * a * a;
+    *B = 2.0 * b * a;
+}
+
+/* nonbond_pp, src/md.f90:13069-13155; arithmetic rule nonbon2_pp :11354-11443 */
 static void nonbond_pp(oracle *o) {
     const qgpu_system_desc *d = &o->d;
     for (int64_t k = 0; k < o->pp.n; ++k) {
@@ -661,32 +674,46 @@ static void nonbond_pp(oracle *o) {
         double r2 = 1.0 / (dx1 * dx1 + dx2 * dx2 + dx3 * dx3), r = sqrt(r2), r6 = r2 * r2 * r2;
         double Vel = d->crg[i] * d->crg[j] * r;
         if (c == 3) Vel *= d->el14_scale;
-        double Va = r6 * r6 * avdw(o, d->iac[i], c) * avdw(o, d->iac[j], c);
-        double Vb = r6 * bvdw(o, d->iac[i], c) * bvdw(o, d->iac[j], c);
+        double Va, Vb;
+        if (d->ivdw_rule == 2) {
+            double A, B;
+            arith_AB(avdw(o, d->iac[i], c), avdw(o, d->iac[j], c), bvdw(o, d->iac[i], c), bvdw(o, d->iac[j], c), &A, &B);
+            Va = A * r6 * r6;
+            Vb = B * r6;
+        } else {
+            Va = r6 * r6 * avdw(o, d->iac[i], c) * avdw(o, d->iac[j], c);
+            Vb = r6 * bvdw(o, d->iac[i], c) * bvdw(o, d->iac[j], c);
+        }
         double dv = r2 * (-Vel - 12.0 * Va + 6.0 * Vb);
         ADD_F(i, j, dv);
         o->E.pp_el += Vel; o->E.pp_vdw += Va - Vb;
     }
 }
 
-/* nonbond_pw, src/md.f90:13282-13365 */
+/* nonbond_pw, src/md.f90:13282-13365; arithmetic rule nonbon2_pw :11569-11654 */
 static void nonbond_pw(oracle *o) {
     const qgpu_system_desc *d = &o->d;
     for (int64_t k = 0; k < o->pw.n; ++k) {
         int i = o->pw.a[k].i, j = o->pw.a[k].j, c = o->pw.a[k].lj;
-        double aLJ = avdw(o, d->iac[i], c) * avdw(o, d->iac[j], c);
-        double bLJ = bvdw(o, d->iac[i], c) * bvdw(o, d->iac[j], c);
+        double aLJ, bLJ;
+        if (d->ivdw_rule == 2)
+            arith_AB(avdw(o, d->iac[i], c), avdw(o, d->iac[j], c), bvdw(o, d->iac[i], c), bvdw(o, d->iac[j], c), &aLJ, &bLJ);
+        else {
+            aLJ = avdw(o, d->iac[i], c) * avdw(o, d->iac[j], c);
+            bLJ = bvdw(o, d->iac[i], c) * bvdw(o, d->iac[j], c);
+        }
         DX(i, j);
         BOX_SHIFT(o->pw.a[k]);
         double r2 = 1.0 / (dx1 * dx1 + dx2 * dx2 + dx3 * dx3), r = sqrt(r2), r6 = r2 * r2 * r2;
-        double Vel = d->crg[i] * d->crg[j] * r, Va = aLJ * r6 * r6, Vb = bLJ * r6;
+        double Vel = d->crg[i] * d->crg[j] * r, Va = aLJ * (r6 * r6), Vb = bLJ * r6;
         double dv = r2 * (-Vel - 12.0 * Va + 6.0 * Vb);
         ADD_F(i, j, dv);
         o->E.pw_el += Vel; o->E.pw_vdw += Va - Vb;
     }
 }
 
-/* nonbond_qp (src/md.f90:13788-13921) and nonbond_qp_qvdw (14097-14230) */
+/* nonbond_qp (src/md.f90:13788-13921) and nonbond_qp_qvdw (14097-14230);
+   arithmetic rule nonbon2_qp :12221-12376 */
 static void nonbond_qp(oracle *o) {
     const qgpu_system_desc *d = &o->d;
     int nt = d->natyps + d->nqat;
@@ -696,6 +723,32 @@ static void nonbond_qp(oracle *o) {
         DX(i, j);
         BOX_SHIFT(o->qp.a[k]);
         double r2 = dx1 * dx1 + dx2 * dx2 + dx3 * dx3;
+        if (d->ivdw_rule == 2) {
+            const double r6hc = r2 * r2 * r2;
+            r2 = 1.0 / r2;
+            const double r = sqrt(r2);
+            for (int s = 0; s < o->S; ++s) {
+                double ai, bi, r6;
+                if (!d->qvdw_flag) {
+                    ai = avdw(o, d->iac[i], c); bi = bvdw(o, d->iac[i], c);
+                    r6 = 1.0 / r6hc;
+                } else {
+                    int ti = d->qiac[iq * o->S + s], cc = c == 2 ? 1 : c;
+                    ai = d->qavdw[ti * 3 + cc - 1]; bi = d->qbvdw[ti * 3 + cc - 1];
+                    r6 = 1.0 / (r6hc + d->sc_lookup[((size_t)iq * nt + tj) * o->S + s]);
+                }
+                double aLJ = ai + avdw(o, tj, c), bLJ = bi * bvdw(o, tj, c);
+                aLJ = aLJ * aLJ;
+                aLJ = aLJ * aLJ * aLJ;
+                double Vel = qcrg(o, iq, s) * d->crg[j] * r;
+                if (c == 3) Vel *= d->el14_scale;
+                double Va = bLJ * aLJ * aLJ * r6 * r6, Vb = 2.0 * bLJ * aLJ * r6;
+                double dv = r2 * (-Vel - (12.0 * Va - 6.0 * Vb) * r6 * r6hc) * d->lambda[s];
+                ADD_F(i, j, dv);
+                o->EQ[s].qp_el += Vel; o->EQ[s].qp_vdw += Va - Vb;
+            }
+            continue;
+        }
         if (!d->qvdw_flag) {
             r2 = 1.0 / r2;
             double r6 = r2 * r2 * r2, r = sqrt(r2);
@@ -765,6 +818,76 @@ static void nonbond_ww_spc(oracle *o) {
     }
 }
 
+/* nonbon2_ww, src/md.f90:12847-12945 (arithmetic rule): Coulomb and LJ on all
+   nine atom pairs of a water pair, records walked in strides of 3 as in
+   nonbond_ww_spc */
+static void nonbon2_ww(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    int ichg = 0;
+    for (int64_t k = 0; k < o->ww.n; k += 3) {
+        if (ichg > 2) ichg = 0;
+        int i = o->ww.a[k].i;
+        double q1 = d->chg_solv[ichg];
+        for (int ip = 0; ip < 3; ++ip) {
+            int ja = o->ww.a[k + ip].j;
+            int c = ljcod(o, d->iac[i], d->iac[ja]);
+            double aLJ = d->aLJ_solv[ichg * 2 + c - 1] + d->aLJ_solv[ip * 2 + c - 1];
+            double bLJ = d->bLJ_solv[ichg * 2 + c - 1] * d->bLJ_solv[ip * 2 + c - 1];
+            aLJ = aLJ * aLJ;
+            aLJ = aLJ * aLJ * aLJ;
+            DX(i, ja);
+            BOX_SHIFT(o->ww.a[k]);
+            double r2 = 1.0 / (dx1 * dx1 + dx2 * dx2 + dx3 * dx3), r = sqrt(r2), r6 = r2 * r2 * r2, r12 = r6 * r6;
+            double Vel = q1 * d->chg_solv[ip] * r;
+            double Va = bLJ * aLJ * aLJ * r12, Vb = 2.0 * bLJ * aLJ * r6;
+            double dv = r2 * (-Vel - 12.0 * Va + 6.0 * Vb);
+            ADD_F(i, ja, dv);
+            o->E.ww_el += Vel; o->E.ww_vdw += Va - Vb;
+        }
+        ichg++;
+    }
+}
+
+/* nonbon2_qw, src/md.f90:12562-12697 (arithmetic rule): every water atom with
+   LJ; softcore by the water atom's type (sc_lookup(iq, iacj, s)) */
+static void nonbon2_qw(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    int nt = d->natyps + d->nqat;
+    for (int64_t k = 0; k < o->qw.n; k += 3) {
+        int iq = o->qw.a[k].i, i = d->iqseq[iq], j0 = o->qw.a[k].j;
+        for (int jw = 0; jw < 3; ++jw) {
+            int j = j0 + jw, c = o->qw.a[k + jw].lj, tj = d->iac[j];
+            double sa = d->aLJ_solv[jw * 2 + c - 1], sb = d->bLJ_solv[jw * 2 + c - 1];
+            DX(i, j);
+            BOX_SHIFT(o->qw.a[k]);
+            double r2 = dx1 * dx1 + dx2 * dx2 + dx3 * dx3;
+            const double r6hc = r2 * r2 * r2;
+            r2 = 1.0 / r2;
+            const double r = sqrt(r2);
+            for (int s = 0; s < o->S; ++s) {
+                double aLJ, bLJ, r6;
+                if (!d->qvdw_flag) {
+                    aLJ = avdw(o, d->iac[i], c); bLJ = bvdw(o, d->iac[i], c);
+                    r6 = 1.0 / r6hc;
+                } else {
+                    int ti = d->qiac[iq * o->S + s], cc = c == 2 ? 1 : c;
+                    aLJ = d->qavdw[ti * 3 + cc - 1]; bLJ = d->qbvdw[ti * 3 + cc - 1];
+                    r6 = 1.0 / (r6hc + d->sc_lookup[((size_t)iq * nt + tj) * o->S + s]);
+                }
+                aLJ = aLJ + sa;
+                bLJ = bLJ * sb;
+                aLJ = aLJ * aLJ;
+                aLJ = aLJ * aLJ * aLJ;
+                double Vel = qcrg(o, iq, s) * d->chg_solv[jw] * r;
+                double Va = bLJ * aLJ * aLJ * r6 * r6, Vb = 2.0 * bLJ * aLJ * r6;
+                double dv = r2 * (-Vel - (12.0 * Va - 6.0 * Vb) * r6 * r6hc) * d->lambda[s];
+                ADD_F(i, j, dv);
+                o->EQ[s].qw_el += Vel; o->EQ[s].qw_vdw += Va - Vb;
+            }
+        }
+    }
+}
+
 /* nonbond_qw_spc, src/md.f90:14411-14570 */
 static void nonbond_qw_spc(oracle *o) {
     const qgpu_system_desc *d = &o->d;
@@ -825,7 +948,34 @@ static void nonbond_qq(oracle *o) {
             int iq = d->nbqq_iq[p], i = d->iqseq[iq], j = d->nbqq_j[p], jq = d->nbqq_jq[p], c = d->nbqq_ljcod[p];
             double qi = qcrg(o, iq, s), qj, aLJ, bLJ;
             double els = d->nbqq_elscale[p];
-            if (!d->qvdw_flag) {
+            const int arith = d->ivdw_rule == 2;
+            if (arith) {
+                /* nonbon2_qq, src/md.f90:11780-11998: sums of the a parameters
+                   (a product for the exponential repulsion of a Q-Q pair with code 2) */
+                if (!d->qvdw_flag) {
+                    int ti = d->iac[i], tj = d->iac[j];
+                    aLJ = avdw(o, ti, c) + avdw(o, tj, c);
+                    bLJ = bvdw(o, ti, c) * bvdw(o, tj, c);
+                    qj = jq >= 0 ? qcrg(o, jq, s) : d->crg[j];
+                } else {
+                    int ti = d->qiac[iq * o->S + s];
+                    aLJ = d->qavdw[ti * 3 + c - 1];
+                    bLJ = d->qbvdw[ti * 3 + c - 1];
+                    if (jq >= 0) {
+                        int tj = d->qiac[jq * o->S + s];
+                        qj = qcrg(o, jq, s);
+                        if (c == 2) aLJ = aLJ * d->qavdw[tj * 3 + c - 1];
+                        else aLJ = aLJ + d->qavdw[tj * 3 + c - 1];
+                        bLJ = bLJ * d->qbvdw[tj * 3 + c - 1];
+                    } else {
+                        if (c == 2) { aLJ = d->qavdw[ti * 3]; bLJ = d->qbvdw[ti * 3]; }
+                        int tj = d->iac[j];
+                        aLJ = aLJ + avdw(o, tj, c);
+                        bLJ = bLJ * bvdw(o, tj, c);
+                        qj = d->crg[j];
+                    }
+                }
+            } else if (!d->qvdw_flag) {
                 int ti = d->iac[i], tj = d->iac[j];
                 aLJ = avdw(o, ti, c) * avdw(o, tj, c);
                 bLJ = bvdw(o, ti, c) * bvdw(o, tj, c);
@@ -863,6 +1013,12 @@ static void nonbond_qq(oracle *o) {
                 Va = aLJ * exp(-bLJ / r);
                 Vb = 0.0;
                 dv = r2 * (-Vel - bLJ * Va / r) * d->lambda[s];
+            } else if (arith) {
+                aLJ = aLJ * aLJ;
+                aLJ = aLJ * aLJ * aLJ;
+                Va = bLJ * aLJ * aLJ * r12;
+                Vb = 2.0 * bLJ * aLJ * r6;
+                dv = r2 * (-Vel - (12.0 * Va - 6.0 * Vb) * r6 * r6hc) * d->lambda[s];
             } else {
                 Va = aLJ * r12;
                 Vb = bLJ * r6;
@@ -1316,7 +1472,10 @@ void oracle_pot_energy(void *h, int terms, double *d_out, qgpu_energies *E_out, 
         nonbond_pp(o);
         nonbond_pw(o);
         nonbond_qp(o);
-        if (d->natom > d->nat_solute) { nonbond_ww_spc(o); nonbond_qw_spc(o); }
+        if (d->natom > d->nat_solute) {
+            if (d->ivdw_rule == 2) { nonbon2_ww(o); nonbon2_qw(o); }
+            else { nonbond_ww_spc(o); nonbond_qw_spc(o); }
+        }
         if (d->use_LRF) lrf_taylor(o);
     }
     if (terms & QGPU_TERMS_BONDED) {

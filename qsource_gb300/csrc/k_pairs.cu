@@ -192,8 +192,8 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
                     const int c = ljc(S, T, ta[a], tb);
-                    const float A = S.avdw[ta[a] * 3 + c - 1] * S.avdw[tb * 3 + c - 1];
-                    const float B = S.bvdw[ta[a] * 3 + c - 1] * S.bvdw[tb * 3 + c - 1];
+                    const int li = lj_index(T, ta[a], tb, c);
+                    const float A = S.ljA[li], B = S.ljB[li];
                     const float3 d = make_float3(dO.x - da[a].x, dO.y - da[a].y, dO.z - da[a].z);
                     const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
                     const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
@@ -203,8 +203,7 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
                     if (EACC) {
                         const double rid = rinv_d(S.x, a0 + a, b, sgd), r6d = rid * rid * rid * rid * rid * rid;
                         eld = qd[a] * S.crg_d[b] * rid;
-                        evd = S.avdw_d[ta[a] * 3 + c - 1] * S.avdw_d[tb * 3 + c - 1] * r6d * r6d -
-                              S.bvdw_d[ta[a] * 3 + c - 1] * S.bvdw_d[tb * 3 + c - 1] * r6d;
+                        evd = S.ljA_d[li] * r6d * r6d - S.ljB_d[li] * r6d;
                     }
                     epw_el.term(Vel, eld); epw_vdw.term(Va - Vb, evd);
                     gx[a] -= dv * d.x; gy[a] -= dv * d.y; gz[a] -= dv * d.z;
@@ -302,8 +301,8 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         auto pair = [&](int j, int c, EAcc<EACC> &e_el, EAcc<EACC> &e_vdw, const float3 sf, const double3 sd) {
             const int tj = S.atype[j];
             const float4 jh = S.pos[j], jl = S.poslo[j];
-            const float A = S.avdw[ti * 3 + c - 1] * S.avdw[tj * 3 + c - 1];
-            const float B = S.bvdw[ti * 3 + c - 1] * S.bvdw[tj * 3 + c - 1];
+            const int li = lj_index(T, ti, tj, c);
+            const float A = S.ljA[li], B = S.ljB[li];
             const float3 d = f3sub(dpos(ih, il, jh, jl), sf);
             const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
             const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
@@ -316,8 +315,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
                 const double rid = rinv_d(S.x, i, j, sd), r6d = rid * rid * rid * rid * rid * rid;
                 eld = qi * S.crg_d[j] * rid;
                 if (c == 3) eld *= (double)T.el14d;
-                evd = S.avdw_d[ti * 3 + c - 1] * S.avdw_d[tj * 3 + c - 1] * r6d * r6d -
-                      S.bvdw_d[ti * 3 + c - 1] * S.bvdw_d[tj * 3 + c - 1] * r6d;
+                evd = S.ljA_d[li] * r6d * r6d - S.ljB_d[li] * r6d;
             }
             e_el.term(Vel, eld); e_vdw.term(Va - Vb, evd);
             gx -= dv * d.x; gy -= dv * d.y; gz -= dv * d.z;
@@ -346,8 +344,8 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         for (int k = 0; k < 3; ++k) {
             const int tw = S.atype[T.atom0 + T.nat_solute + k];
             cw[k] = ljc(S, T, ti, tw);
-            Aw[k] = S.avdw[ti * 3 + cw[k] - 1] * S.avdw[tw * 3 + cw[k] - 1];
-            Bw[k] = S.bvdw[ti * 3 + cw[k] - 1] * S.bvdw[tw * 3 + cw[k] - 1];
+            Aw[k] = S.ljA[lj_index(T, ti, tw, cw[k])];
+            Bw[k] = S.ljB[lj_index(T, ti, tw, cw[k])];
             qw[k] = ih.w * T.chg_solv[k];
         }
         for (int k = lane; k < nw; k += LW) {
@@ -374,8 +372,8 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
                     const int j = b0 + b, tj = S.atype[j];
                     const double rid = rinv_d(S.x, i, j, sgd), r6d = rid * rid * rid * rid * rid * rid;
                     eld = qi * S.crg_d[j] * rid;
-                    evd = S.avdw_d[ti * 3 + cw[b] - 1] * S.avdw_d[tj * 3 + cw[b] - 1] * r6d * r6d -
-                          S.bvdw_d[ti * 3 + cw[b] - 1] * S.bvdw_d[tj * 3 + cw[b] - 1] * r6d;
+                    const int li = lj_index(T, ti, tj, cw[b]);
+                    evd = S.ljA_d[li] * r6d * r6d - S.ljB_d[li] * r6d;
                 }
                 epw_el.term(Vel, eld); epw_vdw.term(Va - Vb, evd);
                 gx -= dv * d.x; gy -= dv * d.y; gz -= dv * d.z;
@@ -563,7 +561,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
 #pragma unroll
                 for (int s = 0; s < QG_MAXS; ++s) {
                     if (s >= NS) break;
-                    const size_t sci = (size_t)T.sc0 + ((size_t)iq * ntq + (size_t)(S.qw_lj[q] - 1)) * QG_MAXS + s;
+                    const size_t sci = (size_t)T.sc0 + ((size_t)iq * ntq + (size_t)S.qw_sc[q]) * QG_MAXS + s;
                     const float A = S.qw_A[q * QG_MAXS + s], B = S.qw_B[q * QG_MAXS + s];
                     const float r6s = T.qvdw ? r6hc + S.sc_f[sci] : r6hc;
                     const float ir6 = __frcp_rn(r6s);
@@ -668,7 +666,32 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
                 if (s >= NS) break;
                 float A, B, r6s;
                 double Ad = 0, Bd = 0, r6sd = r6d;
-                if (!T.qvdw) {
+                if (T.arith) {
+                    // nonbon2_qp (src/md.f90:12221-12376): (a_q + a_j)^6 and b_q b_j,
+                    // a_q/b_q of the Q atom's type, or of its state's Q type
+                    // (code 2 -> 1) with softcore
+                    int ka, kb;
+                    const float *ta_, *tb_;
+                    const double *ta_d, *tb_d;
+                    if (!T.qvdw) { ka = tq * 3 + c - 1; ta_ = S.avdw; tb_ = S.bvdw; ta_d = S.avdw_d; tb_d = S.bvdw_d; r6s = r6; }
+                    else {
+                        ka = S.qiac[q * QG_MAXS + s] * 3 + qc - 1;
+                        ta_ = S.qavdw; tb_ = S.qbvdw; ta_d = S.qavdw_d; tb_d = S.qbvdw_d;
+                        r6s = r6 + S.sc_f[(size_t)T.sc0 + ((size_t)iq * ntq + (tj - T.type0)) * QG_MAXS + s];
+                        if (acc) r6sd = r6d + S.sc_d[(size_t)T.sc0 + ((size_t)iq * ntq + (tj - T.type0)) * QG_MAXS + s];
+                    }
+                    kb = tj * 3 + c - 1;
+                    float a = ta_[ka] + S.avdw[kb];
+                    a = a * a; a = a * a * a;
+                    const float b = tb_[ka] * S.bvdw[kb];
+                    A = b * a * a; B = 2.f * b * a;
+                    if (acc) {
+                        double ad = ta_d[ka] + S.avdw_d[kb];
+                        ad = ad * ad; ad = ad * ad * ad;
+                        const double bd = tb_d[ka] * S.bvdw_d[kb];
+                        Ad = bd * ad * ad; Bd = 2.0 * bd * ad;
+                    }
+                } else if (!T.qvdw) {
                     A = S.avdw[tq * 3 + c - 1] * S.avdw[tj * 3 + c - 1];
                     B = S.bvdw[tq * 3 + c - 1] * S.bvdw[tj * 3 + c - 1];
                     r6s = r6;

@@ -92,7 +92,33 @@ __device__ void qq_block(const DevSys &S, int b, const int *blk_traj, const int 
         const int iql = q - T.q0;
         const R qi = p::qcrg(S, q * QG_MAXS + s);
         R qj, aLJ, bLJ;
-        if (!T.qvdw) {
+        if (T.arith) {
+            // nonbon2_qq (src/md.f90:11780-11998): a parameters summed (the
+            // exponential Q-Q repulsion of code 2 multiplies them), b multiplied
+            if (!T.qvdw) {
+                const int ti = S.atype[i], tj = S.atype[j];
+                aLJ = p::avdw(S, ti * 3 + c - 1) + p::avdw(S, tj * 3 + c - 1);
+                bLJ = p::bvdw(S, ti * 3 + c - 1) * p::bvdw(S, tj * 3 + c - 1);
+                qj = jq >= 0 ? p::qcrg(S, jq * QG_MAXS + s) : p::crg(S, j);
+            } else {
+                const int ti = S.qiac[q * QG_MAXS + s];
+                aLJ = p::qavdw(S, ti * 3 + c - 1);
+                bLJ = p::qbvdw(S, ti * 3 + c - 1);
+                if (jq >= 0) {
+                    const int tj = S.qiac[jq * QG_MAXS + s];
+                    if (c == 2) aLJ = aLJ * p::qavdw(S, tj * 3 + c - 1);
+                    else aLJ = aLJ + p::qavdw(S, tj * 3 + c - 1);
+                    bLJ = bLJ * p::qbvdw(S, tj * 3 + c - 1);
+                    qj = p::qcrg(S, jq * QG_MAXS + s);
+                } else {
+                    if (c == 2) { aLJ = p::qavdw(S, ti * 3); bLJ = p::qbvdw(S, ti * 3); }
+                    const int tj = S.atype[j];
+                    aLJ = aLJ + p::avdw(S, tj * 3 + c - 1);
+                    bLJ = bLJ * p::bvdw(S, tj * 3 + c - 1);
+                    qj = p::crg(S, j);
+                }
+            }
+        } else if (!T.qvdw) {
             const int ti = S.atype[i], tj = S.atype[j];
             aLJ = p::avdw(S, ti * 3 + c - 1) * p::avdw(S, tj * 3 + c - 1);
             bLJ = p::bvdw(S, ti * 3 + c - 1) * p::bvdw(S, tj * 3 + c - 1);
@@ -131,6 +157,12 @@ __device__ void qq_block(const DevSys &S, int b, const int *blk_traj, const int 
             Va = aLJ * exp(-bLJ / r);
             Vb = 0;
             dv = r2 * (-Vel - bLJ * Va / r) * lam;
+        } else if (T.arith) {
+            R a6 = aLJ * aLJ;
+            a6 = a6 * a6 * a6;
+            Va = bLJ * a6 * a6 * r12;
+            Vb = R(2) * bLJ * a6 * r6;
+            dv = r2 * (-Vel - (R(12) * Va - R(6) * Vb) * r6 * r6hc) * lam;
         } else {
             Va = aLJ * r12;
             Vb = bLJ * r6;

@@ -141,7 +141,14 @@ static int validate(const qgpu_system_desc &d, int t) {
     if (d.nat_solute < 0 || d.nat_solute > d.natom) return fail(QGPU_E_INVALID, "traj %d: bad nat_solute", t);
     if (d.solv_atom != 3) return fail(QGPU_E_UNSUPPORTED, "traj %d: only 3-site solvent is supported", t);
     if ((d.natom - d.nat_solute) % 3) return fail(QGPU_E_INVALID, "traj %d: solvent atoms not a multiple of 3", t);
-    if (d.ivdw_rule != 1) return fail(QGPU_E_UNSUPPORTED, "traj %d: only the geometric LJ rule is supported", t);
+    if (d.ivdw_rule != 1 && d.ivdw_rule != 2)
+        return fail(QGPU_E_INVALID, "traj %d: combination rule %d (1 geometric, 2 arithmetic)", t, d.ivdw_rule);
+    // arithmetic rule: nonbon2_ww / nonbon2_qw take LJ on every water atom;
+    // the engine's water kernels take it on O only, exact when the water H
+    // atoms carry no LJ (b = 0)
+    if (d.ivdw_rule == 2 && d.nwat > 0 && (d.bLJ_solv[2] != 0.0 || d.bLJ_solv[3] != 0.0 || d.bLJ_solv[4] != 0.0 ||
+                                           d.bLJ_solv[5] != 0.0))
+        return fail(QGPU_E_UNSUPPORTED, "traj %d: arithmetic rule with LJ on the water hydrogens", t);
     if (d.use_pbc) {
         // the box forms cover the switch-atom lists (nb*list_box*); the
         // any-atom box lists of the reference shift by a different atom pair
@@ -195,7 +202,9 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     std::vector<int8_t> ljcod;
     std::vector<int> g_start{0}, g_atoms, g_switch, g_kind, g_traj, tile_g0, tile_g1;
     std::vector<uint8_t> g_excl;
-    std::vector<int> q_atom, qiac, qw_lj, qp14_first{0}, qp14_q;
+    std::vector<int> q_atom, qiac, qw_lj, qw_sc, qp14_first{0}, qp14_q;
+    std::vector<float> ljA, ljB;
+    std::vector<double> ljA_d, ljB_d;
     std::vector<float> qcrg_f, qavdw, qbvdw, sc_f, qw_A, qw_B;
     std::vector<double> qw_Ad, qw_Bd;
     std::vector<double> qcrg_d, qavdw_d, qbvdw_d, sc_d;
@@ -359,15 +368,37 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
                 avdw_d.push_back(d.avdw[a * 3 + c]); bvdw_d.push_back(d.bvdw[a * 3 + c]);
             }
         for (int k = 0; k < nt * nt; ++k) ljcod.push_back(d.ljcod[k]);
-        // --- water LJ constants (nonbond_ww_spc uses aLJ_solv(1,iLJ)^2)
+        // --- LJ products per (type pair, code): geometric A = a_i a_j,
+        // B = b_i b_j; arithmetic (nonbon2_pp :11354, nonbon2_pw :11569)
+        // A = b_i b_j (a_i + a_j)^12, B = 2 b_i b_j (a_i + a_j)^6
+        T.arith = d.ivdw_rule == 2 ? 1 : 0;
+        auto arith_ab = [](double ai, double aj, double bi, double bj, double &A, double &B) {
+            double a = ai + aj;
+            a = a * a;
+            a = a * a * a;
+            const double b = bi * bj;
+            A = b * a * a;
+            B = 2.0 * b * a;
+        };
+        for (int ta = 0; ta < nt; ++ta)
+            for (int tb = 0; tb < nt; ++tb)
+                for (int c = 0; c < 3; ++c) {
+                    double A, B;
+                    if (T.arith) arith_ab(d.avdw[ta * 3 + c], d.avdw[tb * 3 + c], d.bvdw[ta * 3 + c], d.bvdw[tb * 3 + c], A, B);
+                    else { A = d.avdw[ta * 3 + c] * d.avdw[tb * 3 + c]; B = d.bvdw[ta * 3 + c] * d.bvdw[tb * 3 + c]; }
+                    ljA.push_back((float)A); ljB.push_back((float)B);
+                    ljA_d.push_back(A); ljB_d.push_back(B);
+                }
+        // --- water LJ constants (nonbond_ww_spc uses aLJ_solv(1,iLJ)^2;
+        // nonbon2_ww :12847 the arithmetic form of the O pair)
         if (d.nwat > 0) {
             int tO = d.iac[d.nat_solute];
             int c = d.ljcod[tO * nt + tO];
             T.ww_lj = c;
-            T.ww_A = (float)(d.aLJ_solv[c - 1] * d.aLJ_solv[c - 1]);
-            T.ww_B = (float)(d.bLJ_solv[c - 1] * d.bLJ_solv[c - 1]);
-            T.ww_Ad = d.aLJ_solv[c - 1] * d.aLJ_solv[c - 1];
-            T.ww_Bd = d.bLJ_solv[c - 1] * d.bLJ_solv[c - 1];
+            double A = d.aLJ_solv[c - 1] * d.aLJ_solv[c - 1], B = d.bLJ_solv[c - 1] * d.bLJ_solv[c - 1];
+            if (T.arith) arith_ab(d.aLJ_solv[c - 1], d.aLJ_solv[c - 1], d.bLJ_solv[c - 1], d.bLJ_solv[c - 1], A, B);
+            T.ww_A = (float)A; T.ww_B = (float)B;
+            T.ww_Ad = A; T.ww_Bd = B;
         } else T.ww_lj = 1;
         // --- atoms
         std::vector<int> grp_of(N, 0);
@@ -547,13 +578,23 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
             int tq = d.iac[qa];
             int c = d.ljcod[tO * nt + tq];
             qw_lj.push_back(c);
+            // softcore column of the O: the LJ code (nonbond_qw_spc :14492), its
+            // type for the arithmetic rule (nonbon2_qw :12632)
+            qw_sc.push_back(T.arith ? tO : c - 1);
             for (int s = 0; s < QG_MAXS; ++s) {
                 double qc = s < S ? d.qcrg[iq * S + s] : 0.0;
                 qcrg_d.push_back(qc); qcrg_f.push_back((float)qc);
                 int qt = s < S ? d.qiac[iq * S + s] : 0;
                 qiac.push_back(qlib0 + qt);
                 double A, B;
-                if (!d.qvdw_flag) {
+                if (T.arith) {
+                    // nonbon2_qw: (a_q + a_O)^6, b_q b_O with the Q atom's type or
+                    // its state's Q type (code 2 -> 1)
+                    const int cq = c == 2 ? 1 : c;
+                    const double aq = d.qvdw_flag ? d.qavdw[qt * 3 + cq - 1] : d.avdw[tq * 3 + c - 1];
+                    const double bq = d.qvdw_flag ? d.qbvdw[qt * 3 + cq - 1] : d.bvdw[tq * 3 + c - 1];
+                    arith_ab(aq, d.aLJ_solv[c - 1], bq, d.bLJ_solv[c - 1], A, B);
+                } else if (!d.qvdw_flag) {
                     A = d.avdw[tq * 3 + c - 1] * d.aLJ_solv[c - 1];
                     B = d.bvdw[tq * 3 + c - 1] * d.bLJ_solv[c - 1];
                 } else {
@@ -768,7 +809,8 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         if ((rc = upload(A, qw_A, &p))) return rc; S.qw_A = p;
         if ((rc = upload(A, qw_B, &p))) return rc; S.qw_B = p;
     }
-    UP(qw_lj, qw_lj); UP(qw_Ad, qw_Ad); UP(qw_Bd, qw_Bd);
+    UP(qw_lj, qw_lj); UP(qw_sc, qw_sc); UP(qw_Ad, qw_Ad); UP(qw_Bd, qw_Bd);
+    UP(ljA, ljA); UP(ljB, ljB); UP(ljA_d, ljA_d); UP(ljB_d, ljB_d);
     if ((rc = alloc0(A, (size_t)atom0, &S.qw_member))) return rc;
     if ((rc = alloc0(A, (size_t)atom0, &S.qp_member))) return rc;
     {

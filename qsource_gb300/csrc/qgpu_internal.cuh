@@ -127,6 +127,9 @@ struct TrajInfo {
     // (global index), the molecules put_back_in_box may move (DevSys::mol_start
     // from mol0, nmol of them, the first nsolute_mol solute) and which kinds
     int pbc, qswitch, put_solute, put_solvent, rigid_box;
+    // combination rule: 0 geometric (A = a_i a_j), 1 arithmetic (ivdw_rule 2,
+    // nonbon2_*: A = b_i b_j (a_i + a_j)^12, B = 2 b_i b_j (a_i + a_j)^6)
+    int arith;
     int mol0, nmol, nsolute_mol;
     float boxf[3], iboxf[3];
     double box[3], ibox[3];
@@ -216,6 +219,11 @@ struct DevSys {
     float *qw_A, *qw_B;             // [q*QG_MAXS+s] water-O LJ products
     const double *qw_Ad, *qw_Bd;
     const int *qw_lj;               // [q] LJ code of the water-O / Q-atom pair
+    const int *qw_sc;               // [q] sc_lookup column of the water O (the LJ code, or its type: arithmetic rule)
+    // LJ products per (type pair, code) under the trajectory's combination
+    // rule, [(lj0 + ta*natyps + tb)*3 + code-1] (lj_index)
+    const float *ljA, *ljB;
+    const double *ljA_d, *ljB_d;
     uint8_t *qw_member;             // per water (global water index) in the qw list
     uint8_t *qp_member;             // per atom in the qp list
     int *g_qin;                     // per solute group in a box: the atom that put it on the qp list (its shift)
@@ -466,6 +474,11 @@ __device__ __forceinline__ double dist2_exact_box(const double *x, int i, int j,
         c[k] = __dsub_rn(a, __dmul_rn(T.box[k], round(__dmul_rn(a, T.ibox[k]))));
     }
     return __dadd_rn(__dadd_rn(__dmul_rn(c[0], c[0]), __dmul_rn(c[1], c[1])), __dmul_rn(c[2], c[2]));
+}
+
+// index of the LJ products of local types (ta, tb), code c (1..3), in DevSys::ljA/ljB
+__device__ __forceinline__ int lj_index(const TrajInfo &T, int ta, int tb, int c) {
+    return (T.lj0 + (ta - T.type0) * T.natyps + (tb - T.type0)) * 3 + c - 1;
 }
 
 // exact FP64 squared distance in the reference's operation order (no FMA)

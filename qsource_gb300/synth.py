@@ -101,9 +101,14 @@ def _waters(R: float, solute: np.ndarray, rng: np.random.Generator) -> np.ndarra
 def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, seed: int, *,
               solute_sigma: float = 0.3, T: float = 300.0, stepsize: float = 1.0, tau_T: float = 100.0,
               NBcycle: int = 10, Rc: float = 10.0, offdiag=None, initial_velocities: bool = True,
-              any_atom: bool = False) -> System:
+              any_atom: bool = False, vdw_rule: int = 1, qvdw: bool = False) -> System:
     """Water sphere of radius R around a solute chain of n_solute atoms whose
     first nq atoms are Q atoms with per-state charges qcharges[nq, nstates].
+
+    vdw_rule 2 gives the same LJ types in the arithmetic combination rule
+    (ivdw_rule 2).  qvdw gives the Q atoms their own per-state Q types
+    ([atom_types] / [change_atoms] of the FEP file): state 1 the CT type,
+    the other states a softer copy (A and B halved).
 
     any_atom selects the any-atom cut-off for the solute charge groups
     (topology flag iuse_switch_atom = 0).  The chain's groups are 4
@@ -147,6 +152,8 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
     p14 = [(i, i + 3) for i in range(1, n_solute - 2)]
     av = np.array([[OPLS[t][0], OPLS[t][1], OPLS[t][3]] for t in TYPES])
     bv = np.array([[OPLS[t][2], OPLS[t][4], OPLS[t][4]] for t in TYPES])
+    if vdw_rule == 2:
+        av, bv = _arithmetic_params(av, bv)
     top = {
         "version": 5.06, "ff_type": 2, "natom": natom, "nat_solute": n_solute, "solv_atom": 3,
         "xtop": xtop, "iac": iac,
@@ -157,7 +164,7 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
         "crg": crg, "ncgp_solute": ncgp_solute, "iuse_switch_atom": 0 if any_atom else 1,
         "cgp_first": np.array(first, np.int32), "cgp_last": np.array(last, np.int32),
         "cgp_switch": np.array(sw, np.int32), "cgpatom": np.array(atoms, np.int32),
-        "ivdw_rule": 1, "el14_scale": 0.5, "coulomb_constant": 332.0,
+        "ivdw_rule": vdw_rule, "el14_scale": 0.5, "coulomb_constant": 332.0,
         "mass": np.array([OPLS[t][5] for t in TYPES]), "avdw": av, "bvdw": bv,
         "lj2": np.zeros((0, 2), np.int32),
         "list14": np.array(p14, np.int32).reshape(-1, 2), "list14long": np.zeros((0, 2), np.int32),
@@ -167,10 +174,21 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
         "xpcent": np.zeros(3), "xwcent": np.zeros(3), "nexats": 0, "nexwat": 0,
         "excl": np.zeros(natom, np.uint8),
     }
+    atom_types, change_atoms = [], []
+    if qvdw:
+        ct = TYPES.index("CT")
+        hard = [av[ct, 0] ** 2, bv[ct, 0] ** 2, av[ct, 1] ** 2, bv[ct, 1] ** 2, av[ct, 2] ** 2, bv[ct, 2] ** 2]
+        if vdw_rule == 2:
+            hard = [av[ct, 0], bv[ct, 0], av[ct, 1], bv[ct, 1], av[ct, 2], bv[ct, 2]]
+        # [atom_types] rows hold the parameters as the topology does (sqrt(A), sqrt(B) per code)
+        hard = [math.sqrt(v) for v in hard] if vdw_rule == 1 else hard
+        soft = [v * (0.5 if k % 2 else 0.9) for k, v in enumerate(hard)]
+        atom_types = [("Qhard", hard, 12.011), ("Qsoft", soft, 12.011)]
+        change_atoms = [(i + 1, ["Qhard"] + ["Qsoft"] * (S - 1)) for i in range(nq)]
     fep = {
         "nstates": S, "iqseq": np.arange(1, nq + 1, dtype=np.int32),
         "change_charges": [(i + 1, list(qcharges[i])) for i in range(nq)],
-        "atom_types": [], "change_atoms": [], "soft_pairs": [], "el_scale": [], "excluded_pairs": [],
+        "atom_types": atom_types, "change_atoms": change_atoms, "soft_pairs": [], "el_scale": [], "excluded_pairs": [],
         "bond_types": {}, "change_bonds": [], "angle_types": {}, "change_angles": [],
         "torsion_types": {}, "change_torsions": [], "improper_types": {}, "change_impropers": [],
         "off_diagonals": list(offdiag or []), "unsupported": [],
@@ -190,6 +208,21 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
         sd = np.sqrt(0.001986 * T / m)
         s.v = (rng.normal(size=(natom, 3)) * sd[:, None]).reshape(-1)
     return s
+
+
+def _arithmetic_params(av: np.ndarray, bv: np.ndarray):
+    """The same LJ types for the arithmetic combination rule (ivdw_rule 2):
+    from sqrt(A) = av, sqrt(B) = bv of V = A/r^12 - B/r^6 per type, the
+    radius R* = 2^(1/6) sigma / 2 with sigma^6 = A/B and sqrt(eps) with
+    eps = B^2 / (4 A), so that eps_ij (R*_i + R*_j)^12 / r^12 - 2 eps_ij
+    (R*_i + R*_j)^6 / r^6 reproduces the type's own LJ curve (zero for types
+    without LJ)."""
+    A, B = av ** 2, bv ** 2
+    with np.errstate(divide="ignore", invalid="ignore"):
+        sig6 = np.where(B > 0, A / np.where(B > 0, B, 1.0), 0.0)
+        eps = np.where(A > 0, B ** 2 / (4.0 * np.where(A > 0, A, 1.0)), 0.0)
+    rstar = 0.5 * 2.0 ** (1.0 / 6.0) * sig6 ** (1.0 / 6.0)
+    return rstar, np.sqrt(eps)
 
 
 def neutral_charges(rng: np.random.Generator, n: int, sigma: float) -> np.ndarray:

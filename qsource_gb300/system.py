@@ -54,7 +54,7 @@ class System:
         d.excl, d.shell, d.iqatom = arr(self.excl, np.uint8), arr(self.shell, np.uint8), arr(self.iqatom, np.int32)
         d.mass, d.avdw, d.bvdw = arr(self.mass, np.float64), arr(self.avdw, np.float64), arr(self.bvdw, np.float64)
         d.ljcod = arr(self.ljcod, np.int8)
-        d.el14_scale, d.ivdw_rule, d.ff_type = self.el14_scale, 1, self.ff_type
+        d.el14_scale, d.ivdw_rule, d.ff_type = self.el14_scale, int(getattr(self, "ivdw_rule", 1)), self.ff_type
         for k in range(3):
             d.chg_solv[k] = self.chg_solv[k]
         for k in range(6):
@@ -213,8 +213,8 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
     """qdyn start-up on parsed inputs -> System (0-based)."""
     if top["solv_atom"] != 3 or top["solvent_type"] != 0:
         raise ValueError("only 3-site SPC-type solvent is supported (solvent_type 0)")
-    if top["ivdw_rule"] != 1:
-        raise ValueError("only the geometric combination rule is supported (ivdw_rule 1)")
+    if top["ivdw_rule"] not in (1, 2):
+        raise ValueError(f"unknown combination rule ivdw_rule {top['ivdw_rule']} (1 geometric, 2 arithmetic)")
     if inp["unsupported"]:
         raise ValueError(f"unsupported input sections: {inp['unsupported']}")
     natom, nsol = top["natom"], top["nat_solute"]
@@ -567,6 +567,7 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
         natom=natom, nat_solute=nsol, natyps=natyps, ncgp_solute=ncgp_solute, nqat=nq, nstates=S,
         x=x, v=np.zeros(3 * natom), xtop=xtop, crg=crg, iac=iac, excl=excl, shell=shell, iqatom=iqatom,
         mass=mass, avdw=avdw, bvdw=bvdw, ljcod=ljcod, el14_scale=top["el14_scale"], ff_type=top["ff_type"],
+        ivdw_rule=int(top["ivdw_rule"]),
         chg_solv=chg_solv, aLJ_solv=aLJ_solv, bLJ_solv=bLJ_solv,
         cgp_first=cgp_first, cgp_last=cgp_last, cgp_switch=cgp_switch, cgpatom=cgpatom,
         excl_pairs=np.array(sorted(excl_set), dtype=np.int32).reshape(-1, 2),

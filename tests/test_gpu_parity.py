@@ -44,6 +44,11 @@ def systems(engine_lib):
     # switch-atom cut-off, which the reference's own golden systems also use
     out = {"cfg1": synth.config(1), "cfg2": synth.config(2), "cfg4": synth.config(4),
            "cfg2sw": synth.config(2, any_atom=False)}
+    # the arithmetic combination rule (ivdw_rule 2) and per-state Q atom types
+    out["cfg1ar"] = synth.config(1, vdw_rule=2)
+    out["cfg1qv"] = synth.config(1, qvdw=True)
+    out["cfg1arqv"] = synth.config(1, vdw_rule=2, qvdw=True)
+    out["cfg2ar"] = synth.config(2, vdw_rule=2)
     g = golden_system("basic_sph")
     o = _oracle(g)
     o.maxwell(g.Tmaxw, int(g.seed))
@@ -100,7 +105,7 @@ def test_lrf_multipoles(systems, name):
         assert err <= 1e-5 * scale, (lo, err, scale)
 
 
-@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg2sw", "cfg4"])
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg2sw", "cfg4", "cfg1ar", "cfg1qv", "cfg1arqv", "cfg2ar"])
 def test_forces_and_energies(systems, name):
     s = systems[name]
     e = _engine(s)
@@ -143,12 +148,12 @@ def test_shake_matches_oracle(systems):
     assert np.abs(xg - xo).max() < 1e-9
 
 
-@pytest.mark.parametrize("ene_every", [1, 5])
-def test_short_md_matches_oracle(systems, ene_every):
+@pytest.mark.parametrize("name,ene_every", [("cfg1", 1), ("cfg1", 5), ("cfg1arqv", 5), ("cfg2ar", 5)])
+def test_short_md_matches_oracle(systems, name, ene_every):
     """20 Berendsen leap-frog steps with SHAKE and lists every 10 steps.  With
     ene_every=5 the unrecorded steps run the FP32 path (float master state,
     FP32 SHAKE and bonded terms); recorded steps evaluate energies in FP64."""
-    s = systems["cfg1"]
+    s = systems[name]
     e = _engine(s)
     rows = e.run(20, ene_every=ene_every)[0]
     o = _oracle(s)
@@ -198,7 +203,7 @@ def test_thermostats_match_oracle(systems, thermostat, integrator, precision):
     assert abs(x - xo).max() < 1e-4
 
 
-@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg4"])
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg4", "cfg1arqv", "cfg2ar"])
 def test_step_precision_forces(systems, name):
     """The precision of an unrecorded MD step (QGPU_TERMS_STEP_PRECISION: FP32
     bonded, restraint and Q terms from the float coordinates, FP32 energy sums)
