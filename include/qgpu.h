@@ -78,7 +78,7 @@ typedef struct qgpu_system_desc {
     const double *bvdw;     /* natyps*3                                        */
     const int8_t *ljcod;    /* natyps*natyps, values 1 or 2                    */
     double el14_scale;
-    int32_t ivdw_rule;      /* must be 1 (geometric)                           */
+    int32_t ivdw_rule;      /* 1 geometric, 2 arithmetic (nonbon2_*)           */
     int32_t ff_type;        /* 1 GROMOS, 2 AMBER, 3 CHARMM (improper form)     */
 
     /* SPC-type solvent tables (prep_sim, src/md.f90:16702-16717) */
