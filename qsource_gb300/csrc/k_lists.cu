@@ -333,27 +333,81 @@ __global__ void k_scan_reduce(DevSys S) {
     if (t >= S.ngrp) return;
     const TrajInfo &T = S.traj[S.g_traj[t]];
     const bool ex = S.g_excl[t];
-    float acc = 0.f;
     const int cap = S.nb_cap;
     int *lst = S.nb_list + (size_t)t * cap;
-    int cnt = 0;
-    for (int c = 0; c < T.nchunk; ++c) {
-        const long long slot = T.scr0 + (long long)c * T.ncgp + (t - T.grp0);
-        if (lane < QG_NLRF) acc += S.scr_phi[(size_t)slot * QG_NLRF + lane];
-        const int nw = ex ? 0 : (S.scr_cnt[slot] & 0xffff);
-        const int *seg = S.scr_nb + (size_t)slot * QG_CAPC;
-        for (int k = lane; k < nw; k += 32)
-            if (cnt + k < cap) lst[cnt + k] = seg[k];
-        cnt += nw;
+    const int nch = T.nchunk;
+    const size_t base = (size_t)(T.scr0 + (t - T.grp0)), stride = (size_t)T.ncgp;   // slot(c) = base + c*stride
+    // LRF partials in chunk order, eight chunks' loads in flight at a time
+    float acc = 0.f;
+    if (lane < QG_NLRF) {
+        int c = 0;
+        for (; c + 8 <= nch; c += 8) {
+            float v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = S.scr_phi[(base + (size_t)(c + u) * stride) * QG_NLRF + lane];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) acc += v[u];
+        }
+        for (; c < nch; ++c) acc += S.scr_phi[(base + (size_t)c * stride) * QG_NLRF + lane];
     }
-    const int nwat = cnt;
-    for (int c = 0; c < T.nchunk; ++c) {
-        const long long slot = T.scr0 + (long long)c * T.ncgp + (t - T.grp0);
-        const int ns = ex ? 0 : (S.scr_cnt[slot] >> 16);
-        const int *seg = S.scr_nb + (size_t)slot * QG_CAPC;
-        for (int k = lane; k < ns; k += 32)
-            if (cnt + k < cap) lst[cnt + k] = seg[QG_CAPC - 1 - k];
-        cnt += ns;
+    // near groups: every chunk's counts (chunk r*32 + lane in round r), their
+    // offsets in chunk order by warp prefix sums -- water entries of all
+    // chunks first, then solute entries -- and the segments copied four
+    // chunks at a time (their loads in flight together)
+    int cnt = 0, nwat = 0;
+    if (!ex) {
+        int wtot = 0, stot = 0;
+        for (int r0 = 0; r0 < nch; r0 += 32) {
+            const int c = r0 + lane;
+            const int cc = c < nch ? S.scr_cnt[base + (size_t)c * stride] : 0;
+            wtot += __reduce_add_sync(0xffffffffu, cc & 0xffff);
+            stot += __reduce_add_sync(0xffffffffu, cc >> 16);
+        }
+        nwat = wtot;
+        cnt = wtot + stot;
+        int ow = 0, os = wtot;   // running offsets before the current round
+        for (int r0 = 0; r0 < nch; r0 += 32) {
+            const int c = r0 + lane;
+            const int cc = c < nch ? S.scr_cnt[base + (size_t)c * stride] : 0;
+            const int nw = cc & 0xffff, ns = cc >> 16;
+            int pw = nw, ps = ns;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int yw = __shfl_up_sync(0xffffffffu, pw, o), ys = __shfl_up_sync(0xffffffffu, ps, o);
+                if (lane >= o) { pw += yw; ps += ys; }
+            }
+            const int offw = ow + pw - nw, offs = os + ps - ns;
+            const int nr = min(32, nch - r0);
+            for (int j0 = 0; j0 < nr; j0 += 4) {
+                int vw[4][2], vs[4][2], dw[4], ds[4], kw[4], ks[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int j = min(j0 + u, 31);
+                    const bool on = j0 + u < nr;
+                    kw[u] = on ? __shfl_sync(0xffffffffu, nw, j) : 0;
+                    ks[u] = on ? __shfl_sync(0xffffffffu, ns, j) : 0;
+                    dw[u] = __shfl_sync(0xffffffffu, offw, j);
+                    ds[u] = __shfl_sync(0xffffffffu, offs, j);
+                    const int *seg = S.scr_nb + (base + (size_t)(r0 + j) * stride) * QG_CAPC;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int k = lane + 32 * h;
+                        vw[u][h] = k < kw[u] ? seg[k] : 0;
+                        vs[u][h] = k < ks[u] ? seg[QG_CAPC - 1 - k] : 0;
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int k = lane + 32 * h;
+                        if (k < kw[u] && dw[u] + k < cap) lst[dw[u] + k] = vw[u][h];
+                        if (k < ks[u] && ds[u] + k < cap) lst[ds[u] + k] = vs[u][h];
+                    }
+            }
+            ow += __shfl_sync(0xffffffffu, pw, 31);
+            os += __shfl_sync(0xffffffffu, ps, 31);
+        }
     }
     float a[QG_NLRF];
 #pragma unroll
