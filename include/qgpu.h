@@ -450,6 +450,36 @@ int qgpu_lrf_scan_static(int32_t ngroup, const double *x, const double *crg, con
                          const double *origin, double rc_pp, double rc_pw, double rc_ww, double rc_lrf,
                          double *lrf43, int32_t *near_count, void *stream);
 
+/* ------------------------------------------------------------------------ */
+/* qcalc-style trajectory analysis (src/qcalc.f90 and its calc_* modules) on  */
+/* the device.  frames: nframes x 3*natom FP64 coordinates in host memory     */
+/* (e.g. the frames of a DCD trajectory, src/trj.f90), uploaded once per call;*/
+/* every calculation runs over all frames in one launch.  Atom indices are    */
+/* 0-based; masks are atom lists in topology order.                           */
+/* ------------------------------------------------------------------------ */
+/* RMS deviation of the masked atoms from xref (3*natom, the topology
+   coordinates in qcalc), no fitting: sqrt(sum |x - x0|^2 / nmask)
+   (calc_rms.f90 rms_calc).  out[nframes], A. */
+int qgpu_calc_rms(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
+                  const double *xref, double *out);
+/* Centre of mass of the masked atoms (calc_com.f90 COM_calc); mass per atom
+   (natom).  out[nframes*3]. */
+int qgpu_calc_com(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
+                  const double *mass, double *out);
+/* Geometry (calc_geom.f90 dist_calc / angle_calc / torsion_calc): measurement
+   m uses kind[m] (2 distance, 3 angle, 4 torsion) atoms atoms[4*m ...].
+   out[nframes*nmeas]: A, or degrees (torsions signed). */
+int qgpu_calc_geom(const double *frames, int32_t nframes, int32_t natom, int32_t nmeas, const int32_t *atoms,
+                   const int32_t *kind, double *out);
+/* Radial distribution counts (calc_rdf.f90 RDF_calc): every pair of a mask-1
+   atom and a different mask-2 atom, distance as the reference forms it in
+   single precision (minimum image when box != NULL: boxlength[3]), bin
+   int(dist/radius*nbins + 1) for dist < radius.  counts[nbins] summed over all
+   frames; the normalisation of RDF_finalize (shell volume, frames, mask-1
+   atoms) is the caller's.  nbins <= 8192, nframes <= 65535. */
+int qgpu_calc_rdf(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask1, int32_t n1,
+                  const int32_t *mask2, int32_t n2, double radius, int32_t nbins, const double *box, int64_t *counts);
+
 #ifdef __cplusplus
 }
 #endif

@@ -130,6 +130,10 @@ EXPORTS = {
     "qgpu_mlp_predict": (_i32, [_P, _P, _i32, _P]),
     "qgpu_mlp_train": (_i32, [_P, _P, _P, _P, _P, _i32, _i32, C.c_float, _i32, _P, _P]),
     "qgpu_set_tuning": (_i32, [C.c_void_p, _P]),
+    "qgpu_calc_rms": (_i32, [_P, _i32, _i32, _P, _i32, _P, _P]),
+    "qgpu_calc_com": (_i32, [_P, _i32, _i32, _P, _i32, _P, _P]),
+    "qgpu_calc_geom": (_i32, [_P, _i32, _i32, _i32, _P, _P, _P]),
+    "qgpu_calc_rdf": (_i32, [_P, _i32, _i32, _P, _i32, _P, _i32, _f64, _i32, _P, _P]),
     "qgpu_ene_open": (_i32, [C.c_void_p, _i32, C.c_char_p]),
     "qgpu_ene_close": (_i32, [C.c_void_p, _i32]),
     "qgpu_enefile_write": (_i32, [C.c_char_p, _i32, _i32, C.POINTER(QEnergy), _i32, _P, _P]),

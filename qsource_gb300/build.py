@@ -15,7 +15,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
-SOURCES = ["qgpu_api.cu", "k_lists.cu", "k_pairs.cu", "k_small.cu", "k_md.cu", "k_lrf_static.cu", "qgpu_ene.cu", "k_mlp.cu"]
+SOURCES = ["qgpu_api.cu", "k_lists.cu", "k_pairs.cu", "k_small.cu", "k_md.cu", "k_lrf_static.cu", "qgpu_ene.cu", "k_mlp.cu",
+           "qgpu_calc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include"),
          "-I" + CSRC, "--use_fast_math=false"]

@@ -1,0 +1,297 @@
+// qgpu_calc.cu -- qcalc-style trajectory analysis on the device.
+//
+// The reference's qcalc (src/qcalc.f90) reads the frames qdyn wrote to a DCD
+// trajectory (src/trj.f90) and evaluates, frame by frame, the calculations of
+// its calc_* modules.  Here all frames of a call are uploaded at once and each
+// calculation runs over every frame in one launch:
+//   * RMS deviation from the topology coordinates (calc_rms.f90 rms_calc:
+//     sqrt(sum over the masked atoms of |x - x0|^2 / n), no fitting);
+//   * distances, angles and torsions (calc_geom.f90 dist_calc / angle_calc /
+//     torsion_calc, FP64, angles in degrees);
+//   * radial distribution counts between two atom masks (calc_rdf.f90
+//     RDF_calc: every pair of a mask-1 atom and a different mask-2 atom; the
+//     distance in single precision and the bin index dist/radius*Nbins + 1 in
+//     double, as the reference's real/real(8) mix; minimum image in a box);
+//   * centre of mass of a mask (calc_com.f90 COM_calc).
+// Sums run in FP64 with a fixed reduction order (deterministic); RDF bins are
+// integer counts.
+#include <math.h>
+
+#include <vector>
+
+#include "qgpu_internal.cuh"
+
+namespace {
+
+#define QC_T 256
+
+struct DevBuf {
+    std::vector<void *> p;
+    ~DevBuf() { for (void *q : p) cudaFree(q); }
+    template <class T>
+    cudaError_t up(const T *h, size_t n, T **d) {
+        cudaError_t e = cudaMalloc((void **)d, (n ? n : 1) * sizeof(T));
+        if (e != cudaSuccess) return e;
+        p.push_back(*d);
+        return n ? cudaMemcpy(*d, h, n * sizeof(T), cudaMemcpyHostToDevice) : cudaSuccess;
+    }
+    template <class T>
+    cudaError_t zero(size_t n, T **d) {
+        cudaError_t e = cudaMalloc((void **)d, (n ? n : 1) * sizeof(T));
+        if (e != cudaSuccess) return e;
+        p.push_back(*d);
+        return cudaMemset(*d, 0, (n ? n : 1) * sizeof(T));
+    }
+};
+
+// block sum of one double per thread in a fixed tree order
+__device__ double block_sum(double v, double *sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// rms_calc (calc_rms.f90): one block per frame
+__global__ void k_calc_rms(const double *fr, int natom, const int *mask, int n, const double *x0, double *out) {
+    __shared__ double sh[QC_T];
+    const double *x = fr + (size_t)blockIdx.x * 3 * natom;
+    double s = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int a = mask[k];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double d = x[3 * a + c] - x0[3 * a + c];
+            s += d * d;
+        }
+    }
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) out[blockIdx.x] = sqrt(s / n);
+}
+
+// COM_calc (calc_com.f90): one block per frame, the mass-weighted mean
+__global__ void k_calc_com(const double *fr, int natom, const int *mask, int n, const double *mass, double *out) {
+    __shared__ double sh[QC_T];
+    const double *x = fr + (size_t)blockIdx.x * 3 * natom;
+    double c[3] = {0.0, 0.0, 0.0}, m = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int a = mask[k];
+        m += mass[a];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) c[d] += x[3 * a + d] * mass[a];
+    }
+    const double mt = block_sum(m, sh);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double s = block_sum(c[d], sh);
+        if (threadIdx.x == 0) out[3 * blockIdx.x + d] = s / mt;
+    }
+}
+
+// dist_calc / angle_calc / torsion_calc (calc_geom.f90): one thread per
+// (frame, measurement); kind 2 distance (A), 3 angle, 4 torsion (degrees)
+__global__ void k_calc_geom(const double *fr, int natom, int nframes, int nmeas, const int *atoms, const int *kind,
+                            double *out) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nframes * nmeas) return;
+    const int f = id / nmeas, m = id % nmeas;
+    const double *x = fr + (size_t)f * 3 * natom;
+    const int *at = atoms + 4 * m;
+    const double pi = 4.0 * atan(1.0);
+    auto diff = [&](int a, int b, double (&r)[3]) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[c] = x[3 * a + c] - x[3 * b + c];
+    };
+    auto dot = [](const double (&a)[3], const double (&b)[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+    double v = 0.0;
+    if (kind[m] == 2) {
+        double rji[3];
+        diff(at[0], at[1], rji);
+        v = sqrt(dot(rji, rji));
+    } else if (kind[m] == 3) {
+        double rji[3], rjk[3];
+        diff(at[0], at[1], rji);
+        diff(at[2], at[1], rjk);
+        double scp = dot(rji, rjk) / sqrt(dot(rji, rji) * dot(rjk, rjk));
+        scp = fmin(fmax(scp, -1.0), 1.0);
+        v = acos(scp) * 180.0 / pi;
+    } else {
+        double rji[3], rjk[3], rkl[3], rnj[3], rnk[3];
+        diff(at[0], at[1], rji);
+        diff(at[2], at[1], rjk);
+        diff(at[3], at[2], rkl);
+        rnj[0] = rji[1] * rjk[2] - rji[2] * rjk[1];
+        rnj[1] = rji[2] * rjk[0] - rji[0] * rjk[2];
+        rnj[2] = rji[0] * rjk[1] - rji[1] * rjk[0];
+        rnk[0] = -rjk[1] * rkl[2] + rjk[2] * rkl[1];
+        rnk[1] = -rjk[2] * rkl[0] + rjk[0] * rkl[2];
+        rnk[2] = -rjk[0] * rkl[1] + rjk[1] * rkl[0];
+        double scp = dot(rnj, rnk) / sqrt(dot(rnj, rnj) * dot(rnk, rnk));
+        scp = fmin(fmax(scp, -1.0), 1.0);
+        double phi = acos(scp);
+        const double sgn = rjk[0] * (rnj[1] * rnk[2] - rnj[2] * rnk[1]) + rjk[1] * (rnj[2] * rnk[0] - rnj[0] * rnk[2]) +
+                           rjk[2] * (rnj[0] * rnk[1] - rnj[1] * rnk[0]);
+        if (sgn < 0) phi = -phi;
+        v = phi * 180.0 / pi;
+    }
+    out[(size_t)f * nmeas + m] = v;
+}
+
+// RDF_calc (calc_rdf.f90): the single-precision pair distance of the
+// reference (function r, FP64 difference rounded to real(4), minimum image
+// in double and rounded again, dot product and sqrt in real(4) without
+// contraction) and its bin dist/radius*Nbins + 1 in double.
+__device__ __forceinline__ float rdf_comp(double xa, double xb, double box) {
+    float d = (float)(xa - xb);
+    if (box > 0.0) d = (float)((double)d - box * round((double)d / box));
+    return d;
+}
+// one thread per (frame, mask-1 atom), mask 2 staged through shared memory;
+// counts gathered in shared bins, then added to the global bins (integers)
+__global__ void k_calc_rdf(const double *fr, int natom, const int *m1, int n1, const int *m2, int n2, double radius,
+                           int nbins, double bx, double by, double bz, int use_box, unsigned long long *bins) {
+    extern __shared__ unsigned int sb[];   // nbins counters
+    __shared__ double s2[QC_T][3];
+    __shared__ int si[QC_T];
+    const int f = blockIdx.y;
+    const double *x = fr + (size_t)f * 3 * natom;
+    for (int k = threadIdx.x; k < nbins; k += blockDim.x) sb[k] = 0u;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool on = i < n1;
+    const int a = on ? m1[i] : 0;
+    const double xa = on ? x[3 * a] : 0.0, ya = on ? x[3 * a + 1] : 0.0, za = on ? x[3 * a + 2] : 0.0;
+    for (int j0 = 0; j0 < n2; j0 += blockDim.x) {
+        __syncthreads();
+        const int jj = j0 + threadIdx.x;
+        if (jj < n2) {
+            const int b = m2[jj];
+            si[threadIdx.x] = b;
+            s2[threadIdx.x][0] = x[3 * b]; s2[threadIdx.x][1] = x[3 * b + 1]; s2[threadIdx.x][2] = x[3 * b + 2];
+        }
+        __syncthreads();
+        const int nj = min((int)blockDim.x, n2 - j0);
+        if (!on) continue;
+        for (int j = 0; j < nj; ++j) {
+            if (si[j] == a) continue;
+            const float d1 = rdf_comp(xa, s2[j][0], use_box ? bx : 0.0);
+            const float d2 = rdf_comp(ya, s2[j][1], use_box ? by : 0.0);
+            const float d3 = rdf_comp(za, s2[j][2], use_box ? bz : 0.0);
+            const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(d1, d1), __fmul_rn(d2, d2)), __fmul_rn(d3, d3));
+            const float dist = __fsqrt_rn(r2);
+            if ((double)dist < radius) {
+                const int bin = (int)((double)dist / radius * (double)nbins + 1.0) - 1;
+                if (bin >= 0 && bin < nbins) atomicAdd(&sb[bin], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nbins; k += blockDim.x)
+        if (sb[k]) atomicAdd(&bins[k], (unsigned long long)sb[k]);
+}
+
+int check_atoms(const int32_t *a, int n, int natom) {
+    for (int k = 0; k < n; ++k)
+        if (a[k] < 0 || a[k] >= natom) return 1;
+    return 0;
+}
+
+#define CKC(call)                                                                                     \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return qgpu_fail(QGPU_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+}  // namespace
+
+extern "C" {
+
+int qgpu_calc_rms(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
+                  const double *xref, double *out) {
+    if (!frames || nframes < 1 || natom < 1 || !mask || nmask < 1 || !xref || !out || check_atoms(mask, nmask, natom))
+        return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_rms: bad arguments");
+    DevBuf B;
+    double *fr, *x0, *o;
+    int *m;
+    CKC(B.up(frames, (size_t)nframes * 3 * natom, &fr));
+    CKC(B.up(xref, (size_t)3 * natom, &x0));
+    CKC(B.up(mask, (size_t)nmask, &m));
+    CKC(B.zero((size_t)nframes, &o));
+    k_calc_rms<<<nframes, QC_T>>>(fr, natom, m, nmask, x0, o);
+    CKC(cudaGetLastError());
+    CKC(cudaMemcpy(out, o, (size_t)nframes * sizeof(double), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int qgpu_calc_com(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
+                  const double *mass, double *out) {
+    if (!frames || nframes < 1 || natom < 1 || !mask || nmask < 1 || !mass || !out || check_atoms(mask, nmask, natom))
+        return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_com: bad arguments");
+    DevBuf B;
+    double *fr, *ms, *o;
+    int *m;
+    CKC(B.up(frames, (size_t)nframes * 3 * natom, &fr));
+    CKC(B.up(mass, (size_t)natom, &ms));
+    CKC(B.up(mask, (size_t)nmask, &m));
+    CKC(B.zero((size_t)3 * nframes, &o));
+    k_calc_com<<<nframes, QC_T>>>(fr, natom, m, nmask, ms, o);
+    CKC(cudaGetLastError());
+    CKC(cudaMemcpy(out, o, (size_t)3 * nframes * sizeof(double), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int qgpu_calc_geom(const double *frames, int32_t nframes, int32_t natom, int32_t nmeas, const int32_t *atoms,
+                   const int32_t *kind, double *out) {
+    if (!frames || nframes < 1 || natom < 1 || nmeas < 1 || !atoms || !kind || !out)
+        return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_geom: bad arguments");
+    for (int m = 0; m < nmeas; ++m) {
+        if (kind[m] < 2 || kind[m] > 4) return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_geom: kind %d", kind[m]);
+        if (check_atoms(atoms + 4 * m, kind[m], natom)) return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_geom: atom index");
+    }
+    std::vector<int32_t> at((size_t)4 * nmeas);
+    for (int m = 0; m < nmeas; ++m)
+        for (int k = 0; k < 4; ++k) at[4 * m + k] = k < kind[m] ? atoms[4 * m + k] : 0;
+    DevBuf B;
+    double *fr, *o;
+    int *a, *kd;
+    CKC(B.up(frames, (size_t)nframes * 3 * natom, &fr));
+    CKC(B.up(at.data(), at.size(), &a));
+    CKC(B.up(kind, (size_t)nmeas, &kd));
+    CKC(B.zero((size_t)nframes * nmeas, &o));
+    const int n = nframes * nmeas;
+    k_calc_geom<<<(n + QC_T - 1) / QC_T, QC_T>>>(fr, natom, nframes, nmeas, a, kd, o);
+    CKC(cudaGetLastError());
+    CKC(cudaMemcpy(out, o, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int qgpu_calc_rdf(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask1, int32_t n1,
+                  const int32_t *mask2, int32_t n2, double radius, int32_t nbins, const double *box, int64_t *counts) {
+    if (!frames || nframes < 1 || natom < 1 || !mask1 || n1 < 1 || !mask2 || n2 < 1 || !(radius > 0) || nbins < 1 ||
+        nbins > 8192 || !counts || check_atoms(mask1, n1, natom) || check_atoms(mask2, n2, natom) ||
+        nframes > 65535)
+        return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_rdf: bad arguments");
+    DevBuf B;
+    double *fr;
+    int *a, *b;
+    unsigned long long *bins;
+    CKC(B.up(frames, (size_t)nframes * 3 * natom, &fr));
+    CKC(B.up(mask1, (size_t)n1, &a));
+    CKC(B.up(mask2, (size_t)n2, &b));
+    CKC(B.zero((size_t)nbins, &bins));
+    dim3 grid((n1 + QC_T - 1) / QC_T, nframes);
+    k_calc_rdf<<<grid, QC_T, (size_t)nbins * sizeof(unsigned int)>>>(fr, natom, a, n1, b, n2, radius, nbins,
+                                                                     box ? box[0] : 0.0, box ? box[1] : 0.0,
+                                                                     box ? box[2] : 0.0, box ? 1 : 0, bins);
+    CKC(cudaGetLastError());
+    std::vector<unsigned long long> h(nbins);
+    CKC(cudaMemcpy(h.data(), bins, (size_t)nbins * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < nbins; ++k) counts[k] = (int64_t)h[k];
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,43 @@
+"""Host side of the qcalc-style analysis: the DCD layout of src/trj.f90 and the
+oracle's calc_geom / calc_rdf restatements on configurations with known answers."""
+import math
+import struct
+
+import numpy as np
+
+
+def test_dcd_round_trip_and_layout(tmp_path):
+    from qsource_gb300.qcalc import read_dcd, write_dcd
+    rng = np.random.default_rng(3)
+    frames = rng.normal(0, 10, size=(4, 3 * 7))
+    p = str(tmp_path / "t.dcd")
+    write_dcd(p, frames, interval=25, n_degf=12, topology="lig_w.top")
+    head, back = read_dcd(p)
+    assert head["n_frames"] == 4 and head["interval"] == 25 and head["n_steps"] == 100 and head["n_degf"] == 12
+    assert head["atoms"] == 7 and head["mask_rows"] == ["all"] and head["topology"] == "lig_w.top"
+    assert np.array_equal(back, frames.astype(np.float32).astype(np.float64))
+    raw = open(p, "rb").read()
+    # record 1: 84-byte payload starting with CORD; record 3: the atom count
+    assert struct.unpack("<i", raw[:4])[0] == 84 and raw[4:8] == b"CORD"
+    off = 8 + 84 + 4 + 4 + 3 * 80 + 4
+    assert struct.unpack("<iii", raw[off:off + 12]) == (4, 7, 4)
+
+
+def test_geom_known_answers():
+    from oracle.qcalc_ref import geom
+    # atoms: 0 (1,0,0), 1 (0,0,0), 2 (0,1,0), 3 (0,1,1): angle 0-1-2 = 90, torsion 0-1-2-3 = +-90
+    x = np.array([[1, 0, 0], [0, 0, 0], [0, 1, 0], [0, 1, 1]], dtype=np.float64).reshape(1, -1)
+    g = geom(x, [(0, 1), (0, 1, 2), (0, 1, 2, 3), (0, 2)])
+    assert g[0, 0] == 1.0 and abs(g[0, 1] - 90.0) < 1e-12 and abs(abs(g[0, 2]) - 90.0) < 1e-12
+    assert abs(g[0, 3] - math.sqrt(2.0)) < 1e-15
+
+
+def test_rdf_counts_known_answers():
+    from oracle.qcalc_ref import rdf_counts
+    # three atoms on a line 1 A apart: pairs (0,1) 1 A, (0,2) 2 A, (1,2) 1 A, both orders
+    x = np.array([[0, 0, 0], [1, 0, 0], [2, 0, 0]], dtype=np.float64).reshape(1, -1)
+    c = rdf_counts(x, [0, 1, 2], [0, 1, 2], radius=4.0, nbins=4)
+    assert list(c) == [0, 4, 2, 0]
+    # in a 3 A box the (0, 2) pair is 1 A apart through the boundary
+    c = rdf_counts(x, [0, 1, 2], [0, 1, 2], radius=4.0, nbins=4, box=[3.0, 3.0, 3.0])
+    assert list(c) == [0, 6, 0, 0]
