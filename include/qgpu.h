@@ -226,6 +226,20 @@ typedef struct qgpu_system_desc {
     int32_t nmol;                 /* molecules                                        */
     const int32_t *istart_mol;    /* nmol: first atom of each molecule, 0-based       */
     int32_t nsolute_mol;          /* the first nsolute_mol molecules are solute       */
+
+    /* the other restraints of p_restrain (src/md.f90:15580-15800; input
+       initialize :5234-5358).  state: 0 = every state (energy into each
+       state's restraint term), s >= 1 = that state only, its force weighted by
+       lambda_s.  Wall restraints (sphere only) act on the atoms first..last
+       that are heavy or, with the H flag, any atom. */
+    int32_t nrstr_pos;  const int32_t *rstpos_i;  /* 2n: atom, state                  */
+    const double *rstpos_x;                         /* 6n: x0[3], fk[3]                 */
+    int32_t nrstr_dist; const int32_t *rstdis_i;  /* 3n: atom i, atom j, state        */
+    const double *rstdis_p;                         /* 3n: d1, d2, fk                   */
+    int32_t nrstr_angl; const int32_t *rstang_i;  /* 4n: atoms i, j, k, state         */
+    const double *rstang_p;                         /* 2n: angle (degrees), fk          */
+    int32_t nrstr_wall; const int32_t *rstwal_i;  /* 3n: first, last atom, H flag     */
+    const double *rstwal_p;                         /* 4n: d, fk, aMorse, dMorse        */
 } qgpu_system_desc;
 
 /* Energies, the ENERGIES record of src/nrgy.f90:48-54 (sphere subset). */

@@ -150,6 +150,14 @@ void *oracle_create(const qgpu_system_desc *in) {
     o->d.rstseq_fk = (const double *)dupbuf(in->rstseq_fk, (size_t)in->nrstr_seq * sizeof(double));
     o->d.rstseq_flags = (const int32_t *)dupbuf(in->rstseq_flags, 2 * (size_t)in->nrstr_seq * sizeof(int32_t));
     o->d.heavy = (const uint8_t *)dupbuf(in->heavy, in->heavy ? (size_t)N : 0);
+    o->d.rstpos_i = (const int32_t *)dupbuf(in->rstpos_i, 2 * (size_t)in->nrstr_pos * sizeof(int32_t));
+    o->d.rstpos_x = (const double *)dupbuf(in->rstpos_x, 6 * (size_t)in->nrstr_pos * sizeof(double));
+    o->d.rstdis_i = (const int32_t *)dupbuf(in->rstdis_i, 3 * (size_t)in->nrstr_dist * sizeof(int32_t));
+    o->d.rstdis_p = (const double *)dupbuf(in->rstdis_p, 3 * (size_t)in->nrstr_dist * sizeof(double));
+    o->d.rstang_i = (const int32_t *)dupbuf(in->rstang_i, 4 * (size_t)in->nrstr_angl * sizeof(int32_t));
+    o->d.rstang_p = (const double *)dupbuf(in->rstang_p, 2 * (size_t)in->nrstr_angl * sizeof(double));
+    o->d.rstwal_i = (const int32_t *)dupbuf(in->rstwal_i, 3 * (size_t)in->nrstr_wall * sizeof(int32_t));
+    o->d.rstwal_p = (const double *)dupbuf(in->rstwal_p, 4 * (size_t)in->nrstr_wall * sizeof(double));
     int ns = in->wpol_restr ? in->nwpolr_shell : 0;
     o->d.nwpolr_shell = ns;
     o->theta_corr = (double *)xmalloc((size_t)(ns + 1) * sizeof(double));
@@ -189,6 +197,8 @@ void oracle_destroy(void *h) {
     free(o->ex_first); free(o->ex_j); free(o->p14_first); free(o->p14_j);
     free((void *)o->d.rstseq_ij); free((void *)o->d.rstseq_fk); free((void *)o->d.rstseq_flags);
     free((void *)o->d.heavy);
+    free((void *)o->d.rstpos_i); free((void *)o->d.rstpos_x); free((void *)o->d.rstdis_i); free((void *)o->d.rstdis_p);
+    free((void *)o->d.rstang_i); free((void *)o->d.rstang_p); free((void *)o->d.rstwal_i); free((void *)o->d.rstwal_p);
     free(o->theta_corr); free(o->avtheta); free(o->avn_insh); free(o->n_insh);
     free(o->theta); free(o->tdum); free(o->theta0); free(o->list_sh); free(o->nsort);
     free(o->randva); free(o->randfa);
@@ -1338,6 +1348,110 @@ static void p_restrain_seq(oracle *o) {
 }
 
 /* water dipole / radial unit vectors and the angle between them (watpol) */
+/* The rest of p_restrain, src/md.f90:15580-15800, in its order: atom position,
+   atom-atom distance and angle restraints (state st: 0 = every state, their
+   energy added to each state's restraint term; else state st only, force
+   weighted by its lambda) and, in a sphere, the half-harmonic wall restraints
+   (energy into the protein restraint). */
+static void rst_energy(oracle *o, int st, double e) {
+    if (st == 0) {
+        for (int k = 0; k < o->S; ++k) o->EQ[k].restraint += e;
+        if (o->S == 0) o->E.rst_protein += e;
+    } else {
+        o->EQ[st - 1].restraint += e;
+    }
+}
+static void p_restrain_extra(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    for (int ir = 0; ir < d->nrstr_pos; ++ir) {
+        const int i = d->rstpos_i[2 * ir], st = d->rstpos_i[2 * ir + 1];
+        const double *p = d->rstpos_x + 6 * ir;
+        const double wgt = st ? d->lambda[st - 1] : 1.0;
+        double dr[3];
+        for (int a = 0; a < 3; ++a) dr[a] = o->x[3 * i + a] - p[a];
+        const double e = 0.5 * p[3] * dr[0] * dr[0] + 0.5 * p[4] * dr[1] * dr[1] + 0.5 * p[5] * dr[2] * dr[2];
+        for (int a = 0; a < 3; ++a) o->f[3 * i + a] += p[3 + a] * dr[a] * wgt;
+        rst_energy(o, st, e);
+    }
+    for (int ir = 0; ir < d->nrstr_dist; ++ir) {
+        const int i = d->rstdis_i[3 * ir], j = d->rstdis_i[3 * ir + 1], st = d->rstdis_i[3 * ir + 2];
+        const double d1 = d->rstdis_p[3 * ir], d2 = d->rstdis_p[3 * ir + 1], fk = d->rstdis_p[3 * ir + 2];
+        double dr[3];
+        for (int a = 0; a < 3; ++a) {
+            dr[a] = o->x[3 * j + a] - o->x[3 * i + a];
+            if (d->use_pbc) dr[a] = dr[a] - pbc_shift(o, a, dr[a]);
+        }
+        const double wgt = st ? d->lambda[st - 1] : 1.0;
+        const double b = sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+        double db;
+        if (b < d1) db = b - d1;
+        else if (b > d2) db = b - d2;
+        else continue;
+        const double e = 0.5 * fk * db * db, dv = wgt * fk * db / b;
+        for (int a = 0; a < 3; ++a) { o->f[3 * j + a] += dr[a] * dv; o->f[3 * i + a] -= dr[a] * dv; }
+        rst_energy(o, st, e);
+    }
+    for (int ir = 0; ir < d->nrstr_angl; ++ir) {
+        const int i = d->rstang_i[4 * ir], j = d->rstang_i[4 * ir + 1], k = d->rstang_i[4 * ir + 2];
+        const int st = d->rstang_i[4 * ir + 3];
+        const double ang0 = d->rstang_p[2 * ir], fk = d->rstang_p[2 * ir + 1];
+        double a1[3], a2[3];
+        for (int a = 0; a < 3; ++a) {
+            a1[a] = o->x[3 * i + a] - o->x[3 * j + a];
+            a2[a] = o->x[3 * k + a] - o->x[3 * j + a];
+            if (d->use_pbc) { a1[a] = a1[a] - pbc_shift(o, a, a1[a]); a2[a] = a2[a] - pbc_shift(o, a, a2[a]); }
+        }
+        const double wgt = st ? d->lambda[st - 1] : 1.0;
+        const double r2ij = a1[0] * a1[0] + a1[1] * a1[1] + a1[2] * a1[2];
+        const double r2jk = a2[0] * a2[0] + a2[1] * a2[1] + a2[2] * a2[2];
+        const double rij = sqrt(r2ij), rjk = sqrt(r2jk);
+        double scp = (a1[0] * a2[0] + a1[1] * a2[1] + a1[2] * a2[2]) / (rij * rjk);
+        if (scp > 1.0) scp = 1.0;
+        if (scp < -1.0) scp = -1.0;
+        const double theta = acos(scp);
+        const double db = theta - ang0 * (4.0 * atan(1.0) / 180.0);   /* deg2rad, src/md.f90:527-528 */
+        const double e = 0.5 * fk * db * db, dv = wgt * fk * db;
+        double f1 = sin(theta);
+        if (fabs(f1) < QREAL_EPS) f1 = QREAL_EPS;
+        f1 = -1.0 / f1;
+        double di[3], dk[3];
+        for (int a = 0; a < 3; ++a) {
+            di[a] = f1 * (a2[a] / (rij * rjk) - scp * a1[a] / r2ij);
+            dk[a] = f1 * (a1[a] / (rij * rjk) - scp * a2[a] / r2jk);
+        }
+        for (int a = 0; a < 3; ++a) {
+            o->f[3 * i + a] += dv * di[a];
+            o->f[3 * k + a] += dv * dk[a];
+            o->f[3 * j + a] -= dv * (di[a] + dk[a]);
+        }
+        rst_energy(o, st, e);
+    }
+    if (d->use_pbc) return;
+    for (int ir = 0; ir < d->nrstr_wall; ++ir) {
+        const int i0 = d->rstwal_i[3 * ir], i1 = d->rstwal_i[3 * ir + 1], ih = d->rstwal_i[3 * ir + 2];
+        const double dw = d->rstwal_p[4 * ir], fk = d->rstwal_p[4 * ir + 1];
+        const double aM = d->rstwal_p[4 * ir + 2], dM = d->rstwal_p[4 * ir + 3];
+        for (int i = i0; i <= i1; ++i) {
+            if (!((d->heavy && d->heavy[i]) || ih == 1)) continue;
+            double dr[3];
+            for (int a = 0; a < 3; ++a) dr[a] = o->x[3 * i + a] - d->xwcent[a];
+            const double b = sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+            const double db = b - dw;
+            double e, dv;
+            if (db > 0.0) {
+                e = 0.5 * fk * db * db - dM;
+                dv = fk * db / b;
+            } else {
+                const double fexp = exp(aM * db);
+                e = dM * (fexp * fexp - 2.0 * fexp);
+                dv = -2.0 * dM * aM * (fexp - fexp * fexp) / b;
+            }
+            o->E.rst_protein += e;
+            for (int a = 0; a < 3; ++a) o->f[3 * i + a] += dv * dr[a];
+        }
+    }
+}
+
 static double wat_angle(const oracle *o, int i, double rmu[3], double rcu[3], double *rm, double *rc, double *scp) {
     const double *x = o->x + 3 * i;
     const double *c = o->d.xwcent;
@@ -1492,6 +1606,7 @@ void oracle_pot_energy(void *h, int terms, double *d_out, qgpu_energies *E_out, 
         /* pot_energy order, src/md.f90:16113-16125; no sphere restraints in a box */
         if (!d->use_pbc) fix_shell(o);
         p_restrain_seq(o);
+        p_restrain_extra(o);
         if (d->nwat > 0 && !d->use_pbc) {
             restrain_solvent(o);
             if (d->wpol_restr) watpol(o);

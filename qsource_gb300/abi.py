@@ -76,6 +76,10 @@ class SystemDesc(C.Structure):
         ("use_pbc", _i32), ("boxlength", _f64 * 3), ("boxcentre", _f64 * 3), ("qswitch", _i32),
         ("put_solute_back", _i32), ("put_solvent_back", _i32), ("rigid_box_centre", _i32),
         ("nmol", _i32), ("istart_mol", _P), ("nsolute_mol", _i32),
+        ("nrstr_pos", _i32), ("rstpos_i", _P), ("rstpos_x", _P),
+        ("nrstr_dist", _i32), ("rstdis_i", _P), ("rstdis_p", _P),
+        ("nrstr_angl", _i32), ("rstang_i", _P), ("rstang_p", _P),
+        ("nrstr_wall", _i32), ("rstwal_i", _P), ("rstwal_p", _P),
     ]
 
 

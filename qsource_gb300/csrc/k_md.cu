@@ -459,7 +459,7 @@ __device__ void finalize_traj(const DevSys &S, int tr, int lane, double *v, int 
         for (int s = 0; s < T.nstates; ++s) {
             const double *w = v + EA_Q0 + EQ_N * s;
             const double Vs = w[EQ_B] + w[EQ_A] + w[EQ_T] + w[EQ_I] + (w[EQ_QQ_EL] + w[EQ_QP_EL] + w[EQ_QW_EL]) +
-                              (w[EQ_QQ_VDW] + w[EQ_QP_VDW] + w[EQ_QW_VDW]) + 0.0;
+                              (w[EQ_QQ_VDW] + w[EQ_QP_VDW] + w[EQ_QW_VDW]) + w[EQ_RST];
             ve += T.lambda[s] * Vs;
             vf += T.fep_lamf[s] * Vs;
             vr += T.fep_lamr[s] * Vs;
@@ -519,7 +519,7 @@ __device__ void finalize_traj(const DevSys &S, int tr, int lane, double *v, int 
     if (lane != 0 || row < 0) return;
     double *R = rec + ((size_t)row * S.ntraj + tr) * QG_REC;
     // Q energies per state
-    double qb = 0, qa = 0, qt = 0, qi = 0, qxe = 0, qxv = 0;
+    double qb = 0, qa = 0, qt = 0, qi = 0, qxe = 0, qxv = 0, qr = 0;
     for (int s = 0; s < QG_MAXS; ++s) {
         double *q = R + QG_REC_EQ + 15 * s;
         for (int c = 0; c < 15; ++c) q[c] = 0;
@@ -532,10 +532,10 @@ __device__ void finalize_traj(const DevSys &S, int tr, int lane, double *v, int 
         q[9] = w[EQ_QW_EL]; q[10] = w[EQ_QW_VDW];
         q[11] = q[5] + q[7] + q[9];
         q[12] = q[6] + q[8] + q[10];
-        q[13] = 0.0;
+        q[13] = w[EQ_RST];
         q[14] = q[1] + q[2] + q[3] + q[4] + q[11] + q[12] + q[13];
         qb += q[1] * lam; qa += q[2] * lam; qt += q[3] * lam; qi += q[4] * lam;
-        qxe += q[11] * lam; qxv += q[12] * lam;
+        qxe += q[11] * lam; qxv += q[12] * lam; qr += q[13] * lam;
     }
     double *E = R + QG_REC_E;
     // field order of qgpu_energies
@@ -545,7 +545,8 @@ __device__ void finalize_traj(const DevSys &S, int tr, int lane, double *v, int 
     E[11] = qb; E[12] = qa; E[13] = qt; E[14] = qi;
     E[15] = v[EA_PP_EL]; E[16] = v[EA_PP_VDW]; E[17] = v[EA_PW_EL]; E[18] = v[EA_PW_VDW];
     E[19] = v[EA_WW_EL]; E[20] = v[EA_WW_VDW]; E[21] = qxe; E[22] = qxv;
-    E[24] = v[EA_RST_FIX]; E[25] = v[EA_RST_SHELL]; E[26] = v[EA_RST_PROT]; E[27] = v[EA_RST_RAD];
+    // the per-state restraints enter the protein restraint lambda-weighted (pot_energy)
+    E[24] = v[EA_RST_FIX]; E[25] = v[EA_RST_SHELL]; E[26] = v[EA_RST_PROT] + qr; E[27] = v[EA_RST_RAD];
     E[28] = v[EA_RST_WPOL];
     E[23] = E[24] + E[25] + E[26] + E[27] + E[28];
     E[0] = E[3] + E[7] + E[4] + E[8] + E[5] + E[6] + E[15] + E[16] + E[17] + E[18] + E[19] + E[20] + E[11] + E[12] +

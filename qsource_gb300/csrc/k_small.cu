@@ -575,6 +575,144 @@ __device__ void seqrst_block(const DevSys &S, int b, Red &red) {
     block_energies_fx<1>(S.eacc + (size_t)traj * QG_NE, slots, v, red);
 }
 
+// The other restraints of p_restrain (src/md.f90:15580-15800): atom position,
+// distance and angle restraints (state-dependent: state 0 adds its energy to
+// every state's restraint term, state s only to s with the force weighted by
+// lambda_s; distances and angles take the minimum image in a box) and the
+// sphere's half-harmonic wall restraints (protein restraint energy).  One
+// thread per item; a block holds one trajectory's items.
+template <typename R>
+__device__ void xrst_block(const DevSys &S, int b, Red &red) {
+    typedef P<R> p;
+    const int k = b * blockDim.x + threadIdx.x;
+    const int traj = S.xr_blk_traj[b];
+    const TrajInfo &T = S.traj[traj];
+    R est[QG_MAXS], ewall = 0;
+#pragma unroll
+    for (int s = 0; s < QG_MAXS; ++s) est[s] = 0;
+    const int kind = k < S.nxr ? S.xr_kind[k] : -1;
+    if (kind >= 0) {
+        const int i = S.xr_at[3 * k], j = S.xr_at[3 * k + 1], l = S.xr_at[3 * k + 2], st = S.xr_st[k];
+        const double *pd = S.xr_p + 6 * k;
+        const float *pf = S.xr_pf + 9 * k;
+        const R wgt = st ? p::lambda(T, st - 1) : R(1);
+        auto mimg = [&](R &c, int a) {
+            if (!T.pbc) return;
+            if (sizeof(R) == 8) c = c - R(T.box[a] * round(double(c) * T.ibox[a]));
+            else c = c - R(T.boxf[a] * rintf(float(c) * T.iboxf[a]));
+        };
+        R e = 0;
+        if (kind == 0) {
+            // atom position restraint: x - x0 per axis, force constants per axis
+            R d[3];
+            if (sizeof(R) == 8) {
+                for (int a = 0; a < 3; ++a) d[a] = R(S.x[3 * i + a] - pd[a]);
+            } else {
+                const float4 h = S.pos[i], lo = S.poslo[i];
+                d[0] = R((h.x - pf[0]) + (lo.x - pf[3]));
+                d[1] = R((h.y - pf[1]) + (lo.y - pf[4]));
+                d[2] = R((h.z - pf[2]) + (lo.z - pf[5]));
+            }
+            R fk[3];
+            for (int a = 0; a < 3; ++a) fk[a] = sizeof(R) == 8 ? R(pd[3 + a]) : R(pf[6 + a]);
+            e = R(0.5) * fk[0] * d[0] * d[0] + R(0.5) * fk[1] * d[1] * d[1] + R(0.5) * fk[2] * d[2] * d[2];
+            p::grad(S, i, fk[0] * d[0] * wgt, fk[1] * d[1] * wgt, fk[2] * d[2] * wgt);
+        } else if (kind == 1) {
+            // distance restraint: flat between d1 and d2, harmonic outside
+            const V3<R> v = rel<R>(S, i, j);
+            R dr[3] = {v.x, v.y, v.z};
+            for (int a = 0; a < 3; ++a) mimg(dr[a], a);
+            const R d1 = sizeof(R) == 8 ? R(pd[0]) : R(pf[0]), d2 = sizeof(R) == 8 ? R(pd[1]) : R(pf[1]);
+            const R fk = sizeof(R) == 8 ? R(pd[2]) : R(pf[2]);
+            const R bl = sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+            R db = 0;
+            const bool on = bl < d1 || bl > d2;
+            if (bl < d1) db = bl - d1;
+            else if (bl > d2) db = bl - d2;
+            if (on) {
+                e = R(0.5) * fk * db * db;
+                const R dv = wgt * fk * db / bl;
+                p::grad(S, j, dr[0] * dv, dr[1] * dv, dr[2] * dv);
+                p::grad(S, i, -dr[0] * dv, -dr[1] * dv, -dr[2] * dv);
+            }
+        } else if (kind == 2) {
+            // angle restraint i-j-k
+            const V3<R> v1 = rel<R>(S, j, i), v2 = rel<R>(S, j, l);
+            R a1[3] = {v1.x, v1.y, v1.z}, a2[3] = {v2.x, v2.y, v2.z};
+            for (int a = 0; a < 3; ++a) { mimg(a1[a], a); mimg(a2[a], a); }
+            const R ang0 = sizeof(R) == 8 ? R(pd[0]) : R(pf[0]), fk = sizeof(R) == 8 ? R(pd[1]) : R(pf[1]);
+            const R r2ij = a1[0] * a1[0] + a1[1] * a1[1] + a1[2] * a1[2];
+            const R r2jk = a2[0] * a2[0] + a2[1] * a2[1] + a2[2] * a2[2];
+            const R rij = sqrt(r2ij), rjk = sqrt(r2jk);
+            R scp = (a1[0] * a2[0] + a1[1] * a2[1] + a1[2] * a2[2]) / (rij * rjk);
+            if (scp > R(1)) scp = R(1);
+            if (scp < R(-1)) scp = R(-1);
+            const R theta = acos(scp);
+            const R db = theta - ang0 * R(4.0 * atan(1.0) / 180.0);
+            e = R(0.5) * fk * db * db;
+            const R dv = wgt * fk * db;
+            R f1 = sin(theta);
+            if (fabs(double(f1)) < QREAL_EPS) f1 = R(QREAL_EPS);
+            f1 = R(-1) / f1;
+            R di[3], dk[3];
+            for (int a = 0; a < 3; ++a) {
+                di[a] = f1 * (a2[a] / (rij * rjk) - scp * a1[a] / r2ij);
+                dk[a] = f1 * (a1[a] / (rij * rjk) - scp * a2[a] / r2jk);
+            }
+            p::grad(S, i, dv * di[0], dv * di[1], dv * di[2]);
+            p::grad(S, l, dv * dk[0], dv * dk[1], dv * dk[2]);
+            p::grad(S, j, -dv * (di[0] + dk[0]), -dv * (di[1] + dk[1]), -dv * (di[2] + dk[2]));
+        } else {
+            // wall restraint on one atom (the float coordinates are relative to xwcent)
+            R dr[3];
+            if (sizeof(R) == 8) {
+                for (int a = 0; a < 3; ++a) dr[a] = R(S.x[3 * i + a] - T.xwcent[a]);
+            } else {
+                const float4 h = S.pos[i], lo = S.poslo[i];
+                dr[0] = R(h.x + lo.x); dr[1] = R(h.y + lo.y); dr[2] = R(h.z + lo.z);
+            }
+            R dw, fk, aM, dM;
+            if (sizeof(R) == 8) { dw = R(pd[0]); fk = R(pd[1]); aM = R(pd[2]); dM = R(pd[3]); }
+            else { dw = R(pf[0]); fk = R(pf[1]); aM = R(pf[2]); dM = R(pf[3]); }
+            const R bl = sqrt(dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2]);
+            const R db = bl - dw;
+            R dv;
+            if (db > R(0)) {
+                ewall = R(0.5) * fk * db * db - dM;
+                dv = fk * db / bl;
+            } else {
+                const R fexp = exp(aM * db);
+                ewall = dM * (fexp * fexp - R(2) * fexp);
+                dv = R(-2) * dM * aM * (fexp - fexp * fexp) / bl;
+            }
+            p::grad(S, i, dv * dr[0], dv * dr[1], dv * dr[2]);
+        }
+        if (kind <= 2) {
+            if (st == 0) {
+                for (int s = 0; s < T.nstates; ++s) est[s] = e;
+            } else {
+                est[st - 1] = e;
+            }
+        }
+    }
+    unsigned long long *ea = S.eacc + (size_t)traj * QG_NE;
+    {
+        const int slots[1] = {EA_RST_PROT};
+        long long v[1] = {p::fx(ewall, S.status)};
+        block_energies_fx<1>(ea, slots, v, red);
+    }
+    for (int s0 = 0; s0 < T.nstates; s0 += 4) {
+        int slots[4];
+        long long v[4];
+        for (int q = 0; q < 4; ++q) {
+            const int s = min(s0 + q, T.nstates - 1);
+            slots[q] = EA_Q0 + EQ_N * s + EQ_RST;
+            v[q] = s0 + q < T.nstates ? p::fx(est[s], S.status) : 0;
+        }
+        block_energies_fx<4>(ea, slots, v, red);
+    }
+}
+
 // offdiag, src/md.f90:15444-15470: Hij = A exp(-mu r_kl).  Its only consumer is
 // the energy record, so it runs on the FP64 (recorded / drop-in) evaluations.
 __device__ void offdiag_block(const DevSys &S, int blk) {
@@ -592,7 +730,7 @@ __device__ void offdiag_block(const DevSys &S, int blk) {
 
 // The small terms share one launch: consecutive block ranges select the term.
 struct MiscPlan {
-    int nqq, nbt, nfix, nrad, nqb, nod, nrs;    // blocks per term
+    int nqq, nbt, nfix, nrad, nqb, nod, nrs, nxr;    // blocks per term
 };
 
 template <typename R>
@@ -611,6 +749,8 @@ __device__ __forceinline__ void misc_body(const DevSys &S, const MiscPlan &P, co
     b -= P.nqb;
     if (b < P.nrs) { seqrst_block<R>(S, b, red); return; }
     b -= P.nrs;
+    if (b < P.nxr) { xrst_block<R>(S, b, red); return; }
+    b -= P.nxr;
     if (sizeof(R) == 8 && b < P.nod) offdiag_block(S, b);
 }
 
@@ -634,7 +774,8 @@ void launch_misc(const DevSys &S, const BlockTables &B, LaunchCtx &L, int terms,
     P.nqb = (terms & QGPU_TERMS_QBONDED) ? nblk(S.nqt * QG_MAXS, QG_BLOCK) : 0;
     P.nod = nblk(S.nod, QG_BLOCK);
     P.nrs = (terms & QGPU_TERMS_RESTRAINT) ? S.nrs : 0;
-    const int nb = P.nqq + P.nbt + P.nfix + P.nrad + P.nqb + P.nod + P.nrs;
+    P.nxr = (terms & QGPU_TERMS_RESTRAINT) ? B.nxrblk : 0;
+    const int nb = P.nqq + P.nbt + P.nfix + P.nrad + P.nqb + P.nod + P.nrs + P.nxr;
     if (!nb) return;
     prof_begin(L, "k_misc");
     k_misc<<<nb, QG_BLOCK, 0, L.stream>>>(S, P, B.qqblk_traj, B.qqblk_s, B.satom, B.wgrp, e);

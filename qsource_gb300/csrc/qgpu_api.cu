@@ -223,6 +223,9 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     // sequence restraints, water polarisation
     std::vector<int> rs_i0, rs_i1, rs_ih, rs_tc, rs_traj, wp_traj, wp_scr0;
     std::vector<int> mol_start, pb_traj;     // periodic box: molecules, put_back_in_box trajectories
+    std::vector<int> xr_kind, xr_at, xr_st, xr_blk_traj;   // the other p_restrain restraints
+    std::vector<double> xr_p;
+    std::vector<float> xr_pf;
     std::vector<double> boxc0;
     std::vector<double> rs_fk, wp_state;
     std::vector<uint8_t> aheavy;
@@ -310,6 +313,65 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         }
         for (int i = 0; i < N; ++i)
             aheavy.push_back(d.heavy ? d.heavy[i] : (uint8_t)(d.mass[d.iac[i]] >= 4.0));
+        // --- the other p_restrain restraints (src/md.f90:15580-15800), one item
+        // each (a wall restraint one per selected atom), padded to QG_BLOCK
+        {
+            const size_t n0 = xr_kind.size();
+            auto item = [&](int kind, int i, int j, int k, int st, const double *p, int np) {
+                xr_kind.push_back(kind);
+                xr_at.push_back(atom0 + i); xr_at.push_back(atom0 + j); xr_at.push_back(atom0 + k);
+                xr_st.push_back(st);
+                for (int q = 0; q < 6; ++q) xr_p.push_back(q < np ? p[q] : 0.0);
+                float f[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                if (kind == 0) {
+                    for (int a = 0; a < 3; ++a) {
+                        const double r = p[a] - d.xwcent[a];
+                        f[a] = (float)r;
+                        f[3 + a] = (float)(r - (double)f[a]);
+                        f[6 + a] = (float)p[3 + a];
+                    }
+                } else {
+                    for (int q = 0; q < np; ++q) f[q] = (float)p[q];
+                }
+                for (int q = 0; q < 9; ++q) xr_pf.push_back(f[q]);
+            };
+            auto bad = [&](int a) { return a < 0 || a >= N; };
+            auto bad_st = [&](int st) { return st < 0 || st > S; };
+            for (int r = 0; r < d.nrstr_pos; ++r) {
+                const int i = d.rstpos_i[2 * r], st = d.rstpos_i[2 * r + 1];
+                if (bad(i) || bad_st(st)) return fail(QGPU_E_INVALID, "trajectory %d: atom restraint %d", t, r);
+                item(0, i, i, i, st, d.rstpos_x + 6 * r, 6);
+            }
+            for (int r = 0; r < d.nrstr_dist; ++r) {
+                const int i = d.rstdis_i[3 * r], j = d.rstdis_i[3 * r + 1], st = d.rstdis_i[3 * r + 2];
+                if (bad(i) || bad(j) || bad_st(st)) return fail(QGPU_E_INVALID, "trajectory %d: distance restraint %d", t, r);
+                item(1, i, j, j, st, d.rstdis_p + 3 * r, 3);
+            }
+            for (int r = 0; r < d.nrstr_angl; ++r) {
+                const int i = d.rstang_i[4 * r], j = d.rstang_i[4 * r + 1], k = d.rstang_i[4 * r + 2];
+                const int st = d.rstang_i[4 * r + 3];
+                if (bad(i) || bad(j) || bad(k) || bad_st(st))
+                    return fail(QGPU_E_INVALID, "trajectory %d: angle restraint %d", t, r);
+                item(2, i, j, k, st, d.rstang_p + 2 * r, 2);
+            }
+            for (int r = 0; r < (d.use_pbc ? 0 : d.nrstr_wall); ++r) {
+                const int a0 = d.rstwal_i[3 * r], a1 = d.rstwal_i[3 * r + 1], ih = d.rstwal_i[3 * r + 2];
+                if (bad(a0) || bad(a1) || a0 > a1) return fail(QGPU_E_INVALID, "trajectory %d: wall restraint %d", t, r);
+                for (int i = a0; i <= a1; ++i) {
+                    const bool heavy = d.heavy ? d.heavy[i] : d.mass[d.iac[i]] >= 4.0;
+                    if (heavy || ih == 1) item(3, i, i, i, 0, d.rstwal_p + 4 * r, 4);
+                }
+            }
+            const size_t n = xr_kind.size() - n0;
+            if (n) {
+                const double zero6[6] = {0, 0, 0, 0, 0, 0};
+                while ((xr_kind.size() - n0) % QG_BLOCK) {
+                    item(0, 0, 0, 0, 0, zero6, 6);
+                    xr_kind.back() = -1;
+                }
+                for (size_t b = 0; b < (xr_kind.size() - n0) / QG_BLOCK; ++b) xr_blk_traj.push_back(t);
+            }
+        }
         T.freeze = d.excluded_freeze;
         // --- thermostat / integrator (md_run :6440-6460)
         if (d.thermostat < 0 || d.thermostat > 2 || d.integrator < 0 || d.integrator > 1)
@@ -813,6 +875,9 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     UP(ljA, ljA); UP(ljB, ljB); UP(ljA_d, ljA_d); UP(ljB_d, ljB_d);
     if ((rc = alloc0(A, (size_t)atom0, &S.qw_member))) return rc;
     if ((rc = alloc0(A, (size_t)atom0, &S.qp_member))) return rc;
+    UP(xr_kind, xr_kind); UP(xr_at, xr_at); UP(xr_st, xr_st); UP(xr_blk_traj, xr_blk_traj);
+    UP(xr_p, xr_p); UP(xr_pf, xr_pf);
+    S.nxr = (int)xr_kind.size();
     {
         std::vector<int> gq(grp0, -1);
         UP(gq, g_qin);
@@ -883,6 +948,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         if (B.any_atom && B.pbc)
             return fail(QGPU_E_UNSUPPORTED, "a batch cannot mix any-atom lists and periodic boxes");
         B.npb = (int)pb_traj.size();
+        B.nxrblk = (int)xr_blk_traj.size();
         if (B.npb) {
             int *p_;
             if ((rc = upload(A, pb_traj, &p_))) return rc; B.pb_traj = p_;

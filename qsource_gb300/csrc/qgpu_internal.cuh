@@ -51,7 +51,7 @@ enum {
     EA_RST_FIX, EA_RST_SHELL, EA_RST_RAD, EA_RST_PROT, EA_RST_WPOL,
     EA_Q0  // then per state: QB QA QT QI QQ_EL QQ_VDW QP_EL QP_VDW QW_EL QW_VDW
 };
-enum { EQ_B = 0, EQ_A, EQ_T, EQ_I, EQ_QQ_EL, EQ_QQ_VDW, EQ_QP_EL, EQ_QP_VDW, EQ_QW_EL, EQ_QW_VDW, EQ_N };
+enum { EQ_B = 0, EQ_A, EQ_T, EQ_I, EQ_QQ_EL, EQ_QQ_VDW, EQ_QP_EL, EQ_QP_VDW, EQ_QW_EL, EQ_QW_VDW, EQ_RST, EQ_N };
 #define QG_NE (EA_Q0 + EQ_N * QG_MAXS)
 // energy record row: 29 ENERGIES + QG_MAXS*15 Q_ENERGIES + Temp, Tfree + QG_MAXOD*(Hij, rkl)
 #define QG_REC_E 0
@@ -229,6 +229,14 @@ struct DevSys {
     int *g_qin;                     // per solute group in a box: the atom that put it on the qp list (its shift)
     const int *mol_start;           // molecules of the box trajectories: first atom (global); TrajInfo::mol0
     double *boxc;                   // per trajectory: box centre (put_back_in_box)
+    // the other p_restrain restraints, one item each (wall restraints one per
+    // atom), padded per trajectory to blocks of QG_BLOCK: kind (-1 padding, 0
+    // position, 1 distance, 2 angle, 3 wall), atoms[3], state (0 = all),
+    // parameters xr_p[6] (FP64) / xr_pf[9] (float; positions as hi/lo offsets)
+    const int *xr_kind, *xr_at, *xr_st, *xr_blk_traj;
+    const double *xr_p;
+    const float *xr_pf;
+    int nxr;
     const uint8_t *qp_skip;
     const int *qp14_first, *qp14_q; // per atom CSR of Q atoms with qconn == 4
     // nbqq
@@ -524,6 +532,7 @@ struct BlockTables {
     int pbc;                           // some trajectory is a periodic box
     // put_back_in_box: one block per trajectory that moves molecules
     const int *pb_traj; int npb;
+    int nxrblk;                        // blocks of the p_restrain items (DevSys::xr_*)
 };
 
 void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L);

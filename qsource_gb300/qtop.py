@@ -302,6 +302,24 @@ def read_inp(text: str) -> dict:
             rstseq.append((int(t[0]), int(t[1]), float(t[2]), int(t[3]) if len(t) > 3 else 0,
                            int(t[4]) if len(t) > 4 else 0))
 
+    # [atom_restraints] / [distance_restraints] / [angle_restraints] /
+    # [wall_restraints] (initialize, src/md.f90:5234-5358); the residue:atom
+    # form of distance restraints is not read
+    def rows(sec, nint_lead, nflt, ntail_int):
+        out = []
+        for ln in secs.get(sec, []):
+            t = ln.split()
+            if any(":" in x for x in t):
+                raise ValueError(f"[{sec}]: residue:atom references are not supported")
+            out.append([int(x) for x in t[:nint_lead]] + [float(x) for x in t[nint_lead:nint_lead + nflt]] +
+                       [int(x) for x in t[nint_lead + nflt:nint_lead + nflt + ntail_int]])
+        return out
+
+    rst_pos = rows("atom_restraints", 1, 6, 1)
+    rst_dist = rows("distance_restraints", 2, 3, 1)
+    rst_angl = rows("angle_restraints", 3, 2, 1)
+    rst_wall = rows("wall_restraints", 2, 4, 1)
+
     def real(d, key, default=None):
         return float(d[key]) if key in d else default
 
@@ -342,6 +360,8 @@ def read_inp(text: str) -> dict:
         "polarisation_force": real(solv, "polarisation_force", -1.0),
         "excluded_freeze": onoff(sph.get("excluded_freeze"), False),
         "sequence_restraints": rstseq,
+        "atom_restraints": rst_pos, "distance_restraints": rst_dist, "angle_restraints": rst_angl,
+        "wall_restraints": rst_wall,
         "langevin_friction": real(md, "langevin_friction"),
         "langevin_random": onoff(md.get("langevin_random"), False),
         "nhchains": int(md["nhchains"]) if "nhchains" in md else 10,
@@ -352,8 +372,7 @@ def read_inp(text: str) -> dict:
         "lambdas": lam,
         "topology": files.get("topology"),
         "fep": files.get("fep"),
-        "unsupported": [s for s in secs if s in ("distance_restraints", "angle_restraints", "wall_restraints",
-                                                  "group_contribution")],
+        "unsupported": [s for s in secs if s in ("group_contribution",)],
     }
 
 

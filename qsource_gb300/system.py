@@ -153,6 +153,14 @@ class System:
         d.nmol = len(im)
         d.istart_mol = arr(im, np.int32)
         d.nsolute_mol = int(g("nsolute_mol", 0))
+        for name, ni, nf in (("rstpos", 2, 6), ("rstdis", 3, 3), ("rstang", 4, 2), ("rstwal", 3, 4)):
+            ia = np.asarray(g(f"{name}_i", np.zeros((0, ni), np.int32)), dtype=np.int32).reshape(-1, ni)
+            fa = np.asarray(g(f"{name}_{'x' if name == 'rstpos' else 'p'}", np.zeros((0, nf))),
+                            dtype=np.float64).reshape(-1, nf)
+            setattr(d, {"rstpos": "nrstr_pos", "rstdis": "nrstr_dist", "rstang": "nrstr_angl",
+                        "rstwal": "nrstr_wall"}[name], len(ia))
+            setattr(d, f"{name}_i", arr(ia, np.int32))
+            setattr(d, f"{name}_{'x' if name == 'rstpos' else 'p'}", arr(fa, np.float64))
         return d
 
     @property
@@ -547,6 +555,26 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
             rows.append((rout, dr, cstb, 0.0))
             rout = rout - dr
         wshell = np.array(rows, dtype=np.float64).reshape(-1, 4)
+    # --- the other p_restrain restraints (0-based atoms; state 0 = every state)
+    def _state(st, what):
+        if st < 0 or st > S:
+            raise ValueError(f"{what}: state {st} outside 0..{S}")
+        return st
+    pos = inp.get("atom_restraints", [])
+    dis = inp.get("distance_restraints", [])
+    ang_r = inp.get("angle_restraints", [])
+    wal = [] if use_pbc else inp.get("wall_restraints", [])
+    rst_extra = dict(
+        rstpos_i=np.array([(r[0] - 1, _state(r[7], "atom restraint")) for r in pos], np.int32).reshape(-1, 2),
+        rstpos_x=np.array([r[1:7] for r in pos], np.float64).reshape(-1, 6),
+        rstdis_i=np.array([(r[0] - 1, r[1] - 1, _state(r[5], "distance restraint")) for r in dis], np.int32).reshape(-1, 3),
+        rstdis_p=np.array([r[2:5] for r in dis], np.float64).reshape(-1, 3),
+        rstang_i=np.array([(r[0] - 1, r[1] - 1, r[2] - 1, _state(r[5], "angle restraint")) for r in ang_r],
+                          np.int32).reshape(-1, 4),
+        rstang_p=np.array([r[3:5] for r in ang_r], np.float64).reshape(-1, 2),
+        rstwal_i=np.array([(r[0] - 1, r[1] - 1, r[6]) for r in wal], np.int32).reshape(-1, 3),
+        rstwal_p=np.array([r[2:6] for r in wal], np.float64).reshape(-1, 4))
+
     # --- periodic box: Q-atom switching atom and the molecules put_back_in_box moves
     qswitch = -1
     if use_pbc and nq:
@@ -563,7 +591,7 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
                rigid_box_centre=int(inp.get("rigid_box_centre", False)),
                istart_mol=np.asarray(istart[:-1], dtype=np.int32), nsolute_mol=nmol - nsolvent_mol)
     return System(
-        **box,
+        **box, **rst_extra,
         natom=natom, nat_solute=nsol, natyps=natyps, ncgp_solute=ncgp_solute, nqat=nq, nstates=S,
         x=x, v=np.zeros(3 * natom), xtop=xtop, crg=crg, iac=iac, excl=excl, shell=shell, iqatom=iqatom,
         mass=mass, avdw=avdw, bvdw=bvdw, ljcod=ljcod, el14_scale=top["el14_scale"], ff_type=top["ff_type"],
