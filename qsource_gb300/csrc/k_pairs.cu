@@ -46,11 +46,19 @@ __device__ __forceinline__ double rinv_d(const double *x, int a, int b, const do
 }
 __device__ __forceinline__ double3 dzero3() { return make_double3(0.0, 0.0, 0.0); }
 
-// Energy accumulator: Kahan-summed FP32 partials, or FP64 terms.
-template <bool D>
+// Energy accumulator of a pair kernel's mode E: 0 Kahan-summed FP32 partials,
+// 1 FP64 terms, 2 none (MD steps whose energies nobody reads).
+template <int E>
 struct EAcc;
 template <>
-struct EAcc<false> {
+struct EAcc<2> {
+    __device__ __forceinline__ void zero() {}
+    __device__ __forceinline__ void term(float, double) {}
+    __device__ __forceinline__ void flush() {}
+    __device__ __forceinline__ long long fx(float, int *) const { return 0; }
+};
+template <>
+struct EAcc<0> {
     KSum k;
     float part;
     __device__ __forceinline__ void zero() { k.zero(); part = 0.f; }
@@ -59,7 +67,7 @@ struct EAcc<false> {
     __device__ __forceinline__ long long fx(float scale, int *st) const { return k.fx(scale, st); }
 };
 template <>
-struct EAcc<true> {
+struct EAcc<1> {
     double s;
     __device__ __forceinline__ void zero() { s = 0.0; }
     __device__ __forceinline__ void term(float, double d) { s += d; }
@@ -74,15 +82,16 @@ struct EAcc<true> {
 // lanes' partial gradients are summed by an xor butterfly (fixed order).
 // BOX: some trajectory of the batch is a periodic box (its kernels subtract
 // the pair shifts; sphere trajectories of the batch have a zero box).
-template <bool EACC, int LW, int MINB, int U, bool BOX>
+template <int E, int LW, int MINB, int U, bool BOX>
 __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int *wgrp, int lrf) {
+    constexpr bool EACC = E == 1;
     __shared__ long long red[5][QG_BLOCK / 32];
     const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LW;
     const int lane = threadIdx.x & (LW - 1);
     const int w = wgrp[idx];
     const int traj = traj_of_entry(S, w, true);
     const TrajInfo &T = S.traj[traj];
-    EAcc<EACC> eww_el, eww_vdw, epw_el, epw_vdw;
+    EAcc<E> eww_el, eww_vdw, epw_el, epw_vdw;
     eww_el.zero(); eww_vdw.zero(); epw_el.zero(); epw_vdw.zero();
     float elrf = 0.f;
     const bool valid = w >= 0 && !S.g_excl[w];
@@ -244,6 +253,7 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
             }
         }
     }
+    if (E == 2) return;   // no energies on this step
     // pair energies are summed from both sides: half of each thread's sum
     const int slots[5] = {EA_WW_EL, EA_WW_VDW, EA_PW_EL, EA_PW_VDW, EA_LRF};
     long long ev[5] = {eww_el.fx(0.5f, S.status), eww_vdw.fx(0.5f, S.status), epw_el.fx(0.5f, S.status),
@@ -271,15 +281,16 @@ __device__ __forceinline__ PairFlags pair_flags(const DevSys &S, int i, int j) {
 
 // nonbond_pp (src/md.f90:13069-13155) and the solute side of nonbond_pw, plus
 // lrf_taylor, for one non-Q solute atom.
-template <bool EACC, int LW, bool BOX>
+template <int E, int LW, bool BOX>
 __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *satom, int lrf) {
+    constexpr bool EACC = E == 1;
     __shared__ long long red[5][QG_BLOCK / 32];
     const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LW;
     const int lane = threadIdx.x & (LW - 1);
     const int i = satom[idx];
     const int traj = traj_of_entry(S, i, false);
     const TrajInfo &T = S.traj[traj];
-    EAcc<EACC> epp_el, epp_vdw, epw_el, epw_vdw;
+    EAcc<E> epp_el, epp_vdw, epw_el, epw_vdw;
     epp_el.zero(); epp_vdw.zero(); epw_el.zero(); epw_vdw.zero();
     float elrf = 0.f;
     const bool valid = i >= 0 && S.aq[i] < 0 && !S.g_excl[S.agrp[i]];
@@ -298,7 +309,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         if (pbc) { swh = S.pos[swg]; swl = S.poslo[swg]; }
         // one pair term: LJ code c, el14 factor for 1-4 pairs (nonbond_pp :13102-13111),
         // periodic shift (sf, sd) of the group pair (nonbond_pp_box :13226-13228)
-        auto pair = [&](int j, int c, EAcc<EACC> &e_el, EAcc<EACC> &e_vdw, const float3 sf, const double3 sd) {
+        auto pair = [&](int j, int c, EAcc<E> &e_el, EAcc<E> &e_vdw, const float3 sf, const double3 sd) {
             const int tj = S.atype[j];
             const float4 jh = S.pos[j], jl = S.poslo[j];
             const int li = lj_index(T, ti, tj, c);
@@ -415,6 +426,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
             fx_addf(S.fx + 3 * i + 2, gz, S.status);
         }
     }
+    if (E == 2) return;   // no energies on this step
     const int slots[5] = {EA_PP_EL, EA_PP_VDW, EA_PW_EL, EA_PW_VDW, EA_LRF};
     long long ev[5] = {epp_el.fx(0.5f, S.status), epp_vdw.fx(0.5f, S.status), epw_el.fx(0.5f, S.status),
                        epw_vdw.fx(0.5f, S.status), f2fx_chk(elrf, S.status)};
@@ -745,51 +757,55 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
 // blocks 1 or 6) and its neighbours per loop iteration (1/2/4); lanes per
 // solute atom (4/8/16).  The FP64-energy
 // variants (drop-in calls) use 8 lanes.
-template <int LW, int MINB, bool BOX>
+template <int E, int LW, int MINB, bool BOX>
 static void water_fp32(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf) {
     const int nb = B.nwgrp * LW / QG_BLOCK;
-    if (B.tune.unroll_water == 1) k_nb_water<false, LW, MINB, 1, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
-    else if (B.tune.unroll_water == 4) k_nb_water<false, LW, MINB, 4, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
-    else k_nb_water<false, LW, MINB, 2, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    if (B.tune.unroll_water == 1) k_nb_water<E, LW, MINB, 1, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    else if (B.tune.unroll_water == 4) k_nb_water<E, LW, MINB, 4, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    else k_nb_water<E, LW, MINB, 2, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
 }
-template <bool BOX>
-static void water_launch(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
-    if (fp64_energy) {
-        k_nb_water<true, 8, 1, 2, BOX><<<B.nwgrp * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
-    } else {
-        const bool m6 = B.tune.minb_water == 6;
-        switch (B.tune.lw_water) {
-        case 4: m6 ? water_fp32<4, 6, BOX>(S, B, L, lrf) : water_fp32<4, 1, BOX>(S, B, L, lrf); break;
-        case 16: m6 ? water_fp32<16, 6, BOX>(S, B, L, lrf) : water_fp32<16, 1, BOX>(S, B, L, lrf); break;
-        default: m6 ? water_fp32<8, 6, BOX>(S, B, L, lrf) : water_fp32<8, 1, BOX>(S, B, L, lrf); break;
-        }
+template <int E, bool BOX>
+static void water_shapes(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf) {
+    const bool m6 = B.tune.minb_water == 6;
+    switch (B.tune.lw_water) {
+    case 4: m6 ? water_fp32<E, 4, 6, BOX>(S, B, L, lrf) : water_fp32<E, 4, 1, BOX>(S, B, L, lrf); break;
+    case 16: m6 ? water_fp32<E, 16, 6, BOX>(S, B, L, lrf) : water_fp32<E, 16, 1, BOX>(S, B, L, lrf); break;
+    default: m6 ? water_fp32<E, 8, 6, BOX>(S, B, L, lrf) : water_fp32<E, 8, 1, BOX>(S, B, L, lrf); break;
     }
 }
-void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
+template <bool BOX>
+static void water_launch(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, int emode) {
+    if (emode == QG_PAIR_E_FP64) k_nb_water<1, 8, 1, 2, BOX><<<B.nwgrp * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    else if (emode == QG_PAIR_E_NONE) water_shapes<2, BOX>(S, B, L, lrf);
+    else water_shapes<0, BOX>(S, B, L, lrf);
+}
+void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, int emode) {
     if (!B.nwgrp) return;
     prof_begin(L, "k_nb_water");
-    if (B.pbc) water_launch<true>(S, B, L, lrf, fp64_energy);
-    else water_launch<false>(S, B, L, lrf, fp64_energy);
+    if (B.pbc) water_launch<true>(S, B, L, lrf, emode);
+    else water_launch<false>(S, B, L, lrf, emode);
     prof_end(L);
     (*L.nlaunch)++;
 }
-template <bool BOX>
-static void solute_launch(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
-    if (fp64_energy) {
-        k_nb_solute<true, 8, BOX><<<B.nsatom * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf);
-    } else {
-        switch (B.tune.lw_solute) {
-        case 4: k_nb_solute<false, 4, BOX><<<B.nsatom * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
-        case 16: k_nb_solute<false, 16, BOX><<<B.nsatom * 16 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
-        default: k_nb_solute<false, 8, BOX><<<B.nsatom * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
-        }
+template <int E, bool BOX>
+static void solute_shapes(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf) {
+    switch (B.tune.lw_solute) {
+    case 4: k_nb_solute<E, 4, BOX><<<B.nsatom * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
+    case 16: k_nb_solute<E, 16, BOX><<<B.nsatom * 16 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
+    default: k_nb_solute<E, 8, BOX><<<B.nsatom * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf); break;
     }
 }
-void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy) {
+template <bool BOX>
+static void solute_launch(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, int emode) {
+    if (emode == QG_PAIR_E_FP64) k_nb_solute<1, 8, BOX><<<B.nsatom * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, lrf);
+    else if (emode == QG_PAIR_E_NONE) solute_shapes<2, BOX>(S, B, L, lrf);
+    else solute_shapes<0, BOX>(S, B, L, lrf);
+}
+void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, int emode) {
     if (!B.nsatom) return;
     prof_begin(L, "k_nb_solute");
-    if (B.pbc) solute_launch<true>(S, B, L, lrf, fp64_energy);
-    else solute_launch<false>(S, B, L, lrf, fp64_energy);
+    if (B.pbc) solute_launch<true>(S, B, L, lrf, emode);
+    else solute_launch<false>(S, B, L, lrf, emode);
     prof_end(L);
     (*L.nlaunch)++;
 }

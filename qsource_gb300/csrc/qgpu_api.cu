@@ -1028,7 +1028,7 @@ static void list_ops(qgpu_handle *h, LaunchCtx &L, bool md = true) {
 // does not depend on their order): they run concurrently on side streams that
 // fork from and join back into the handle's stream (also inside graph
 // capture).  The per-kernel profiler keeps them in one stream.
-static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, bool fp64_energy, EaccSel esel) {
+static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, int emode, EaccSel esel) {
     const bool wpol = (terms & QGPU_TERMS_RESTRAINT) != 0;
     if (!(terms & QGPU_TERMS_NONBOND)) {
         launch_misc(h->S, h->B, L, terms, esel);
@@ -1036,8 +1036,8 @@ static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, bool fp64_energy,
         return;
     }
     if (L.prof || !h->ev_fork) {
-        launch_nb_water(h->S, h->B, L, 1, fp64_energy);
-        launch_nb_solute(h->S, h->B, L, 1, fp64_energy);
+        launch_nb_water(h->S, h->B, L, 1, emode);
+        launch_nb_solute(h->S, h->B, L, 1, emode);
         launch_qw(h->S, h->B, L, esel);
         launch_qp(h->S, h->B, L, esel);
         launch_misc(h->S, h->B, L, terms, esel);
@@ -1050,8 +1050,8 @@ static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, bool fp64_energy,
         cudaStreamWaitEvent(h->side[k], h->ev_fork, 0);
         Ls[k] = LaunchCtx{h->side[k], L.nlaunch};
     }
-    launch_nb_water(h->S, h->B, L, 1, fp64_energy);
-    launch_nb_solute(h->S, h->B, Ls[0], 1, fp64_energy);
+    launch_nb_water(h->S, h->B, L, 1, emode);
+    launch_nb_solute(h->S, h->B, Ls[0], 1, emode);
     launch_qw(h->S, h->B, Ls[1], esel);
     launch_qp(h->S, h->B, Ls[2], esel);
     launch_misc(h->S, h->B, Ls[2], terms, esel);
@@ -1062,7 +1062,12 @@ static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, bool fp64_energy,
     }
 }
 
-static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every);
+static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every, int emode);
+// Pair-energy mode of an MD step: its pair energies are read only when the
+// step is recorded (step % ene_every == 0).
+static int step_emode(long long step, int ene_every) {
+    return step % ene_every == 0 ? QG_PAIR_E_FP32 : QG_PAIR_E_NONE;
+}
 
 // One NBcycle block (list build + NBcycle steps + record-counter tick),
 // captured once as a CUDA graph and replayed.
@@ -1074,7 +1079,16 @@ static int replay_block(qgpu_handle *h, LaunchCtx &L, int ene_every) {
         long long before = h->nlaunch;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
         list_ops(h, L);
-        for (int k = 0; k < NB; ++k) step_ops(h, L, k, ene_every);
+        // a replayed block starts at a multiple of NB: where ene_every divides
+        // NB the recorded steps of the block are fixed; where NB divides
+        // ene_every only the block's first step can be recorded; elsewhere the
+        // pair kernels keep their energies on every step
+        for (int k = 0; k < NB; ++k) {
+            int em = QG_PAIR_E_FP32;
+            if (NB % ene_every == 0) em = step_emode(k, ene_every);
+            else if (ene_every % NB == 0) em = k == 0 ? QG_PAIR_E_FP32 : QG_PAIR_E_NONE;
+            step_ops(h, L, k, ene_every, em);
+        }
         launch_tick(L, h->recctl_d, NB);
         CK(cudaStreamEndCapture(h->stream, &g));
         CK(cudaGraphInstantiate(&h->graph, g, 0));
@@ -1089,9 +1103,9 @@ static int replay_block(qgpu_handle *h, LaunchCtx &L, int ene_every) {
     return 0;
 }
 
-static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every) {
+static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every, int emode) {
     EaccSel esel{EACC_RECORD, h->recctl_d, k, ene_every};
-    force_ops(h, L, QGPU_TERMS_ALL, false, esel);
+    force_ops(h, L, QGPU_TERMS_ALL, emode, esel);
     if (h->all_fused) {
         // the update's last block per trajectory ends the step
         launch_update_f(h->S, h->B, L, esel, h->NBcycle, 0, FIN_TEMP | FIN_STEP | FIN_NH, h->rec_d, h->rec_cap);
@@ -1214,9 +1228,9 @@ int qgpu_forces(qgpu_handle *h, int32_t traj, int32_t terms, double *d, qgpu_ene
     ensure_double(h, L);
     CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
     if (terms & QGPU_TERMS_STEP_PRECISION)
-        force_ops(h, L, terms, false, EaccSel{EACC_FP32, h->recctl_d, 0, 1});
+        force_ops(h, L, terms, QG_PAIR_E_FP32, EaccSel{EACC_FP32, h->recctl_d, 0, 1});
     else
-        force_ops(h, L, terms, true, EaccSel{EACC_FP64, h->recctl_d, 0, 1});
+        force_ops(h, L, terms, QG_PAIR_E_FP64, EaccSel{EACC_FP64, h->recctl_d, 0, 1});
     launch_finalize(h->S, L, 0, h->ecur_d, h->zero_d, 0, 1, 1);
     std::vector<double> row(QG_REC);
     CK(cudaMemcpyAsync(row.data(), h->ecur_d + (size_t)traj * QG_REC, QG_REC * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1340,7 +1354,7 @@ int qgpu_profile(qgpu_handle *h, int32_t nsteps, char *names, double *ms, int64_
     ensure_double(h, L);
     for (int k = 0; k < nsteps; ++k) {
         if (h->step % h->NBcycle == 0) { list_ops(h, L); h->lists_built = 1; }
-        step_ops(h, L, 0, ene_every);
+        step_ops(h, L, 0, ene_every, step_emode(h->step, ene_every));
         launch_tick(L, h->recctl_d, 1);
         h->step += 1;
     }
@@ -1397,7 +1411,7 @@ int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every) {
             if (int rc = replay_block(h, L, ene_every)) return rc;
         } else {
             if (h->step % NB == 0) { list_ops(h, L); h->lists_built = 1; }
-            step_ops(h, L, 0, ene_every);
+            step_ops(h, L, 0, ene_every, step_emode(h->step, ene_every));
             launch_tick(L, h->recctl_d, 1);
             h->step += 1;
         }
@@ -1451,8 +1465,9 @@ static int time_variant(qgpu_handle *h, LaunchCtx &L, void (*launch)(qgpu_handle
     return 0;
 }
 
-static void tune_water(qgpu_handle *h, LaunchCtx &L) { launch_nb_water(h->S, h->B, L, 1, false); }
-static void tune_solute(qgpu_handle *h, LaunchCtx &L) { launch_nb_solute(h->S, h->B, L, 1, false); }
+// the shapes are timed in the form most MD steps run (no pair energies)
+static void tune_water(qgpu_handle *h, LaunchCtx &L) { launch_nb_water(h->S, h->B, L, 1, QG_PAIR_E_NONE); }
+static void tune_solute(qgpu_handle *h, LaunchCtx &L) { launch_nb_solute(h->S, h->B, L, 1, QG_PAIR_E_NONE); }
 static void tune_qw(qgpu_handle *h, LaunchCtx &L) {
     launch_qw(h->S, h->B, L, EaccSel{EACC_FP32, h->zero_d, 0, 1});
 }
@@ -1709,7 +1724,7 @@ int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink si
             if (int rc = replay_block(h, L, ene_every)) return rc;
         } else {
             if (h->step % NB == 0) { list_ops(h, L); h->lists_built = 1; }
-            step_ops(h, L, 0, ene_every);
+            step_ops(h, L, 0, ene_every, step_emode(h->step, ene_every));
             launch_tick(L, h->recctl_d, 1);
             h->step += 1;
         }

@@ -550,8 +550,11 @@ struct EaccSel {
     const int *recctl;
     int k, ene_every;
 };
-void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy);
-void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, bool fp64_energy);
+// pair-energy mode of the water and solute pair kernels: FP32 Kahan sums,
+// FP64 terms (drop-in calls), or none (MD steps whose energies are not recorded)
+enum { QG_PAIR_E_FP32 = 0, QG_PAIR_E_FP64 = 1, QG_PAIR_E_NONE = 2 };
+void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, int emode);
+void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, int emode);
 void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
 void launch_qp(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
 // nonbond_qq, Q bonded, classical bonded, restraints and off-diagonals in one launch
