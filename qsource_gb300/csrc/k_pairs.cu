@@ -489,6 +489,8 @@ __device__ __forceinline__ bool eacc_on(const EaccSel &e) {
     if (e.mode == EACC_RECORD) return e.ene_every > 0 && ((e.recctl[0] + e.k) % e.ene_every) == 0;
     return false;
 }
+// energies wanted at all: every drop-in call, and the recorded MD steps
+__device__ __forceinline__ bool energies_on(const EaccSel &e) { return e.mode != EACC_RECORD || eacc_on(e); }
 
 // per-state energy sums of one thread: Kahan FP32, or FP64 terms
 struct QE {
@@ -528,7 +530,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
     const int w = wgrp[idx];
     const int traj = traj_of_entry(S, w, true);
     const TrajInfo &T = S.traj[traj];
-    const bool acc = eacc_on(esel);
+    const bool acc = eacc_on(esel), want = energies_on(esel);
     q_load(S, T, sh);
     const int NS = T.nstates;
     QE eel, evdw;
@@ -584,7 +586,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
                         const double r6sd = T.qvdw ? r6hcd + S.sc_d[sci] : r6hcd;
                         eel.d[s] += S.crg_d[a0] * S.qcrg_d[q * QG_MAXS + s] * rid;
                         evdw.d[s] += S.qw_Ad[q * QG_MAXS + s] / (r6sd * r6sd) - S.qw_Bd[q * QG_MAXS + s] / r6sd;
-                    } else {
+                    } else if (want) {
                         eel.k[s].add(Vel); evdw.k[s].add(Va - Vb);
                     }
                 }
@@ -603,7 +605,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
                     if (s >= NS) break;
                     const float Vel = ah[a].w * S.qcrg_f[q * QG_MAXS + s] * ri;
                     if (acc) eel.d[s] += S.crg_d[a0 + a] * S.qcrg_d[q * QG_MAXS + s] * rid;
-                    else eel.k[s].add(Vel);
+                    else if (want) eel.k[s].add(Vel);
                     dv -= lam[s] * ri2 * Vel;
                 }
                 gx[a] += dv * d.x; gy[a] += dv * d.y; gz[a] += dv * d.z;
@@ -622,7 +624,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
             fx_addf(S.fx + 3 * (a0 + a) + 2, gz[a], S.status);
         }
     q_flush(S, T, sh);
-    q_energies(S, traj, NS, eel, evdw, acc, EQ_QW_EL, EQ_QW_VDW, sh);
+    if (want) q_energies(S, traj, NS, eel, evdw, acc, EQ_QW_EL, EQ_QW_VDW, sh);
 }
 
 // nonbond_qp (src/md.f90:13788-13921) / nonbond_qp_qvdw (14097-14230).
@@ -635,7 +637,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
     const int j = satom[idx];
     const int traj = traj_of_entry(S, j, false);
     const TrajInfo &T = S.traj[traj];
-    const bool acc = eacc_on(esel);
+    const bool acc = eacc_on(esel), want = energies_on(esel);
     q_load(S, T, sh);
     const int NS = T.nstates;
     QE eel, evdw;
@@ -733,7 +735,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
                     if (c == 3) Veld *= T.el14d;
                     eel.d[s] += Veld;
                     evdw.d[s] += Ad / (r6sd * r6sd) - Bd / r6sd;
-                } else {
+                } else if (want) {
                     eel.k[s].add(Vel); evdw.k[s].add(Va - Vb);
                 }
             }
@@ -749,7 +751,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, Eac
         fx_addf(S.fx + 3 * j + 2, gz, S.status);
     }
     q_flush(S, T, sh);
-    q_energies(S, traj, NS, eel, evdw, acc, EQ_QP_EL, EQ_QP_VDW, sh);
+    if (want) q_energies(S, traj, NS, eel, evdw, acc, EQ_QP_EL, EQ_QP_VDW, sh);
 }
 
 // Launch shapes (the autotuner's choice, BlockTables::tune): lanes per water
