@@ -331,14 +331,19 @@ def main():
     vs = torch.empty(n3, dtype=torch.float64).pin_memory().numpy()
     eng.coords_all(xs, vs)
     e2e_blocks = max(2, min(nblk // 2, 100))
+    from qsource_gb300 import abi
+    cap = 4 * ntraj
+    E_rows, EQ_rows = (abi.Energies * cap)(), (abi.QEnergy * (cap * abi.MAX_STATES))()
+    tr_rows, st_rows = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     nrows = 0
     for b in range(e2e_blocks):
         eng.set_coords_all(xs, vs)
-        rows = eng.run(NB, ene_every=NB)
-        nrows += sum(len(r) for r in rows)
+        nrows += eng.run_rows(NB, NB, E_rows, EQ_rows, tr_rows, st_rows)
         eng.coords_all(xs, vs)
+    if nrows != ntraj * e2e_blocks:
+        raise RuntimeError(f"e2e: {nrows} energy records for {e2e_blocks} blocks of {ntraj} trajectories")
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e = world * ntraj * e2e_blocks * NB * FS_PER_STEP * 1e-6 * 86400.0 / e2e_s
@@ -390,7 +395,8 @@ def main():
                                      if tuning else "default")},
         "e2e": {"value": round(e2e, 3), "unit": "ns/day", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "how": "per 10-step block: qgpu_set_coords_all of x,v of all 32 trajectories from pinned memory, "
-                       "qgpu_run with an energy sink, qgpu_get_coords_all (host wall clock)"},
+                       "qgpu_run_rows (the block's energy records of every trajectory into host arrays), "
+                       "qgpu_get_coords_all (host wall clock)"},
         "roofline": roof,
         "kernel_share": share,
         "kernel_roofline": per_kernel,

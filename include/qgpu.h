@@ -325,6 +325,13 @@ int qgpu_shake(qgpu_handle *h, int32_t traj, const double *xx, double *x, int32_
    and handed to `sink` after the block (sink may be NULL). */
 int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every,
              qgpu_ene_sink sink, void *user);
+/* qgpu_run with the energy records written to host arrays instead of a
+   callback (a Fortran host's put_ene loop reads them in bulk): row r is
+   E_rows[r], EQ_rows[r*QGPU_MAX_STATES ...], step_rows[r], traj_rows[r], in
+   the order qgpu_run's sink would see them; at most cap rows, *nrows gets the
+   count written (rows beyond cap are dropped, *nrows says how many came). */
+int qgpu_run_rows(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_energies *E_rows,
+                  qgpu_qenergy *EQ_rows, int32_t *traj_rows, int32_t *step_rows, int32_t cap, int32_t *nrows);
 
 /* Autotuner.  Times every launch shape of the pair kernels on this handle's
    own lists -- lanes per target water (4/8/16), the water kernel's register

@@ -134,6 +134,7 @@ EXPORTS = {
     "qgpu_mlp_predict": (_i32, [_P, _P, _i32, _P]),
     "qgpu_mlp_train": (_i32, [_P, _P, _P, _P, _P, _i32, _i32, C.c_float, _i32, _P, _P]),
     "qgpu_set_tuning": (_i32, [C.c_void_p, _P]),
+    "qgpu_run_rows": (_i32, [C.c_void_p, _i32, _i32, _P, _P, _P, _P, _i32, _P]),
     "qgpu_calc_rms": (_i32, [_P, _i32, _i32, _P, _i32, _P, _P]),
     "qgpu_calc_com": (_i32, [_P, _i32, _i32, _P, _i32, _P, _P]),
     "qgpu_calc_geom": (_i32, [_P, _i32, _i32, _i32, _P, _P, _P]),

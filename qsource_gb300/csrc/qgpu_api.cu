@@ -1655,6 +1655,37 @@ int qgpu_fep_result(qgpu_handle *h, double *dgf, double *dgr, double *dg, double
     return 0;
 }
 
+struct RowSink {
+    qgpu_energies *E;
+    qgpu_qenergy *EQ;
+    int32_t *traj, *step;
+    int32_t cap, n;
+};
+static void row_sink(void *user, int32_t traj, int32_t step, const qgpu_qenergy *eq, int32_t ns, const qgpu_energies *e) {
+    RowSink *r = (RowSink *)user;
+    if (r->n < r->cap) {
+        if (r->E) r->E[r->n] = *e;
+        if (r->EQ)
+            for (int s = 0; s < QGPU_MAX_STATES; ++s) {
+                qgpu_qenergy q{};
+                if (s < ns) q = eq[s];
+                r->EQ[(size_t)r->n * QGPU_MAX_STATES + s] = q;
+            }
+        if (r->traj) r->traj[r->n] = traj;
+        if (r->step) r->step[r->n] = step;
+    }
+    r->n++;
+}
+
+int qgpu_run_rows(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_energies *E_rows, qgpu_qenergy *EQ_rows,
+                  int32_t *traj_rows, int32_t *step_rows, int32_t cap, int32_t *nrows) {
+    if (!h || cap < 0 || !nrows) return fail(QGPU_E_INVALID, "qgpu_run_rows: bad arguments");
+    RowSink r{E_rows, EQ_rows, traj_rows, step_rows, cap, 0};
+    const int rc = qgpu_run(h, nsteps, ene_every, ene_every > 0 ? row_sink : nullptr, &r);
+    *nrows = r.n;
+    return rc;
+}
+
 int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink sink, void *user) {
     if (!h || nsteps < 0) return fail(QGPU_E_INVALID, "bad arguments");
     if (ene_every <= 0) ene_every = 1 << 30;

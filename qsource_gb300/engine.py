@@ -189,6 +189,15 @@ class Engine:
         raw = names.raw
         return {raw[64 * k:64 * (k + 1)].split(b"\0")[0].decode(): (float(ms[k]), int(cnt[k])) for k in range(n.value)}
 
+    def run_rows(self, nsteps: int, ene_every: int, E, EQ, traj, step) -> int:
+        """qgpu_run_rows: the energy records in preallocated arrays (E:
+        Energies[cap], EQ: QEnergy[cap * MAX_STATES], traj/step: int32[cap]).
+        Returns the number of rows the run produced."""
+        n = C.c_int32()
+        self._check(self.lib.qgpu_run_rows(self.h, nsteps, ene_every, C.cast(E, C.c_void_p), C.cast(EQ, C.c_void_p),
+                                           abi.ptr(traj), abi.ptr(step), len(traj), C.byref(n)))
+        return n.value
+
     def run(self, nsteps: int, ene_every: int = 0, collect: bool = True):
         """Run nsteps MD steps of every trajectory on the device.  Returns a
         list per trajectory of (step, E dict, [EQ dicts]) rows."""

@@ -228,6 +228,23 @@ def test_step_precision_forces(systems, name):
         assert not energies_close(EQ[s_], EQo[s_], EQ_KEYS)
 
 
+def test_run_rows_equals_the_sink(systems):
+    """qgpu_run_rows hands over the same records as qgpu_run's callback."""
+    from qsource_gb300 import abi
+    s = systems["cfg1"]
+    a, b = _engine([s, s]), _engine([s, s])
+    rows = a.run(20, ene_every=5)
+    cap = 16
+    E, EQ = (abi.Energies * cap)(), (abi.QEnergy * (cap * abi.MAX_STATES))()
+    tr, st = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
+    n = b.run_rows(20, 5, E, EQ, tr, st)
+    assert n == 8
+    for r in range(n):
+        step, e, eq = rows[tr[r]][[x[0] for x in rows[tr[r]]].index(st[r])]
+        assert E[r].as_dict() == e
+        assert [EQ[r * abi.MAX_STATES + k].as_dict() for k in range(s.nstates)] == eq
+
+
 def test_run_is_bit_deterministic(systems):
     s = systems["cfg2"]
     a = _engine(s)
