@@ -58,6 +58,20 @@ def features(lam: np.ndarray, stats: np.ndarray, kT: float) -> np.ndarray:
     return X
 
 
+def window_spread(lam: np.ndarray, stats: np.ndarray) -> np.ndarray:
+    """s(lambda) at each window from qgpu_fep_result statistics: the pooled
+    standard deviation of the forward and backward energy gaps divided by the
+    lambda step (kcal/mol per unit lambda) -- the network's training target
+    when stats come from a long run."""
+    n = len(lam)
+    dl = np.abs(np.gradient(lam)) if n > 1 else np.ones(1)
+    out = np.empty(n)
+    for w in range(n):
+        v = ([stats[w, 2]] if w + 1 < n else []) + ([stats[w, 5]] if w > 0 else [])
+        out[w] = np.sqrt(max(float(np.mean(v)), 0.0)) / dl[w]
+    return out
+
+
 def place(lam_pilot: np.ndarray, s_pilot: np.ndarray, nwin: int) -> np.ndarray:
     """nwin windows from 0 to 1 at equal increments of the thermodynamic
     length of the piecewise-linear s(lambda) through the pilot points."""
@@ -119,6 +133,22 @@ class MLP:
             self._check(self.lib.qgpu_mlp_predict(abi.ptr(self.params), abi.ptr(xb), len(xb), abi.ptr(ob)))
             out[a:a + BATCH] = ob
         return out
+
+    def train_batches(self, X: np.ndarray, Y: np.ndarray, epochs: int, iters: int = 20, lr: float = 1e-3, seed: int = 0):
+        """Adam over more than 64 rows: each epoch walks a seeded shuffle of
+        the rows in batches of up to 64, `iters` steps per batch (the Adam
+        state carries over).  Returns the loss of the last step of each batch."""
+        X = np.asarray(X, dtype=np.float32)
+        Y = np.asarray(Y, dtype=np.float32)
+        rng = np.random.default_rng(seed)
+        out = []
+        for _ in range(epochs):
+            idx = rng.permutation(len(X))
+            for a in range(0, len(X), BATCH):
+                sel = idx[a:a + BATCH]
+                loss, _ = self.train(X[sel], Y[sel], iters, lr)
+                out.append(float(loss[-1]))
+        return np.array(out)
 
     def train(self, X: np.ndarray, Y: np.ndarray, iters: int, lr: float = 1e-3):
         """Full-batch Adam on up to 64 rows; returns (loss per step, last gradient)."""
