@@ -522,15 +522,27 @@ __device__ __forceinline__ void q_energies(const DevSys &S, int traj, int NS, co
 }
 
 // nonbond_qw_spc, src/md.f90:14411-14570.  LG lanes per water.
-template <int LG>
-__global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, EaccSel esel) {
+// E: 0 energies as esel asks (FP32 Kahan or FP64 terms); 2 none (MD steps
+// whose energies are not recorded: fewer registers, more resident blocks).
+// The per-state O-side constants of every Q atom (A, B, charge, soft-core
+// term) are staged in shared memory with the Q positions.
+template <int LG, int E>
+__global__ void __launch_bounds__(QG_BLOCK, E == 2 ? 6 : 1) k_qw(DevSys S, const int *wgrp, EaccSel esel) {
     __shared__ QShared sh;
+    __shared__ float4 qwp[QG_MAXQ * QG_MAXS];
     const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LG;
     const int lane = threadIdx.x & (LG - 1);
     const int w = wgrp[idx];
     const int traj = traj_of_entry(S, w, true);
     const TrajInfo &T = S.traj[traj];
-    const bool acc = eacc_on(esel), want = energies_on(esel);
+    const bool acc = E != 2 && eacc_on(esel), want = E != 2 && energies_on(esel);
+    const int ntq = T.natyps + T.nqat;
+    for (int k = threadIdx.x; k < T.nqat * QG_MAXS; k += blockDim.x) {
+        const int q = T.q0 + k / QG_MAXS, s = k % QG_MAXS;
+        const size_t sci = (size_t)T.sc0 + ((size_t)(k / QG_MAXS) * ntq + (size_t)S.qw_sc[q]) * QG_MAXS + s;
+        qwp[k] = make_float4(S.qw_A[q * QG_MAXS + s], S.qw_B[q * QG_MAXS + s], S.qcrg_f[q * QG_MAXS + s],
+                             T.qvdw ? S.sc_f[sci] : 0.f);
+    }
     q_load(S, T, sh);
     const int NS = T.nstates;
     QE eel, evdw;
@@ -556,7 +568,6 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
     float lam[QG_MAXS];
 #pragma unroll
     for (int s = 0; s < QG_MAXS; ++s) lam[s] = T.lambdaf[s];
-    const int ntq = T.natyps + T.nqat;
     for (int iq0 = 0; iq0 < T.nqat; iq0 += LG) {
         const int iq = iq0 + lane;
         const bool on = iq < T.nqat;
@@ -575,14 +586,14 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
 #pragma unroll
                 for (int s = 0; s < QG_MAXS; ++s) {
                     if (s >= NS) break;
-                    const size_t sci = (size_t)T.sc0 + ((size_t)iq * ntq + (size_t)S.qw_sc[q]) * QG_MAXS + s;
-                    const float A = S.qw_A[q * QG_MAXS + s], B = S.qw_B[q * QG_MAXS + s];
-                    const float r6s = T.qvdw ? r6hc + S.sc_f[sci] : r6hc;
+                    const float4 p = qwp[iq * QG_MAXS + s];
+                    const float r6s = T.qvdw ? r6hc + p.w : r6hc;
                     const float ir6 = __frcp_rn(r6s);
-                    const float Va = A * ir6 * ir6, Vb = B * ir6;
-                    const float Vel = ah[0].w * S.qcrg_f[q * QG_MAXS + s] * ri;
+                    const float Va = p.x * ir6 * ir6, Vb = p.y * ir6;
+                    const float Vel = ah[0].w * p.z * ri;
                     dv += lam[s] * ri2 * (-Vel - (12.f * Va - 6.f * Vb) * (r6hc * ir6));
                     if (acc) {
+                        const size_t sci = (size_t)T.sc0 + ((size_t)iq * ntq + (size_t)S.qw_sc[q]) * QG_MAXS + s;
                         const double r6sd = T.qvdw ? r6hcd + S.sc_d[sci] : r6hcd;
                         eel.d[s] += S.crg_d[a0] * S.qcrg_d[q * QG_MAXS + s] * rid;
                         evdw.d[s] += S.qw_Ad[q * QG_MAXS + s] / (r6sd * r6sd) - S.qw_Bd[q * QG_MAXS + s] / r6sd;
@@ -603,7 +614,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
 #pragma unroll
                 for (int s = 0; s < QG_MAXS; ++s) {
                     if (s >= NS) break;
-                    const float Vel = ah[a].w * S.qcrg_f[q * QG_MAXS + s] * ri;
+                    const float Vel = ah[a].w * qwp[iq * QG_MAXS + s].z * ri;
                     if (acc) eel.d[s] += S.crg_d[a0 + a] * S.qcrg_d[q * QG_MAXS + s] * rid;
                     else if (want) eel.k[s].add(Vel);
                     dv -= lam[s] * ri2 * Vel;
@@ -629,15 +640,16 @@ __global__ void __launch_bounds__(QG_BLOCK) k_qw(DevSys S, const int *wgrp, Eacc
 
 // nonbond_qp (src/md.f90:13788-13921) / nonbond_qp_qvdw (14097-14230).
 // LG lanes per solute atom of the qp list.
-template <int LG>
-__global__ void __launch_bounds__(QG_BLOCK) k_qp(DevSys S, const int *satom, EaccSel esel) {
+// E as in k_qw.
+template <int LG, int E>
+__global__ void __launch_bounds__(QG_BLOCK, E == 2 ? 6 : 1) k_qp(DevSys S, const int *satom, EaccSel esel) {
     __shared__ QShared sh;
     const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LG;
     const int lane = threadIdx.x & (LG - 1);
     const int j = satom[idx];
     const int traj = traj_of_entry(S, j, false);
     const TrajInfo &T = S.traj[traj];
-    const bool acc = eacc_on(esel), want = energies_on(esel);
+    const bool acc = E != 2 && eacc_on(esel), want = E != 2 && energies_on(esel);
     q_load(S, T, sh);
     const int NS = T.nstates;
     QE eel, evdw;
@@ -819,20 +831,28 @@ static int qw_lanes(const BlockTables &B) {
     return B.max_nqat <= 16 ? 1 : (B.max_nqat <= 48 ? 2 : 4);
 }
 
-void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
+template <int E>
+static void qw_shapes(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
+    const int lg = qw_lanes(B);
+    if (lg == 1) k_qw<1, E><<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+    else if (lg == 2) k_qw<2, E><<<B.nwgrp * 2 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+    else k_qw<4, E><<<B.nwgrp * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+}
+// emode QG_PAIR_E_NONE (an MD step whose energies are not recorded) takes the
+// energy-free instantiation; every other mode lets esel decide on the device.
+void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int emode) {
     if (!B.nwgrp) return;
     prof_begin(L, "k_qw");
-    const int lg = qw_lanes(B);
-    if (lg == 1) k_qw<1><<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
-    else if (lg == 2) k_qw<2><<<B.nwgrp * 2 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
-    else k_qw<4><<<B.nwgrp * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+    if (emode == QG_PAIR_E_NONE) qw_shapes<2>(S, B, L, e);
+    else qw_shapes<0>(S, B, L, e);
     prof_end(L);
     (*L.nlaunch)++;
 }
-void launch_qp(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
+void launch_qp(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int emode) {
     if (!B.nsatom) return;
     prof_begin(L, "k_qp");
-    k_qp<4><<<B.nsatom * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, e);
+    if (emode == QG_PAIR_E_NONE) k_qp<4, 2><<<B.nsatom * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, e);
+    else k_qp<4, 0><<<B.nsatom * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.satom, e);
     prof_end(L);
     (*L.nlaunch)++;
 }

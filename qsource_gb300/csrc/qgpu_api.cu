@@ -1038,8 +1038,8 @@ static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, int emode, EaccSe
     if (L.prof || !h->ev_fork) {
         launch_nb_water(h->S, h->B, L, 1, emode);
         launch_nb_solute(h->S, h->B, L, 1, emode);
-        launch_qw(h->S, h->B, L, esel);
-        launch_qp(h->S, h->B, L, esel);
+        launch_qw(h->S, h->B, L, esel, emode);
+        launch_qp(h->S, h->B, L, esel, emode);
         launch_misc(h->S, h->B, L, terms, esel);
         if (wpol) launch_watpol(h->S, h->B, L, esel);
         return;
@@ -1052,8 +1052,8 @@ static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, int emode, EaccSe
     }
     launch_nb_water(h->S, h->B, L, 1, emode);
     launch_nb_solute(h->S, h->B, Ls[0], 1, emode);
-    launch_qw(h->S, h->B, Ls[1], esel);
-    launch_qp(h->S, h->B, Ls[2], esel);
+    launch_qw(h->S, h->B, Ls[1], esel, emode);
+    launch_qp(h->S, h->B, Ls[2], esel, emode);
     launch_misc(h->S, h->B, Ls[2], terms, esel);
     if (wpol) launch_watpol(h->S, h->B, Ls[1], esel);
     for (int k = 0; k < QG_NSIDE; ++k) {
@@ -1469,7 +1469,7 @@ static int time_variant(qgpu_handle *h, LaunchCtx &L, void (*launch)(qgpu_handle
 static void tune_water(qgpu_handle *h, LaunchCtx &L) { launch_nb_water(h->S, h->B, L, 1, QG_PAIR_E_NONE); }
 static void tune_solute(qgpu_handle *h, LaunchCtx &L) { launch_nb_solute(h->S, h->B, L, 1, QG_PAIR_E_NONE); }
 static void tune_qw(qgpu_handle *h, LaunchCtx &L) {
-    launch_qw(h->S, h->B, L, EaccSel{EACC_FP32, h->zero_d, 0, 1});
+    launch_qw(h->S, h->B, L, EaccSel{EACC_FP32, h->zero_d, 0, 1}, QG_PAIR_E_NONE);
 }
 
 int qgpu_set_tuning(qgpu_handle *h, const int32_t *tuning) {

@@ -555,8 +555,8 @@ struct EaccSel {
 enum { QG_PAIR_E_FP32 = 0, QG_PAIR_E_FP64 = 1, QG_PAIR_E_NONE = 2 };
 void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, int emode);
 void launch_nb_solute(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, int emode);
-void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
-void launch_qp(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e);
+void launch_qw(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int emode);
+void launch_qp(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int emode);
 // nonbond_qq, Q bonded, classical bonded, restraints and off-diagonals in one launch
 // On each launch the kernel evaluates in FP64 from x when eacc_on(e), else in
 // FP32 from the float coordinates.
