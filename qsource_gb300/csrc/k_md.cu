@@ -244,6 +244,14 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
     const int next = esel.recctl[0] + esel.k + 1;
     const bool want_x = !ekin_only && ((next % nbcycle == 0) ||
                         (esel.mode == EACC_RECORD && esel.ene_every > 0 && next % esel.ene_every == 0));
+    // warp 0's SHAKE inputs (first constraint of its water, d0^2), loaded
+    // before the atom's own chain of loads so that their latencies overlap
+    int c0 = -1;
+    float2 d2[3] = {};
+    if (water_blk && !ekin_only && t < 32) {
+        c0 = ucon[blockIdx.x * QG_UBLK + 3 * t];
+        if (c0 >= 0) { d2[0] = S.shk_d2hl[c0]; d2[1] = S.shk_d2hl[c0 + 1]; d2[2] = S.shk_d2hl[c0 + 2]; }
+    }
     const int tr = a >= 0 ? S.atraj[a] : -1 - a;
     const TrajInfo &T = S.traj[tr];
     float4 h = make_float4(0, 0, 0, 0), l = h;
@@ -282,7 +290,6 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
     if (water_blk && !ekin_only) {
         __syncthreads();
         if (t < 32) {
-            const int c0 = ucon[blockIdx.x * QG_UBLK + 3 * t];
             int nits = 0;
             if (c0 >= 0) {
                 float4 wh[3], wl[3];
@@ -294,7 +301,6 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
                     wh[k] = s_h[q]; wl[k] = s_l[q]; ww[k] = s_w[q];
                     wD[k] = make_float3(s_D[0][q], s_D[1][q], s_D[2][q]);
                 }
-                const float2 d2[3] = {S.shk_d2hl[c0], S.shk_d2hl[c0 + 1], S.shk_d2hl[c0 + 2]};
                 bool fail = false;
                 nits = shake_water_f(wh, wl, ww, d2, wD, &fail);
                 if (fail) { atomicOr(S.status, ST_SHAKE); atomicCAS(S.status + 1, 0, tr + 1); }
@@ -475,13 +481,14 @@ __device__ void finalize_traj(const DevSys &S, int tr, int lane, double *v, int 
         }
     }
     if (do_temp) {
-        float e4[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            float p = 0.f;
-            for (int b = lane; b < T.ekin_nblk; b += 32) p += __ldcg(S.ekin_part + (size_t)(T.ekin_blk0 + b) * 4 + c);
-            e4[c] = warp_sum_f(p);
+        // the four partials of a block are one float4 (slots 4 b .. 4 b + 3)
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 *ep = reinterpret_cast<const float4 *>(S.ekin_part) + T.ekin_blk0;
+        for (int b = lane; b < T.ekin_nblk; b += 32) {
+            const float4 q = __ldcg(ep + b);
+            p.x += q.x; p.y += q.y; p.z += q.z; p.w += q.w;
         }
+        const float e4[4] = {warp_sum_f(p.x), warp_sum_f(p.y), warp_sum_f(p.z), warp_sum_f(p.w)};
         if (lane == 0) {
             float Tfsu = e4[1], Tfsv = e4[3];
             const float Ekin = e4[0] + e4[2];
