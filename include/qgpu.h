@@ -385,6 +385,48 @@ int qgpu_ene_close(qgpu_handle *h, int32_t traj);
    pairs, offd_Hr: nframes*noffd (Hij, rkl)).  No device involved. */
 int qgpu_enefile_write(const char *path, int32_t nframes, int32_t nstates, const qgpu_qenergy *frames,
                        int32_t noffd, const int32_t *offd_ij, const double *offd_Hr);
+
+/* qfep's input (src/qfep.f90:110-230), in the order it reads it. */
+#define QGPU_QFEP_MAXCOUP 45                       /* state pairs of QGPU_MAX_STATES states */
+#define QGPU_QFEP_P2 (5 + QGPU_MAX_STATES)          /* doubles per Part 2 row */
+#define QGPU_QFEP_P3 7                              /* doubles per Part 3 row */
+typedef struct {
+    int32_t nstates;      /* states per frame */
+    int32_t noffd;        /* off-diagonal elements stored in the files ("predefined") */
+    double kT;
+    int32_t nskip;        /* frames skipped at the start of every file */
+    int32_t gas;          /* 1: V_s = Q bonded + qq (el + vdW) + restraint ("calculation mode") */
+    int32_t nbins;        /* energy-gap bins */
+    int32_t nmin;         /* minimum points per bin (>= 1) */
+    double alpha[QGPU_MAX_STATES];  /* shift of each state's energy; alpha[0] is taken as 0 */
+    double scale_hij;     /* noffd > 0: Hij(1,2) = scale_hij * the file's Hij when > 0 (two states) */
+    int32_t ncoup;        /* noffd == 0: couplings Hij = A exp(-mu (r - r0)) exp(-eta (r - r0)^2),
+                             r = the first file coupling's distance; the files then hold ncoup
+                             off-diagonal entries per frame */
+    int32_t coup_ij[2 * QGPU_QFEP_MAXCOUP];       /* 1-based state pairs */
+    double coup_A[QGPU_QFEP_MAXCOUP], coup_mu[QGPU_QFEP_MAXCOUP], coup_eta[QGPU_QFEP_MAXCOUP],
+        coup_rxy0[QGPU_QFEP_MAXCOUP];
+    double coeff[QGPU_MAX_STATES];  /* reaction coordinate: gap = sum_s coeff[s] (V_s + alpha[s]) */
+} qgpu_qfep_params;
+/* qfep Parts 1-3 (src/qfep.f90:416-835) on nfiles energy files in lambda
+   order, host code.  Per frame the state energies are shifted by alpha, the
+   EVB ground state Eg is the lowest eigenvalue of H (H_ii = V_i, H_ij the
+   coupling; two states: the closed form of qfep with the mixing c1 = 1/(1 +
+   ((Eg - V_1)/H_12)^2), c2 = 1 - c1), the gap is sum_s coeff_s V_s.
+     part1[3 w + 0..2]: dGf(w) (0 for the last window), dGr(w) (0 for the
+       first), dG(w) (Part 1);
+     gaprange[2]: smallest and largest gap over the frames after nskip;
+     part2[(w nbins + b) QGPU_QFEP_P2]: window w, bin b: points, gap at the
+       bin centre, dGg (ground state), <c1>, <c2>, dGv_1 .. dGv_nstates
+       (diabatic curves); values are written where points >= nmin, else 0;
+     part3[b QGPU_QFEP_P3]: points over all windows, gap, <dGg>, <dGg> - min,
+       <c1>, <c2>, <r_xy> of the bin (values where points >= nmin);
+       min is qfep's: over every bin's sum including empty ones (0);
+     npts[w]: frames read from file w.
+   Returns QGPU_E_INVALID for unreadable files, bad parameters or a zero gap
+   range. */
+int qgpu_qfep_evb(int32_t nfiles, const char *const *paths, const qgpu_qfep_params *p, double *part1,
+                  double *gaprange, double *part2, double *part3, int32_t *npts);
 /* Free-energy perturbation over a chain of lambda windows, accumulated on
    the device from every recorded frame with a nonzero step (qfep Part 1,
    src/qfep.f90:609-661): window w = trajectory chain[w]; per frame

@@ -107,6 +107,21 @@ class QEnergy(C.Structure):
         return d
 
 
+MAX_STATES = 10
+QFEP_MAXCOUP = 45
+QFEP_P2 = 5 + MAX_STATES
+QFEP_P3 = 7
+
+
+class QfepParams(C.Structure):
+    """qgpu_qfep_params: qfep's input in the order it reads it."""
+    _fields_ = [("nstates", _i32), ("noffd", _i32), ("kT", _f64), ("nskip", _i32), ("gas", _i32), ("nbins", _i32),
+                ("nmin", _i32), ("alpha", _f64 * MAX_STATES), ("scale_hij", _f64), ("ncoup", _i32),
+                ("coup_ij", _i32 * (2 * QFEP_MAXCOUP)), ("coup_A", _f64 * QFEP_MAXCOUP),
+                ("coup_mu", _f64 * QFEP_MAXCOUP), ("coup_eta", _f64 * QFEP_MAXCOUP),
+                ("coup_rxy0", _f64 * QFEP_MAXCOUP), ("coeff", _f64 * MAX_STATES)]
+
+
 ENE_SINK = C.CFUNCTYPE(None, C.c_void_p, _i32, _i32, C.POINTER(QEnergy), _i32, C.POINTER(Energies))
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
@@ -142,6 +157,7 @@ EXPORTS = {
     "qgpu_ene_open": (_i32, [C.c_void_p, _i32, C.c_char_p]),
     "qgpu_ene_close": (_i32, [C.c_void_p, _i32]),
     "qgpu_enefile_write": (_i32, [C.c_char_p, _i32, _i32, C.POINTER(QEnergy), _i32, _P, _P]),
+    "qgpu_qfep_evb": (_i32, [_i32, C.POINTER(C.c_char_p), C.POINTER(QfepParams), _P, _P, _P, _P, _P]),
     "qgpu_fep_start": (_i32, [C.c_void_p, _i32, _P, _f64, _i32]),
     "qgpu_fep_result": (_i32, [C.c_void_p, _P, _P, _P, _P]),
     "qgpu_sync": (_i32, [C.c_void_p]),

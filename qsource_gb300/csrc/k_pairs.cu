@@ -831,9 +831,12 @@ static int qw_lanes(const BlockTables &B) {
     return B.max_nqat <= 16 ? 1 : (B.max_nqat <= 48 ? 2 : 4);
 }
 
+// The shape is tuned on the energy-free form; the energy form (165 registers,
+// Kahan sums per state) needs at least two lanes per water to hide latency.
 template <int E>
 static void qw_shapes(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
-    const int lg = qw_lanes(B);
+    int lg = qw_lanes(B);
+    if (E != 2 && lg == 1) lg = 2;
     if (lg == 1) k_qw<1, E><<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
     else if (lg == 2) k_qw<2, E><<<B.nwgrp * 2 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
     else k_qw<4, E><<<B.nwgrp * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
