@@ -335,6 +335,43 @@ def test_fep_sums_match_qfep_on_engine_files(engine_lib, tmp_path):
         assert np.allclose(a, b, rtol=1e-9, atol=1e-9), (a, b)
 
 
+def test_evb_mapping_on_engine_files(engine_lib, tmp_path):
+    """Seven windows of a two-state EVB droplet (coupling 15 exp(-0.3 r_12)
+    between Q atoms 1 and 2) run as one batch with energy files attached:
+    every frame's Hij is A exp(-mu rkl) of its own distance; qfep Parts 1-3
+    on the engine's files (qgpu_qfep_evb) equal the numpy restatement of
+    qfep, and Part 1 equals the device's streaming FEP sums."""
+    from oracle import qfep_ref
+    from qsource_gb300 import qfep, synth
+    nw, kT, nskip = 7, 0.596163, 4
+    qa = synth.neutral_charges(np.random.default_rng(77), 8, 0.5)
+    qb = synth.neutral_charges(np.random.default_rng(78), 8, 0.5)
+    systems = [synth.synthetic(18.0, 8, 8, np.stack([qa, qb], 1), (1 - w / (nw - 1), w / (nw - 1)), 4100 + w,
+                               offdiag=[(1, 2, 1, 2, 15.0, 0.3)]) for w in range(nw)]
+    e = _engine(systems)
+    paths = [str(tmp_path / f"evb{w}.en") for w in range(nw)]
+    for w, p in enumerate(paths):
+        e.ene_open(w, p)
+    e.fep_start(list(range(nw)), kT, nskip)
+    e.run(300, ene_every=5)
+    for w in range(nw):
+        e.ene_close(w)
+    for p in paths:
+        _, frames = qfep_ref.read_en(p, 2, 1)
+        assert len(frames) == 59
+        for _, od in frames:
+            (i, j, hij, rkl), = od
+            assert (i, j) == (1, 2) and abs(hij - 15.0 * np.exp(-0.3 * rkl)) <= 1e-12 * 15.0
+    kw = dict(noffd=1, scale_hij=1.0, nskip=nskip, nbins=10, nmin=3)
+    got = qfep.evb(paths, 2, kT, lib=engine_lib, **kw)
+    ref = qfep_ref.evb(paths, 2, kT, **kw)
+    for key in ("part1", "gap", "part2", "part3"):
+        np.testing.assert_allclose(got[key], ref[key], rtol=0, atol=1e-9, err_msg=key)
+    dgf, dgr, dg, _ = e.fep_result()
+    assert np.allclose(got["part1"][:, 2], dg, rtol=1e-9, atol=1e-9)
+    assert (got["part3"][:, 0] >= 3).sum() >= 5
+
+
 @pytest.mark.parametrize("shape", [[4, 1, 4, 1, 1], [8, 6, 8, 2, 2], [16, 1, 16, 4, 4], [16, 6, 8, 0, 1]])
 def test_every_launch_shape_matches_oracle(systems, shape):
     """Each launch shape the autotuner may pick (lanes per water / register
