@@ -230,28 +230,25 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
             gy[a] += __shfl_xor_sync(S_GROUP_MASK, gy[a], o, LW);
             gz[a] += __shfl_xor_sync(S_GROUP_MASK, gz[a], o, LW);
         }
-    {
-        if (valid && lane == 0) {
-            if (lrf) {
-                const float *ph = S.g_phif + (size_t)w * QG_NPHI;
-                const float4 c = S.g_centf[w];
-#pragma unroll
-                for (int a = 0; a < 3; ++a)
-                {
-                    // centre - x_a = ((c - O_hi) - O_lo) - d_a
-                    const float3 da = a == 0 ? make_float3(0.f, 0.f, 0.f)
-                                             : (a == 1 ? make_float3(r0.w, r1.w, r2.x) : make_float3(r2.y, r2.z, r2.w));
-                    elrf += lrf_atom(ph, ((c.x - r0.x) - r1.x) - da.x, ((c.y - r0.y) - r1.y) - da.y,
-                                     ((c.z - r0.z) - r1.z) - da.z, T.chg_solv[a], gx[a], gy[a], gz[a]);
-                }
-            }
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                fx_addf(S.fx + 3 * (a0 + a), gx[a], S.status);
-                fx_addf(S.fx + 3 * (a0 + a) + 1, gy[a], S.status);
-                fx_addf(S.fx + 3 * (a0 + a) + 2, gz[a], S.status);
-            }
+    // after the butterfly every lane holds the three sums: lane a (0..2)
+    // adds the Taylor term of atom a and stores its gradient
+    if (valid && lane < 3) {
+        const int a = lane;
+        float fx = a == 0 ? gx[0] : (a == 1 ? gx[1] : gx[2]);
+        float fy = a == 0 ? gy[0] : (a == 1 ? gy[1] : gy[2]);
+        float fz = a == 0 ? gz[0] : (a == 1 ? gz[1] : gz[2]);
+        if (lrf) {
+            const float *ph = S.g_phif + (size_t)w * QG_NPHI;
+            const float4 c = S.g_centf[w];
+            // centre - x_a = ((c - O_hi) - O_lo) - d_a
+            const float3 da = a == 0 ? make_float3(0.f, 0.f, 0.f)
+                                     : (a == 1 ? make_float3(r0.w, r1.w, r2.x) : make_float3(r2.y, r2.z, r2.w));
+            elrf += lrf_atom(ph, ((c.x - r0.x) - r1.x) - da.x, ((c.y - r0.y) - r1.y) - da.y,
+                             ((c.z - r0.z) - r1.z) - da.z, T.chg_solv[a], fx, fy, fz);
         }
+        fx_addf(S.fx + 3 * (a0 + a), fx, S.status);
+        fx_addf(S.fx + 3 * (a0 + a) + 1, fy, S.status);
+        fx_addf(S.fx + 3 * (a0 + a) + 2, fz, S.status);
     }
     if (E == 2) return;   // no energies on this step
     // pair energies are summed from both sides: half of each thread's sum

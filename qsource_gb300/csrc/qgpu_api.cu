@@ -1468,6 +1468,11 @@ static int time_variant(qgpu_handle *h, LaunchCtx &L, void (*launch)(qgpu_handle
 // the shapes are timed in the form most MD steps run (no pair energies)
 static void tune_water(qgpu_handle *h, LaunchCtx &L) { launch_nb_water(h->S, h->B, L, 1, QG_PAIR_E_NONE); }
 static void tune_solute(qgpu_handle *h, LaunchCtx &L) { launch_nb_solute(h->S, h->B, L, 1, QG_PAIR_E_NONE); }
+// the whole force stage of an unrecorded MD step, its kernels concurrent on
+// the side streams as in the step itself
+static void tune_forces(qgpu_handle *h, LaunchCtx &L) {
+    force_ops(h, L, QGPU_TERMS_ALL, QG_PAIR_E_NONE, EaccSel{EACC_RECORD, h->zero_d, 0, 0});
+}
 static void tune_qw(qgpu_handle *h, LaunchCtx &L) {
     launch_qw(h->S, h->B, L, EaccSel{EACC_FP32, h->zero_d, 0, 1}, QG_PAIR_E_NONE);
 }
@@ -1524,6 +1529,37 @@ int qgpu_autotune(qgpu_handle *h, int32_t *tuning) {
             }
         }
         h->B.tune = best;
+        // Second pass: in a step the force kernels share the GPU (side
+        // streams), and the shape that is fastest alone is not always the
+        // one that overlaps best.  Coordinate descent from the first pass's
+        // choice on the time of the concurrent force stage.
+        if (h->B.nwgrp && h->ev_fork) {
+            tb = 1e30f;
+            for (int lw : {4, 8, 16})
+                for (int mb : {1, 6})
+                    for (int uw : {1, 2, 4}) {
+                        h->B.tune.lw_water = lw; h->B.tune.minb_water = mb; h->B.tune.unroll_water = uw;
+                        if (int rc = time_variant(h, L, tune_forces, &t)) return rc;
+                        if (t < tb) { tb = t; best.lw_water = lw; best.minb_water = mb; best.unroll_water = uw; }
+                    }
+            h->B.tune = best;
+            if (h->B.nsatom) {
+                tb = 1e30f;
+                for (int ls : {4, 8, 16}) {
+                    h->B.tune.lw_solute = ls;
+                    if (int rc = time_variant(h, L, tune_forces, &t)) return rc;
+                    if (t < tb) { tb = t; best.lw_solute = ls; }
+                }
+                h->B.tune = best;
+            }
+            tb = 1e30f;
+            for (int lq : {1, 2, 4}) {
+                h->B.tune.lg_qw = lq;
+                if (int rc = time_variant(h, L, tune_forces, &t)) return rc;
+                if (t < tb) { tb = t; best.lg_qw = lq; }
+            }
+            h->B.tune = best;
+        }
         // the timing launches added into the gradient and energies
         CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
         CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
