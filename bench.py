@@ -244,6 +244,10 @@ def main():
     ap.add_argument("--ref-max-steps", type=int, default=100, help="cap on the reference arm's timed steps")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
+    ap.add_argument("--tuning", default=None,
+                    help="fixed launch shapes lanes_water,min_blocks_water,lanes_solute,lanes_qw,unroll_water "
+                         "instead of the autotuner's (profiling runs: the autotuner's timings mean nothing "
+                         "under a profiler that serialises kernels)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                     help="MD step precision (qgpu_set_precision): double-float master / FP64 master")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-trajectory-at-a-time GPU form")
@@ -291,7 +295,11 @@ def main():
     ntraj = len(systems)
     natoms = sum(s.natom for s in systems)
     eng = Engine(systems)
-    tuning = eng.autotune() if not args.no_tune else None
+    if args.tuning:
+        tuning = [int(v) for v in args.tuning.split(",")]
+        eng.set_tuning(tuning)
+    else:
+        tuning = eng.autotune() if not args.no_tune else None
     if args.precision == "fp64":
         from qsource_gb300.abi import QGPU_PRECISION_FP64
         eng.set_precision(QGPU_PRECISION_FP64)

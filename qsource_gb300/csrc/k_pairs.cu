@@ -37,12 +37,31 @@ __device__ __forceinline__ float lrf_atom(const float *ph, float dx, float dy, f
     return 0.5f * q * V;
 }
 
-// FP64 inverse distance from the master coordinates (accurate-energy mode),
+// FP64 reciprocal square root and reciprocal by Newton-Raphson iteration
+// from an FP32 hardware estimate: y <- y (3 - x y^2) / 2 and y <- y (2 - x y)
+// square the relative error each step, so two steps take the FP32 estimate's
+// ~1e-7 below FP64 rounding.  The FP64 energy paths use them in place of FP64
+// rsqrt and division (GB300 issues FP64 at 1/64 of the FP32 rate).
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    double y = (double)rsqrtf((float)x);
+    y = y * (1.5 - 0.5 * x * y * y);
+    return y * (1.5 - 0.5 * x * y * y);
+}
+__device__ __forceinline__ double rcp_nr(double x) {
+    double y = (double)__frcp_rn((float)x);
+    y = y * (2.0 - x * y);
+    return y * (2.0 - x * y);
+}
+
+// FP64 squared distance from the master coordinates (accurate-energy mode),
 // of the difference x_b - x_a less the pair's periodic shift s (zero in a sphere)
-__device__ __forceinline__ double rinv_d(const double *x, int a, int b, const double3 s) {
+__device__ __forceinline__ double dist2_d(const double *x, int a, int b, const double3 s) {
     const double dx = (x[3 * b] - x[3 * a]) - s.x, dy = (x[3 * b + 1] - x[3 * a + 1]) - s.y,
                  dz = (x[3 * b + 2] - x[3 * a + 2]) - s.z;
-    return rsqrt(dx * dx + dy * dy + dz * dz);
+    return dx * dx + dy * dy + dz * dz;
+}
+__device__ __forceinline__ double rinv_d(const double *x, int a, int b, const double3 s) {
+    return rsqrt_nr(dist2_d(x, a, b, s));
 }
 __device__ __forceinline__ double3 dzero3() { return make_double3(0.0, 0.0, 0.0); }
 
@@ -578,7 +597,7 @@ __global__ void __launch_bounds__(QG_BLOCK, E == 2 ? 6 : 1) k_qw(DevSys S, const
                 const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
                 const float r6hc = r2 * r2 * r2, ri = rsqrtf(r2), ri2 = ri * ri;
                 double rid = 0.0, r6hcd = 0.0;
-                if (acc) { rid = rinv_d(S.x, qa, a0, swd); const double r2d = 1.0 / (rid * rid); r6hcd = r2d * r2d * r2d; }
+                if (acc) { const double r2d = dist2_d(S.x, qa, a0, swd); rid = rsqrt_nr(r2d); r6hcd = r2d * r2d * r2d; }
                 float dv = 0.f;
 #pragma unroll
                 for (int s = 0; s < QG_MAXS; ++s) {
@@ -593,7 +612,8 @@ __global__ void __launch_bounds__(QG_BLOCK, E == 2 ? 6 : 1) k_qw(DevSys S, const
                         const size_t sci = (size_t)T.sc0 + ((size_t)iq * ntq + (size_t)S.qw_sc[q]) * QG_MAXS + s;
                         const double r6sd = T.qvdw ? r6hcd + S.sc_d[sci] : r6hcd;
                         eel.d[s] += S.crg_d[a0] * S.qcrg_d[q * QG_MAXS + s] * rid;
-                        evdw.d[s] += S.qw_Ad[q * QG_MAXS + s] / (r6sd * r6sd) - S.qw_Bd[q * QG_MAXS + s] / r6sd;
+                        const double ir6d = rcp_nr(r6sd);
+                        evdw.d[s] += S.qw_Ad[q * QG_MAXS + s] * ir6d * ir6d - S.qw_Bd[q * QG_MAXS + s] * ir6d;
                     } else if (want) {
                         eel.k[s].add(Vel); evdw.k[s].add(Va - Vb);
                     }
@@ -682,7 +702,7 @@ __global__ void __launch_bounds__(QG_BLOCK, E == 2 ? 6 : 1) k_qp(DevSys S, const
             const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
             const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = r2 * r2 * r2;
             double rid = 0.0, r6d = 0.0;
-            if (acc) { rid = rinv_d(S.x, qa, j, sqd); const double r2d = 1.0 / (rid * rid); r6d = r2d * r2d * r2d; }
+            if (acc) { const double r2d = dist2_d(S.x, qa, j, sqd); rid = rsqrt_nr(r2d); r6d = r2d * r2d * r2d; }
             float dv = 0.f;
 #pragma unroll
             for (int s = 0; s < QG_MAXS; ++s) {
@@ -743,7 +763,8 @@ __global__ void __launch_bounds__(QG_BLOCK, E == 2 ? 6 : 1) k_qp(DevSys S, const
                     double Veld = S.qcrg_d[q * QG_MAXS + s] * S.crg_d[j] * rid;
                     if (c == 3) Veld *= T.el14d;
                     eel.d[s] += Veld;
-                    evdw.d[s] += Ad / (r6sd * r6sd) - Bd / r6sd;
+                    const double ir6d = rcp_nr(r6sd);
+                    evdw.d[s] += Ad * ir6d * ir6d - Bd * ir6d;
                 } else if (want) {
                     eel.k[s].add(Vel); evdw.k[s].add(Va - Vb);
                 }
