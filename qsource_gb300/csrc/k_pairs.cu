@@ -849,12 +849,13 @@ static int qw_lanes(const BlockTables &B) {
     return B.max_nqat <= 16 ? 1 : (B.max_nqat <= 48 ? 2 : 4);
 }
 
-// The shape is tuned on the energy-free form; the energy form (165 registers,
-// Kahan sums per state) needs at least two lanes per water to hide latency.
+// The shape is tuned on the energy-free form.  The energy form of a recorded
+// MD step evaluates the per-state energies in FP64 and is bound by the FP64
+// pipe: one lane per water is its fastest shape on the benchmark batch (70 us
+// against 81 with four lanes and 93 with two).
 template <int E>
 static void qw_shapes(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
-    int lg = qw_lanes(B);
-    if (E != 2 && lg == 1) lg = 2;
+    const int lg = E == 2 ? qw_lanes(B) : 1;
     if (lg == 1) k_qw<1, E><<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
     else if (lg == 2) k_qw<2, E><<<B.nwgrp * 2 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
     else k_qw<4, E><<<B.nwgrp * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
