@@ -335,6 +335,40 @@ def test_fep_sums_match_qfep_on_engine_files(engine_lib, tmp_path):
         assert np.allclose(a, b, rtol=1e-9, atol=1e-9), (a, b)
 
 
+def test_dg_matches_oracle_dynamics(engine_lib):
+    """The benchmark metric's qualifier, |dG - oracle| <= 0.1 kcal/mol: five
+    lambda windows of the 18 A droplet run 200 steps from the same start on
+    the GPU (mixed precision, qfep Part 1 sums on the device from the frames
+    at steps 5, 10, ..., 195) and in the FP64 oracle (qfep's Zwanzig sums of
+    its own per-step state energies at the same steps)."""
+    from qsource_gb300 import synth
+    nw, kT, n, every = 5, 0.596163, 200, 5
+    systems = [synth.config(1, window=w, lambdas=(1 - w / (nw - 1), w / (nw - 1))) for w in range(nw)]
+    e = _engine(systems)
+    e.fep_start(list(range(nw)), kT, 0)
+    e.run(n, ene_every=every, collect=False)
+    _, _, dg, st = e.fep_result()
+    V, lam = [], []
+    for s in systems:
+        o = _oracle(s)
+        o.temperature()
+        rc, _, oq, _ = o.md_run(n)
+        assert rc == 0
+        V.append(np.array([[oq[k][i]["total"] for i in range(2)] for k in range(every, n, every)]))
+        lam.append(np.array(s.lambdas[:2], dtype=float))
+    assert np.all(st[:, 0] == len(V[0]))
+
+    def zwanzig(a, b):
+        dv = V[a] @ lam[b] - V[a] @ lam[a]
+        return -kT * np.log(np.mean(np.exp(-dv / kT)))
+    G = [0.0]
+    for w in range(1, nw):
+        G.append(G[-1] + 0.5 * (zwanzig(w - 1, w) - zwanzig(w, w - 1)))
+    err = np.abs(np.array(G) - dg).max()
+    print("dG GPU", np.round(dg, 4).tolist(), "oracle", np.round(G, 4).tolist(), "max |diff|", err)
+    assert err <= 0.1
+
+
 def test_evb_mapping_on_engine_files(engine_lib, tmp_path):
     """Seven windows of a two-state EVB droplet (coupling 15 exp(-0.3 r_12)
     between Q atoms 1 and 2) run as one batch with energy files attached:
