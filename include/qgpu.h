@@ -335,7 +335,8 @@ int qgpu_run_rows(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_energi
 
 /* Autotuner.  Times every launch shape of the pair kernels on this handle's
    own lists -- lanes per target water (4/8/16), the water kernel's register
-   bound (1 or 6 resident blocks) and neighbours per loop iteration (1/2/4),
+   bound (1 or 6 resident blocks) and neighbours per loop iteration (1/2/4; 3: a software
+   pipeline, one neighbour per iteration with the next one's loads in flight),
    lanes per Q-water item (1/2/4), lanes per solute atom (4/8/16) -- keeps the
    fastest, and caches the choice per device and system size for later
    handles of the process.  tuning[5] (may be NULL) receives {lanes_water,

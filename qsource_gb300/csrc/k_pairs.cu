@@ -181,9 +181,31 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
             }
             eww_el.flush(); eww_vdw.flush();
         };
-        // U neighbours per iteration keep U sets of loads in flight
+        // U neighbours per iteration keep U sets of loads in flight; U == 3 is
+        // a software pipeline instead: while one neighbour computes, the next
+        // one's record and the index after it are in flight
         int k = lane;
-        for (; k + (U - 1) * LW < nw; k += U * LW) {
+        if (U == 3) {
+            if (k < nw) {
+                int b = lst[k];
+                float4 q0 = S.wrec[b], q1 = S.wrec[b + 1], q2 = S.wrec[b + 2];
+                int bn = k + LW < nw ? lst[k + LW] : 0;
+                for (;;) {
+                    const bool more = k + LW < nw;
+                    float4 n0 = make_float4(0.f, 0.f, 0.f, 0.f), n1 = n0, n2 = n0;
+                    int bnn = 0;
+                    if (more) {
+                        n0 = S.wrec[bn]; n1 = S.wrec[bn + 1]; n2 = S.wrec[bn + 2];
+                        if (k + 2 * LW < nw) bnn = lst[k + 2 * LW];
+                    }
+                    ww(b, q0, q1, q2);
+                    if (!more) break;
+                    k += LW; b = bn; bn = bnn; q0 = n0; q1 = n1; q2 = n2;
+                }
+            }
+            k = nw;
+        }
+        for (; U != 3 && k + (U - 1) * LW < nw; k += U * LW) {
             int bb[U];
             float4 p[U][3];
 #pragma unroll
@@ -793,6 +815,7 @@ template <int E, int LW, int MINB, bool BOX>
 static void water_fp32(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf) {
     const int nb = B.nwgrp * LW / QG_BLOCK;
     if (B.tune.unroll_water == 1) k_nb_water<E, LW, MINB, 1, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
+    else if (B.tune.unroll_water == 3) k_nb_water<E, LW, MINB, 3, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
     else if (B.tune.unroll_water == 4) k_nb_water<E, LW, MINB, 4, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
     else k_nb_water<E, LW, MINB, 2, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
 }

@@ -1481,7 +1481,7 @@ int qgpu_set_tuning(qgpu_handle *h, const int32_t *tuning) {
     if (!h || !tuning) return fail(QGPU_E_INVALID, "qgpu_set_tuning: bad arguments");
     const int lw = tuning[0], mb = tuning[1], ls = tuning[2], lq = tuning[3], uw = tuning[4];
     if ((lw != 4 && lw != 8 && lw != 16) || (mb != 1 && mb != 6) || (ls != 4 && ls != 8 && ls != 16) ||
-        (lq != 0 && lq != 1 && lq != 2 && lq != 4) || (uw != 1 && uw != 2 && uw != 4))
+        (lq != 0 && lq != 1 && lq != 2 && lq != 4) || (uw != 1 && uw != 2 && uw != 3 && uw != 4))
         return fail(QGPU_E_INVALID, "qgpu_set_tuning: unsupported shape");
     CK(cudaStreamSynchronize(h->stream));
     h->B.tune.lw_water = lw; h->B.tune.minb_water = mb; h->B.tune.lw_solute = ls; h->B.tune.lg_qw = lq;
@@ -1505,7 +1505,7 @@ int qgpu_autotune(qgpu_handle *h, int32_t *tuning) {
         if (h->B.nwgrp) {
             for (int lw : {4, 8, 16})
                 for (int mb : {1, 6})
-                    for (int uw : {1, 2, 4}) {
+                    for (int uw : {1, 2, 3, 4}) {
                         h->B.tune.lw_water = lw; h->B.tune.minb_water = mb; h->B.tune.unroll_water = uw;
                         if (int rc = time_variant(h, L, tune_water, &t)) return rc;
                         if (t < tb) { tb = t; best.lw_water = lw; best.minb_water = mb; best.unroll_water = uw; }
@@ -1537,7 +1537,7 @@ int qgpu_autotune(qgpu_handle *h, int32_t *tuning) {
             tb = 1e30f;
             for (int lw : {4, 8, 16})
                 for (int mb : {1, 6})
-                    for (int uw : {1, 2, 4}) {
+                    for (int uw : {1, 2, 3, 4}) {
                         h->B.tune.lw_water = lw; h->B.tune.minb_water = mb; h->B.tune.unroll_water = uw;
                         if (int rc = time_variant(h, L, tune_forces, &t)) return rc;
                         if (t < tb) { tb = t; best.lw_water = lw; best.minb_water = mb; best.unroll_water = uw; }

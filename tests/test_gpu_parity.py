@@ -406,7 +406,7 @@ def test_evb_mapping_on_engine_files(engine_lib, tmp_path):
     assert (got["part3"][:, 0] >= 3).sum() >= 5
 
 
-@pytest.mark.parametrize("shape", [[4, 1, 4, 1, 1], [8, 6, 8, 2, 2], [16, 1, 16, 4, 4], [16, 6, 8, 0, 1]])
+@pytest.mark.parametrize("shape", [[4, 1, 4, 1, 1], [8, 6, 8, 2, 2], [16, 1, 16, 4, 4], [16, 6, 8, 0, 1], [4, 6, 8, 1, 3]])
 def test_every_launch_shape_matches_oracle(systems, shape):
     """Each launch shape the autotuner may pick (lanes per water / register
     bound / lanes per solute atom / lanes per Q-water item) gives the oracle's
