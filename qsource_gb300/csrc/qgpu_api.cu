@@ -1176,7 +1176,9 @@ int qgpu_set_coords_all(qgpu_handle *h, const double *x, const double *v) {
     if (!h) return fail(QGPU_E_INVALID, "null handle");
     const size_t n = 3 * (size_t)h->S.natom;
     LaunchCtx L{h->stream, &h->nlaunch};
-    ensure_double(h, L);
+    // x and v both replaced: nothing of the float master needs keeping
+    if (x && v) h->master = 0;
+    else ensure_double(h, L);
     if (x) CK(cudaMemcpyAsync(h->S.x, x, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (v) CK(cudaMemcpyAsync(h->S.v, v, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     launch_mirror_range(h->S, L, 0, h->S.natom);
