@@ -427,6 +427,22 @@ def test_every_launch_shape_matches_oracle(systems, shape):
         assert not energies_close(EQ[s_], EQo[s_], EQ_KEYS)
 
 
+def test_pipelined_water_loop_is_bit_identical(systems):
+    """The software-pipelined neighbour loop (unroll_water 3) visits each
+    lane's neighbours in the order of the one-per-iteration loop, so forces
+    and energies are bit-identical."""
+    from qsource_gb300.abi import QGPU_TERMS_STEP_PRECISION
+    out = []
+    for uw in (1, 3):
+        e = _engine(systems["cfg2"])
+        e.set_tuning([4, 6, 8, 1, uw])
+        e.make_pair_lists()
+        d, E, _ = e.pot_energy(0, terms=0x1F | QGPU_TERMS_STEP_PRECISION)
+        out.append((np.array(d), E))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert out[0][1] == out[1][1]
+
+
 def test_autotune_picks_a_valid_shape_and_is_cached(systems):
     s = systems["cfg1"]
     a = _engine(s)
