@@ -8,14 +8,22 @@ engine handle; Berendsen 300 K, 1 fs, SHAKE on waters, lists + LRF every 10
 steps, each 10-step block replayed from one CUDA graph.  Synthetic seeded
 systems (qsource_gb300.synth), not a public data set.
 
+Precision: the FP64-master step (QGPU_PRECISION_FP64: FP64 x, v, leap-frog,
+SHAKE and temperatures; FP32 pair terms; int64 fixed-point sums) unless
+--precision mixed.
+
 Printed: one JSON line (rank 0).  `value` = aggregate ns/day from CUDA events
 on the engine's stream around the timed 10-step blocks (L2 flushed with a
 256 MB write before each block); `e2e` = the same through the public API with
 host buffers (coordinates and velocities uploaded from pinned memory and read
-back, energies read back every block); `plain_form` = the same trajectories
-run one at a time, each alone in its own handle (the unbatched GPU form), and
-`batched_over_plain` = value / plain_form.  --impl reference times the FP64
-CPU restatement of the reference (oracle/) on all host cores instead.
+back, energies read back every block, a .en energy file written per
+trajectory and the device FEP sums of the 21-window chain accumulated);
+`mixed_form` = the same timed loop with the mixed-precision step (float
+master state), a secondary figure with its own dtype; `plain_form` = the same
+trajectories run one at a time, each alone in its own autotuned handle (the
+unbatched GPU form), and `batched_over_plain` = value / plain_form.
+--impl reference times the FP64 CPU restatement of the reference (oracle/) on
+all host cores instead.
 """
 from __future__ import annotations
 
@@ -35,6 +43,16 @@ sys.path.insert(0, ROOT)
 METRIC = "agg. ns/day (λ-window batch, 1 GB300) at ≤0.1 kcal/mol ΔG vs plain-form GPU"
 NB = 10
 FS_PER_STEP = 1.0
+# what each step form computes in which arithmetic
+DTYPE = {
+    "fp64": ("f64 master x/v, thermostat + leap-frog update, SHAKE and temperature; f64 list cut-off test and "
+             "recorded-step per-state Q energies; f32 pair/LRF terms from double-float coordinate differences; int64 "
+             "fixed-point force and energy sums"),
+    "mixed": ("double-float (~48-bit) master positions, f32 velocities, f32 3-site-water SHAKE and temperature, f32 "
+              "pair/bonded terms on unrecorded steps; f64 list cut-off test and recorded-step energies; int64 "
+              "fixed-point sums"),
+}
+KT_300 = 0.001986 * 300.0   # Boltz * T (src/md.f90:54), the FEP sums' kT
 WORKLOAD = ("lambda-window batch: 21 windows of the 18 A droplet (8 Q atoms, 2 states) + 11 uneven replicas "
             "(20/25/30 A spheres, 500-2000-atom solutes) = 32 trajectories")
 
@@ -195,19 +213,24 @@ def kernel_flops(name, wc):
     return None
 
 
-def plain_form(systems, flush, nblk: int, world: int) -> dict:
+def plain_form(systems, flush, nblk: int, world: int, precision: str, tune: bool) -> dict:
     """The same trajectories on the same GPU kernels, one trajectory per
     handle and one after another (the uniform-window form without batching):
-    each trajectory gets its own handle with the default launch shapes, one
-    untimed block, then nblk timed 10-step graph replays with the L2 flushed
-    before each.  Aggregate ns/day = all simulated time / the summed device
-    time, the throughput of running the windows one by one."""
+    each trajectory gets its own handle (launch shapes from the autotuner,
+    as the batched handle's, unless tune is False), the same step precision,
+    one untimed block, then nblk timed 10-step graph replays with the L2
+    flushed before each.  Aggregate ns/day = all simulated time / the summed
+    device time, the throughput of running the windows one by one."""
     import torch
+    from qsource_gb300.abi import PRECISION
     from qsource_gb300.engine import Engine
     ms_total = 0.0
     per = []
     for s in systems:
         e = Engine([s])
+        if tune:
+            e.autotune()
+        e.set_precision(PRECISION[precision])
         e.enqueue(NB, 0)
         e.sync()
         ext = torch.cuda.ExternalStream(e.stream())
@@ -228,7 +251,8 @@ def plain_form(systems, flush, nblk: int, world: int) -> dict:
     value = aggregate_ns_per_day(world, len(systems), nblk * NB, ms_total)
     return {"value": round(value, 3), "unit": "ns/day",
             "ms_per_step_min": round(min(per), 5), "ms_per_step_max": round(max(per), 5),
-            "how": f"each of the {len(systems)} trajectories alone in its own handle (default launch shapes), "
+            "how": f"each of the {len(systems)} trajectories alone in its own handle "
+                   f"({'autotuned' if tune else 'default'} launch shapes, {precision} step), "
                    f"one after another: 1 untimed + {nblk} timed 10-step CUDA-graph blocks each, L2 flushed "
                    f"before every block; aggregate = simulated ns / summed device time"}
 
@@ -248,8 +272,9 @@ def main():
                     help="fixed launch shapes lanes_water,min_blocks_water,lanes_solute,lanes_qw,unroll_water "
                          "instead of the autotuner's (profiling runs: the autotuner's timings mean nothing "
                          "under a profiler that serialises kernels)")
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
-                    help="MD step precision (qgpu_set_precision): double-float master / FP64 master")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="MD step precision of the headline (qgpu_set_precision): FP64 master / double-float master")
+    ap.add_argument("--no-mixed", action="store_true", help="skip timing the mixed-precision form")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-trajectory-at-a-time GPU form")
     ap.add_argument("--plain-blocks", type=int, default=20, help="timed 10-step blocks per trajectory, plain form")
     args = ap.parse_args()
@@ -300,35 +325,15 @@ def main():
         eng.set_tuning(tuning)
     else:
         tuning = eng.autotune() if not args.no_tune else None
-    if args.precision == "fp64":
-        from qsource_gb300.abi import QGPU_PRECISION_FP64
-        eng.set_precision(QGPU_PRECISION_FP64)
+    from qsource_gb300.abi import PRECISION
+    eng.set_precision(PRECISION[args.precision])
     eng.enqueue(warm, 0)
     eng.sync()
 
     ext = torch.cuda.ExternalStream(eng.stream())
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     nblk = steps // NB
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nblk)]
-    clocks = Clocks()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    l0 = eng.kernel_launches()
-    with torch.cuda.stream(ext):
-        for b in range(nblk):
-            flush.fill_(float(b))
-            ev[b][0].record(ext)
-            eng.enqueue(NB, NB)
-            ev[b][1].record(ext)
-    eng.sync()
-    torch.cuda.synchronize()
-    launches = eng.kernel_launches() - l0
-    clk = clocks.stop()
-    ms = sum(a.elapsed_time(b) for a, b in ev)
-    if dist:
-        ms = max_over_ranks(dist, ms, "cuda")
+    ms, launches, clk = timed_blocks(eng, ext, flush, nblk, dist)
     ns_per_day = aggregate_ns_per_day(world, ntraj, steps, ms)
 
     # --- end to end through the public API with host buffers: per block the
@@ -343,17 +348,33 @@ def main():
     cap = 4 * ntraj
     E_rows, EQ_rows = (abi.Energies * cap)(), (abi.QEnergy * (cap * abi.MAX_STATES))()
     tr_rows, st_rows = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
+    # the metric's Delta-G machinery runs inside the timed region: one .en file
+    # per trajectory (qdyn's energy output, written by the host sink) and the
+    # device's qfep Part 1 sums over the 21-window chain of the droplet
+    import tempfile
+    endir = tempfile.mkdtemp(prefix="qgpu_bench_en_")
+    nwin = 21
+    eng.fep_start(list(range(nwin)), KT_300)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    for t in range(ntraj):
+        eng.ene_open(t, os.path.join(endir, f"traj{t:02d}.en"))
     nrows = 0
     for b in range(e2e_blocks):
         eng.set_coords_all(xs, vs)
         nrows += eng.run_rows(NB, NB, E_rows, EQ_rows, tr_rows, st_rows)
         eng.coords_all(xs, vs)
+    for t in range(ntraj):
+        eng.ene_close(t)
     if nrows != ntraj * e2e_blocks:
         raise RuntimeError(f"e2e: {nrows} energy records for {e2e_blocks} blocks of {ntraj} trajectories")
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    fep_frames = int(eng.fep_result()[3][0, 0])
+    en_bytes = sum(os.path.getsize(os.path.join(endir, f)) for f in os.listdir(endir))
+    for f in os.listdir(endir):
+        os.remove(os.path.join(endir, f))
+    os.rmdir(endir)
     e2e = world * ntraj * e2e_blocks * NB * FS_PER_STEP * 1e-6 * 86400.0 / e2e_s
     h2d = sum(2 * 3 * s.natom * 8 for s in systems) / NB
     d2h = (sum(2 * 3 * s.natom * 8 for s in systems) + ntraj * (29 + 15 * 4) * 8) / NB
@@ -382,7 +403,19 @@ def main():
                 "unit": "TFLOP/s", "frac": round(achieved / peak, 4), "traffic": committed_traffic(name),
                 "peak_source": "measured in this run: FP32 FMA-chain kernel over all SMs (qgpu_fp32_peak)",
                 "avg_launch_ms": round(kms / kcnt, 5), "flops_per_launch": fl}
-    plain = None if args.no_plain else plain_form(systems, flush, args.plain_blocks, world)
+    mixed = None
+    if not args.no_mixed and args.precision != "mixed":
+        eng.set_precision(PRECISION["mixed"])
+        eng.enqueue(NB, 0)
+        eng.sync()
+        mblk = min(nblk, 100)
+        mms, _, _ = timed_blocks(eng, ext, flush, mblk, dist)
+        mixed = {"value": round(aggregate_ns_per_day(world, ntraj, mblk * NB, mms), 3), "unit": "ns/day",
+                 "ms_per_step": round(mms / (mblk * NB), 5), "steps": mblk * NB, "dtype": DTYPE["mixed"],
+                 "how": "the same handle, launch shapes and timed loop with qgpu_set_precision(QGPU_PRECISION_MIXED)"}
+        eng.set_precision(PRECISION[args.precision])
+    plain = None if args.no_plain else plain_form(systems, flush, args.plain_blocks, world, args.precision,
+                                                  tune=not args.no_tune and not args.tuning)
     if rank != 0:
         return
     cpu = cpu_baseline(pool, args.cpu_steps) if pool else None
@@ -391,7 +424,7 @@ def main():
     out = {
         "metric": METRIC, "value": round(ns_per_day, 3), "unit": "ns/day", "n_gpus": world, "steps": steps,
         "warmup": warm, "ms_per_step": round(ms / steps, 5), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 pair terms, f64 integration/SHAKE/list test, int64 fixed-point sums",
+        "vs_baseline": None, "dtype": DTYPE[args.precision],
         "data": "synthetic (seeded water spheres, random-init)",
         "config": {"workload": WORKLOAD, "trajectories": ntraj, "atoms": natoms, "dt_fs": FS_PER_STEP, "nbcycle": NB,
                    "timed": f"{nblk} blocks of {NB} steps, each one CUDA-graph replay",
@@ -403,8 +436,11 @@ def main():
                                      if tuning else "default")},
         "e2e": {"value": round(e2e, 3), "unit": "ns/day", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "how": "per 10-step block: qgpu_set_coords_all of x,v of all 32 trajectories from pinned memory, "
-                       "qgpu_run_rows (the block's energy records of every trajectory into host arrays), "
-                       "qgpu_get_coords_all (host wall clock)"},
+                       "qgpu_run_rows (the block's energy records of every trajectory into host arrays and a .en "
+                       "frame per trajectory), qgpu_get_coords_all (host wall clock); qgpu_fep_start over the "
+                       "21-window chain before, the .en files opened and closed inside the timed region",
+                "en_bytes": int(en_bytes), "fep_frames_window0": fep_frames},
+        "mixed_form": mixed,
         "roofline": roof,
         "kernel_share": share,
         "kernel_roofline": per_kernel,
@@ -417,6 +453,37 @@ def main():
         "work": wc,
     }
     print(json.dumps(out))
+
+
+def timed_blocks(eng, ext, flush, nblk: int, dist):
+    """nblk 10-step graph replays on the engine's stream, each bracketed by
+    CUDA events and preceded by an L2 flush (a 256 MB write); barrier and
+    synchronize on both sides.  Returns (ms, the engine's kernel launches,
+    the clocks sampled during the region); ms is the max over ranks."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nblk)]
+    clocks = Clocks()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    l0 = eng.kernel_launches()
+    with torch.cuda.stream(ext):
+        for b in range(nblk):
+            flush.fill_(float(b))
+            ev[b][0].record(ext)
+            eng.enqueue(NB, NB)
+            ev[b][1].record(ext)
+    eng.sync()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches = eng.kernel_launches() - l0
+    clk = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    if dist:
+        ms = max_over_ranks(dist, ms, "cuda")
+    return ms, launches, clk
 
 
 def max_over_ranks(dist, value: float, device: str = "cpu") -> float:

@@ -353,18 +353,26 @@ int qgpu_set_tuning(qgpu_handle *h, const int32_t *tuning);
 int qgpu_set_step(qgpu_handle *h, int64_t istep);
 
 /* Precision of the persistent MD step (qgpu_run / qgpu_enqueue).
-   QGPU_PRECISION_MIXED (the default): master positions as a double-float
-     (about 48 significant bits), FP32 velocities, SHAKE of 3-site waters in
-     FP32 on relative vectors, FP32 bonded/restraint terms on unrecorded steps;
-     FP64 energies on recorded steps.  Used when every trajectory's
-     constraints are 3-site waters (O-H, O-H, H-H), else the FP64 form runs.
-   QGPU_PRECISION_FP64: FP64 master x and v with the reference's FP64
-     leap-frog (newvel_ber, src/md.f90:6194-6223) and FP64 SHAKE
-     (src/md.f90:17581-17679) every step.
-   Pair terms are FP32 with int64 fixed-point sums in both.  Switching keeps
-   the current coordinates and velocities. */
+   QGPU_PRECISION_FP64 (the default): FP64 master x and v with the
+     reference's FP64 leap-frog / velocity-Verlet and thermostat updates
+     (newvel_ber, src/md.f90:6194-6223; newvel_lan, newvel_nos), FP64 SHAKE
+     (src/md.f90:17581-17679) and FP64 temperatures and Berendsen scales
+     (temperature, src/md.f90:6098-6190, from exact integer sums of the
+     per-atom kinetic energies) every step.  When every trajectory's
+     constraints are 3-site waters (O-H, O-H, H-H) the update, SHAKE and the
+     step's end run as one fused kernel; otherwise as separate kernels.
+   QGPU_PRECISION_FP64_UNFUSED: the same FP64 arithmetic in the separate
+     update, SHAKE and step-end kernels whatever the constraints.
+   QGPU_PRECISION_MIXED: master positions as a double-float (about 48
+     significant bits), FP32 velocities, SHAKE of 3-site waters in FP32 on
+     relative vectors, FP32 temperature, FP32 bonded/restraint terms on
+     unrecorded steps; FP64 energies on recorded steps.  Used when every
+     trajectory's constraints are 3-site waters, else the FP64 form runs.
+   Pair terms are FP32 with int64 fixed-point sums in every mode.  Switching
+   keeps the current coordinates and velocities. */
 #define QGPU_PRECISION_MIXED 0
 #define QGPU_PRECISION_FP64  1
+#define QGPU_PRECISION_FP64_UNFUSED 2
 int qgpu_set_precision(qgpu_handle *h, int32_t mode);
 
 /* Queues nsteps of the same device work as qgpu_run without waiting for it

@@ -22,6 +22,9 @@ QGPU_TERMS_ALL = 0x1F
 QGPU_TERMS_STEP_PRECISION = 0x100
 QGPU_PRECISION_MIXED = 0
 QGPU_PRECISION_FP64 = 1
+QGPU_PRECISION_FP64_UNFUSED = 2
+# step precision by name (bench and tests)
+PRECISION = {"mixed": QGPU_PRECISION_MIXED, "fp64": QGPU_PRECISION_FP64, "fp64_unfused": QGPU_PRECISION_FP64_UNFUSED}
 
 STATUS = {0: "ok", 1: "invalid", 2: "cuda", 3: "list overflow", 4: "shake failure", 5: "nan",
           6: "unsupported", 7: "fixed-point range"}

@@ -9,6 +9,9 @@
 #define BOLTZ 0.001986          // src/md.f90:54
 #define SHAKE_TOL 0.0001        // src/md.f90:460
 #define SHAKE_MAX_ITER 1000     // src/md.f90:461
+#ifndef QG_UPD_D_MINB
+#define QG_UPD_D_MINB 8         // k_update_d register bound: 8 resident blocks, the grid of the batch in one wave
+#endif
 
 // The thermostat's velocity and position update of one atom (md_run
 // :6577-6590): Berendsen newvel_ber (v = (v - d winv dv)*Tscale), Langevin
@@ -22,7 +25,7 @@ __global__ void k_integrate(DevSys S) {
     const int tr = S.atraj[i];
     const TrajInfo &T = S.traj[tr];
     const TrajState &TS = S.tstate[tr];
-    const double ts = (i - T.atom0) < T.nat_solute ? TS.tsf_solute : TS.tsf_solvent;
+    const double ts = (i - T.atom0) < T.nat_solute ? TS.tsd_solute : TS.tsd_solvent;
     const double wi = S.winv[i], dt = T.dt, dvm = T.dvm;
     double rf[3] = {0.0, 0.0, 0.0};
     if (T.thermostat == 1) langevin_force<double>(S, T, TS.rnd, i, rf);
@@ -96,11 +99,15 @@ __global__ void k_shake(DevSys S, int traj_filter) {
 //   mode 0: kinetic energy + float mirror only (temperature before step 0);
 //   mode 2: v = (x - xx)/dt after k_integrate + k_shake (md_run
 //           :6596-6597), mirror, Ekin.
-// Ekin partials (solute, free solute, solvent, free solvent) per block.
+// Ekin partials (solute, free solute, solvent, free solvent) per block, as
+// float and as int64 fixed point (each atom's 0.5 m v^2 rounded to 2^-32
+// kcal/mol, then integer sums: independent of the summation order).
 __global__ void __launch_bounds__(QG_BLOCK) k_update(DevSys S, const int *items, int mode) {
     __shared__ double red[4][QG_BLOCK / 32];
+    __shared__ long long redq[4][QG_BLOCK / 32];
     const int it = items[blockIdx.x * blockDim.x + threadIdx.x];
     double ek[4] = {0, 0, 0, 0};
+    long long ekq[4] = {0, 0, 0, 0};
     if (it >= 0) {
         const bool mol = (it >> 30) & 1;
         const int m = it & 0x3fffffff;
@@ -125,9 +132,10 @@ __global__ void __launch_bounds__(QG_BLOCK) k_update(DevSys S, const int *items,
                 vv += v[a] * v[a];
             }
             const double e = 0.5 * S.mass[i] * vv;
+            const long long eq = d2fx_chk(e, S.status);
             const bool fr = !S.aexcl[i];
-            if ((i - T.atom0) < T.nat_solute) { ek[0] += e; ek[1] += fr ? e : 0; }
-            else { ek[2] += e; ek[3] += fr ? e : 0; }
+            if ((i - T.atom0) < T.nat_solute) { ek[0] += e; ek[1] += fr ? e : 0; ekq[0] += eq; ekq[1] += fr ? eq : 0; }
+            else { ek[2] += e; ek[3] += fr ? e : 0; ekq[2] += eq; ekq[3] += fr ? eq : 0; }
             float4 h, l;
             const double r0 = x[0] - T.origin[0], r1 = x[1] - T.origin[1], r2 = x[2] - T.origin[2];
             h.x = (float)r0; h.y = (float)r1; h.z = (float)r2; h.w = S.pos[i].w;
@@ -139,13 +147,17 @@ __global__ void __launch_bounds__(QG_BLOCK) k_update(DevSys S, const int *items,
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int k = 0; k < 4; ++k) {
         const double v = warp_sum_d(ek[k]);
-        if (lane == 0) red[k][warp] = v;
+        long long q = ekq[k];
+        for (int o = 16; o > 0; o >>= 1) q += __shfl_down_sync(0xffffffffu, q, o);
+        if (lane == 0) { red[k][warp] = v; redq[k][warp] = q; }
     }
     __syncthreads();
     if (threadIdx.x < 4) {
         double s = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
+        long long q = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { s += red[threadIdx.x][w]; q += redq[threadIdx.x][w]; }
         S.ekin_part[(size_t)blockIdx.x * 4 + threadIdx.x] = (float)s;
+        S.ekin_fx[(size_t)blockIdx.x * 4 + threadIdx.x] = q;
     }
 }
 
@@ -382,6 +394,281 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
     if (t == 0) S.fin_cnt[tr] = 0;
 }
 
+// ------------------------------------------------ FP64-master fused step
+// On GB300 an FP64 warp instruction holds its SM sub-partition's FP64 unit
+// for about 64-76 cycles whatever lanes are active (1.7 lane-FMAs per clock
+// per SM against about 120 in FP32), and the same unit runs the conversions
+// between double, float and int64.  The FP64-master step therefore keeps its
+// FP64 work to the arithmetic of the reference and converts with integer
+// instructions where it can.
+
+// int64 q (|q| < 2^51) as a double: q added to the bits of 1.5*2^52, whose
+// ulp is 1, then 1.5*2^52 subtracted (one FP64 add)
+__device__ __forceinline__ double ll2d_magic(long long q) {
+    return __longlong_as_double(0x4338000000000000LL + q) - 6755399441055744.0;
+}
+// round-to-nearest-even int64 of v (|v| < 2^51): v + 1.5*2^52 carries the
+// rounded integer in its low mantissa bits
+__device__ __forceinline__ long long d2ll_magic(double v) {
+    return __double_as_longlong(v + 6755399441055744.0) - 0x4338000000000000LL;
+}
+__device__ __forceinline__ bool magic_range(long long q) {
+    return (unsigned long long)(q + (1LL << 51)) < (1ULL << 52);
+}
+
+// Round-to-nearest-even float of r from its bits: the 52-bit mantissa is
+// rounded at bit 29 (ties to even), the exponent rebiased from 1023 to 127.
+// rh receives the float's value as a double.  Values outside the normal float
+// range (and zero) take the conversion instruction.
+__device__ __forceinline__ float d2f_bits(double r, double &rh) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(r);
+    const int e = (int)((b >> 52) & 0x7ffu);
+    if (e < 897 || e > 1149) {
+        const float f = __double2float_rn(r);
+        rh = (double)f;
+        return f;
+    }
+    const unsigned long long rem = b & 0x1fffffffull, half = 0x10000000ull;
+    unsigned long long t = b >> 29;                      // sign | exponent | 23 mantissa bits
+    t += (rem > half || (rem == half && (t & 1ull))) ? 1ull : 0ull;
+    rh = __longlong_as_double((long long)(t << 29));
+    const unsigned mag = (unsigned)((t & 0x3ffffffffull) - (896ull << 23));
+    return __uint_as_float(mag | (unsigned)((b >> 63) << 31));
+}
+// hi/lo float pair of r: hi = float(r), lo = float(r - hi) (r - hi is exact)
+__device__ __forceinline__ void split_hl(double r, float &h, float &l) {
+    double rh, rl;
+    h = d2f_bits(r, rh);
+    const double d = r - rh;
+    l = d == 0.0 ? 0.f : d2f_bits(d, rl);
+}
+
+// diff / den: the PTX approximate FP64 reciprocal (a special-function unit
+// instruction) refined by two Newton-Raphson steps y <- y (2 - den y), then
+// multiplied
+__device__ __forceinline__ double div_nr(double diff, double den) {
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(den));
+    y = y * (2.0 - den * y);
+    y = y * (2.0 - den * y);
+    return diff * y;
+}
+
+// SHAKE of one water in FP64 (shake, src/md.f90:17581-17679), in the
+// reference's arithmetic: per constraint xij = x_i - x_j of the current
+// positions, diff = d0^2 - |xij|^2, ready once |diff| < SHAKE_TOL d0^2 (the
+// correction of that visit is still applied), xxij = xx_i - xx_j of the
+// positions before the step, corr = diff / (2 scp (winv_i + winv_j)) with
+// scp = xij.xxij, x_i += xxij corr winv_i, x_j -= xxij corr winv_j;
+// Gauss-Seidel over O-H1, O-H2, H1-H2; constraints that met the tolerance are
+// not revisited; at most SHAKE_MAX_ITER sweeps.  The tolerance test compares
+// the bit patterns of |diff| and the (positive) tolerance as integers.
+__device__ int shake_water_d(double (&x)[3][3], const double (&xx)[3][3], const double (&w)[3], const double (&d2)[3],
+                             bool *fail) {
+    double xxij[3][3], den0[3];
+    long long tolb[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const int i = c == 2 ? 1 : 0, j = c == 0 ? 1 : 2;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) xxij[c][a] = xx[i][a] - xx[j][a];
+        // 2 scp (w_i + w_j) = scp * (2 (w_i + w_j)) exactly (scaling by 2)
+        den0[c] = 2.0 * (w[i] + w[j]);
+        tolb[c] = __double_as_longlong(SHAKE_TOL * d2[c]);
+    }
+    unsigned ready = 0u;
+    int nits = 0;
+    for (;;) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (ready & (1u << c)) continue;
+            const int i = c == 2 ? 1 : 0, j = c == 0 ? 1 : 2;
+            const double xij0 = x[i][0] - x[j][0], xij1 = x[i][1] - x[j][1], xij2 = x[i][2] - x[j][2];
+            const double diff = d2[c] - (xij0 * xij0 + xij1 * xij1 + xij2 * xij2);
+            if ((__double_as_longlong(diff) & 0x7fffffffffffffffLL) < tolb[c]) ready |= 1u << c;
+            const double scp = xij0 * xxij[c][0] + xij1 * xxij[c][1] + xij2 * xxij[c][2];
+            const double corr = div_nr(diff, scp * den0[c]);
+            const double ci = corr * w[i], cj = corr * w[j];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                x[i][a] += xxij[c][a] * ci;
+                x[j][a] -= xxij[c][a] * cj;
+            }
+        }
+        nits++;
+        if (ready == 7u) break;
+        if (nits >= SHAKE_MAX_ITER) { *fail = true; break; }
+    }
+    return nits;
+}
+
+// One MD step with the FP64 master state, in the fused update's layout (one
+// thread per atom in blocks of QG_UBLK: unconstrained atoms first, then
+// blocks of 32 waters): per atom the thermostat's FP64 velocity and position
+// update of k_integrate (newvel_ber / newvel_lan / newvel_nos, md_run
+// :6577-6590); in water blocks warp 0 then runs the FP64 SHAKE of one water
+// per lane on the positions held in shared memory; then per atom
+// v = (x - xx)/dt (md_run :6596-6600, Nose-Hoover second scale), the FP64
+// x/v stores, the float coordinates of the pair kernels (hi/lo of
+// x - origin), the packed water records and the Ekin partials (each atom's
+// 0.5 m v^2 rounded to 2^-32 kcal/mol, integer sums).  x and v are the
+// master: no float state is carried from step to step.  ekin_only: Ekin of
+// the current v (temperature before the first step).  fin: the step's end in
+// the last block of each trajectory, as in k_update_f.  The per-atom FP64
+// work is spread over the block's three warps; the SHAKE of 32 waters is one
+// warp's (its FP64 instructions cost the same for any number of active lanes).
+__global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, const int *uatom, const int *ucon,
+                                                                     const uint8_t *ublk_water, EaccSel esel,
+                                                                     int ekin_only, int fin, double *rec, int rec_cap) {
+    __shared__ double s_x[3][QG_UBLK], s_xx[3][QG_UBLK];
+    __shared__ float4 s_h[QG_UBLK], s_l[QG_UBLK];
+    __shared__ long long red[4][QG_UBLK / 32];
+    const int t = threadIdx.x;
+    const int a = uatom[blockIdx.x * QG_UBLK + t];
+    const bool water_blk = ublk_water[blockIdx.x] != 0;
+    int c0 = -1;
+    double d2[3] = {0.0, 0.0, 0.0};
+    if (water_blk && !ekin_only && t < 32) {
+        c0 = ucon[blockIdx.x * QG_UBLK + 3 * t];
+        if (c0 >= 0) { d2[0] = S.shk_d2[c0]; d2[1] = S.shk_d2[c0 + 1]; d2[2] = S.shk_d2[c0 + 2]; }
+    }
+    const int tr = a >= 0 ? S.atraj[a] : -1 - a;
+    const TrajInfo &T = S.traj[tr];
+    double x[3] = {0.0, 0.0, 0.0}, xo[3] = {0.0, 0.0, 0.0}, v[3] = {0.0, 0.0, 0.0};
+    if (a >= 0) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[c] = S.v[3 * a + c];
+        if (!ekin_only) {
+            const TrajState &TS = S.tstate[tr];
+            const double wi = S.winv[a];
+            const double ts = (a - T.atom0) < T.nat_solute ? TS.tsd_solute : TS.tsd_solvent;
+            // gradient (fixed point, 2^-32 units) times winv dv: the 2^-32 is
+            // exact, folded into dv
+            const double kq = wi * (T.dvm * (1.0 / QG_FSCALE));
+            double rf[3] = {0.0, 0.0, 0.0};
+            if (T.thermostat == 1) langevin_force<double>(S, T, TS.rnd, a, rf);
+            bool bad = false;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const int k = 3 * a + c;
+                xo[c] = S.x[k];
+                const long long q = (long long)S.fx[k];
+                S.fx[k] = 0ull;
+                bad |= !magic_range(q);
+                const double gq = ll2d_magic(q);
+                double u = v[c];
+                if (T.thermostat == 1) u = u * T.lfric - (gq * kq - rf[c] * wi * T.dvm);
+                else if (T.thermostat == 2) u = u * TS.nh_s1 - gq * kq;
+                else u = (u - gq * kq) * ts;
+                x[c] = xo[c] + u * T.dt;
+                if (T.integrator == 1) {
+                    if (T.thermostat == 1) u = u * T.lfric - (gq * kq - rf[c] * wi * T.dvm);
+                    else if (T.thermostat == 2) u = u - gq * kq;
+                    else u = (u - gq * kq) * ts;
+                }
+                v[c] = u;
+            }
+            if (bad) atomicOr(S.status, ST_FIXED);
+            if (water_blk)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) { s_x[c][t] = x[c]; s_xx[c][t] = xo[c]; }
+        }
+    }
+    if (water_blk && !ekin_only) {
+        __syncthreads();
+        if (t < 32) {
+            int nits = 0;
+            if (c0 >= 0) {
+                double wx[3][3], wxx[3][3], ww[3];
+                const int o = S.shk_i[c0];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int q = 3 * t + k;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) { wx[k][c] = s_x[c][q]; wxx[k][c] = s_xx[c][q]; }
+                    ww[k] = S.winv[o + k];
+                }
+                bool failed = false;
+                nits = shake_water_d(wx, wxx, ww, d2, &failed);
+                if (failed) { atomicOr(S.status, ST_SHAKE); atomicCAS(S.status + 1, 0, tr + 1); }
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) s_x[c][3 * t + k] = wx[k][c];
+            }
+            for (int o = 16; o > 0; o >>= 1) nits += __shfl_down_sync(0xffffffffu, nits, o);
+            if (t == 0 && nits) atomicAdd(&S.tstate[tr].shake_iters, nits);
+        }
+        __syncthreads();
+        if (a >= 0)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) x[c] = s_x[c][t];
+    }
+    long long ek[4] = {0, 0, 0, 0};
+    if (a >= 0) {
+        if (!ekin_only) {
+            if (T.nshake_mol > 0) {
+                const double s2 = T.thermostat == 2 ? S.tstate[tr].nh_s2 : 1.0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    v[c] = (x[c] - xo[c]) * T.inv_dt;
+                    if (T.thermostat == 2) v[c] *= s2;
+                }
+            }
+            float4 h, l;
+            split_hl(x[0] - T.origin[0], h.x, l.x);
+            split_hl(x[1] - T.origin[1], h.y, l.y);
+            split_hl(x[2] - T.origin[2], h.z, l.z);
+            h.w = S.pos[a].w;
+            l.w = 0.f;
+            S.pos[a] = h; S.poslo[a] = l;
+            if (water_blk) { s_h[t] = h; s_l[t] = l; }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { S.x[3 * a + c] = x[c]; S.v[3 * a + c] = v[c]; }
+        }
+        // 0.5 m v^2 in FP64, rounded to 2^-32 kcal/mol: integer sums from here
+        const double e = (S.mass[a] * (0.5 * QG_FSCALE)) * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        long long q = d2ll_magic(e);
+        if (!(e < 2251799813685248.0)) { atomicOr(S.status, ST_FIXED); q = 0; }   // 2^51, NaN
+        const bool fr = !S.aexcl[a];
+        if ((a - T.atom0) < T.nat_solute) { ek[0] = q; ek[1] = fr ? q : 0; }
+        else { ek[2] = q; ek[3] = fr ? q : 0; }
+    }
+    if (water_blk && !ekin_only) {
+        __syncthreads();
+        const int w3 = t - t % 3;
+        if (ucon[blockIdx.x * QG_UBLK + w3] >= 0) {
+            const float4 wh[3] = {s_h[w3], s_h[w3 + 1], s_h[w3 + 2]};
+            const float4 wl[3] = {s_l[w3], s_l[w3 + 1], s_l[w3 + 2]};
+            S.wrec[uatom[blockIdx.x * QG_UBLK + w3] + t % 3] = wrec_part(wh, wl, t % 3);
+        }
+    }
+    const int lane = t & 31, warp = t >> 5;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        long long r = ek[k];
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+        if (lane == 0) red[k][warp] = r;
+    }
+    __syncthreads();
+    if (t < 4) {
+        long long sum = 0;
+        for (int w = 0; w < QG_UBLK / 32; ++w) sum += red[t][w];
+        S.ekin_fx[(size_t)blockIdx.x * 4 + t] = sum;
+        __threadfence();
+    }
+    if (!fin) return;
+    __shared__ int s_last;
+    __shared__ double s_fin[QG_NE];
+    __syncthreads();
+    if (t == 0) s_last = atomicAdd(S.fin_cnt + tr, 1) == T.ekin_nblk - 1;
+    __syncthreads();
+    if (!s_last || t >= 32) return;
+    __threadfence();
+    finalize_traj(S, tr, t, s_fin, fin, rec, esel.recctl, esel.k, esel.ene_every, rec_cap);
+    if (t == 0) S.fin_cnt[tr] = 0;
+}
+
 // x = origin + (hi + lo), v = velf: the FP64 view of the float master.
 __global__ void k_sync_double(DevSys S) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -480,7 +767,56 @@ __device__ void finalize_traj(const DevSys &S, int tr, int lane, double *v, int 
             A[5] += exp(-dv / T.fep_kT); A[6] += dv; A[7] += dv * dv; A[8] += dv * dv * dv;
         }
     }
-    if (do_temp) {
+    if (do_temp & FIN_EK64) {
+        // temperature (src/md.f90:6098-6190) in FP64 from the int64 partials:
+        // exact integer sums, then the reference's operation order
+        long long p[4] = {0, 0, 0, 0};
+        const long long *ep = S.ekin_fx + 4 * (size_t)T.ekin_blk0;
+        for (int b = lane; b < T.ekin_nblk; b += 32)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) p[k] += __ldcg(ep + 4 * b + k);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            for (int o = 16; o > 0; o >>= 1) p[k] += __shfl_down_sync(0xffffffffu, p[k], o);
+        if (lane == 0) {
+            const double e_su = fx_get((unsigned long long)p[0]), f_su = fx_get((unsigned long long)p[1]);
+            const double e_sv = fx_get((unsigned long long)p[2]), f_sv = fx_get((unsigned long long)p[3]);
+            const double Ekin = e_su + e_sv;
+            const double Temp = T.Ndegf > 0 ? 2.0 * Ekin / BOLTZ / (double)T.Ndegf : 0.0;
+            const double Tfree = T.Ndegfree > 0 ? 2.0 * (f_sv + f_su) / BOLTZ / (double)T.Ndegfree : 0.0;
+            double Tfsu = f_su, Tfsv = f_sv;
+            if (T.detail_temps) {
+                Tfsu = T.Ndegfree_solute > 0 ? 2.0 * Tfsu / BOLTZ / (double)T.Ndegfree_solute : 0.0;
+                Tfsv = T.Ndegfree_solvent > 0 ? 2.0 * Tfsv / BOLTZ / (double)T.Ndegfree_solvent : 0.0;
+            }
+            double ts = TS.tsd_solvent, tu = TS.tsd_solute;
+            if (T.thermostat != 0) {
+                ts = 1.0; tu = 1.0;
+            } else if (T.separate_scaling) {
+                if (Tfsv != 0.0) ts = T.Temp0 / Tfsv - 1.0;
+                ts = sqrt(1.0 + T.dt_taud * ts);
+                if (Tfsu != 0.0) tu = T.Temp0 / Tfsu - 1.0;
+                tu = sqrt(1.0 + T.dt_taud * tu);
+            } else {
+                if (Tfree != 0.0) ts = T.Temp0 / Tfree - 1.0;
+                ts = sqrt(1.0 + T.dt_taud * ts);
+                tu = ts;
+            }
+            TS.Ekin_d = Ekin; TS.Temp_d = Temp; TS.Tfree_d = Tfree;
+            TS.tsd_solute = tu; TS.tsd_solvent = ts;
+            TS.Ekin = (float)Ekin; TS.Temp = (float)Temp; TS.Tfree = (float)Tfree;
+            TS.tsf_solute = (float)tu; TS.tsf_solvent = (float)ts;
+            TS.wshiftf = T.fk_wsphere != 0.0 ? (float)sqrt(BOLTZ * Tfree / T.fk_wsphere) : 0.f;
+            if (Temp != Temp) atomicOr(S.status, ST_NAN);
+            if (T.thermostat == 1 && (do_temp & FIN_STEP))
+                TS.rnd = (unsigned)((T.lcgA * TS.rnd + T.lcgC) % QG_LCG_M);
+            if (T.thermostat == 2 && (do_temp & FIN_NH)) {
+                double *vnh = S.nh_state + (size_t)tr * 2 * QG_MAXNH, *xnh = vnh + QG_MAXNH;
+                TS.nh_s1 = nh_prop(T, vnh, xnh, Temp);
+                TS.nh_s2 = T.nshake_mol > 0 ? nh_prop(T, vnh, xnh, Temp) : 1.0;
+            }
+        }
+    } else if (do_temp) {
         // the four partials of a block are one float4 (slots 4 b .. 4 b + 3)
         float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 *ep = reinterpret_cast<const float4 *>(S.ekin_part) + T.ekin_blk0;
@@ -509,6 +845,8 @@ __device__ void finalize_traj(const DevSys &S, int tr, int lane, double *v, int 
             }
             TS.Ekin = Ekin; TS.Temp = Temp; TS.Tfree = Tfree;
             TS.tsf_solute = tu; TS.tsf_solvent = ts;
+            TS.Ekin_d = Ekin; TS.Temp_d = Temp; TS.Tfree_d = Tfree;
+            TS.tsd_solute = tu; TS.tsd_solvent = ts;
             TS.wshiftf = T.fk_wspheref != 0.f ? sqrtf(0.001986f * Tfree / T.fk_wspheref) : 0.f;
             if (Temp != Temp) atomicOr(S.status, ST_NAN);
             if (T.thermostat == 1 && (do_temp & FIN_STEP))
@@ -558,9 +896,9 @@ __device__ void finalize_traj(const DevSys &S, int tr, int lane, double *v, int 
     E[23] = E[24] + E[25] + E[26] + E[27] + E[28];
     E[0] = E[3] + E[7] + E[4] + E[8] + E[5] + E[6] + E[15] + E[16] + E[17] + E[18] + E[19] + E[20] + E[11] + E[12] +
            E[13] + E[14] + E[21] + E[22] + E[23] + E[2];
-    E[1] = (double)TS.Ekin;
-    R[QG_REC_T] = (double)TS.Temp;
-    R[QG_REC_T + 1] = (double)TS.Tfree;
+    E[1] = TS.Ekin_d;
+    R[QG_REC_T] = TS.Temp_d;
+    R[QG_REC_T + 1] = TS.Tfree_d;
     for (int c = 0; c < 2 * QG_MAXOD; ++c) R[QG_REC_OD + c] = S.od_out[(size_t)tr * QG_MAXOD * 2 + c];
 }
 
@@ -607,6 +945,14 @@ void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSe
     prof_begin(L, "k_update_f");
     k_update_f<<<B.nuatom / QG_UBLK, QG_UBLK, 0, L.stream>>>(S, B.uatom, B.ucon, B.ublk_water, e, nbcycle, ekin_only,
                                                              fin, rec, rec_cap);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_update_d(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int ekin_only, int fin,
+                     double *rec, int rec_cap) {
+    prof_begin(L, "k_update_d");
+    k_update_d<<<B.nuatom / QG_UBLK, QG_UBLK, 0, L.stream>>>(S, B.uatom, B.ucon, B.ublk_water, e, ekin_only, fin, rec,
+                                                             rec_cap);
     prof_end(L);
     (*L.nlaunch)++;
 }

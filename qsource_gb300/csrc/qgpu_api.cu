@@ -92,7 +92,8 @@ struct qgpu_handle {
     double fep_kT = 0;
     int fep_nskip = 0;
     std::vector<char> fused;   // per trajectory: SHAKE fused into the update kernel
-    bool all_fused = true;
+    bool all_fused = false;    // the fused step with the float master (QGPU_PRECISION_MIXED)
+    bool fused_d = true;       // the fused step with the FP64 master (QGPU_PRECISION_FP64)
     bool can_fuse = true;      // every trajectory's constraints allow the fused update
     std::vector<int> ek_u0, ek_un, ek_a0, ek_an;   // Ekin block ranges of the two update layouts
     // 0: x/v and the float coordinates agree; 1: the float master (fused
@@ -189,6 +190,17 @@ static int validate(const qgpu_system_desc &d, int t) {
     return 0;
 }
 
+// Ekin partial slots of each trajectory for the update kernel in use: the
+// atom blocks of the fused steps (float or FP64 master), or the item blocks of
+// the separate kernels (TrajInfo only; the caller uploads it).
+static void set_ekin_layout(qgpu_handle *h) {
+    for (int t = 0; t < h->ntraj; ++t) {
+        TrajInfo &T = h->info[t];
+        if (h->all_fused || h->fused_d) { T.ekin_blk0 = h->ek_a0[t]; T.ekin_nblk = h->ek_an[t]; }
+        else { T.ekin_blk0 = h->ek_u0[t]; T.ekin_nblk = h->ek_un[t]; }
+    }
+}
+
 static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h) {
     h->ntraj = ntraj;
     std::vector<double> x, v, xtop, winv, mass_atom, crg_d;
@@ -279,6 +291,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
             T.cT = c(d.Ndegf); T.cTfree = c(d.Ndegfree);
             T.cTfsu = c(d.Ndegfree_solute); T.cTfsv = c(d.Ndegfree_solvent);
             T.dt_tau = (float)(d.dt / d.tau_T); T.Temp0f = (float)d.Temp0;
+            T.dt_taud = d.dt / d.tau_T;
         }
         T.separate_scaling = d.separate_scaling; T.detail_temps = d.detail_temps;
         T.any_atom = d.any_atom_lists ? 1 : 0;
@@ -805,6 +818,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     for (auto &q : tsh) {
         q.Temp = q.Tfree = q.Ekin = 0.f; q.shake_iters = 0;
         q.tsf_solute = q.tsf_solvent = 1.f; q.wshiftf = 0.f;
+        q.Ekin_d = q.Temp_d = q.Tfree_d = 0.0; q.tsd_solute = q.tsd_solvent = 1.0;
         q.rnd = rnd0[&q - tsh.data()]; q.nh_s1 = q.nh_s2 = 1.0;
     }
     if ((rc = upload(A, tsh, &ts))) return rc;
@@ -910,18 +924,17 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     if ((rc = alloc0(A, (size_t)ntraj, &S.fin_cnt))) return rc;
     h->ene_files.assign(ntraj, nullptr);
     if (!wp_state.empty()) { double *p_; if ((rc = upload(A, wp_state, &p_))) return rc; S.wp_state = p_; }
-    for (char f : h->fused) h->all_fused = h->all_fused && f;
-    h->can_fuse = h->all_fused;
+    for (char f : h->fused) h->can_fuse = h->can_fuse && f;
+    h->all_fused = false;
+    h->fused_d = h->can_fuse;
     h->ek_u0 = ek_u0; h->ek_un = ek_un; h->ek_a0 = ek_a0; h->ek_an = ek_an;
     {
         const size_t nblk_ek = std::max(uitem.size() / QG_BLOCK, uatom.size() / QG_UBLK) + 1;
         if ((rc = alloc0(A, (size_t)4 * nblk_ek, &S.ekin_part))) return rc;
+        if ((rc = alloc0(A, (size_t)4 * nblk_ek, &S.ekin_fx))) return rc;
     }
-    // the Ekin partials follow the update kernel in use (fused: atom layout)
-    for (int t = 0; t < ntraj; ++t) {
-        h->info[t].ekin_blk0 = h->all_fused ? ek_a0[t] : ek_u0[t];
-        h->info[t].ekin_nblk = h->all_fused ? ek_an[t] : ek_un[t];
-    }
+    // the Ekin partials follow the update kernel in use
+    set_ekin_layout(h);
     CK(cudaMemcpy((void *)S.traj, h->info.data(), h->info.size() * sizeof(TrajInfo), cudaMemcpyHostToDevice));
     if ((rc = alloc0(A, 2, &S.status))) return rc;   // [0] status bits, [1] 1 + trajectory of a SHAKE failure
     // block tables
@@ -1009,6 +1022,7 @@ static void after_steps(qgpu_handle *h) { h->master = h->all_fused ? 1 : 0; }
 // Ekin partials of the update layout in use
 static void temperature_init(qgpu_handle *h, LaunchCtx &L) {
     if (h->all_fused) launch_update_f(h->S, h->B, L, EaccSel{EACC_FP32, h->zero_d, 0, 1}, h->NBcycle, 1);
+    else if (h->fused_d) launch_update_d(h->S, h->B, L, EaccSel{EACC_FP32, h->zero_d, 0, 1}, 1);
     else { launch_update(h->S, h->B, L, 0); launch_wrec(h->S, h->B, L); }
 }
 
@@ -1109,12 +1123,15 @@ static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every, int emo
     if (h->all_fused) {
         // the update's last block per trajectory ends the step
         launch_update_f(h->S, h->B, L, esel, h->NBcycle, 0, FIN_TEMP | FIN_STEP | FIN_NH, h->rec_d, h->rec_cap);
+    } else if (h->fused_d) {
+        launch_update_d(h->S, h->B, L, esel, 0, FIN_TEMP | FIN_STEP | FIN_NH | FIN_EK64, h->rec_d, h->rec_cap);
     } else {
         launch_integrate(h->S, h->B, L);
         launch_shake(h->S, h->B, L, -1);
         launch_update(h->S, h->B, L, 2);
         launch_wrec(h->S, h->B, L);
-        launch_finalize(h->S, L, FIN_TEMP | FIN_STEP | FIN_NH, h->rec_d, h->recctl_d, k, ene_every, h->rec_cap);
+        launch_finalize(h->S, L, FIN_TEMP | FIN_STEP | FIN_NH | FIN_EK64, h->rec_d, h->recctl_d, k, ene_every,
+                        h->rec_cap);
     }
 }
 
@@ -1269,7 +1286,7 @@ int qgpu_get_temperature(qgpu_handle *h, int32_t traj, double *out4) {
     TrajState ts;
     CK(cudaMemcpyAsync(&ts, h->S.tstate + traj, sizeof ts, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    out4[0] = ts.Temp; out4[1] = ts.Tfree; out4[2] = ts.tsf_solute; out4[3] = ts.tsf_solvent;
+    out4[0] = ts.Temp_d; out4[1] = ts.Tfree_d; out4[2] = ts.tsd_solute; out4[3] = ts.tsd_solvent;
     return 0;
 }
 
@@ -1400,7 +1417,8 @@ int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every) {
         CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
         CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
         temperature_init(h, L);
-        launch_finalize(h->S, L, FIN_TEMP | (h->nh_ready ? 0 : FIN_NH), nullptr, h->zero_d, 0, 1, 0);
+        launch_finalize(h->S, L, FIN_TEMP | (h->nh_ready ? 0 : FIN_NH) | (h->all_fused ? 0 : FIN_EK64), nullptr,
+                        h->zero_d, 0, 1, 0);
         h->nh_ready = 1;
         h->temp_init = 1;
     }
@@ -1589,18 +1607,19 @@ int qgpu_set_step(qgpu_handle *h, int64_t istep) {
 }
 
 int qgpu_set_precision(qgpu_handle *h, int32_t mode) {
-    if (!h || (mode != QGPU_PRECISION_MIXED && mode != QGPU_PRECISION_FP64))
+    if (!h || (mode != QGPU_PRECISION_MIXED && mode != QGPU_PRECISION_FP64 && mode != QGPU_PRECISION_FP64_UNFUSED))
         return fail(QGPU_E_INVALID, "qgpu_set_precision: bad arguments");
-    const bool fused = mode == QGPU_PRECISION_MIXED && h->can_fuse;
-    if (fused == h->all_fused) return 0;
+    const bool fused_f = mode == QGPU_PRECISION_MIXED && h->can_fuse;
+    const bool fused_d = mode == QGPU_PRECISION_FP64 && h->can_fuse;
+    if (fused_f == h->all_fused && fused_d == h->fused_d) return 0;
     LaunchCtx L{h->stream, &h->nlaunch};
     ensure_double(h, L);          // x/v from the float master before leaving it
+    // entering the float master: its velocities (and hi/lo positions) from x/v
+    if (fused_f) launch_mirror(h->S, h->B, L);
     CK(cudaStreamSynchronize(h->stream));
-    h->all_fused = fused;
-    for (int t = 0; t < h->ntraj; ++t) {
-        h->info[t].ekin_blk0 = fused ? h->ek_a0[t] : h->ek_u0[t];
-        h->info[t].ekin_nblk = fused ? h->ek_an[t] : h->ek_un[t];
-    }
+    h->all_fused = fused_f;
+    h->fused_d = fused_d;
+    set_ekin_layout(h);
     CK(cudaMemcpy((void *)h->S.traj, h->info.data(), h->info.size() * sizeof(TrajInfo), cudaMemcpyHostToDevice));
     if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     // the Ekin partials of the new layout are formed again before the next step
@@ -1746,7 +1765,8 @@ int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink si
     if (!h->temp_init) {
         // temperature() before the first step (md_run, src/md.f90:6395-6398)
         temperature_init(h, L);
-        launch_finalize(h->S, L, FIN_TEMP | (h->nh_ready ? 0 : FIN_NH), nullptr, h->zero_d, 0, 1, 0);
+        launch_finalize(h->S, L, FIN_TEMP | (h->nh_ready ? 0 : FIN_NH) | (h->all_fused ? 0 : FIN_EK64), nullptr,
+                        h->zero_d, 0, 1, 0);
         h->nh_ready = 1;
         h->temp_init = 1;
     }

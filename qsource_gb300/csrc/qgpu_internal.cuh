@@ -25,6 +25,7 @@
 #define FIN_TEMP 1              // temperature() and the Berendsen scales
 #define FIN_STEP 2              // a step has been taken: advance the Langevin random stream
 #define FIN_NH 4                // propagate the Nose-Hoover chain for the next step
+#define FIN_EK64 8              // FP64 step forms: Ekin from the int64 partials, temperatures and scales in FP64
 #define QG_WPBLK 512            // threads of the water polarisation kernel (one block per trajectory)
 #define S_GROUP_MASK 0xffffffffu
 #define QG_MAXS 4               // states handled by the engine (<= QGPU_MAX_STATES)
@@ -96,6 +97,7 @@ struct TrajInfo {
     float dtf, inv_dtf;
     // temperature(): T = Ekin * c, c = 2/(Boltz*Ndegf...); dt/tau_T; Temp0
     float cT, cTfree, cTfsu, cTfsv, dt_tau, Temp0f;
+    double dt_taud;             // dt/tau_T in FP64 (the FP64 step forms)
     // float copies of the restraint parameters for the per-step kernels
     float fk_wspheref, rwatf, Dwmzf, awmzf, fk_pshellf, fk_fixf;
     int separate_scaling, detail_temps;
@@ -157,6 +159,10 @@ struct TrajState {
     unsigned rnd;                   // randm state before the next step's random forces
     int fep_n;                      // recorded frames seen by the FEP accumulation
     double nh_s1, nh_s2;            // Nose-Hoover velocity scales of the next step
+    // FP64 copies: formed in FP64 from the int64 Ekin partials in the FP64
+    // step forms (FIN_EK64), widened from the float values otherwise
+    double Ekin_d, Temp_d, Tfree_d;
+    double tsd_solute, tsd_solvent; // Berendsen scales of the next step
 };
 
 struct DevSys {
@@ -284,6 +290,7 @@ struct DevSys {
     // energies and reductions
     unsigned long long *eacc;       // QG_NE per trajectory
     float *ekin_part;               // 4 per Ekin block
+    long long *ekin_fx;             // 4 per Ekin block: fixed-point (2^-32 kcal/mol) partials, FP64 step forms
     int *status;
 };
 
@@ -569,6 +576,9 @@ void launch_update(const DevSys &S, const BlockTables &B, LaunchCtx &L, int mode
 // step lists or records (e: the record selector of this step, nbcycle)
 void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int nbcycle, int ekin_only,
                      int fin = 0, double *rec = nullptr, int rec_cap = 0);
+// the fused step with the FP64 master (x, v, leap-frog and SHAKE in FP64)
+void launch_update_d(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int ekin_only, int fin = 0,
+                     double *rec = nullptr, int rec_cap = 0);
 // x = origin + hi + lo, v = velf for every atom
 void launch_sync_double(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *rec, const int *rec_base, int k,

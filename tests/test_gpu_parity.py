@@ -148,13 +148,17 @@ def test_shake_matches_oracle(systems):
     assert np.abs(xg - xo).max() < 1e-9
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name,ene_every", [("cfg1", 1), ("cfg1", 5), ("cfg1arqv", 5), ("cfg2ar", 5)])
-def test_short_md_matches_oracle(systems, name, ene_every):
-    """20 Berendsen leap-frog steps with SHAKE and lists every 10 steps.  With
-    ene_every=5 the unrecorded steps run the FP32 path (float master state,
-    FP32 SHAKE and bonded terms); recorded steps evaluate energies in FP64."""
+def test_short_md_matches_oracle(systems, name, ene_every, precision):
+    """20 Berendsen leap-frog steps with SHAKE and lists every 10 steps, with
+    the FP64 master (FP64 x, v, leap-frog and SHAKE; FP32 pair terms) and the
+    mixed form (float master state, FP32 SHAKE and bonded terms on unrecorded
+    steps); recorded steps evaluate energies in FP64."""
+    from qsource_gb300.abi import PRECISION
     s = systems[name]
     e = _engine(s)
+    e.set_precision(PRECISION[precision])
     rows = e.run(20, ene_every=ene_every)[0]
     o = _oracle(s)
     o.temperature()
@@ -171,7 +175,53 @@ def test_short_md_matches_oracle(systems, name, ene_every):
     assert np.abs(x - xo).max() < 1e-4
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("name", ["cfg1", "cfg2ar"])
+def test_fused_fp64_step_equals_unfused(systems, name):
+    """The fused FP64-master update (leap-frog, SHAKE of one water per lane
+    and the step's end in one kernel) against the separate FP64 update,
+    SHAKE and step-end kernels over 30 steps (three list updates): the same
+    arithmetic up to the association of products, with temperatures from the
+    same exact integer sums, so coordinates agree to 1e-10 A, velocities to
+    1e-9 and recorded energies to 1e-9 relative."""
+    from qsource_gb300.abi import PRECISION
+    s = systems[name]
+    out = []
+    for p in ("fp64", "fp64_unfused"):
+        e = _engine(s)
+        e.set_precision(PRECISION[p])
+        rows = e.run(30, ene_every=5)[0]
+        x, v = e.coords(0)
+        out.append((rows, x, v))
+    (ra, xa, va), (rb, xb, vb) = out
+    assert len(ra) == len(rb) == 6
+    assert np.abs(xa - xb).max() < 1e-10
+    assert np.abs(va - vb).max() < 1e-9
+    for a, b in zip(ra, rb):
+        for key in ("potential", "kinetic"):
+            assert abs(a[1][key] - b[1][key]) <= 1e-9 * max(1.0, abs(b[1][key])), (a[0], key)
+
+
+def test_fp64_step_float_coordinates_are_the_rounded_master(systems):
+    """The FP64-master step forms the pair kernels' float coordinates
+    (hi = float(x - origin), lo = float(x - origin - hi), and the packed
+    water records) from the bits of x with integer instructions.  Forming
+    them again from the same x with the conversion instructions
+    (qgpu_set_coords) must give bit-identical step-precision forces and
+    energies."""
+    from qsource_gb300.abi import PRECISION, QGPU_TERMS_STEP_PRECISION
+    s = systems["cfg2ar"]
+    e = _engine(s)
+    e.set_precision(PRECISION["fp64"])
+    e.run(15, ene_every=0)
+    d1, E1, EQ1 = e.pot_energy(0, terms=0x1F | QGPU_TERMS_STEP_PRECISION)
+    x, v = e.coords(0)
+    e.set_coords(0, x, v)
+    d2, E2, EQ2 = e.pot_energy(0, terms=0x1F | QGPU_TERMS_STEP_PRECISION)
+    assert np.array_equal(d1, d2)
+    assert E1 == E2
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64", "fp64_unfused"])
 @pytest.mark.parametrize("integrator", [0, 1])
 @pytest.mark.parametrize("thermostat", [0, 1, 2])
 def test_thermostats_match_oracle(systems, thermostat, integrator, precision):
@@ -182,12 +232,11 @@ def test_thermostats_match_oracle(systems, thermostat, integrator, precision):
     the FP64 oracle from the same start: recorded potential and kinetic
     energies to 1e-4 relative, coordinates to 1e-4 A."""
     import copy
-    from qsource_gb300.abi import QGPU_PRECISION_FP64
+    from qsource_gb300.abi import PRECISION
     s = copy.copy(systems["golden"])
     s.thermostat, s.integrator = thermostat, integrator
     e = _engine(s)
-    if precision == "fp64":
-        e.set_precision(QGPU_PRECISION_FP64)
+    e.set_precision(PRECISION[precision])
     rows = e.run(20, ene_every=5)[0]
     o = _oracle(s)
     o.temperature()

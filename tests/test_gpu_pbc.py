@@ -142,18 +142,17 @@ def test_pbc_results_do_not_depend_on_the_image(box):
     assert not _close(E1, Eo, E_KEYS)
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("precision", ["mixed", "fp64", "fp64_unfused"])
 @pytest.mark.parametrize("start", ["in_box", "images"])
 def test_pbc_md_matches_oracle(box, precision, start):
     """30 leap-frog Berendsen steps (0.1 fs, lists every 25 steps, solvent put
     back in the box before each list update).  From "images" the first
     put_back_in_box moves a third of the molecules: the engine and the oracle
     must move the same ones."""
-    from qsource_gb300.abi import QGPU_PRECISION_FP64
+    from qsource_gb300.abi import PRECISION
     s = _images(box) if start == "images" else box
     e = _engine(s)
-    if precision == "fp64":
-        e.set_precision(QGPU_PRECISION_FP64)
+    e.set_precision(PRECISION[precision])
     rows = e.run(30, ene_every=5)[0]
     o = _oracle(s)
     o.temperature()

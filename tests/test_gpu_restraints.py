@@ -58,16 +58,15 @@ def test_restraints_across_the_box(engine_lib):
     assert not _close(E, Eo, ["rst_protein", "rst_total"])
 
 
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+@pytest.mark.parametrize("precision", ["mixed", "fp64", "fp64_unfused"])
 def test_restrained_md_matches_oracle(engine_lib, precision):
     from oracle.oracle import Oracle
     from qsource_gb300 import synth
-    from qsource_gb300.abi import QGPU_PRECISION_FP64
+    from qsource_gb300.abi import PRECISION
     from qsource_gb300.engine import Engine
     s = with_restraints(synth.config(1, lambdas=(0.7, 0.3)))
     e = Engine(s)
-    if precision == "fp64":
-        e.set_precision(QGPU_PRECISION_FP64)
+    e.set_precision(PRECISION[precision])
     rows = e.run(20, ene_every=5)[0]
     o = Oracle(s)
     o.temperature()
