@@ -1,8 +1,9 @@
 """Writes the golden fixtures of the reference's own step-0 energy pins.
 
-Run in a container where the reference tree is mounted at /root/reference:
+Run with the path of the reference tree (qusers/qsource) as the argument, or
+in the environment variable QSOURCE_REFERENCE:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference tree>
 
 For each pinned system it parses the reference's .top/.fep/.inp inputs with
 qsource_gb300.system.System.from_files and stores the resulting start-up state
@@ -122,4 +123,7 @@ def main(ref: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("QSOURCE_REFERENCE", "")
+    if not ref or not os.path.isdir(ref):
+        sys.exit("usage: make_golden.py <reference tree>  (or set QSOURCE_REFERENCE)")
+    main(ref)
