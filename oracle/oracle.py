@@ -61,6 +61,9 @@ def lib() -> C.CDLL:
         L.oracle_rand_state.restype = C.c_int32
         L.oracle_rand_state.argtypes = [vp]
         L.oracle_put_back_in_box.argtypes = [vp]
+        L.oracle_qconn.restype = C.c_int
+        L.oracle_qconn.argtypes = [C.c_int] * 3 + [vp] * 4 + [C.c_int, C.c_int, vp, C.c_int, vp, C.c_int, vp, C.c_int,
+                                                       C.c_int, vp, C.c_int, vp, vp, vp, C.c_int] + [vp] * 9
         L.oracle_qfep_fep.restype = C.c_int
         L.oracle_qfep_fep.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_int, C.c_double, C.c_int, vp, vp, vp, vp]
         L.oracle_sizeof_desc.restype = C.c_int
@@ -181,3 +184,42 @@ def qfep_fep(paths, nstates: int, kT: float, nskip: int = 0):
     if rc:
         raise RuntimeError("qfep: cannot read the energy files")
     return dgf, dgr, dg, npts
+
+
+def qconn_lists(system):
+    """make_qconn + nbqqlist restated in C (oracle_qconn) from the topology
+    inputs kept on `system` (System.qconn_in): returns (qconn[ns, nsol, nq],
+    per-state nbqq records [(iq, j, jq, lj, el_scale)], qp_skip[nsol],
+    qp14 pairs [(iq, atom)])."""
+    qi = system.qconn_in
+    ns, nsol, nq = int(system.nstates), int(system.nat_solute), int(system.nqat)
+    iqseq = np.ascontiguousarray(system.iqseq, np.int32)
+    iqatom = np.ascontiguousarray(np.asarray(system.iqatom)[:nsol], np.int32)
+    iac = np.ascontiguousarray(np.asarray(system.iac)[:nsol], np.int32)
+    ljcod = np.ascontiguousarray(system.ljcod, np.int8)
+    natyps = int(system.natyps)
+    arr = {k: np.ascontiguousarray(qi[k], dt) for k, dt in
+           (("bnd", np.int32), ("qbnd", np.int32), ("exspec", np.int32), ("soft", np.int32), ("els_ij", np.int32),
+            ("els_v", np.float64))}
+    cap = 8 * (nq * nq + nsol * nq) * ns + 16
+    qconn = np.zeros((ns, nsol, max(nq, 1)), np.int8)
+    count = np.zeros(ns, np.int32)
+    o = {k: np.zeros(cap, np.int32) for k in ("iq", "j", "jq", "lj")}
+    els = np.zeros(cap)
+    qp_skip = np.zeros(max(nsol, 1), np.uint8)
+    nqp14 = np.zeros(1, np.int32)
+    qp14 = np.zeros(2 * cap, np.int32)
+    rc = lib().oracle_qconn(nsol, nq, ns, _p(iqseq), _p(iqatom), _p(iac), _p(ljcod), natyps,
+                            len(arr["bnd"]), _p(arr["bnd"]), len(arr["qbnd"]), _p(arr["qbnd"]),
+                            len(arr["exspec"]), _p(arr["exspec"]), int(qi["qvdw"]), len(arr["soft"]), _p(arr["soft"]),
+                            len(arr["els_ij"]), _p(arr["els_ij"]), _p(arr["els_v"]), _p(qconn), cap, _p(count),
+                            _p(o["iq"]), _p(o["j"]), _p(o["jq"]), _p(o["lj"]), _p(els), _p(qp_skip), _p(nqp14), _p(qp14))
+    if rc:
+        raise RuntimeError("oracle_qconn: capacity")
+    per_state, k = [], 0
+    for s in range(ns):
+        per_state.append([(int(o["iq"][k + r]), int(o["j"][k + r]), int(o["jq"][k + r]), int(o["lj"][k + r]),
+                           float(els[k + r])) for r in range(count[s])])
+        k += count[s]
+    pairs = [(int(qp14[2 * r]), int(qp14[2 * r + 1])) for r in range(nqp14[0])]
+    return qconn[:, :, :nq], per_state, qp_skip[:nsol], pairs

@@ -2059,3 +2059,155 @@ int oracle_qfep_fep(int nfiles, const char **paths, int nstates, double rt, int 
     free(V); free(lam);
     return rc;
 }
+
+/* ------------------------------------------------------------------------
+ * make_qconn (src/md.f90:9582-9620), find_bonded (:9625-9680), nbqqlist
+ * (:9716-9804) and the Q-atom / solute skip data that nbqplist reads
+ * (:10288 any(qconn(:,j,:) <= 3), :10306 qconn(1,j,iq) == 4 -> LJcod 3),
+ * restated from the topology.  Indices are 0-based; the Fortran 1-based
+ * levels are kept (1 = the Q atom itself, 2 bonded, 3 angle, 4 torsion,
+ * 9 = farther, 0 = special exclusion).
+ *
+ * Inputs: nsol solute atoms, nq Q atoms in ns states; iqseq[nq]; iqatom[nsol]
+ * (-1 = not a Q atom); iac[nsol] and the natyps x natyps ljcod matrix;
+ * the solute bond list before shrink_topology (nb rows of i, j, cod; cod 0 =
+ * redefined and skipped, -1 = shaken and kept); Q bonds (nqb rows of i, j,
+ * cod[ns]); special exclusions (nex rows of i, j, flag[ns]); the Q-Q pairs
+ * of the soft-pair list (nsoft rows of iq, jq) for LJ code 2 with qvdw_flag;
+ * Q-Q electrostatic scales (nels rows of iq, jq; els_v[nels*ns]).
+ * Outputs: qconn[ns][nsol][nq] (int8), per state the nbqq records in the
+ * reference's order concatenated (count[s]; iq, j, jq (-1 for a non-Q atom),
+ * LJ code, el_scale; capacity cap per state-concatenated arrays), qp_skip[nsol]
+ * and the (iq, atom) pairs with qconn(1, atom, iq) == 4 among atoms not
+ * skipped, atom-major.  Returns 0, or -1 when cap is too small.
+ * ------------------------------------------------------------------------ */
+typedef struct {
+    int nsol, nq, ns;
+    const int *iqatom, *bnd, *qbnd;
+    int nb, nqb;
+    int8_t *qconn;
+} qconn_ctx;
+
+#define QCONN(c, s, i, q) (c)->qconn[((size_t)(s) * (c)->nsol + (i)) * (c)->nq + (q)]
+
+static void find_bonded(qconn_ctx *c, int origin, int current, int level, int state) {
+    const int oq = c->iqatom[origin];
+    for (int b = 0; b < c->nb; ++b) {
+        const int bi = c->bnd[3 * b], bj = c->bnd[3 * b + 1], cod = c->bnd[3 * b + 2];
+        if (cod == 0) continue;   /* redefined (but not shaken) */
+        int next = -1;
+        if (bi == current) next = bj;
+        else if (bj == current) next = bi;
+        if (next < 0) continue;
+        const int nl = level + 1;
+        if (QCONN(c, state, next, oq) > nl) {
+            QCONN(c, state, next, oq) = (int8_t)nl;
+            if (nl < 4) find_bonded(c, origin, next, nl, state);
+        }
+    }
+    const int w = 2 + c->ns;
+    for (int b = 0; b < c->nqb; ++b) {
+        if (c->qbnd[w * b + 2 + state] <= 0) continue;
+        const int bi = c->qbnd[w * b], bj = c->qbnd[w * b + 1];
+        int next = -1;
+        if (bi == current) next = bj;
+        else if (bj == current) next = bi;
+        if (next < 0) continue;
+        const int nl = level + 1;
+        if (QCONN(c, state, next, oq) > nl) {
+            QCONN(c, state, next, oq) = (int8_t)nl;
+            if (nl < 4) find_bonded(c, origin, next, nl, state);
+        }
+    }
+}
+
+int oracle_qconn(int nsol, int nq, int ns, const int *iqseq, const int *iqatom, const int *iac, const int8_t *ljcod,
+                 int natyps, int nb, const int *bnd, int nqb, const int *qbnd, int nex, const int *exspec,
+                 int qvdw_flag, int nsoft, const int *soft, int nels, const int *els_ij, const double *els_v,
+                 int8_t *qconn, int cap, int *count, int *o_iq, int *o_j, int *o_jq, int *o_lj, double *o_els,
+                 uint8_t *qp_skip, int *nqp14, int *qp14) {
+    qconn_ctx c = {nsol, nq, ns, iqatom, bnd, qbnd, nb, nqb, qconn};
+    memset(qconn, 9, (size_t)ns * nsol * nq);
+    for (int iq = 0; iq < nq; ++iq)
+        for (int s = 0; s < ns; ++s) QCONN(&c, s, iqseq[iq], iq) = 1;
+    for (int iq = 0; iq < nq; ++iq)
+        for (int s = 0; s < ns; ++s) find_bonded(&c, iqseq[iq], iqseq[iq], 1, s);
+    /* special exclusions: both directions, in the states flagged */
+    for (int k = 0; k < nex; ++k) {
+        const int *e = exspec + (size_t)k * (2 + ns);
+        for (int d = 0; d < 2; ++d) {
+            const int a = e[d], other = e[1 - d];
+            const int iq = iqatom[a];
+            if (iq < 0) continue;
+            for (int s = 0; s < ns; ++s)
+                if (e[2 + s]) QCONN(&c, s, other, iq) = 0;
+        }
+    }
+    int n = 0;
+    for (int s = 0; s < ns; ++s) {
+        count[s] = 0;
+        /* Q-Q */
+        for (int iq = 0; iq < nq - 1; ++iq)
+            for (int jq = iq + 1; jq < nq; ++jq) {
+                const int j = iqseq[jq];
+                const int qc = QCONN(&c, s, j, iq);
+                if (qc <= 3) continue;
+                if (n >= cap) return -1;
+                int lj;
+                if (qc == 4) lj = 3;
+                else if (!qvdw_flag) lj = ljcod[iac[iqseq[iq]] * natyps + iac[j]];
+                else {
+                    lj = 1;
+                    for (int p = 0; p < nsoft; ++p)
+                        if ((iq == soft[2 * p] && jq == soft[2 * p + 1]) || (jq == soft[2 * p] && iq == soft[2 * p + 1])) {
+                            lj = 2;
+                            break;
+                        }
+                }
+                /* the reference's loop: the first matching entry wins, else 1 */
+                double els = 1.0;
+                for (int p = 0; p < nels; ++p) {
+                    const int k = els_ij[2 * p], l = els_ij[2 * p + 1];
+                    if ((iq == k && jq == l) || (iq == l && jq == k)) { els = els_v[(size_t)p * ns + s]; break; }
+                }
+                o_iq[n] = iq; o_j[n] = j; o_jq[n] = jq; o_lj[n] = lj; o_els[n] = els;
+                n++; count[s]++;
+            }
+        /* Q-non-Q: solute atoms bonded or angled to a Q atom in some state */
+        for (int j = 0; j < nsol; ++j) {
+            if (iqatom[j] >= 0) continue;
+            int near = 0;
+            for (int s2 = 0; s2 < ns && !near; ++s2)
+                for (int iq = 0; iq < nq; ++iq)
+                    if (QCONN(&c, s2, j, iq) <= 3) { near = 1; break; }
+            if (!near) continue;
+            for (int iq = 0; iq < nq; ++iq) {
+                const int qc = QCONN(&c, s, j, iq);
+                if (qc < 4) continue;
+                if (n >= cap) return -1;
+                o_iq[n] = iq; o_j[n] = j; o_jq[n] = -1;
+                o_lj[n] = qc == 4 ? 3 : (qvdw_flag ? 1 : ljcod[iac[iqseq[iq]] * natyps + iac[j]]);
+                o_els[n] = 1.0;
+                n++; count[s]++;
+            }
+        }
+    }
+    /* nbqplist's skips (:10288) and 1-4 codes from state 1 (:10306) */
+    int np = 0;
+    for (int j = 0; j < nsol; ++j) {
+        int skip = 0;
+        for (int s = 0; s < ns && !skip; ++s)
+            for (int iq = 0; iq < nq; ++iq)
+                if (QCONN(&c, s, j, iq) <= 3) { skip = 1; break; }
+        qp_skip[j] = (uint8_t)skip;
+        if (skip) continue;
+        for (int iq = 0; iq < nq; ++iq)
+            if (QCONN(&c, 0, j, iq) == 4) {
+                if (np >= cap) return -1;
+                qp14[2 * np] = iq; qp14[2 * np + 1] = j;
+                np++;
+            }
+    }
+    *nqp14 = np;
+    return 0;
+}

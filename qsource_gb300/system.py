@@ -414,7 +414,18 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
     shake_j = np.array([c[1] for c in flat], dtype=np.int32)
     shake_d2 = np.array([c[2] for c in flat], dtype=np.float64)
 
-    # --- make_qconn (src/md.f90:9582-9611) and nbqqlist (9691-9804)
+    # --- make_qconn (src/md.f90:9582-9611) and nbqqlist (9691-9804); their
+    # inputs are kept on the System so that the oracle's restatement can
+    # rebuild the lists independently (tests/test_oracle_qconn.py)
+    qconn_in = {
+        "bnd": np.asarray(bnd[:top["nbonds_solute"], :3], dtype=np.int32).reshape(-1, 3),
+        "qbnd": np.asarray(qbnd, dtype=np.int32).reshape(-1, 2 + S),
+        "exspec": np.array([[i, j] + [int(bool(x)) for x in f[:S]] for i, j, f in exspec], dtype=np.int32).reshape(-1, 2 + S),
+        "soft": np.array(soft_pairs, dtype=np.int32).reshape(-1, 2),
+        "els_ij": np.array([(a, b) for a, b, _ in el_scale], dtype=np.int32).reshape(-1, 2),
+        "els_v": np.array([list(v[:S]) for _, _, v in el_scale], dtype=np.float64).reshape(-1, S),
+        "qvdw": np.int32(1 if qvdw_flag else 0),
+    }
     qconn = np.full((S, nsol, nq), 9, dtype=np.int8)
     adj_cl: dict[int, list[int]] = {}
     for b in range(top["nbonds_solute"]):
@@ -603,7 +614,7 @@ def build(top: dict, fep: dict | None, inp: dict) -> System:
         iqseq=iqseq.astype(np.int32), qcrg=qcrg, qvdw_flag=qvdw_flag, qiac=qiac, qavdw=qavdw, qbvdw=qbvdw,
         sc_lookup=sc_lookup, lambdas=lam[:S] + [0.0] * (MAX_STATES - S),
         qp_skip=qp_skip, qp14_pairs=np.array(qp14, dtype=np.int32).reshape(-1, 2),
-        nbqq_count=nbqq_count + [0] * (MAX_STATES - S), nbqq=nbqq,
+        nbqq_count=nbqq_count + [0] * (MAX_STATES - S), nbqq=nbqq, qconn_in=qconn_in,
         qbnd=qbnd, qbondlib=qbondlib, qang=qang, qanglib=qanglib, qtor=qtor, qtorlib=qtorlib,
         qimp=qimp, qimplib=qimplib,
         bnd=bnd, nbonds_solute=nb_sol, bondlib=top["bondlib"], ang=ang, nangles_solute=na_sol, anglib=anglib,
