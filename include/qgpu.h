@@ -473,6 +473,14 @@ int qgpu_mlp_train(float *params, float *adam_m, float *adam_v, const float *X, 
    (g1 < g2), with g1,g2 0-based group indices.  Returns the count in *npairs;
    rows are written only if cap >= count. */
 int qgpu_get_group_pairs(qgpu_handle *h, int32_t traj, int32_t *pairs, int64_t cap, int64_t *npairs);
+/* Q-atom lists of the last list build (nbqplist / nbqplis2 / nbqplist_box,
+   src/md.f90:10215, :9946, :10327; nbqwlist / nbqwlist_box, :10464, :10554):
+   the solute atoms paired with every Q atom (0-based atom indices, ascending;
+   atoms that nbqplist skips, :10288, are absent) and the waters paired with
+   every Q atom (their O atoms, ascending).  Counts in *nqp / *nqw; rows are
+   written up to cap_qp / cap_qw. */
+int qgpu_get_q_lists(qgpu_handle *h, int32_t traj, int32_t *qp_atoms, int64_t cap_qp, int64_t *nqp,
+                     int32_t *qw_waters, int64_t cap_qw, int64_t *nqw);
 /* LRF records of the last list build: ncgp rows of 3 centre + 1 + 3 + 9 + 27
    doubles (cgp_cent, phi0, phi1, phi2, phi3), the LRF_TYPE of md.f90:444-450. */
 int qgpu_get_lrf(qgpu_handle *h, int32_t traj, double *lrf43);

@@ -136,6 +136,7 @@ EXPORTS = {
     "qgpu_destroy": (_i32, [C.c_void_p]),
     "qgpu_last_error": (_i32, [C.c_char_p, _i32]),
     "qgpu_ntraj": (_i32, [C.c_void_p]),
+    "qgpu_get_q_lists": (_i32, [C.c_void_p, _i32, _P, C.c_int64, _P, _P, C.c_int64, _P]),
     "qgpu_set_coords": (_i32, [C.c_void_p, _i32, _P, _P]),
     "qgpu_get_coords": (_i32, [C.c_void_p, _i32, _P, _P]),
     "qgpu_set_coords_all": (_i32, [C.c_void_p, _P, _P]),

@@ -1313,6 +1313,32 @@ int qgpu_get_group_pairs(qgpu_handle *h, int32_t traj, int32_t *pairs, int64_t c
     return 0;
 }
 
+int qgpu_get_q_lists(qgpu_handle *h, int32_t traj, int32_t *qp_atoms, int64_t cap_qp, int64_t *nqp,
+                     int32_t *qw_waters, int64_t cap_qw, int64_t *nqw) {
+    if (!h || traj < 0 || traj >= h->ntraj) return fail(QGPU_E_INVALID, "bad trajectory index");
+    const int N = h->natom[traj], a0 = h->atom0[traj];
+    std::vector<uint8_t> qp(N), qw(N);
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(qp.data(), h->S.qp_member + a0, N, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(qw.data(), h->S.qw_member + a0, N, cudaMemcpyDeviceToHost));
+    const int nsol = h->info[traj].nat_solute;
+    int64_t np = 0, nw = 0;
+    for (int i = 0; i < N; ++i) {
+        if (i < nsol && qp[i]) {
+            if (qp_atoms && np < cap_qp) qp_atoms[np] = i;
+            np++;
+        }
+        // water O atoms: the first atom of each 3-atom solvent molecule
+        if (i >= nsol && (i - nsol) % 3 == 0 && qw[i]) {
+            if (qw_waters && nw < cap_qw) qw_waters[nw] = i;
+            nw++;
+        }
+    }
+    if (nqp) *nqp = np;
+    if (nqw) *nqw = nw;
+    return 0;
+}
+
 int qgpu_get_lrf(qgpu_handle *h, int32_t traj, double *lrf43) {
     if (!h || traj < 0 || traj >= h->ntraj || !lrf43) return fail(QGPU_E_INVALID, "bad arguments");
     int G = h->ncgp[traj], g0 = h->grp0[traj];

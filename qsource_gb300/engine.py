@@ -121,6 +121,16 @@ class Engine:
         self._check(self.lib.qgpu_get_group_pairs(self.h, traj, abi.ptr(out), n.value, C.byref(n)))
         return out[: n.value]
 
+    def q_lists(self, traj: int = 0):
+        """(solute atoms, water O atoms) on the Q-atom lists of the last list
+        build (qgpu_get_q_lists), 0-based, ascending."""
+        n = self.systems[traj].natom
+        qp, qw = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        npp, nww = C.c_int64(), C.c_int64()
+        self._check(self.lib.qgpu_get_q_lists(self.h, traj, abi.ptr(qp), n, C.byref(npp), abi.ptr(qw), n,
+                                              C.byref(nww)))
+        return qp[:npp.value].copy(), qw[:nww.value].copy()
+
     def lrf(self, traj: int = 0) -> np.ndarray:
         out = np.zeros((len(self.systems[traj].cgp_first), 43))
         self._check(self.lib.qgpu_get_lrf(self.h, traj, abi.ptr(out)))

@@ -252,6 +252,50 @@ def test_thermostats_match_oracle(systems, thermostat, integrator, precision):
     assert abs(x - xo).max() < 1e-4
 
 
+def q_lists_of_oracle(o, nsol, nq):
+    """Partner atoms of the oracle's nbqp records and O atoms of its nbqw
+    records, with the record counts."""
+    qp, qw = o.get_list("qp"), o.get_list("qw")
+    atoms = np.unique(qp[:, 1]) if len(qp) else np.zeros(0, np.int32)
+    wat = qw[:, 1] - (qw[:, 1] - nsol) % 3 if len(qw) else np.zeros(0, np.int32)
+    return atoms, np.unique(wat), len(qp), len(qw)
+
+
+@pytest.mark.parametrize("rcq", [None, 12.0])
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg2sw", "cfg4"])
+def test_q_lists_exact(systems, name, rcq):
+    """The Q-atom lists (nbqplist / nbqplis2, nbqwlist; src/md.f90:10215,
+    :9946, :10464) are index work: the engine's solute partners and waters
+    equal the oracle's record sets exactly, every partner paired with every
+    Q atom (3 records per water and Q atom), skipped atoms (:10288) absent.
+    With Rcq = 12 A the lists are rebuilt at every list update and cut
+    through the system; they are compared again after 20 MD steps."""
+    import copy
+    s = copy.copy(systems[name])
+    if rcq:
+        s.Rcq = rcq
+    nsol, nq = int(s.nat_solute), int(s.nqat)
+    e = _engine(s)
+    e.make_pair_lists()
+    o = _oracle(s)
+    o.make_pair_lists()
+    for stage in ("start", "after 20 steps"):
+        qp, qw = e.q_lists(0)
+        atoms, wat, nrec_p, nrec_w = q_lists_of_oracle(o, nsol, nq)
+        assert np.array_equal(qp, atoms), stage
+        assert np.array_equal(qw, wat), stage
+        assert nrec_p == nq * len(qp) and nrec_w == 3 * nq * len(qw), stage
+        if rcq:
+            assert 0 < len(qw) < int(s.nwat), stage
+        if stage == "start":
+            if not rcq:
+                break
+            e.run(20, ene_every=0)
+            x, v = e.coords(0)
+            o.set_coords(x, v)
+            o.make_pair_lists()
+
+
 @pytest.mark.parametrize("name", ["golden", "cfg1", "cfg4", "cfg1arqv", "cfg2ar"])
 def test_step_precision_forces(systems, name):
     """The precision of an unrecorded MD step (QGPU_TERMS_STEP_PRECISION: FP32

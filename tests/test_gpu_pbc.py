@@ -142,6 +142,22 @@ def test_pbc_results_do_not_depend_on_the_image(box):
     assert not _close(E1, Eo, E_KEYS)
 
 
+def test_pbc_q_lists_exact(box):
+    """nbqplist_box / nbqwlist_box (src/md.f90:10327, :10554): partners
+    within Rcq of the Q switching atom, minimum image, rebuilt at every
+    list update; equal to the oracle's record sets."""
+    from test_gpu_parity import q_lists_of_oracle
+    e = _engine(box)
+    e.make_pair_lists()
+    o = _oracle(box)
+    o.make_pair_lists()
+    qp, qw = e.q_lists(0)
+    atoms, wat, nrec_p, nrec_w = q_lists_of_oracle(o, int(box.nat_solute), int(box.nqat))
+    assert np.array_equal(qp, atoms) and np.array_equal(qw, wat)
+    assert nrec_w == 3 * int(box.nqat) * len(qw)
+    assert 0 < len(qw) < int(box.nwat)
+
+
 @pytest.mark.parametrize("precision", ["mixed", "fp64", "fp64_unfused"])
 @pytest.mark.parametrize("start", ["in_box", "images"])
 def test_pbc_md_matches_oracle(box, precision, start):
