@@ -223,3 +223,22 @@ def qconn_lists(system):
         k += count[s]
     pairs = [(int(qp14[2 * r]), int(qp14[2 * r + 1])) for r in range(nqp14[0])]
     return qconn[:, :, :nq], per_state, qp_skip[:nsol], pairs
+
+
+def md_frames(system, nsteps: int, ene_every: int, couplings):
+    """One window's MD run with the oracle, as the frames of qdyn's energy
+    file: at every recorded nonzero step (md_run writes frames there, src/
+    md.f90:6630) the per-state totals EQ(s)%total, and for each coupling
+    (i, j, A) of a constant off-diagonal element (mu = 0) the record
+    (i, j, A, 0).  Returns (lambdas, frames) as qfep_ref.read_en does."""
+    o = Oracle(system)
+    o.temperature()
+    rc, _, qrows, _ = o.md_run(nsteps)
+    if rc:
+        raise RuntimeError(f"oracle md_run status {rc}")
+    S = int(system.nstates)
+    lam = [float(system.lambdas[s]) for s in range(S)]
+    frames = []
+    for k in range(ene_every, nsteps, ene_every):
+        frames.append(([qrows[k][s]["total"] for s in range(S)], [(i, j, a, 0.0) for i, j, a in couplings]))
+    return lam, frames

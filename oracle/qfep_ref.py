@@ -53,6 +53,17 @@ def read_en(path, nstates, num_offd, gas=False):
 
 def evb(paths, nstates, kT, noffd=0, nskip=0, gas=False, nbins=20, nmin=1, alpha=None, scale_hij=0.0,
         couplings=(), coeff=None):
+    """qfep Parts 1-3 on energy files (one per window, in lambda order)."""
+    num_offd = noffd if noffd != 0 else len(couplings)
+    windows = [read_en(p, nstates, num_offd, gas) for p in paths]
+    return evb_windows(windows, nstates, kT, noffd, nskip, nbins, nmin, alpha, scale_hij, couplings, coeff)
+
+
+def evb_windows(windows, nstates, kT, noffd=0, nskip=0, nbins=20, nmin=1, alpha=None, scale_hij=0.0,
+                couplings=(), coeff=None):
+    """qfep Parts 1-3 on windows given as (lambdas, frames), each frame
+    (per-state energies, [(i, j, Hij, rkl) per coupling]) as read_en returns
+    them."""
     S = nstates
     rt = kT
     num_offd = noffd if noffd != 0 else len(couplings)
@@ -64,8 +75,7 @@ def evb(paths, nstates, kT, noffd=0, nskip=0, gas=False, nbins=20, nmin=1, alpha
             A[i - 1, j - 1], mu[i - 1, j - 1], eta[i - 1, j - 1], r0[i - 1, j - 1] = a, m, e, r
     gapmin, gapmax = 999.0, -999.0
     F = []
-    for path in paths:
-        lam, frames = read_en(path, S, num_offd, gas)
+    for lam, frames in windows:
         v, vg, c1, c2, gap, rr = [], [], [], [], [], []
         for ipt, (E, od) in enumerate(frames, start=1):
             E = [E[i] + alfa[i] for i in range(S)]
