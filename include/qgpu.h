@@ -499,6 +499,13 @@ int qgpu_profile(qgpu_handle *h, int32_t nsteps, char *names, double *ms, int64_
    over all SMs, timed with CUDA events); the roofline denominator of the
    FP32-bound pair and LRF kernels. */
 int qgpu_fp32_peak(double *tflops);
+/* FP64 FMA throughput of the current device in TFLOP/s (independent DFMA
+   chains on every SM), the denominator of the FP64 update's roofline. */
+int qgpu_fp64_peak(double *tflops);
+/* SHAKE work since the last call, over all trajectories: molecule sweeps
+   (every step form) and constraint visits (the FP64 fused step); the
+   counters are reset. */
+int qgpu_shake_counts(qgpu_handle *h, int64_t *sweeps, int64_t *visits);
 
 /* ---- allocation-free scan ----------------------------------------------- */
 /* Has no counterpart in the reference.  For callers that may not allocate

@@ -467,7 +467,7 @@ __device__ __forceinline__ double div_nr(double diff, double den) {
 // not revisited; at most SHAKE_MAX_ITER sweeps.  The tolerance test compares
 // the bit patterns of |diff| and the (positive) tolerance as integers.
 __device__ int shake_water_d(double (&x)[3][3], const double (&xx)[3][3], const double (&w)[3], const double (&d2)[3],
-                             bool *fail) {
+                             bool *fail, int *visits) {
     double xxij[3][3], den0[3];
     long long tolb[3];
 #pragma unroll
@@ -480,11 +480,12 @@ __device__ int shake_water_d(double (&x)[3][3], const double (&xx)[3][3], const 
         tolb[c] = __double_as_longlong(SHAKE_TOL * d2[c]);
     }
     unsigned ready = 0u;
-    int nits = 0;
+    int nits = 0, nv = 0;
     for (;;) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             if (ready & (1u << c)) continue;
+            nv++;
             const int i = c == 2 ? 1 : 0, j = c == 0 ? 1 : 2;
             const double xij0 = x[i][0] - x[j][0], xij1 = x[i][1] - x[j][1], xij2 = x[i][2] - x[j][2];
             const double diff = d2[c] - (xij0 * xij0 + xij1 * xij1 + xij2 * xij2);
@@ -502,6 +503,7 @@ __device__ int shake_water_d(double (&x)[3][3], const double (&xx)[3][3], const 
         if (ready == 7u) break;
         if (nits >= SHAKE_MAX_ITER) { *fail = true; break; }
     }
+    *visits = nv;
     return nits;
 }
 
@@ -590,7 +592,7 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
     if (water_blk && !ekin_only) {
         __syncthreads();
         if (t < 32) {
-            int nits = 0;
+            int nits = 0, nvis = 0;
             if (c0 >= 0) {
                 double wx[3][3], wxx[3][3], ww[3];
                 const int o = S.shk_i[c0];
@@ -602,7 +604,7 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
                     ww[k] = S.winv[o + k];
                 }
                 bool failed = false;
-                nits = shake_water_d(wx, wxx, ww, d2, &failed);
+                nits = shake_water_d(wx, wxx, ww, d2, &failed, &nvis);
                 if (failed) { atomicOr(S.status, ST_SHAKE); atomicCAS(S.status + 1, 0, tr + 1); }
                 S.msweep[m_sh] = (uint8_t)min(nits, 255);
 #pragma unroll
@@ -610,8 +612,11 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
 #pragma unroll
                     for (int c = 0; c < 3; ++c) s_x[c][3 * t + k] = wx[k][c];
             }
-            for (int o = 16; o > 0; o >>= 1) nits += __shfl_down_sync(0xffffffffu, nits, o);
-            if (t == 0 && nits) atomicAdd(&S.tstate[tr].shake_iters, nits);
+            for (int o = 16; o > 0; o >>= 1) {
+                nits += __shfl_down_sync(0xffffffffu, nits, o);
+                nvis += __shfl_down_sync(0xffffffffu, nvis, o);
+            }
+            if (t == 0 && nits) { atomicAdd(&S.tstate[tr].shake_iters, nits); atomicAdd(&S.tstate[tr].shake_visits, nvis); }
         }
         __syncthreads();
         if (a >= 0)
@@ -1059,6 +1064,46 @@ __global__ void k_fma_peak(float *out, int iters, float a, float b) {
     }
     const float s = r0 + r1 + r2 + r3 + r4 + r5 + r6 + r7;
     if (s == 12345.678f) out[0] = s;   // keeps the chains live
+}
+
+// FP64 FMA throughput probe: 8 independent DFMA chains per thread.
+__global__ void k_dfma_peak(double *out, int iters, double a, double b) {
+    double r0 = threadIdx.x, r1 = r0 + 1, r2 = r0 + 2, r3 = r0 + 3, r4 = r0 + 4, r5 = r0 + 5, r6 = r0 + 6, r7 = r0 + 7;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            r0 = fma(r0, a, b); r1 = fma(r1, a, b); r2 = fma(r2, a, b); r3 = fma(r3, a, b);
+            r4 = fma(r4, a, b); r5 = fma(r5, a, b); r6 = fma(r6, a, b); r7 = fma(r7, a, b);
+        }
+    }
+    const double s = r0 + r1 + r2 + r3 + r4 + r5 + r6 + r7;
+    if (s == 12345.678) out[0] = s;   // keeps the chains live
+}
+
+extern "C" int qgpu_fp64_peak(double *tflops) {
+    if (!tflops) return 1;
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 2;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    double *out = nullptr;
+    if (cudaMalloc(&out, sizeof(double)) != cudaSuccess) return 2;
+    const int threads = 256, blocks = nsm * 2, iters = 64;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    k_dfma_peak<<<blocks, threads>>>(out, 4, 0.999, 0.001);   // warm-up
+    cudaEventRecord(a);
+    k_dfma_peak<<<blocks, threads>>>(out, iters, 0.999, 0.001);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    const double flops = 2.0 * 8 * 4 * (double)iters * threads * blocks;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 extern "C" int qgpu_fp32_peak(double *tflops) {

@@ -827,7 +827,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     S.traj = ti;
     std::vector<TrajState> tsh(ntraj);
     for (auto &q : tsh) {
-        q.Temp = q.Tfree = q.Ekin = 0.f; q.shake_iters = 0;
+        q.Temp = q.Tfree = q.Ekin = 0.f; q.shake_iters = 0; q.shake_visits = 0;
         q.tsf_solute = q.tsf_solvent = 1.f; q.wshiftf = 0.f;
         q.Ekin_d = q.Temp_d = q.Tfree_d = 0.0; q.tsd_solute = q.tsd_solvent = 1.0;
         q.rnd = rnd0[&q - tsh.data()]; q.nh_s1 = q.nh_s2 = 1.0;
@@ -1294,6 +1294,22 @@ int qgpu_shake(qgpu_handle *h, int32_t traj, const double *xx, double *x, int32_
     CK(cudaMemcpyAsync(&it, &h->S.tstate[traj].shake_iters, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     if (int rc = check_status(h)) return rc;
     if (niter) *niter = h->info[traj].nshake_mol ? it / h->info[traj].nshake_mol : 0;
+    return 0;
+}
+
+int qgpu_shake_counts(qgpu_handle *h, int64_t *sweeps, int64_t *visits) {
+    if (!h) return fail(QGPU_E_INVALID, "null handle");
+    std::vector<TrajState> ts(h->ntraj);
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(ts.data(), h->S.tstate, ts.size() * sizeof(TrajState), cudaMemcpyDeviceToHost));
+    int64_t sw = 0, vi = 0;
+    for (const TrajState &q : ts) { sw += (unsigned)q.shake_iters; vi += (unsigned)q.shake_visits; }
+    for (int t = 0; t < h->ntraj; ++t) {
+        CK(cudaMemset(&h->S.tstate[t].shake_iters, 0, sizeof(int)));
+        CK(cudaMemset(&h->S.tstate[t].shake_visits, 0, sizeof(int)));
+    }
+    if (sweeps) *sweeps = sw;
+    if (visits) *visits = vi;
     return 0;
 }
 

@@ -155,7 +155,8 @@ struct TrajState {
     float Temp, Tfree, Ekin;
     float tsf_solute, tsf_solvent;  // Berendsen scales of the next step
     float wshiftf;                  // sqrt(Boltz*Tfree/fk_wsphere), restrain_solvent
-    int shake_iters;
+    int shake_iters;                // SHAKE sweeps (molecule sweeps) since the counter was read
+    int shake_visits;               // constraint visits of the FP64 fused step's SHAKE (same)
     unsigned rnd;                   // randm state before the next step's random forces
     int fep_n;                      // recorded frames seen by the FEP accumulation
     double nh_s1, nh_s2;            // Nose-Hoover velocity scales of the next step

@@ -131,6 +131,13 @@ class Engine:
                                               C.byref(nww)))
         return qp[:npp.value].copy(), qw[:nww.value].copy()
 
+    def shake_counts(self):
+        """(molecule sweeps, constraint visits) of SHAKE since the last call
+        (qgpu_shake_counts; the counters restart)."""
+        sw, vi = C.c_int64(), C.c_int64()
+        self._check(self.lib.qgpu_shake_counts(self.h, C.byref(sw), C.byref(vi)))
+        return sw.value, vi.value
+
     def lrf(self, traj: int = 0) -> np.ndarray:
         out = np.zeros((len(self.systems[traj].cgp_first), 43))
         self._check(self.lib.qgpu_get_lrf(self.h, traj, abi.ptr(out)))
