@@ -9,9 +9,6 @@
 #define BOLTZ 0.001986          // src/md.f90:54
 #define SHAKE_TOL 0.0001        // src/md.f90:460
 #define SHAKE_MAX_ITER 1000     // src/md.f90:461
-#ifndef QG_UPD_SORT
-#define QG_UPD_SORT 1           // order the waters of the FP64 step by their last SHAKE sweeps
-#endif
 #ifndef QG_UPD_D_MINB
 #define QG_UPD_D_MINB 8         // k_update_d register bound: 8 resident blocks, the grid of the batch in one wave
 #endif
@@ -521,11 +518,7 @@ __device__ int shake_water_d(double (&x)[3][3], const double (&xx)[3][3], const 
 // the current v (temperature before the first step).  fin: the step's end in
 // the last block of each trajectory, as in k_update_f.  The per-atom FP64
 // work is spread over the block's three warps; the SHAKE of 32 waters is one
-// warp's (its FP64 instructions cost the same for any number of active lanes),
-// and that warp loops until its slowest water converges: the block takes its
-// waters through S.wslot, which k_water_order fills so that waters needing
-// similar sweep counts in the last step share a warp.  Every water's update is
-// independent and the Ekin sums are integer: the order changes no result.
+// warp's (its FP64 instructions cost the same for any number of active lanes).
 __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, const int *uatom, const int *ucon,
                                                                      const uint8_t *ublk_water, EaccSel esel,
                                                                      int ekin_only, int fin, double *rec, int rec_cap) {
@@ -533,21 +526,15 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
     __shared__ float4 s_h[QG_UBLK], s_l[QG_UBLK];
     __shared__ long long red[4][QG_UBLK / 32];
     const int t = threadIdx.x;
+    const int a = uatom[blockIdx.x * QG_UBLK + t];
     const bool water_blk = ublk_water[blockIdx.x] != 0;
-    int a = uatom[blockIdx.x * QG_UBLK + t];
-    const int tr = a >= 0 ? S.atraj[a] : -1 - a;
-    // water blocks: thread t is atom t % 3 of the water in slot t / 3
-    const int m_own = water_blk ? S.wslot[blockIdx.x * 32 + t / 3] : -1;
-    if (water_blk) a = m_own >= 0 ? S.shk_i[S.shk_first[m_own]] + t % 3 : -1 - tr;
-    int c0 = -1, m_sh = -1;
+    int c0 = -1;
     double d2[3] = {0.0, 0.0, 0.0};
     if (water_blk && !ekin_only && t < 32) {
-        m_sh = S.wslot[blockIdx.x * 32 + t];
-        if (m_sh >= 0) {
-            c0 = S.shk_first[m_sh];
-            d2[0] = S.shk_d2[c0]; d2[1] = S.shk_d2[c0 + 1]; d2[2] = S.shk_d2[c0 + 2];
-        }
+        c0 = ucon[blockIdx.x * QG_UBLK + 3 * t];
+        if (c0 >= 0) { d2[0] = S.shk_d2[c0]; d2[1] = S.shk_d2[c0 + 1]; d2[2] = S.shk_d2[c0 + 2]; }
     }
+    const int tr = a >= 0 ? S.atraj[a] : -1 - a;
     const TrajInfo &T = S.traj[tr];
     double x[3] = {0.0, 0.0, 0.0}, xo[3] = {0.0, 0.0, 0.0}, v[3] = {0.0, 0.0, 0.0};
     if (a >= 0) {
@@ -606,7 +593,6 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
                 bool failed = false;
                 nits = shake_water_d(wx, wxx, ww, d2, &failed, &nvis);
                 if (failed) { atomicOr(S.status, ST_SHAKE); atomicCAS(S.status + 1, 0, tr + 1); }
-                S.msweep[m_sh] = (uint8_t)min(nits, 255);
 #pragma unroll
                 for (int k = 0; k < 3; ++k)
 #pragma unroll
@@ -656,10 +642,10 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
     if (water_blk && !ekin_only) {
         __syncthreads();
         const int w3 = t - t % 3;
-        if (m_own >= 0) {
+        if (ucon[blockIdx.x * QG_UBLK + w3] >= 0) {
             const float4 wh[3] = {s_h[w3], s_h[w3 + 1], s_h[w3 + 2]};
             const float4 wl[3] = {s_l[w3], s_l[w3 + 1], s_l[w3 + 2]};
-            S.wrec[a] = wrec_part(wh, wl, t % 3);   // part t % 3 of the record, at the water's O + t % 3
+            S.wrec[uatom[blockIdx.x * QG_UBLK + w3] + t % 3] = wrec_part(wh, wl, t % 3);
         }
     }
     const int lane = t & 31, warp = t >> 5;
@@ -686,50 +672,6 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
     __threadfence();
     finalize_traj(S, tr, t, s_fin, fin, rec, esel.recctl, esel.k, esel.ene_every, rec_cap);
     if (t == 0) S.fin_cnt[tr] = 0;
-}
-
-// Water slots of one trajectory (wrange: first slot, waters; one block per
-// trajectory) reordered by the SHAKE sweeps each water needed in the last
-// step: rank 0 needs the most (counting sort over 32 bins); ranks go to
-// groups of 32 (one SHAKE warp each), and the groups are laid out heavy,
-// light, next heavy, next light ... so that consecutive blocks, which the
-// block scheduler tends to place on the same SM, mix heavy and light warps.
-// Segments of QG_WORD_SEG waters are ordered independently.  The order
-// within a bin is whatever the shared-memory atomics give: the update's
-// results do not depend on the order.
-#define QG_WORD_SEG 4096
-__global__ void k_water_order(DevSys S, const int2 *wrange) {
-    __shared__ int s_m[QG_WORD_SEG];
-    __shared__ int hist[32], off[32], cnt;
-    const int2 R = wrange[blockIdx.x];
-    for (int seg = 0; seg < R.y; seg += QG_WORD_SEG) {
-        const int n = min(QG_WORD_SEG, R.y - seg);
-        const int G = (n + 31) / 32, Gh = (G + 1) / 2;
-        int *slot = S.wslot + R.x + seg;          // G * 32 slots, n of them hold waters
-        if (threadIdx.x < 32) hist[threadIdx.x] = 0;
-        if (threadIdx.x == 0) cnt = 0;
-        __syncthreads();
-        for (int k = threadIdx.x; k < G * 32; k += blockDim.x) {
-            const int m = slot[k];
-            if (m < 0) continue;
-            s_m[atomicAdd(&cnt, 1)] = m;
-            atomicAdd(&hist[31 - min((int)S.msweep[m], 31)], 1);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int acc = 0;
-            for (int b = 0; b < 32; ++b) { off[b] = acc; acc += hist[b]; }
-        }
-        for (int k = threadIdx.x; k < G * 32; k += blockDim.x) slot[k] = -1;
-        __syncthreads();
-        for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
-            const int m = s_m[k];
-            const int r = atomicAdd(&off[31 - min((int)S.msweep[m], 31)], 1);
-            const int j = r >> 5, p = j < Gh ? 2 * j : 2 * (G - 1 - j) + 1;
-            slot[32 * p + (r & 31)] = m;
-        }
-        __syncthreads();
-    }
 }
 
 // x = origin + (hi + lo), v = velf: the FP64 view of the float master.
@@ -1016,13 +958,6 @@ void launch_update_d(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSe
     prof_begin(L, "k_update_d");
     k_update_d<<<B.nuatom / QG_UBLK, QG_UBLK, 0, L.stream>>>(S, B.uatom, B.ucon, B.ublk_water, e, ekin_only, fin, rec,
                                                              rec_cap);
-    prof_end(L);
-    (*L.nlaunch)++;
-}
-void launch_water_order(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
-    if (!B.nwrange || !QG_UPD_SORT) return;
-    prof_begin(L, "k_water_order");
-    k_water_order<<<B.nwrange, 256, 0, L.stream>>>(S, B.wrange);
     prof_end(L);
     (*L.nlaunch)++;
 }

@@ -246,8 +246,6 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     std::vector<double> randva;
     std::vector<unsigned> lcg_a, lcg_c, rnd0;
     std::vector<int> uatom, ucon;
-    std::vector<int> wslot;        // per water-block slot of the fused layout: SHAKE molecule (or -1)
-    std::vector<int2> wrange;      // per trajectory with fused waters: first slot, waters
     std::vector<uint8_t> ublk_water;
     std::vector<int> ek_u0, ek_un, ek_a0, ek_an;   // Ekin block ranges of the two update layouts
     long long scr_slots = 0;
@@ -639,15 +637,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
             }
             const size_t nb_all = (uatom.size() - u0) / QG_UBLK;
             for (size_t b = 0; b < nb_all; ++b) ublk_water.push_back(b >= nb_plain ? 1 : 0);
-            // water slots of the FP64 fused step: 32 per block, initially the
-            // k-th water of the trajectory's water blocks is its molecule k
-            for (size_t b = 0; b < nb_all; ++b)
-                for (int k = 0; k < 32; ++k) {
-                    const long long q = ((long long)b - (long long)nb_plain) * 32 + k;
-                    wslot.push_back(fuse && b >= nb_plain && q < d.shake_molecules ? shk_base + (int)q : -1);
-                }
-            if (fuse && d.shake_molecules > 0)
-                wrange.push_back(make_int2((int)((u0 / QG_UBLK + nb_plain) * 32), d.shake_molecules));
+
             ek_a0.push_back((int)(u0 / QG_UBLK)); ek_an.push_back((int)nb_all);
         }
         // --- Q atoms
@@ -961,10 +951,6 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         if ((rc = upload(A, uitem, &p))) return rc; B.uitem = p; B.nuitem = (int)uitem.size();
         if ((rc = upload(A, uatom, &p))) return rc; B.uatom = p; B.nuatom = (int)uatom.size();
         if ((rc = upload(A, ucon, &p))) return rc; B.ucon = p;
-        if ((rc = upload(A, wslot, &p))) return rc; S.wslot = p;
-        if ((rc = alloc0(A, std::max<size_t>(1, shk_traj.size()), &S.msweep))) return rc;
-        int2 *p2;
-        if ((rc = upload(A, wrange, &p2))) return rc; B.wrange = p2; B.nwrange = (int)wrange.size();
         uint8_t *pb;
         if ((rc = upload(A, ublk_water, &pb))) return rc; B.ublk_water = pb;
         if ((rc = upload(A, qqblk_traj, &p))) return rc; B.qqblk_traj = p;
@@ -1140,7 +1126,6 @@ static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every, int emo
         launch_update_f(h->S, h->B, L, esel, h->NBcycle, 0, FIN_TEMP | FIN_STEP | FIN_NH, h->rec_d, h->rec_cap);
     } else if (h->fused_d) {
         launch_update_d(h->S, h->B, L, esel, 0, FIN_TEMP | FIN_STEP | FIN_NH | FIN_EK64, h->rec_d, h->rec_cap);
-        launch_water_order(h->S, h->B, L);
     } else {
         launch_integrate(h->S, h->B, L);
         launch_shake(h->S, h->B, L, -1);

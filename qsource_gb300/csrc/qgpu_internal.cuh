@@ -293,11 +293,6 @@ struct DevSys {
     float *ekin_part;               // 4 per Ekin block
     long long *ekin_fx;             // 4 per Ekin block: fixed-point (2^-32 kcal/mol) partials, FP64 step forms
     int *status;
-    // FP64-master fused step: the SHAKE molecule of every water slot of the
-    // fused layout's water blocks (reordered every step, see k_water_order),
-    // and the SHAKE sweeps of each molecule in its last step
-    int *wslot;
-    uint8_t *msweep;
 };
 
 // ------------------------------------------------------------- helpers
@@ -546,7 +541,6 @@ struct BlockTables {
     // put_back_in_box: one block per trajectory that moves molecules
     const int *pb_traj; int npb;
     int nxrblk;                        // blocks of the p_restrain items (DevSys::xr_*)
-    const int2 *wrange; int nwrange;   // per trajectory with fused waters: first water slot, waters
 };
 
 void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L);
@@ -586,8 +580,6 @@ void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSe
 // the fused step with the FP64 master (x, v, leap-frog and SHAKE in FP64)
 void launch_update_d(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e, int ekin_only, int fin = 0,
                      double *rec = nullptr, int rec_cap = 0);
-// water slots of each trajectory ordered by their last SHAKE sweeps (after k_update_d)
-void launch_water_order(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 // x = origin + hi + lo, v = velf for every atom
 void launch_sync_double(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *rec, const int *rec_base, int k,

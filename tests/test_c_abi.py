@@ -2,9 +2,10 @@
 include/qgpu.h and linked to libqgpu.so, makes qdyn's call sequence
 (qgpu_create, qgpu_build_lists, qgpu_forces, qgpu_shake, qgpu_destroy) on the
 reference's sphere test system at step 0 and checks the 12 printed columns of
-tests/basic_tests/SPH_leap-frog_berendsen_benchmark.en row 1 itself, plus the
-SHAKE tolerance on every constraint.  No Python binding is involved in the
-calls: the test only writes the descriptor file and runs the program."""
+tests/basic_tests/SPH_leap-frog_berendsen_benchmark.en row 1 itself.  Its
+SHAKE result (every atom displaced, then qgpu_shake) is compared here with
+the oracle's SHAKE of the same coordinates.  No Python binding is involved in
+the calls: the test only writes the descriptor file and runs the program."""
 import ctypes as C
 import os
 import shutil
@@ -101,8 +102,15 @@ def test_c_host_reproduces_the_golden_columns(tmp_path, golden):
     write_descriptor(g, desc)
     exe = build_program(str(tmp_path))
     want = [f"{golden['basic_sph'][c]:.2f}" for c in COLUMNS]
-    res = subprocess.run([exe, desc, *want], capture_output=True, text=True, timeout=300)
+    xout = os.path.join(str(tmp_path), "x_shaken.bin")
+    res = subprocess.run([exe, desc, xout, *want], capture_output=True, text=True, timeout=300)
     print(res.stdout)
     assert res.returncode == 0, res.stdout + res.stderr
     assert "all checks passed" in res.stdout
-    assert np.isfinite(float(res.stdout.split()[1]))
+    # the same displacement as the program's, then the oracle's SHAKE
+    xx = np.asarray(g.x, dtype=np.float64).copy()
+    k = np.arange(xx.size)
+    x = xx + 0.004 * np.sin(0.37 * k + 1.0)
+    assert o.shake(xx.copy(), x) >= 1
+    xg = np.fromfile(xout, dtype=np.float64)
+    assert np.abs(xg - x).max() < 1e-9
