@@ -101,14 +101,16 @@ def _waters(R: float, solute: np.ndarray, rng: np.random.Generator) -> np.ndarra
 def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, seed: int, *,
               solute_sigma: float = 0.3, T: float = 300.0, stepsize: float = 1.0, tau_T: float = 100.0,
               NBcycle: int = 10, Rc: float = 10.0, offdiag=None, initial_velocities: bool = True,
-              any_atom: bool = False, vdw_rule: int = 1, qvdw: bool = False) -> System:
+              any_atom: bool = False, vdw_rule: int = 1, qvdw: bool = False, q_lj_scale=(0.9, 0.5)) -> System:
     """Water sphere of radius R around a solute chain of n_solute atoms whose
     first nq atoms are Q atoms with per-state charges qcharges[nq, nstates].
 
     vdw_rule 2 gives the same LJ types in the arithmetic combination rule
     (ivdw_rule 2).  qvdw gives the Q atoms their own per-state Q types
     ([atom_types] / [change_atoms] of the FEP file): state 1 the CT type,
-    the other states a softer copy (A and B halved).
+    the other states a softer copy (sqrt(A) and sqrt(B) of the CT type scaled
+    by q_lj_scale; (0, 0) makes the Q atoms vanish from the LJ terms in those
+    states, the end-point case of a decoupling free energy).
 
     any_atom selects the any-atom cut-off for the solute charge groups
     (topology flag iuse_switch_atom = 0).  The chain's groups are 4
@@ -182,7 +184,7 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
             hard = [av[ct, 0], bv[ct, 0], av[ct, 1], bv[ct, 1], av[ct, 2], bv[ct, 2]]
         # [atom_types] rows hold the parameters as the topology does (sqrt(A), sqrt(B) per code)
         hard = [math.sqrt(v) for v in hard] if vdw_rule == 1 else hard
-        soft = [v * (0.5 if k % 2 else 0.9) for k, v in enumerate(hard)]
+        soft = [v * (q_lj_scale[1] if k % 2 else q_lj_scale[0]) for k, v in enumerate(hard)]
         atom_types = [("Qhard", hard, 12.011), ("Qsoft", soft, 12.011)]
         change_atoms = [(i + 1, ["Qhard"] + ["Qsoft"] * (S - 1)) for i in range(nq)]
     fep = {
