@@ -280,6 +280,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="MD step precision of the headline (qgpu_set_precision): FP64 master / double-float master")
     ap.add_argument("--no-mixed", action="store_true", help="skip timing the mixed-precision form")
+    ap.add_argument("--branches", type=int, default=0,
+                    help="independent trajectory groups of the replayed blocks (qgpu_set_branches; 0: library default)")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-trajectory-at-a-time GPU form")
     ap.add_argument("--plain-blocks", type=int, default=20, help="timed 10-step blocks per trajectory, plain form")
     args = ap.parse_args()
@@ -332,6 +334,8 @@ def main():
         tuning = eng.autotune() if not args.no_tune else None
     from qsource_gb300.abi import PRECISION
     eng.set_precision(PRECISION[args.precision])
+    if args.branches:
+        eng.set_branches(args.branches)
     eng.enqueue(warm, 0)
     eng.sync()
 
@@ -446,6 +450,7 @@ def main():
                    "timed": f"{nblk} blocks of {NB} steps, each one CUDA-graph replay",
                    "l2": "flushed before every timed 10-step block (256 MB write on the engine stream)",
                    "parallelism": "replicas" if world > 1 else "single GPU, one handle",
+                   "graph_branches": eng.branches(),
                    "precision": args.precision,
                    "launch_shapes": ({"lanes_water": tuning[0], "min_blocks_water": tuning[1],
                                       "lanes_solute": tuning[2], "lanes_qw": tuning[3], "unroll_water": tuning[4]}

@@ -370,6 +370,18 @@ int qgpu_set_step(qgpu_handle *h, int64_t istep);
      trajectory's constraints are 3-site waters, else the FP64 form runs.
    Pair terms are FP32 with int64 fixed-point sums in every mode.  Switching
    keeps the current coordinates and velocities. */
+/* Concurrency of a batch's replayed 10-step blocks (qgpu_run /
+   qgpu_enqueue with the fused step forms): the trajectories are split into n
+   groups of consecutive trajectories with about equal atom counts (1 <= n <=
+   4, at most the trajectory count; default 4), and each group's list build
+   and steps form an independent branch of the block's CUDA graph, so that one
+   group's FP64 update (FP64-unit bound) runs beside another group's force
+   kernels (FP32 and memory bound).  Results do not depend on n: every
+   trajectory's arithmetic is the same.  qgpu_get_branches returns the number
+   of groups in use. */
+int qgpu_set_branches(qgpu_handle *h, int32_t n);
+int qgpu_get_branches(const qgpu_handle *h);
+
 #define QGPU_PRECISION_MIXED 0
 #define QGPU_PRECISION_FP64  1
 #define QGPU_PRECISION_FP64_UNFUSED 2

@@ -173,6 +173,8 @@ EXPORTS = {
     "qgpu_profile": (_i32, [C.c_void_p, _i32, C.c_char_p, _P, _P, _i32, C.POINTER(_i32)]),
     "qgpu_fp32_peak": (_i32, [C.POINTER(_f64)]),
     "qgpu_fp64_peak": (_i32, [C.POINTER(_f64)]),
+    "qgpu_set_branches": (_i32, [C.c_void_p, _i32]),
+    "qgpu_get_branches": (_i32, [C.c_void_p]),
     "qgpu_shake_counts": (_i32, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "qgpu_lrf_scan_static": (_i32, [_i32, _P, _P, _P, _P, _P, _P, C.POINTER(_f64), _f64, _f64, _f64, _f64,
                                     _P, _P, _P]),

@@ -52,9 +52,10 @@ __global__ void k_wrec(DevSys S, const int *wgrp, int n) {
 
 // cgp_centers, src/md.f90:2253-2288: mean of the member coordinates (FP64),
 // and its float offset from the trajectory origin for the per-step kernels.
-__global__ void k_centers(DevSys S) {
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= S.ngrp) return;
+__global__ void k_centers(DevSys S, int gb, int gn) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= gn) return;
+    const int g = gb + k;
     double c0 = 0, c1 = 0, c2 = 0;
     int a0 = S.g_start[g], a1 = S.g_start[g + 1];
     for (int k = a0; k < a1; ++k) {
@@ -327,10 +328,11 @@ __global__ void __launch_bounds__(QG_BLOCK, QG_SCAN_MINB) k_scan(DevSys S, const
 // lanes copy the chunks' near-group segments into the neighbour list (water
 // entries of every chunk first, then solute entries) -- and lane 0 forms the
 // symmetric Taylor coefficients.  No FP64: this runs over every group.
-__global__ void k_scan_reduce(DevSys S) {
-    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void k_scan_reduce(DevSys S, int gb, int gn) {
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (t >= S.ngrp) return;
+    if (k >= gn) return;
+    const int t = gb + k;
     const TrajInfo &T = S.traj[S.g_traj[t]];
     const bool ex = S.g_excl[t];
     const int cap = S.nb_cap;
@@ -438,9 +440,10 @@ __global__ void k_scan_reduce(DevSys S) {
 // Q-atom list membership (nbqplist src/md.f90:10215-10322, nbqwlist
 // :10464-10549): waters whose O and solute groups whose switch atom lie within
 // Rcq of the solute centre.  Built once when Rcq > rexcl_o, as the reference.
-__global__ void k_qmember(DevSys S, int first) {
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= S.ngrp) return;
+__global__ void k_qmember(DevSys S, int first, int gb, int gn) {
+    const int kk = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kk >= gn) return;
+    const int g = gb + kk;
     const TrajInfo &T = S.traj[S.g_traj[g]];
     if (!first && T.q_static) return;
     if (T.nqat == 0) return;
@@ -587,7 +590,7 @@ void launch_mirror(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
 }
 void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
     prof_begin(L, "k_centers");
-    k_centers<<<nblk(S.ngrp, 256), 256, 0, L.stream>>>(S);
+    k_centers<<<nblk(B.ng, 256), 256, 0, L.stream>>>(S, B.g0, B.ng);
     prof_end(L);
     (*L.nlaunch)++;
 }
@@ -603,13 +606,13 @@ void launch_scan(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
     prof_end(L);
     (*L.nlaunch)++;
     prof_begin(L, "k_scan_reduce");
-    k_scan_reduce<<<nblk(S.ngrp * 32, 128), 128, 0, L.stream>>>(S);
+    k_scan_reduce<<<nblk(B.ng * 32, 128), 128, 0, L.stream>>>(S, B.g0, B.ng);
     prof_end(L);
     (*L.nlaunch)++;
 }
 void launch_qmember(const DevSys &S, const BlockTables &B, LaunchCtx &L, int first) {
     prof_begin(L, "k_qmember");
-    k_qmember<<<nblk(S.ngrp, 256), 256, 0, L.stream>>>(S, first);
+    k_qmember<<<nblk(B.ng, 256), 256, 0, L.stream>>>(S, first, B.g0, B.ng);
     prof_end(L);
     (*L.nlaunch)++;
 }

@@ -245,7 +245,7 @@ __device__ void finalize_traj(const DevSys &S, int tr, int lane, double *v, int 
 // record), run by the last block of each trajectory (0: none)
 __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom, const int *ucon,
                                                       const uint8_t *ublk_water, EaccSel esel, int nbcycle,
-                                                      int ekin_only, int fin, double *rec, int rec_cap) {
+                                                      int ekin_only, int fin, double *rec, int rec_cap, int ekb0) {
     __shared__ float4 s_h[QG_UBLK], s_l[QG_UBLK];
     __shared__ float s_D[3][QG_UBLK];
     __shared__ float s_w[QG_UBLK];
@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(QG_UBLK) k_update_f(DevSys S, const int *uatom
     if (t < 4) {
         float s = 0.f;
         for (int w = 0; w < QG_UBLK / 32; ++w) s += red[t][w];
-        S.ekin_part[(size_t)blockIdx.x * 4 + t] = s;
+        S.ekin_part[((size_t)blockIdx.x + ekb0) * 4 + t] = s;
         __threadfence();
     }
     if (!fin) return;
@@ -521,7 +521,8 @@ __device__ int shake_water_d(double (&x)[3][3], const double (&xx)[3][3], const 
 // warp's (its FP64 instructions cost the same for any number of active lanes).
 __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, const int *uatom, const int *ucon,
                                                                      const uint8_t *ublk_water, EaccSel esel,
-                                                                     int ekin_only, int fin, double *rec, int rec_cap) {
+                                                                     int ekin_only, int fin, double *rec, int rec_cap,
+                                                                     int ekb0) {
     __shared__ double s_x[3][QG_UBLK], s_xx[3][QG_UBLK];
     __shared__ float4 s_h[QG_UBLK], s_l[QG_UBLK];
     __shared__ long long red[4][QG_UBLK / 32];
@@ -659,7 +660,7 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
     if (t < 4) {
         long long sum = 0;
         for (int w = 0; w < QG_UBLK / 32; ++w) sum += red[t][w];
-        S.ekin_fx[(size_t)blockIdx.x * 4 + t] = sum;
+        S.ekin_fx[((size_t)blockIdx.x + ekb0) * 4 + t] = sum;
         __threadfence();
     }
     if (!fin) return;
@@ -949,7 +950,7 @@ void launch_update_f(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSe
                      int fin, double *rec, int rec_cap) {
     prof_begin(L, "k_update_f");
     k_update_f<<<B.nuatom / QG_UBLK, QG_UBLK, 0, L.stream>>>(S, B.uatom, B.ucon, B.ublk_water, e, nbcycle, ekin_only,
-                                                             fin, rec, rec_cap);
+                                                             fin, rec, rec_cap, B.ublk0);
     prof_end(L);
     (*L.nlaunch)++;
 }
@@ -957,7 +958,7 @@ void launch_update_d(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSe
                      double *rec, int rec_cap) {
     prof_begin(L, "k_update_d");
     k_update_d<<<B.nuatom / QG_UBLK, QG_UBLK, 0, L.stream>>>(S, B.uatom, B.ucon, B.ublk_water, e, ekin_only, fin, rec,
-                                                             rec_cap);
+                                                             rec_cap, B.ublk0);
     prof_end(L);
     (*L.nlaunch)++;
 }

@@ -307,11 +307,12 @@ __device__ __forceinline__ void apply_dp(const DevSys &S, const int *at, R dv, c
 // qbond/qangle/qtorsion/qimproper (src/md.f90:17022-17538) without EVB
 // angle/torsion couplings.  One thread per (term, state).
 template <typename R>
-__device__ void qbonded_block(const DevSys &S, int b) {
+__device__ void qbonded_block(const DevSys &S, int b, int qt0, int nqt) {
     typedef P<R> p;
     const int id = b * blockDim.x + threadIdx.x;
-    const int term = id / QG_MAXS, s = id % QG_MAXS;
-    if (term >= S.nqt) return;
+    const int s = id % QG_MAXS;
+    if (id / QG_MAXS >= nqt) return;
+    const int term = qt0 + id / QG_MAXS;
     const int traj = S.qt_traj[term];
     const TrajInfo &T = S.traj[traj];
     if (s >= T.nstates) return;
@@ -715,9 +716,10 @@ __device__ void xrst_block(const DevSys &S, int b, Red &red) {
 
 // offdiag, src/md.f90:15444-15470: Hij = A exp(-mu r_kl).  Its only consumer is
 // the energy record, so it runs on the FP64 (recorded / drop-in) evaluations.
-__device__ void offdiag_block(const DevSys &S, int blk) {
-    const int k = blk * blockDim.x + threadIdx.x;
-    if (k >= S.nod) return;
+__device__ void offdiag_block(const DevSys &S, int blk, int od0, int nod) {
+    const int kk = blk * blockDim.x + threadIdx.x;
+    if (kk >= nod) return;
+    const int k = od0 + kk;
     const int traj = S.od_traj[k];
     const int a = S.q_atom[S.od_kl[2 * k]], b = S.q_atom[S.od_kl[2 * k + 1]];
     const V3<double> d = rel<double>(S, a, b);
@@ -731,6 +733,10 @@ __device__ void offdiag_block(const DevSys &S, int blk) {
 // The small terms share one launch: consecutive block ranges select the term.
 struct MiscPlan {
     int nqq, nbt, nfix, nrad, nqb, nod, nrs, nxr;    // blocks per term
+    // the tables' part of the batch (BlockTables ranges): first classical
+    // bonded block, Q bonded terms [qt0, qt0 + nqt), off-diagonal items
+    // [od0, od0 + nodi), first sequence restraint, first p_restrain block
+    int bt0, qt0, nqt, od0, nodi, rs0, xr0;
 };
 
 template <typename R>
@@ -739,19 +745,19 @@ __device__ __forceinline__ void misc_body(const DevSys &S, const MiscPlan &P, co
     int b = blockIdx.x;
     if (b < P.nqq) { qq_block<R>(S, b, qq_traj, qq_s, red); return; }
     b -= P.nqq;
-    if (b < P.nbt) { bonded_block<R>(S, b, red); return; }
+    if (b < P.nbt) { bonded_block<R>(S, b + P.bt0, red); return; }
     b -= P.nbt;
     if (b < P.nfix) { fix_shell_block<R>(S, b, satom, red); return; }
     b -= P.nfix;
     if (b < P.nrad) { restrain_solvent_block<R>(S, b, wgrp, red); return; }
     b -= P.nrad;
-    if (b < P.nqb) { qbonded_block<R>(S, b); return; }
+    if (b < P.nqb) { qbonded_block<R>(S, b, P.qt0, P.nqt); return; }
     b -= P.nqb;
-    if (b < P.nrs) { seqrst_block<R>(S, b, red); return; }
+    if (b < P.nrs) { seqrst_block<R>(S, b + P.rs0, red); return; }
     b -= P.nrs;
-    if (b < P.nxr) { xrst_block<R>(S, b, red); return; }
+    if (b < P.nxr) { xrst_block<R>(S, b + P.xr0, red); return; }
     b -= P.nxr;
-    if (sizeof(R) == 8 && b < P.nod) offdiag_block(S, b);
+    if (sizeof(R) == 8 && b < P.nod) offdiag_block(S, b, P.od0, P.nodi);
 }
 
 __global__ void __launch_bounds__(QG_BLOCK) k_misc(DevSys S, MiscPlan P, const int *qq_traj, const int *qq_s,
@@ -768,12 +774,13 @@ static inline int nblk(int n, int b) { return (n + b - 1) / b; }
 void launch_misc(const DevSys &S, const BlockTables &B, LaunchCtx &L, int terms, EaccSel e) {
     MiscPlan P{};
     P.nqq = (terms & QGPU_TERMS_QQ) ? B.nqqblk : 0;
-    P.nbt = (terms & QGPU_TERMS_BONDED) ? S.nbt / QG_BLOCK : 0;
+    P.nbt = (terms & QGPU_TERMS_BONDED) ? B.nbtblk : 0;
     P.nfix = (terms & QGPU_TERMS_RESTRAINT) ? B.nsatom / QG_BLOCK : 0;
     P.nrad = (terms & QGPU_TERMS_RESTRAINT) ? B.nwgrp / QG_BLOCK : 0;
-    P.nqb = (terms & QGPU_TERMS_QBONDED) ? nblk(S.nqt * QG_MAXS, QG_BLOCK) : 0;
-    P.nod = nblk(S.nod, QG_BLOCK);
-    P.nrs = (terms & QGPU_TERMS_RESTRAINT) ? S.nrs : 0;
+    P.nqb = (terms & QGPU_TERMS_QBONDED) ? nblk(B.nqt * QG_MAXS, QG_BLOCK) : 0;
+    P.nod = nblk(B.nod, QG_BLOCK);
+    P.nrs = (terms & QGPU_TERMS_RESTRAINT) ? B.nrs : 0;
+    P.bt0 = B.bt0; P.qt0 = B.qt0; P.nqt = B.nqt; P.od0 = B.od0; P.nodi = B.nod; P.rs0 = B.rs0; P.xr0 = B.xr0;
     P.nxr = (terms & QGPU_TERMS_RESTRAINT) ? B.nxrblk : 0;
     const int nb = P.nqq + P.nbt + P.nfix + P.nrad + P.nqb + P.nod + P.nrs + P.nxr;
     if (!nb) return;

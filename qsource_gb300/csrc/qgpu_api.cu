@@ -83,6 +83,19 @@ struct qgpu_handle {
     // one another (each adds into the fixed-point gradient and energies)
     cudaStream_t side[QG_NSIDE] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[QG_NSIDE] = {};
+    // Independent branches of the replayed block: groups of consecutive
+    // trajectories, each with its own tables view, stream, side streams and
+    // events (branch 0..nbranch-1; nbranch 1 = the whole batch on `stream`).
+    int nbranch = 1;
+    std::vector<BlockTables> Bg;
+    cudaStream_t bstream[QG_MAXBRANCH] = {}, bside[QG_MAXBRANCH][QG_NSIDE] = {};
+    cudaEvent_t bfork[QG_MAXBRANCH] = {}, bjoin[QG_MAXBRANCH][QG_NSIDE] = {}, bdone[QG_MAXBRANCH] = {};
+    cudaEvent_t ev_branch = nullptr;
+    // first index of every per-trajectory list, per trajectory (ntraj + 1 rows)
+    struct ListStarts {
+        int wgrp, satom, scan, ublk, qqblk, wp, pb, bt, qt, od, rs, xr, grp;
+    };
+    std::vector<ListStarts> lstart;
     long long nlaunch = 0;
     int NBcycle = 10;
     int lists_built = 0, temp_init = 0, any_shake = 0, any_wpol = 0;
@@ -199,6 +212,45 @@ static void set_ekin_layout(qgpu_handle *h) {
         if (h->all_fused || h->fused_d) { T.ekin_blk0 = h->ek_a0[t]; T.ekin_nblk = h->ek_an[t]; }
         else { T.ekin_blk0 = h->ek_u0[t]; T.ekin_nblk = h->ek_un[t]; }
     }
+}
+
+// The replayed block's branches: n groups of consecutive trajectories with
+// about equal atom counts, each a view of the handle's tables (pointers into
+// the group's part of every per-trajectory list, and its ranges).
+static void make_branches(qgpu_handle *h, int n) {
+    n = std::max(1, std::min(std::min(n, QG_MAXBRANCH), h->ntraj));
+    h->Bg.clear();
+    h->nbranch = 1;
+    if (n == 1 || h->lstart.empty()) return;
+    long long tot = 0, acc = 0;
+    for (int t = 0; t < h->ntraj; ++t) tot += h->natom[t];
+    std::vector<int> cut{0};
+    for (int t = 0; t + 1 < h->ntraj && (int)cut.size() < n; ++t) {
+        acc += h->natom[t];
+        if (acc * n >= tot * (long long)cut.size()) cut.push_back(t + 1);
+    }
+    cut.push_back(h->ntraj);
+    const BlockTables &B = h->B;
+    for (size_t g = 0; g + 1 < cut.size(); ++g) {
+        const qgpu_handle::ListStarts &a = h->lstart[cut[g]], &b = h->lstart[cut[g + 1]];
+        BlockTables V = B;
+        V.wgrp = B.wgrp + a.wgrp; V.nwgrp = b.wgrp - a.wgrp;
+        V.satom = B.satom + a.satom; V.nsatom = b.satom - a.satom;
+        V.scan_t0 = B.scan_t0 + a.scan; V.scan_tn = B.scan_tn + a.scan; V.scan_traj = B.scan_traj + a.scan;
+        V.scan_chunk = B.scan_chunk + a.scan; V.nscan = b.scan - a.scan;
+        V.uatom = B.uatom + (size_t)a.ublk * QG_UBLK; V.ucon = B.ucon + (size_t)a.ublk * QG_UBLK;
+        V.ublk_water = B.ublk_water + a.ublk; V.nuatom = (b.ublk - a.ublk) * QG_UBLK; V.ublk0 = a.ublk;
+        V.qqblk_traj = B.qqblk_traj + a.qqblk; V.qqblk_s = B.qqblk_s + a.qqblk; V.nqqblk = b.qqblk - a.qqblk;
+        if (B.nwp) { V.wp_traj = B.wp_traj + a.wp; V.wp_scr0 = B.wp_scr0 + a.wp; }
+        V.nwp = b.wp - a.wp;
+        if (B.npb) V.pb_traj = B.pb_traj + a.pb;
+        V.npb = b.pb - a.pb;
+        V.g0 = a.grp; V.ng = b.grp - a.grp;
+        V.qt0 = a.qt; V.nqt = b.qt - a.qt; V.od0 = a.od; V.nod = b.od - a.od;
+        V.bt0 = a.bt; V.nbtblk = b.bt - a.bt; V.rs0 = a.rs; V.nrs = b.rs - a.rs; V.xr0 = a.xr; V.nxrblk = b.xr - a.xr;
+        h->Bg.push_back(V);
+    }
+    h->nbranch = (int)h->Bg.size();
 }
 
 static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h) {
@@ -963,6 +1015,29 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
             return fail(QGPU_E_UNSUPPORTED, "a batch cannot mix any-atom lists and periodic boxes");
         B.npb = (int)pb_traj.size();
         B.nxrblk = (int)xr_blk_traj.size();
+        // the whole batch
+        B.g0 = 0; B.ng = S.ngrp; B.ublk0 = 0; B.qt0 = 0; B.nqt = S.nqt; B.od0 = 0; B.nod = S.nod;
+        B.bt0 = 0; B.nbtblk = S.nbt / QG_BLOCK; B.rs0 = 0; B.nrs = S.nrs; B.xr0 = 0;
+        // where each trajectory's part of every list starts (lists are in
+        // trajectory order; padding entries carry -1 - trajectory)
+        {
+            auto first_at = [&](const std::vector<int> &tr, int t) {
+                return (int)(std::lower_bound(tr.begin(), tr.end(), t) - tr.begin());
+            };
+            std::vector<int> tw, ts, tq;
+            for (int e : wgrp) tw.push_back(e >= 0 ? g_traj[e] : -1 - e);
+            for (int e : satom) ts.push_back(e >= 0 ? atraj[e] : -1 - e);
+            h->lstart.resize(ntraj + 1);
+            for (int t = 0; t <= ntraj; ++t) {
+                qgpu_handle::ListStarts &L = h->lstart[t];
+                L.wgrp = first_at(tw, t); L.satom = first_at(ts, t); L.scan = first_at(scan_traj, t);
+                L.ublk = t < ntraj ? ek_a0[t] : (int)(uatom.size() / QG_UBLK);
+                L.qqblk = first_at(qqblk_traj, t); L.wp = first_at(wp_traj, t); L.pb = first_at(pb_traj, t);
+                L.bt = first_at(bt_blk_traj, t); L.qt = first_at(qt_traj, t); L.od = first_at(od_traj, t);
+                L.rs = first_at(rs_traj, t); L.xr = first_at(xr_blk_traj, t);
+                L.grp = t < ntraj ? h->info[t].grp0 : S.ngrp;
+            }
+        }
         if (B.npb) {
             int *p_;
             if ((rc = upload(A, pb_traj, &p_))) return rc; B.pb_traj = p_;
@@ -982,6 +1057,17 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     if ((rc = alloc0(A, 2, &h->recctl_d))) return rc;
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&h->ev_branch, cudaEventDisableTiming));
+    make_branches(h, QG_MAXBRANCH);
+    for (int g = 0; g < QG_MAXBRANCH; ++g) {
+        CK(cudaStreamCreateWithFlags(&h->bstream[g], cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&h->bfork[g], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&h->bdone[g], cudaEventDisableTiming));
+        for (int k = 0; k < QG_NSIDE; ++k) {
+            CK(cudaStreamCreateWithFlags(&h->bside[g][k], cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&h->bjoin[g][k], cudaEventDisableTiming));
+        }
+    }
     for (int k = 0; k < QG_NSIDE; ++k) {
         CK(cudaStreamCreateWithFlags(&h->side[k], cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&h->ev_join[k], cudaEventDisableTiming));
@@ -1029,12 +1115,13 @@ static void temperature_init(qgpu_handle *h, LaunchCtx &L) {
 
 // md: a list build of the MD loop, which first puts molecules back in the box
 // (md_run :6483-6485); qgpu_build_lists alone is make_pair_lists.
-static void list_ops(qgpu_handle *h, LaunchCtx &L, bool md = true) {
-    if (md) launch_put_back(h->S, h->B, L);
-    launch_centers(h->S, h->B, L);
-    launch_scan(h->S, h->B, L);
-    launch_qmember(h->S, h->B, L, h->lists_built ? 0 : 1);
+static void list_ops(qgpu_handle *h, const BlockTables &B, LaunchCtx &L, bool md = true) {
+    if (md) launch_put_back(h->S, B, L);
+    launch_centers(h->S, B, L);
+    launch_scan(h->S, B, L);
+    launch_qmember(h->S, B, L, h->lists_built ? 0 : 1);
 }
+static void list_ops(qgpu_handle *h, LaunchCtx &L, bool md = true) { list_ops(h, h->B, L, md); }
 
 // fp64_energy: every pair energy in FP64 (drop-in call); otherwise FP32 pair
 // energies, with FP64 Q-atom energies on recorded steps (esel).
@@ -1043,41 +1130,53 @@ static void list_ops(qgpu_handle *h, LaunchCtx &L, bool md = true) {
 // does not depend on their order): they run concurrently on side streams that
 // fork from and join back into the handle's stream (also inside graph
 // capture).  The per-kernel profiler keeps them in one stream.
-static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, int emode, EaccSel esel) {
+// The stream set a force stage forks onto: a fork event, side streams and
+// their join events (the handle's own, or one branch's).
+struct SideSet {
+    cudaEvent_t fork;
+    const cudaStream_t *side;
+    const cudaEvent_t *join;
+};
+static void force_ops(qgpu_handle *h, const BlockTables &B, LaunchCtx &L, int terms, int emode, EaccSel esel,
+                      SideSet ss) {
     const bool wpol = (terms & QGPU_TERMS_RESTRAINT) != 0;
     if (!(terms & QGPU_TERMS_NONBOND)) {
-        launch_misc(h->S, h->B, L, terms, esel);
-        if (wpol) launch_watpol(h->S, h->B, L, esel);
+        launch_misc(h->S, B, L, terms, esel);
+        if (wpol) launch_watpol(h->S, B, L, esel);
         return;
     }
-    if (L.prof || !h->ev_fork) {
-        launch_nb_water(h->S, h->B, L, 1, emode);
-        launch_nb_solute(h->S, h->B, L, 1, emode);
-        launch_qw(h->S, h->B, L, esel, emode);
-        launch_qp(h->S, h->B, L, esel, emode);
-        launch_misc(h->S, h->B, L, terms, esel);
-        if (wpol) launch_watpol(h->S, h->B, L, esel);
+    if (L.prof || !ss.fork) {
+        launch_nb_water(h->S, B, L, 1, emode);
+        launch_nb_solute(h->S, B, L, 1, emode);
+        launch_qw(h->S, B, L, esel, emode);
+        launch_qp(h->S, B, L, esel, emode);
+        launch_misc(h->S, B, L, terms, esel);
+        if (wpol) launch_watpol(h->S, B, L, esel);
         return;
     }
-    cudaEventRecord(h->ev_fork, L.stream);
+    cudaEventRecord(ss.fork, L.stream);
     LaunchCtx Ls[QG_NSIDE];
     for (int k = 0; k < QG_NSIDE; ++k) {
-        cudaStreamWaitEvent(h->side[k], h->ev_fork, 0);
-        Ls[k] = LaunchCtx{h->side[k], L.nlaunch};
+        cudaStreamWaitEvent(ss.side[k], ss.fork, 0);
+        Ls[k] = LaunchCtx{ss.side[k], L.nlaunch};
     }
-    launch_nb_water(h->S, h->B, L, 1, emode);
-    launch_nb_solute(h->S, h->B, Ls[0], 1, emode);
-    launch_qw(h->S, h->B, Ls[1], esel, emode);
-    launch_qp(h->S, h->B, Ls[2], esel, emode);
-    launch_misc(h->S, h->B, Ls[2], terms, esel);
-    if (wpol) launch_watpol(h->S, h->B, Ls[1], esel);
+    launch_nb_water(h->S, B, L, 1, emode);
+    launch_nb_solute(h->S, B, Ls[0], 1, emode);
+    launch_qw(h->S, B, Ls[1], esel, emode);
+    launch_qp(h->S, B, Ls[2], esel, emode);
+    launch_misc(h->S, B, Ls[2], terms, esel);
+    if (wpol) launch_watpol(h->S, B, Ls[1], esel);
     for (int k = 0; k < QG_NSIDE; ++k) {
-        cudaEventRecord(h->ev_join[k], h->side[k]);
-        cudaStreamWaitEvent(L.stream, h->ev_join[k], 0);
+        cudaEventRecord(ss.join[k], ss.side[k]);
+        cudaStreamWaitEvent(L.stream, ss.join[k], 0);
     }
+}
+static void force_ops(qgpu_handle *h, LaunchCtx &L, int terms, int emode, EaccSel esel) {
+    force_ops(h, h->B, L, terms, emode, esel, SideSet{h->ev_fork, h->side, h->ev_join});
 }
 
 static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every, int emode);
+static void step_ops(qgpu_handle *h, const BlockTables &B, LaunchCtx &L, SideSet ss, int k, int ene_every, int emode);
 // Pair-energy mode of an MD step: its pair energies are read only when the
 // step is recorded (step % ene_every == 0).
 static int step_emode(long long step, int ene_every) {
@@ -1093,16 +1192,35 @@ static int replay_block(qgpu_handle *h, LaunchCtx &L, int ene_every) {
         cudaGraph_t g;
         long long before = h->nlaunch;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        list_ops(h, L);
         // a replayed block starts at a multiple of NB: where ene_every divides
         // NB the recorded steps of the block are fixed; where NB divides
         // ene_every only the block's first step can be recorded; elsewhere the
         // pair kernels keep their energies on every step
-        for (int k = 0; k < NB; ++k) {
+        auto emode_of = [&](int k) {
             int em = QG_PAIR_E_FP32;
             if (NB % ene_every == 0) em = step_emode(k, ene_every);
             else if (ene_every % NB == 0) em = k == 0 ? QG_PAIR_E_FP32 : QG_PAIR_E_NONE;
-            step_ops(h, L, k, ene_every, em);
+            return em;
+        };
+        if (h->nbranch > 1 && (h->all_fused || h->fused_d)) {
+            // the trajectory groups are independent for the whole block: one
+            // branch each (list build and NB steps), joined before the tick,
+            // so that one group's FP64 update overlaps another's force kernels
+            cudaEventRecord(h->ev_branch, h->stream);
+            for (int g = 0; g < h->nbranch; ++g) {
+                BlockTables &V = h->Bg[g];
+                V.tune = h->B.tune;
+                cudaStreamWaitEvent(h->bstream[g], h->ev_branch, 0);
+                LaunchCtx Lg{h->bstream[g], L.nlaunch};
+                const SideSet ss{h->bfork[g], h->bside[g], h->bjoin[g]};
+                list_ops(h, V, Lg);
+                for (int k = 0; k < NB; ++k) step_ops(h, V, Lg, ss, k, ene_every, emode_of(k));
+                cudaEventRecord(h->bdone[g], h->bstream[g]);
+                cudaStreamWaitEvent(h->stream, h->bdone[g], 0);
+            }
+        } else {
+            list_ops(h, L);
+            for (int k = 0; k < NB; ++k) step_ops(h, L, k, ene_every, emode_of(k));
         }
         launch_tick(L, h->recctl_d, NB);
         CK(cudaStreamEndCapture(h->stream, &g));
@@ -1116,6 +1234,17 @@ static int replay_block(qgpu_handle *h, LaunchCtx &L, int ene_every) {
     h->nlaunch += h->graph_nodes;
     h->step += NB;
     return 0;
+}
+
+// one MD step of the trajectories of tables B on L's stream (fused forms);
+// the separate-kernel forms always run the whole batch
+static void step_ops(qgpu_handle *h, const BlockTables &B, LaunchCtx &L, SideSet ss, int k, int ene_every, int emode) {
+    EaccSel esel{EACC_RECORD, h->recctl_d, k, ene_every};
+    force_ops(h, B, L, QGPU_TERMS_ALL, emode, esel, ss);
+    if (h->all_fused)
+        launch_update_f(h->S, B, L, esel, h->NBcycle, 0, FIN_TEMP | FIN_STEP | FIN_NH, h->rec_d, h->rec_cap);
+    else
+        launch_update_d(h->S, B, L, esel, 0, FIN_TEMP | FIN_STEP | FIN_NH | FIN_EK64, h->rec_d, h->rec_cap);
 }
 
 static void step_ops(qgpu_handle *h, LaunchCtx &L, int k, int ene_every, int emode) {
@@ -1167,6 +1296,16 @@ int qgpu_destroy(qgpu_handle *h) {
         if (h->ev_join[k]) cudaEventDestroy(h->ev_join[k]);
     }
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_branch) cudaEventDestroy(h->ev_branch);
+    for (int g = 0; g < QG_MAXBRANCH; ++g) {
+        if (h->bstream[g]) { cudaStreamSynchronize(h->bstream[g]); cudaStreamDestroy(h->bstream[g]); }
+        if (h->bfork[g]) cudaEventDestroy(h->bfork[g]);
+        if (h->bdone[g]) cudaEventDestroy(h->bdone[g]);
+        for (int k = 0; k < QG_NSIDE; ++k) {
+            if (h->bside[g][k]) { cudaStreamSynchronize(h->bside[g][k]); cudaStreamDestroy(h->bside[g][k]); }
+            if (h->bjoin[g][k]) cudaEventDestroy(h->bjoin[g][k]);
+        }
+    }
     for (FILE *f : h->ene_files)
         if (f) fclose(f);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -1648,6 +1787,16 @@ int qgpu_set_step(qgpu_handle *h, int64_t istep) {
     CK(cudaStreamSynchronize(h->stream));
     return 0;
 }
+
+int qgpu_set_branches(qgpu_handle *h, int32_t n) {
+    if (!h || n < 1 || n > QG_MAXBRANCH) return fail(QGPU_E_INVALID, "qgpu_set_branches: n must be 1..%d", QG_MAXBRANCH);
+    CK(cudaStreamSynchronize(h->stream));
+    make_branches(h, n);
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    return 0;
+}
+
+int qgpu_get_branches(const qgpu_handle *h) { return h ? h->nbranch : 0; }
 
 int qgpu_set_precision(qgpu_handle *h, int32_t mode) {
     if (!h || (mode != QGPU_PRECISION_MIXED && mode != QGPU_PRECISION_FP64 && mode != QGPU_PRECISION_FP64_UNFUSED))

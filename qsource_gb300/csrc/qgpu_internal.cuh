@@ -16,6 +16,7 @@
 #define QG_UBLK 96              // threads per block of the fused update (32 waters)
 #define QG_LW 8                 // lanes that share one target in the pair kernels
 #define QG_NSIDE 3              // side streams of the concurrent force kernels
+#define QG_MAXBRANCH 4          // independent trajectory groups of a replayed block
 #define QG_TREG 4               // target-group atoms held in registers by the any-atom scan test
 #define QG_MAXSHELL 8           // water polarisation shells per trajectory
 #define QG_MAXNH 16             // Nose-Hoover chain length
@@ -541,6 +542,15 @@ struct BlockTables {
     // put_back_in_box: one block per trajectory that moves molecules
     const int *pb_traj; int npb;
     int nxrblk;                        // blocks of the p_restrain items (DevSys::xr_*)
+    // The trajectories a set of tables covers: the whole batch, or one group
+    // of consecutive trajectories whose kernels run as an independent branch
+    // of the replayed graph (the list pointers above then point into the
+    // group's part of each list).  Charge groups [g0, g0 + ng); the first
+    // fused-update block (Ekin slot base); Q bonded terms [qt0, qt0 + nqt);
+    // off-diagonal items [od0, od0 + nod); classical bonded blocks from bt0;
+    // sequence restraints from rs0; p_restrain item blocks from xr0.
+    int g0 = 0, ng = 0, ublk0 = 0, qt0 = 0, nqt = 0, od0 = 0, nod = 0, bt0 = 0, nbtblk = 0, rs0 = 0, nrs = 0,
+        xr0 = 0;
 };
 
 void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L);

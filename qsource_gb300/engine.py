@@ -180,6 +180,13 @@ class Engine:
     def set_step(self, istep: int):
         self._check(self.lib.qgpu_set_step(self.h, istep))
 
+    def set_branches(self, n: int):
+        """Independent trajectory groups of the replayed blocks (qgpu_set_branches)."""
+        self._check(self.lib.qgpu_set_branches(self.h, n))
+
+    def branches(self) -> int:
+        return int(self.lib.qgpu_get_branches(self.h))
+
     def set_precision(self, mode: int):
         """QGPU_PRECISION_MIXED (default) or QGPU_PRECISION_FP64 for the MD
         step (see qgpu_set_precision)."""

@@ -7,9 +7,11 @@ FP64 / int64 fixed point):
   * energies: |dE| <= 1e-5 * (sum of |terms| scale) -- see ENERGY_TOL below;
   * LRF multipoles: |d phi| <= 1e-5 * max|phi| per component family;
   * SHAKE (drop-in, FP64): 1e-9 absolute on coordinates;
-  * MD (float master state, FP32 SHAKE on unrecorded steps): recorded
-    potential and kinetic energies 1e-4 relative, coordinates 1e-4 A after
-    20 steps.
+  * MD (the FP64-master step, and the mixed form with its float master
+    state and FP32 SHAKE): recorded potential and kinetic energies 1e-4
+    relative, coordinates 1e-4 A after 20 steps;
+  * bit-identity where the arithmetic is the same: batch vs single
+    trajectory, one vs several graph branches, run to run.
 """
 from collections import Counter
 
@@ -363,6 +365,28 @@ def test_batch_equals_single(systems):
     batch.run(12)
     single.run(12)
     assert np.array_equal(batch.coords(1)[0], single.coords(0)[0])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_branches_are_bit_identical(systems, precision):
+    """The replayed blocks of a batch split into independent branches (groups
+    of consecutive trajectories, qgpu_set_branches) give bitwise the same
+    coordinates, velocities and energy records as one branch: 4 trajectories
+    of three sizes, 30 steps (three list builds, records every 5 steps)."""
+    from qsource_gb300.abi import PRECISION
+    batch = [systems["cfg1"], systems["cfg2"], systems["cfg1ar"], systems["cfg2ar"]]
+    out = []
+    for nb in (1, 4):
+        e = _engine(batch)
+        e.set_precision(PRECISION[precision])
+        e.set_branches(nb)
+        assert e.branches() == nb
+        rows = e.run(30, ene_every=5)
+        x, v = e.coords_all()
+        out.append((rows, x, v))
+    (ra, xa, va), (rb, xb, vb) = out
+    assert np.array_equal(xa, xb) and np.array_equal(va, vb)
+    assert ra == rb
 
 
 def test_shake_failure_is_reported(systems):
