@@ -372,8 +372,8 @@ int qgpu_set_step(qgpu_handle *h, int64_t istep);
    keeps the current coordinates and velocities. */
 /* Concurrency of a batch's replayed 10-step blocks (qgpu_run /
    qgpu_enqueue with the fused step forms): the trajectories are split into n
-   groups of consecutive trajectories with about equal atom counts (1 <= n <=
-   4, at most the trajectory count; default 4), and each group's list build
+   at most n groups of consecutive trajectories with about equal atom counts
+   (1 <= n <= 4; default 4), and each group's list build
    and steps form an independent branch of the block's CUDA graph, so that one
    group's FP64 update (FP64-unit bound) runs beside another group's force
    kernels (FP32 and memory bound).  Results do not depend on n: every

@@ -380,7 +380,8 @@ def test_branches_are_bit_identical(systems, precision):
         e = _engine(batch)
         e.set_precision(PRECISION[precision])
         e.set_branches(nb)
-        assert e.branches() == nb
+        # groups of about equal atom counts: at most nb of them
+        assert (e.branches() == 1) if nb == 1 else (1 < e.branches() <= nb)
         rows = e.run(30, ene_every=5)
         x, v = e.coords_all()
         out.append((rows, x, v))
