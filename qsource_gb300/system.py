@@ -31,10 +31,13 @@ class System:
 
     # ---------------------------------------------------------------- desc
     def desc(self) -> SystemDesc:
-        """Fill a qgpu_system_desc.  The numpy arrays stay owned by self."""
+        """Fill a qgpu_system_desc.  The arrays it points to are held by the
+        returned descriptor (and by self._keep until the next call), so a
+        descriptor stays valid however many others are made later."""
         d = SystemDesc()
-        keep = self._keep
-        keep.clear()
+        keep: list = []
+        self._keep = keep
+        d._keep = keep
 
         def arr(a, dt):
             if a is None:

@@ -25,3 +25,31 @@ def test_lambda_batch_members_are_the_batch():
     for i, s in enumerate(b):
         t = synth.lambda_batch_member(i, nwindows=3, replicas=2)
         assert s.natom == t.natom and np.array_equal(s.x, t.x) and np.array_equal(s.crg, t.crg)
+
+
+def test_descriptor_outlives_later_descriptors():
+    """A descriptor keeps its arrays alive when later descriptors of the same
+    system are made (an engine built after an oracle of the same system must
+    not free the oracle's arrays): every pointer of the first descriptor is
+    still the address of an array that it holds after more descriptors and a
+    collection, and the oracle built on it gives the same energies."""
+    import ctypes as C
+    import gc
+
+    from oracle.oracle import Oracle
+    from qsource_gb300 import synth
+    from qsource_gb300.abi import SystemDesc
+    s = synth.config(1)
+    o = Oracle(s)
+    o.make_pair_lists()
+    d0, E0, _ = o.pot_energy()
+    for _ in range(3):
+        s.desc()
+    gc.collect()
+    held = {a.ctypes.data for a in o._desc._keep}
+    for name, typ in SystemDesc._fields_:
+        if typ is C.c_void_p and getattr(o._desc, name):
+            assert getattr(o._desc, name) in held, name
+    o.make_pair_lists()
+    d1, E1, _ = o.pot_energy()
+    assert np.array_equal(d0, d1) and E0 == E1
