@@ -371,9 +371,9 @@ int qgpu_set_step(qgpu_handle *h, int64_t istep);
    Pair terms are FP32 with int64 fixed-point sums in every mode.  Switching
    keeps the current coordinates and velocities. */
 /* Concurrency of a batch's replayed 10-step blocks (qgpu_run /
-   qgpu_enqueue with the fused step forms): the trajectories are split into n
+   qgpu_enqueue with the fused step forms): the trajectories are split into
    at most n groups of consecutive trajectories with about equal atom counts
-   (1 <= n <= 4; default 4), and each group's list build
+   (1 <= n <= 8; default 4), and each group's list build
    and steps form an independent branch of the block's CUDA graph, so that one
    group's FP64 update (FP64-unit bound) runs beside another group's force
    kernels (FP32 and memory bound).  Results do not depend on n: every

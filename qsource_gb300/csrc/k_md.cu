@@ -435,23 +435,22 @@ __device__ __forceinline__ float d2f_bits(double r, double &rh) {
     const unsigned mag = (unsigned)((t & 0x3ffffffffull) - (896ull << 23));
     return __uint_as_float(mag | (unsigned)((b >> 63) << 31));
 }
-// hi/lo float pair of r: hi = float(r), lo = float(r - hi) (r - hi is exact)
+// hi/lo float pair of r: hi = float(r), lo = float(r - hi) (r - hi is exact;
+// it is zero exactly when hi's double has the bits of r, an integer test)
 __device__ __forceinline__ void split_hl(double r, float &h, float &l) {
     double rh, rl;
     h = d2f_bits(r, rh);
     const double d = r - rh;
-    l = d == 0.0 ? 0.f : d2f_bits(d, rl);
+    l = __double_as_longlong(r) == __double_as_longlong(rh) ? 0.f : d2f_bits(d, rl);
 }
 
-// diff / den: the PTX approximate FP64 reciprocal (a special-function unit
-// instruction) refined by two Newton-Raphson steps y <- y (2 - den y), then
-// multiplied
-__device__ __forceinline__ double div_nr(double diff, double den) {
+// 1/den: the PTX approximate FP64 reciprocal (a special-function unit
+// instruction) refined by two Newton-Raphson steps y <- y (2 - den y)
+__device__ __forceinline__ double rcp_nr(double den) {
     double y;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(den));
     y = y * (2.0 - den * y);
-    y = y * (2.0 - den * y);
-    return diff * y;
+    return y * (2.0 - den * y);
 }
 
 // SHAKE of one water in FP64 (shake, src/md.f90:17581-17679), in the
@@ -462,20 +461,30 @@ __device__ __forceinline__ double div_nr(double diff, double den) {
 // scp = xij.xxij, x_i += xxij corr winv_i, x_j -= xxij corr winv_j;
 // Gauss-Seidel over O-H1, O-H2, H1-H2; constraints that met the tolerance are
 // not revisited; at most SHAKE_MAX_ITER sweeps.  The tolerance test compares
-// the bit patterns of |diff| and the (positive) tolerance as integers.
-__device__ int shake_water_d(double (&x)[3][3], const double (&xx)[3][3], const double (&w)[3], const double (&d2)[3],
-                             bool *fail, int *visits) {
-    double xxij[3][3], den0[3];
-    long long tolb[3];
+// the bit patterns of |diff| and the (positive) tolerance as integers.  The
+// constant factors a = winv / (2 (winv_i + winv_j)) are formed once per water,
+// so a visit takes corr winv_i = (diff / scp) a_i: 23 FP64 instructions and
+// one reciprocal estimate.  Per-constraint constants (a_i, a_j, d0^2 and the
+// tolerance) live in the calling lane's column of cst (shared memory), which
+// keeps the registers for the positions.
+__device__ __forceinline__ int shake_water_d(double (&x)[3][3], const double (&xx)[3][3], const double (&w)[3],
+                                             const double (&d2)[3], double (*cst)[3][32], int lane, bool *fail,
+                                             int *visits) {
+    double xxij[3][3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const int i = c == 2 ? 1 : 0, j = c == 0 ? 1 : 2;
 #pragma unroll
         for (int a = 0; a < 3; ++a) xxij[c][a] = xx[i][a] - xx[j][a];
-        // 2 scp (w_i + w_j) = scp * (2 (w_i + w_j)) exactly (scaling by 2)
-        den0[c] = 2.0 * (w[i] + w[j]);
-        tolb[c] = __double_as_longlong(SHAKE_TOL * d2[c]);
+        const double den0 = 2.0 * (w[i] + w[j]);
+        cst[0][c][lane] = w[i] / den0;
+        cst[1][c][lane] = w[j] / den0;
+        cst[2][c][lane] = d2[c];
+        cst[3][c][lane] = SHAKE_TOL * d2[c];
     }
+    // (each lane reads back only its own column: no synchronisation)
+    // read at every visit (volatile: not hoisted into registers)
+    const volatile double (*vc)[3][32] = cst;
     unsigned ready = 0u;
     int nits = 0, nv = 0;
     for (;;) {
@@ -485,11 +494,12 @@ __device__ int shake_water_d(double (&x)[3][3], const double (&xx)[3][3], const 
             nv++;
             const int i = c == 2 ? 1 : 0, j = c == 0 ? 1 : 2;
             const double xij0 = x[i][0] - x[j][0], xij1 = x[i][1] - x[j][1], xij2 = x[i][2] - x[j][2];
-            const double diff = d2[c] - (xij0 * xij0 + xij1 * xij1 + xij2 * xij2);
-            if ((__double_as_longlong(diff) & 0x7fffffffffffffffLL) < tolb[c]) ready |= 1u << c;
+            const double diff = vc[2][c][lane] - (xij0 * xij0 + xij1 * xij1 + xij2 * xij2);
+            if ((__double_as_longlong(diff) & 0x7fffffffffffffffLL) < __double_as_longlong(vc[3][c][lane]))
+                ready |= 1u << c;
             const double scp = xij0 * xxij[c][0] + xij1 * xxij[c][1] + xij2 * xxij[c][2];
-            const double corr = div_nr(diff, scp * den0[c]);
-            const double ci = corr * w[i], cj = corr * w[j];
+            const double q = diff * rcp_nr(scp);
+            const double ci = q * vc[0][c][lane], cj = q * vc[1][c][lane];
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 x[i][a] += xxij[c][a] * ci;
@@ -526,6 +536,7 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
     __shared__ double s_x[3][QG_UBLK], s_xx[3][QG_UBLK];
     __shared__ float4 s_h[QG_UBLK], s_l[QG_UBLK];
     __shared__ long long red[4][QG_UBLK / 32];
+    __shared__ double s_cst[4][3][32];
     const int t = threadIdx.x;
     const int a = uatom[blockIdx.x * QG_UBLK + t];
     const bool water_blk = ublk_water[blockIdx.x] != 0;
@@ -547,7 +558,7 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
             const double ts = (a - T.atom0) < T.nat_solute ? TS.tsd_solute : TS.tsd_solvent;
             // gradient (fixed point, 2^-32 units) times winv dv: the 2^-32 is
             // exact, folded into dv
-            const double kq = wi * (T.dvm * (1.0 / QG_FSCALE));
+            const double kq = wi * T.dvm_q;
             double rf[3] = {0.0, 0.0, 0.0};
             if (T.thermostat == 1) langevin_force<double>(S, T, TS.rnd, a, rf);
             bool bad = false;
@@ -592,7 +603,7 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
                     ww[k] = S.winv[o + k];
                 }
                 bool failed = false;
-                nits = shake_water_d(wx, wxx, ww, d2, &failed, &nvis);
+                nits = shake_water_d(wx, wxx, ww, d2, s_cst, t, &failed, &nvis);
                 if (failed) { atomicOr(S.status, ST_SHAKE); atomicCAS(S.status + 1, 0, tr + 1); }
 #pragma unroll
                 for (int k = 0; k < 3; ++k)
@@ -606,14 +617,16 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
             if (t == 0 && nits) { atomicAdd(&S.tstate[tr].shake_iters, nits); atomicAdd(&S.tstate[tr].shake_visits, nvis); }
         }
         __syncthreads();
+        // x and xx of this thread's atom come back from shared memory, so
+        // that they (and v, formed again below) need no registers during SHAKE
         if (a >= 0)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) x[c] = s_x[c][t];
+            for (int c = 0; c < 3; ++c) { x[c] = s_x[c][t]; xo[c] = s_xx[c][t]; }
     }
     long long ek[4] = {0, 0, 0, 0};
     if (a >= 0) {
         if (!ekin_only) {
-            if (T.nshake_mol > 0) {
+            if (water_blk || T.nshake_mol > 0) {
                 const double s2 = T.thermostat == 2 ? S.tstate[tr].nh_s2 : 1.0;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
@@ -635,7 +648,8 @@ __global__ void __launch_bounds__(QG_UBLK, QG_UPD_D_MINB) k_update_d(DevSys S, c
         // 0.5 m v^2 in FP64, rounded to 2^-32 kcal/mol: integer sums from here
         const double e = (S.mass[a] * (0.5 * QG_FSCALE)) * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
         long long q = d2ll_magic(e);
-        if (!(e < 2251799813685248.0)) { atomicOr(S.status, ST_FIXED); q = 0; }   // 2^51, NaN
+        // e >= 0: below 2^51 exactly when its bits are (NaN and inf above)
+        if (__double_as_longlong(e) >= 0x4320000000000000LL) { atomicOr(S.status, ST_FIXED); q = 0; }
         const bool fr = !S.aexcl[a];
         if ((a - T.atom0) < T.nat_solute) { ek[0] = q; ek[1] = fr ? q : 0; }
         else { ek[2] = q; ek[3] = fr ? q : 0; }

@@ -446,6 +446,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         T.thermostat = d.thermostat; T.integrator = d.integrator; T.lgauss = d.langevin_gauss ? 1 : 0;
         T.dvm = d.integrator == 1 ? 0.5 * d.dt : d.dt;
         T.dvmf = (float)T.dvm;
+        T.dvm_q = T.dvm * (1.0 / QG_FSCALE);
         T.lfric = 1.0 - d.friction * T.dvm;
         T.lfricf = (float)T.lfric;
         T.kbT = 0.001986 * d.Temp0;
@@ -1058,7 +1059,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&h->ev_branch, cudaEventDisableTiming));
-    make_branches(h, QG_MAXBRANCH);
+    make_branches(h, QG_DEFBRANCH);
     for (int g = 0; g < QG_MAXBRANCH; ++g) {
         CK(cudaStreamCreateWithFlags(&h->bstream[g], cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&h->bfork[g], cudaEventDisableTiming));

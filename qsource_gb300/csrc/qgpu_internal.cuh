@@ -16,7 +16,8 @@
 #define QG_UBLK 96              // threads per block of the fused update (32 waters)
 #define QG_LW 8                 // lanes that share one target in the pair kernels
 #define QG_NSIDE 3              // side streams of the concurrent force kernels
-#define QG_MAXBRANCH 4          // independent trajectory groups of a replayed block
+#define QG_MAXBRANCH 8          // independent trajectory groups of a replayed block (at most)
+#define QG_DEFBRANCH 4          // the groups a new handle forms
 #define QG_TREG 4               // target-group atoms held in registers by the any-atom scan test
 #define QG_MAXSHELL 8           // water polarisation shells per trajectory
 #define QG_MAXNH 16             // Nose-Hoover chain length
@@ -119,6 +120,7 @@ struct TrajInfo {
     // (0 leap-frog, 1 velocity-verlet); dv_mod = dt or dt/2 (md_run :6440-6460)
     int thermostat, integrator, lgauss, nhc;
     double dvm, lfric, kbT;
+    double dvm_q;                    // dvm * 2^-32: the fixed-point gradient's unit folded in (exact)
     float dvmf, lfricf;
     unsigned long long lcgA, lcgC;   // randm stream advance of one step (3N or 36N numbers)
     double qnh[QG_MAXNH];
