@@ -318,7 +318,12 @@ __device__ __forceinline__ PairFlags pair_flags(const DevSys &S, int i, int j) {
 }
 
 // nonbond_pp (src/md.f90:13069-13155) and the solute side of nonbond_pw, plus
-// lrf_taylor, for one non-Q solute atom.
+// lrf_taylor, for one non-Q solute atom.  Per pair: LJ code c (3 = a 1-4 pair
+// with the el14 factor, nonbond_pp :13102-13111) and the periodic shift (sf,
+// sd) of the group pair (nonbond_pp_box :13226-13228).
+#ifndef QG_PPB
+#define QG_PPB 4   // solute atoms of a neighbour group loaded together
+#endif
 template <int E, int LW, bool BOX>
 __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *satom, int lrf) {
     constexpr bool EACC = E == 1;
@@ -345,42 +350,69 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
         const int swg = S.g_switch[g];
         float4 swh = {}, swl = {};
         if (pbc) { swh = S.pos[swg]; swl = S.poslo[swg]; }
-        // one pair term: LJ code c, el14 factor for 1-4 pairs (nonbond_pp :13102-13111),
-        // periodic shift (sf, sd) of the group pair (nonbond_pp_box :13226-13228)
-        auto pair = [&](int j, int c, EAcc<E> &e_el, EAcc<E> &e_vdw, const float3 sf, const double3 sd) {
-            const int tj = S.atype[j];
-            const float4 jh = S.pos[j], jl = S.poslo[j];
-            const int li = lj_index(T, ti, tj, c);
-            const float A = S.ljA[li], B = S.ljB[li];
-            const float3 d = f3sub(dpos(ih, il, jh, jl), sf);
-            const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
-            const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
-            float Vel = ih.w * jh.w * ri;
-            if (c == 3) Vel *= el14;
-            const float Va = A * r6 * r6, Vb = B * r6;
-            const float dv = ri2 * (-Vel - 12.f * Va + 6.f * Vb);
-            double eld = 0.0, evd = 0.0;
-            if (EACC) {
-                const double rid = rinv_d(S.x, i, j, sd), r6d = rid * rid * rid * rid * rid * rid;
-                eld = qi * S.crg_d[j] * rid;
-                if (c == 3) eld *= (double)T.el14d;
-                evd = S.ljA_d[li] * r6d * r6d - S.ljB_d[li] * r6d;
+        // pp pairs with exclusion / 1-4 handling (nbpplist_lrf :8108-8166):
+        // the atoms of a neighbour group in batches of QG_PPB, each batch's
+        // records, types, LJ codes and LJ products loaded together before any
+        // pair is formed (the loads of a batch are in flight at once)
+        const unsigned long long exm = S.exmask[i], p14m = S.p14mask[i];
+        const int ljrow = T.lj0 + (ti - T.type0) * T.natyps - T.type0;
+        auto pp_range = [&](int a0, int a1, int step, const float3 sf, const double3 sd) {
+            for (int kk = a0; kk < a1; kk += QG_PPB * step) {
+                int jj[QG_PPB], cc[QG_PPB];
+                float4 jh[QG_PPB], jl[QG_PPB];
+                float2 ab[QG_PPB];
+#pragma unroll
+                for (int u = 0; u < QG_PPB; ++u) jj[u] = kk + u * step < a1 ? S.g_atoms[kk + u * step] : -1;
+#pragma unroll
+                for (int u = 0; u < QG_PPB; ++u) {
+                    cc[u] = -1;   // else (type << 2) | LJ code (1, 2; 3 = 1-4 pair)
+                    if (jj[u] < 0 || jj[u] == i || S.aq[jj[u]] >= 0) continue;
+                    const int j = jj[u], rel = j - i;
+                    bool excl, p14;
+                    if (rel >= -32 && rel < 32) {
+                        excl = (exm >> (rel + 32)) & 1ull;
+                        p14 = (p14m >> (rel + 32)) & 1ull;
+                    } else {
+                        const PairFlags f = pair_flags(S, i, j);
+                        excl = f.excl; p14 = f.p14;
+                    }
+                    if (excl) continue;
+                    jh[u] = S.pos[j]; jl[u] = S.poslo[j];
+                    const int tj = S.atype[j];
+                    cc[u] = (tj << 2) | (p14 ? 3 : S.ljcod[ljrow + tj]);
+                }
+#pragma unroll
+                for (int u = 0; u < QG_PPB; ++u)
+                    if (cc[u] >= 0) {
+                        const int li = (ljrow + (cc[u] >> 2)) * 3 + (cc[u] & 3) - 1;
+                        ab[u] = make_float2(S.ljA[li], S.ljB[li]);
+                    }
+#pragma unroll
+                for (int u = 0; u < QG_PPB; ++u) {
+                    if (cc[u] < 0) continue;
+                    const int j = jj[u], c = cc[u] & 3;
+                    const float3 d = f3sub(dpos(ih, il, jh[u], jl[u]), sf);
+                    const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+                    const float ri = rsqrtf(r2), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
+                    float Vel = ih.w * jh[u].w * ri;
+                    if (c == 3) Vel *= el14;
+                    const float Va = ab[u].x * r6 * r6, Vb = ab[u].y * r6;
+                    const float dv = ri2 * (-Vel - 12.f * Va + 6.f * Vb);
+                    double eld = 0.0, evd = 0.0;
+                    if (EACC) {
+                        const int li = (ljrow + (cc[u] >> 2)) * 3 + c - 1;
+                        const double rid = rinv_d(S.x, i, j, sd), r6d = rid * rid * rid * rid * rid * rid;
+                        eld = qi * S.crg_d[j] * rid;
+                        if (c == 3) eld *= (double)T.el14d;
+                        evd = S.ljA_d[li] * r6d * r6d - S.ljB_d[li] * r6d;
+                    }
+                    epp_el.term(Vel, eld); epp_vdw.term(Va - Vb, evd);
+                    gx -= dv * d.x; gy -= dv * d.y; gz -= dv * d.z;
+                }
             }
-            e_el.term(Vel, eld); e_vdw.term(Va - Vb, evd);
-            gx -= dv * d.x; gy -= dv * d.y; gz -= dv * d.z;
-        };
-        // pp pair with exclusion / 1-4 handling (nbpplist_lrf :8108-8166)
-        auto pp = [&](int j, const float3 sf, const double3 sd) {
-            const PairFlags f = pair_flags(S, i, j);
-            if (f.excl) return;
-            pair(j, f.p14 ? 3 : ljc(S, T, ti, S.atype[j]), epp_el, epp_vdw, sf, sd);
         };
         const float3 zf = make_float3(0.f, 0.f, 0.f);
-        for (int kk = S.g_start[g] + lane; kk < S.g_start[g + 1]; kk += LW) {
-            const int j = S.g_atoms[kk];
-            if (j == i || S.aq[j] >= 0) continue;
-            pp(j, zf, dzero3());
-        }
+        pp_range(S.g_start[g] + lane, S.g_start[g + 1], LW, zf, dzero3());
         epp_el.flush(); epp_vdw.flush();
         const int n = S.nb_count[g], nw = S.nb_nw[g];
         const int *lst = S.nb_list + (size_t)g * S.nb_cap;
@@ -438,11 +470,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
                 sf = box_shift(T, dpos(swh, swl, S.pos[swn], S.poslo[swn]));
                 if (EACC) sd = box_shift_d(T, S.x, swg, swn);
             }
-            for (int kk = S.g_start[h]; kk < S.g_start[h + 1]; ++kk) {
-                const int j = S.g_atoms[kk];
-                if (S.aq[j] >= 0) continue;
-                pp(j, sf, sd);
-            }
+            pp_range(S.g_start[h], S.g_start[h + 1], 1, sf, sd);
             epp_el.flush(); epp_vdw.flush();
         }
     }

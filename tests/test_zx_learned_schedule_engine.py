@@ -7,9 +7,10 @@ steps, a pilot of 1,000 steps and a long run of 8,000 steps with the device
 FEP sums on (energies every 10 steps).
   * discharge (the config 3 windows): charges N(0, sigma) in state A, zero in
     state B, same LJ; s(lambda) is nearly flat;
-  * vanish (a decoupling end point): the same discharge, and the Q atoms' LJ
-    parameters (sqrt A, sqrt B) scaled by 0.3 in state B; the energy-gap
-    spread grows steeply towards pure state B, the case that uniform windows
+  * vanish (towards a decoupling end point): the same discharge, and the Q
+    atoms' LJ parameters (sqrt A, sqrt B) scaled by 0.12 in state B; waters
+    come close to the weakly repulsive Q atoms near pure state B, so the
+    energy-gap spread grows steeply there, the case that uniform windows
     sample badly.
 The network (the library's GPU kernels) is trained on 6 systems of each
 family -- pilot statistics in, long-run log-spread out -- and places 11
@@ -41,7 +42,7 @@ def _windows(k):
     qa = synth.neutral_charges(rng, 8, [0.3, 0.45, 0.6][k % 3])
     vanish = k % 2 == 1
     return [synth.synthetic(16.0, 8, 8, np.stack([qa, np.zeros(8)], 1), (l, 1.0 - l), 9000 + 37 * k,
-                            qvdw=vanish, q_lj_scale=(0.3, 0.3)) for l in LAM]
+                            qvdw=vanish, q_lj_scale=(0.12, 0.12)) for l in LAM]
 
 
 def _stats(k):
