@@ -1,4 +1,5 @@
-"""CPU restatement of qcalc's calculations (TEST INFRASTRUCTURE).
+"""CPU restatement of qcalc's calculations (TEST INFRASTRUCTURE; parity unpinned
+by reference data: the reference ships no qcalc test output).
 
 Only the tests load this file, as the checker of qsource_gb300's qgpu_calc_*
 entry points.  Each function follows one calc_* module of the reference

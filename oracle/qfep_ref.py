@@ -1,4 +1,5 @@
-"""CPU restatement of qfep's Parts 1-3 (TEST INFRASTRUCTURE).
+"""CPU restatement of qfep's Parts 1-3 (TEST INFRASTRUCTURE; parity unpinned by
+reference data for Parts 2-3: the reference ships no EVB mapping output).
 
 Only the tests load this file, as the checker of qgpu_qfep_evb.  It follows
 src/qfep.f90 of the reference (qusers/qsource, Q 5.06) statement by

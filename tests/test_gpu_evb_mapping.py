@@ -14,8 +14,9 @@ mapping protocol), FP64-master step, energy files written by the engine.
     the free-energy profiles (Parts 1-3) agree within the stated tolerances.
     Over 50 steps the engine's and the oracle's trajectories stay within
     about 1e-4 kcal/mol of each other, far below the 0.1 kcal/mol bar.
-The reference ships no EVB mapping output for this system (parity of the
-mapping's arithmetic is pinned by the restatement of qfep)."""
+Parity unpinned by reference data: the reference ships no EVB mapping output
+for this system, so the mapping's arithmetic is pinned by the restatement of
+qfep and the dynamics by the oracle."""
 import copy
 import multiprocessing as mp
 import os

@@ -3,6 +3,9 @@ restatement of the reference's calc_* modules (oracle/qcalc_ref.py), on frames
 of the engine's own MD: the 18 A droplet (sphere) and the reference's PBC
 system (box).
 
+Parity unpinned by reference data: the reference ships no qcalc test output,
+so these quantities are pinned by the restatement only.
+
 Tolerances: RMSD, centre of mass and geometry 1e-10 relative (FP64 sums in a
 different order); RDF bin counts exact (the reference's single-precision
 distance and double-precision binning reproduced operation for operation)."""

@@ -1,8 +1,8 @@
 """The oracle's arithmetic combination rule (ivdw_rule 2, the reference's
 nonbon2_* routines, src/md.f90:11354-13068).
 
-The reference ships no system that uses the arithmetic rule, so there is no
-golden energy for it.  These tests pin the oracle's restatement two ways:
+Parity unpinned by reference data: the reference ships no system that uses
+the arithmetic rule, so there is no golden energy for it.  These tests pin the oracle's restatement two ways:
   * the synthetic LJ types converted to the arithmetic form (radius R* and
     sqrt(eps) per type, qsource_gb300.synth._arithmetic_params) reproduce every
     same-type LJ curve, so the water-water LJ energy (O-O pairs only) equals

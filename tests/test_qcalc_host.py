@@ -1,5 +1,6 @@
 """Host side of the qcalc-style analysis: the DCD layout of src/trj.f90 and the
-oracle's calc_geom / calc_rdf restatements on configurations with known answers."""
+oracle's calc_geom / calc_rdf restatements on configurations with known answers
+(parity unpinned by reference data: the reference ships no qcalc test output)."""
 import math
 import struct
 
