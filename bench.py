@@ -289,7 +289,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     steps = max(NB, int(math.ceil(args.steps / NB)) * NB)
-    warm = max(3, args.warmup)
+    # warm-up in whole 10-step blocks, so that the timed blocks start at a list
+    # update and replay the block graphs (a block that starts between list
+    # updates runs step by step)
+    warm = max(NB, int(math.ceil(max(3, args.warmup) / NB)) * NB)
 
     if args.impl == "reference":
         if rank != 0:

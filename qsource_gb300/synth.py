@@ -101,7 +101,8 @@ def _waters(R: float, solute: np.ndarray, rng: np.random.Generator) -> np.ndarra
 def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, seed: int, *,
               solute_sigma: float = 0.3, T: float = 300.0, stepsize: float = 1.0, tau_T: float = 100.0,
               NBcycle: int = 10, Rc: float = 10.0, offdiag=None, initial_velocities: bool = True,
-              any_atom: bool = False, vdw_rule: int = 1, qvdw: bool = False, q_lj_scale=(0.9, 0.5)) -> System:
+              any_atom: bool = False, vdw_rule: int = 1, qvdw: bool = False, q_lj_scale=(0.9, 0.5),
+              solute_restraint: float = 0.0) -> System:
     """Water sphere of radius R around a solute chain of n_solute atoms whose
     first nq atoms are Q atoms with per-state charges qcharges[nq, nstates].
 
@@ -111,6 +112,12 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
     the other states a softer copy (sqrt(A) and sqrt(B) of the CT type scaled
     by q_lj_scale; (0, 0) makes the Q atoms vanish from the LJ terms in those
     states, the end-point case of a decoupling free energy).
+
+    solute_restraint > 0 adds a sequence restraint ([sequence_restraints] of
+    the .inp: atoms 1..n_solute, centre to the centre of the topology
+    positions) with that force constant in kcal/(mol A^2), which keeps a small
+    solute inside the droplet over long runs; without it a neutral chain can
+    leave the sphere (nothing restrains the solute).
 
     any_atom selects the any-atom cut-off for the solute charge groups
     (topology flag iuse_switch_atom = 0).  The chain's groups are 4
@@ -203,6 +210,7 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
         "shell_radius": None, "shell_force": 10.0, "excluded_force": 200.0, "solvent_radius": None,
         "radial_force": -1.0, "polarisation": False, "morse_depth": -1.0, "morse_width": -1.0,
         "non_bond": NBcycle, "lambdas": list(lambdas), "topology": None, "fep": None, "unsupported": [],
+        "sequence_restraints": [(1, n_solute, solute_restraint, 0, 1)] if solute_restraint > 0 else [],
     }
     s = build(top, fep, inp)
     if initial_velocities:
