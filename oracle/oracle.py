@@ -44,6 +44,8 @@ def lib() -> C.CDLL:
         L.oracle_make_pair_lists.argtypes = [vp]
         L.oracle_get_list.restype = C.c_int64
         L.oracle_get_list.argtypes = [vp, C.c_int, vp, C.c_int64]
+        L.oracle_get_list_shift.restype = C.c_int64
+        L.oracle_get_list_shift.argtypes = [vp, C.c_int, vp, C.c_int64]
         L.oracle_get_lrf.argtypes = [vp, vp]
         L.oracle_pot_energy.argtypes = [vp, C.c_int, vp, C.POINTER(Energies), C.POINTER(QEnergy)]
         L.oracle_shake_arrays.restype = C.c_int
@@ -113,6 +115,15 @@ class Oracle:
         n = self.L.oracle_get_list(self.h, w, None, 0)
         out = np.zeros((max(n, 1), 3), dtype=np.int32)
         self.L.oracle_get_list(self.h, w, _p(out), n)
+        return out[:n]
+
+    def get_list_shift(self, name: str) -> np.ndarray:
+        """Records of a list as rows (i, j, si, sj): si, sj the atoms whose
+        difference fixes the periodic shift (-1 in a sphere)."""
+        w = LIST_NAMES[name]
+        n = self.L.oracle_get_list_shift(self.h, w, None, 0)
+        out = np.zeros((max(n, 1), 4), dtype=np.int32)
+        self.L.oracle_get_list_shift(self.h, w, _p(out), n)
         return out[:n]
 
     def get_lrf(self) -> np.ndarray:

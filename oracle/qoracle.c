@@ -483,6 +483,85 @@ static void nbpwlis2_lrf(oracle *o) {
     }
 }
 
+/* nbpplis2_box_lrf, src/md.f90:7241-7439 (periodic box, iuse_switch_atom = 0):
+   a solute group pair (count-once parity rule) is inside when some atom pair
+   (Q atoms included, ig's atoms outer, jg's inner, minimum images) lies within
+   Rcpp; the first such pair is the pair's shift record (nbpp_cgp).  Not
+   inside: both LRF updates when some tested pair lies within RcLRF. */
+static void nbpplis2_box_lrf(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    double rc2 = d->Rcpp * d->Rcpp, rl2 = d->RcLRF * d->RcLRF;
+    o->pp.n = 0;
+    for (int ig = 0; ig < d->ncgp_solute; ++ig) {
+        for (int jg = 0; jg < d->ncgp_solute; ++jg) {
+            if (parity_skip(ig, jg)) continue;
+            int inside = 0, inside_lrf = 0, si = -1, sj = -1;
+            for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig] && !inside; ++ka)
+                for (int kb = d->cgp_first[jg]; kb <= d->cgp_last[jg] && !inside; ++kb) {
+                    const int i = d->cgpatom[ka], j = d->cgpatom[kb];
+                    const double r2 = dist2m(o, i, j);
+                    if (r2 <= rc2) { inside = 1; si = i; sj = j; }
+                    else if (r2 <= rl2) inside_lrf = 1;
+                }
+            if (inside) {
+                for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig]; ++ka) {
+                    int i = d->cgpatom[ka];
+                    if (is_q(o, i)) continue;
+                    for (int kb = d->cgp_first[jg]; kb <= d->cgp_last[jg]; ++kb) {
+                        int j = d->cgpatom[kb];
+                        if (is_q(o, j)) continue;
+                        if (ig == jg && i >= j) continue;
+                        if (excluded(o, i, j)) continue;
+                        int lj = ljcod(o, d->iac[i], d->iac[j]);
+                        if (is14(o, i, j)) lj = 3;
+                        nb_push_s(&o->pp, i, j, lj, lj, si, sj);
+                    }
+                }
+            } else if (d->use_LRF && inside_lrf) {
+                lrf_update(o, ig, jg);
+                lrf_update(o, jg, ig);
+            }
+        }
+    }
+}
+
+/* nbpwlis2_box_lrf, src/md.f90:8745-8900: a solute group and a water are
+   inside when some atom of the group lies within Rcpw of the water O
+   (minimum image); that atom and the O are the shift record (nbpw_cgp).  Not
+   inside: both LRF updates when some atom of the group lies within RcLRF of
+   the O. */
+static void nbpwlis2_box_lrf(oracle *o) {
+    const qgpu_system_desc *d = &o->d;
+    double rc2 = d->Rcpw * d->Rcpw, rl2 = d->RcLRF * d->RcLRF;
+    o->pw.n = 0;
+    for (int ig = 0; ig < d->ncgp_solute; ++ig) {
+        for (int jw = 0; jw < d->nwat; ++jw) {
+            const int ja = d->nat_solute + 3 * jw, jg = o->iwhich[ja];
+            int inside = 0, inside_lrf = 0, si = -1;
+            for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig] && !inside; ++ka) {
+                const int i = d->cgpatom[ka];
+                const double r2 = dist2m(o, i, ja);
+                if (r2 <= rc2) { inside = 1; si = i; }
+                else if (r2 <= rl2) inside_lrf = 1;
+            }
+            if (inside) {
+                for (int ka = d->cgp_first[ig]; ka <= d->cgp_last[ig]; ++ka) {
+                    int i = d->cgpatom[ka];
+                    if (is_q(o, i)) continue;
+                    for (int s = 0; s < 3; ++s) {
+                        int j = ja + s;
+                        if (all_zero(o, i, j)) continue;
+                        nb_push_s(&o->pw, i, j, ljcod(o, d->iac[i], d->iac[j]), 0, si, ja);
+                    }
+                }
+            } else if (d->use_LRF && inside_lrf) {
+                lrf_update(o, ig, jg);
+                lrf_update(o, jg, ig);
+            }
+        }
+    }
+}
+
 /* nbqplist, src/md.f90:10215-10322 (built once when Rcq > rexcl_o) */
 /* nbqplist_box, src/md.f90:10327-10459: rebuilt at every list update; a
    solute group is inside when one of its atoms lies within Rcq of the Q
@@ -614,12 +693,15 @@ static void nbqwlist(oracle *o) {
     o->qw_done = 1;
 }
 
-/* make_pair_lists, LRF branches, src/md.f90:6003-6058: sphere (switch-atom or
-   any-atom lists) or periodic box (switch-atom lists, minimum images) */
+/* make_pair_lists, LRF branches, src/md.f90:6003-6058: sphere or periodic box,
+   switch-atom or any-atom lists (minimum images in the box) */
 void oracle_make_pair_lists(void *h) {
     oracle *o = (oracle *)h;
     if (o->d.use_LRF) cgp_centers(o);
-    if (o->d.any_atom_lists) {
+    if (o->d.any_atom_lists && o->d.use_pbc) {
+        nbpplis2_box_lrf(o);
+        nbpwlis2_box_lrf(o);
+    } else if (o->d.any_atom_lists) {
         nbpplis2_lrf(o);
         nbpwlis2_lrf(o);
     } else {
@@ -638,6 +720,18 @@ int64_t oracle_get_list(void *h, int which, int32_t *out, int64_t cap) {
     if (out && cap >= l->n)
         for (int64_t k = 0; k < l->n; ++k) {
             out[3 * k] = l->a[k].i; out[3 * k + 1] = l->a[k].j; out[3 * k + 2] = l->a[k].lj;
+        }
+    return l->n;
+}
+/* the same records as (i, j, si, sj): si, sj the atom pair whose difference
+   fixes the record's periodic shift (-1 in a sphere) */
+int64_t oracle_get_list_shift(void *h, int which, int32_t *out, int64_t cap) {
+    oracle *o = (oracle *)h;
+    nblist *l = which == 0 ? &o->pp : which == 1 ? &o->pw : which == 2 ? &o->ww : which == 3 ? &o->qp : &o->qw;
+    if (out && cap >= l->n)
+        for (int64_t k = 0; k < l->n; ++k) {
+            out[4 * k] = l->a[k].i; out[4 * k + 1] = l->a[k].j;
+            out[4 * k + 2] = l->a[k].si; out[4 * k + 3] = l->a[k].sj;
         }
     return l->n;
 }

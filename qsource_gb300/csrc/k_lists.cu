@@ -105,6 +105,18 @@ __device__ __forceinline__ float d2hi(const float4 a, const float4 b) {
     const float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
     return dx * dx + dy * dy + dz * dz;
 }
+// the minimum-image forms of the two, for an atom pair in a periodic box
+__device__ __forceinline__ float d2hi_box(const float4 a, const float4 b, const TrajInfo &T) {
+    float3 d = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
+    d = f3sub(d, box_shift(T, d));
+    return d.x * d.x + d.y * d.y + d.z * d.z;
+}
+__device__ __forceinline__ bool within_hi_box(float d2, float rc2, double drc2, const double *x, int a, int b,
+                                              const TrajInfo &T) {
+    if (d2 < rc2 * (1.f - 1e-4f)) return true;
+    if (d2 > rc2 * (1.f + 1e-4f)) return false;
+    return dist2_exact_box(x, a, b, T) <= drc2;
+}
 
 // lrf_update (src/md.f90:5896-5981) of one source atom p (charge in .w) at
 // the target centre c: the 24 symmetric FP32 sums of the multipole expansion.
@@ -207,6 +219,7 @@ __global__ void __launch_bounds__(QG_BLOCK, QG_SCAN_MINB) k_scan(DevSys S, const
     }
     const long long slot = T.scr0 + (long long)chunk * T.ncgp + (t - T.grp0);
     int *nbseg = S.scr_nb + (size_t)slot * QG_CAPC;
+    int2 *shseg = (ANY && PBC && S.scr_sha) ? S.scr_sha + (size_t)slot * QG_CAPC : nullptr;
     float acc[QG_NLRF];
 #pragma unroll
     for (int k = 0; k < QG_NLRF; ++k) acc[k] = 0.f;
@@ -249,7 +262,47 @@ __global__ void __launch_bounds__(QG_BLOCK, QG_SCAN_MINB) k_scan(DevSys S, const
                 if (PBC) d = f3sub(d, box_shift(T, d));
                 float d2 = d.x * d.x + d.y * d.y + d.z * d.z;
                 bool near_, far_lrf;
-                if (any_atom && !(kind_t & kind_s)) {
+                int2 rec = make_int2(-1, -1);
+                if (ANY && PBC && any_atom && T.pbc && !(kind_t & kind_s)) {
+                    // nbpplis2_box_lrf (src/md.f90:7241-7439) / nbpwlis2_box_lrf
+                    // (:8745-8900): minimum-image atom pairs (a water counts by
+                    // its O) in the reference's loop order -- the outer group is
+                    // the solute group of a solute-water pair, and of a solute
+                    // pair the group the count-once rule keeps first.  The first
+                    // pair inside the cut-off is the pair's shift record; not
+                    // inside, the LRF holds when some pair lies within RcLRF.
+                    const int sa0 = ab + s_aoff[s], sa1 = ab + s_aoff[s + 1];
+                    const int sb1 = kind_s ? sa0 + 1 : sa1;
+                    const float ea = kind_t ? 0.f : ext_t, eb = kind_s ? 0.f : s_ext[s];
+                    const float rn = sqrtf(rc2) + ea + eb, rf = sqrtf(rc2_lrf) + ea + eb;
+                    near_ = false;
+                    far_lrf = false;
+                    if (d2 <= rf * rf * (1.f + 1e-4f)) {
+                        const int tl = t - T.grp0, sl = g - T.grp0;
+                        const bool t_outer = kind_t != kind_s
+                                                 ? kind_t == 0
+                                                 : !((tl > sl && ((tl + sl) & 1) == 0) || (tl < sl && ((tl + sl) & 1) == 1));
+                        const bool test_near = d2 <= rn * rn * (1.f + 1e-4f);
+                        bool anyl = false;
+                        const int nt = ta1 - ta0, nsrc = sb1 - sa0;
+                        const int no = t_outer ? nt : nsrc, ni = t_outer ? nsrc : nt;
+                        for (int io = 0; io < no && !near_; ++io)
+                            for (int ii = 0; ii < ni && !near_; ++ii) {
+                                const int kt = t_outer ? io : ii, ks = t_outer ? ii : io;
+                                const int ia = kt < ntreg ? s_ti[kt][tid] : S.g_atoms[ta0 + kt];
+                                const float4 pa = kt < ntreg ? s_tp[kt][tid] : S.pos[ia];
+                                const int jb = S.g_atoms[sa0 + ks];
+                                const float r2 = d2hi_box(pa, s_atom[sa0 + ks - ab], T);
+                                if (test_near && within_hi_box(r2, rc2, drc2, S.x, ia, jb, T)) {
+                                    near_ = true;
+                                    rec = make_int2(ia, jb);
+                                } else if (lrf && !anyl) {
+                                    anyl = within_hi_box(r2, rc2_lrf, T.drc2_lrf, S.x, ia, jb, T);
+                                }
+                            }
+                        far_lrf = !near_ && anyl;
+                    }
+                } else if (any_atom && !(kind_t & kind_s)) {
                     // nbpplis2_lrf (src/md.f90:7518-7545) / nbpwlis2_lrf
                     // (:8970-8985): inside when any atom pair is within the
                     // cut-off (a water counts by its O); else the LRF test
@@ -287,8 +340,13 @@ __global__ void __launch_bounds__(QG_BLOCK, QG_SCAN_MINB) k_scan(DevSys S, const
                 if (near_) {
                     // at most QG_CAPC groups per chunk: water neighbours (as
                     // their O atom) from the front, solute groups from the back
-                    if (kind_s) nbseg[cntw++] = s_rep[s];
-                    else nbseg[QG_CAPC - 1 - cnts++] = g;
+                    if (kind_s) {
+                        if (shseg) shseg[cntw] = rec;
+                        nbseg[cntw++] = s_rep[s];
+                    } else {
+                        if (shseg) shseg[QG_CAPC - 1 - cnts] = rec;
+                        nbseg[QG_CAPC - 1 - cnts++] = g;
+                    }
                 } else if (far_lrf) {
                     const int k0 = s_aoff[s];
                     // in a box the expansion centre moves by the periodic
@@ -328,6 +386,7 @@ __global__ void __launch_bounds__(QG_BLOCK, QG_SCAN_MINB) k_scan(DevSys S, const
 // lanes copy the chunks' near-group segments into the neighbour list (water
 // entries of every chunk first, then solute entries) -- and lane 0 forms the
 // symmetric Taylor coefficients.  No FP64: this runs over every group.
+template <bool SHA>
 __global__ void k_scan_reduce(DevSys S, int gb, int gn) {
     const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -381,7 +440,7 @@ __global__ void k_scan_reduce(DevSys S, int gb, int gn) {
             const int offw = ow + pw - nw, offs = os + ps - ns;
             const int nr = min(32, nch - r0);
             for (int j0 = 0; j0 < nr; j0 += 4) {
-                int vw[4][2], vs[4][2], dw[4], ds[4], kw[4], ks[4];
+                int vw[4][QG_CAPC / 32], vs[4][QG_CAPC / 32], dw[4], ds[4], kw[4], ks[4];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const int j = min(j0 + u, 31);
@@ -392,7 +451,7 @@ __global__ void k_scan_reduce(DevSys S, int gb, int gn) {
                     ds[u] = __shfl_sync(0xffffffffu, offs, j);
                     const int *seg = S.scr_nb + (base + (size_t)(r0 + j) * stride) * QG_CAPC;
 #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
+                    for (int h = 0; h < QG_CAPC / 32; ++h) {
                         const int k = lane + 32 * h;
                         vw[u][h] = k < kw[u] ? seg[k] : 0;
                         vs[u][h] = k < ks[u] ? seg[QG_CAPC - 1 - k] : 0;
@@ -401,11 +460,23 @@ __global__ void k_scan_reduce(DevSys S, int gb, int gn) {
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
 #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
+                    for (int h = 0; h < QG_CAPC / 32; ++h) {
                         const int k = lane + 32 * h;
                         if (k < kw[u] && dw[u] + k < cap) lst[dw[u] + k] = vw[u][h];
                         if (k < ks[u] && ds[u] + k < cap) lst[ds[u] + k] = vs[u][h];
                     }
+                // any-atom lists in a box: the shift records go along
+                if (SHA) {
+                    int2 *rl = S.nb_sha + (size_t)t * cap;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int2 *sseg = S.scr_sha + (base + (size_t)(r0 + min(j0 + u, 31)) * stride) * QG_CAPC;
+                        for (int k = lane; k < kw[u]; k += 32)
+                            if (dw[u] + k < cap) rl[dw[u] + k] = sseg[k];
+                        for (int k = lane; k < ks[u]; k += 32)
+                            if (ds[u] + k < cap) rl[ds[u] + k] = sseg[QG_CAPC - 1 - k];
+                    }
+                }
             }
             ow += __shfl_sync(0xffffffffu, pw, 31);
             os += __shfl_sync(0xffffffffu, ps, 31);
@@ -596,8 +667,11 @@ void launch_centers(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
 }
 void launch_scan(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
     prof_begin(L, "k_scan");
-    // a batch mixes no any-atom and box trajectories (refused at creation)
-    if (B.any_atom)
+    // one form covers the whole batch: both flags per trajectory when the
+    // batch holds any-atom lists and periodic boxes
+    if (B.any_atom && B.pbc)
+        k_scan<true, true><<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
+    else if (B.any_atom)
         k_scan<true, false><<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
     else if (B.pbc)
         k_scan<false, true><<<B.nscan, QG_BLOCK, 0, L.stream>>>(S, B.scan_t0, B.scan_tn, B.scan_traj, B.scan_chunk);
@@ -606,7 +680,8 @@ void launch_scan(const DevSys &S, const BlockTables &B, LaunchCtx &L) {
     prof_end(L);
     (*L.nlaunch)++;
     prof_begin(L, "k_scan_reduce");
-    k_scan_reduce<<<nblk(B.ng * 32, 128), 128, 0, L.stream>>>(S, B.g0, B.ng);
+    if (S.nb_sha) k_scan_reduce<true><<<nblk(B.ng * 32, 128), 128, 0, L.stream>>>(S, B.g0, B.ng);
+    else k_scan_reduce<false><<<nblk(B.ng * 32, 128), 128, 0, L.stream>>>(S, B.g0, B.ng);
     prof_end(L);
     (*L.nlaunch)++;
 }

@@ -225,11 +225,12 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
         for (int kk = nw + lane; kk < n; kk += LW) {
             const int g = lst[kk];
             // box: the image of the group's switch atom relative to this O
-            // (nonbond_pw_box :13395-13405)
+            // (nonbond_pw_box :13395-13405); with any-atom lists the solute
+            // atom of the pair's shift record (nbpwlis2_box_lrf :8835-8836)
             float3 sg = make_float3(0.f, 0.f, 0.f);
             double3 sgd = dzero3();
             if (pbc) {
-                const int sw = S.g_switch[g];
+                const int sw = T.any_atom ? S.nb_sha[(size_t)w * S.nb_cap + kk].y : S.g_switch[g];
                 sg = box_shift(T, dpos(oh, ol, S.pos[sw], S.poslo[sw]));
                 if (EACC) sgd = box_shift_d(T, S.x, a0, sw);
             }
@@ -434,11 +435,19 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
             const float4 w0 = S.wrec[b0], w1 = S.wrec[b0 + 1], w2 = S.wrec[b0 + 2];
             const float4 oh = make_float4(w0.x, w0.y, w0.z, 0.f), ol = make_float4(w1.x, w1.y, w1.z, 0.f);
             float3 dO = dpos(ih, il, oh, ol);
-            // box: the O image relative to this group's switch atom (nonbond_pw_box)
+            // box: the O image relative to this group's switch atom (nonbond_pw_box);
+            // with any-atom lists relative to the solute atom of the pair's
+            // shift record (nbpwlis2_box_lrf :8835-8836)
             double3 sgd = dzero3();
             if (pbc) {
-                dO = f3sub(dO, box_shift(T, dpos(swh, swl, oh, ol)));
-                if (EACC) sgd = box_shift_d(T, S.x, swg, b0);
+                if (T.any_atom) {
+                    const int sa = S.nb_sha[(size_t)g * S.nb_cap + k].x;
+                    dO = f3sub(dO, box_shift(T, dpos(S.pos[sa], S.poslo[sa], oh, ol)));
+                    if (EACC) sgd = box_shift_d(T, S.x, sa, b0);
+                } else {
+                    dO = f3sub(dO, box_shift(T, dpos(swh, swl, oh, ol)));
+                    if (EACC) sgd = box_shift_d(T, S.x, swg, b0);
+                }
             }
             const float3 dk[3] = {make_float3(0.f, 0.f, 0.f), make_float3(w0.w, w1.w, w2.x), make_float3(w2.y, w2.z, w2.w)};
 #pragma unroll
@@ -466,9 +475,15 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
             float3 sf = zf;
             double3 sd = dzero3();
             if (pbc) {
-                const int swn = S.g_switch[h];
-                sf = box_shift(T, dpos(swh, swl, S.pos[swn], S.poslo[swn]));
-                if (EACC) sd = box_shift_d(T, S.x, swg, swn);
+                // the switch atoms of the group pair; with any-atom lists the
+                // pair's shift record (nbpplis2_box_lrf :7338-7339)
+                int sa = swg, sb = S.g_switch[h];
+                if (T.any_atom) {
+                    const int2 r = S.nb_sha[(size_t)g * S.nb_cap + k];
+                    sa = r.x; sb = r.y;
+                }
+                sf = box_shift(T, dpos(S.pos[sa], S.poslo[sa], S.pos[sb], S.poslo[sb]));
+                if (EACC) sd = box_shift_d(T, S.x, sa, sb);
             }
             pp_range(S.g_start[h], S.g_start[h + 1], 1, sf, sd);
             epp_el.flush(); epp_vdw.flush();

@@ -164,10 +164,6 @@ static int validate(const qgpu_system_desc &d, int t) {
                                            d.bLJ_solv[5] != 0.0))
         return fail(QGPU_E_UNSUPPORTED, "traj %d: arithmetic rule with LJ on the water hydrogens", t);
     if (d.use_pbc) {
-        // the box forms cover the switch-atom lists (nb*list_box*); the
-        // any-atom box lists of the reference shift by a different atom pair
-        if (d.any_atom_lists)
-            return fail(QGPU_E_UNSUPPORTED, "traj %d: periodic box with any-atom lists (iuse_switch_atom = 0)", t);
         for (int k = 0; k < 3; ++k)
             if (!(d.boxlength[k] > 0.0)) return fail(QGPU_E_INVALID, "traj %d: box length %d not > 0", t, k);
         if (d.nqat > 0 && (d.qswitch < 0 || d.qswitch >= d.natom))
@@ -1012,8 +1008,13 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         for (int t = 0; t < ntraj; ++t) B.max_nqat = std::max(B.max_nqat, h->info[t].nqat);
         for (int t = 0; t < ntraj; ++t) B.any_atom |= h->info[t].any_atom;
         for (int t = 0; t < ntraj; ++t) B.pbc |= h->info[t].pbc;
-        if (B.any_atom && B.pbc)
-            return fail(QGPU_E_UNSUPPORTED, "a batch cannot mix any-atom lists and periodic boxes");
+        // any-atom lists in a box: the shift records of every neighbour entry
+        bool anybox = false;
+        for (int t = 0; t < ntraj; ++t) anybox |= h->info[t].any_atom && h->info[t].pbc;
+        if (anybox) {
+            if ((rc = alloc0(A, (size_t)S.ngrp * S.nb_cap, &S.nb_sha))) return rc;
+            if ((rc = alloc0(A, (size_t)scr_slots * QG_CAPC, &S.scr_sha))) return rc;
+        }
         B.npb = (int)pb_traj.size();
         B.nxrblk = (int)xr_blk_traj.size();
         // the whole batch

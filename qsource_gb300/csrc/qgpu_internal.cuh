@@ -217,6 +217,12 @@ struct DevSys {
     float *scr_phi;                 // QG_NLRF per slot
     int *scr_cnt;                   // per slot
     int *scr_nb;                    // QG_CAPC per slot
+    // periodic box with any-atom lists only (else null): per neighbour entry
+    // the atom pair that fixes the group pair's periodic shift (the first pair
+    // inside the cut-off in the reference's loop order: nbpp_cgp / nbpw_cgp of
+    // nbpplis2_box_lrf and nbpwlis2_box_lrf), (atom of the list's own group,
+    // atom of the neighbour); parallel to nb_list and to scr_nb
+    int2 *nb_sha = nullptr, *scr_sha = nullptr;
     // Q atoms
     const int *q_atom;              // global atom of each global Q index
     const float *qcrg_f;            // [q*QG_MAXS+s]

@@ -71,13 +71,23 @@ def _chain(n: int, R: float, rng: np.random.Generator) -> np.ndarray:
     return pos
 
 
-def _waters(R: float, solute: np.ndarray, rng: np.random.Generator) -> np.ndarray:
+def _waters(R: float, solute: np.ndarray, rng: np.random.Generator, box: float = 0.0) -> np.ndarray:
+    """Water O on a jittered lattice inside the sphere of radius R, or filling
+    the periodic cube of side `box` (a whole number of lattice cells, so the
+    lattice continues across the faces), with random orientations; waters
+    closer than 2.6 A to the solute are left out."""
     a = (1.0 / DENSITY) ** (1.0 / 3.0)
-    m = int(math.ceil(R / a)) + 1
-    g = np.arange(-m, m + 1) * a
-    O = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
-    O = O + rng.uniform(-0.25, 0.25, size=O.shape)
-    O = O[np.linalg.norm(O, axis=1) <= R]
+    if box > 0.0:
+        m = int(round(box / a))
+        g = (np.arange(m) + 0.5) * (box / m) - 0.5 * box
+        O = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+        O = O + rng.uniform(-0.25, 0.25, size=O.shape)
+    else:
+        m = int(math.ceil(R / a)) + 1
+        g = np.arange(-m, m + 1) * a
+        O = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+        O = O + rng.uniform(-0.25, 0.25, size=O.shape)
+        O = O[np.linalg.norm(O, axis=1) <= R]
     # random orientations: uniform unit quaternions
     q = rng.normal(size=(len(O), 4))
     q /= np.linalg.norm(q, axis=1)[:, None]
@@ -91,8 +101,11 @@ def _waters(R: float, solute: np.ndarray, rng: np.random.Generator) -> np.ndarra
     loc = np.array([[0, 0, 0], [R_OH * math.sin(h), 0, R_OH * math.cos(h)], [-R_OH * math.sin(h), 0, R_OH * math.cos(h)]])
     W = O[:, None, :] + np.einsum("nij,aj->nai", Rm, loc)
     if len(solute):
-        tree = cKDTree(solute)
-        d, _ = tree.query(W.reshape(-1, 3))
+        tree = cKDTree(solute, boxsize=None)
+        Wq = W.reshape(-1, 3)
+        if box > 0.0:   # minimum image: solute images across the faces count
+            Wq = Wq - box * np.round(Wq / box)
+        d, _ = tree.query(Wq)
         keep = d.reshape(-1, 3).min(axis=1) >= 2.6
         W = W[keep]
     return W.reshape(-1, 3)
@@ -102,7 +115,7 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
               solute_sigma: float = 0.3, T: float = 300.0, stepsize: float = 1.0, tau_T: float = 100.0,
               NBcycle: int = 10, Rc: float = 10.0, offdiag=None, initial_velocities: bool = True,
               any_atom: bool = False, vdw_rule: int = 1, qvdw: bool = False, q_lj_scale=(0.9, 0.5),
-              solute_restraint: float = 0.0) -> System:
+              solute_restraint: float = 0.0, box: float = 0.0) -> System:
     """Water sphere of radius R around a solute chain of n_solute atoms whose
     first nq atoms are Q atoms with per-state charges qcharges[nq, nstates].
 
@@ -119,6 +132,11 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
     solute inside the droplet over long runs; without it a neutral chain can
     leave the sphere (nothing restrains the solute).
 
+    box > 0 builds a periodic cube of that side instead of the sphere: waters
+    fill it, the chain grows within R of its centre, the Q switching atom is
+    the first Q atom, and the solvent is put back in the box at each list
+    update (R must stay below box / 2 minus the cut-off).
+
     any_atom selects the any-atom cut-off for the solute charge groups
     (topology flag iuse_switch_atom = 0).  The chain's groups are 4
     consecutive atoms with no angle terms, so two atoms of groups whose
@@ -129,7 +147,7 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
     S = qcharges.shape[1]
     n_solute = max(n_solute, nq)
     chain = _chain(n_solute, R, rng)
-    W = _waters(R, chain, rng)
+    W = _waters(R, chain, rng, box)
     nw = len(W) // 3
     natom = n_solute + 3 * nw
     xtop = np.concatenate([chain.reshape(-1), W.reshape(-1)])
@@ -182,7 +200,10 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
         "solvent_type": 0, "rexcl_o": R + 2.0, "rwat": R,
         "xpcent": np.zeros(3), "xwcent": np.zeros(3), "nexats": 0, "nexwat": 0,
         "excl": np.zeros(natom, np.uint8),
+        "nres": 1 + nw, "nres_solute": 1,
     }
+    if box > 0.0:
+        top.update({"use_pbc": True, "boxlength": np.full(3, float(box)), "boxcentre": np.zeros(3)})
     atom_types, change_atoms = [], []
     if qvdw:
         ct = TYPES.index("CT")
@@ -201,6 +222,7 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
         "bond_types": {}, "change_bonds": [], "angle_types": {}, "change_angles": [],
         "torsion_types": {}, "change_torsions": [], "improper_types": {}, "change_impropers": [],
         "off_diagonals": list(offdiag or []), "unsupported": [],
+        "qswitch": 1 if box > 0.0 and nq else None,
     }
     inp = {
         "steps": 0, "stepsize": stepsize, "temperature": T, "bath_coupling": tau_T, "thermostat": "berendsen",
@@ -211,6 +233,7 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
         "radial_force": -1.0, "polarisation": False, "morse_depth": -1.0, "morse_width": -1.0,
         "non_bond": NBcycle, "lambdas": list(lambdas), "topology": None, "fep": None, "unsupported": [],
         "sequence_restraints": [(1, n_solute, solute_restraint, 0, 1)] if solute_restraint > 0 else [],
+        "pbc": box > 0.0, "put_solvent_back_in_box": box > 0.0,
     }
     s = build(top, fep, inp)
     if initial_velocities:
