@@ -300,6 +300,93 @@ __global__ void __launch_bounds__(QG_BLOCK, MINB) k_nb_water(DevSys S, const int
     block_energies_fx<5>(S.eacc + (size_t)traj * QG_NE, slots, ev, red);
 }
 
+// Water-water LJ of the eight atom pairs beside O-O, for trajectories whose
+// water hydrogens carry LJ under the arithmetic rule (nonbon2_ww,
+// src/md.f90:12847-12944, takes LJ on all nine pairs; k_nb_water has the
+// Coulomb terms of all nine and the O-O LJ).  LW lanes per water over its
+// water neighbours, the same relative vectors and periodic image as
+// k_nb_water; the forces of this water's atoms, and half of each pair energy
+// (the pair is met from both sides).
+template <int E, bool BOX>
+__global__ void __launch_bounds__(QG_BLOCK) k_ww_hlj(DevSys S, const int *wgrp) {
+    constexpr int LW = 8;
+    constexpr bool EACC = E == 1;
+    __shared__ long long red[1][QG_BLOCK / 32];
+    const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LW;
+    const int lane = threadIdx.x & (LW - 1);
+    const int w = wgrp[idx];
+    const int traj = traj_of_entry(S, w, true);
+    const TrajInfo &T = S.traj[traj];
+    EAcc<E> evdw;
+    evdw.zero();
+    const bool valid = w >= 0 && !S.g_excl[w] && T.hlj;
+    int a0 = 0;
+    float gx[3] = {0, 0, 0}, gy[3] = {0, 0, 0}, gz[3] = {0, 0, 0};
+    if (valid) {
+        a0 = S.g_atoms[S.g_start[w]];
+        const int nw = S.nb_nw[w];
+        const int *lst = S.nb_list + (size_t)w * S.nb_cap;
+        const float4 r0 = S.wrec[a0], r1 = S.wrec[a0 + 1], r2 = S.wrec[a0 + 2];
+        const float3 da[3] = {make_float3(0.f, 0.f, 0.f), make_float3(r0.w, r1.w, r2.x), make_float3(r2.y, r2.z, r2.w)};
+        const bool pbc = BOX && T.pbc != 0;
+        for (int k = lane; k < nw; k += LW) {
+            const int b0 = lst[k];
+            const float4 q0 = S.wrec[b0], q1 = S.wrec[b0 + 1], q2 = S.wrec[b0 + 2];
+            float3 dO = make_float3((q0.x - r0.x) + (q1.x - r1.x), (q0.y - r0.y) + (q1.y - r1.y),
+                                    (q0.z - r0.z) + (q1.z - r1.z));
+            double3 shd = dzero3();
+            if (pbc) {
+                dO = f3sub(dO, box_shift(T, dO));
+                if (EACC) shd = box_shift_d(T, S.x, a0, b0);
+            }
+            const float3 db[3] = {make_float3(0.f, 0.f, 0.f), make_float3(q0.w, q1.w, q2.x),
+                                  make_float3(q2.y, q2.z, q2.w)};
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) {
+                    if (a == 0 && b == 0) continue;
+                    const float3 d = make_float3(dO.x + (db[b].x - da[a].x), dO.y + (db[b].y - da[a].y),
+                                                 dO.z + (db[b].z - da[a].z));
+                    const float r2f = d.x * d.x + d.y * d.y + d.z * d.z;
+                    const float ri = rsqrtf(r2f), ri2 = ri * ri, r6 = ri2 * ri2 * ri2;
+                    const float Va = T.wwh_A[3 * a + b] * r6 * r6, Vb = T.wwh_B[3 * a + b] * r6;
+                    const float dv = ri2 * (-12.f * Va + 6.f * Vb);
+                    double ed = 0.0;
+                    if (EACC) {
+                        const double rid = rinv_d(S.x, a0 + a, b0 + b, shd);
+                        const double r6d = rid * rid * rid * rid * rid * rid;
+                        ed = T.wwh_Ad[3 * a + b] * r6d * r6d - T.wwh_Bd[3 * a + b] * r6d;
+                    }
+                    evdw.term(Va - Vb, ed);
+                    gx[a] -= dv * d.x; gy[a] -= dv * d.y; gz[a] -= dv * d.z;
+                }
+            evdw.flush();
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int o = LW / 2; o > 0; o >>= 1) {
+            gx[a] += __shfl_xor_sync(0xffffffffu, gx[a], o, LW);
+            gy[a] += __shfl_xor_sync(0xffffffffu, gy[a], o, LW);
+            gz[a] += __shfl_xor_sync(0xffffffffu, gz[a], o, LW);
+        }
+    if (valid && lane < 3) {
+        const int a = lane;
+        const float fx = a == 0 ? gx[0] : (a == 1 ? gx[1] : gx[2]);
+        const float fy = a == 0 ? gy[0] : (a == 1 ? gy[1] : gy[2]);
+        const float fz = a == 0 ? gz[0] : (a == 1 ? gz[1] : gz[2]);
+        fx_addf(S.fx + 3 * (a0 + a), fx, S.status);
+        fx_addf(S.fx + 3 * (a0 + a) + 1, fy, S.status);
+        fx_addf(S.fx + 3 * (a0 + a) + 2, fz, S.status);
+    }
+    if (E == 2) return;
+    const int slots[1] = {EA_WW_VDW};
+    long long ev[1] = {evdw.fx(0.5f, S.status)};
+    block_energies_fx<1>(S.eacc + (size_t)traj * QG_NE, slots, ev, red);
+}
+
 // ------------------------------------------------------- solute atoms
 struct PairFlags { bool excl, p14; };
 
@@ -607,7 +694,7 @@ __device__ __forceinline__ void q_energies(const DevSys &S, int traj, int NS, co
 // whose energies are not recorded: fewer registers, more resident blocks).
 // The per-state O-side constants of every Q atom (A, B, charge, soft-core
 // term) are staged in shared memory with the Q positions.
-template <int LG, int E>
+template <int LG, int E, bool HLJ>
 __global__ void __launch_bounds__(QG_BLOCK, E == 2 ? 6 : 1) k_qw(DevSys S, const int *wgrp, EaccSel esel) {
     __shared__ QShared sh;
     __shared__ float4 qwp[QG_MAXQ * QG_MAXS];
@@ -700,6 +787,30 @@ __global__ void __launch_bounds__(QG_BLOCK, E == 2 ? 6 : 1) k_qw(DevSys S, const
                     if (acc) eel.d[s] += S.crg_d[a0 + a] * S.qcrg_d[q * QG_MAXS + s] * rid;
                     else if (want) eel.k[s].add(Vel);
                     dv -= lam[s] * ri2 * Vel;
+                }
+                if (HLJ && T.hlj) {
+                    // nonbon2_qw (src/md.f90:12562-12695) with LJ on the H:
+                    // its products with the Q atom's (state) type, soft-core
+                    // column the H's type
+                    const float r6hc = r2 * r2 * r2;
+                    double r6hcd = 0.0;
+                    if (acc) { const double r2d = dist2_d(S.x, qa, a0 + a, swd); r6hcd = r2d * r2d * r2d; }
+#pragma unroll
+                    for (int s = 0; s < QG_MAXS; ++s) {
+                        if (s >= NS) break;
+                        const int hi = (q * QG_MAXS + s) * 2 + (a - 1);
+                        const size_t sci = (size_t)T.sc0 + ((size_t)iq * ntq + (size_t)T.wh_col[a - 1]) * QG_MAXS + s;
+                        const float r6s = T.qvdw ? r6hc + S.sc_f[sci] : r6hc;
+                        const float ir6 = __frcp_rn(r6s);
+                        const float Va = S.qwh_A[hi] * ir6 * ir6, Vb = S.qwh_B[hi] * ir6;
+                        dv -= lam[s] * ri2 * (12.f * Va - 6.f * Vb) * (r6hc * ir6);
+                        if (acc) {
+                            const double ir6d = rcp_nr(T.qvdw ? r6hcd + S.sc_d[sci] : r6hcd);
+                            evdw.d[s] += S.qwh_Ad[hi] * ir6d * ir6d - S.qwh_Bd[hi] * ir6d;
+                        } else if (want) {
+                            evdw.k[s].add(Va - Vb);
+                        }
+                    }
                 }
                 gx[a] += dv * d.x; gy[a] += dv * d.y; gz[a] += dv * d.z;
                 qfx -= dv * d.x; qfy -= dv * d.y; qfz -= dv * d.z;
@@ -876,6 +987,13 @@ static void water_launch(const DevSys &S, const BlockTables &B, LaunchCtx &L, in
     if (emode == QG_PAIR_E_FP64) k_nb_water<1, 8, 1, 2, BOX><<<B.nwgrp * 8 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, lrf);
     else if (emode == QG_PAIR_E_NONE) water_shapes<2, BOX>(S, B, L, lrf);
     else water_shapes<0, BOX>(S, B, L, lrf);
+    if (!B.hlj) return;
+    // the LJ of the water hydrogens (arithmetic rule), on the same stream
+    const int nb = B.nwgrp * 8 / QG_BLOCK;
+    if (emode == QG_PAIR_E_FP64) k_ww_hlj<1, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp);
+    else if (emode == QG_PAIR_E_NONE) k_ww_hlj<2, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp);
+    else k_ww_hlj<0, BOX><<<nb, QG_BLOCK, 0, L.stream>>>(S, B.wgrp);
+    (*L.nlaunch)++;
 }
 void launch_nb_water(const DevSys &S, const BlockTables &B, LaunchCtx &L, int lrf, int emode) {
     if (!B.nwgrp) return;
@@ -919,12 +1037,19 @@ static int qw_lanes(const BlockTables &B) {
 // MD step evaluates the per-state energies in FP64 and is bound by the FP64
 // pipe: one lane per water is its fastest shape on the benchmark batch (70 us
 // against 81 with four lanes and 93 with two).
+template <int E, bool HLJ>
+static void qw_shapes_h(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
+    const int lg = E == 2 ? qw_lanes(B) : 1;
+    if (lg == 1) k_qw<1, E, HLJ><<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+    else if (lg == 2) k_qw<2, E, HLJ><<<B.nwgrp * 2 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+    else k_qw<4, E, HLJ><<<B.nwgrp * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+}
+// batches with LJ on some trajectory's water hydrogens take the form that
+// adds the Q-H LJ terms
 template <int E>
 static void qw_shapes(const DevSys &S, const BlockTables &B, LaunchCtx &L, EaccSel e) {
-    const int lg = E == 2 ? qw_lanes(B) : 1;
-    if (lg == 1) k_qw<1, E><<<B.nwgrp / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
-    else if (lg == 2) k_qw<2, E><<<B.nwgrp * 2 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
-    else k_qw<4, E><<<B.nwgrp * 4 / QG_BLOCK, QG_BLOCK, 0, L.stream>>>(S, B.wgrp, e);
+    if (B.hlj) qw_shapes_h<E, true>(S, B, L, e);
+    else qw_shapes_h<E, false>(S, B, L, e);
 }
 // emode QG_PAIR_E_NONE (an MD step whose energies are not recorded) takes the
 // energy-free instantiation; every other mode lets esel decide on the device.

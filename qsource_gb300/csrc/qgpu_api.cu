@@ -157,12 +157,6 @@ static int validate(const qgpu_system_desc &d, int t) {
     if ((d.natom - d.nat_solute) % 3) return fail(QGPU_E_INVALID, "traj %d: solvent atoms not a multiple of 3", t);
     if (d.ivdw_rule != 1 && d.ivdw_rule != 2)
         return fail(QGPU_E_INVALID, "traj %d: combination rule %d (1 geometric, 2 arithmetic)", t, d.ivdw_rule);
-    // arithmetic rule: nonbon2_ww / nonbon2_qw take LJ on every water atom;
-    // the engine's water kernels take it on O only, exact when the water H
-    // atoms carry no LJ (b = 0)
-    if (d.ivdw_rule == 2 && d.nwat > 0 && (d.bLJ_solv[2] != 0.0 || d.bLJ_solv[3] != 0.0 || d.bLJ_solv[4] != 0.0 ||
-                                           d.bLJ_solv[5] != 0.0))
-        return fail(QGPU_E_UNSUPPORTED, "traj %d: arithmetic rule with LJ on the water hydrogens", t);
     if (d.use_pbc) {
         for (int k = 0; k < 3; ++k)
             if (!(d.boxlength[k] > 0.0)) return fail(QGPU_E_INVALID, "traj %d: box length %d not > 0", t, k);
@@ -265,8 +259,8 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
     std::vector<int> q_atom, qiac, qw_lj, qw_sc, qp14_first{0}, qp14_q;
     std::vector<float> ljA, ljB;
     std::vector<double> ljA_d, ljB_d;
-    std::vector<float> qcrg_f, qavdw, qbvdw, sc_f, qw_A, qw_B;
-    std::vector<double> qw_Ad, qw_Bd;
+    std::vector<float> qcrg_f, qavdw, qbvdw, sc_f, qw_A, qw_B, qwh_A, qwh_B;
+    std::vector<double> qw_Ad, qw_Bd, qwh_Ad, qwh_Bd;
     std::vector<double> qcrg_d, qavdw_d, qbvdw_d, sc_d;
     std::vector<int> qq_iq, qq_j, qq_jq;
     std::vector<int8_t> qq_lj;
@@ -523,7 +517,30 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
             if (T.arith) arith_ab(d.aLJ_solv[c - 1], d.aLJ_solv[c - 1], d.bLJ_solv[c - 1], d.bLJ_solv[c - 1], A, B);
             T.ww_A = (float)A; T.ww_B = (float)B;
             T.ww_Ad = A; T.ww_Bd = B;
-        } else T.ww_lj = 1;
+            // arithmetic rule: nonbon2_ww (:12847-12944) takes LJ on all nine
+            // atom pairs, (a_i + a_j)^6 and b_i b_j of aLJ_solv / bLJ_solv with
+            // each pair's own LJ code; the eight pairs beside O-O are the
+            // extra kernel's when some hydrogen carries LJ
+            T.hlj = 0;
+            for (int k = 0; k < 9; ++k) { T.wwh_A[k] = T.wwh_B[k] = 0.f; T.wwh_Ad[k] = T.wwh_Bd[k] = 0.0; }
+            if (T.arith && (d.bLJ_solv[2] != 0.0 || d.bLJ_solv[3] != 0.0 || d.bLJ_solv[4] != 0.0 ||
+                            d.bLJ_solv[5] != 0.0)) {
+                T.hlj = 1;
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) {
+                        if (a == 0 && b == 0) continue;
+                        const int ta = d.iac[d.nat_solute + a], tb = d.iac[d.nat_solute + b];
+                        const int cc = d.ljcod[ta * nt + tb];
+                        double Ah, Bh;
+                        arith_ab(d.aLJ_solv[a * 2 + cc - 1], d.aLJ_solv[b * 2 + cc - 1], d.bLJ_solv[a * 2 + cc - 1],
+                                 d.bLJ_solv[b * 2 + cc - 1], Ah, Bh);
+                        T.wwh_A[3 * a + b] = (float)Ah; T.wwh_B[3 * a + b] = (float)Bh;
+                        T.wwh_Ad[3 * a + b] = Ah; T.wwh_Bd[3 * a + b] = Bh;
+                    }
+                T.wh_col[0] = d.iac[d.nat_solute + 1];
+                T.wh_col[1] = d.iac[d.nat_solute + 2];
+            }
+        } else { T.ww_lj = 1; T.hlj = 0; }
         // --- atoms
         std::vector<int> grp_of(N, 0);
         for (int g = 0; g < d.ncgp; ++g)
@@ -728,6 +745,20 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
                 }
                 qw_A.push_back((float)A); qw_B.push_back((float)B);
                 qw_Ad.push_back(A); qw_Bd.push_back(B);
+                // nonbon2_qw with the two water hydrogens: aLJ_solv / bLJ_solv of
+                // the H and the LJ code of the (H, Q atom) pair
+                for (int h = 0; h < 2; ++h) {
+                    double Ah = 0.0, Bh = 0.0;
+                    if (T.hlj) {
+                        const int tH = d.iac[d.nat_solute + 1 + h];
+                        const int ch = d.ljcod[tH * nt + tq], cq = ch == 2 ? 1 : ch;
+                        const double aq = d.qvdw_flag ? d.qavdw[qt * 3 + cq - 1] : d.avdw[tq * 3 + ch - 1];
+                        const double bq = d.qvdw_flag ? d.qbvdw[qt * 3 + cq - 1] : d.bvdw[tq * 3 + ch - 1];
+                        arith_ab(aq, d.aLJ_solv[(1 + h) * 2 + ch - 1], bq, d.bLJ_solv[(1 + h) * 2 + ch - 1], Ah, Bh);
+                    }
+                    qwh_A.push_back((float)Ah); qwh_B.push_back((float)Bh);
+                    qwh_Ad.push_back(Ah); qwh_Bd.push_back(Bh);
+                }
             }
         }
         int ntq = nt + nq;
@@ -936,6 +967,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         if ((rc = upload(A, qw_B, &p))) return rc; S.qw_B = p;
     }
     UP(qw_lj, qw_lj); UP(qw_sc, qw_sc); UP(qw_Ad, qw_Ad); UP(qw_Bd, qw_Bd);
+    UP(qwh_A, qwh_A); UP(qwh_B, qwh_B); UP(qwh_Ad, qwh_Ad); UP(qwh_Bd, qwh_Bd);
     UP(ljA, ljA); UP(ljB, ljB); UP(ljA_d, ljA_d); UP(ljB_d, ljB_d);
     if ((rc = alloc0(A, (size_t)atom0, &S.qw_member))) return rc;
     if ((rc = alloc0(A, (size_t)atom0, &S.qp_member))) return rc;
@@ -1008,6 +1040,7 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         for (int t = 0; t < ntraj; ++t) B.max_nqat = std::max(B.max_nqat, h->info[t].nqat);
         for (int t = 0; t < ntraj; ++t) B.any_atom |= h->info[t].any_atom;
         for (int t = 0; t < ntraj; ++t) B.pbc |= h->info[t].pbc;
+        for (int t = 0; t < ntraj; ++t) B.hlj |= h->info[t].hlj;
         // any-atom lists in a box: the shift records of every neighbour entry
         bool anybox = false;
         for (int t = 0; t < ntraj; ++t) anybox |= h->info[t].any_atom && h->info[t].pbc;

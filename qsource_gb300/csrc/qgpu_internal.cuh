@@ -84,6 +84,14 @@ struct TrajInfo {
     int ww_lj;                  // ljcod of the water O pair
     float ww_A, ww_B;           // O-O LJ products (aLJ_solv(1,c)^2, bLJ_solv(1,c)^2)
     double ww_Ad, ww_Bd;
+    // arithmetic rule with LJ on the water hydrogens (nonbon2_ww :12847,
+    // nonbon2_qw :12562 take LJ on every water atom): hlj set, the products of
+    // the water atom pairs [3*a+b] other than O-O (that one is ww_A/ww_B, and
+    // entry 0 is zero), and the sc_lookup columns of the two H (their types)
+    int hlj;
+    float wwh_A[9], wwh_B[9];
+    double wwh_Ad[9], wwh_Bd[9];
+    int wh_col[2];
     float chg_solv[3];
     float wwqq[9];              // chg_solv(a)*chg_solv(b), nonbond_ww_spc charge products
     float el14;
@@ -236,6 +244,10 @@ struct DevSys {
     const double *qw_Ad, *qw_Bd;
     const int *qw_lj;               // [q] LJ code of the water-O / Q-atom pair
     const int *qw_sc;               // [q] sc_lookup column of the water O (the LJ code, or its type: arithmetic rule)
+    // arithmetic rule with LJ on the water hydrogens: [(q*QG_MAXS+s)*2 + h]
+    // LJ products of Q atom q in state s with water H h (0, 1); null otherwise
+    const float *qwh_A, *qwh_B;
+    const double *qwh_Ad, *qwh_Bd;
     // LJ products per (type pair, code) under the trajectory's combination
     // rule, [(lj0 + ta*natyps + tb)*3 + code-1] (lj_index)
     const float *ljA, *ljB;
@@ -547,6 +559,7 @@ struct BlockTables {
     const int *wp_traj, *wp_scr0; double *wp_scr; int nwp;
     int any_atom;                      // some trajectory uses the any-atom cut-off
     int pbc;                           // some trajectory is a periodic box
+    int hlj;                           // some trajectory has LJ on the water hydrogens (arithmetic rule)
     // put_back_in_box: one block per trajectory that moves molecules
     const int *pb_traj; int npb;
     int nxrblk;                        // blocks of the p_restrain items (DevSys::xr_*)

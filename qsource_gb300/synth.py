@@ -115,7 +115,7 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
               solute_sigma: float = 0.3, T: float = 300.0, stepsize: float = 1.0, tau_T: float = 100.0,
               NBcycle: int = 10, Rc: float = 10.0, offdiag=None, initial_velocities: bool = True,
               any_atom: bool = False, vdw_rule: int = 1, qvdw: bool = False, q_lj_scale=(0.9, 0.5),
-              solute_restraint: float = 0.0, box: float = 0.0) -> System:
+              solute_restraint: float = 0.0, box: float = 0.0, water_h_lj: bool = False) -> System:
     """Water sphere of radius R around a solute chain of n_solute atoms whose
     first nq atoms are Q atoms with per-state charges qcharges[nq, nstates].
 
@@ -131,6 +131,8 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
     positions) with that force constant in kcal/(mol A^2), which keeps a small
     solute inside the droplet over long runs; without it a neutral chain can
     leave the sphere (nothing restrains the solute).
+
+    water_h_lj (arithmetic rule only) gives the water hydrogens LJ parameters.
 
     box > 0 builds a periodic cube of that side instead of the sphere: waters
     fill it, the chain grows within R of its centre, the Q switching atom is
@@ -181,6 +183,12 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
     bv = np.array([[OPLS[t][2], OPLS[t][4], OPLS[t][4]] for t in TYPES])
     if vdw_rule == 2:
         av, bv = _arithmetic_params(av, bv)
+        if water_h_lj:
+            # water hydrogens with LJ (R*/2 = 0.2245 A, eps = 0.046 kcal/mol in
+            # every code), the case nonbon2_ww / nonbon2_qw take on all atoms
+            hw = TYPES.index("HW")
+            av[hw, :] = 0.2245
+            bv[hw, :] = math.sqrt(0.046)
     top = {
         "version": 5.06, "ff_type": 2, "natom": natom, "nat_solute": n_solute, "solv_atom": 3,
         "xtop": xtop, "iac": iac,

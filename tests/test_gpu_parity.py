@@ -51,6 +51,10 @@ def systems(engine_lib):
     out["cfg1qv"] = synth.config(1, qvdw=True)
     out["cfg1arqv"] = synth.config(1, vdw_rule=2, qvdw=True)
     out["cfg2ar"] = synth.config(2, vdw_rule=2)
+    # arithmetic rule with LJ on the water hydrogens (nonbon2_ww / nonbon2_qw
+    # take LJ on every water atom)
+    out["cfg1arh"] = synth.config(1, vdw_rule=2, water_h_lj=True)
+    out["cfg1arqvh"] = synth.config(1, vdw_rule=2, qvdw=True, water_h_lj=True)
     g = golden_system("basic_sph")
     o = _oracle(g)
     o.maxwell(g.Tmaxw, int(g.seed))
@@ -107,7 +111,8 @@ def test_lrf_multipoles(systems, name):
         assert err <= 1e-5 * scale, (lo, err, scale)
 
 
-@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg2sw", "cfg4", "cfg1ar", "cfg1qv", "cfg1arqv", "cfg2ar"])
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg2", "cfg2sw", "cfg4", "cfg1ar", "cfg1qv", "cfg1arqv", "cfg2ar",
+                                  "cfg1arh", "cfg1arqvh"])
 def test_forces_and_energies(systems, name):
     s = systems[name]
     e = _engine(s)
@@ -151,7 +156,7 @@ def test_shake_matches_oracle(systems):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("name,ene_every", [("cfg1", 1), ("cfg1", 5), ("cfg1arqv", 5), ("cfg2ar", 5)])
+@pytest.mark.parametrize("name,ene_every", [("cfg1", 1), ("cfg1", 5), ("cfg1arqv", 5), ("cfg2ar", 5), ("cfg1arqvh", 5)])
 def test_short_md_matches_oracle(systems, name, ene_every, precision):
     """20 Berendsen leap-frog steps with SHAKE and lists every 10 steps, with
     the FP64 master (FP64 x, v, leap-frog and SHAKE; FP32 pair terms) and the
@@ -298,7 +303,7 @@ def test_q_lists_exact(systems, name, rcq):
             o.make_pair_lists()
 
 
-@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg4", "cfg1arqv", "cfg2ar"])
+@pytest.mark.parametrize("name", ["golden", "cfg1", "cfg4", "cfg1arqv", "cfg2ar", "cfg1arqvh"])
 def test_step_precision_forces(systems, name):
     """The precision of an unrecorded MD step (QGPU_TERMS_STEP_PRECISION: FP32
     bonded, restraint and Q terms from the float coordinates, FP32 energy sums)
