@@ -561,6 +561,12 @@ int qgpu_lrf_scan_static(int32_t ngroup, const double *x, const double *crg, con
    (calc_rms.f90 rms_calc).  out[nframes], A. */
 int qgpu_calc_rms(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
                   const double *xref, double *out);
+/* RMS fluctuation of the masked atoms (calc_rmsf.f90 RMSF_calc): after each
+   frame, per atom sqrt(mean of |x|^2 - |running mean of x|^2) over the frames
+   so far (the reference's running-mean update), averaged over the mask.
+   out[nframes], A: the value qcalc prints at each frame. */
+int qgpu_calc_rmsf(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
+                   double *out);
 /* Centre of mass of the masked atoms (calc_com.f90 COM_calc); mass per atom
    (natom).  out[nframes*3]. */
 int qgpu_calc_com(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,

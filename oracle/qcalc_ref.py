@@ -6,6 +6,7 @@ entry points.  Each function follows one calc_* module of the reference
 (qusers/qsource, Q 5.06) frame by frame, in plain numpy:
   rms   calc_rms.f90 rms_calc      sqrt(sum((x - x0)**2) / n), no fit
   com   calc_com.f90 COM_calc      dot_product(x, mass) / total mass
+  rmsf  calc_rmsf.f90 RMSF_calc    running mean / mean square per atom
   geom  calc_geom.f90 dist_calc / angle_calc / torsion_calc (degrees)
   rdf   calc_rdf.f90 rdf_make_list + RDF_calc: the pair distance in real(4)
         (the FP64 difference rounded to single precision, minimum image in
@@ -26,6 +27,27 @@ def rms(frames, mask, x0):
         x = fr.reshape(-1, 3)[m]
         out.append(math.sqrt(float(np.sum((x - x0) ** 2)) / len(m)))
     return np.array(out)
+
+
+def rmsf(frames, mask):
+    """calc_rmsf.f90 RMSF_calc (:56-80), frame by frame: x2 += x**2,
+    x0 = x0*(1 - 1/n) + x/n, rmsf(atom) = sqrt(1/n*sum(x2) - sum(x0**2)),
+    the printed value (1/N)*sum(rmsf) over the mask after each frame."""
+    fr = np.asarray(frames, dtype=np.float64)
+    nf = fr.shape[0]
+    fr = fr.reshape(nf, -1, 3)
+    m = np.asarray(mask)
+    x0 = np.zeros((len(m), 3))
+    x2 = np.zeros((len(m), 3))
+    out = np.zeros(nf)
+    for f in range(nf):
+        n = float(f + 1)
+        x = fr[f, m]
+        x2 = x2 + x ** 2
+        x0 = x0 * (1.0 - 1.0 / n) + x / n
+        r = np.sqrt(1.0 / n * x2.sum(axis=1) - (x0 ** 2).sum(axis=1))
+        out[f] = 1.0 / len(m) * r.sum()
+    return out
 
 
 def com(frames, mask, mass):

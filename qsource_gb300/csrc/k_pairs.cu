@@ -412,8 +412,11 @@ __device__ __forceinline__ PairFlags pair_flags(const DevSys &S, int i, int j) {
 #ifndef QG_PPB
 #define QG_PPB 4   // solute atoms of a neighbour group loaded together
 #endif
+#ifndef QG_SOL_MINB
+#define QG_SOL_MINB 1   // k_nb_solute register bound (minimum resident blocks)
+#endif
 template <int E, int LW, bool BOX>
-__global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *satom, int lrf) {
+__global__ void __launch_bounds__(QG_BLOCK, QG_SOL_MINB) k_nb_solute(DevSys S, const int *satom, int lrf) {
     constexpr bool EACC = E == 1;
     __shared__ long long red[5][QG_BLOCK / 32];
     const int idx = (blockIdx.x * blockDim.x + threadIdx.x) / LW;
@@ -610,6 +613,7 @@ __global__ void __launch_bounds__(QG_BLOCK) k_nb_solute(DevSys S, const int *sat
 // chosen per launch: more lanes when the Q atoms are many or the items few.
 struct QShared {
     float4 qh[QG_MAXQ], ql[QG_MAXQ];
+    int qa[QG_MAXQ], qt[QG_MAXQ];   // Q atom index and its LJ type
     float qf[QG_BLOCK / 32][QG_MAXQ][3];
     long long red[2 * QG_MAXS][QG_BLOCK / 32];
 };
@@ -641,6 +645,7 @@ __device__ __forceinline__ void q_load(const DevSys &S, const TrajInfo &T, QShar
     for (int k = threadIdx.x; k < T.nqat; k += blockDim.x) {
         const int a = S.q_atom[T.q0 + k];
         sh.qh[k] = S.pos[a]; sh.ql[k] = S.poslo[a];
+        sh.qa[k] = a; sh.qt[k] = S.atype[a];
     }
     __syncthreads();
 }
@@ -862,16 +867,19 @@ __global__ void __launch_bounds__(QG_BLOCK, E == 2 ? 6 : 1) k_qp(DevSys S, const
     }
     float gx = 0.f, gy = 0.f, gz = 0.f;
     const int ntq = T.natyps + T.nqat;
+    // per solute atom, loaded once: its LJ row and its 1-4 Q partners
+    const int ljrow = T.lj0 + (tj - T.type0) * T.natyps - T.type0;
+    const int p14a = valid ? S.qp14_first[j] : 0, p14b = valid ? S.qp14_first[j + 1] : 0;
     for (int iq0 = 0; iq0 < T.nqat; iq0 += LG) {
         const int iq = iq0 + lane;
         const bool on = iq < T.nqat;
         float qfx = 0.f, qfy = 0.f, qfz = 0.f;
         if (valid && on) {
             const int q = T.q0 + iq;
-            const int qa = S.q_atom[q];
-            const int tq = S.atype[qa];
-            int c = ljc(S, T, tj, tq);
-            for (int k = S.qp14_first[j]; k < S.qp14_first[j + 1]; ++k)
+            const int qa = sh.qa[iq];
+            const int tq = sh.qt[iq];
+            int c = S.ljcod[ljrow + tq];
+            for (int k = p14a; k < p14b; ++k)
                 if (S.qp14_q[k] == q) c = 3;
             const int qc = c == 2 ? 1 : c;
             const float3 d = f3sub(dpos(sh.qh[iq], sh.ql[iq], jh, jl), sq);

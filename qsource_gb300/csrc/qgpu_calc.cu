@@ -12,7 +12,10 @@
 //     RDF_calc: every pair of a mask-1 atom and a different mask-2 atom; the
 //     distance in single precision and the bin index dist/radius*Nbins + 1 in
 //     double, as the reference's real/real(8) mix; minimum image in a box);
-//   * centre of mass of a mask (calc_com.f90 COM_calc).
+//   * centre of mass of a mask (calc_com.f90 COM_calc);
+//   * RMS fluctuation of a mask (calc_rmsf.f90 RMSF_calc): per atom the
+//     running mean and mean square over the frames so far, the frame's value
+//     the mean over the mask.
 // Sums run in FP64 with a fixed reduction order (deterministic); RDF bins are
 // integer counts.
 #include <math.h>
@@ -55,6 +58,40 @@ __device__ double block_sum(double v, double *sh) {
     const double r = sh[0];
     __syncthreads();
     return r;
+}
+
+// RMSF_calc (calc_rmsf.f90:56-80): one thread per masked atom, frames in
+// order.  The running mean takes the reference's update x0 <- x0 (1 - 1/n) +
+// x/n, the squares a running sum; after frame n the atom's fluctuation is
+// sqrt(1/n sum_k x2_k - sum_k x0_k^2), stored as scr[f * nmask + k].  Each
+// operation is rounded on its own, in the reference's order (no fused
+// multiply-add): the difference of the two sums is exactly zero at the first
+// frame, as in the reference, instead of a rounding residue of either sign.
+__global__ void k_calc_rmsf_atoms(const double *fr, int natom, int nframes, const int *mask, int nmask, double *scr) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nmask) return;
+    const int a = mask[k];
+    double x0[3] = {0.0, 0.0, 0.0}, x2[3] = {0.0, 0.0, 0.0};
+    for (int f = 0; f < nframes; ++f) {
+        const double n = (double)(f + 1), rn = __ddiv_rn(1.0, n);
+        const double *x = fr + ((size_t)f * natom + a) * 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            x2[c] = __dadd_rn(x2[c], __dmul_rn(x[c], x[c]));
+            x0[c] = __dadd_rn(__dmul_rn(x0[c], __dsub_rn(1.0, rn)), __ddiv_rn(x[c], n));
+        }
+        const double s2 = __dadd_rn(__dadd_rn(x2[0], x2[1]), x2[2]);
+        const double s0 = __dadd_rn(__dadd_rn(__dmul_rn(x0[0], x0[0]), __dmul_rn(x0[1], x0[1])), __dmul_rn(x0[2], x0[2]));
+        scr[(size_t)f * nmask + k] = sqrt(__dsub_rn(__dmul_rn(rn, s2), s0));
+    }
+}
+// the frame's value: (1/nmask) * the sum over the mask, one block per frame
+__global__ void k_calc_rmsf_frames(const double *scr, int nmask, double *out) {
+    __shared__ double sh[QC_T];
+    double v = 0.0;
+    for (int k = threadIdx.x; k < nmask; k += blockDim.x) v += scr[(size_t)blockIdx.x * nmask + k];
+    const double sum = block_sum(v, sh);
+    if (threadIdx.x == 0) out[blockIdx.x] = 1.0 / nmask * sum;
 }
 
 // rms_calc (calc_rms.f90): one block per frame
@@ -222,6 +259,25 @@ int qgpu_calc_rms(const double *frames, int32_t nframes, int32_t natom, const in
     CKC(B.up(mask, (size_t)nmask, &m));
     CKC(B.zero((size_t)nframes, &o));
     k_calc_rms<<<nframes, QC_T>>>(fr, natom, m, nmask, x0, o);
+    CKC(cudaGetLastError());
+    CKC(cudaMemcpy(out, o, (size_t)nframes * sizeof(double), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int qgpu_calc_rmsf(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
+                   double *out) {
+    if (!frames || nframes < 1 || natom < 1 || !mask || nmask < 1 || !out || check_atoms(mask, nmask, natom))
+        return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_rmsf: bad arguments");
+    DevBuf B;
+    double *fr, *scr, *o;
+    int *m;
+    CKC(B.up(frames, (size_t)nframes * 3 * natom, &fr));
+    CKC(B.up(mask, (size_t)nmask, &m));
+    CKC(B.zero((size_t)nframes * nmask, &scr));
+    CKC(B.zero((size_t)nframes, &o));
+    k_calc_rmsf_atoms<<<(nmask + QC_T - 1) / QC_T, QC_T>>>(fr, natom, nframes, m, nmask, scr);
+    CKC(cudaGetLastError());
+    k_calc_rmsf_frames<<<nframes, QC_T>>>(scr, nmask, o);
     CKC(cudaGetLastError());
     CKC(cudaMemcpy(out, o, (size_t)nframes * sizeof(double), cudaMemcpyDeviceToHost));
     return 0;

@@ -117,6 +117,14 @@ class Calc:
         self._check(self.lib.qgpu_calc_rms(abi.ptr(fr), nf, na, abi.ptr(m), len(m), abi.ptr(x0), abi.ptr(out)))
         return out
 
+    def rmsf(self, frames, mask) -> np.ndarray:
+        """RMS fluctuation of the mask after each frame (calc_rmsf.f90)."""
+        fr, nf, na = self._frames(frames)
+        m = np.ascontiguousarray(mask, dtype=np.int32)
+        out = np.zeros(nf)
+        self._check(self.lib.qgpu_calc_rmsf(abi.ptr(fr), nf, na, abi.ptr(m), len(m), abi.ptr(out)))
+        return out
+
     def com(self, frames, mask, mass) -> np.ndarray:
         fr, nf, na = self._frames(frames)
         m = np.ascontiguousarray(mask, dtype=np.int32)

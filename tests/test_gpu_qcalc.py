@@ -49,6 +49,20 @@ def test_rms_com_geom_match_oracle(droplet):
     assert np.allclose(c.geom(fr, meas), ref.geom(fr, meas), rtol=1e-10, atol=1e-9)
 
 
+def test_rmsf_matches_oracle(droplet):
+    """RMS fluctuation after every frame (calc_rmsf.f90 RMSF_calc), the value
+    qcalc prints per frame: the first frame's is zero, later ones grow with
+    the spread of the positions."""
+    from oracle import qcalc_ref as ref
+    from qsource_gb300.qcalc import Calc
+    s, fr = droplet
+    mask = np.arange(0, s.natom, 3)
+    got = Calc().rmsf(fr, mask)
+    want = ref.rmsf(fr, mask)
+    assert np.allclose(got, want, rtol=1e-9, atol=1e-12)
+    assert abs(got[0]) < 1e-6 and got[-1] > 0
+
+
 def test_rdf_counts_match_oracle_sphere(droplet):
     from oracle import qcalc_ref as ref
     from qsource_gb300.qcalc import Calc

@@ -42,3 +42,15 @@ def test_rdf_counts_known_answers():
     # in a 3 A box the (0, 2) pair is 1 A apart through the boundary
     c = rdf_counts(x, [0, 1, 2], [0, 1, 2], radius=4.0, nbins=4, box=[3.0, 3.0, 3.0])
     assert list(c) == [0, 6, 0, 0]
+
+
+def test_rmsf_known_answer():
+    """Two atoms alternating between two positions 2 A apart along x: after
+    an even number of frames each atom's fluctuation is 1 A."""
+    from oracle import qcalc_ref as ref
+    frames = np.zeros((4, 2, 3))
+    frames[0::2, :, 0] = 0.0
+    frames[1::2, :, 0] = 2.0
+    got = ref.rmsf(frames.reshape(4, -1), [0, 1])
+    assert got[0] == 0.0
+    assert abs(got[1] - 1.0) < 1e-12 and abs(got[3] - 1.0) < 1e-12
