@@ -567,6 +567,17 @@ int qgpu_calc_rms(const double *frames, int32_t nframes, int32_t natom, const in
    out[nframes], A: the value qcalc prints at each frame. */
 int qgpu_calc_rmsf(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
                    double *out);
+/* Least-squares fit (calc_fit.f90 fit_calc, LSQSTR): every frame's solute
+   atoms (the first nsol) superposed on the topology coordinates xref by the
+   mass-weighted fit of the masked atoms (mask: solute atom indices), the
+   rotation from the eigenvectors of [[0, U], [U^T, 0]] with U the correlation
+   of the centred, sqrt(mass)-weighted coordinates; solvent atoms copied.
+   out[nframes*3*natom] the fitted frames (the coordinates qcalc's later
+   calculations of the frame see); status[nframes] 0, 1 (|det U| < 1e-9) or 2
+   (det U < 0 with a degenerate pair), where the frame is only moved to the
+   reference's centre of mass, as qcalc leaves it. */
+int qgpu_calc_fit(const double *frames, int32_t nframes, int32_t natom, int32_t nsol, const int32_t *mask,
+                  int32_t nmask, const double *mass, const double *xref, double *out, int32_t *status);
 /* Centre of mass of the masked atoms (calc_com.f90 COM_calc); mass per atom
    (natom).  out[nframes*3]. */
 int qgpu_calc_com(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,

@@ -7,6 +7,7 @@ entry points.  Each function follows one calc_* module of the reference
   rms   calc_rms.f90 rms_calc      sqrt(sum((x - x0)**2) / n), no fit
   com   calc_com.f90 COM_calc      dot_product(x, mass) / total mass
   rmsf  calc_rmsf.f90 RMSF_calc    running mean / mean square per atom
+  fit   calc_fit.f90 fit_calc      mass-weighted least-squares superposition
   geom  calc_geom.f90 dist_calc / angle_calc / torsion_calc (degrees)
   rdf   calc_rdf.f90 rdf_make_list + RDF_calc: the pair distance in real(4)
         (the FP64 difference rounded to single precision, minimum image in
@@ -48,6 +49,44 @@ def rmsf(frames, mask):
         r = np.sqrt(1.0 / n * x2.sum(axis=1) - (x0 ** 2).sum(axis=1))
         out[f] = 1.0 / len(m) * r.sum()
     return out
+
+
+def fit(frames, nsol, mask, mass, xref):
+    """calc_fit.f90 fit_calc + LSQSTR, frame by frame: centre the solute on the
+    mask's centre of mass, weight by sqrt(mass), U = sum over the mask of
+    X XP^T, rotation R = B diag(1, 1, sign det U) A^T from the singular value
+    decomposition U = A S B^T (the three largest eigenpairs of [[0, U],
+    [U^T, 0]] in LSQSTR), X <- R X, x = X/sqrt(m) + xrcm.  Status 1 when
+    |det U| < 1e-9, 2 when det U < 0 and the two smallest singular values are
+    within 1e-5: the frame is then only moved to xrcm."""
+    fr = np.asarray(frames, dtype=np.float64)
+    nf = fr.shape[0]
+    fr = fr.reshape(nf, -1, 3)
+    m = np.asarray(mask)
+    ms = np.asarray(mass, dtype=np.float64)
+    x0 = np.asarray(xref, dtype=np.float64).reshape(-1, 3)
+    sq = np.sqrt(ms[:nsol])[:, None]
+    xrcm = (x0[m] * ms[m][:, None]).sum(axis=0) / ms[m].sum()
+    xp = (x0[:nsol] - xrcm) * sq
+    out = fr.copy()
+    status = np.zeros(nf, dtype=np.int32)
+    for f in range(nf):
+        x = fr[f]
+        xcm = (x[m] * ms[m][:, None]).sum(axis=0) / ms[m].sum()
+        X = (x[:nsol] - xcm) * sq
+        U = X[m].T @ xp[m]
+        du = np.linalg.det(U)
+        R = np.eye(3)
+        if abs(du) < 1e-9:
+            status[f] = 1
+        else:
+            a, sv, bt = np.linalg.svd(U)
+            if du < 0 and abs(sv[1] - sv[2]) < 1e-5:
+                status[f] = 2
+            else:
+                R = bt.T @ np.diag([1.0, 1.0, np.sign(du)]) @ a.T
+        out[f, :nsol] = (X @ R.T) / sq + xrcm
+    return out.reshape(nf, -1), status
 
 
 def com(frames, mask, mass):

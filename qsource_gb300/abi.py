@@ -157,6 +157,7 @@ EXPORTS = {
     "qgpu_calc_rms": (_i32, [_P, _i32, _i32, _P, _i32, _P, _P]),
     "qgpu_calc_com": (_i32, [_P, _i32, _i32, _P, _i32, _P, _P]),
     "qgpu_calc_rmsf": (_i32, [_P, _i32, _i32, _P, _i32, _P]),
+    "qgpu_calc_fit": (_i32, [_P, _i32, _i32, _i32, _P, _i32, _P, _P, _P, _P]),
     "qgpu_calc_geom": (_i32, [_P, _i32, _i32, _i32, _P, _P, _P]),
     "qgpu_calc_rdf": (_i32, [_P, _i32, _i32, _P, _i32, _P, _i32, _f64, _i32, _P, _P]),
     "qgpu_ene_open": (_i32, [C.c_void_p, _i32, C.c_char_p]),

@@ -15,7 +15,12 @@
 //   * centre of mass of a mask (calc_com.f90 COM_calc);
 //   * RMS fluctuation of a mask (calc_rmsf.f90 RMSF_calc): per atom the
 //     running mean and mean square over the frames so far, the frame's value
-//     the mean over the mask.
+//     the mean over the mask;
+//   * least-squares fit of the solute onto the topology coordinates
+//     (calc_fit.f90 fit_calc / LSQSTR): mass-weighted superposition of a mask;
+//     the centres and correlation matrices of all frames on the device, the
+//     rotation from each frame's six-dimensional eigenproblem on the host, and
+//     the rotation of every solute atom of every frame on the device.
 // Sums run in FP64 with a fixed reduction order (deterministic); RDF bins are
 // integer counts.
 #include <math.h>
@@ -92,6 +97,141 @@ __global__ void k_calc_rmsf_frames(const double *scr, int nmask, double *out) {
     for (int k = threadIdx.x; k < nmask; k += blockDim.x) v += scr[(size_t)blockIdx.x * nmask + k];
     const double sum = block_sum(v, sh);
     if (threadIdx.x == 0) out[blockIdx.x] = 1.0 / nmask * sum;
+}
+
+// Eigenvalues (descending) and eigenvectors (columns of V) of the symmetric
+// 6x6 matrix A by cyclic Jacobi rotations (at most 60 sweeps, stopping when
+// the off-diagonal sum of squares falls below 1e-30 of the total); A is
+// overwritten.  Host code: the fit's six-dimensional eigenproblem is solved
+// per frame on the host, between the two device passes.
+static void jacobi6(double (&A)[6][6], double (&V)[6][6], double (&ev)[6]) {
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) V[i][j] = i == j ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) {
+                tot += A[i][j] * A[i][j];
+                if (i != j) off += A[i][j] * A[i][j];
+            }
+        if (!(off > 1e-30 * tot)) break;
+        for (int p = 0; p < 5; ++p)
+            for (int q = p + 1; q < 6; ++q) {
+                const double apq = A[p][q];
+                if (apq == 0.0) continue;
+                const double app = A[p][p], aqq = A[q][q];
+                const double th = (aqq - app) / (2.0 * apq);
+                const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+                for (int k = 0; k < 6; ++k) {
+                    if (k == p || k == q) continue;
+                    const double akp = A[k][p], akq = A[k][q];
+                    const double np = c * akp - sn * akq, nq = sn * akp + c * akq;
+                    A[k][p] = np; A[p][k] = np;
+                    A[k][q] = nq; A[q][k] = nq;
+                }
+                A[p][p] = app - t * apq;
+                A[q][q] = aqq + t * apq;
+                A[p][q] = 0.0; A[q][p] = 0.0;
+                for (int k = 0; k < 6; ++k) {
+                    const double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - sn * vkq;
+                    V[k][q] = sn * vkp + c * vkq;
+                }
+            }
+    }
+    for (int i = 0; i < 6; ++i) ev[i] = A[i][i];
+    for (int i = 0; i < 5; ++i) {   // descending (selection sort of the pairs)
+        int m = i;
+        for (int j = i + 1; j < 6; ++j)
+            if (ev[j] > ev[m]) m = j;
+        if (m != i) {
+            const double e = ev[i]; ev[i] = ev[m]; ev[m] = e;
+            for (int k = 0; k < 6; ++k) { const double v = V[k][i]; V[k][i] = V[k][m]; V[k][m] = v; }
+        }
+    }
+}
+
+// LSQSTR (calc_fit.f90:188-283) from the correlation matrix U: status 0 and
+// the rotation R = sum_k b_k a_k^T over the three largest eigenpairs (a; b)
+// of [[0, U], [U^T, 0]] (each half scaled by sqrt 2; the third with the sign
+// of det U); 1 when |det U| < 1e-9; 2 when det U < 0 and the second and third
+// eigenvalues are within 1e-5.  R is the identity unless the status is 0.
+static int lsq_rotation(const double (&U)[3][3], double (&R)[3][3]) {
+    const double du = U[0][0] * U[1][1] * U[2][2] + U[0][2] * U[1][0] * U[2][1] + U[0][1] * U[1][2] * U[2][0] -
+                      U[2][0] * U[1][1] * U[0][2] - U[2][2] * U[1][0] * U[0][1] - U[2][1] * U[1][2] * U[0][0];
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) R[r][q] = r == q ? 1.0 : 0.0;
+    if (fabs(du) < 1e-9) return 1;
+    double A[6][6] = {}, V[6][6], ev[6];
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) { A[r][3 + q] = U[r][q]; A[3 + q][r] = U[r][q]; }
+    jacobi6(A, V, ev);
+    if (du < 0.0 && fabs(ev[1] - ev[2]) < 1e-5) return 2;
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < 3; ++q) {
+            double v = 0.0;
+            for (int k = 0; k < 3; ++k) v += (k == 2 && du < 0.0 ? -2.0 : 2.0) * V[3 + r][k] * V[q][k];
+            R[r][q] = v;
+        }
+    return 0;
+}
+
+// fit_calc (calc_fit.f90:86-130), first device pass, one block per frame: the
+// mass-weighted centre xcm of the mask and the correlation matrix U(r, s) =
+// sum over the mask of X_r XP_s, X = (x - xcm) sqrt(m), XP the topology
+// coordinates treated the same way about their own centre.  cu[12 f ..]:
+// xcm, then U row by row.
+__global__ void k_calc_fit_corr(const double *fr, int natom, const int *mask, int nmask, const double *mass,
+                                const double *xp, double *cu) {
+    __shared__ double sh[QC_T];
+    __shared__ double s_cm[3];
+    const double *x = fr + (size_t)blockIdx.x * 3 * natom;
+    double c[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int k = threadIdx.x; k < nmask; k += blockDim.x) {
+        const int a = mask[k];
+        const double m = mass[a];
+        c[0] += x[3 * a] * m; c[1] += x[3 * a + 1] * m; c[2] += x[3 * a + 2] * m; c[3] += m;
+    }
+    double cm[4];
+    for (int q = 0; q < 4; ++q) cm[q] = block_sum(c[q], sh);
+    if (threadIdx.x == 0)
+        for (int r = 0; r < 3; ++r) { s_cm[r] = cm[r] / cm[3]; cu[12 * (size_t)blockIdx.x + r] = s_cm[r]; }
+    __syncthreads();
+    double u[9];
+    for (int q = 0; q < 9; ++q) u[q] = 0.0;
+    for (int k = threadIdx.x; k < nmask; k += blockDim.x) {
+        const int a = mask[k];
+        const double sm = sqrt(mass[a]);
+        double X[3];
+        for (int r = 0; r < 3; ++r) X[r] = (x[3 * a + r] - s_cm[r]) * sm;
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) u[3 * r + q] += X[r] * xp[3 * a + q];
+    }
+    for (int q = 0; q < 9; ++q) {
+        const double v = block_sum(u[q], sh);
+        if (threadIdx.x == 0) cu[12 * (size_t)blockIdx.x + 3 + q] = v;
+    }
+}
+// second device pass: every solute atom X = (x - xcm) sqrt(m) becomes
+// R X / sqrt(m) + xrcm (rot[12 f ..]: xcm, then R row by row); solvent
+// atoms are copied
+__global__ void k_calc_fit_apply(const double *fr, int natom, int nsol, const double *mass, const double *rot,
+                                 const double *xrcm, double *out) {
+    const double *x = fr + (size_t)blockIdx.x * 3 * natom;
+    double *y = out + (size_t)blockIdx.x * 3 * natom;
+    const double *f = rot + 12 * (size_t)blockIdx.x;
+    for (int a = threadIdx.x; a < natom; a += blockDim.x) {
+        if (a >= nsol) {
+            for (int r = 0; r < 3; ++r) y[3 * a + r] = x[3 * a + r];
+            continue;
+        }
+        const double sm = sqrt(mass[a]);
+        double X[3];
+        for (int r = 0; r < 3; ++r) X[r] = (x[3 * a + r] - f[r]) * sm;
+        for (int r = 0; r < 3; ++r)
+            y[3 * a + r] = (f[3 + 3 * r] * X[0] + f[4 + 3 * r] * X[1] + f[5 + 3 * r] * X[2]) / sm + xrcm[r];
+    }
 }
 
 // rms_calc (calc_rms.f90): one block per frame
@@ -280,6 +420,54 @@ int qgpu_calc_rmsf(const double *frames, int32_t nframes, int32_t natom, const i
     k_calc_rmsf_frames<<<nframes, QC_T>>>(scr, nmask, o);
     CKC(cudaGetLastError());
     CKC(cudaMemcpy(out, o, (size_t)nframes * sizeof(double), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int qgpu_calc_fit(const double *frames, int32_t nframes, int32_t natom, int32_t nsol, const int32_t *mask,
+                  int32_t nmask, const double *mass, const double *xref, double *out, int32_t *status) {
+    if (!frames || nframes < 1 || natom < 1 || nsol < 1 || nsol > natom || !mask || nmask < 1 || !mass || !xref ||
+        !out || !status || check_atoms(mask, nmask, nsol))
+        return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_fit: bad arguments");
+    // the reference frame (fit_make_ref, calc_fit.f90:133-155): its centre of
+    // mass over the mask and every solute atom's (xtop - xrcm) sqrt(m)
+    double xrcm[3] = {0.0, 0.0, 0.0}, tm = 0.0;
+    for (int k = 0; k < nmask; ++k) {
+        const int a = mask[k];
+        for (int r = 0; r < 3; ++r) xrcm[r] += xref[3 * a + r] * mass[a];
+        tm += mass[a];
+    }
+    if (!(tm > 0.0)) return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_fit: zero mass");
+    for (int r = 0; r < 3; ++r) xrcm[r] = xrcm[r] / tm;
+    std::vector<double> xp(3 * (size_t)natom, 0.0);
+    for (int a = 0; a < nsol; ++a)
+        for (int r = 0; r < 3; ++r) xp[3 * a + r] = (xref[3 * a + r] - xrcm[r]) * sqrt(mass[a]);
+    DevBuf B;
+    double *fr, *ms, *xpd, *rc, *o, *cu, *rot;
+    int *m;
+    CKC(B.up(frames, (size_t)nframes * 3 * natom, &fr));
+    CKC(B.up(mass, (size_t)natom, &ms));
+    CKC(B.up(xp.data(), xp.size(), &xpd));
+    CKC(B.up(xrcm, (size_t)3, &rc));
+    CKC(B.up(mask, (size_t)nmask, &m));
+    CKC(B.zero((size_t)nframes * 3 * natom, &o));
+    CKC(B.zero((size_t)nframes * 12, &cu));
+    k_calc_fit_corr<<<nframes, QC_T>>>(fr, natom, m, nmask, ms, xpd, cu);
+    CKC(cudaGetLastError());
+    // the per-frame 6x6 eigenproblems on the host
+    std::vector<double> h((size_t)nframes * 12);
+    CKC(cudaMemcpy(h.data(), cu, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int f = 0; f < nframes; ++f) {
+        double U[3][3], R[3][3];
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) U[r][q] = h[12 * (size_t)f + 3 + 3 * r + q];
+        status[f] = lsq_rotation(U, R);
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) h[12 * (size_t)f + 3 + 3 * r + q] = R[r][q];
+    }
+    CKC(B.up(h.data(), h.size(), &rot));
+    k_calc_fit_apply<<<nframes, QC_T>>>(fr, natom, nsol, ms, rot, rc, o);
+    CKC(cudaGetLastError());
+    CKC(cudaMemcpy(out, o, (size_t)nframes * 3 * natom * sizeof(double), cudaMemcpyDeviceToHost));
     return 0;
 }
 

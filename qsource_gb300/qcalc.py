@@ -125,6 +125,19 @@ class Calc:
         self._check(self.lib.qgpu_calc_rmsf(abi.ptr(fr), nf, na, abi.ptr(m), len(m), abi.ptr(out)))
         return out
 
+    def fit(self, frames, nsol: int, mask, mass, xref):
+        """Frames with their solute superposed on xref (calc_fit.f90), and the
+        per-frame status (0 fitted; 1, 2 only moved, as qcalc)."""
+        fr, nf, na = self._frames(frames)
+        m = np.ascontiguousarray(mask, dtype=np.int32)
+        ms = np.ascontiguousarray(mass, dtype=np.float64)
+        x0 = np.ascontiguousarray(xref, dtype=np.float64)
+        out = np.zeros((nf, 3 * na))
+        st = np.zeros(nf, dtype=np.int32)
+        self._check(self.lib.qgpu_calc_fit(abi.ptr(fr), nf, na, int(nsol), abi.ptr(m), len(m), abi.ptr(ms),
+                                           abi.ptr(x0), abi.ptr(out), abi.ptr(st)))
+        return out, st
+
     def com(self, frames, mask, mass) -> np.ndarray:
         fr, nf, na = self._frames(frames)
         m = np.ascontiguousarray(mask, dtype=np.int32)

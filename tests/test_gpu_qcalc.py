@@ -63,6 +63,36 @@ def test_rmsf_matches_oracle(droplet):
     assert abs(got[0]) < 1e-6 and got[-1] > 0
 
 
+def test_fit_matches_oracle(droplet):
+    """Least-squares fit of the solute (calc_fit.f90): the engine's frames and
+    rigidly moved copies of the topology coordinates (fitted back onto them
+    to 1e-9 A), against the restatement."""
+    from oracle import qcalc_ref as ref
+    from qsource_gb300.qcalc import Calc
+    s, fr = droplet
+    ns = int(s.nat_solute)
+    mass = np.asarray(s.mass)[np.asarray(s.iac)]
+    mask = np.arange(ns)
+    got, st = Calc().fit(fr, ns, mask, mass, s.xtop)
+    want, wst = ref.fit(fr, ns, mask, mass, s.xtop)
+    assert np.array_equal(st, wst)
+    assert np.abs(got - want).max() < 1e-9
+    # rigid copies of the reference come back onto it
+    rng = np.random.default_rng(9)
+    x0 = np.asarray(s.xtop).reshape(-1, 3)
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, a, b, c = q
+    R = np.array([[1 - 2 * (b * b + c * c), 2 * (a * b - c * w), 2 * (a * c + b * w)],
+                  [2 * (a * b + c * w), 1 - 2 * (a * a + c * c), 2 * (b * c - a * w)],
+                  [2 * (a * c - b * w), 2 * (b * c + a * w), 1 - 2 * (a * a + b * b)]])
+    moved = x0.copy()
+    moved[:ns] = x0[:ns] @ R.T + np.array([3.0, -2.0, 7.5])
+    back, st2 = Calc().fit(moved.ravel()[None, :], ns, mask, mass, s.xtop)
+    assert st2[0] == 0
+    assert np.abs(back.reshape(-1, 3)[:ns] - x0[:ns]).max() < 1e-9
+
+
 def test_rdf_counts_match_oracle_sphere(droplet):
     from oracle import qcalc_ref as ref
     from qsource_gb300.qcalc import Calc

@@ -54,3 +54,34 @@ def test_rmsf_known_answer():
     got = ref.rmsf(frames.reshape(4, -1), [0, 1])
     assert got[0] == 0.0
     assert abs(got[1] - 1.0) < 1e-12 and abs(got[3] - 1.0) < 1e-12
+
+
+def _rotation(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def test_fit_known_answer():
+    """Frames that are rigid rotations and translations of the reference are
+    fitted back onto it exactly; solvent atoms are left alone."""
+    from oracle import qcalc_ref as ref
+    rng = np.random.default_rng(5)
+    nsol, natom = 12, 15
+    xref = rng.normal(0, 3, size=(natom, 3))
+    mass = rng.uniform(1, 16, size=natom)
+    frames = []
+    for _ in range(3):
+        R, t = _rotation(rng), rng.normal(0, 5, size=3)
+        fr = xref.copy()
+        fr[:nsol] = xref[:nsol] @ R.T + t
+        frames.append(fr.ravel())
+    out, st = ref.fit(np.array(frames), nsol, np.arange(0, nsol, 2), mass, xref.ravel())
+    assert np.array_equal(st, [0, 0, 0])
+    for f in range(3):
+        got = out[f].reshape(-1, 3)
+        assert np.abs(got[:nsol] - xref[:nsol]).max() < 1e-10
+        assert np.array_equal(got[nsol:], np.array(frames[f]).reshape(-1, 3)[nsol:])
