@@ -595,6 +595,21 @@ int qgpu_calc_geom(const double *frames, int32_t nframes, int32_t natom, int32_t
    atoms) is the caller's.  nbins <= 8192, nframes <= 65535. */
 int qgpu_calc_rdf(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask1, int32_t n1,
                   const int32_t *mask2, int32_t n2, double radius, int32_t nbins, const double *box, int64_t *counts);
+/* Nonbonded energies between two atom masks (calc_nb.f90 nb_calc_lists,
+   replaces the per-frame call at qcalc.f90:745): for each frame the sums over
+   the npair pairs (pairs[2*p], pairs[2*p+1]) of
+     Vlj += lambdas[s]*(AA*r^-12 - BB*r^-6)                      (arith 0)
+     Vlj += lambdas[s]*(sqrt(BB)*AA^6*r^-6*(AA^6*r^-6 - 2))       (arith 1)
+     Vel += lambdas[s]*qq/r
+   over the states s < nstates, with the per-pair products AA, BB, qq stored
+   pair-major ([p*nstates + s]; one state with lambdas {1} for the plain
+   topology form).  A pair at r = 0 adds nothing.  The list and its products
+   are the caller's (nb_make_list, calc_nb.f90:334-759, built once before the
+   frames).  out[2*nframes]: (Vlj, Vel) per frame, kcal/mol.  nframes <=
+   65535. */
+int qgpu_calc_nb(const double *frames, int32_t nframes, int32_t natom, int64_t npair, const int32_t *pairs,
+                 int32_t nstates, const double *lambdas, const double *AA, const double *BB, const double *qq,
+                 int32_t arith, double *out);
 
 #ifdef __cplusplus
 }

@@ -13,6 +13,9 @@ entry points.  Each function follows one calc_* module of the reference
         (the FP64 difference rounded to single precision, minimum image in
         double rounded again, dot product and sqrt in single precision),
         bin int(dist/radius*Nbins + 1) in double
+  nb    calc_nb.f90 nb_make_list + nb_calc_lists: the pair list between two
+        masks with its LJ and charge products, and per frame the summed
+        LJ and Coulomb energies, in plain Python loops
 The reference ships no qcalc test data, so these restatements are the pin.
 """
 import math
@@ -144,3 +147,125 @@ def rdf_counts(frames, mask1, mask2, radius, nbins, box=None):
         bins = bins[(bins >= 0) & (bins < nbins)]
         counts += np.bincount(bins, minlength=nbins)[:nbins]
     return counts
+
+
+def nb_make_list(g, mask1, mask2, fep=False):
+    """calc_nb.f90 nb_make_list (:334-759), pair by pair in the reference's
+    loop order (every mask-1 atom, then every mask-2 atom, both ascending).
+
+    A pair is dropped when
+      * atom1 >= atom2 and atom2 is in both masks (:401-410; the pairs inside
+        the overlap are taken once, and also any pair whose second atom is in
+        the overlap and whose first atom has the larger index);
+      * the two atoms share an angle of the topology (:412-425).
+    LJ code: the topology's type pair code (1, or 2 for the polar pairs),
+    3 for a 1-4 pair (:442-461).  Per state s (one state without fep):
+      geometric rule  AA = a1*a2, BB = b1*b2;  arithmetic rule AA = a1 + a2,
+      BB = b1*b2, with a, b the atom's parameters at the LJ code; a Q atom
+      (a solute atom with a Q index, fep only) takes its state's Q type and,
+      for code 2 with a non-Q partner, its code-1 value (:463-683);
+      charge product: fep q1*q2*(el14 scale if 1-4 else 1), Q atoms at their
+      state's charge (:684-740); without fep crg1*crg2*el14_scale for every
+      pair (:742, as the reference has it).
+    The charges of g carry sqrt(Coulomb constant), so the products are the
+    reference's charge product times the constant.
+    Returns (pairs [n, 2], AA [n, S], BB [n, S], qq [n, S])."""
+    natom, nsol = int(g.natom), int(g.nat_solute)
+    in1 = np.zeros(natom, bool); in1[np.asarray(mask1, dtype=np.int64)] = True
+    in2 = np.zeros(natom, bool); in2[np.asarray(mask2, dtype=np.int64)] = True
+    group1 = [j for j in range(natom) if in1[j]]
+    group2 = [k for k in range(natom) if in2[k]]
+    mutual = set(j for j in group1 if in2[j])
+    angles = [tuple(int(v) for v in a[:3]) for a in np.asarray(g.ang).reshape(len(g.ang), -1)] \
+        if len(g.ang) else []
+    p14 = set(tuple(sorted((int(a), int(b)))) for a, b in np.asarray(g.pairs14).reshape(-1, 2))
+    iac = np.asarray(g.iac)
+    avdw, bvdw = np.asarray(g.avdw), np.asarray(g.bvdw)
+    ljcod = np.asarray(g.ljcod)
+    crg = np.asarray(g.crg)
+    S = int(g.nstates) if fep else 1
+    iqatom = np.asarray(g.iqatom)
+    qiac, qcrg = np.asarray(g.qiac), np.asarray(g.qcrg)
+    qavdw, qbvdw = np.asarray(g.qavdw), np.asarray(g.qbvdw)
+    arith = int(getattr(g, "ivdw_rule", 1)) == 2
+    el14 = float(g.el14_scale)
+
+    def is_q(a):
+        return fep and a < nsol and iqatom[a] >= 0
+
+    pairs, AA, BB, QQ = [], [], [], []
+    for j in group1:
+        for k in group2:
+            if j >= k and k in mutual:
+                continue
+            if any((a == j and (b == k or c == k)) or (b == j and (a == k or c == k)) or
+                   (c == j and (a == k or b == k)) for a, b, c in angles):
+                continue
+            code = int(ljcod[iac[j], iac[k]])
+            if (min(j, k), max(j, k)) in p14:
+                code = 3
+            aa, bb, qq = [], [], []
+            for s in range(S):
+                par = []
+                for me, other in ((j, k), (k, j)):
+                    if is_q(me):
+                        c = 1 if (code == 2 and not is_q(other)) else code
+                        t = qiac[iqatom[me], s]
+                        par.append((qavdw[t, c - 1], qbvdw[t, c - 1], qcrg[iqatom[me], s]))
+                    else:
+                        par.append((avdw[iac[me], code - 1], bvdw[iac[me], code - 1], crg[me]))
+                (a1, b1, q1), (a2, b2, q2) = par
+                aa.append(a1 + a2 if arith else a1 * a2)
+                bb.append(b1 * b2)
+                if fep:
+                    qq.append(q1 * q2 * el14 if code == 3 else q1 * q2)
+                else:
+                    qq.append(q1 * q2 * el14)
+            pairs.append((j, k)); AA.append(aa); BB.append(bb); QQ.append(qq)
+    f = lambda v: np.array(v, dtype=np.float64).reshape(-1, S)
+    return np.array(pairs, dtype=np.int64).reshape(-1, 2), f(AA), f(BB), f(QQ)
+
+
+def nb_calc(frames, pairs, AA, BB, qq, lambdas=None, arith=False):
+    """calc_nb.f90 nb_calc_lists (:257-328): per frame, pair by pair in list
+    order, r = sqrt(dx**2 + dy**2 + dz**2); a pair at r = 0 adds nothing;
+    invr6 = invr**6 (six products), invr12 = invr6**2;
+      geometric  Vlj += lam_s*(AA*invr12 - BB*invr6)
+      arithmetic Vlj += lam_s*(sqrt(BB)*AA**6*invr6*(AA**6*invr6 - 2))
+      Vel += lam_s*qq*invr
+    over the states s (lam = 1 and one state without fep).
+    Returns [nframes, 2] (Vlj, Vel)."""
+    S = AA.shape[1]
+    lam = [1.0] if lambdas is None else [float(v) for v in lambdas]
+    out = []
+    for fr in np.asarray(frames, dtype=np.float64):
+        x = fr.reshape(-1, 3)
+        vlj = vel = 0.0
+        for p in range(len(pairs)):
+            j, k = int(pairs[p, 0]), int(pairs[p, 1])
+            r = math.sqrt((x[j, 0] - x[k, 0]) ** 2 + (x[j, 1] - x[k, 1]) ** 2 + (x[j, 2] - x[k, 2]) ** 2)
+            if r == 0:
+                continue
+            invr = 1.0 / r
+            invr6 = invr * invr * invr * invr * invr * invr
+            invr12 = invr6 * invr6
+            for s in range(S):
+                a, b = float(AA[p, s]), float(BB[p, s])
+                if arith:
+                    a6 = a ** 6
+                    vlj += lam[s] * (math.sqrt(b) * a6 * invr6 * (a6 * invr6 - 2.0))
+                else:
+                    vlj += lam[s] * (a * invr12 - b * invr6)
+                vel += lam[s] * (float(qq[p, s]) * invr)
+        out.append((vlj, vel))
+    return np.array(out, dtype=np.float64).reshape(-1, 2)
+
+
+def nb_averages(values):
+    """calc_nb.f90 nb_calc (:248-251): the running averages
+    ave = (ave*n + V)/(n + 1) after each frame; returns the last."""
+    ave, n = 0.0, 0
+    for v in values:
+        ave = (ave * n + float(v)) / (n + 1)
+        n += 1
+    return ave

@@ -933,6 +933,15 @@ __global__ void k_tick(int *rec_base, int n) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *rec_base += n;
 }
 
+// Writes the record control words from launch arguments: a copy from pageable
+// host memory would make the host wait for the stream.
+__global__ void k_set_ctl(int *ctl, int n, int a, int b) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        ctl[0] = a;
+        if (n > 1) ctl[1] = b;
+    }
+}
+
 __global__ void k_grad_to_double(DevSys S, double *out, int atom0, int n3) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n3) return;
@@ -992,6 +1001,12 @@ void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *
 void launch_tick(LaunchCtx &L, int *rec_base, int n) {
     prof_begin(L, "k_tick");
     k_tick<<<1, 32, 0, L.stream>>>(rec_base, n);
+    prof_end(L);
+    (*L.nlaunch)++;
+}
+void launch_set_ctl(LaunchCtx &L, int *ctl, int n, int a, int b) {
+    prof_begin(L, "k_set_ctl");
+    k_set_ctl<<<1, 32, 0, L.stream>>>(ctl, n, a, b);
     prof_end(L);
     (*L.nlaunch)++;
 }

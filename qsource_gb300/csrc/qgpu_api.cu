@@ -1586,7 +1586,7 @@ int qgpu_profile(qgpu_handle *h, int32_t nsteps, char *names, double *ms, int64_
     }
     const int ene_every = 1 << 30;
     int ctl[2] = {(int)h->step, (int)((h->step + ene_every - 1) / ene_every)};
-    CK(cudaMemcpyAsync(h->recctl_d, ctl, sizeof ctl, cudaMemcpyHostToDevice, h->stream));
+    launch_set_ctl(L, h->recctl_d, 2, ctl[0], ctl[1]);
     ensure_double(h, L);
     for (int k = 0; k < nsteps; ++k) {
         if (h->step % h->NBcycle == 0) { list_ops(h, L); h->lists_built = 1; }
@@ -1640,7 +1640,7 @@ int qgpu_enqueue(qgpu_handle *h, int32_t nsteps, int32_t ene_every) {
         h->temp_init = 1;
     }
     int ctl[2] = {(int)h->step, (int)((h->step + ene_every - 1) / ene_every)};
-    CK(cudaMemcpyAsync(h->recctl_d, ctl, sizeof ctl, cudaMemcpyHostToDevice, h->stream));
+    launch_set_ctl(L, h->recctl_d, 2, ctl[0], ctl[1]);
     const int NB = h->NBcycle;
     const long long end = h->step + nsteps;
     while (h->step < end) {
@@ -1817,8 +1817,9 @@ int qgpu_autotune(qgpu_handle *h, int32_t *tuning) {
 int qgpu_set_step(qgpu_handle *h, int64_t istep) {
     if (!h || istep < 0 || istep > 2000000000LL) return fail(QGPU_E_INVALID, "qgpu_set_step: bad arguments");
     h->step = istep;
-    const int ctl = (int)istep;
-    CK(cudaMemcpyAsync(h->recctl_d, &ctl, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    LaunchCtx L{h->stream, &h->nlaunch};
+    launch_set_ctl(L, h->recctl_d, 1, (int)istep);
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(h->stream));
     return 0;
 }
@@ -1984,7 +1985,7 @@ int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink si
         if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     }
     int ctl[2] = {(int)h->step, (int)((h->step + ene_every - 1) / ene_every)};
-    CK(cudaMemcpyAsync(h->recctl_d, ctl, sizeof ctl, cudaMemcpyHostToDevice, h->stream));
+    launch_set_ctl(L, h->recctl_d, 2, ctl[0], ctl[1]);
     int row0 = ctl[1];
     CK(cudaMemsetAsync(h->S.fx, 0, 3 * (size_t)h->S.natom * sizeof(unsigned long long), h->stream));
     CK(cudaMemsetAsync(h->S.eacc, 0, (size_t)h->ntraj * QG_NE * sizeof(unsigned long long), h->stream));
@@ -2033,8 +2034,7 @@ int qgpu_run(qgpu_handle *h, int32_t nsteps, int32_t ene_every, qgpu_ene_sink si
             if (int rc = check_status(h)) return rc;
             flush(h->step);
             row0 = (int)((h->step + ene_every - 1) / ene_every);
-            int c2[2] = {(int)h->step, row0};
-            CK(cudaMemcpyAsync(h->recctl_d, c2, sizeof c2, cudaMemcpyHostToDevice, h->stream));
+            launch_set_ctl(L, h->recctl_d, 2, (int)h->step, row0);
         }
         if (h->step % NB == 0 && end - h->step >= NB && h->lists_built) {
             if (int rc = replay_block(h, L, ene_every)) return rc;

@@ -371,6 +371,59 @@ __global__ void k_calc_rdf(const double *fr, int natom, const int *m1, int n1, c
         if (sb[k]) atomicAdd(&bins[k], (unsigned long long)sb[k]);
 }
 
+// nb_calc_lists (calc_nb.f90:257-328): block (c, f) sums pairs
+// [c*QC_NBCH, (c+1)*QC_NBCH) of the list at frame f, the per-state products
+// stored pair-major (AA[p*S + s]).  A pair at r = 0 adds nothing.
+#define QC_NBCH 2048
+__global__ void k_calc_nb(const double *fr, int natom, const int2 *pairs, long long npair, int S, const double *lam,
+                          const double *AA, const double *BB, const double *qq, int arith, double *part) {
+    __shared__ double sh[QC_T];
+    const int f = blockIdx.y;
+    const double *x = fr + (size_t)f * 3 * natom;
+    const long long p0 = (long long)blockIdx.x * QC_NBCH;
+    const long long p1 = min(npair, p0 + QC_NBCH);
+    double lj = 0.0, el = 0.0;
+    for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+        const int2 a = pairs[p];
+        const double dx = x[3 * a.x] - x[3 * a.y], dy = x[3 * a.x + 1] - x[3 * a.y + 1];
+        const double dz = x[3 * a.x + 2] - x[3 * a.y + 2];
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        if (r == 0.0) continue;
+        const double invr = 1.0 / r;
+        const double invr2 = invr * invr;
+        const double invr6 = invr2 * invr2 * invr2;
+        const double invr12 = invr6 * invr6;
+        for (int s = 0; s < S; ++s) {
+            const double A = AA[p * S + s], B = BB[p * S + s];
+            double v;
+            if (arith) {
+                const double A2 = A * A, A6 = A2 * A2 * A2;
+                v = sqrt(B) * A6 * invr6 * (A6 * invr6 - 2.0);
+            } else {
+                v = A * invr12 - B * invr6;
+            }
+            lj += lam[s] * v;
+            el += lam[s] * (qq[p * S + s] * invr);
+        }
+    }
+    lj = block_sum(lj, sh);
+    el = block_sum(el, sh);
+    if (threadIdx.x == 0) {
+        part[2 * ((size_t)f * gridDim.x + blockIdx.x)] = lj;
+        part[2 * ((size_t)f * gridDim.x + blockIdx.x) + 1] = el;
+    }
+}
+
+// one thread per (frame, term): the blocks' sums in block order
+__global__ void k_calc_nb_frames(const double *part, int nch, int nframes, double *out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * nframes) return;
+    const int f = t >> 1, e = t & 1;
+    double v = 0.0;
+    for (int c = 0; c < nch; ++c) v += part[2 * ((size_t)f * nch + c) + e];
+    out[t] = v;
+}
+
 int check_atoms(const int32_t *a, int n, int natom) {
     for (int k = 0; k < n; ++k)
         if (a[k] < 0 || a[k] >= natom) return 1;
@@ -535,6 +588,42 @@ int qgpu_calc_rdf(const double *frames, int32_t nframes, int32_t natom, const in
     std::vector<unsigned long long> h(nbins);
     CKC(cudaMemcpy(h.data(), bins, (size_t)nbins * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
     for (int k = 0; k < nbins; ++k) counts[k] = (int64_t)h[k];
+    return 0;
+}
+
+int qgpu_calc_nb(const double *frames, int32_t nframes, int32_t natom, int64_t npair, const int32_t *pairs,
+                 int32_t nstates, const double *lambdas, const double *AA, const double *BB, const double *qq,
+                 int32_t arith, double *out) {
+    if (!frames || nframes < 1 || nframes > 65535 || natom < 1 || npair < 0 || (npair > 0 && !pairs) ||
+        nstates < 1 || nstates > QGPU_MAX_STATES || !lambdas || (npair > 0 && (!AA || !BB || !qq)) || !out ||
+        (arith != 0 && arith != 1) || npair > (int64_t)1 << 40)
+        return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_nb: bad arguments");
+    for (int64_t k = 0; k < 2 * npair; ++k)
+        if (pairs[k] < 0 || pairs[k] >= natom) return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_nb: atom out of range");
+    if (npair == 0) {
+        for (int k = 0; k < 2 * nframes; ++k) out[k] = 0.0;
+        return 0;
+    }
+    const long long nch = (npair + QC_NBCH - 1) / QC_NBCH;
+    if (nch > 0x7fffffffLL) return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_nb: list too long");
+    DevBuf B;
+    double *fr, *lam, *a, *b, *q, *part, *o;
+    int32_t *pr;
+    const size_t ns = (size_t)npair * nstates;
+    CKC(B.up(frames, (size_t)nframes * 3 * natom, &fr));
+    CKC(B.up(pairs, (size_t)2 * npair, &pr));
+    CKC(B.up(lambdas, (size_t)nstates, &lam));
+    CKC(B.up(AA, ns, &a));
+    CKC(B.up(BB, ns, &b));
+    CKC(B.up(qq, ns, &q));
+    CKC(B.zero((size_t)2 * nframes * nch, &part));
+    CKC(B.zero((size_t)2 * nframes, &o));
+    k_calc_nb<<<dim3((unsigned)nch, nframes), QC_T>>>(fr, natom, (const int2 *)pr, npair, nstates, lam, a, b, q, arith,
+                                                      part);
+    CKC(cudaGetLastError());
+    k_calc_nb_frames<<<(2 * nframes + QC_T - 1) / QC_T, QC_T>>>(part, (int)nch, nframes, o);
+    CKC(cudaGetLastError());
+    CKC(cudaMemcpy(out, o, (size_t)2 * nframes * sizeof(double), cudaMemcpyDeviceToHost));
     return 0;
 }
 

@@ -616,6 +616,7 @@ void launch_sync_double(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_finalize(const DevSys &S, LaunchCtx &L, int do_temperature, double *rec, const int *rec_base, int k,
                      int ene_every, int rec_cap);
 void launch_tick(LaunchCtx &L, int *rec_base, int n);
+void launch_set_ctl(LaunchCtx &L, int *ctl, int n, int a, int b = 0);   // ctl[0] = a, and ctl[1] = b when n > 1
 void launch_mirror(const DevSys &S, const BlockTables &B, LaunchCtx &L);   // also refreshes wrec
 void launch_wrec(const DevSys &S, const BlockTables &B, LaunchCtx &L);
 void launch_mirror_range(const DevSys &S, LaunchCtx &L, int a0, int n);   // one trajectory's atoms

@@ -169,6 +169,121 @@ class Calc:
                                            abi.ptr(out)))
         return out
 
+    def nb(self, frames, lst: "NbList", lambdas=None) -> np.ndarray:
+        """Per frame (Vlj, Vel) over the pair list (calc_nb.f90 nb_calc_lists);
+        lambdas: one weight per state of the list (None: all 1)."""
+        fr, nf, na = self._frames(frames)
+        S = lst.AA.shape[1]
+        lam = np.ones(S) if lambdas is None else np.ascontiguousarray(lambdas, dtype=np.float64)
+        if lam.shape != (S,):
+            raise ValueError(f"{S} states in the list, {lam.size} lambdas")
+        n = len(lst.pairs)
+        pr = np.ascontiguousarray(lst.pairs, dtype=np.int32).reshape(-1) if n else np.zeros(2, np.int32)
+        dd = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1) if n else np.zeros(S)
+        A, B, Q = dd(lst.AA), dd(lst.BB), dd(lst.qq)
+        out = np.zeros((nf, 2))
+        self._check(self.lib.qgpu_calc_nb(abi.ptr(fr), nf, na, C.c_int64(n), abi.ptr(pr), S, abi.ptr(lam),
+                                          abi.ptr(A), abi.ptr(B), abi.ptr(Q), int(lst.arith), abi.ptr(out)))
+        return out
+
+
+class NbList:
+    """The pair list of a nonbonded calculation between two masks and its
+    per-state LJ and charge products (AA, BB, qq: [npair, nstates])."""
+
+    def __init__(self, pairs, AA, BB, qq, arith):
+        self.pairs, self.AA, self.BB, self.qq, self.arith = pairs, AA, BB, qq, bool(arith)
+
+
+def nb_make_list(g, mask1, mask2, fep: bool = False, chunk: int = 1 << 22) -> NbList:
+    """nb_make_list (calc_nb.f90:334-759) for the system g: every pair of a
+    mask-1 atom and a mask-2 atom (both ascending, mask-1 atom outer), except
+      * pairs whose first atom is not below the second when the second is in
+        both masks (:401-410);
+      * pairs of atoms that share an angle of the topology (:412-425).
+    LJ code: the type pair code (1, or 2 for the polar pairs), 3 for a 1-4
+    pair (:442-461).  Per state, AA = a1*a2 (geometric rule) or a1 + a2
+    (arithmetic), BB = b1*b2 at that code; with fep a Q atom (a solute atom
+    with a Q index) takes its state's Q type and charge, and for code 2 with a
+    non-Q partner its code-1 parameters (:463-683).  Charge products: with fep
+    q1*q2, times the 1-4 scale for 1-4 pairs (:684-740); without fep
+    crg1*crg2*el14_scale for every pair (:742).  The system's charges carry
+    sqrt(Coulomb constant).  The pairs are built chunk by chunk of mask-1
+    atoms (about `chunk` pairs at a time)."""
+    natom, nsol = int(g.natom), int(g.nat_solute)
+    in1 = np.zeros(natom, bool); in1[np.asarray(mask1, dtype=np.int64)] = True
+    in2 = np.zeros(natom, bool); in2[np.asarray(mask2, dtype=np.int64)] = True
+    g1, g2 = np.flatnonzero(in1), np.flatnonzero(in2)
+    mutual = in1 & in2
+    N = np.int64(natom)
+
+    def keys(a, b):
+        a, b = np.asarray(a, np.int64), np.asarray(b, np.int64)
+        return np.minimum(a, b) * N + np.maximum(a, b)
+
+    ang = np.asarray(g.ang).reshape(len(g.ang), -1)[:, :3].astype(np.int64) if len(g.ang) else np.zeros((0, 3), np.int64)
+    akeys = np.unique(np.concatenate([keys(ang[:, 0], ang[:, 1]), keys(ang[:, 0], ang[:, 2]),
+                                      keys(ang[:, 1], ang[:, 2])]))
+    p14 = np.asarray(g.pairs14, dtype=np.int64).reshape(-1, 2)
+    pkeys = np.unique(keys(p14[:, 0], p14[:, 1]))
+    iac = np.asarray(g.iac, dtype=np.int64)
+    avdw, bvdw = np.asarray(g.avdw, np.float64), np.asarray(g.bvdw, np.float64)
+    ljcod = np.asarray(g.ljcod, dtype=np.int64)
+    crg = np.asarray(g.crg, np.float64)
+    arith = int(getattr(g, "ivdw_rule", 1)) == 2
+    el14 = float(g.el14_scale)
+    S = int(g.nstates) if fep else 1
+    iqatom = np.asarray(g.iqatom, dtype=np.int64)
+    isq = np.zeros(natom, bool)
+    if fep:
+        isq[:nsol] = iqatom[:nsol] >= 0
+    qiac = np.asarray(g.qiac, dtype=np.int64).reshape(-1, int(g.nstates)) if fep else None
+    qcrg = np.asarray(g.qcrg, np.float64).reshape(-1, int(g.nstates)) if fep else None
+    qavdw, qbvdw = np.asarray(g.qavdw, np.float64), np.asarray(g.qbvdw, np.float64)
+
+    def params(me, other, code, s):
+        a = avdw[iac[me], code - 1]
+        b = bvdw[iac[me], code - 1]
+        q = crg[me].copy()
+        if fep:
+            qm = isq[me]
+            if qm.any():
+                m = me[qm]
+                c = np.where((code[qm] == 2) & ~isq[other[qm]], 1, code[qm])
+                t = qiac[iqatom[m], s]
+                a[qm], b[qm], q[qm] = qavdw[t, c - 1], qbvdw[t, c - 1], qcrg[iqatom[m], s]
+        return a, b, q
+
+    out = {k: [] for k in ("p", "A", "B", "Q")}
+    rows = max(1, chunk // max(1, len(g2)))
+    for r0 in range(0, len(g1), rows):
+        J = np.repeat(g1[r0:r0 + rows], len(g2))
+        K = np.tile(g2, len(g1[r0:r0 + rows]))
+        key = keys(J, K)
+        keep = ~((J >= K) & mutual[K]) & ~np.isin(key, akeys)
+        J, K, key = J[keep], K[keep], key[keep]
+        code = np.where(np.isin(key, pkeys), 3, ljcod[iac[J], iac[K]])
+        A = np.empty((len(J), S)); B = np.empty((len(J), S)); Q = np.empty((len(J), S))
+        for s in range(S):
+            a1, b1, q1 = params(J, K, code, s)
+            a2, b2, q2 = params(K, J, code, s)
+            A[:, s] = a1 + a2 if arith else a1 * a2
+            B[:, s] = b1 * b2
+            Q[:, s] = np.where(code == 3, q1 * q2 * el14, q1 * q2) if fep else q1 * q2 * el14
+        out["p"].append(np.stack([J, K], 1)); out["A"].append(A); out["B"].append(B); out["Q"].append(Q)
+    cat = lambda k, shape: np.concatenate(out[k]) if out[k] else np.zeros(shape)
+    return NbList(cat("p", (0, 2)).astype(np.int32), cat("A", (0, S)), cat("B", (0, S)), cat("Q", (0, S)), arith)
+
+
+def nb_averages(values) -> float:
+    """The running average qcalc prints after the last frame (calc_nb.f90
+    nb_calc :248-251): ave <- (ave*n + V)/(n + 1)."""
+    ave, n = 0.0, 0
+    for v in values:
+        ave = (ave * n + float(v)) / (n + 1)
+        n += 1
+    return ave
+
 
 def rdf_normalise(counts: np.ndarray, radius: float, nframes: int, n1: int) -> np.ndarray:
     """RDF_finalize (calc_rdf.f90): counts / shell volume / frames / mask-1 atoms."""

@@ -85,3 +85,77 @@ def test_fit_known_answer():
         got = out[f].reshape(-1, 3)
         assert np.abs(got[:nsol] - xref[:nsol]).max() < 1e-10
         assert np.array_equal(got[nsol:], np.array(frames[f]).reshape(-1, 3)[nsol:])
+
+
+def _nb_system(vdw_rule=1, qvdw=True):
+    """A seeded synthetic droplet with two Q states (per-state Q types and
+    charges) and the chain's consecutive-atom angles added (the synthetic
+    topology has none), so every rule of the nonbond list is exercised."""
+    from qsource_gb300 import synth
+    rng = np.random.default_rng(5)
+    qa = synth.neutral_charges(rng, 6, 0.4)
+    g = synth.synthetic(8.0, 24, 6, np.stack([qa, -qa], 1), (0.5, 0.5), 11, vdw_rule=vdw_rule, qvdw=qvdw)
+    n = int(g.nat_solute)
+    g.ang = np.array([(i, i + 1, i + 2, 1) for i in range(0, n - 2, 3)], dtype=np.int32)
+    return g
+
+
+def _same_list(a, b):
+    pa, A, B, Q = b
+    assert np.array_equal(a.pairs.astype(np.int64), pa)
+    for x, y in ((a.AA, A), (a.BB, B), (a.qq, Q)):
+        assert x.shape == y.shape and np.array_equal(x, y)
+
+
+def test_nb_list_matches_restatement_on_reference_topology():
+    """The reference's own topology (46 solute atoms with angles and 1-4
+    pairs): solute against solute and 150 water atoms (overlapping masks)."""
+    from conftest import golden_system
+    from oracle import qcalc_ref as ref
+    from qsource_gb300.qcalc import nb_make_list
+    g = golden_system("basic_sph")
+    nsol = int(g.nat_solute)
+    m1 = np.arange(nsol)
+    m2 = np.concatenate([np.arange(nsol), np.arange(nsol, nsol + 150)])
+    got = nb_make_list(g, m1, m2)
+    want = ref.nb_make_list(g, m1, m2)
+    _same_list(got, want)
+    # the overlap's pairs once each; angle pairs dropped; 1-4 pairs at el14 scale
+    n_self = nsol * (nsol - 1) // 2
+    ang = {tuple(sorted(p)) for a in np.asarray(g.ang)[:, :3] for p in ((a[0], a[1]), (a[0], a[2]), (a[1], a[2]))}
+    assert len(got.pairs) == n_self - len(ang) + nsol * 150
+    assert not {tuple(sorted(p)) for p in got.pairs.tolist()} & ang
+
+
+def test_nb_list_fep_geometric_and_arithmetic_match_restatement():
+    from oracle import qcalc_ref as ref
+    from qsource_gb300.qcalc import nb_make_list
+    for rule in (1, 2):
+        g = _nb_system(vdw_rule=rule)
+        nsol = int(g.nat_solute)
+        q = np.flatnonzero(np.asarray(g.iqatom)[:nsol] >= 0)
+        m2 = np.concatenate([np.arange(nsol), np.arange(nsol, nsol + 30)])
+        for fep in (False, True):
+            got = nb_make_list(g, q, m2, fep=fep)
+            assert got.arith == (rule == 2)
+            _same_list(got, ref.nb_make_list(g, q, m2, fep=fep))
+            assert got.AA.shape[1] == (2 if fep else 1)
+
+
+def test_nb_energy_known_answers():
+    from oracle import qcalc_ref as ref
+    # atoms 0 and 1 two A apart, atom 2 on top of atom 0 (r = 0 adds nothing)
+    x = np.array([[0, 0, 0], [2, 0, 0], [0, 0, 0]], dtype=np.float64).reshape(1, -1)
+    pairs = np.array([[0, 1], [0, 2]])
+    A, B, Q = np.array([[3.0], [7.0]]), np.array([[5.0], [7.0]]), np.array([[11.0], [7.0]])
+    v = ref.nb_calc(x, pairs, A, B, Q)
+    assert np.allclose(v[0], [3.0 / 4096 - 5.0 / 64, 5.5], rtol=1e-15, atol=0)
+    # arithmetic rule: sqrt(BB)*AA^6/r^6*(AA^6/r^6 - 2) is -sqrt(BB) at r = AA
+    va = ref.nb_calc(x, pairs[:1], np.array([[2.0]]), np.array([[0.25]]), np.array([[0.0]]), arith=True)
+    assert abs(va[0, 0] + 0.5) < 1e-15
+    # two states weighted by lambda
+    v2 = ref.nb_calc(x, pairs[:1], np.array([[3.0, 0.0]]), np.array([[5.0, 0.0]]), np.array([[11.0, 1.0]]),
+                     lambdas=[0.25, 0.75])
+    assert np.allclose(v2[0], [0.25 * (3.0 / 4096 - 5.0 / 64), 0.25 * 5.5 + 0.75 * 0.5], rtol=1e-15, atol=0)
+    from qsource_gb300.qcalc import nb_averages
+    assert nb_averages([1.0, 2.0, 3.0, 4.0]) == ref.nb_averages([1.0, 2.0, 3.0, 4.0]) == 2.5
