@@ -582,6 +582,17 @@ int qgpu_calc_fit(const double *frames, int32_t nframes, int32_t natom, int32_t 
    (natom).  out[nframes*3]. */
 int qgpu_calc_com(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
                   const double *mass, double *out);
+/* Kinetic energy of the centre of mass of a mask (calc_com_ke.f90
+   COM_KE_calc) from consecutive frames frame_length fs apart: translational
+   0.5 M |c_f - c_{f-1}|^2 / dt^2 and rotational sum over the principal axes j
+   of the frame's inertia tensor of |L_j|^2 / (2 I_j), L_j the angular
+   momentum of the atoms' positions relative to the centre, less their
+   components along axis j, with velocities from the change of those relative
+   positions; both times 2390 (the reference's integer conversion factor,
+   g/mol A^2/fs^2 to kcal/mol).  Frame 0 is its own predecessor (zero).  mass
+   per atom (natom).  out[2*nframes]: (translational, rotational) kcal/mol. */
+int qgpu_calc_com_ke(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
+                     const double *mass, double frame_length, double *out);
 /* Geometry (calc_geom.f90 dist_calc / angle_calc / torsion_calc): measurement
    m uses kind[m] (2 distance, 3 angle, 4 torsion) atoms atoms[4*m ...].
    out[nframes*nmeas]: A, or degrees (torsions signed). */
@@ -595,21 +606,22 @@ int qgpu_calc_geom(const double *frames, int32_t nframes, int32_t natom, int32_t
    atoms) is the caller's.  nbins <= 8192, nframes <= 65535. */
 int qgpu_calc_rdf(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask1, int32_t n1,
                   const int32_t *mask2, int32_t n2, double radius, int32_t nbins, const double *box, int64_t *counts);
-/* Nonbonded energies between two atom masks (calc_nb.f90 nb_calc_lists,
-   replaces the per-frame call at qcalc.f90:745): for each frame the sums over
-   the npair pairs (pairs[2*p], pairs[2*p+1]) of
+/* Nonbonded energies over pair lists (calc_nb.f90 nb_calc_lists; replaces
+   the per-frame calls of qcalc.f90:745, nb_calc, and of nb_qp_calc, one list
+   per residue): for each frame and list l the sums over its pairs p in
+   [list_start[l], list_start[l+1]) (atoms pairs[2*p], pairs[2*p+1]) of
      Vlj += lambdas[s]*(AA*r^-12 - BB*r^-6)                      (arith 0)
      Vlj += lambdas[s]*(sqrt(BB)*AA^6*r^-6*(AA^6*r^-6 - 2))       (arith 1)
      Vel += lambdas[s]*qq/r
    over the states s < nstates, with the per-pair products AA, BB, qq stored
    pair-major ([p*nstates + s]; one state with lambdas {1} for the plain
-   topology form).  A pair at r = 0 adds nothing.  The list and its products
-   are the caller's (nb_make_list, calc_nb.f90:334-759, built once before the
-   frames).  out[2*nframes]: (Vlj, Vel) per frame, kcal/mol.  nframes <=
-   65535. */
-int qgpu_calc_nb(const double *frames, int32_t nframes, int32_t natom, int64_t npair, const int32_t *pairs,
-                 int32_t nstates, const double *lambdas, const double *AA, const double *BB, const double *qq,
-                 int32_t arith, double *out);
+   topology form).  A pair at r = 0 adds nothing.  The lists and their
+   products are the caller's (nb_make_list, calc_nb.f90:334-759, built once
+   before the frames).  list_start[nlist + 1], list_start[0] = 0.
+   out[(f*nlist + l)*2 ..]: (Vlj, Vel), kcal/mol.  nframes <= 65535. */
+int qgpu_calc_nb(const double *frames, int32_t nframes, int32_t natom, int32_t nlist, const int64_t *list_start,
+                 const int32_t *pairs, int32_t nstates, const double *lambdas, const double *AA, const double *BB,
+                 const double *qq, int32_t arith, double *out);
 
 #ifdef __cplusplus
 }

@@ -13,6 +13,8 @@ entry points.  Each function follows one calc_* module of the reference
         (the FP64 difference rounded to single precision, minimum image in
         double rounded again, dot product and sqrt in single precision),
         bin int(dist/radius*Nbins + 1) in double
+  com_ke calc_com_ke.f90 COM_KE_calc: translational and rotational kinetic
+        energy of a mask's centre of mass from consecutive frames
   nb    calc_nb.f90 nb_make_list + nb_calc_lists: the pair list between two
         masks with its LJ and charge products, and per frame the summed
         LJ and Coulomb energies, in plain Python loops
@@ -149,6 +151,58 @@ def rdf_counts(frames, mask1, mask2, radius, nbins, box=None):
     return counts
 
 
+def com_ke(frames, mask, mass, frame_length):
+    """calc_com_ke.f90 COM_KE_calc (:156-298), frame by frame; the first
+    frame is its own predecessor.  Per frame, with the mask's masses m and
+    total M (COM_KE_put_mass :301-322):
+      c, p = mass-weighted centres of this and the previous frame;
+      rel = x - c, rel' = x' - p, v = (rel - rel')/dt;
+      inertia tensor of rel (Ixx = sum m (y^2 + z^2), Ixy = -sum y x m, ...);
+      its eigenpairs (I_j, e_j) (EIGEN, :227-233);
+      rad_j = rel - (e_j . rel) e_j, L_j = sum (rad_j x v) m;
+      rotational sum_j |L_j|^2/(2 I_j) * 2390, translational
+      0.5 M |p - c|^2 / dt^2 * 2390 (the integer conversion factor, :33).
+    Returns [nframes, 2] (translational, rotational)."""
+    conv = 2390
+    fr = np.asarray(frames, dtype=np.float64)
+    nf = fr.shape[0]
+    fr = fr.reshape(nf, -1, 3)
+    mk = np.asarray(mask)
+    m = np.asarray(mass, dtype=np.float64)[mk]
+    M = 0.0
+    for w in m:
+        M += float(w)
+    out = []
+    prev = fr[0][mk]
+    for f in range(nf):
+        x = fr[f][mk]
+        c = np.array([float(np.dot(x[:, r], m)) / M for r in range(3)])
+        p = np.array([float(np.dot(prev[:, r], m)) / M for r in range(3)])
+        rel, relp = x - c, prev - p
+        Ixx = float(np.dot(rel[:, 1] ** 2 + rel[:, 2] ** 2, m))
+        Iyy = float(np.dot(rel[:, 0] ** 2 + rel[:, 2] ** 2, m))
+        Izz = float(np.dot(rel[:, 1] ** 2 + rel[:, 0] ** 2, m))
+        Ixy = -float(np.sum(rel[:, 1] * rel[:, 0] * m))
+        Ixz = -float(np.sum(rel[:, 0] * rel[:, 2] * m))
+        Iyz = -float(np.sum(rel[:, 1] * rel[:, 2] * m))
+        v = (rel - relp) / frame_length
+        I = np.array([[Ixx, Ixy, Ixz], [Ixy, Iyy, Iyz], [Ixz, Iyz, Izz]])
+        ev, E = np.linalg.eigh(I)
+        rot = 0.0
+        for j in range(3):
+            e = E[:, j]
+            dp = rel @ e
+            rad = rel - dp[:, None] * e[None, :]
+            L = np.array([np.sum(rad[:, 1] * v[:, 2] * m - rad[:, 2] * v[:, 1] * m),
+                          np.sum(rad[:, 2] * v[:, 0] * m - rad[:, 0] * v[:, 2] * m),
+                          np.sum(rad[:, 0] * v[:, 1] * m - rad[:, 1] * v[:, 0] * m)])
+            rot += float(L @ L) / (2 * ev[j]) * conv
+        ke = 0.5 * M * float(np.sum((p - c) ** 2)) / frame_length ** 2 * conv
+        out.append((ke, rot))
+        prev = x
+    return np.array(out)
+
+
 def nb_make_list(g, mask1, mask2, fep=False):
     """calc_nb.f90 nb_make_list (:334-759), pair by pair in the reference's
     loop order (every mask-1 atom, then every mask-2 atom, both ascending).
@@ -259,6 +313,17 @@ def nb_calc(frames, pairs, AA, BB, qq, lambdas=None, arith=False):
                 vel += lam[s] * (float(qq[p, s]) * invr)
         out.append((vlj, vel))
     return np.array(out, dtype=np.float64).reshape(-1, 2)
+
+
+def nb_qp(frames, g, residues, qmask, fep=False, lambdas=None):
+    """calc_nb.f90 nb_qp_add / nb_qp_calc (:778-959): per residue the list of
+    its atoms against the Q-atom mask (nb_make_list), and per frame each
+    residue's nb_calc_lists.  Returns [nframes, nresidues, 2]."""
+    out = []
+    for r in residues:
+        p, A, B, Q = nb_make_list(g, r, qmask, fep=fep)
+        out.append(nb_calc(frames, p, A, B, Q, lambdas=lambdas, arith=int(getattr(g, "ivdw_rule", 1)) == 2))
+    return np.stack(out, 1)
 
 
 def nb_averages(values):

@@ -156,11 +156,12 @@ EXPORTS = {
     "qgpu_run_rows": (_i32, [C.c_void_p, _i32, _i32, _P, _P, _P, _P, _i32, _P]),
     "qgpu_calc_rms": (_i32, [_P, _i32, _i32, _P, _i32, _P, _P]),
     "qgpu_calc_com": (_i32, [_P, _i32, _i32, _P, _i32, _P, _P]),
+    "qgpu_calc_com_ke": (_i32, [_P, _i32, _i32, _P, _i32, _P, _f64, _P]),
     "qgpu_calc_rmsf": (_i32, [_P, _i32, _i32, _P, _i32, _P]),
     "qgpu_calc_fit": (_i32, [_P, _i32, _i32, _i32, _P, _i32, _P, _P, _P, _P]),
     "qgpu_calc_geom": (_i32, [_P, _i32, _i32, _i32, _P, _P, _P]),
     "qgpu_calc_rdf": (_i32, [_P, _i32, _i32, _P, _i32, _P, _i32, _f64, _i32, _P, _P]),
-    "qgpu_calc_nb": (_i32, [_P, _i32, _i32, C.c_int64, _P, _i32, _P, _P, _P, _P, _i32, _P]),
+    "qgpu_calc_nb": (_i32, [_P, _i32, _i32, _i32, _P, _P, _i32, _P, _P, _P, _P, _i32, _P]),
     "qgpu_ene_open": (_i32, [C.c_void_p, _i32, C.c_char_p]),
     "qgpu_ene_close": (_i32, [C.c_void_p, _i32]),
     "qgpu_enefile_write": (_i32, [C.c_char_p, _i32, _i32, C.POINTER(QEnergy), _i32, _P, _P]),

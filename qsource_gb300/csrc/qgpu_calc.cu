@@ -25,6 +25,7 @@
 // integer counts.
 #include <math.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "qgpu_internal.cuh"
@@ -100,30 +101,32 @@ __global__ void k_calc_rmsf_frames(const double *scr, int nmask, double *out) {
 }
 
 // Eigenvalues (descending) and eigenvectors (columns of V) of the symmetric
-// 6x6 matrix A by cyclic Jacobi rotations (at most 60 sweeps, stopping when
+// N x N matrix A by cyclic Jacobi rotations (at most 60 sweeps, stopping when
 // the off-diagonal sum of squares falls below 1e-30 of the total); A is
-// overwritten.  Host code: the fit's six-dimensional eigenproblem is solved
-// per frame on the host, between the two device passes.
-static void jacobi6(double (&A)[6][6], double (&V)[6][6], double (&ev)[6]) {
-    for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 6; ++j) V[i][j] = i == j ? 1.0 : 0.0;
+// overwritten.  Host code: the fit's six-dimensional and the kinetic
+// energy's three-dimensional eigenproblems are solved per frame on the host,
+// between two device passes.
+template <int N>
+static void jacobi(double (&A)[N][N], double (&V)[N][N], double (&ev)[N]) {
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) V[i][j] = i == j ? 1.0 : 0.0;
     for (int sweep = 0; sweep < 60; ++sweep) {
         double off = 0.0, tot = 0.0;
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) {
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) {
                 tot += A[i][j] * A[i][j];
                 if (i != j) off += A[i][j] * A[i][j];
             }
         if (!(off > 1e-30 * tot)) break;
-        for (int p = 0; p < 5; ++p)
-            for (int q = p + 1; q < 6; ++q) {
+        for (int p = 0; p < N - 1; ++p)
+            for (int q = p + 1; q < N; ++q) {
                 const double apq = A[p][q];
                 if (apq == 0.0) continue;
                 const double app = A[p][p], aqq = A[q][q];
                 const double th = (aqq - app) / (2.0 * apq);
                 const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
                 const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
-                for (int k = 0; k < 6; ++k) {
+                for (int k = 0; k < N; ++k) {
                     if (k == p || k == q) continue;
                     const double akp = A[k][p], akq = A[k][q];
                     const double np = c * akp - sn * akq, nq = sn * akp + c * akq;
@@ -133,21 +136,21 @@ static void jacobi6(double (&A)[6][6], double (&V)[6][6], double (&ev)[6]) {
                 A[p][p] = app - t * apq;
                 A[q][q] = aqq + t * apq;
                 A[p][q] = 0.0; A[q][p] = 0.0;
-                for (int k = 0; k < 6; ++k) {
+                for (int k = 0; k < N; ++k) {
                     const double vkp = V[k][p], vkq = V[k][q];
                     V[k][p] = c * vkp - sn * vkq;
                     V[k][q] = sn * vkp + c * vkq;
                 }
             }
     }
-    for (int i = 0; i < 6; ++i) ev[i] = A[i][i];
-    for (int i = 0; i < 5; ++i) {   // descending (selection sort of the pairs)
+    for (int i = 0; i < N; ++i) ev[i] = A[i][i];
+    for (int i = 0; i < N - 1; ++i) {   // descending (selection sort of the pairs)
         int m = i;
-        for (int j = i + 1; j < 6; ++j)
+        for (int j = i + 1; j < N; ++j)
             if (ev[j] > ev[m]) m = j;
         if (m != i) {
             const double e = ev[i]; ev[i] = ev[m]; ev[m] = e;
-            for (int k = 0; k < 6; ++k) { const double v = V[k][i]; V[k][i] = V[k][m]; V[k][m] = v; }
+            for (int k = 0; k < N; ++k) { const double v = V[k][i]; V[k][i] = V[k][m]; V[k][m] = v; }
         }
     }
 }
@@ -166,7 +169,7 @@ static int lsq_rotation(const double (&U)[3][3], double (&R)[3][3]) {
     double A[6][6] = {}, V[6][6], ev[6];
     for (int r = 0; r < 3; ++r)
         for (int q = 0; q < 3; ++q) { A[r][3 + q] = U[r][q]; A[3 + q][r] = U[r][q]; }
-    jacobi6(A, V, ev);
+    jacobi<6>(A, V, ev);
     if (du < 0.0 && fabs(ev[1] - ev[2]) < 1e-5) return 2;
     for (int r = 0; r < 3; ++r)
         for (int q = 0; q < 3; ++q) {
@@ -231,6 +234,90 @@ __global__ void k_calc_fit_apply(const double *fr, int natom, int nsol, const do
         for (int r = 0; r < 3; ++r) X[r] = (x[3 * a + r] - f[r]) * sm;
         for (int r = 0; r < 3; ++r)
             y[3 * a + r] = (f[3 + 3 * r] * X[0] + f[4 + 3 * r] * X[1] + f[5 + 3 * r] * X[2]) / sm + xrcm[r];
+    }
+}
+
+// COM_KE_calc (calc_com_ke.f90:156-298), first device pass, one block per
+// frame f: with the masses m of the mask and M their sum, the centre c of
+// frame f, the centre p of the frame before (of frame f itself at f = 0,
+// where the reference's previous coordinates are the current ones), and the
+// inertia sums of rel = x - c: Ixx = sum m (y^2 + z^2), Iyy = sum m (x^2 +
+// z^2), Izz = sum m (y^2 + x^2), Ixy = -sum y x m, Ixz = -sum x z m, Iyz =
+// -sum y z m.  ci[13 f ..]: c, p, Ixx, Ixy, Iyy, Ixz, Iyz, Izz, M.
+__global__ void k_calc_comke_inertia(const double *fr, int natom, const int *mask, int nmask, const double *mass,
+                                     double *ci) {
+    __shared__ double sh[QC_T];
+    __shared__ double s_c[3];
+    const int f = blockIdx.x;
+    const double *x = fr + (size_t)f * 3 * natom;
+    const double *xp = fr + (size_t)(f > 0 ? f - 1 : 0) * 3 * natom;
+    double c[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k = threadIdx.x; k < nmask; k += blockDim.x) {
+        const int a = mask[k];
+        const double m = mass[a];
+        for (int r = 0; r < 3; ++r) { c[r] += x[3 * a + r] * m; c[3 + r] += xp[3 * a + r] * m; }
+        c[6] += m;
+    }
+    double t[7];
+    for (int q = 0; q < 7; ++q) t[q] = block_sum(c[q], sh);
+    double *o = ci + 13 * (size_t)f;
+    if (threadIdx.x == 0) {
+        for (int r = 0; r < 3; ++r) { s_c[r] = t[r] / t[6]; o[r] = s_c[r]; o[3 + r] = t[3 + r] / t[6]; }
+        o[12] = t[6];
+    }
+    __syncthreads();
+    double I[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int k = threadIdx.x; k < nmask; k += blockDim.x) {
+        const int a = mask[k];
+        const double m = mass[a];
+        const double rx = x[3 * a] - s_c[0], ry = x[3 * a + 1] - s_c[1], rz = x[3 * a + 2] - s_c[2];
+        I[0] += (ry * ry + rz * rz) * m;
+        I[1] += ry * rx * m;
+        I[2] += (rx * rx + rz * rz) * m;
+        I[3] += rx * rz * m;
+        I[4] += ry * rz * m;
+        I[5] += (ry * ry + rx * rx) * m;
+    }
+    for (int q = 0; q < 6; ++q) {
+        const double v = block_sum(I[q], sh);
+        if (threadIdx.x == 0) o[6 + q] = (q == 1 || q == 3 || q == 4) ? -v : v;
+    }
+}
+
+// COM_KE_calc second pass, one block per frame: the velocity v = (rel -
+// rel')/dt of every mask atom relative to its frame's centre (rel' about
+// the previous frame's centre), and for each principal axis e_j of the
+// inertia tensor (ax[12 f + 3 j ..], from the host) the angular momentum
+// L_j = sum m (rad_j x v), rad_j = rel - (e_j . rel) e_j.  lm[9 f + 3 j ..].
+__global__ void k_calc_comke_angmom(const double *fr, int natom, const int *mask, int nmask, const double *mass,
+                                    const double *ci, const double *ax, double dt, double *lm) {
+    __shared__ double sh[QC_T];
+    const int f = blockIdx.x;
+    const double *x = fr + (size_t)f * 3 * natom;
+    const double *xp = fr + (size_t)(f > 0 ? f - 1 : 0) * 3 * natom;
+    const double *c = ci + 13 * (size_t)f;
+    const double *e = ax + 12 * (size_t)f;
+    double L[9];
+    for (int q = 0; q < 9; ++q) L[q] = 0.0;
+    for (int k = threadIdx.x; k < nmask; k += blockDim.x) {
+        const int a = mask[k];
+        const double m = mass[a];
+        double rel[3], v[3];
+        for (int r = 0; r < 3; ++r) {
+            rel[r] = x[3 * a + r] - c[r];
+            v[r] = (rel[r] - (xp[3 * a + r] - c[3 + r])) / dt;
+        }
+        for (int j = 0; j < 3; ++j) {
+            const double dp = e[3 * j] * rel[0] + e[3 * j + 1] * rel[1] + e[3 * j + 2] * rel[2];
+            const double rx = rel[0] - dp * e[3 * j], ry = rel[1] - dp * e[3 * j + 1], rz = rel[2] - dp * e[3 * j + 2];
+            L[3 * j] += ry * v[2] * m - rz * v[1] * m;
+            L[3 * j + 1] += rz * v[0] * m - rx * v[2] * m;
+            L[3 * j + 2] += rx * v[1] * m - ry * v[0] * m;
+        }
+    }
+    for (int q = 0; q < 9; ++q) {
+        const double s = block_sum(L[q], sh);
+        if (threadIdx.x == 0) lm[9 * (size_t)f + q] = s;
     }
 }
 
@@ -371,17 +458,17 @@ __global__ void k_calc_rdf(const double *fr, int natom, const int *m1, int n1, c
         if (sb[k]) atomicAdd(&bins[k], (unsigned long long)sb[k]);
 }
 
-// nb_calc_lists (calc_nb.f90:257-328): block (c, f) sums pairs
-// [c*QC_NBCH, (c+1)*QC_NBCH) of the list at frame f, the per-state products
-// stored pair-major (AA[p*S + s]).  A pair at r = 0 adds nothing.
+// nb_calc_lists (calc_nb.f90:257-328): block (c, f) sums the pairs of chunk
+// c at frame f, pairs [ch[c].x, ch[c].y) of one list (a chunk never spans
+// two lists), the per-state products stored pair-major (AA[p*S + s]).  A
+// pair at r = 0 adds nothing.
 #define QC_NBCH 2048
-__global__ void k_calc_nb(const double *fr, int natom, const int2 *pairs, long long npair, int S, const double *lam,
+__global__ void k_calc_nb(const double *fr, int natom, const int2 *pairs, const longlong2 *ch, int S, const double *lam,
                           const double *AA, const double *BB, const double *qq, int arith, double *part) {
     __shared__ double sh[QC_T];
     const int f = blockIdx.y;
     const double *x = fr + (size_t)f * 3 * natom;
-    const long long p0 = (long long)blockIdx.x * QC_NBCH;
-    const long long p1 = min(npair, p0 + QC_NBCH);
+    const long long p0 = ch[blockIdx.x].x, p1 = ch[blockIdx.x].y;
     double lj = 0.0, el = 0.0;
     for (long long p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
         const int2 a = pairs[p];
@@ -414,13 +501,16 @@ __global__ void k_calc_nb(const double *fr, int natom, const int2 *pairs, long l
     }
 }
 
-// one thread per (frame, term): the blocks' sums in block order
-__global__ void k_calc_nb_frames(const double *part, int nch, int nframes, double *out) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= 2 * nframes) return;
-    const int f = t >> 1, e = t & 1;
+// one thread per (frame, list, term): the list's chunk sums in chunk order
+// (chunks c0[l] .. c0[l+1]-1)
+__global__ void k_calc_nb_lists(const double *part, const int *c0, int nch, int nlist, int nframes, double *out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2LL * nlist * nframes) return;
+    const int e = (int)(t & 1);
+    const long long fl = t >> 1;
+    const int f = (int)(fl / nlist), l = (int)(fl % nlist);
     double v = 0.0;
-    for (int c = 0; c < nch; ++c) v += part[2 * ((size_t)f * nch + c) + e];
+    for (int c = c0[l]; c < c0[l + 1]; ++c) v += part[2 * ((size_t)f * nch + c) + e];
     out[t] = v;
 }
 
@@ -524,6 +614,56 @@ int qgpu_calc_fit(const double *frames, int32_t nframes, int32_t natom, int32_t 
     return 0;
 }
 
+int qgpu_calc_com_ke(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
+                     const double *mass, double frame_length, double *out) {
+    if (!frames || nframes < 1 || natom < 1 || !mask || nmask < 1 || !mass || !(frame_length > 0) || !out ||
+        check_atoms(mask, nmask, natom))
+        return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_com_ke: bad arguments");
+    // g/mol A^2/fs^2 to kcal/mol: the reference declares the factor 2390.0574
+    // as an integer parameter (calc_com_ke.f90:33), so it is 2390
+    const double conv = 2390.0;
+    DevBuf B;
+    double *fr, *ms, *ci, *ax, *lm;
+    int *m;
+    CKC(B.up(frames, (size_t)nframes * 3 * natom, &fr));
+    CKC(B.up(mass, (size_t)natom, &ms));
+    CKC(B.up(mask, (size_t)nmask, &m));
+    CKC(B.zero((size_t)nframes * 13, &ci));
+    CKC(B.zero((size_t)nframes * 9, &lm));
+    k_calc_comke_inertia<<<nframes, QC_T>>>(fr, natom, m, nmask, ms, ci);
+    CKC(cudaGetLastError());
+    std::vector<double> h((size_t)nframes * 13), e((size_t)nframes * 12), iv((size_t)nframes * 3);
+    CKC(cudaMemcpy(h.data(), ci, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int f = 0; f < nframes; ++f) {
+        // EIGEN of the packed (Ixx, Ixy, Iyy, Ixz, Iyz, Izz): principal moments
+        // and axes (calc_com_ke.f90:226-232)
+        const double *I = &h[13 * (size_t)f + 6];
+        double A[3][3] = {{I[0], I[1], I[3]}, {I[1], I[2], I[4]}, {I[3], I[4], I[5]}}, V[3][3], ev[3];
+        jacobi<3>(A, V, ev);
+        for (int j = 0; j < 3; ++j) {
+            iv[3 * (size_t)f + j] = ev[j];
+            for (int r = 0; r < 3; ++r) e[12 * (size_t)f + 3 * j + r] = V[r][j];
+        }
+    }
+    CKC(B.up(e.data(), e.size(), &ax));
+    k_calc_comke_angmom<<<nframes, QC_T>>>(fr, natom, m, nmask, ms, ci, ax, frame_length, lm);
+    CKC(cudaGetLastError());
+    std::vector<double> L((size_t)nframes * 9);
+    CKC(cudaMemcpy(L.data(), lm, L.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int f = 0; f < nframes; ++f) {
+        const double *c = &h[13 * (size_t)f];
+        double rot = 0.0;
+        for (int j = 0; j < 3; ++j) {
+            const double *l = &L[9 * (size_t)f + 3 * j];
+            rot += (l[0] * l[0] + l[1] * l[1] + l[2] * l[2]) / (2.0 * iv[3 * (size_t)f + j]) * conv;
+        }
+        const double d0 = c[3] - c[0], d1 = c[4] - c[1], d2 = c[5] - c[2];
+        out[2 * f] = 0.5 * c[12] * (d0 * d0 + d1 * d1 + d2 * d2) / (frame_length * frame_length) * conv;
+        out[2 * f + 1] = rot;
+    }
+    return 0;
+}
+
 int qgpu_calc_com(const double *frames, int32_t nframes, int32_t natom, const int32_t *mask, int32_t nmask,
                   const double *mass, double *out) {
     if (!frames || nframes < 1 || natom < 1 || !mask || nmask < 1 || !mass || !out || check_atoms(mask, nmask, natom))
@@ -591,24 +731,42 @@ int qgpu_calc_rdf(const double *frames, int32_t nframes, int32_t natom, const in
     return 0;
 }
 
-int qgpu_calc_nb(const double *frames, int32_t nframes, int32_t natom, int64_t npair, const int32_t *pairs,
-                 int32_t nstates, const double *lambdas, const double *AA, const double *BB, const double *qq,
-                 int32_t arith, double *out) {
-    if (!frames || nframes < 1 || nframes > 65535 || natom < 1 || npair < 0 || (npair > 0 && !pairs) ||
-        nstates < 1 || nstates > QGPU_MAX_STATES || !lambdas || (npair > 0 && (!AA || !BB || !qq)) || !out ||
-        (arith != 0 && arith != 1) || npair > (int64_t)1 << 40)
+int qgpu_calc_nb(const double *frames, int32_t nframes, int32_t natom, int32_t nlist, const int64_t *list_start,
+                 const int32_t *pairs, int32_t nstates, const double *lambdas, const double *AA, const double *BB,
+                 const double *qq, int32_t arith, double *out) {
+    if (!frames || nframes < 1 || nframes > 65535 || natom < 1 || nlist < 1 || !list_start || nstates < 1 ||
+        nstates > QGPU_MAX_STATES || !lambdas || !out || (arith != 0 && arith != 1))
         return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_nb: bad arguments");
+    if (list_start[0] != 0) return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_nb: list_start[0] must be 0");
+    for (int l = 0; l < nlist; ++l)
+        if (list_start[l + 1] < list_start[l]) return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_nb: list_start decreases");
+    const int64_t npair = list_start[nlist];
+    if (npair > ((int64_t)1 << 40) || (npair > 0 && (!pairs || !AA || !BB || !qq)))
+        return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_nb: bad pair arrays");
     for (int64_t k = 0; k < 2 * npair; ++k)
         if (pairs[k] < 0 || pairs[k] >= natom) return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_nb: atom out of range");
-    if (npair == 0) {
-        for (int k = 0; k < 2 * nframes; ++k) out[k] = 0.0;
+    // chunks of at most QC_NBCH pairs, none spanning two lists
+    std::vector<long long> chs;
+    std::vector<int> c0((size_t)nlist + 1, 0);
+    for (int l = 0; l < nlist; ++l) {
+        c0[l] = (int)(chs.size() / 2);
+        for (int64_t p = list_start[l]; p < list_start[l + 1]; p += QC_NBCH) {
+            chs.push_back(p);
+            chs.push_back(std::min<int64_t>(list_start[l + 1], p + QC_NBCH));
+        }
+        if (chs.size() / 2 > 0x7fffffffu) return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_nb: lists too long");
+    }
+    const int nch = (int)(chs.size() / 2);
+    c0[nlist] = nch;
+    if (nch == 0) {
+        for (long long k = 0; k < 2LL * nframes * nlist; ++k) out[k] = 0.0;
         return 0;
     }
-    const long long nch = (npair + QC_NBCH - 1) / QC_NBCH;
-    if (nch > 0x7fffffffLL) return qgpu_fail(QGPU_E_INVALID, "qgpu_calc_nb: list too long");
     DevBuf B;
     double *fr, *lam, *a, *b, *q, *part, *o;
     int32_t *pr;
+    long long *chd;
+    int *c0d;
     const size_t ns = (size_t)npair * nstates;
     CKC(B.up(frames, (size_t)nframes * 3 * natom, &fr));
     CKC(B.up(pairs, (size_t)2 * npair, &pr));
@@ -616,14 +774,17 @@ int qgpu_calc_nb(const double *frames, int32_t nframes, int32_t natom, int64_t n
     CKC(B.up(AA, ns, &a));
     CKC(B.up(BB, ns, &b));
     CKC(B.up(qq, ns, &q));
+    CKC(B.up(chs.data(), chs.size(), &chd));
+    CKC(B.up(c0.data(), c0.size(), &c0d));
     CKC(B.zero((size_t)2 * nframes * nch, &part));
-    CKC(B.zero((size_t)2 * nframes, &o));
-    k_calc_nb<<<dim3((unsigned)nch, nframes), QC_T>>>(fr, natom, (const int2 *)pr, npair, nstates, lam, a, b, q, arith,
-                                                      part);
+    CKC(B.zero((size_t)2 * nframes * nlist, &o));
+    k_calc_nb<<<dim3((unsigned)nch, nframes), QC_T>>>(fr, natom, (const int2 *)pr, (const longlong2 *)chd, nstates, lam,
+                                                      a, b, q, arith, part);
     CKC(cudaGetLastError());
-    k_calc_nb_frames<<<(2 * nframes + QC_T - 1) / QC_T, QC_T>>>(part, (int)nch, nframes, o);
+    const long long nt = 2LL * nframes * nlist;
+    k_calc_nb_lists<<<(unsigned)((nt + QC_T - 1) / QC_T), QC_T>>>(part, c0d, nch, nlist, nframes, o);
     CKC(cudaGetLastError());
-    CKC(cudaMemcpy(out, o, (size_t)2 * nframes * sizeof(double), cudaMemcpyDeviceToHost));
+    CKC(cudaMemcpy(out, o, (size_t)nt * sizeof(double), cudaMemcpyDeviceToHost));
     return 0;
 }
 

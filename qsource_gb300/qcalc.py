@@ -146,6 +146,17 @@ class Calc:
         self._check(self.lib.qgpu_calc_com(abi.ptr(fr), nf, na, abi.ptr(m), len(m), abi.ptr(ms), abi.ptr(out)))
         return out
 
+    def com_ke(self, frames, mask, mass, frame_length: float) -> np.ndarray:
+        """Per frame (translational, rotational) kinetic energy of the mask's
+        centre of mass, kcal/mol (calc_com_ke.f90); frame_length in fs."""
+        fr, nf, na = self._frames(frames)
+        m = np.ascontiguousarray(mask, dtype=np.int32)
+        ms = np.ascontiguousarray(mass, dtype=np.float64)
+        out = np.zeros((nf, 2))
+        self._check(self.lib.qgpu_calc_com_ke(abi.ptr(fr), nf, na, abi.ptr(m), len(m), abi.ptr(ms),
+                                              C.c_double(frame_length), abi.ptr(out)))
+        return out
+
     def geom(self, frames, measurements) -> np.ndarray:
         """measurements: list of atom tuples (2 distance, 3 angle, 4 torsion)."""
         fr, nf, na = self._frames(frames)
@@ -170,29 +181,45 @@ class Calc:
         return out
 
     def nb(self, frames, lst: "NbList", lambdas=None) -> np.ndarray:
-        """Per frame (Vlj, Vel) over the pair list (calc_nb.f90 nb_calc_lists);
-        lambdas: one weight per state of the list (None: all 1)."""
+        """Per frame and list (Vlj, Vel) (calc_nb.f90 nb_calc_lists), shape
+        [nframes, nlist, 2]; lambdas: one weight per state (None: all 1)."""
         fr, nf, na = self._frames(frames)
         S = lst.AA.shape[1]
         lam = np.ones(S) if lambdas is None else np.ascontiguousarray(lambdas, dtype=np.float64)
         if lam.shape != (S,):
             raise ValueError(f"{S} states in the list, {lam.size} lambdas")
         n = len(lst.pairs)
+        st = np.ascontiguousarray(lst.starts, dtype=np.int64)
         pr = np.ascontiguousarray(lst.pairs, dtype=np.int32).reshape(-1) if n else np.zeros(2, np.int32)
         dd = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1) if n else np.zeros(S)
         A, B, Q = dd(lst.AA), dd(lst.BB), dd(lst.qq)
-        out = np.zeros((nf, 2))
-        self._check(self.lib.qgpu_calc_nb(abi.ptr(fr), nf, na, C.c_int64(n), abi.ptr(pr), S, abi.ptr(lam),
+        nl = len(st) - 1
+        out = np.zeros((nf, nl, 2))
+        self._check(self.lib.qgpu_calc_nb(abi.ptr(fr), nf, na, nl, abi.ptr(st), abi.ptr(pr), S, abi.ptr(lam),
                                           abi.ptr(A), abi.ptr(B), abi.ptr(Q), int(lst.arith), abi.ptr(out)))
         return out
 
 
 class NbList:
-    """The pair list of a nonbonded calculation between two masks and its
-    per-state LJ and charge products (AA, BB, qq: [npair, nstates])."""
+    """Pair lists of nonbonded calculations and their per-state LJ and charge
+    products (AA, BB, qq: [npair, nstates]); list l is pairs
+    [starts[l], starts[l+1])."""
 
-    def __init__(self, pairs, AA, BB, qq, arith):
+    def __init__(self, pairs, AA, BB, qq, arith, starts=None):
         self.pairs, self.AA, self.BB, self.qq, self.arith = pairs, AA, BB, qq, bool(arith)
+        self.starts = np.array([0, len(pairs)], dtype=np.int64) if starts is None else np.asarray(starts, np.int64)
+
+
+def nb_qp_make_lists(g, residues, qmask, fep: bool = False) -> NbList:
+    """nb_qp_add (calc_nb.f90:778-938): one list per residue, the residue's
+    atoms against the Q-atom mask (nb_make_list each); residues: the atom
+    index arrays of the residues, in order."""
+    parts = [nb_make_list(g, r, qmask, fep=fep) for r in residues]
+    S = int(g.nstates) if fep else 1
+    starts = np.concatenate([[0], np.cumsum([len(p.pairs) for p in parts])]).astype(np.int64)
+    cat = lambda k, shape: np.concatenate([getattr(p, k) for p in parts]) if parts else np.zeros(shape)
+    return NbList(cat("pairs", (0, 2)).astype(np.int32), cat("AA", (0, S)), cat("BB", (0, S)), cat("qq", (0, S)),
+                  int(getattr(g, "ivdw_rule", 1)) == 2, starts)
 
 
 def nb_make_list(g, mask1, mask2, fep: bool = False, chunk: int = 1 << 22) -> NbList:

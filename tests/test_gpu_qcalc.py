@@ -9,7 +9,8 @@ so these quantities are pinned by the restatement only.
 Tolerances: RMSD, centre of mass and geometry 1e-10 relative (FP64 sums in a
 different order); RDF bin counts exact (the reference's single-precision
 distance and double-precision binning reproduced operation for operation);
-nonbonded LJ and Coulomb sums 1e-10 of (1 + |V|) (FP64 sums of up to 1.6e5
+centre-of-mass kinetic energies 1e-8 relative (principal axes from a
+different eigen-solver); nonbonded LJ and Coulomb sums 1e-10 of (1 + |V|) (FP64 sums of up to 1.6e5
 pairs in blocks instead of one running sum)."""
 import numpy as np
 import pytest
@@ -49,6 +50,23 @@ def test_rms_com_geom_match_oracle(droplet):
     o = s.nat_solute
     meas = [(0, 1), (o, o + 1), (0, 1, 2), (o + 1, o, o + 2), (0, 1, 2, 3), (4, 5, 6, 7), (o, o + 3, o + 6, o + 9)]
     assert np.allclose(c.geom(fr, meas), ref.geom(fr, meas), rtol=1e-10, atol=1e-9)
+
+
+def test_com_ke_matches_oracle(droplet):
+    """Translational and rotational kinetic energy of the solute's and of a
+    water subset's centre of mass over consecutive engine frames (10 steps
+    apart)."""
+    from oracle import qcalc_ref as ref
+    from qsource_gb300.qcalc import Calc
+    s, fr = droplet
+    mass = np.asarray(s.mass)[np.asarray(s.iac)]
+    dt = 20.0                                   # fs between frames (10 steps of 2 fs)
+    for mask in (np.arange(s.nat_solute), np.arange(s.nat_solute, s.natom, 5)):
+        got = Calc().com_ke(fr, mask, mass, dt)
+        want = ref.com_ke(fr, mask, mass, dt)
+        assert np.array_equal(got[0], [0.0, 0.0])
+        assert np.all(want[1:] > 0)
+        assert np.allclose(got, want, rtol=1e-8, atol=0), (got, want)
 
 
 def test_rmsf_matches_oracle(droplet):
@@ -142,7 +160,7 @@ def test_nb_energies_match_oracle_reference_topology(engine_lib):
     fr = np.array([x0 + rng.normal(0, 0.05, x0.shape) for _ in range(3)])
     lst = nb_make_list(g, np.arange(g.nat_solute), np.arange(g.natom))
     assert len(lst.pairs) > 150000
-    got = Calc().nb(fr, lst)
+    got = Calc().nb(fr, lst)[:, 0]
     want = ref.nb_calc(fr, lst.pairs, lst.AA, lst.BB, lst.qq)
     assert np.all(np.abs(got - want) <= 1e-10 * (1 + np.abs(want))), (got, want)
 
@@ -167,7 +185,7 @@ def test_nb_energies_fep_both_rules_match_oracle(engine_lib):
         fr[1, 3 * w:3 * w + 3] = fr[1, 3 * q[0]:3 * q[0] + 3]
         lst = nb_make_list(g, q, m2, fep=True)
         lam = np.array([0.3, 0.7])
-        got = Calc().nb(fr, lst, lam)
+        got = Calc().nb(fr, lst, lam)[:, 0]
         want = ref.nb_calc(fr, lst.pairs, lst.AA, lst.BB, lst.qq, lambdas=lam, arith=lst.arith)
         assert np.all(np.isfinite(got))
         assert np.all(np.abs(got - want) <= 1e-10 * (1 + np.abs(want))), (rule, got, want)
@@ -180,4 +198,30 @@ def test_nb_empty_list(engine_lib):
     lst = nb_make_list(g, [3], [3])
     assert len(lst.pairs) == 0
     got = Calc().nb(np.array([g.x, g.x]), lst)
-    assert np.array_equal(got, np.zeros((2, 2)))
+    assert np.array_equal(got, np.zeros((2, 1, 2)))
+
+
+def test_nb_residue_lists_match_oracle(engine_lib):
+    """nb_qp: one list per residue against the Q-atom mask (here the first
+    60 water molecules as residues against the 46 Q atoms of the reference's
+    topology), all lists summed in one call, and the per-residue averages over
+    the frames."""
+    from oracle import qcalc_ref as ref
+    from qsource_gb300.qcalc import Calc, nb_averages, nb_qp_make_lists
+    g = golden_system("basic_sph")
+    nsol = int(g.nat_solute)
+    rng = np.random.default_rng(4)
+    x0 = np.asarray(g.x, dtype=np.float64)
+    fr = np.array([x0 + rng.normal(0, 0.05, x0.shape) for _ in range(4)])
+    residues = [np.arange(nsol + 3 * w, nsol + 3 * w + 3) for w in range(60)]
+    qmask = np.arange(nsol)
+    lst = nb_qp_make_lists(g, residues, qmask)
+    assert len(lst.starts) == 61 and lst.starts[-1] == 60 * 3 * nsol
+    got = Calc().nb(fr, lst)
+    want = ref.nb_qp(fr, g, residues, qmask)
+    assert got.shape == want.shape == (4, 60, 2)
+    assert np.all(np.abs(got - want) <= 1e-10 * (1 + np.abs(want)))
+    for r in (0, 17, 59):
+        for e in (0, 1):
+            a, b = nb_averages(got[:, r, e]), ref.nb_averages(want[:, r, e])
+            assert abs(a - b) <= 1e-10 * (1 + abs(b))

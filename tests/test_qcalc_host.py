@@ -159,3 +159,25 @@ def test_nb_energy_known_answers():
     assert np.allclose(v2[0], [0.25 * (3.0 / 4096 - 5.0 / 64), 0.25 * 5.5 + 0.75 * 0.5], rtol=1e-15, atol=0)
     from qsource_gb300.qcalc import nb_averages
     assert nb_averages([1.0, 2.0, 3.0, 4.0]) == ref.nb_averages([1.0, 2.0, 3.0, 4.0]) == 2.5
+
+
+def test_com_ke_known_answers():
+    """A rectangle of four equal masses, (+-a, 0, 0) and (0, +-b, 0), turned by
+    theta about z between frames: the centre stays put (no translational
+    energy) and the three principal axes give L^2/(2I) = m s^2 (a^2 + b^2),
+    m s^2 b^2 and m s^2 a^2 per dt^2 (s = sin theta), so the rotational energy
+    is 2 m s^2 (a^2 + b^2)/dt^2 * 2390.  The same body moved by d per frame
+    has 0.5 M |d|^2/dt^2 * 2390 and no rotation.  Frame 0 gives zeros."""
+    from oracle import qcalc_ref as ref
+    m, a, b, th, dt = 12.0, 1.5, 0.8, 0.01, 2.0
+    x0 = np.array([[a, 0, 0], [-a, 0, 0], [0, b, 0], [0, -b, 0]])
+    R = np.array([[math.cos(th), -math.sin(th), 0], [math.sin(th), math.cos(th), 0], [0, 0, 1]])
+    frames = np.array([x0.ravel(), (x0 @ R.T).ravel()])
+    v = ref.com_ke(frames, [0, 1, 2, 3], np.full(4, m), dt)
+    assert np.array_equal(v[0], [0.0, 0.0])
+    want = 2 * m * math.sin(th) ** 2 * (a * a + b * b) / dt ** 2 * 2390
+    assert abs(v[1, 0]) < 1e-20 and abs(v[1, 1] - want) < 1e-12 * want
+    d = np.array([0.3, -0.1, 0.2])
+    frames = np.array([x0.ravel(), (x0 + d).ravel()])
+    v = ref.com_ke(frames, [0, 1, 2, 3], np.full(4, m), dt)
+    assert abs(v[1, 0] - 0.5 * 4 * m * float(d @ d) / dt ** 2 * 2390) < 1e-12 and abs(v[1, 1]) < 1e-20
