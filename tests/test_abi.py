@@ -43,3 +43,31 @@ def test_error_reporting_without_device(engine_lib):
     rc = engine_lib.qgpu_create(None, 1, C.byref(h))
     assert rc != 0
     assert "bad arguments" in last_error(engine_lib)
+
+
+def test_calc_entries_refuse_bad_arguments_without_device(engine_lib):
+    """The qcalc entry points check their arguments on the host before any
+    device call: a decreasing list offset, a pair atom out of range, a
+    non-positive frame interval and an empty mask are refused with a message."""
+    import numpy as np
+    from qsource_gb300 import abi
+    from qsource_gb300.abi import last_error
+    fr = np.zeros((1, 3 * 4))
+    lam = np.ones(1)
+    A = np.ones(2)
+    out = np.zeros(8)
+    pairs = np.array([0, 1, 2, 3], dtype=np.int32)
+    p = abi.ptr
+    rc = engine_lib.qgpu_calc_nb(p(fr), 1, 4, 2, p(np.array([0, 2, 1], dtype=np.int64)), p(pairs), 1, p(lam),
+                                 p(A), p(A), p(A), 0, p(out))
+    assert rc != 0 and "decreases" in last_error(engine_lib)
+    bad = np.array([0, 1, 2, 9], dtype=np.int32)
+    rc = engine_lib.qgpu_calc_nb(p(fr), 1, 4, 1, p(np.array([0, 2], dtype=np.int64)), p(bad), 1, p(lam),
+                                 p(A), p(A), p(A), 0, p(out))
+    assert rc != 0 and "out of range" in last_error(engine_lib)
+    mask = np.array([0, 1], dtype=np.int32)
+    mass = np.ones(4)
+    rc = engine_lib.qgpu_calc_com_ke(p(fr), 1, 4, p(mask), 2, p(mass), C.c_double(0.0), p(out))
+    assert rc != 0 and "bad arguments" in last_error(engine_lib)
+    rc = engine_lib.qgpu_calc_rmsf(p(fr), 1, 4, p(mask), 0, p(out))
+    assert rc != 0 and "bad arguments" in last_error(engine_lib)
