@@ -395,6 +395,25 @@ def test_branches_are_bit_identical(systems, precision):
     assert ra == rb
 
 
+def test_set_step_moves_the_record_steps(systems):
+    """qgpu_set_step sets md_run's step counter on the device (a one-thread
+    kernel writes the record window's control words): the same 20 steps run
+    from step 100 give records at the same offsets plus 100, and bitwise the
+    same coordinates (nothing else of this Berendsen system reads the counter)."""
+    out = []
+    for start in (0, 100):
+        e = _engine([systems["cfg1"]])
+        if start:
+            e.set_step(start)
+        rows = e.run(20, ene_every=5)
+        x, v = e.coords_all()
+        out.append(([r[0] for r in rows[0]], [r[1] for r in rows[0]], x, v))
+    (s0, e0, x0, v0), (s1, e1, x1, v1) = out
+    assert len(s0) == 4 and s1 == [k + 100 for k in s0]
+    assert e0 == e1
+    assert np.array_equal(x0, x1) and np.array_equal(v0, v1)
+
+
 def test_shake_failure_is_reported(systems):
     """Coincident reference positions make SHAKE diverge: the bounded
     iteration stops at 1000 sweeps and the call returns QGPU_E_SHAKE."""
