@@ -127,6 +127,45 @@ def test_forces_and_energies(systems, name):
         assert not energies_close(q, qo, EQ_KEYS)
 
 
+def test_ragged_batch_with_a_trajectory_without_q_atoms(systems):
+    """A batch of uneven content: a 9 A droplet around a 20-atom chain with no
+    Q atoms and one state (a plain MD system), beside the two-state Q droplet.
+    Forces and energies of each trajectory match the oracle at step 0, the
+    Q-free trajectory's per-state Q energies are zero, and 20 FP64-master MD
+    steps match the oracle's dynamics of both."""
+    from qsource_gb300 import synth
+    from qsource_gb300.abi import PRECISION
+    plain = synth.synthetic(9.0, 20, 0, np.zeros((0, 1)), (1.0,), 5)
+    batch = [plain, systems["cfg1"]]
+    e = _engine(batch)
+    e.make_pair_lists()
+    for t, s in enumerate(batch):
+        d, E, EQ = e.pot_energy(t, terms=0x1F)
+        o = _oracle(s)
+        o.make_pair_lists()
+        do, Eo, EQo = o.pot_energy(0x1F)
+        assert rel_rms(d, do) <= FORCE_RTOL
+        assert not energies_close(E, Eo, E_KEYS)
+        for q, qo in zip(EQ, EQo):
+            assert not energies_close(q, qo, EQ_KEYS)
+        if t == 0:
+            assert len(EQ) == 1 and all(EQ[0][k] == 0.0 for k in ("qq_el", "qp_el", "qw_el", "qp_vdw", "qw_vdw"))
+    e = _engine(batch)
+    e.set_precision(PRECISION["fp64"])
+    rows = e.run(20, ene_every=10)
+    for t, s in enumerate(batch):
+        o = _oracle(s)
+        o.temperature()
+        rc, orows, oq, T = o.md_run(20)
+        assert rc == 0 and len(rows[t]) == 2
+        for r in rows[t]:
+            k = r[0]
+            assert abs(r[1]["potential"] - orows[k]["potential"]) <= 1e-4 * max(1.0, abs(orows[k]["potential"]))
+        x, _ = e.coords(t)
+        xo, _ = o.coords()
+        assert np.abs(x - xo).max() < 1e-4
+
+
 def test_golden_columns_on_gpu(systems, golden):
     """The GPU path reproduces the reference's printed step-0 values."""
     s = systems["golden"]
