@@ -150,6 +150,107 @@ void prof_end(LaunchCtx &L) {
 }
 
 // ---------------------------------------------------------------- create
+// Every index the device will follow is checked on the host first, so that a
+// malformed descriptor is refused with QGPU_E_INVALID and never reaches a
+// kernel as an out-of-range address.
+static int validate_indices(const qgpu_system_desc &d, int t) {
+    const int N = d.natom, S = d.nstates, nq = d.nqat;
+    auto in = [](long long v, long long lo, long long hi) { return v >= lo && v < hi; };
+    auto bad = [&](const char *what, long long k) {
+        return fail(QGPU_E_INVALID, "traj %d: %s %lld out of range", t, what, k);
+    };
+    if (d.natyps < 1 || !d.avdw || !d.bvdw || !d.ljcod) return fail(QGPU_E_INVALID, "traj %d: atom type tables", t);
+    for (int i = 0; i < N; ++i)
+        if (!in(d.iac[i], 0, d.natyps)) return bad("atom type of atom", i);
+    for (long long k = 0; k < (long long)d.natyps * d.natyps; ++k)
+        if (d.ljcod[k] != 1 && d.ljcod[k] != 2) return bad("LJ code", k);
+    if (d.iqatom)
+        for (int i = 0; i < N; ++i)
+            if (!in(d.iqatom[i], -1, nq)) return bad("Q index of atom", i);
+    // charge groups
+    if (d.ncgp < 1 || d.ncgp_solute < 0 || d.ncgp_solute > d.ncgp || !d.cgp_last || !d.cgp_switch || !d.cgpatom)
+        return fail(QGPU_E_INVALID, "traj %d: charge groups", t);
+    for (int g = 0; g < d.ncgp; ++g) {
+        const int f = d.cgp_first[g], l = d.cgp_last[g];
+        if (f < 0 || l < f || l >= N || !in(d.cgp_switch[g], 0, N)) return bad("charge group", g);
+        for (int k = f; k <= l; ++k)
+            if (!in(d.cgpatom[k], 0, N)) return bad("atom of charge group", g);
+    }
+    // neighbour exclusions and 1-4 pairs
+    if (d.nexcl < 0 || (d.nexcl && !d.excl_pairs) || d.n14 < 0 || (d.n14 && !d.pairs14))
+        return fail(QGPU_E_INVALID, "traj %d: exclusion or 1-4 lists", t);
+    for (long long k = 0; k < 2LL * d.nexcl; ++k)
+        if (!in(d.excl_pairs[k], 0, N)) return bad("excluded pair", k / 2);
+    for (long long k = 0; k < 2LL * d.n14; ++k)
+        if (!in(d.pairs14[k], 0, N)) return bad("1-4 pair", k / 2);
+    // Q atoms and their lists
+    if (nq > 0) {
+        if (!d.iqseq || !d.qcrg || !d.qiac || d.nqlib < 1 || !d.qavdw || !d.qbvdw || !d.sc_lookup)
+            return fail(QGPU_E_INVALID, "traj %d: Q-atom tables", t);
+        for (int q = 0; q < nq; ++q) {
+            if (!in(d.iqseq[q], 0, d.nat_solute)) return bad("atom of Q atom", q);
+            for (int st = 0; st < S; ++st)
+                if (!in(d.qiac[q * S + st], 0, d.nqlib)) return bad("Q type of Q atom", q);
+        }
+    }
+    if (d.nqp14 < 0 || (d.nqp14 && !d.qp14_pairs)) return fail(QGPU_E_INVALID, "traj %d: Q 1-4 pairs", t);
+    for (int k = 0; k < d.nqp14; ++k)
+        if (!in(d.qp14_pairs[2 * k], 0, nq) || !in(d.qp14_pairs[2 * k + 1], 0, N)) return bad("Q 1-4 pair", k);
+    long long nqq = 0;
+    for (int st = 0; st < S; ++st) {
+        if (d.nbqq_count[st] < 0) return bad("Q-Q pair count of state", st);
+        nqq += d.nbqq_count[st];
+    }
+    if (nqq && (!d.nbqq_iq || !d.nbqq_j || !d.nbqq_jq || !d.nbqq_ljcod || !d.nbqq_elscale))
+        return fail(QGPU_E_INVALID, "traj %d: Q-Q pair list", t);
+    for (long long p = 0; p < nqq; ++p)
+        if (!in(d.nbqq_iq[p], 0, nq) || !in(d.nbqq_j[p], 0, N) || !in(d.nbqq_jq[p], -1, nq) ||
+            !in(d.nbqq_ljcod[p], 1, 4))
+            return bad("Q-Q pair", p);
+    // bonded rows: nat atoms then per-state (Q) or one (classical) code
+    auto rows_ok = [&](const int32_t *rows, int n, int nat, int ncode, int code_lo, int ncod, const void *lib) {
+        if (n < 0 || (n && !rows) || ncod < 0 || (ncod && !lib)) return false;
+        const int w = nat + ncode;
+        for (long long r = 0; r < n; ++r) {
+            for (int a = 0; a < nat; ++a)
+                if (!in(rows[r * w + a], 0, N)) return false;
+            for (int c = 0; c < ncode; ++c)
+                if (!in(rows[r * w + nat + c], code_lo, (long long)ncod + 1)) return false;
+        }
+        return true;
+    };
+    if (!rows_ok(d.qbnd, d.nqbond, 2, S, 0, d.nqbcod, d.qbondlib) ||
+        !rows_ok(d.qang, d.nqangle, 3, S, 0, d.nqacod, d.qanglib) ||
+        !rows_ok(d.qtor, d.nqtor, 4, S, 0, d.nqtcod, d.qtorlib) ||
+        !rows_ok(d.qimp, d.nqimp, 4, S, 0, d.nqicod, d.qimplib))
+        return fail(QGPU_E_INVALID, "traj %d: Q bonded terms", t);
+    if (d.nbonds_solute < 0 || d.nbonds_solute > d.nbonds || d.nangles_solute < 0 || d.nangles_solute > d.nangles ||
+        d.ntors_solute < 0 || d.ntors_solute > d.ntors || d.nimps_solute < 0 || d.nimps_solute > d.nimps)
+        return fail(QGPU_E_INVALID, "traj %d: solute bonded counts outside 0..total", t);
+    if (!rows_ok(d.bnd, d.nbonds, 2, 1, 1, d.nbndcod, d.bondlib) ||
+        !rows_ok(d.ang, d.nangles, 3, 1, 1, d.nangcod, d.anglib) ||
+        !rows_ok(d.tor, d.ntors, 4, 1, 1, d.ntorcod, d.torlib) ||
+        !rows_ok(d.imp, d.nimps, 4, 1, 1, d.nimpcod, d.implib))
+        return fail(QGPU_E_INVALID, "traj %d: bonded terms (atoms or parameter codes)", t);
+    // SHAKE constraints
+    if (d.shake_molecules < 0) return fail(QGPU_E_INVALID, "traj %d: shake_molecules < 0", t);
+    if (d.shake_molecules > 0) {
+        if (!d.shake_first || !d.shake_i || !d.shake_j || !d.shake_dist2 || d.shake_first[0] != 0)
+            return fail(QGPU_E_INVALID, "traj %d: SHAKE tables", t);
+        for (int m = 0; m < d.shake_molecules; ++m) {
+            if (d.shake_first[m + 1] < d.shake_first[m]) return bad("SHAKE molecule", m);
+            for (int c = d.shake_first[m]; c < d.shake_first[m + 1]; ++c)
+                if (!in(d.shake_i[c], 0, N) || !in(d.shake_j[c], 0, N)) return bad("SHAKE constraint", c);
+        }
+    }
+    // off-diagonal couplings: state pairs and Q-atom pairs
+    if (d.noffd < 0 || (d.noffd && (!d.offd_ij || !d.offd_kl || !d.offd_Amu)))
+        return fail(QGPU_E_INVALID, "traj %d: off-diagonal couplings", t);
+    for (long long k = 0; k < 2LL * d.noffd; ++k)
+        if (!in(d.offd_ij[k], 0, S) || !in(d.offd_kl[k], 0, nq)) return bad("off-diagonal coupling", k / 2);
+    return 0;
+}
+
 static int validate(const qgpu_system_desc &d, int t) {
     if (d.natom <= 0) return fail(QGPU_E_INVALID, "traj %d: natom must be > 0", t);
     if (d.nat_solute < 0 || d.nat_solute > d.natom) return fail(QGPU_E_INVALID, "traj %d: bad nat_solute", t);
@@ -176,6 +277,7 @@ static int validate(const qgpu_system_desc &d, int t) {
     if (d.noffd > QG_MAXOD) return fail(QGPU_E_UNSUPPORTED, "traj %d: noffd %d > %d", t, d.noffd, QG_MAXOD);
     if (!d.x || !d.crg || !d.iac || !d.mass || !d.cgp_first) return fail(QGPU_E_INVALID, "traj %d: missing arrays", t);
     if (d.NBcycle <= 0) return fail(QGPU_E_INVALID, "traj %d: NBcycle must be > 0", t);
+    if (int rc = validate_indices(d, t)) return rc;
     for (int g = d.ncgp_solute; g < d.ncgp; ++g) {
         int f = d.cgp_first[g], l = d.cgp_last[g];
         if (l - f != 2) return fail(QGPU_E_INVALID, "traj %d: solvent group %d has %d atoms", t, g, l - f + 1);
@@ -1311,6 +1413,9 @@ int qgpu_last_error(char *buf, int32_t len) {
 
 int qgpu_create(const qgpu_system_desc *descs, int32_t ntraj, qgpu_handle **out) {
     if (!descs || ntraj <= 0 || !out) return fail(QGPU_E_INVALID, "qgpu_create: bad arguments");
+    // every descriptor is checked before any device call
+    for (int t = 0; t < ntraj; ++t)
+        if (int rc = validate(descs[t], t)) return rc;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(QGPU_E_CUDA, "no CUDA device");
     qgpu_handle *h = new qgpu_handle();

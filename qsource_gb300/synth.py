@@ -192,7 +192,7 @@ def synthetic(R: float, n_solute: int, nq: int, qcharges: np.ndarray, lambdas, s
     top = {
         "version": 5.06, "ff_type": 2, "natom": natom, "nat_solute": n_solute, "solv_atom": 3,
         "xtop": xtop, "iac": iac,
-        "nbonds_solute": n_solute - 1, "bnd": np.array(bnd, dtype=np.int32).reshape(-1, 3), "bondlib": bondlib,
+        "nbonds_solute": max(0, n_solute - 1), "bnd": np.array(bnd, dtype=np.int32).reshape(-1, 3), "bondlib": bondlib,
         "nangles_solute": 0, "ang": np.zeros((0, 4), np.int32), "anglib": np.zeros((0, 4)),
         "ntors_solute": 0, "tor": np.zeros((0, 5), np.int32), "torlib": np.zeros((0, 4)),
         "nimps_solute": 0, "imp": np.zeros((0, 5), np.int32), "imp_type": 2, "implib": np.zeros((0, 2)),

@@ -71,3 +71,37 @@ def test_calc_entries_refuse_bad_arguments_without_device(engine_lib):
     assert rc != 0 and "bad arguments" in last_error(engine_lib)
     rc = engine_lib.qgpu_calc_rmsf(p(fr), 1, 4, p(mask), 0, p(out))
     assert rc != 0 and "bad arguments" in last_error(engine_lib)
+
+
+def test_create_refuses_malformed_descriptors_without_device(engine_lib):
+    """qgpu_create checks every index the device would follow before any
+    device call: a negative solute bond count, a bond or SHAKE atom outside
+    the system, a parameter code outside its library, a charge group outside
+    the atoms and a Q atom outside the solute are refused with a message (a
+    well-formed descriptor gets as far as the device check)."""
+    import numpy as np
+    from qsource_gb300 import abi, synth
+    from qsource_gb300.abi import last_error
+
+    def create(g):
+        arr = (abi.SystemDesc * 1)(g.desc())
+        h = C.c_void_p()
+        return engine_lib.qgpu_create(arr, 1, C.byref(h)), last_error(engine_lib)
+
+    def fresh():
+        qa = synth.neutral_charges(np.random.default_rng(1), 4, 0.4)
+        return synth.synthetic(8.0, 12, 4, np.stack([qa, -qa], 1), (0.5, 0.5), 3)
+
+    g = fresh()
+    rc, msg = create(g)
+    assert "out of range" not in msg and "bonded" not in msg
+    cases = []
+    g = fresh(); g.nbonds_solute = -1; cases.append((g, "solute bonded counts"))
+    g = fresh(); g.bnd = np.array(g.bnd).copy(); g.bnd[0, 1] = g.natom + 7; cases.append((g, "bonded terms"))
+    g = fresh(); g.bnd = np.array(g.bnd).copy(); g.bnd[0, 2] = len(g.bondlib) + 1; cases.append((g, "bonded terms"))
+    g = fresh(); g.shake_j = np.array(g.shake_j).copy(); g.shake_j[0] = -2; cases.append((g, "SHAKE constraint"))
+    g = fresh(); g.cgp_last = np.array(g.cgp_last).copy(); g.cgp_last[-1] = g.natom; cases.append((g, "charge group"))
+    g = fresh(); g.iqseq = np.array(g.iqseq).copy(); g.iqseq[0] = g.nat_solute; cases.append((g, "Q atom"))
+    for g, want in cases:
+        rc, msg = create(g)
+        assert rc == 1 and want in msg, (want, rc, msg)        # QGPU_E_INVALID

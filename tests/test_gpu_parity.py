@@ -127,16 +127,11 @@ def test_forces_and_energies(systems, name):
         assert not energies_close(q, qo, EQ_KEYS)
 
 
-def test_ragged_batch_with_a_trajectory_without_q_atoms(systems):
-    """A batch of uneven content: a 9 A droplet around a 20-atom chain with no
-    Q atoms and one state (a plain MD system), beside the two-state Q droplet.
-    Forces and energies of each trajectory match the oracle at step 0, the
-    Q-free trajectory's per-state Q energies are zero, and 20 FP64-master MD
-    steps match the oracle's dynamics of both."""
-    from qsource_gb300 import synth
+def _ragged_check(batch, qfree=()):
+    """Step-0 forces and energies of every trajectory of the batch against the
+    oracle (per-state Q energies zero for the trajectories in qfree), then 20
+    FP64-master MD steps against the oracle's dynamics of each."""
     from qsource_gb300.abi import PRECISION
-    plain = synth.synthetic(9.0, 20, 0, np.zeros((0, 1)), (1.0,), 5)
-    batch = [plain, systems["cfg1"]]
     e = _engine(batch)
     e.make_pair_lists()
     for t, s in enumerate(batch):
@@ -148,7 +143,7 @@ def test_ragged_batch_with_a_trajectory_without_q_atoms(systems):
         assert not energies_close(E, Eo, E_KEYS)
         for q, qo in zip(EQ, EQo):
             assert not energies_close(q, qo, EQ_KEYS)
-        if t == 0:
+        if t in qfree:
             assert len(EQ) == 1 and all(EQ[0][k] == 0.0 for k in ("qq_el", "qp_el", "qw_el", "qp_vdw", "qw_vdw"))
     e = _engine(batch)
     e.set_precision(PRECISION["fp64"])
@@ -164,6 +159,24 @@ def test_ragged_batch_with_a_trajectory_without_q_atoms(systems):
         x, _ = e.coords(t)
         xo, _ = o.coords()
         assert np.abs(x - xo).max() < 1e-4
+
+
+def test_ragged_batch_with_a_trajectory_without_q_atoms(systems):
+    """A batch of uneven content: a 9 A droplet around a 20-atom chain with no
+    Q atoms and one state (a plain MD system), beside the two-state Q droplet."""
+    from qsource_gb300 import synth
+    plain = synth.synthetic(9.0, 20, 0, np.zeros((0, 1)), (1.0,), 5)
+    _ragged_check([plain, systems["cfg1"]], qfree=(0,))
+
+
+def test_ragged_batch_with_a_water_only_trajectory(systems):
+    """A droplet of water alone (no solute, no Q atoms: no solute items, no
+    solute groups in the lists, no bonded terms) beside the two-state Q
+    droplet."""
+    from qsource_gb300 import synth
+    water = synth.synthetic(9.0, 0, 0, np.zeros((0, 1)), (1.0,), 5)
+    assert water.nat_solute == 0 and water.nbonds_solute == 0
+    _ragged_check([systems["cfg1"], water], qfree=(1,))
 
 
 def test_golden_columns_on_gpu(systems, golden):
