@@ -256,6 +256,8 @@ static int validate(const qgpu_system_desc &d, int t) {
     if (d.nat_solute < 0 || d.nat_solute > d.natom) return fail(QGPU_E_INVALID, "traj %d: bad nat_solute", t);
     if (d.solv_atom != 3) return fail(QGPU_E_UNSUPPORTED, "traj %d: only 3-site solvent is supported", t);
     if ((d.natom - d.nat_solute) % 3) return fail(QGPU_E_INVALID, "traj %d: solvent atoms not a multiple of 3", t);
+    if (d.nwat != (d.natom - d.nat_solute) / 3)
+        return fail(QGPU_E_INVALID, "traj %d: nwat %d is not the number of solvent molecules", t, d.nwat);
     if (d.ivdw_rule != 1 && d.ivdw_rule != 2)
         return fail(QGPU_E_INVALID, "traj %d: combination rule %d (1 geometric, 2 arithmetic)", t, d.ivdw_rule);
     if (d.use_pbc) {
@@ -567,6 +569,8 @@ static int create_impl(const qgpu_system_desc *descs, int ntraj, qgpu_handle *h)
         // --- water polarisation shells (watpol, wat_shells)
         T.wp0 = (int)(wp_state.size() / 3);
         if (d.wpol_restr && d.nwat > 0 && d.nwpolr_shell > 0) {
+            if (!d.wshell_rout || !d.wshell_dr || !d.wshell_cstb || !d.wshell_theta_corr)
+                return fail(QGPU_E_INVALID, "trajectory %d: polarisation shell tables", t);
             if (d.nwpolr_shell > QG_MAXSHELL)
                 return fail(QGPU_E_UNSUPPORTED, "trajectory %d: %d polarisation shells (max %d)", t, d.nwpolr_shell,
                             QG_MAXSHELL);
