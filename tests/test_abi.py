@@ -102,7 +102,12 @@ def test_create_refuses_malformed_descriptors_without_device(engine_lib):
     g = fresh(); g.shake_j = np.array(g.shake_j).copy(); g.shake_j[0] = -2; cases.append((g, "SHAKE constraint"))
     g = fresh(); g.cgp_last = np.array(g.cgp_last).copy(); g.cgp_last[-1] = g.natom; cases.append((g, "charge group"))
     g = fresh(); g.iqseq = np.array(g.iqseq).copy(); g.iqseq[0] = g.nat_solute; cases.append((g, "Q atom"))
-    g = fresh(); g.nwat = g.nwat + 1; cases.append((g, "nwat"))
     for g, want in cases:
         rc, msg = create(g)
         assert rc == 1 and want in msg, (want, rc, msg)        # QGPU_E_INVALID
+    # a water count that disagrees with the solvent atoms
+    d = fresh().desc()
+    d.nwat += 1
+    h = C.c_void_p()
+    rc = engine_lib.qgpu_create((abi.SystemDesc * 1)(d), 1, C.byref(h))
+    assert rc == 1 and "nwat" in last_error(engine_lib)
